@@ -1,0 +1,261 @@
+/*
+ * mpgpu.h -- C-ABI of the GB300 implementation of Millepede-II pede's hot
+ * path: per-record local fits, deterministic accumulation of the
+ * Schur-complement updates into the packed or mpbits-sparse global matrix,
+ * and the global solve (QL constraint elimination, inversion, Cholesky,
+ * MINRES).
+ *
+ * Every entry point returns an int32 status: 0 on success, otherwise a code
+ * that follows pede's exit codes (doc/exitCodes.md, peend in
+ * pede.f90:11390-11409) where one exists.  No exception or abort crosses
+ * this boundary.  Arrays are plain host pointers owned by the caller; the
+ * context owns all device memory and keeps it resident between calls.
+ * Index arrays hold the reference's 1-based parameter / group numbers.
+ * One host thread per context; several contexts may run concurrently.
+ *
+ * The seams replaced (file:line in the Millepede-II sources):
+ *   mpgpu_set_layout      loop2 results: globalAllIndexGroups,
+ *                         sparseMatrixOffsets/Columns (pede.f90:6509-6545,
+ *                         7174, 7426)
+ *   mpgpu_set_constraints feasma / qldecb (pede.f90:1377-1544,
+ *                         mpqldec.f90:219-393)
+ *   mpgpu_upload_records  readFromBinary + prepareRecords(1) buffers
+ *                         (pede.f90:1714-2075, mppar.f90:282-321)
+ *   mpgpu_loopbf          CALL loopbf(nrejec,nfiles,jfd,cfd,dfd)
+ *                         (pede.f90:2613; routine at 3387-4442) with the
+ *                         mgupdt flush (pede.f90:3219-3357)
+ *   mpgpu_mupdat          CALL mupdat(i,j,add) (pede.f90:3134-3204)
+ *   mpgpu_solve           CALL minver / mchdec / mminrs (pede.f90:8832-8855)
+ *   mpgpu_avprod          SUBROUTINE avprod(n,x,b) (pede.f90:5331-5358)
+ *   mpgpu_download_matrix globalMatD after the data loop
+ */
+#ifndef MPGPU_H
+#define MPGPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MPGPU_OK 0
+#define MPGPU_ERR_BADRECORD 20     /* malformed record (pede code 20) */
+#define MPGPU_ERR_BADINDEX 23      /* index outside the matrix (pede 23) */
+#define MPGPU_ERR_SIZE 24          /* size mismatch (pede 24) */
+#define MPGPU_ERR_NAN 25           /* NaN in the solution (pede 25) */
+#define MPGPU_ERR_TOOMANYREJ 26    /* more than 1/3 of records rejected (pede 26) */
+#define MPGPU_ERR_QL 27            /* singular constraints (pede 27) */
+#define MPGPU_ERR_FACTOR 29        /* factorisation failed */
+#define MPGPU_ERR_ALLOC 30         /* device allocation failed */
+#define MPGPU_ERR_GROUPS 35        /* record/group mismatch (pede 35) */
+#define MPGPU_ERR_TIMEOUT 41       /* a bounded device wait ran out */
+#define MPGPU_ERR_BUDGET 42        /* job rejected by the HBM budget */
+#define MPGPU_ERR_CUDA 43          /* CUDA runtime error */
+#define MPGPU_ERR_ARG 44           /* invalid argument / call order */
+#define MPGPU_ERR_LIMIT 45         /* record larger than the kernel limits */
+
+typedef struct mpgpu_ctx mpgpu_ctx;
+
+typedef struct mpgpu_cfg {
+    int32_t device;             /* CUDA device ordinal */
+    int32_t flags;              /* reserved, 0 */
+    int64_t staging_bytes;      /* per-record update staging (0: default 4 GiB) */
+} mpgpu_cfg;
+
+int32_t mpgpu_create(mpgpu_ctx **ctx, const mpgpu_cfg *cfg);
+int32_t mpgpu_destroy(mpgpu_ctx *ctx);
+/* last error message of the context (static storage inside ctx) */
+const char *mpgpu_last_error(const mpgpu_ctx *ctx);
+
+/* Global-parameter layout.  varIndexOfTotal[nTotal]: variable index (1..nVar)
+ * of each total parameter index, <=0 for fixed (globalParLabelIndex(2,:)).
+ * allIndexGroups[nGroups+1]: first variable index of each parameter group,
+ * last entry nVar+1.  matsto 1: packed lower triangle; matsto 2: mpbits
+ * sparse storage described by sparseOffsets[2*(nGroups+1)] (column-major
+ * 2 x (nGroups+1), sparseMatrixOffsets) and sparseColumns[ncolw]
+ * (sparseMatrixColumns); nmat = length of globalMatD. */
+int32_t mpgpu_set_layout(mpgpu_ctx *ctx, int32_t nTotal, const int32_t *varIndexOfTotal,
+                         int32_t nVar, int32_t nGroups, const int32_t *allIndexGroups,
+                         int32_t matsto, const int64_t *sparseOffsets,
+                         const int32_t *sparseColumns, int64_t ncolw, int64_t nmat);
+
+/* Linear constraints over the variable parameters, eliminated by QL:
+ * A[ncon*nVar], row k = constraint k (the reference's matConstraintsT). */
+int32_t mpgpu_set_constraints(mpgpu_ctx *ctx, int32_t ncon, const double *A);
+
+/* Records in the Mille layout (pede.f90:1693-1713) with labels already
+ * translated to total parameter indices (prepareRecords(1)).  Record r
+ * occupies words [recPtr[r], recPtr[r+1]); recFile[nrec] holds the 1-based
+ * file of each record (NULL: all file 1), fileWeight[nfiles] the file
+ * weights (NULL: 1).  Replaces any previously uploaded records. */
+int32_t mpgpu_upload_records(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr,
+                             const int32_t *inder, const double *glder,
+                             const int32_t *recFile, int32_t nfiles,
+                             const double *fileWeight);
+
+typedef struct mpgpu_fitopts {
+    int32_t icalcm;    /* 1: build the global matrix */
+    int32_t nloopn;    /* data-loop counter (1 = first) */
+    int32_t lhuber;    /* outlier down-weighting iterations */
+    int32_t lfitbb;    /* bordered-band detection for the local fit */
+    float chicut;      /* chi2 cut factor (<0: none) */
+    float chhuge;      /* cut for unreasonable chi2 */
+    float dwcut;       /* down-weight fraction cut */
+    float cndlmx;      /* max log10(condition) of the band part */
+} mpgpu_fitopts;
+
+typedef struct mpgpu_fitstats {
+    int64_t nrej[6];    /* NaN, rank, condition, ndf<=0, huge chi2, chi2 cut */
+    int64_t chi2SumI;   /* integer part of sum(chi2*w) (addsums) */
+    double chi2SumD;    /* remainder */
+    int64_t ndfSum;
+    double ndfSumW;
+    int32_t nbndr[2];   /* records solved as bordered band (left / right) */
+    int32_t nbdrx, nbndx;
+    int64_t naccepted;
+} mpgpu_fitstats;
+
+/* One data loop (loopbf): local fits of all records with the given global
+ * parameters (globalParameter[nTotal], host), then - if icalcm == 1 - the
+ * deterministic accumulation of the updates into the device-resident global
+ * matrix (zeroed first).  globalVector[nVar] / globalCounter[nVar] (host,
+ * may be NULL) receive the gradient and the entry counts; naccf/chi2f/ndff
+ * [nfiles] (may be NULL) the per-file statistics.  The vector stays on the
+ * device for mpgpu_solve. */
+int32_t mpgpu_loopbf(mpgpu_ctx *ctx, const mpgpu_fitopts *opt, const double *globalParameter,
+                     double *globalVector, int64_t *globalCounter, mpgpu_fitstats *stats,
+                     int32_t *naccf, float *chi2f, int32_t *ndff);
+
+/* Same loop with the global parameters, vector and counters left on the
+ * device (device pointers; globalParameter is read, the others written). */
+int32_t mpgpu_loopbf_device(mpgpu_ctx *ctx, const mpgpu_fitopts *opt,
+                            const double *d_globalParameter, mpgpu_fitstats *stats);
+
+/* mupdat for n elements: matrix(i[k], j[k]) += add[k] (1-based variable
+ * indices), applied in order on the device; the vector side (globalVector
+ * += vadd) is applied when vidx != NULL. */
+int32_t mpgpu_mupdat(mpgpu_ctx *ctx, int32_t n, const int32_t *i, const int32_t *j,
+                     const double *add);
+int32_t mpgpu_vector_add(mpgpu_ctx *ctx, int32_t n, const int32_t *vidx, const double *vadd);
+
+int32_t mpgpu_download_matrix(mpgpu_ctx *ctx, double *globalMatD);
+int32_t mpgpu_download_vector(mpgpu_ctx *ctx, double *globalVector, int64_t *globalCounter);
+/* per-record outcome of the last loop: 0 accepted, 1..6 rejection class
+ * (nrej index + 1), -1 no local parameters */
+int32_t mpgpu_download_record_status(mpgpu_ctx *ctx, int32_t *status);
+
+typedef struct mpgpu_solveinfo {
+    int32_t nrank;      /* rank found by inversion / decomposition */
+    int32_t itn;        /* MINRES iterations */
+    int32_t istop;      /* MINRES stop reason */
+    int32_t pad;
+    double evmin, evmax;  /* decomposition pivot range */
+    double ms;          /* device time of the solve */
+} mpgpu_solveinfo;
+
+/* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES)
+ * of the matrix built by the last mpgpu_loopbf plus mupdat calls.
+ * consResiduals[ncon] = d - C p (addcst); correction[nVar] receives the
+ * step; errors[nVar] (metsol 1, may be NULL) the diagonal of the covariance
+ * (sqrt gives the parameter errors).  rtol/itnlim: MINRES tolerance and
+ * iteration limit.  The matrix is consumed (factorised in place). */
+int32_t mpgpu_solve(mpgpu_ctx *ctx, int32_t metsol, const double *consResiduals,
+                    double rtol, int32_t itnlim, double *correction, double *errors,
+                    mpgpu_solveinfo *info);
+
+/* b = Q^T A Q x restricted to the first n = nVar - ncon components
+ * (avprod), x and b host arrays of length n. */
+int32_t mpgpu_avprod(mpgpu_ctx *ctx, int32_t n, const double *x, double *b);
+
+/* ------------------------------------------------------------------
+ * Host side of pede (stand-in for the Fortran host): label table, groups,
+ * sparse structure, iteration control and millepede.res.
+ * ---------------------------------------------------------------- */
+typedef struct mpgpu_steer {
+    int32_t metsol;     /* 1 inversion, 3 decomposition, 4 MINRES */
+    int32_t matsto;     /* 1 packed, 2 sparse */
+    int32_t mitera;     /* number of iterations (solutions) */
+    int32_t lhuber;     /* outlierdownweighting */
+    float chicut, chirem, chhuge, dwcut, cndlmx;
+    int32_t lfitbb;
+    int32_t mreqenf, mreqena, mreqpe;
+    double mrestl;
+    int32_t itnlim;
+    int32_t nthreads;   /* host threads for the structure passes */
+} mpgpu_steer;
+
+typedef struct mpgpu_job {
+    int64_t nrec; const int64_t *recPtr; const int32_t *inder; const double *glder;
+    const int32_t *recFile; int32_t nfiles; const double *fileWeight;
+    int32_t npar; const int32_t *parLabel; const double *parValue; const double *parSigma;
+    int32_t ncon; const int32_t *conStart; const int32_t *conLabel; const double *conCoef;
+    const double *conRhs;
+    int32_t nmeas; const int32_t *msStart; const int32_t *msLabel; const double *msCoef;
+    const double *msRhs; const double *msSigma;
+} mpgpu_job;
+
+typedef struct mpgpu_result {
+    int32_t cap;
+    int32_t nTotal, nVar, nVarGroups, nFit;
+    int32_t *labels; double *parameter; double *presigma; double *error; int64_t *counts;
+    int32_t *varIndex;
+    int64_t nrej[6];
+    double fvalue; int64_t ndf;
+    int32_t nrank; int32_t minresItn, minresIstop;
+    int32_t nloopn;
+    int32_t exitCode;
+    double msBuild, msSolve;   /* device time of the last build / solve */
+} mpgpu_result;
+
+/* loop1 equivalent: label table (sorted), entries per label, parameter
+ * groups and variable indices.  Returns nTotal or <0. */
+int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                          const double *glder, int32_t nsteer, const int32_t *steerLabels,
+                          int32_t npre, const int32_t *preLabel, const double *preSigma,
+                          int32_t mreqenf, int32_t cap, int32_t *labels, int64_t *counter,
+                          int32_t *varIndex, int32_t *totGroup, int32_t *nVar,
+                          int32_t *nVarGroups);
+/* translation labels -> total indices (prepareRecords(1)) */
+int32_t mpgpu_host_translate(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                             const double *glder, int32_t nTotal, const int32_t *labels,
+                             int32_t *outInder);
+/* loop2 sparse structure (matsto 2, mreqpe 1): sparseMatrixOffsets /
+ * Columns; returns 0 or <0 (capacity) */
+int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                          const double *glder, const int32_t *varIndexOfTotal, int32_t nVar,
+                          int32_t nG, const int32_t *allIndexGroups, int64_t cap,
+                          int64_t *offsets, int32_t *columns, int64_t *ncolw, int64_t *nmat);
+
+/* Whole alignment job on the GPU (iteration control of xloopn without line
+ * search); ctx may be NULL (a private context is created). */
+int32_t mpgpu_pede_run(mpgpu_ctx *ctx, const mpgpu_steer *st, const mpgpu_job *job,
+                       mpgpu_result *res);
+int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors);
+
+/* ------------------------------------------------------------------
+ * Synthetic Mille data (role of pede -t / mptest1 / mptest2)
+ * ---------------------------------------------------------------- */
+typedef struct mpgen_cfg {
+    int32_t kind;        /* 1 telescope, 2 barrel helices, 3 barrel broken lines */
+    int32_t nlayers;     /* telescope layers */
+    int32_t nmod;        /* telescope: modules per layer; barrel: total modules */
+    int32_t minHits, maxHits;  /* broken lines */
+    int64_t ntracks;
+    uint64_t seed;
+    double sigma1, sigma2;     /* hit resolutions (cm) */
+    double misal;              /* misalignment scale (cm) */
+    double outlierFrac;        /* fraction of hits with 20x wider noise */
+    double theta0;             /* multiple-scattering angle (rad) */
+} mpgen_cfg;
+
+int mpgen_count(const mpgen_cfg *cfg, int64_t *nrec, int64_t *nwords, int32_t *nlabels);
+int mpgen_fill(const mpgen_cfg *cfg, int64_t *recPtr, int32_t *inder, double *glder,
+               double *truth);
+int mpgen_constraints(const mpgen_cfg *cfg, int32_t *ncon, int32_t *conStart,
+                      int32_t *conLabel, double *conCoef);
+int mpgen_constraint_words(const mpgen_cfg *cfg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

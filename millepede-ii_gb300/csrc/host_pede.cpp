@@ -1,0 +1,511 @@
+// host_pede.cpp -- host side of pede around the device hot path: label
+// table and parameter groups (loop1), the mpbits sparse structure (loop2),
+// the iteration control (xloopn/loopn/addcst without line search) and the
+// millepede.res writer (prtglo).  In a Fortran pede build these steps stay
+// in pede itself; this C++ version drives the C-ABI for tests, the
+// benchmark and the pede_gpu command.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mpgpu.h"
+
+namespace {
+
+// measurement boundaries of one record (decodeNextMeasurement,
+// pede.f90:2428-2468); positions absolute
+template <class F>
+bool for_each_measurement(const int32_t *in, const double *gl, int64_t w0, int64_t w1, F f) {
+    int64_t lg = w0;
+    const int64_t end = w1 - 1;
+    for (;;) {
+        if (lg >= end) return true;
+        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
+        const int64_t sl = lg;
+        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
+        const int64_t sg = lg;
+        if (sl + 1 == sg && gl[sg] < 0.0) {
+            lg = lg + (int64_t)(-gl[sg] + 0.5);
+            continue;
+        }
+        while (lg < end && in[lg + 1] != 0) lg++;
+        f(sl, sg, lg);
+    }
+}
+
+int32_t find_label(const std::vector<int32_t> &lab, int32_t item) {
+    auto it = std::lower_bound(lab.begin(), lab.end(), item);
+    if (it == lab.end() || *it != item) return -1;
+    return (int32_t)(it - lab.begin());
+}
+
+}  // namespace
+
+// loop1: labels (ascending order defines the total index), entries per
+// label counted per equation over non-zero derivatives (mcount = 0), the
+// parameter groups and the variable-parameter numbering.  A group is a
+// maximal run of consecutive total indices that no equation splits: every
+// equation's sorted index list cuts before its first element, after its
+// last element and at each of its gaps (the fixed point of pargrp,
+// pede.f90:2311-2404, over all equations).
+extern "C" int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                     const double *glder, int32_t nsteer,
+                                     const int32_t *steerLabels, int32_t npre,
+                                     const int32_t *preLabel, const double *preSigma,
+                                     int32_t mreqenf, int32_t cap, int32_t *labels,
+                                     int64_t *counter, int32_t *varIndex, int32_t *totGroup,
+                                     int32_t *nVar, int32_t *nVarGroups) {
+    std::vector<int32_t> all;
+    all.reserve((size_t)(recPtr[nrec] - recPtr[0]) / 2 + nsteer);
+    for (int32_t i = 0; i < nsteer; ++i)
+        if (steerLabels[i] > 0) all.push_back(steerLabels[i]);
+    for (int64_t r = 0; r < nrec; ++r) {
+        bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
+                                       [&](int64_t, int64_t sg, int64_t lg) {
+                                           for (int64_t w = sg + 1; w <= lg; ++w)
+                                               if (inder[w] > 0) all.push_back(inder[w]);
+                                       });
+        if (!ok) return -20;
+    }
+    std::sort(all.begin(), all.end());
+    all.erase(std::unique(all.begin(), all.end()), all.end());
+    const int32_t n = (int32_t)all.size();
+    if (n > cap) return -1;
+    // cut[i] (0-based): a group boundary between index i and i+1
+    std::vector<uint8_t> cut(n + 1, 0), seen(n, 0);
+    std::vector<int64_t> cnt(n, 0);
+    std::vector<int32_t> list;
+    for (int64_t r = 0; r < nrec; ++r) {
+        for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
+            list.clear();
+            for (int64_t w = sg + 1; w <= lg; ++w) {
+                if (glder[w] == 0.0) continue;
+                list.push_back(find_label(all, inder[w]));
+            }
+            if (list.empty()) return;
+            std::sort(list.begin(), list.end());
+            for (int32_t x : list) { cnt[x]++; seen[x] = 1; }
+            if (list.front() > 0) cut[list.front() - 1] = 1;
+            for (size_t q = 0; q + 1 < list.size(); ++q)
+                if (list[q + 1] != list[q] + 1) {
+                    cut[list[q]] = 1;
+                    if (list[q + 1] > 0) cut[list[q + 1] - 1] = 1;
+                }
+            cut[list.back()] = 1;
+        });
+    }
+    std::vector<double> ps(n, 0.0);
+    for (int32_t i = 0; i < npre; ++i) {
+        int32_t li = find_label(all, preLabel[i]);
+        if (li >= 0) ps[li] = preSigma[i];
+    }
+    int32_t nv = 0, ntg = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        labels[i] = all[i];
+        counter[i] = cnt[i];
+        if (ps[i] < 0.0) varIndex[i] = -1;
+        else if (cnt[i] < mreqenf) varIndex[i] = -2;
+        else varIndex[i] = ++nv;
+        totGroup[i] = 0;
+        if (!seen[i]) continue;
+        if (i == 0 || cut[i - 1] || !seen[i - 1]) ntg++;
+        totGroup[i] = ntg;
+    }
+    int32_t nvg = 0, lgrp = -1;
+    for (int32_t i = 0; i < n; ++i) {
+        if (varIndex[i] <= 0) continue;
+        if (totGroup[i] != lgrp) nvg++;
+        lgrp = totGroup[i];
+    }
+    *nVar = nv;
+    *nVarGroups = nvg;
+    return n;
+}
+
+extern "C" int32_t mpgpu_host_translate(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                        const double *glder, int32_t nTotal, const int32_t *labels,
+                                        int32_t *outInder) {
+    std::vector<int32_t> lab(labels, labels + nTotal);
+    std::memcpy(outInder + recPtr[0], inder + recPtr[0], sizeof(int32_t) * (size_t)(recPtr[nrec] - recPtr[0]));
+    for (int64_t r = 0; r < nrec; ++r) {
+        bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
+                                       [&](int64_t, int64_t sg, int64_t lg) {
+                                           for (int64_t w = sg + 1; w <= lg; ++w)
+                                               outInder[w] = find_label(lab, inder[w]) + 1;
+                                       });
+        if (!ok) return 20;
+    }
+    return 0;
+}
+
+// loop2 sparse structure: every pair of parameter groups met in one record
+// (pede.f90:6889-6908) is stored; per row group the columns are kept either
+// as a list of parameter indices or, when that is shorter, as regions of
+// consecutive groups (offset, first group) closed by (end offset, nG+1)
+// (ndbits/spbits, mpbits.f90:305-566, 1220-1350).
+extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                     const double *glder, const int32_t *varIndexOfTotal,
+                                     int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
+                                     int64_t cap, int64_t *offsets, int32_t *columns,
+                                     int64_t *ncolw, int64_t *nmat) {
+    std::vector<int32_t> p2g(nVar);
+    for (int32_t g = 1; g <= nG; ++g)
+        for (int32_t v = allIndexGroups[g - 1]; v < allIndexGroups[g]; ++v) p2g[v - 1] = g;
+    // lower-triangular bitmap over group pairs, row I holds J = 1..I
+    std::vector<uint64_t> rowWord(nG + 2, 0);   // first word of row I
+    for (int32_t I = 1; I <= nG; ++I) rowWord[I + 1] = rowWord[I] + ((uint64_t)I + 63) / 64;
+    std::vector<uint64_t> bits(rowWord[nG + 1] + 1, 0);
+    const int nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    // records split over threads; bits set with atomic OR (idempotent)
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) {
+        th.emplace_back([&, t] {
+            std::vector<int32_t> grp;
+            for (int64_t r = nrec * t / nt; r < nrec * (t + 1) / nt; ++r) {
+                grp.clear();
+                for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
+                    for (int64_t w = sg + 1; w <= lg; ++w) {
+                        const int32_t v = varIndexOfTotal[inder[w] - 1];
+                        if (v > 0) grp.push_back(p2g[v - 1]);
+                    }
+                });
+                std::sort(grp.begin(), grp.end());
+                grp.erase(std::unique(grp.begin(), grp.end()), grp.end());
+                for (size_t a = 0; a < grp.size(); ++a)
+                    for (size_t b = 0; b <= a; ++b) {
+                        const uint64_t bit = rowWord[grp[a]] * 64 + (uint64_t)(grp[b] - 1);
+                        __atomic_fetch_or(&bits[bit >> 6], 1ull << (bit & 63), __ATOMIC_RELAXED);
+                    }
+            }
+        });
+    }
+    for (auto &x : th) x.join();
+    auto test = [&](int32_t I, int32_t J) {
+        const uint64_t bit = rowWord[I] * 64 + (uint64_t)(J - 1);
+        return (bits[bit >> 6] >> (bit & 63)) & 1ull;
+    };
+    const int64_t nd = allIndexGroups[nG] - allIndexGroups[0];
+    std::vector<int64_t> nw(nG + 1), nm(nG + 1);
+    std::vector<uint8_t> comp(nG + 1, 0);
+    for (int32_t I = 1; I <= nG; ++I) {
+        int64_t inr = 0, irgn = 1;
+        bool last = false;
+        for (int32_t J = 1; J <= I; ++J) {
+            const bool on = test(I, J);
+            if (on) {
+                inr += allIndexGroups[J] - allIndexGroups[J - 1];
+                if (!last) irgn++;
+            }
+            last = on;
+        }
+        const int64_t np = allIndexGroups[I] - allIndexGroups[I - 1];
+        comp[I] = inr > 0 && 2 * irgn < inr;
+        nw[I] = comp[I] ? 2 * irgn : inr;
+        nm[I] = inr * np;
+    }
+    int64_t lb = 0, ll = nd;
+    for (int32_t I = 1; I <= nG; ++I) {
+        offsets[2 * (I - 1)] = lb;
+        offsets[2 * (I - 1) + 1] = ll;
+        lb += nw[I];
+        ll += nm[I];
+    }
+    offsets[2 * nG] = lb;
+    offsets[2 * nG + 1] = ll;
+    if (lb > cap) return -1;
+    for (int32_t I = 1; I <= nG; ++I) {
+        int64_t k = offsets[2 * (I - 1)];
+        int64_t width = 0;
+        bool last = false;
+        for (int32_t J = 1; J <= I; ++J) {
+            const bool on = test(I, J);
+            const int32_t nj = allIndexGroups[J] - allIndexGroups[J - 1];
+            if (on) {
+                if (comp[I]) {
+                    if (!last) { columns[k++] = (int32_t)width; columns[k++] = J; }
+                } else {
+                    for (int32_t q = 0; q < nj; ++q) columns[k++] = allIndexGroups[J - 1] + q;
+                }
+                width += nj;
+            }
+            last = on;
+        }
+        if (comp[I]) { columns[k++] = (int32_t)width; columns[k++] = nG + 1; }
+    }
+    *ncolw = lb;
+    *nmat = ll;
+    return 0;
+}
+
+// ------------------------------------------------------------------ job
+namespace {
+
+struct Timer {
+    double ms = 0.0;
+};
+
+int32_t qlbsub_host(int32_t ncon, const std::vector<double> &, const double *, double *) { return ncon; }
+
+}  // namespace
+
+// Whole alignment job: structure on the host, data loops and solves on the
+// device.  Iteration control of xloopn (pede.f90:8501-9334) without line
+// search and function-value loops: every iteration rebuilds the matrix,
+// solves and adds the correction; chi2-cut factors per loop as in loopn
+// (pede.f90:2583-2593).
+extern "C" int32_t mpgpu_pede_run(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job,
+                                  mpgpu_result *res) {
+    if (!st || !job || !res) return MPGPU_ERR_ARG;
+    mpgpu_ctx *ctx = ctxIn;
+    if (!ctx) {
+        mpgpu_cfg cfg{0, 0, 0};
+        int32_t rc = mpgpu_create(&ctx, &cfg);
+        if (rc) return rc;
+    }
+    int32_t rc = 0;
+    std::vector<int32_t> steer;
+    for (int32_t i = 0; i < job->npar; ++i) steer.push_back(job->parLabel[i]);
+    if (job->ncon) for (int32_t i = 0; i < job->conStart[job->ncon]; ++i) steer.push_back(job->conLabel[i]);
+    if (job->nmeas) for (int32_t i = 0; i < job->msStart[job->nmeas]; ++i) steer.push_back(job->msLabel[i]);
+    const int32_t cap = res->cap;
+    std::vector<int64_t> counter(cap);
+    std::vector<int32_t> totGroup(cap);
+    int32_t nVar = 0, nG = 0;
+    int32_t ntot = mpgpu_host_labels(job->nrec, job->recPtr, job->inder, job->glder, (int32_t)steer.size(),
+                                     steer.data(), job->npar, job->parLabel, job->parSigma, st->mreqenf,
+                                     cap, res->labels, counter.data(), res->varIndex, totGroup.data(),
+                                     &nVar, &nG);
+    if (ntot < 0) { res->exitCode = 20; if (!ctxIn) mpgpu_destroy(ctx); return 20; }
+    res->nTotal = ntot;
+    res->nVar = nVar;
+    res->nVarGroups = nG;
+    std::vector<int32_t> lab(res->labels, res->labels + ntot);
+    std::vector<int32_t> aig(nG + 1);
+    {
+        int32_t cur = 0, prev = -1;
+        for (int32_t i = 0; i < ntot; ++i) {
+            if (res->varIndex[i] <= 0) continue;
+            if (totGroup[i] != prev) { aig[cur++] = res->varIndex[i]; prev = totGroup[i]; }
+        }
+        aig[nG] = nVar + 1;
+    }
+    const int64_t nw = job->recPtr[job->nrec];
+    std::vector<int32_t> tinder(nw);
+    mpgpu_host_translate(job->nrec, job->recPtr, job->inder, job->glder, ntot, res->labels, tinder.data());
+    std::vector<int64_t> offsets;
+    std::vector<int32_t> columns;
+    int64_t ncolw = 0, nmat = 0;
+    if (st->matsto == 2) {
+        offsets.resize(2 * (nG + 1));
+        int64_t capc = 1 << 20;
+        for (;;) {
+            columns.assign(capc, 0);
+            if (mpgpu_host_mpbits(job->nrec, job->recPtr, tinder.data(), job->glder, res->varIndex, nVar, nG,
+                                  aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat) == 0)
+                break;
+            capc *= 4;
+        }
+    }
+    rc = mpgpu_set_layout(ctx, ntot, res->varIndex, nVar, nG, aig.data(), st->matsto,
+                          offsets.empty() ? nullptr : offsets.data(), columns.empty() ? nullptr : columns.data(),
+                          ncolw, nmat);
+    const int32_t ncon = job->ncon;
+    std::vector<double> A;
+    if (!rc && ncon > 0) {
+        A.assign((size_t)ncon * nVar, 0.0);
+        for (int32_t c = 0; c < ncon; ++c)
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; ++k) {
+                int32_t li = find_label(lab, job->conLabel[k]);
+                if (li < 0) continue;
+                if (res->varIndex[li] > 0) A[(size_t)c * nVar + res->varIndex[li] - 1] += job->conCoef[k];
+            }
+        rc = mpgpu_set_constraints(ctx, ncon, A.data());
+    }
+    if (!rc) rc = mpgpu_upload_records(ctx, job->nrec, job->recPtr, tinder.data(), job->glder, job->recFile,
+                                       job->nfiles, job->fileWeight);
+    const int32_t nfit = nVar - ncon;
+    res->nFit = nfit;
+    std::vector<double> gpar(ntot, 0.0), psig(ntot, 0.0);
+    for (int32_t i = 0; i < job->npar; ++i) {
+        int32_t li = find_label(lab, job->parLabel[i]);
+        if (li < 0) continue;
+        if (job->parValue) gpar[li] = job->parValue[i];
+        if (job->parSigma) psig[li] = job->parSigma[i];
+    }
+    std::vector<int32_t> v2t(nVar);
+    for (int32_t i = 0; i < ntot; ++i)
+        if (res->varIndex[i] > 0) v2t[res->varIndex[i] - 1] = i;
+    std::vector<int32_t> pi, pj;
+    std::vector<double> pa;
+    for (int32_t i = 0; i < nVar; ++i) {
+        const double s = psig[v2t[i]];
+        if (s > 0.0) { pi.push_back(i + 1); pj.push_back(i + 1); pa.push_back(1.0 / (s * s)); }
+    }
+    std::vector<double> gvec(nVar), corr(nVar), err(nVar, 0.0), cres(ncon > 0 ? ncon : 1, 0.0);
+    std::vector<int64_t> gcnt(nVar);
+    bool haveErr = false;
+    float chicut = st->chicut;
+    int64_t nrejTot = 0;
+    std::memset(res->nrej, 0, sizeof(res->nrej));
+    res->msBuild = res->msSolve = 0.0;
+    for (int32_t iter = 1; !rc && iter <= st->mitera; ++iter) {
+        const int32_t nloopn = iter;
+        if (nloopn > 1) {
+            if (nloopn == 2) chicut = st->chirem;
+            else {
+                chicut = std::sqrt(chicut);
+                if (chicut != 0.0f && chicut < 1.5f) chicut = 1.0f;
+                if (chicut != 0.0f && nrejTot == 0) chicut = 1.0f;
+            }
+        }
+        mpgpu_fitopts fo{1, nloopn, st->lhuber, st->lfitbb, chicut, st->chhuge, st->dwcut, st->cndlmx};
+        mpgpu_fitstats fs;
+        rc = mpgpu_loopbf(ctx, &fo, gpar.data(), nullptr, nullptr, &fs, nullptr, nullptr, nullptr);
+        if (rc) break;
+        nrejTot = 0;
+        for (int k = 0; k < 6; ++k) { res->nrej[k] = fs.nrej[k]; nrejTot += fs.nrej[k]; }
+        if (3 * nrejTot > job->nrec) { rc = MPGPU_ERR_TOOMANYREJ; break; }
+        if (!pi.empty()) rc = mpgpu_mupdat(ctx, (int32_t)pi.size(), pi.data(), pj.data(), pa.data());
+        if (rc) break;
+        double chi2D = fs.chi2SumD;
+        int64_t chi2I = fs.chi2SumI, ndfS = fs.ndfSum;
+        // measurement lines (loopn, pede.f90:2743-2798)
+        if (job->nmeas > 0) {
+            std::vector<int32_t> mi, mj, vi;
+            std::vector<double> ma, va;
+            for (int32_t m = 0; m < job->nmeas; ++m) {
+                const double rhs = job->msRhs[m], sgm = job->msSigma[m];
+                const double weight = sgm > 0.0 ? 1.0 / (sgm * sgm) : 0.0;
+                double dsum = -rhs;
+                const int32_t ia = job->msStart[m], ib = job->msStart[m + 1];
+                for (int32_t q = ia; q < ib; ++q) {
+                    int32_t li = find_label(lab, job->msLabel[q]);
+                    if (li >= 0) dsum = dsum + job->msCoef[q] * gpar[li];
+                }
+                for (int32_t q = ia; q < ib; ++q) {
+                    const double fj = job->msCoef[q];
+                    if (fj == 0.0) continue;
+                    int32_t li = find_label(lab, job->msLabel[q]);
+                    const int32_t ivj = li >= 0 ? res->varIndex[li] : 0;
+                    if (ivj <= 0) continue;
+                    vi.push_back(ivj);
+                    va.push_back(-weight * dsum * fj);
+                    for (int32_t k = ia; k <= q; ++k) {
+                        int32_t lk = find_label(lab, job->msLabel[k]);
+                        const int32_t ivk = lk >= 0 ? res->varIndex[lk] : 0;
+                        if (ivk > 0) { mi.push_back(ivj); mj.push_back(ivk); ma.push_back(weight * fj * job->msCoef[k]); }
+                    }
+                }
+                const double add = weight * dsum * dsum;
+                const int64_t nadd = (int64_t)add;
+                chi2I += nadd;
+                chi2D += add - (double)nadd;
+                ndfS += 1;
+            }
+            rc = mpgpu_vector_add(ctx, (int32_t)vi.size(), vi.data(), va.data());
+            if (!rc) rc = mpgpu_mupdat(ctx, (int32_t)mi.size(), mi.data(), mj.data(), ma.data());
+            if (rc) break;
+        }
+        res->fvalue = chi2D + (double)chi2I;
+        res->ndf = ndfS;
+        rc = mpgpu_download_vector(ctx, nullptr, gcnt.data());
+        if (rc) break;
+        // addcst: constraint residuals d - C p
+        for (int32_t c = 0; c < ncon; ++c) {
+            double rhs = job->conRhs ? job->conRhs[c] : 0.0;
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; ++k) {
+                int32_t li = find_label(lab, job->conLabel[k]);
+                if (li >= 0) rhs = rhs - job->conCoef[k] * gpar[li];
+            }
+            cres[c] = rhs;
+        }
+        mpgpu_solveinfo si;
+        const bool wantErr = (st->metsol == 1 && iter == st->mitera);
+        rc = mpgpu_solve(ctx, st->metsol, cres.data(), st->mrestl, st->itnlim, corr.data(),
+                         wantErr ? err.data() : nullptr, &si);
+        if (rc) break;
+        res->msSolve = si.ms;
+        res->nrank = si.nrank;
+        res->minresItn = si.itn;
+        res->minresIstop = si.istop;
+        if (wantErr) haveErr = true;
+        for (int32_t i = 0; i < nVar; ++i) {
+            if (!(corr[i] <= 0.0) && !(corr[i] > 0.0)) { rc = MPGPU_ERR_NAN; break; }
+            gpar[v2t[i]] += corr[i];
+        }
+        res->nloopn = nloopn;
+    }
+    for (int32_t i = 0; i < ntot; ++i) {
+        res->parameter[i] = gpar[i];
+        res->presigma[i] = psig[i];
+        res->error[i] = 0.0;
+        res->counts[i] = 0;
+        const int32_t iv = res->varIndex[i];
+        if (iv > 0) {
+            res->counts[i] = gcnt[iv - 1];
+            if (haveErr) {
+                const double e = std::sqrt(std::fabs(err[iv - 1]));
+                res->error[i] = err[iv - 1] < 0.0 ? -e : e;
+            }
+        }
+    }
+    res->exitCode = rc;
+    if (!ctxIn) mpgpu_destroy(ctx);
+    (void)qlbsub_host;
+    return rc;
+}
+
+namespace {
+// Fortran G14.5 edit descriptor as used by prtglo (pede.f90:4643)
+std::string fmt_g145(double v) {
+    char t[64], f[64], out[64];
+    if (v == 0.0) {
+        snprintf(out, sizeof out, "%14s", "0.0000    ");
+        return out;
+    }
+    snprintf(t, sizeof t, "%.4E", v);
+    const char *e = std::strchr(t, 'E');
+    const int ex = std::atoi(e + 1) + 1;  // v = 0.ddddd * 10^ex
+    if (ex >= 0 && ex <= 5) {
+        snprintf(f, sizeof f, "%.*f    ", 5 - ex, v);
+    } else {
+        std::string mant;
+        for (const char *p = t; p < e; ++p)
+            if (*p >= '0' && *p <= '9') mant += *p;
+        snprintf(f, sizeof f, "%s0.%sE%c%02d", v < 0 ? "-" : "", mant.c_str(), ex < 0 ? '-' : '+',
+                 ex < 0 ? -ex : ex);
+    }
+    snprintf(out, sizeof out, "%14s", f);
+    return out;
+}
+}  // namespace
+
+// millepede.res in the layout of prtglo (pede.f90:4477-4651): label,
+// value, pre-sigma and, for variable parameters, the difference to the
+// start value and (inversion) the error, in single precision.
+extern "C" int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors) {
+    FILE *f = std::fopen(path, "w");
+    if (!f) return MPGPU_ERR_ARG;
+    std::fprintf(f, " Parameter   ! first 3 elements per line are significant (if used as input)\n");
+    for (int32_t i = 0; i < res->nTotal; ++i) {
+        const std::string a = fmt_g145((double)(float)res->parameter[i]);
+        const std::string b = fmt_g145((double)(float)res->presigma[i]);
+        if (res->varIndex[i] <= 0) {
+            std::fprintf(f, "%10d  %s%s\n", res->labels[i], a.c_str(), b.c_str());
+        } else {
+            const std::string d = fmt_g145((double)(float)res->parameter[i]);
+            if (errors) {
+                const std::string e = fmt_g145((double)(float)res->error[i]);
+                std::fprintf(f, "%10d  %s%s%s%s\n", res->labels[i], a.c_str(), b.c_str(), d.c_str(), e.c_str());
+            } else {
+                std::fprintf(f, "%10d  %s%s%s\n", res->labels[i], a.c_str(), b.c_str(), d.c_str());
+            }
+        }
+    }
+    std::fclose(f);
+    return 0;
+}

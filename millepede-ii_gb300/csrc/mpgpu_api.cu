@@ -1,0 +1,725 @@
+// mpgpu_api.cu -- the C-ABI entry points (include/mpgpu.h): context,
+// layout, constraints, record upload, the data loop and the solver dispatch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "mpgpu_ctx.h"
+
+// ------------------------------------------------------------------ errors
+int32_t set_err(mpgpu_ctx *c, int32_t code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int32_t cuda_err(mpgpu_ctx *c, cudaError_t e, const char *where) {
+    if (c) c->err = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? MPGPU_ERR_ALLOC : MPGPU_ERR_CUDA;
+}
+
+namespace {
+
+template <class T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+template <class T>
+cudaError_t dalloc(T *&p, int64_t n) {
+    dfree(p);
+    if (n <= 0) n = 1;
+    return cudaMalloc((void **)&p, sizeof(T) * (size_t)n);
+}
+
+template <class T>
+cudaError_t dupload(T *&p, const T *h, int64_t n, cudaStream_t s) {
+    cudaError_t e = dalloc(p, n);
+    if (e != cudaSuccess) return e;
+    if (n > 0 && h) return cudaMemcpyAsync(p, h, sizeof(T) * (size_t)n, cudaMemcpyHostToDevice, s);
+    return cudaSuccess;
+}
+
+int nthreads_host() {
+    unsigned n = std::thread::hardware_concurrency();
+    if (n < 1) n = 1;
+    if (n > 64) n = 64;
+    return (int)n;
+}
+
+template <class F>
+void parallel_for(int64_t n, F f) {
+    const int nt = nthreads_host();
+    if (n < 4096 || nt == 1) {
+        f(0, n, 0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) {
+        int64_t a = n * t / nt, b = n * (t + 1) / nt;
+        th.emplace_back([=, &f] { f(a, b, t); });
+    }
+    for (auto &x : th) x.join();
+}
+
+void free_records(DevJob &j) {
+    dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
+    dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
+    dfree(j.fileWeight); dfree(j.status); dfree(j.chi2add); dfree(j.ndfadd); dfree(j.chndf);
+    dfree(j.vstage); dfree(j.entries); dfree(j.eStart); dfree(j.stage);
+    j.chunkRec.clear();
+    j.nrec = 0;
+}
+
+void free_layout(DevJob &j) {
+    dfree(j.varOfTot); dfree(j.aig); dfree(j.p2g); dfree(j.off); dfree(j.col);
+    dfree(j.matD); dfree(j.gvec); dfree(j.gcnt); dfree(j.gpar); dfree(j.work);
+}
+
+void free_constraints(DevJob &j) {
+    dfree(j.qlV); dfree(j.qlVk); dfree(j.qlR2);
+    j.ncon = 0;
+}
+
+// decodeNextMeasurement (pede.f90:2428-2468) on one record; positions
+// relative to the record start; returns false for a malformed record
+struct Eq { int32_t sl, sg, lg; };
+bool decode_record(const int32_t *in, const double *gl, int32_t nw, std::vector<Eq> &eqs) {
+    eqs.clear();
+    int32_t lg = 0;
+    const int32_t end = nw - 1;
+    for (;;) {
+        if (lg >= end) return true;
+        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
+        const int32_t sl = lg;
+        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
+        const int32_t sg = lg;
+        if (sl + 1 == sg && gl[sg] < 0.0) {
+            lg = lg + (int32_t)(-gl[sg] + 0.5);  // special data block
+            continue;
+        }
+        while (lg < end && in[lg + 1] != 0) lg++;
+        eqs.push_back({sl, sg, lg});
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+extern "C" int32_t mpgpu_create(mpgpu_ctx **out, const mpgpu_cfg *cfg) {
+    if (!out) return MPGPU_ERR_ARG;
+    *out = nullptr;
+    mpgpu_ctx *c = new mpgpu_ctx();
+    c->device = cfg ? cfg->device : 0;
+    c->stagingBytes = (cfg && cfg->staging_bytes > 0) ? cfg->staging_bytes : (int64_t)4 << 30;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&c->scal, 4096);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hscal, 4096);
+    if (e != cudaSuccess) {
+        int32_t rc = cuda_err(c, e, "mpgpu_create");
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
+    if (!c) return MPGPU_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_records(c->j);
+    free_layout(c->j);
+    free_constraints(c->j);
+    if (c->scal) cudaFree(c->scal);
+    if (c->hscal) cudaFreeHost(c->hscal);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MPGPU_OK;
+}
+
+extern "C" const char *mpgpu_last_error(const mpgpu_ctx *c) { return c ? c->err.c_str() : ""; }
+
+// ------------------------------------------------------------------ layout
+extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t *varIndexOfTotal,
+                                    int32_t nVar, int32_t nGroups, const int32_t *allIndexGroups,
+                                    int32_t matsto, const int64_t *sparseOffsets,
+                                    const int32_t *sparseColumns, int64_t ncolw, int64_t nmat) {
+    if (!c || nTotal <= 0 || nVar <= 0 || nGroups <= 0 || !varIndexOfTotal || !allIndexGroups)
+        return set_err(c, MPGPU_ERR_ARG, "mpgpu_set_layout: bad arguments");
+    if (matsto != 1 && matsto != 2) return set_err(c, MPGPU_ERR_ARG, "matsto must be 1 or 2");
+    if (matsto == 2 && (!sparseOffsets || !sparseColumns))
+        return set_err(c, MPGPU_ERR_ARG, "sparse storage needs offsets and columns");
+    if (matsto == 1) nmat = (int64_t)nVar * (nVar + 1) / 2;
+    if (allIndexGroups[nGroups] != nVar + 1) return set_err(c, MPGPU_ERR_SIZE, "groups do not end at nVar+1");
+    cudaSetDevice(c->device);
+    DevJob &j = c->j;
+    free_layout(j);
+    free_records(j);
+    j.nTotal = nTotal; j.nVar = nVar; j.nG = nGroups; j.matsto = matsto;
+    j.nmat = nmat; j.ncolw = ncolw;
+    j.hAig.assign(allIndexGroups, allIndexGroups + nGroups + 1);
+    std::vector<int32_t> p2g(nVar);
+    for (int32_t g = 1; g <= nGroups; ++g)
+        for (int32_t v = allIndexGroups[g - 1]; v < allIndexGroups[g]; ++v) {
+            if (v < 1 || v > nVar) return set_err(c, MPGPU_ERR_SIZE, "bad group table");
+            p2g[v - 1] = g;
+        }
+    cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(j.varOfTot, varIndexOfTotal, nTotal, s));
+    MPG_CUDA(c, dupload(j.aig, allIndexGroups, nGroups + 1, s));
+    MPG_CUDA(c, dupload(j.p2g, p2g.data(), nVar, s));
+    if (matsto == 2) {
+        MPG_CUDA(c, dupload(j.off, sparseOffsets, 2 * (int64_t)(nGroups + 1), s));
+        MPG_CUDA(c, dupload(j.col, sparseColumns, ncolw, s));
+    }
+    MPG_CUDA(c, dalloc(j.matD, nmat));
+    MPG_CUDA(c, cudaMemsetAsync(j.matD, 0, sizeof(double) * (size_t)nmat, s));
+    MPG_CUDA(c, dalloc(j.gvec, nVar));
+    MPG_CUDA(c, dalloc(j.gcnt, nVar));
+    MPG_CUDA(c, dalloc(j.gpar, nTotal));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    return MPGPU_OK;
+}
+
+// ------------------------------------------------------------------ constraints
+// QL decomposition of the constraint matrix (qldec, mpqldec.f90:125-196,
+// one parameter block) done on the host at set-up; the Householder vectors
+// stay on the device for the Q / Q^T products of every solve.
+extern "C" int32_t mpgpu_set_constraints(mpgpu_ctx *c, int32_t ncon, const double *A) {
+    if (!c) return MPGPU_ERR_ARG;
+    DevJob &j = c->j;
+    if (j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the constraints");
+    free_constraints(j);
+    if (ncon <= 0) return MPGPU_OK;
+    if (ncon >= j.nVar) return set_err(c, MPGPU_ERR_SIZE, "more constraints than parameters");
+    const int32_t npar = j.nVar;
+    std::vector<double> V(A, A + (size_t)ncon * npar), L((size_t)ncon * ncon, 0.0), Vk(ncon, 0.0);
+    std::vector<int32_t> r1(ncon, 1), r2(ncon, 0);
+    std::vector<double> vn(npar);
+    for (int32_t k = ncon; k >= 1; --k) {
+        const int32_t kn = npar + k - ncon;
+        double *row = &V[(size_t)(k - 1) * npar];
+        double nrm = 0.0;
+        for (int32_t q = 0; q < kn; ++q) { vn[q] = row[q]; nrm = nrm + vn[q] * vn[q]; }
+        nrm = std::sqrt(nrm);
+        if (nrm == 0.0) return set_err(c, MPGPU_ERR_QL, "empty constraint");
+        if (vn[kn - 1] >= 0.0) vn[kn - 1] = vn[kn - 1] + nrm;
+        else vn[kn - 1] = vn[kn - 1] - nrm;
+        nrm = 0.0;
+        for (int32_t q = 0; q < kn; ++q) nrm = nrm + vn[q] * vn[q];
+        nrm = std::sqrt(nrm);
+        for (int32_t q = 0; q < kn; ++q) vn[q] = vn[q] / nrm;
+        for (int32_t i = 1; i <= k; ++i) {
+            double *ri = &V[(size_t)(i - 1) * npar];
+            double sp = 0.0;
+            for (int32_t q = 0; q < kn; ++q) sp = sp + vn[q] * ri[q];
+            for (int32_t q = 0; q < kn; ++q) ri[q] = ri[q] - 2.0 * vn[q] * sp;
+        }
+        for (int32_t cc = k; cc <= ncon; ++cc) L[(size_t)(k - 1) * ncon + cc - 1] = row[kn - 1 + cc - k];
+        for (int32_t q = 0; q < kn - 1; ++q) row[q] = vn[q];
+        for (int32_t q = kn - 1; q < npar; ++q) row[q] = 0.0;
+        r2[k - 1] = kn - 1;
+        Vk[k - 1] = vn[kn - 1];
+    }
+    for (int32_t k = 0; k < ncon; ++k)
+        if (L[(size_t)k * ncon + k] == 0.0) return set_err(c, MPGPU_ERR_QL, "singular constraints");
+    j.ncon = ncon;
+    j.hV = V; j.hVk = Vk; j.hL = L; j.hR1 = r1; j.hR2 = r2;
+    cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(j.qlV, V.data(), (int64_t)ncon * npar, s));
+    MPG_CUDA(c, dupload(j.qlVk, Vk.data(), ncon, s));
+    MPG_CUDA(c, dupload(j.qlR2, r2.data(), ncon, s));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    return MPGPU_OK;
+}
+
+// ------------------------------------------------------------------ records
+// One host pass builds the per-record tables the kernels need (measurement
+// boundaries, sorted variable parameters, parameter groups, band structure
+// of the local matrix, owner lists per parameter group); the records then
+// stay resident on the device for all data loops of the job.
+extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
+                                        const int32_t *inder, const double *glder,
+                                        const int32_t *recFile, int32_t nfiles,
+                                        const double *fileWeight) {
+    if (!c || nrec < 0 || !recPtr || !inder || !glder) return MPGPU_ERR_ARG;
+    DevJob &j = c->j;
+    if (j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the records");
+    cudaSetDevice(c->device);
+    free_records(j);
+    if (nfiles < 1) nfiles = 1;
+    j.nfiles = nfiles;
+    j.nrec = nrec;
+    j.nw = recPtr[nrec] - recPtr[0];
+    const int32_t nVar = j.nVar, nTotal = j.nTotal;
+    std::vector<int32_t> varOfTot(nTotal);
+    MPG_CUDA(c, cudaMemcpy(varOfTot.data(), j.varOfTot, sizeof(int32_t) * nTotal, cudaMemcpyDeviceToHost));
+    const std::vector<int32_t> &aig = j.hAig;
+    std::vector<int32_t> p2g(nVar);
+    for (int32_t g = 1; g <= j.nG; ++g)
+        for (int32_t v = aig[g - 1]; v < aig[g]; ++v) p2g[v - 1] = g;
+
+    // ---- pass A: sizes and structure per record
+    std::vector<RecInfo> rec(nrec);
+    std::vector<int32_t> errRec(nthreads_host() + 1, 0);
+    std::vector<int64_t> errAt(nthreads_host() + 1, -1);
+    parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
+        std::vector<Eq> eqs;
+        std::vector<int32_t> stamp(nVar + 1, 0), ibandh;
+        std::vector<int32_t> sl;
+        for (int64_t r = a; r < b; ++r) {
+            RecInfo &ri = rec[r];
+            memset(&ri, 0, sizeof(ri));
+            const int64_t w0 = recPtr[r];
+            const int64_t nw64 = recPtr[r + 1] - w0;
+            const int32_t *in = inder + w0;
+            const double *gl = glder + w0;
+            ri.w0 = w0 - recPtr[0];
+            ri.file = recFile ? recFile[r] : 1;
+            if (nw64 < 1 || nw64 > MPG_WORDS_MAX || ri.file < 1 || ri.file > nfiles ||
+                !decode_record(in, gl, (int32_t)nw64, eqs)) {
+                errRec[t] = MPGPU_ERR_BADRECORD; errAt[t] = r; return;
+            }
+            ri.nw = (int32_t)nw64;
+            ri.neq = (int32_t)eqs.size();
+            int32_t nalc = 0, nalg = 0, nsw = 0;
+            bool nonmono = false;
+            sl.clear();
+            for (const Eq &e : eqs) {
+                int32_t prev = 0;
+                for (int32_t q = e.sl + 1; q < e.sg; ++q) {
+                    const int32_t li = in[q];
+                    if (li <= 0) { errRec[t] = MPGPU_ERR_BADRECORD; errAt[t] = r; return; }
+                    if (li > nalc) nalc = li;
+                    if (li <= prev) nonmono = true;
+                    prev = li;
+                }
+                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
+                    const int32_t ti = in[q];
+                    if (ti < 1 || ti > nTotal) { errRec[t] = MPGPU_ERR_BADINDEX; errAt[t] = r; return; }
+                    const int32_t v = varOfTot[ti - 1];
+                    if (v > 0) {
+                        nsw++;
+                        if (stamp[v] != (int32_t)(r - a + 1)) { stamp[v] = (int32_t)(r - a + 1); sl.push_back(v); }
+                    }
+                }
+            }
+            nalg = (int32_t)sl.size();
+            ri.nalc = nalc;
+            ri.nalg = nalg;
+            // groups of the sorted variable parameters; the record must hold
+            // complete groups (loopbf's npar == nalg check, pede.f90:3710-3724)
+            std::sort(sl.begin(), sl.end());
+            int32_t ngrp = 0, prevg = -1, npar = 0;
+            for (int32_t v : sl) {
+                const int32_t g = p2g[v - 1];
+                if (g != prevg) { ngrp++; prevg = g; npar += aig[g] - aig[g - 1]; }
+            }
+            if (nalc > 0 && npar != nalg) { errRec[t] = MPGPU_ERR_GROUPS; errAt[t] = r; return; }
+            if (ngrp > MPG_NGRP_MAX) { errRec[t] = MPGPU_ERR_LIMIT; errAt[t] = r; return; }
+            ri.ngrp = ngrp;
+            // bordered band structure of the local matrix (pede.f90:3812-3874)
+            ri.mbnd = -1; ri.mbdr = (int16_t)nalc; ri.mside = -1;
+            if (nalc > 5) {
+                ibandh.assign(2 * nalc + 2, 0);
+                for (const Eq &e : eqs)
+                    for (int32_t jq = e.sl + 1; jq < e.sg; ++jq)
+                        for (int32_t kq = e.sl + 1; kq <= jq; ++kq) {
+                            const int32_t ij = in[jq], ik = in[kq];
+                            const int32_t id = std::abs(ij - ik) + 1;
+                            int32_t im = std::min(ij, ik);
+                            ibandh[id] = std::max(ibandh[id], im);
+                            im = std::min(nalc + 1 - ij, nalc + 1 - ik);
+                            ibandh[nalc + id] = std::max(ibandh[nalc + id], im);
+                        }
+                int32_t kx = -1, kbdrx = 0, kbdr = 0, side = -1;
+                int64_t icmn = (int64_t)nalc * nalc * nalc;
+                for (int32_t k = nalc; k >= 2; --k) {
+                    const int32_t kbnd = k - 2;
+                    kbdr = std::max(kbdr, ibandh[k]);
+                    const int64_t w = kbnd + kbdr + 1;
+                    const int64_t icost = 6 * (int64_t)(nalc - kbdr) * w * w + 2 * (int64_t)kbdr * kbdr * kbdr;
+                    if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 1; }
+                }
+                if (kx < 0) {
+                    kbdr = 0;
+                    for (int32_t k = nalc; k >= 2; --k) {
+                        const int32_t kbnd = k - 2;
+                        kbdr = std::max(kbdr, ibandh[k + nalc]);
+                        const int64_t w = kbnd + kbdr + 1;
+                        const int64_t icost = 6 * (int64_t)(nalc - kbdr) * w * w + 2 * (int64_t)kbdr * kbdr * kbdr;
+                        if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 2; }
+                    }
+                }
+                if (kx > 0) { ri.mbnd = (int16_t)(kx - 2); ri.mbdr = (int16_t)kbdrx; ri.mside = side; }
+            }
+            ri.mside = (ri.mside & 0xff) | (nonmono ? 0x100 : 0);
+            ri.measOff = nsw;  // temporarily: number of slot words
+        }
+    });
+    for (size_t t = 0; t < errRec.size(); ++t)
+        if (errRec[t]) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "record %lld rejected at upload (code %d)", (long long)errAt[t], errRec[t]);
+            return set_err(c, errRec[t], buf);
+        }
+
+    // ---- pass B: offsets, maxima, chunks by staging size
+    int64_t neqT = 0, nslotT = 0, nswT = 0, ngrpT = 0;
+    j.maxNw = j.maxNeq = j.maxNalc = j.maxNalg = 0;
+    j.maxBand = -1; j.maxBdr = 0;
+    j.nbndr[0] = j.nbndr[1] = 0; j.nbdrx = j.nbndx = 0;
+    const int64_t stageElems = std::max<int64_t>(c->stagingBytes / 8, 1);
+    j.chunkRec.assign(1, 0);
+    int64_t upd = 0, maxStage = 0;
+    for (int64_t r = 0; r < nrec; ++r) {
+        RecInfo &ri = rec[r];
+        const int64_t nsw = ri.measOff;
+        ri.measOff = neqT; neqT += ri.neq;
+        ri.slotOff = nslotT; nslotT += ri.nalg + 1;
+        ri.swOff = nswT; nswT += nsw;
+        ri.grpOff = ngrpT; ngrpT += ri.ngrp;
+        const int64_t ngg = (int64_t)ri.nalg * (ri.nalg + 1) / 2;
+        if (ngg > stageElems) return set_err(c, MPGPU_ERR_LIMIT, "record update larger than the staging buffer");
+        if (upd + ngg > stageElems) { j.chunkRec.push_back(r); maxStage = std::max(maxStage, upd); upd = 0; }
+        ri.updOff = upd;
+        upd += ngg;
+        j.maxNw = std::max(j.maxNw, ri.nw);
+        j.maxNeq = std::max(j.maxNeq, ri.neq);
+        j.maxNalc = std::max(j.maxNalc, ri.nalc);
+        j.maxNalg = std::max(j.maxNalg, ri.nalg);
+        if (ri.mbnd >= 0) {
+            j.maxBand = std::max<int32_t>(j.maxBand, ri.mbnd);
+            j.maxBdr = std::max<int32_t>(j.maxBdr, ri.mbdr);
+            j.nbndr[(ri.mside & 0xff) - 1]++;
+            j.nbdrx = std::max<int32_t>(j.nbdrx, ri.mbdr);
+            j.nbndx = std::max<int32_t>(j.nbndx, ri.mbnd);
+        }
+    }
+    j.chunkRec.push_back(nrec);
+    maxStage = std::max(maxStage, upd);
+    j.neqTot = neqT; j.nslotTot = nslotT; j.nswTot = nswT; j.ngrpTot = ngrpT;
+    if (j.maxNalc > MPG_NALC_MAX) return set_err(c, MPGPU_ERR_LIMIT, "local system larger than the fit kernel limit");
+
+    // ---- pass C: fill the tables
+    std::vector<int32_t> meas(3 * neqT), slots(nslotT), slotCnt(nslotT), swStart(nslotT), sw(nswT);
+    std::vector<int32_t> grpId(ngrpT), grpSlot(ngrpT);
+    parallel_for(nrec, [&](int64_t a, int64_t b, int) {
+        std::vector<Eq> eqs;
+        std::vector<int32_t> pos(nVar + 1, -1), cnt;
+        for (int64_t r = a; r < b; ++r) {
+            const RecInfo &ri = rec[r];
+            const int32_t *in = inder + recPtr[r];
+            const double *gl = glder + recPtr[r];
+            decode_record(in, gl, ri.nw, eqs);
+            for (int32_t e = 0; e < ri.neq; ++e) {
+                meas[3 * (ri.measOff + e)] = eqs[e].sl;
+                meas[3 * (ri.measOff + e) + 1] = eqs[e].sg;
+                meas[3 * (ri.measOff + e) + 2] = eqs[e].lg;
+            }
+            // sorted slots
+            int32_t *sl = &slots[ri.slotOff];
+            int32_t n = 0;
+            for (const Eq &e : eqs)
+                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
+                    const int32_t v = varOfTot[in[q] - 1];
+                    if (v > 0 && pos[v] < 0) { pos[v] = 0; sl[n++] = v; }
+                }
+            std::sort(sl, sl + n);
+            sl[n] = 0;
+            for (int32_t s = 0; s < n; ++s) pos[sl[s]] = s;
+            // word lists per slot, in equation order (counting sort)
+            cnt.assign(n + 1, 0);
+            int32_t *cs = &slotCnt[ri.slotOff];
+            for (int32_t s = 0; s <= n; ++s) cs[s] = 0;
+            for (const Eq &e : eqs)
+                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
+                    const int32_t v = varOfTot[in[q] - 1];
+                    if (v > 0) {
+                        cnt[pos[v] + 1]++;
+                        if (gl[q] != 0.0) cs[pos[v]]++;
+                    }
+                }
+            int32_t *ss = &swStart[ri.slotOff];
+            ss[0] = 0;
+            for (int32_t s = 0; s < n; ++s) ss[s + 1] = ss[s] + cnt[s + 1];
+            std::vector<int32_t> fillp(ss, ss + n);
+            for (int32_t e = 0; e < ri.neq; ++e)
+                for (int32_t q = eqs[e].sg + 1; q <= eqs[e].lg; ++q) {
+                    const int32_t v = varOfTot[in[q] - 1];
+                    if (v > 0) sw[ri.swOff + fillp[pos[v]]++] = (e << 16) | q;
+                }
+            // groups
+            int32_t g = 0, prevg = -1;
+            for (int32_t s = 0; s < n; ++s) {
+                const int32_t gg = p2g[sl[s] - 1];
+                if (gg != prevg) {
+                    grpId[ri.grpOff + g] = gg;
+                    grpSlot[ri.grpOff + g] = s;
+                    g++;
+                    prevg = gg;
+                }
+            }
+            for (int32_t s = 0; s < n; ++s) pos[sl[s]] = -1;
+        }
+    });
+
+    // ---- pass D: owner lists per parameter group and chunk (record order)
+    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
+    const int32_t nG = j.nG;
+    std::vector<int64_t> eStart((size_t)nchunk * (nG + 1));
+    std::vector<int64_t> entries(ngrpT);
+    int64_t ebase = 0;
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        int64_t *es = &eStart[(size_t)ch * (nG + 1)];
+        std::vector<int64_t> cntg(nG + 1, 0);
+        for (int64_t r = j.chunkRec[ch]; r < j.chunkRec[ch + 1]; ++r)
+            if (rec[r].nalc > 0)
+                for (int32_t q = 0; q < rec[r].ngrp; ++q) cntg[grpId[rec[r].grpOff + q]]++;
+        es[0] = ebase;
+        for (int32_t g = 1; g <= nG; ++g) es[g] = es[g - 1] + cntg[g];
+        std::vector<int64_t> fillp(es, es + nG);
+        for (int64_t r = j.chunkRec[ch]; r < j.chunkRec[ch + 1]; ++r)
+            if (rec[r].nalc > 0)
+                for (int32_t q = 0; q < rec[r].ngrp; ++q) {
+                    const int32_t g = grpId[rec[r].grpOff + q];
+                    entries[fillp[g - 1]++] = (r << 8) | q;
+                }
+        ebase = es[nG];
+    }
+
+    // ---- upload
+    cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(j.inder, inder + recPtr[0], j.nw, s));
+    MPG_CUDA(c, dupload(j.glder, glder + recPtr[0], j.nw, s));
+    MPG_CUDA(c, dupload(j.rec, rec.data(), nrec, s));
+    MPG_CUDA(c, dupload(j.meas, meas.data(), 3 * neqT, s));
+    MPG_CUDA(c, dupload(j.slots, slots.data(), nslotT, s));
+    MPG_CUDA(c, dupload(j.slotCnt, slotCnt.data(), nslotT, s));
+    MPG_CUDA(c, dupload(j.swStart, swStart.data(), nslotT, s));
+    MPG_CUDA(c, dupload(j.sw, sw.data(), nswT, s));
+    MPG_CUDA(c, dupload(j.grpId, grpId.data(), ngrpT, s));
+    MPG_CUDA(c, dupload(j.grpSlot, grpSlot.data(), ngrpT, s));
+    MPG_CUDA(c, dupload(j.entries, entries.data(), ebase, s));
+    MPG_CUDA(c, dupload(j.eStart, eStart.data(), (int64_t)eStart.size(), s));
+    std::vector<double> fw(nfiles, 1.0);
+    if (fileWeight) fw.assign(fileWeight, fileWeight + nfiles);
+    MPG_CUDA(c, dupload(j.fileWeight, fw.data(), nfiles, s));
+    MPG_CUDA(c, dalloc(j.status, nrec));
+    MPG_CUDA(c, dalloc(j.chi2add, nrec));
+    MPG_CUDA(c, dalloc(j.ndfadd, nrec));
+    MPG_CUDA(c, dalloc(j.chndf, nrec));
+    MPG_CUDA(c, dalloc(j.vstage, nslotT));
+    j.stageLen = maxStage;
+    MPG_CUDA(c, dalloc(j.stage, maxStage));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    return MPGPU_OK;
+}
+
+// ------------------------------------------------------------------ data loop
+static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *stats,
+                        int32_t *naccf, float *chi2f, int32_t *ndff) {
+    DevJob &j = c->j;
+    cudaStream_t s = c->stream;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    int32_t *errFlag = (int32_t *)c->scal;
+    MPG_CUDA(c, cudaMemsetAsync(errFlag, 0, 64, s));
+    MPG_CUDA(c, cudaMemsetAsync(j.gvec, 0, sizeof(double) * j.nVar, s));
+    MPG_CUDA(c, cudaMemsetAsync(j.gcnt, 0, sizeof(int64_t) * j.nVar, s));
+    if (opt->icalcm == 1) MPG_CUDA(c, cudaMemsetAsync(j.matD, 0, sizeof(double) * (size_t)j.nmat, s));
+    FitParams fp{};
+    fp.rec = j.rec; fp.inder = j.inder; fp.glder = j.glder; fp.meas = j.meas;
+    fp.slots = j.slots; fp.swStart = j.swStart; fp.sw = j.sw; fp.gpar = j.gpar;
+    fp.varOfTot = j.varOfTot; fp.fileWeight = j.fileWeight;
+    fp.icalcm = opt->icalcm; fp.nloopn = opt->nloopn; fp.lhuber = opt->lhuber; fp.lfitbb = opt->lfitbb;
+    fp.chicut = opt->chicut; fp.chhuge = opt->chhuge; fp.dwcut = opt->dwcut; fp.cndlmx = opt->cndlmx;
+    fp.stage = j.stage; fp.vstage = j.vstage; fp.status = j.status; fp.chi2add = j.chi2add;
+    fp.ndfadd = j.ndfadd; fp.chndf = j.chndf;
+    fp.wmax = std::max(j.maxNw, 1); fp.neqmax = std::max(j.maxNeq, 1);
+    fp.nalcmax = std::max(j.maxNalc, 1); fp.nalgmax = std::max(j.maxNalg, 1);
+    fp.bandmax = opt->lfitbb > 0 ? j.maxBand : -1; fp.bdrmax = j.maxBdr;
+    fp.errFlag = errFlag;
+    if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
+    AccParams ap{};
+    ap.rec = j.rec; ap.entries = j.entries; ap.grpId = j.grpId; ap.grpSlot = j.grpSlot;
+    ap.status = j.status; ap.stage = j.stage; ap.vstage = j.vstage; ap.slotCnt = j.slotCnt;
+    ap.aig = j.aig; ap.off = j.off; ap.col = j.col; ap.nG = j.nG; ap.matsto = j.matsto;
+    ap.icalcm = opt->icalcm; ap.matD = j.matD; ap.gvec = j.gvec; ap.gcnt = j.gcnt; ap.errFlag = errFlag;
+    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        fp.r0 = j.chunkRec[ch];
+        fp.r1 = j.chunkRec[ch + 1];
+        if (fp.r1 <= fp.r0) continue;
+        MPG_CUDA(c, launch_fit(fp, nsm, s));
+        ap.eStart = j.eStart + ch * (j.nG + 1);
+        MPG_CUDA(c, launch_accumulate(ap, nsm, s));
+    }
+    // statistics
+    const int32_t nf = j.nfiles;
+    int64_t *iout = (int64_t *)(c->scal + 8);
+    double *dout = c->scal + 4;
+    float *fout = (float *)(c->scal + 256);
+    const int64_t nint = 9 + 2 * (int64_t)nf;
+    if (nint > 240 || nf > 400) return set_err(c, MPGPU_ERR_LIMIT, "too many files for the statistics buffer");
+    MPG_CUDA(c, cudaMemsetAsync(iout, 0, sizeof(int64_t) * nint, s));
+    StatParams sp{j.status, j.chi2add, j.ndfadd, j.chndf, j.rec, j.fileWeight, j.nrec, nf,
+                  dout, iout, fout};
+    MPG_CUDA(c, launch_stats(sp, s));
+    MPG_CUDA(c, cudaMemcpyAsync(c->hscal, c->scal, 4096, cudaMemcpyDeviceToHost, s));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    const int32_t *hflag = (const int32_t *)c->hscal;
+    if (hflag[0]) return set_err(c, hflag[0], "device index error in the data loop");
+    const int64_t *hi = (const int64_t *)(c->hscal + 8);
+    const double *hd = c->hscal + 4;
+    const float *hf = (const float *)(c->hscal + 256);
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        for (int k = 0; k < 6; ++k) stats->nrej[k] = hi[2 + k];
+        stats->chi2SumI = hi[0];
+        stats->chi2SumD = hd[0];
+        stats->ndfSum = hi[1];
+        stats->ndfSumW = hd[1];
+        if (opt->nloopn == 1 && opt->lfitbb > 0) {
+            stats->nbndr[0] = j.nbndr[0]; stats->nbndr[1] = j.nbndr[1];
+            stats->nbdrx = j.nbdrx; stats->nbndx = j.nbndx;
+        }
+        stats->naccepted = hi[8];
+    }
+    c->lastNaccepted = hi[8];
+    for (int32_t f = 0; f < nf; ++f) {
+        if (naccf) naccf[f] += (int32_t)hi[9 + f];
+        if (ndff) ndff[f] += (int32_t)hi[9 + nf + f];
+        if (chi2f) chi2f[f] += hf[f];
+    }
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_loopbf_device(mpgpu_ctx *c, const mpgpu_fitopts *opt,
+                                       const double *d_globalParameter, mpgpu_fitstats *stats) {
+    if (!c || !opt) return MPGPU_ERR_ARG;
+    if (c->j.nrec <= 0 || !c->j.rec) return set_err(c, MPGPU_ERR_ARG, "no records uploaded");
+    cudaSetDevice(c->device);
+    if (d_globalParameter && d_globalParameter != c->j.gpar)
+        MPG_CUDA(c, cudaMemcpyAsync(c->j.gpar, d_globalParameter, sizeof(double) * c->j.nTotal,
+                                    cudaMemcpyDeviceToDevice, c->stream));
+    return run_loop(c, opt, stats, nullptr, nullptr, nullptr);
+}
+
+extern "C" int32_t mpgpu_loopbf(mpgpu_ctx *c, const mpgpu_fitopts *opt, const double *globalParameter,
+                                double *globalVector, int64_t *globalCounter, mpgpu_fitstats *stats,
+                                int32_t *naccf, float *chi2f, int32_t *ndff) {
+    if (!c || !opt || !globalParameter) return MPGPU_ERR_ARG;
+    if (c->j.nrec <= 0 || !c->j.rec) return set_err(c, MPGPU_ERR_ARG, "no records uploaded");
+    cudaSetDevice(c->device);
+    DevJob &j = c->j;
+    MPG_CUDA(c, cudaMemcpyAsync(j.gpar, globalParameter, sizeof(double) * j.nTotal,
+                                cudaMemcpyHostToDevice, c->stream));
+    int32_t rc = run_loop(c, opt, stats, naccf, chi2f, ndff);
+    if (rc) return rc;
+    if (globalVector)
+        MPG_CUDA(c, cudaMemcpyAsync(globalVector, j.gvec, sizeof(double) * j.nVar, cudaMemcpyDeviceToHost, c->stream));
+    if (globalCounter)
+        MPG_CUDA(c, cudaMemcpyAsync(globalCounter, j.gcnt, sizeof(int64_t) * j.nVar, cudaMemcpyDeviceToHost, c->stream));
+    MPG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_mupdat(mpgpu_ctx *c, int32_t n, const int32_t *i, const int32_t *jj,
+                                const double *add) {
+    if (!c || n < 0) return MPGPU_ERR_ARG;
+    if (n == 0) return MPGPU_OK;
+    DevJob &j = c->j;
+    int32_t *di = nullptr, *dj = nullptr;
+    double *da = nullptr;
+    cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(di, i, n, s));
+    MPG_CUDA(c, dupload(dj, jj, n, s));
+    MPG_CUDA(c, dupload(da, add, n, s));
+    int32_t *errFlag = (int32_t *)c->scal;
+    MPG_CUDA(c, cudaMemsetAsync(errFlag, 0, 4, s));
+    MPG_CUDA(c, launch_mupdat(n, di, dj, da, j, errFlag, s));
+    int32_t h = 0;
+    MPG_CUDA(c, cudaMemcpyAsync(&h, errFlag, 4, cudaMemcpyDeviceToHost, s));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    dfree(di); dfree(dj); dfree(da);
+    if (h) return set_err(c, h, "mupdat index outside the matrix");
+    return MPGPU_OK;
+}
+
+namespace {
+__global__ void k_vadd(int32_t n, const int32_t *idx, const double *v, double *gvec, int32_t nVar) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int32_t q = 0; q < n; ++q)
+        if (idx[q] >= 1 && idx[q] <= nVar) gvec[idx[q] - 1] += v[q];
+}
+}  // namespace
+
+extern "C" int32_t mpgpu_vector_add(mpgpu_ctx *c, int32_t n, const int32_t *vidx, const double *vadd) {
+    if (!c || n < 0) return MPGPU_ERR_ARG;
+    if (n == 0) return MPGPU_OK;
+    int32_t *di = nullptr;
+    double *da = nullptr;
+    cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(di, vidx, n, s));
+    MPG_CUDA(c, dupload(da, vadd, n, s));
+    k_vadd<<<1, 32, 0, s>>>(n, di, da, c->j.gvec, c->j.nVar);
+    MPG_CUDA(c, cudaGetLastError());
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    dfree(di); dfree(da);
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_download_matrix(mpgpu_ctx *c, double *globalMatD) {
+    if (!c || !globalMatD) return MPGPU_ERR_ARG;
+    MPG_CUDA(c, cudaMemcpy(globalMatD, c->j.matD, sizeof(double) * (size_t)c->j.nmat, cudaMemcpyDeviceToHost));
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_download_vector(mpgpu_ctx *c, double *globalVector, int64_t *globalCounter) {
+    if (!c) return MPGPU_ERR_ARG;
+    if (globalVector)
+        MPG_CUDA(c, cudaMemcpy(globalVector, c->j.gvec, sizeof(double) * c->j.nVar, cudaMemcpyDeviceToHost));
+    if (globalCounter)
+        MPG_CUDA(c, cudaMemcpy(globalCounter, c->j.gcnt, sizeof(int64_t) * c->j.nVar, cudaMemcpyDeviceToHost));
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_download_record_status(mpgpu_ctx *c, int32_t *status) {
+    if (!c || !status) return MPGPU_ERR_ARG;
+    std::vector<int8_t> st(c->j.nrec);
+    MPG_CUDA(c, cudaMemcpy(st.data(), c->j.status, c->j.nrec, cudaMemcpyDeviceToHost));
+    for (int64_t r = 0; r < c->j.nrec; ++r) status[r] = st[r];
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_solve(mpgpu_ctx *c, int32_t metsol, const double *consResiduals,
+                               double rtol, int32_t itnlim, double *correction, double *errors,
+                               mpgpu_solveinfo *info) {
+    if (!c || !correction) return MPGPU_ERR_ARG;
+    cudaSetDevice(c->device);
+    mpgpu_solveinfo tmp;
+    if (!info) info = &tmp;
+    memset(info, 0, sizeof(*info));
+    if (metsol == 1 || metsol == 3) {
+        if (c->j.matsto != 1) return set_err(c, MPGPU_ERR_ARG, "inversion/decomposition need packed storage");
+        return solve_inversion(c, consResiduals, correction, errors, info, metsol == 3);
+    }
+    if (metsol == 4) return solve_minres(c, consResiduals, rtol, itnlim, correction, info);
+    return set_err(c, MPGPU_ERR_ARG, "unsupported solution method");
+}
+
+extern "C" int32_t mpgpu_avprod(mpgpu_ctx *c, int32_t n, const double *x, double *b) {
+    if (!c || !x || !b) return MPGPU_ERR_ARG;
+    if (n != c->j.nVar - c->j.ncon) return set_err(c, MPGPU_ERR_SIZE, "avprod: vector/matrix size mismatch");
+    cudaSetDevice(c->device);
+    return avprod_host(c, n, x, b);
+}

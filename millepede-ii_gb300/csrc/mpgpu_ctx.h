@@ -1,0 +1,189 @@
+// mpgpu_ctx.h -- device-resident state of one alignment job and the kernel
+// interfaces shared by the translation units of libmpgpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/mpgpu.h"
+
+#define MPG_WARPS_FIT 8        // warps per CTA of the local-fit kernel
+#define MPG_NALC_MAX 96        // largest local system handled by the fit kernel
+#define MPG_NGRP_MAX 255       // parameter groups per record (entry encoding)
+#define MPG_WORDS_MAX 65535    // words per record (16-bit word positions)
+
+// Per-record description built once at upload (host pass over the records).
+struct alignas(16) RecInfo {
+    int64_t w0;        // first word (error-count word) in the record arrays
+    int64_t measOff;   // first equation in the measurement table
+    int64_t slotOff;   // first entry of the per-slot arrays (stride nalg+1)
+    int64_t updOff;    // first element of the update matrix in the chunk staging
+    int64_t swOff;     // first entry of the slot-word lists
+    int64_t grpOff;    // first entry of the group list
+    int32_t nw, neq, nalc, nalg;
+    int32_t ngrp;
+    int16_t mbnd, mbdr;   // bordered band structure (mbnd < 0: dense)
+    int32_t mside;        // 1 upper/left, 2 lower/right border
+    int32_t file;         // 1-based file index
+};
+
+// Device arrays of one job.  Every pointer is owned by the context.
+struct DevJob {
+    // layout
+    int32_t nTotal = 0, nVar = 0, nG = 0, matsto = 1;
+    int64_t nmat = 0, ncolw = 0;
+    int32_t *varOfTot = nullptr;   // [nTotal]
+    int32_t *aig = nullptr;        // [nG+1] first variable index of each group
+    int32_t *p2g = nullptr;        // [nVar]
+    int64_t *off = nullptr;        // [2*(nG+1)] sparseMatrixOffsets
+    int32_t *col = nullptr;        // [ncolw] sparseMatrixColumns
+    double *matD = nullptr;        // [nmat]
+    double *gvec = nullptr;        // [nVar]
+    int64_t *gcnt = nullptr;       // [nVar]
+    double *gpar = nullptr;        // [nTotal]
+    // records
+    int64_t nrec = 0, nw = 0, neqTot = 0, nslotTot = 0, nswTot = 0, ngrpTot = 0;
+    int32_t nfiles = 1;
+    int32_t *inder = nullptr;
+    double *glder = nullptr;
+    RecInfo *rec = nullptr;
+    int32_t *meas = nullptr;       // 3 per equation: startLocal, startGlobal, lastGlobal
+    int32_t *slots = nullptr;      // sorted variable indices per record (+1 spare)
+    int32_t *slotCnt = nullptr;    // accepted-entry count per slot (structural)
+    int32_t *swStart = nullptr;    // per slot: start of its word list (relative)
+    int32_t *sw = nullptr;         // (eq << 16) | word position
+    int32_t *grpId = nullptr;      // group of each record group entry
+    int32_t *grpSlot = nullptr;    // first slot of each record group entry
+    double *fileWeight = nullptr;  // [nfiles]
+    // per-loop outputs
+    int8_t *status = nullptr;
+    double *chi2add = nullptr;
+    int32_t *ndfadd = nullptr;
+    float *chndf = nullptr;
+    double *vstage = nullptr;      // per-slot vector contributions
+    // chunks of records sharing one update staging buffer
+    std::vector<int64_t> chunkRec;     // [nchunk+1] record boundaries
+    int64_t *entries = nullptr;        // (record << 8) | group position
+    int64_t *eStart = nullptr;         // [nchunk*(nG+1)]
+    double *stage = nullptr;
+    int64_t stageLen = 0;
+    // limits over the job (fit kernel shared memory sizing)
+    int32_t maxNw = 0, maxNeq = 0, maxNalc = 0, maxNalg = 0, maxBand = -1, maxBdr = 0;
+    int32_t nbndr[2] = {0, 0}, nbdrx = 0, nbndx = 0;
+    // constraints (QL of the constraint matrix, kept on the device)
+    int32_t ncon = 0;
+    double *qlV = nullptr;         // [ncon*nVar] Householder vectors (row k)
+    double *qlVk = nullptr;        // [ncon]
+    int32_t *qlR2 = nullptr;       // [ncon] last non-zero index of each vector
+    std::vector<double> hL;        // [ncon*ncon] lower triangle L (host)
+    std::vector<double> hV, hVk;
+    std::vector<int32_t> hR1, hR2;
+    // host copies needed by the host-side control
+    std::vector<int32_t> hAig;
+    // solver workspace
+    double *work = nullptr;
+    int64_t workLen = 0;
+};
+
+struct mpgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int64_t stagingBytes = 0;
+    std::string err;
+    DevJob j;
+    double *scal = nullptr;      // small device scalar area
+    double *hscal = nullptr;     // pinned mirror
+    int64_t lastNaccepted = 0;
+};
+
+// ---------------------------------------------------------------- kernels
+struct FitParams {
+    const RecInfo *rec;
+    const int32_t *inder;
+    const double *glder;
+    const int32_t *meas;
+    const int32_t *slots;
+    const int32_t *swStart;
+    const int32_t *sw;
+    const double *gpar;
+    const int32_t *varOfTot;
+    const double *fileWeight;
+    int64_t r0, r1;           // record range
+    int32_t icalcm, nloopn, lhuber, lfitbb;
+    float chicut, chhuge, dwcut, cndlmx;
+    double *stage;            // update staging of this chunk
+    double *vstage;
+    int8_t *status;
+    double *chi2add;
+    int32_t *ndfadd;
+    float *chndf;
+    int32_t wmax, neqmax, nalcmax, nalgmax, bandmax, bdrmax;  // shared-memory sizing
+    int32_t *errFlag;
+};
+
+int fit_smem_per_warp(const FitParams &p);
+int fit_warps_per_cta(const FitParams &p);
+cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s);
+
+struct AccParams {
+    const RecInfo *rec;
+    const int64_t *entries;
+    const int64_t *eStart;
+    const int32_t *grpId, *grpSlot;
+    const int8_t *status;
+    const double *stage;
+    const double *vstage;
+    const int32_t *slotCnt;
+    const int32_t *aig;
+    const int64_t *off;
+    const int32_t *col;
+    int32_t nG, matsto, icalcm;
+    double *matD;
+    double *gvec;
+    int64_t *gcnt;
+    int32_t *errFlag;
+};
+cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s);
+
+struct StatParams {
+    const int8_t *status;
+    const double *chi2add;
+    const int32_t *ndfadd;
+    const float *chndf;
+    const RecInfo *rec;
+    const double *fileWeight;
+    int64_t nrec;
+    int32_t nfiles;
+    double *out;     // device: [0] fraction sum, [1] ndfSumW
+    int64_t *iout;   // device: [0] chi2 int, [1] ndf, [2..7] nrej, [8] naccepted,
+                     //         then naccf[nfiles], ndff[nfiles]
+    float *fout;     // device: chi2f[nfiles]
+};
+cudaError_t launch_stats(const StatParams &p, cudaStream_t s);
+
+// matrix-element updates (mupdat), applied in order by one thread
+cudaError_t launch_mupdat(int32_t n, const int32_t *i, const int32_t *j, const double *add,
+                          const DevJob &d, int32_t *errFlag, cudaStream_t s);
+
+// device version of ijpgrp (pede.f90:5371-5461); returns the 1-based index
+// of the first element of block (itema, itemb) and its row length
+__device__ int64_t d_ijpgrp(int32_t itema, int32_t itemb, int32_t nG, const int32_t *aig,
+                            const int64_t *off, const int32_t *col, int32_t *lr);
+
+// ---------------------------------------------------------------- solvers
+int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corr, double *errs,
+                        mpgpu_solveinfo *info, bool decomposition);
+int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
+                     double *corr, mpgpu_solveinfo *info);
+int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b);
+
+// error helpers
+int32_t set_err(mpgpu_ctx *c, int32_t code, const std::string &msg);
+int32_t cuda_err(mpgpu_ctx *c, cudaError_t e, const char *where);
+#define MPG_CUDA(c, call)                                      \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_err((c), e_, #call); \
+    } while (0)

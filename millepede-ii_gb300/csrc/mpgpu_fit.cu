@@ -1,0 +1,865 @@
+// mpgpu_fit.cu -- per-record local fit and Schur-complement update.
+//
+// One warp per record (records of one chunk distributed grid-stride).  The
+// record words, its measurement table and slot lists are staged in shared
+// memory; all decision-relevant arithmetic (global-parameter subtraction,
+// normal equations, Gauss-Jordan inversion, residuals, chi2 sums, down-
+// weighting, cuts) keeps the operation order of pede's loopbf
+// (pede.f90:3387-4442) and this file is compiled with -fmad=false, so the
+// accept/reject decision of every record is bit-identical to the reference
+// arithmetic.  The update  -Gt W G + B Gamma^-1 Bt  is then formed with
+// fused multiply-adds and written to the chunk staging buffer (packed over
+// the record's sorted variable parameters) for the deterministic owner-
+// computes accumulation (mpgpu_accum.cu).
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "mpgpu_ctx.h"
+
+namespace {
+
+constexpr double kChuber = 1.345;   // Huber constant (pede.f90:3515)
+constexpr double kCauchy = 2.3849;  // Cauchy constant (pede.f90:3516)
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// chindl (mpnum.f90:2078-2115), single precision
+__device__ float d_chindl(int n, int nd) {
+    const float sn[3] = {0.47523f, 1.690140f, 2.782170f};
+    const float t3[30] = {9.0000f, 5.9146f, 4.7184f, 4.0628f, 3.6410f, 3.3436f, 3.1209f,
+                          2.9468f, 2.8063f, 2.6902f, 2.5922f, 2.5082f, 2.4352f, 2.3711f,
+                          2.3143f, 2.2635f, 2.2178f, 2.1764f, 2.1386f, 2.1040f, 2.0722f,
+                          2.0428f, 2.0155f, 1.9901f, 1.9665f, 1.9443f, 1.9235f, 1.9040f,
+                          1.8855f, 1.8681f};
+    const float t2[30] = {4.0000f, 3.0900f, 2.6750f, 2.4290f, 2.2628f, 2.1415f, 2.0481f,
+                          1.9736f, 1.9124f, 1.8610f, 1.8171f, 1.7791f, 1.7457f, 1.7161f,
+                          1.6897f, 1.6658f, 1.6442f, 1.6246f, 1.6065f, 1.5899f, 1.5745f,
+                          1.5603f, 1.5470f, 1.5346f, 1.5230f, 1.5120f, 1.5017f, 1.4920f,
+                          1.4829f, 1.4742f};
+    const float t1[30] = {1.0000f, 1.1479f, 1.1753f, 1.1798f, 1.1775f, 1.1730f, 1.1680f,
+                          1.1630f, 1.1581f, 1.1536f, 1.1493f, 1.1454f, 1.1417f, 1.1383f,
+                          1.1351f, 1.1321f, 1.1293f, 1.1266f, 1.1242f, 1.1218f, 1.1196f,
+                          1.1175f, 1.1155f, 1.1136f, 1.1119f, 1.1101f, 1.1085f, 1.1070f,
+                          1.1055f, 1.1040f};
+    if (nd < 1) return 0.0f;
+    int m = n < 3 ? n : 3;
+    if (m < 1) m = 1;
+    if (nd <= 30) return m == 3 ? t3[nd - 1] : (m == 2 ? t2[nd - 1] : t1[nd - 1]);
+    float x = sn[m - 1] + sqrtf((float)(nd + nd - 1));
+    return (x * x) / (float)(nd + nd);
+}
+
+// ------------------------------------------------------------------------
+// Gauss-Jordan inversion with diagonal pivoting (sqminv, mpnum.f90:97-213),
+// warp-parallel over the packed elements.  v, b, diag 0-based; used[] flags.
+// The pivot is the first remaining index with the largest |v_jj| among
+// those above 16*eps*|original diagonal|, which is what the sequential
+// linked-list scan of the reference selects.
+__device__ void warp_sqminv(double *v, double *b, int n, int *nrank_out, double *diag,
+                            double *ocol, double *scol, int *used) {
+    const int ln = lane_id();
+    const double eps = 16.0 * 2.220446049250313e-16;
+    const int np = (n * n + n) / 2;
+    for (int i = ln; i < n; i += 32) {
+        diag[i] = fabs(v[(i + 1) * (i + 2) / 2 - 1]);
+        used[i] = 0;
+    }
+    __syncwarp();
+    int nrank = 0;
+    bool deficient = false;
+    for (int it = 0; it < n; ++it) {
+        // pivot search: per lane best candidate, then warp argmax (ties -> low index)
+        double best = -1.0;
+        int bk = -1;
+        for (int j = ln; j < n; j += 32) {
+            if (used[j]) continue;
+            double a = fabs(v[(j + 1) * (j + 2) / 2 - 1]);
+            if (a > eps * diag[j] && a > best) { best = a; bk = j; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            double ob = __shfl_xor_sync(0xffffffffu, best, o);
+            int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (ob > best || (ob == best && ok >= 0 && (bk < 0 || ok < bk))) { best = ob; bk = ok; }
+        }
+        if (bk < 0) { deficient = true; break; }
+        const int k = bk;              // 0-based pivot
+        const int kk = (k + 1) * (k + 2) / 2 - 1;
+        const double vkk = 1.0 / v[kk];
+        // stage the pivot column (original) and its scaled copy
+        for (int j = ln; j < n; j += 32) {
+            if (j == k) continue;
+            int jk = j > k ? (j * (j + 1)) / 2 + k : (k * (k + 1)) / 2 + j;
+            double o = v[jk];
+            ocol[j] = o;
+            scol[j] = vkk * o;
+        }
+        __syncwarp();
+        if (ln == 0) {
+            used[k] = 1;
+        }
+        const double bk_new = b[k] * vkk;
+        // elimination of every element not in row/column k
+        {
+            int r = 0, c = ln;
+            while (c > r) { c -= r + 1; r++; }
+            for (int idx = ln; idx < np; idx += 32) {
+                if (r != k && c != k) v[idx] = v[idx] - scol[c] * ocol[r];
+                c += 32;
+                while (c > r) { c -= r + 1; r++; }
+            }
+        }
+        for (int j = ln; j < n; j += 32) {
+            if (j == k) continue;
+            b[j] = b[j] - bk_new * ocol[j];
+            int jk = j > k ? (j * (j + 1)) / 2 + k : (k * (k + 1)) / 2 + j;
+            v[jk] = scol[j];
+        }
+        __syncwarp();
+        if (ln == 0) {
+            b[k] = bk_new;
+            v[kk] = -vkk;
+        }
+        nrank++;
+        __syncwarp();
+    }
+    if (deficient) {
+        // clear the rows/columns that found no pivot
+        int r = 0, c = ln;
+        while (c > r) { c -= r + 1; r++; }
+        for (int idx = ln; idx < np; idx += 32) {
+            if (!used[r] && !used[c]) v[idx] = 0.0;
+            c += 32;
+            while (c > r) { c -= r + 1; r++; }
+        }
+        for (int j = ln; j < n; j += 32)
+            if (!used[j]) b[j] = 0.0;
+        __syncwarp();
+    }
+    for (int idx = ln; idx < np; idx += 32) v[idx] = -v[idx];
+    __syncwarp();
+    *nrank_out = nrank;
+}
+
+// ------------------------------------------------------------------------
+// Sequential bordered-band solvers (one lane), Dbandmatrix.f90:459-638 and
+// mpnum.f90:3118-3600.  All arrays 1-based.
+#define WB(r, c) w[((c) - 1) * mp1 + (r)]
+__device__ void s_dbcdec(double *w, int mp1, int n, double *aux) {
+    for (int i = 1; i <= n; i++) aux[i] = 16.0 * WB(1, i);
+    for (int i = 1; i <= n; i++) {
+        if (WB(1, i) + aux[i] != aux[i]) WB(1, i) = 1.0 / WB(1, i);
+        else WB(1, i) = 0.0;
+        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+        for (int j = 1; j <= mj; j++) {
+            double rxw = WB(j + 1, i) * WB(1, i);
+            for (int k = 1; k <= mj + 1 - j; k++) WB(k, i + j) = WB(k, i + j) - WB(k + j, i) * rxw;
+            WB(j + 1, i) = rxw;
+        }
+    }
+}
+__device__ void s_dbcslv(const double *w, int mp1, int n, const double *b, double *x) {
+    for (int i = 1; i <= n; i++) x[i] = b[i];
+    for (int i = 1; i <= n; i++) {
+        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+        for (int j = 1; j <= mj; j++) x[j + i] = x[j + i] - WB(j + 1, i) * x[i];
+    }
+    for (int i = n; i >= 1; i--) {
+        double rxw = x[i] * WB(1, i);
+        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+        for (int j = 1; j <= mj; j++) rxw = rxw - WB(j + 1, i) * x[j + i];
+        x[i] = rxw;
+    }
+}
+__device__ void s_dbcinv(const double *w, int mp1, int n, double *vs, bool bandOnly) {
+    for (int i = n; i >= 1; i--) {
+        double rxw = WB(1, i);
+        int jlo = bandOnly ? ((1 > i - mp1 + 1) ? 1 : i - mp1 + 1) : 1;
+        for (int j = i; j >= jlo; j--) {
+            int khi = (n < j + mp1 - 1) ? n : j + mp1 - 1;
+            for (int k = j + 1; k <= khi; k++) {
+                int a = i > k ? i : k, c = i > k ? k : i;
+                rxw = rxw - vs[(a * (a - 1)) / 2 + c] * WB(1 + k - j, j);
+            }
+            vs[(i * i - i) / 2 + j] = rxw;
+            rxw = 0.0;
+        }
+    }
+}
+#undef WB
+
+// sequential sqminv for the border part (1-based)
+__device__ void s_sqminv(double *v, double *b, int n, int *nrank, double *diag, int *next) {
+    const double eps = 16.0 * 2.220446049250313e-16;
+    int next0 = 1, l = 1;
+    for (int i = 1; i <= n; i++) { next[i] = i + 1; diag[i] = fabs(v[(i * i + i) / 2]); }
+    next[n] = -1;
+    *nrank = 0;
+    for (int i = 1; i <= n; i++) {
+        int k = 0, j = next0, last = 0;
+        double vkk = 0.0;
+        while (j > 0) {
+            int jj = (j * j + j) / 2;
+            double lim = fabs(vkk) > eps * diag[j] ? fabs(vkk) : eps * diag[j];
+            if (fabs(v[jj]) > lim) { vkk = v[jj]; k = j; l = last; }
+            last = j;
+            j = next[last];
+        }
+        if (k != 0) {
+            int kk = (k * k + k) / 2;
+            if (l == 0) next0 = next[k]; else next[l] = next[k];
+            next[k] = 0;
+            (*nrank)++;
+            vkk = 1.0 / vkk;
+            v[kk] = -vkk;
+            b[k] = b[k] * vkk;
+            int jk = kk - k, jl = 0;
+            for (j = 1; j <= n; j++) {
+                if (j == k) { jk = kk; jl = jl + j; continue; }
+                if (j < k) jk = jk + 1; else jk = jk + j - 1;
+                double vjk = v[jk];
+                v[jk] = vkk * vjk;
+                b[j] = b[j] - b[k] * vjk;
+                int lk = kk - k;
+                for (int ll = 1; ll <= j; ll++) {
+                    jl = jl + 1;
+                    if (ll == k) { lk = kk; continue; }
+                    if (ll < k) lk = lk + 1; else lk = lk + ll - 1;
+                    v[jl] = v[jl] - v[lk] * vjk;
+                }
+            }
+        } else {
+            for (k = 1; k <= n; k++)
+                if (next[k] != 0) {
+                    b[k] = 0.0;
+                    for (j = 1; j <= k; j++) if (next[j] != 0) v[(k * k - k) / 2 + j] = 0.0;
+                }
+            break;
+        }
+    }
+    for (int ij = 1; ij <= (n * n + n) / 2; ij++) v[ij] = -v[ij];
+}
+
+struct BandWork {
+    double *vbnd, *vbdr, *aux, *vbk, *vzru, *scdiag;
+    int *scflag;
+};
+
+// sqmibb (side 1, upper/left border) and sqmibb2 (side 2) in one routine;
+// v, b 1-based.
+__device__ void s_sqmibb(int side, double *v, double *b, int n, int nbdr, int nbnd, int inv,
+                         int *nrank, double *evdmin, double *evdmax, BandWork &wk) {
+    double *vbnd = wk.vbnd, *vbdr = wk.vbdr, *aux = wk.aux, *vbk = wk.vbk, *vzru = wk.vzru;
+    int mp1 = nbnd + 1, nmb = n - nbdr, ip, is, ioff, joff, ij, nrankb;
+    *nrank = 0;
+    if (side == 1) {
+        int nb1 = nbdr + 1;
+        for (int i = nb1; i <= n; i++) {
+            ip = (i * (i + 1)) / 2; is = 0;
+            int jhi = (n < i + nbnd) ? n : i + nbnd;
+            for (int j = i; j <= jhi; j++) { ip += is; is = j; vbnd[j - i + 1 + (i - nb1) * mp1] = v[ip]; }
+        }
+        ioff = 0;
+        for (int i = 1; i <= nbdr; i++) {
+            ip = (i * (i + 1)) / 2; is = 0;
+            for (int j = i; j <= n; j++) { ip += is; is = j; vbdr[ioff + j] = v[ip]; }
+            ioff += n;
+        }
+    } else {
+        int nb1 = nmb + 1;
+        for (int i = 1; i <= nmb; i++) {
+            ip = (i * (i + 1)) / 2; is = 0;
+            int jhi = (nmb < i + nbnd) ? nmb : i + nbnd;
+            for (int j = i; j <= jhi; j++) { ip += is; is = j; vbnd[j - i + 1 + (i - 1) * mp1] = v[ip]; }
+        }
+        ioff = 0;
+        for (int i = nb1; i <= n; i++) {
+            ip = (i * (i - 1)) / 2;
+            for (int j = 1; j <= i; j++) vbdr[ioff + j] = v[ip + j];
+            ioff += n;
+        }
+    }
+    s_dbcdec(vbnd, mp1, nmb, aux);
+    ip = 1;
+    *evdmin = 0.0; *evdmax = 0.0;
+    for (int i = 1; i <= nmb; i++) {
+        if (vbnd[ip] <= 0.0) {
+            for (int q = 1; q <= n; q++) b[q] = 0.0;
+            for (int q = 1; q <= (n * n + n) / 2; q++) v[q] = 0.0;
+            *nrank = 0;
+            return;
+        }
+        (*nrank)++;
+        if (*nrank == 1) { *evdmin = vbnd[ip]; *evdmax = vbnd[ip]; }
+        else { if (vbnd[ip] < *evdmin) *evdmin = vbnd[ip]; if (vbnd[ip] > *evdmax) *evdmax = vbnd[ip]; }
+        ip += mp1;
+    }
+    if (nbdr == 0) {
+        s_dbcslv(vbnd, mp1, nmb, b, b);
+        if (inv > 0) s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
+        return;
+    }
+    if (side == 1) {
+        int nb1 = nbdr + 1;
+        ioff = nb1;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            s_dbcslv(vbnd, mp1, nmb, vbdr + ioff - 1, aux + ioff - 1);
+            vzru[ib] = b[ib];
+            for (int i = 0; i <= nmb - 1; i++) vzru[ib] = vzru[ib] - b[nb1 + i] * aux[ioff + i];
+            ioff += n;
+        }
+        s_dbcslv(vbnd, mp1, nmb, b + nb1 - 1, b + nb1 - 1);
+        ip = 0; ioff = nb1;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            joff = nb1;
+            for (int jb = 1; jb <= ib; jb++) {
+                ip++;
+                vbk[ip] = v[ip];
+                for (int i = 0; i <= nmb - 1; i++) vbk[ip] = vbk[ip] - vbdr[ioff + i] * aux[joff + i];
+                joff += n;
+            }
+            ioff += n;
+        }
+        s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
+        if (nrankb == nbdr) *nrank += nbdr;
+        else {
+            for (int ib = 1; ib <= nbdr; ib++) vzru[ib] = 0.0;
+            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) vbk[q] = 0.0;
+        }
+        ioff = nb1;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            b[ib] = vzru[ib];
+            for (int i = 0; i <= nmb - 1; i++) b[nb1 + i] = b[nb1 + i] - b[ib] * aux[ioff + i];
+            ioff += n;
+        }
+        if (inv > 0) {
+            s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
+            int ip1 = (nmb * nmb + nmb) / 2, ip2 = (n * n + n) / 2;
+            for (int i = nmb - 1; i >= 0; i--) {
+                int j0 = 0;
+                if (inv == 1) j0 = (0 > i - nbnd) ? 0 : i - nbnd;
+                for (int j = i; j >= j0; j--) {
+                    v[ip2] = v[ip1];
+                    ioff = nb1;
+                    for (int ib = 1; ib <= nbdr; ib++) {
+                        joff = nb1;
+                        for (int jb = 1; jb <= nbdr; jb++) {
+                            ij = ib > jb ? ib : jb;
+                            ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
+                            v[ip2] = v[ip2] + vbk[ij] * aux[ioff + i] * aux[joff + j];
+                            joff += n;
+                        }
+                        ioff += n;
+                    }
+                    ip1--; ip2--;
+                }
+                ip1 -= j0; ip2 -= j0;
+                for (int ib = nbdr; ib >= 1; ib--) {
+                    v[ip2] = 0.0;
+                    joff = nb1;
+                    for (int jb = 1; jb <= nbdr; jb++) {
+                        ij = ib > jb ? ib : jb;
+                        ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
+                        v[ip2] = v[ip2] - vbk[ij] * aux[i + joff];
+                        joff += n;
+                    }
+                    ip2--;
+                }
+            }
+            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) { v[ip2] = vbk[q]; ip2--; }
+        }
+    } else {
+        ioff = 0;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            s_dbcslv(vbnd, mp1, nmb, vbdr + ioff, aux + ioff);
+            vzru[ib] = b[nmb + ib];
+            for (int i = 1; i <= nmb; i++) vzru[ib] = vzru[ib] - b[i] * aux[ioff + i];
+            ioff += n;
+        }
+        s_dbcslv(vbnd, mp1, nmb, b, b);
+        ip = 0; ioff = 0;
+        int koff = nmb;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            joff = 0;
+            for (int jb = 1; jb <= ib; jb++) {
+                ip++;
+                vbk[ip] = vbdr[koff + jb];
+                for (int i = 1; i <= nmb; i++) vbk[ip] = vbk[ip] - vbdr[ioff + i] * aux[joff + i];
+                joff += n;
+            }
+            ioff += n; koff += n;
+        }
+        s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
+        if (nrankb == nbdr) *nrank += nbdr;
+        else {
+            for (int ib = 1; ib <= nbdr; ib++) vzru[ib] = 0.0;
+            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) vbk[q] = 0.0;
+        }
+        ioff = 0;
+        for (int ib = 1; ib <= nbdr; ib++) {
+            for (int i = 1; i <= nmb; i++) b[i] = b[i] - vzru[ib] * aux[ioff + i];
+            ioff += n;
+            b[nmb + ib] = vzru[ib];
+        }
+        if (inv > 0) {
+            s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
+            int ip1 = (nmb * nmb + nmb) / 2;
+            for (int i = nmb - 1; i >= 0; i--) {
+                int j0 = 0;
+                if (inv == 1) j0 = (0 > i - nbnd) ? 0 : i - nbnd;
+                for (int j = i; j >= j0; j--) {
+                    ioff = 1;
+                    for (int ib = 1; ib <= nbdr; ib++) {
+                        joff = 1;
+                        for (int jb = 1; jb <= nbdr; jb++) {
+                            ij = ib > jb ? ib : jb;
+                            ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
+                            v[ip1] = v[ip1] + vbk[ij] * aux[ioff + i] * aux[joff + j];
+                            joff += n;
+                        }
+                        ioff += n;
+                    }
+                    ip1--;
+                }
+                ip1 -= j0;
+            }
+            ip1 = (nmb * nmb + nmb) / 2;
+            ip = 0;
+            for (int ib = 1; ib <= nbdr; ib++) {
+                for (int i = 1; i <= nmb; i++) {
+                    ip1++;
+                    v[ip1] = 0.0;
+                    joff = 0;
+                    for (int jb = 1; jb <= nbdr; jb++) {
+                        ij = ib > jb ? ib : jb;
+                        ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
+                        v[ip1] = v[ip1] - vbk[ij] * aux[i + joff];
+                        joff += n;
+                    }
+                }
+                for (int jb = 1; jb <= ib; jb++) { ip1++; ip++; v[ip1] = vbk[ip]; }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// shared-memory carve-up of one warp
+struct WarpMem {
+    double *gl, *rm1, *lcor, *lwgt, *res, *t1, *t2, *clmat, *blvec, *diag, *ocol, *scol;
+    double *B, *W;
+    double *bnd;   // band scratch (may be null)
+    int32_t *in, *mq, *slots, *swS, *sw, *used;
+};
+
+__host__ __device__ inline int64_t align8(int64_t x) { return (x + 7) & ~int64_t(7); }
+
+__host__ __device__ inline int64_t band_doubles(int nalc, int bandmax, int bdrmax) {
+    if (bandmax < 0) return 0;
+    int64_t n = nalc, b = bandmax, d = bdrmax;
+    // vbnd n*(b+1), vbdr n*d, aux n*d+n, vbk d*d, vzru n, scdiag n (+1 each)
+    return n * (b + 1) + 2 * n * d + 3 * n + d * d + 16;
+}
+
+__host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax, int nalgmax,
+                                              int bandmax, int bdrmax) {
+    int64_t d = 0;
+    d += wmax;                          // gl
+    d += 6 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2
+    d += (int64_t)nalcmax * (nalcmax + 1) / 2 + 4 * (int64_t)nalcmax;  // clmat blvec diag ocol scol
+    d += 2 * (int64_t)nalcmax * nalgmax;  // B W
+    d += band_doubles(nalcmax, bandmax, bdrmax);
+    int64_t i = 0;
+    i += wmax;            // in
+    i += 3 * (int64_t)neqmax;
+    i += nalgmax;         // slots
+    i += nalgmax + 1;     // swS
+    i += wmax;            // sw
+    i += nalcmax + 2;     // used / scflag
+    return align8(d * 8 + i * 4 + 64);
+}
+
+__device__ WarpMem carve(char *base, const FitParams &p) {
+    WarpMem m;
+    double *d = (double *)base;
+    m.gl = d; d += p.wmax;
+    m.rm1 = d; d += p.neqmax;
+    m.lcor = d; d += p.neqmax;
+    m.lwgt = d; d += p.neqmax;
+    m.res = d; d += p.neqmax;
+    m.t1 = d; d += p.neqmax;
+    m.t2 = d; d += p.neqmax;
+    m.clmat = d; d += (int64_t)p.nalcmax * (p.nalcmax + 1) / 2;
+    m.blvec = d; d += p.nalcmax;
+    m.diag = d; d += p.nalcmax;
+    m.ocol = d; d += p.nalcmax;
+    m.scol = d; d += p.nalcmax;
+    m.B = d; d += (int64_t)p.nalcmax * p.nalgmax;
+    m.W = d; d += (int64_t)p.nalcmax * p.nalgmax;
+    m.bnd = p.bandmax >= 0 ? d : nullptr;
+    d += band_doubles(p.nalcmax, p.bandmax, p.bdrmax);
+    int32_t *q = (int32_t *)d;
+    m.in = q; q += p.wmax;
+    m.mq = q; q += 3 * p.neqmax;
+    m.slots = q; q += p.nalgmax;
+    m.swS = q; q += p.nalgmax + 1;
+    m.sw = q; q += p.wmax;
+    m.used = q;
+    return m;
+}
+
+__device__ __forceinline__ double wsum_serial(const double *a, int n) {
+    // sequential sum in index order on lane 0, broadcast to the warp
+    double s = 0.0;
+    if (lane_id() == 0)
+        for (int e = 0; e < n; ++e) s = s + a[e];
+    return __shfl_sync(0xffffffffu, s, 0);
+}
+
+__global__ void __launch_bounds__(32 * MPG_WARPS_FIT)
+k_fit(FitParams p, int perWarp) {
+    extern __shared__ __align__(16) char smem[];
+    const int ln = lane_id();
+    const int wib = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+    WarpMem m = carve(smem + (int64_t)wib * perWarp, p);
+    const int64_t nwarps = (int64_t)gridDim.x * wpc;
+
+    for (int64_t r = p.r0 + (int64_t)blockIdx.x * wpc + wib; r < p.r1; r += nwarps) {
+        const RecInfo ri = p.rec[r];
+        const int nw = ri.nw, neq = ri.neq, nalc = ri.nalc, nalg = ri.nalg;
+        for (int i = ln; i < nw; i += 32) {
+            m.gl[i] = p.glder[ri.w0 + i];
+            m.in[i] = p.inder[ri.w0 + i];
+        }
+        for (int i = ln; i < 3 * neq; i += 32) m.mq[i] = p.meas[3 * ri.measOff + i];
+        for (int i = ln; i < nalg; i += 32) m.slots[i] = p.slots[ri.slotOff + i];
+        for (int i = ln; i <= nalg; i += 32) m.swS[i] = p.swStart[ri.slotOff + i];
+        __syncwarp();
+        const int nswr = m.swS[nalg];
+        for (int i = ln; i < nswr; i += 32) m.sw[i] = p.sw[ri.swOff + i];
+
+        int st = 0;          // 0 accepted, 1..6 rejection class, -1 no locals
+        double chi2add = 0.0;
+        int ndfadd = 0;
+        float chndf = 0.0f;
+        if (nalc <= 0) {
+            st = -1;
+        } else {
+            const double dw1 = p.fileWeight ? p.fileWeight[ri.file - 1] : 1.0;
+            const double dw2 = sqrt(dw1);
+            // ---- first loop: subtract the current global parameters
+            for (int e = ln; e < neq; e += 32) {
+                const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1], lg = m.mq[3 * e + 2];
+                double rm = m.gl[sl];
+                for (int j = 1; j <= lg - sg; ++j) {
+                    const int li = m.in[sg + j];
+                    rm = rm - m.gl[sg + j] * p.gpar[li - 1];
+                }
+                m.rm1[e] = rm;
+                m.lcor[e] = 0.0;
+            }
+            __syncwarp();
+            const int nter = (p.nloopn != 1 && p.lhuber != 0) ? p.lhuber : 1;
+            const bool band = ri.mbnd >= 0 && p.lfitbb > 0 && nalc > 5;
+            const bool seqNormal = ((ri.mside >> 8) & 1) != 0;
+            const int npk = (nalc * nalc + nalc) / 2;
+            int nrank = 0, ndf = 0;
+            double summ = 0.0;
+            float cndl10 = 0.0f, resing = 0.0f;
+            for (int iter = 1; iter <= nter; ++iter) {
+                const bool down = (p.nloopn != 1 && iter != 1 && p.lhuber != 0);
+                for (int e = ln; e < neq; e += 32) {
+                    const int sg = m.mq[3 * e + 1];
+                    const double rerr = m.gl[sg];
+                    double wght = 1.0 / (rerr * rerr);
+                    const double resid = m.rm1[e] - m.lcor[e];
+                    if (down) {
+                        if (iter <= 3) {
+                            if (fabs(resid) > kChuber * rerr) wght = wght * kChuber * rerr / fabs(resid);
+                        } else {
+                            const double t = resid / rerr / kCauchy;
+                            wght = wght / (1.0 + t * t);
+                        }
+                    }
+                    m.lwgt[e] = wght;
+                }
+                for (int i = ln; i < npk; i += 32) m.clmat[i] = 0.0;
+                for (int i = ln; i < nalc; i += 32) m.blvec[i] = 0.0;
+                __syncwarp();
+                // ---- second loop: normal equations, equation by equation
+                for (int e = 0; e < neq; ++e) {
+                    const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
+                    const int nl = sg - sl - 1;
+                    const double wght = m.lwgt[e], rm = m.rm1[e];
+                    if (!seqNormal) {
+                        const int npair = (nl * nl + nl) / 2;
+                        int j = 1, k = 1 + ln;
+                        while (k > j) { k -= j; j++; }
+                        for (int q = ln; q < npair; q += 32) {
+                            const int ij = m.in[sl + j], ik = m.in[sl + k];
+                            const int jk = (ij * ij - ij) / 2 + ik;
+                            m.clmat[jk - 1] = m.clmat[jk - 1] + wght * m.gl[sl + j] * m.gl[sl + k];
+                            k += 32;
+                            while (k > j) { k -= j; j++; }
+                        }
+                        for (int jj = 1 + ln; jj <= nl; jj += 32) {
+                            const int ij = m.in[sl + jj];
+                            m.blvec[ij - 1] = m.blvec[ij - 1] + wght * rm * m.gl[sl + jj];
+                        }
+                    } else if (ln == 0) {
+                        // local indices not strictly increasing: reference order, one lane
+                        for (int jj = 1; jj <= nl; ++jj) {
+                            const int ij = m.in[sl + jj];
+                            m.blvec[ij - 1] = m.blvec[ij - 1] + wght * rm * m.gl[sl + jj];
+                            for (int kk = 1; kk <= jj; ++kk) {
+                                const int ik = m.in[sl + kk];
+                                const int jk = (ij * ij - ij) / 2 + ik;
+                                m.clmat[jk - 1] = m.clmat[jk - 1] + wght * m.gl[sl + jj] * m.gl[sl + kk];
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+                // ---- local solve
+                if (band) {
+                    double evdmin = 0.0, evdmax = 0.0;
+                    int nr = 0;
+                    if (ln == 0) {
+                        int inv = 0;
+                        if (iter == 1) inv = 1;
+                        if (p.icalcm == 1) inv = 2;
+                        const int nb = ri.mbdr, nbd = ri.mbnd, n = nalc;
+                        BandWork wk;
+                        double *q = m.bnd;
+                        wk.vbnd = q - 1; q += (int64_t)n * (nbd + 1) + 1;
+                        wk.vbdr = q - 1; q += (int64_t)n * nb + 1;
+                        wk.aux = q - 1; q += (int64_t)n * nb + n + 1;
+                        wk.vbk = q - 1; q += (int64_t)nb * nb + 1;
+                        wk.vzru = q - 1; q += n + 1;
+                        wk.scdiag = q - 1; q += n + 1;
+                        wk.scflag = m.used - 1;
+                        s_sqmibb(ri.mside & 0xff, m.clmat - 1, m.blvec - 1, n, nb, nbd, inv, &nr,
+                                 &evdmin, &evdmax, wk);
+                        if (evdmin > 0.0) cndl10 = log10f((float)(evdmax / evdmin));
+                        else cndl10 = 0.0f;
+                    }
+                    __syncwarp();
+                    nrank = __shfl_sync(0xffffffffu, nr, 0);
+                    cndl10 = __shfl_sync(0xffffffffu, cndl10, 0);
+                } else {
+                    cndl10 = 0.0f;
+                    warp_sqminv(m.clmat, m.blvec, nalc, &nrank, m.diag, m.ocol, m.scol, m.used);
+                }
+                int nanl = 0;
+                for (int k = ln; k < nalc; k += 32) {
+                    const double bv = m.blvec[k];
+                    if (!(bv <= 0.0) && !(bv > 0.0)) nanl = 1;
+                }
+                const bool nan = __any_sync(0xffffffffu, nanl) != 0;
+                // ---- third loop: residuals and chi2
+                for (int e = ln; e < neq; e += 32) {
+                    const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
+                    const double rerr = m.gl[sg];
+                    double wght = 1.0 / (rerr * rerr);
+                    double rmloc = 0.0;
+                    for (int j = 1; j <= sg - sl - 1; ++j) {
+                        const int ij = m.in[sl + j];
+                        rmloc = rmloc + m.gl[sl + j] * m.blvec[ij - 1];
+                    }
+                    m.lcor[e] = rmloc;
+                    const double rm = m.rm1[e] - rmloc;
+                    double dchi2 = wght * rm * rm;
+                    if (down) {
+                        if (iter <= 3) {
+                            if (fabs(rm) > kChuber * rerr) {
+                                wght = wght * kChuber * rerr / fabs(rm);
+                                dchi2 = 2.0 * kChuber * (fabs(rm) / rerr - 0.5 * kChuber);
+                            }
+                        } else {
+                            const double t = rm / rerr / kCauchy;
+                            wght = wght / (1.0 + t * t);
+                            dchi2 = log(1.0 + t * t) * (kCauchy * kCauchy);
+                        }
+                    }
+                    const double dn = 1.0 / sqrt(wght);
+                    m.t1[e] = dchi2;
+                    m.t2[e] = rerr / dn;
+                }
+                __syncwarp();
+                summ = wsum_serial(m.t1, neq);
+                const double suwt = wsum_serial(m.t2, neq);
+                ndf = neq - nrank;
+                resing = ((float)neq - (float)suwt) / (float)neq;
+                if (nan) { st = 1; break; }
+                if (nrank != nalc) { st = 2; break; }
+                if (cndl10 > p.cndlmx) { st = 3; break; }
+                if (ndf <= 0) { st = 4; break; }
+                chndf = (float)(summ / (double)ndf);
+            }
+            // ---- rejection cuts (pede.f90:4106-4144)
+            if (st == 0) {
+                const float chichi = d_chindl(3, ndf) * (float)ndf;
+                if (p.chicut >= 0.0f) {
+                    if (summ > (double)(p.chhuge * chichi)) {
+                        st = 5;
+                    } else if (p.chicut > 0.0f) {
+                        const float chlimt = p.chicut * chichi;
+                        if (summ > (double)chlimt) {
+                            st = 6;
+                            chi2add = (double)chlimt;
+                            ndfadd = ndf;
+                        }
+                    }
+                }
+                if (st == 0 && p.lhuber > 1 && p.dwcut != 0.0f && resing > p.dwcut) {
+                    st = 6;
+                    chi2add = summ;
+                    ndfadd = ndf;
+                }
+            }
+            if (st == 0) {
+                // ---- fourth loop: residuals, weights and chi2 of the accepted fit
+                for (int e = ln; e < neq; e += 32) {
+                    const int sg = m.mq[3 * e + 1];
+                    const double rm = m.rm1[e] - m.lcor[e];
+                    const double rerr = m.gl[sg];
+                    double wght = 1.0 / (rerr * rerr);
+                    double dchi2 = wght * rm * rm;
+                    if (p.nloopn != 1 && p.lhuber != 0) {
+                        const double resid = fabs(rm);
+                        if (nter <= 3) {
+                            if (resid > kChuber * rerr)
+                                dchi2 = 2.0 * kChuber * (resid / rerr - 0.5 * kChuber);
+                        } else {
+                            const double t = resid / rerr / kCauchy;
+                            dchi2 = log(1.0 + t * t) * (kCauchy * kCauchy);
+                        }
+                        wght = m.lwgt[e];
+                    }
+                    m.res[e] = rm;
+                    m.lwgt[e] = wght;
+                    m.t1[e] = dchi2;
+                }
+                __syncwarp();
+                chi2add = wsum_serial(m.t1, neq);
+                ndfadd = ndf;
+                // ---- global vector and local-global matrix B, one lane per slot
+                for (int s = ln; s < nalg; s += 32) {
+                    double v = 0.0;
+                    if (p.icalcm == 1)
+                        for (int k = 0; k < nalc; ++k) m.B[k * nalg + s] = 0.0;
+                    for (int q = m.swS[s]; q < m.swS[s + 1]; ++q) {
+                        const int ent = m.sw[q];
+                        const int e = ent >> 16, wp = ent & 0xffff;
+                        const double g = m.gl[wp];
+                        const double wv = m.lwgt[e];
+                        if (g != 0.0) v = v + dw1 * wv * m.res[e] * g;
+                        if (p.icalcm == 1) {
+                            const double cb = dw2 * wv * g;
+                            const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
+                            for (int jj = 1; jj <= sg - sl - 1; ++jj) {
+                                const int k = m.in[sl + jj] - 1;
+                                m.B[k * nalg + s] = __fma_rn(cb, m.gl[sl + jj], m.B[k * nalg + s]);
+                            }
+                        }
+                    }
+                    p.vstage[ri.slotOff + s] = v;
+                }
+                __syncwarp();
+                if (p.icalcm == 1) {
+                    // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432)
+                    for (int s = ln; s < nalg; s += 32) {
+                        for (int k = 1; k <= nalc; ++k) {
+                            double cik = 0.0;
+                            const int lkl = (k * k - k) / 2;
+                            for (int l = 1; l <= k; ++l)
+                                cik = __fma_rn(m.B[(l - 1) * nalg + s], m.clmat[lkl + l - 1], cik);
+                            for (int l = k + 1; l <= nalc; ++l)
+                                cik = __fma_rn(m.B[(l - 1) * nalg + s], m.clmat[(l * l - l) / 2 + k - 1], cik);
+                            m.W[s * nalc + k - 1] = cik;
+                        }
+                    }
+                    __syncwarp();
+                    // U(a,b) = -sum_eq dw1 w g_a g_b + sum_k W(a,k) B(b,k), a >= b
+                    double *U = p.stage + ri.updOff;
+                    const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
+                    int a = 0, b = ln;
+                    while (b > a) { b -= a + 1; a++; }
+                    for (int64_t idx = ln; idx < ngg; idx += 32) {
+                        double u = 0.0;
+                        // Gt W G: equations shared by slots a and b (merge of the
+                        // equation-ordered word lists), pair taken in the
+                        // reference's order (later word first)
+                        int qa = m.swS[a], qae = m.swS[a + 1];
+                        int qb = m.swS[b], qbe = m.swS[b + 1];
+                        while (qa < qae && qb < qbe) {
+                            const int ea = m.sw[qa] >> 16, eb = m.sw[qb] >> 16;
+                            if (ea < eb) { qa++; continue; }
+                            if (eb < ea) { qb++; continue; }
+                            // same equation: all word pairs of a and b in it
+                            int qa2 = qa, qb2 = qb;
+                            while (qa2 < qae && (m.sw[qa2] >> 16) == ea) qa2++;
+                            while (qb2 < qbe && (m.sw[qb2] >> 16) == ea) qb2++;
+                            const double cw = dw1 * m.lwgt[ea];
+                            for (int x = qa; x < qa2; ++x)
+                                for (int y = qb; y < qb2; ++y) {
+                                    const int wa = m.sw[x] & 0xffff, wb = m.sw[y] & 0xffff;
+                                    if (a == b && wb > wa) continue;  // pair once
+                                    const int wj = wa > wb ? wa : wb, wk = wa > wb ? wb : wa;
+                                    const double gj = m.gl[wj];
+                                    if (gj == 0.0) continue;
+                                    u = u - cw * gj * m.gl[wk];
+                                }
+                            qa = qa2;
+                            qb = qb2;
+                        }
+                        const double *wa = m.W + a * nalc;
+                        for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], m.B[k * nalg + b], u);
+                        U[idx] = u;
+                        b += 32;
+                        while (b > a) { b -= a + 1; a++; }
+                    }
+                }
+            }
+        }
+        if (ln == 0) {
+            p.status[r] = (int8_t)st;
+            p.chi2add[r] = chi2add;
+            p.ndfadd[r] = ndfadd;
+            p.chndf[r] = st == 0 ? chndf : 0.0f;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+int fit_smem_per_warp(const FitParams &p) {
+    return (int)warp_bytes(p.wmax, p.neqmax, p.nalcmax, p.nalgmax, p.bandmax, p.bdrmax);
+}
+
+// warps per CTA so that one CTA fits the 227 KB of shared memory
+int fit_warps_per_cta(const FitParams &p) {
+    const int per = fit_smem_per_warp(p);
+    int wpc = MPG_WARPS_FIT;
+    while (wpc > 1 && (int64_t)per * wpc > 220 * 1024) wpc--;
+    return (int64_t)per * wpc > 220 * 1024 ? 0 : wpc;
+}
+
+cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s) {
+    const int per = fit_smem_per_warp(p);
+    const int wpc = fit_warps_per_cta(p);
+    if (wpc < 1) return cudaErrorInvalidConfiguration;
+    const int bytes = per * wpc;
+    cudaError_t e = cudaFuncSetAttribute(k_fit, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e != cudaSuccess) return e;
+    int perSM = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_fit, 32 * wpc, bytes);
+    if (perSM < 1) perSM = 1;
+    int64_t nrec = p.r1 - p.r0;
+    int64_t grid = (int64_t)nsm * perSM;
+    int64_t need = (nrec + wpc - 1) / wpc;
+    if (grid > need) grid = need;
+    if (grid < 1) grid = 1;
+    k_fit<<<(unsigned)grid, 32 * wpc, bytes, s>>>(p, per);
+    return cudaGetLastError();
+}

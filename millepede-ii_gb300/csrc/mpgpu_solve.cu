@@ -1,0 +1,910 @@
+// mpgpu_solve.cu -- global solvers on the device: QL constraint
+// elimination products, packed Gauss-Jordan inversion (sqminl), root-free
+// Cholesky (chdec2/chslv2), the sparse and packed symmetric matrix-vector
+// product (avprd0) and preconditioned MINRES.  All reductions have a fixed
+// shape, so repeated solves give bit-identical results.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "mpgpu_ctx.h"
+
+namespace {
+
+constexpr int kDotBlocks = 304;   // 2 x 152 SMs, fixed for determinism
+constexpr int kThreads = 256;
+
+template <class T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_dot_partial(int64_t n, const double *a, const double *b, double *part) {
+    __shared__ double sh[kThreads];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void k_sum_final(const double *part, int n, double *out) {
+    __shared__ double sh[kThreads];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) *out = s;
+}
+
+void dot(const double *a, const double *b, int64_t n, double *part, double *out, cudaStream_t s) {
+    k_dot_partial<<<kDotBlocks, kThreads, 0, s>>>(n, a, b, part);
+    k_sum_final<<<1, kThreads, 0, s>>>(part, kDotBlocks, out);
+}
+
+// ---------------------------------------------------------------- QL products
+// qlmlq (mpqldec.f90:404-454) for one vector, one CTA walking the
+// reflections k = kfirst, kfirst+step, ..., klast in that order
+// (Q x: 1..ncon; Q^T x: ncon..1).
+__global__ void k_qlapply(double *x, const double *V, const double *Vk, const int32_t *r2, int32_t npar,
+                          int32_t ncon, int kfirst, int klast, int step) {
+    __shared__ double sh[1024];
+    if (step == 0) return;
+    for (int k = kfirst; step > 0 ? k <= klast : k >= klast; k += step) {
+        const int kn = npar + k - ncon;
+        const int ilast = r2[k - 1];
+        const double *v = V + (int64_t)(k - 1) * npar;
+        const double vk = Vk[k - 1];
+        double s = 0.0;
+        for (int i = threadIdx.x; i < ilast; i += blockDim.x) s += v[i] * x[i];
+        s = block_sum(s, sh);
+        const double sp = s + vk * x[kn - 1];
+        __syncthreads();
+        for (int i = threadIdx.x; i < ilast; i += blockDim.x) x[i] = x[i] - 2.0 * v[i] * sp;
+        if (threadIdx.x == 0) x[kn - 1] = x[kn - 1] - 2.0 * vk * sp;
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- packed products
+// y = A x for the packed symmetric matrix, one warp per row: lower part of
+// row i (contiguous) plus the column part below the diagonal.
+__global__ void k_packed_matvec(int32_t n, const double *A, const double *x, double *y) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w; i < n; i += nw) {
+        const int64_t ro = i * (i + 1) / 2;  // 0-based row i start
+        double s = 0.0;
+        for (int64_t j = ln; j <= i; j += 32) s += A[ro + j] * x[j];
+        for (int64_t r = i + 1 + ln; r < n; r += 32) s += A[r * (r + 1) / 2 + i] * x[r];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (ln == 0) y[i] = s;
+    }
+}
+
+// qlssq update of one reflection on the packed matrix (mpqldec.f90:
+// 644-686): rows 1..kn get 2(2 v_i vtAv - Av_i) v_c for c in [1, min(ilast,i)],
+// rows ilast and below in [1, ilast] get -2 Av_c v_i, the diagonal (kn,kn)
+// its combined term and rows > kn their -2 v_c Av_i parts.
+__global__ void k_qlssq_update(int32_t n, double *A, const double *v, double vk, const double *Av,
+                               const double *vtAvp, int32_t ilast, int32_t kn) {
+    const double vtAv = *vtAvp;
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i1 = 1 + w; i1 <= n; i1 += nw) {   // 1-based row
+        double *row = A + (i1 * i1 - i1) / 2 - 1;     // row[c] = A(i1, c), c 1-based
+        const double vi = (i1 <= ilast) ? v[i1 - 1] : (i1 == kn ? vk : 0.0);
+        if (i1 <= kn) {
+            const int64_t il = ilast < i1 ? ilast : i1;
+            const double f = 2.0 * vi * vtAv - Av[i1 - 1];
+            for (int64_t cc = 1 + ln; cc <= il; cc += 32) row[cc] = row[cc] + 2.0 * (f * v[cc - 1]);
+        }
+        if (i1 <= ilast) {
+            for (int64_t cc = 1 + ln; cc <= i1; cc += 32) row[cc] = row[cc] - 2.0 * Av[cc - 1] * vi;
+        }
+        if (i1 == kn && ln == 0) row[kn] = row[kn] + 2.0 * ((2.0 * vk * vtAv - Av[kn - 1]) * vk - Av[kn - 1] * vk);
+        if (i1 > kn) {
+            const double avi = Av[i1 - 1];
+            for (int64_t cc = 1 + ln; cc <= ilast; cc += 32) row[cc] = row[cc] - 2.0 * v[cc - 1] * avi;
+            if (ln == 0) row[kn] = row[kn] - 2.0 * vk * avi;
+        }
+    }
+}
+
+__global__ void k_vec_with_kn(const double *v, int32_t ilast, double vk, int32_t kn, int32_t n, double *out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = i < ilast ? v[i] : (i == kn - 1 ? vk : 0.0);
+}
+
+// sqminl pivot step part 1 (one CTA): choose the pivot (first remaining
+// index with the largest |v_jj| above 1e-10 * |original diagonal|, the
+// choice of the reference's linked-list scan), scale the pivot row/column.
+__global__ void k_sqminl_pivot(int32_t n, double *v, double *b, const double *diag, int32_t *used,
+                               double *vk, double *scal, int32_t *pivot) {
+    __shared__ double sb[1024];
+    __shared__ int sk[1024];
+    const double eps = 1.0E-10;
+    double best = -1.0;
+    int bk = -1;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        if (used[j]) continue;
+        const double a = fabs(v[(int64_t)(j + 1) * (j + 2) / 2 - 1]);
+        if (a > eps * diag[j] && a > best) { best = a; bk = j; }
+    }
+    sb[threadIdx.x] = best;
+    sk[threadIdx.x] = bk;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            const double ob = sb[threadIdx.x + s];
+            const int ok = sk[threadIdx.x + s];
+            if (ob > sb[threadIdx.x] || (ob == sb[threadIdx.x] && ok >= 0 && (sk[threadIdx.x] < 0 || ok < sk[threadIdx.x]))) {
+                sb[threadIdx.x] = ob;
+                sk[threadIdx.x] = ok;
+            }
+        }
+        __syncthreads();
+    }
+    const int k = sk[0];
+    if (threadIdx.x == 0) *pivot = k;
+    if (k < 0) return;
+    const int64_t kk = (int64_t)(k + 1) * (k + 2) / 2 - 1;
+    const double vkk = 1.0 / v[kk];
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        if (j == k) { vk[j] = 0.0; continue; }
+        const int64_t jk = j > k ? (int64_t)j * (j + 1) / 2 + k : (int64_t)k * (k + 1) / 2 + j;
+        const double s = v[jk] * vkk;
+        v[jk] = s;
+        vk[j] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        v[kk] = -vkk;
+        b[k] = b[k] * vkk;
+        used[k] = 1;
+        scal[0] = vkk;
+    }
+}
+
+// sqminl pivot step part 2: rank-1 elimination of rows j != k
+__global__ void k_sqminl_elim(int32_t n, double *v, double *b, const double *vk, const double *scal,
+                              const int32_t *pivot) {
+    const int k = *pivot;
+    if (k < 0) return;
+    const double vkk = scal[0];
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double bk = b[k];
+    for (int64_t j = w; j < n; j += nw) {
+        if (j == k) continue;
+        const double vjk = vk[j] / vkk;
+        if (ln == 0) b[j] = b[j] - bk * vjk;
+        double *row = v + j * (j + 1) / 2;
+        for (int64_t c = ln; c <= j; c += 32) row[c] = row[c] - vk[c] * vjk;
+    }
+}
+
+__global__ void k_sqminl_deficit(int32_t n, double *v, double *b, const int32_t *used, const int32_t *pivot) {
+    if (*pivot >= 0) return;
+    for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+        if (used[j]) continue;
+        if (threadIdx.x == 0) b[j] = 0.0;
+        double *row = v + j * (j + 1) / 2;
+        for (int64_t c = threadIdx.x; c <= j; c += blockDim.x)
+            if (!used[c]) row[c] = 0.0;
+    }
+}
+
+__global__ void k_negate(int64_t n, double *v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = -v[i];
+}
+
+__global__ void k_diag_abs(int32_t n, const double *v, double *d) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = fabs(v[(i + 1) * (i + 2) / 2 - 1]);
+}
+
+// chdec2 step i (1-based): pivot, then the rank-1 update of rows 1..i-1
+__global__ void k_chdec_pivot(int64_t i, double *g, double *stat) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int64_t ii = i * (i + 1) / 2 - 1;
+    if (g[ii] > 0.0) {
+        const double d = g[ii];
+        if (stat[2] == 0.0) { stat[0] = d; stat[1] = d; }
+        else { stat[0] = fmax(stat[0], d); stat[1] = fmin(stat[1], d); }
+        stat[2] += 1.0;
+        g[ii] = 1.0 / d;
+    }
+}
+
+__global__ void k_chdec_update(int64_t i, double *g) {
+    const int64_t rowi = (i * i - i) / 2 - 1;   // g[rowi + c] = G(i, c), c 1-based
+    const double gii = g[rowi + i];
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t j = 1 + w; j <= i - 1; j += nw) {
+        const double ratio = g[rowi + j] * gii;
+        if (ratio == 0.0) continue;
+        double *rowj = g + (j * j - j) / 2 - 1;
+        for (int64_t c = 1 + ln; c <= j; c += 32) rowj[c] = rowj[c] - g[rowi + c] * ratio;
+    }
+}
+
+__global__ void k_chdec_scale(int64_t i, double *g) {
+    const int64_t rowi = (i * i - i) / 2 - 1;
+    const double gii = g[rowi + i];
+    for (int64_t c = 1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c <= i - 1; c += (int64_t)gridDim.x * blockDim.x)
+        g[rowi + c] = g[rowi + c] * gii;
+}
+
+// chslv2 (mpnum.f90:953-987), one CTA: backward then forward substitution
+__global__ void k_chslv2(const double *g, double *x, int32_t n) {
+    __shared__ double sh[1024];
+    // backward: x(i) -= sum_{k>i} G(k,i) x(k)
+    for (int64_t i = n; i >= 1; --i) {
+        double s = 0.0;
+        for (int64_t k = i + 1 + threadIdx.x; k <= n; k += blockDim.x) s += g[(k * k - k) / 2 + i - 1] * x[k - 1];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) x[i - 1] = x[i - 1] - s;
+        __syncthreads();
+    }
+    for (int64_t i = 1; i <= n; ++i) {
+        const int64_t ro = (i * i - i) / 2 - 1;
+        double s = 0.0;
+        for (int64_t k = 1 + threadIdx.x; k <= i - 1; k += blockDim.x) s += g[ro + k] * x[k - 1];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) x[i - 1] = x[i - 1] * g[ro + i] - s;
+        __syncthreads();
+    }
+}
+
+// corr(i) -= sum_j A'(nfit+j, i) y(j), i <= nfit (minver/mchdec rhs)
+__global__ void k_cons_rhs(int32_t nfit, int32_t ncon, const double *A, const double *y, double *corr) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nfit; i += (int64_t)gridDim.x * blockDim.x) {
+        double cval = corr[i];
+        for (int j = 0; j < ncon; ++j) {
+            const int64_t r = nfit + j + 1;
+            cval = cval - A[(r * r - r) / 2 + i] * y[j];
+        }
+        corr[i] = cval;
+    }
+}
+
+__global__ void k_zero_rows(int32_t nfit, int32_t n, double *A) {
+    for (int64_t r = nfit + 1 + blockIdx.x; r <= n; r += gridDim.x) {
+        double *row = A + (r * r - r) / 2;
+        for (int64_t c = threadIdx.x; c < r; c += blockDim.x) row[c] = 0.0;
+    }
+}
+
+__global__ void k_get_diag(int32_t n, const double *A, double *d) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        d[i] = A[(i + 1) * (i + 2) / 2 - 1];
+}
+
+// ---------------------------------------------------------------- sparse SpMV
+// Block table of the mpbits storage: for every stored block (I, J <= I) the
+// 0-based offset of element (0,0) in globalMatD and the row stride.
+struct SparseBlocks {
+    int64_t nblk = 0;
+    int64_t *rowStart = nullptr;   // [nG+1] blocks of row group I
+    int32_t *bcol = nullptr;       // column group
+    int64_t *boff = nullptr;
+    int32_t *bld = nullptr;
+    int64_t *tOff = nullptr;       // transposed-product buffer offset (off-diagonal blocks)
+    int64_t *colStart = nullptr;   // [nG+1] incoming blocks of column group J
+    int64_t *colBlk = nullptr;     // block ids ordered by (J, I)
+    double *tbuf = nullptr;
+    int64_t tlen = 0;
+};
+
+// phase 1: warp per row group I: y_I = D_I x_I + sum_J A_IJ x_J, the
+// strictly-lower part of the diagonal block also transposed into y_I, and
+// t_IJ = A_IJ^T x_I for J < I into tbuf
+__global__ void k_spmv_rows(int32_t nG, const int32_t *aig, const int64_t *rowStart, const int32_t *bcol,
+                            const int64_t *boff, const int32_t *bld, const int64_t *tOff,
+                            const double *matD, const double *x, double *y, double *tbuf) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t I = 1 + w; I <= nG; I += nw) {
+        const int32_t ia = aig[I - 1] - 1, np = aig[I] - 1 - ia;
+        for (int ii = 0; ii < np; ++ii) {
+            double s = 0.0;
+            for (int64_t bl = rowStart[I - 1]; bl < rowStart[I]; ++bl) {
+                const int32_t J = bcol[bl];
+                const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
+                const double *row = matD + boff[bl] + (int64_t)ii * bld[bl];
+                if (J == I) {
+                    for (int jj = ln; jj < ii; jj += 32) s += row[jj] * x[ja + jj];
+                    // transposed strictly-lower part: A(r, ii) for r > ii
+                    for (int rr = ii + 1 + ln; rr < np; rr += 32)
+                        s += matD[boff[bl] + (int64_t)rr * bld[bl] + ii] * x[ia + rr];
+                } else {
+                    for (int jj = ln; jj < nj; jj += 32) s += row[jj] * x[ja + jj];
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (ln == 0) y[ia + ii] = matD[ia + ii] * x[ia + ii] + s;
+        }
+        // transposed products of the off-diagonal blocks
+        for (int64_t bl = rowStart[I - 1]; bl < rowStart[I]; ++bl) {
+            const int32_t J = bcol[bl];
+            if (J == I) continue;
+            const int32_t nj = aig[J] - aig[J - 1];
+            for (int jj = ln; jj < nj; jj += 32) {
+                double t = 0.0;
+                for (int ii = 0; ii < np; ++ii) t += matD[boff[bl] + (int64_t)ii * bld[bl] + jj] * x[ia + ii];
+                tbuf[tOff[bl] + jj] = t;
+            }
+        }
+    }
+}
+
+// phase 2: warp per column group J adds the transposed products in a fixed order
+__global__ void k_spmv_cols(int32_t nG, const int32_t *aig, const int64_t *colStart, const int64_t *colBlk,
+                            const int64_t *tOff, const double *tbuf, double *y) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t J = 1 + w; J <= nG; J += nw) {
+        const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
+        for (int jj = ln; jj < nj; jj += 32) {
+            double s = y[ja + jj];
+            for (int64_t q = colStart[J - 1]; q < colStart[J]; ++q) s += tbuf[tOff[colBlk[q]] + jj];
+            y[ja + jj] = s;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- MINRES state
+struct MinresState {
+    double beta1, beta, oldb, alfa, dbar, epsln, oldeps, delta, gbar, root, gamma, cs, sn, phi, phibar;
+    double tnorm2, gmax, gmin, Anorm, ynorm, rnorm, denom, rtol;
+    double dotv;       // scratch result of the last dot
+    int itn, itnlim, istop, done;
+};
+
+__global__ void k_mr_init(MinresState *S, double rtol, int itnlim) {
+    if (threadIdx.x) return;
+    // beta1 = sqrt(r1 . y) is in S->dotv
+    double b1 = S->dotv;
+    memset(S, 0, sizeof(MinresState));
+    S->rtol = rtol;
+    S->itnlim = itnlim;
+    S->cs = -1.0;
+    S->gmin = 1.0e300;
+    if (b1 <= 0.0) { S->istop = b1 < 0.0 ? 9 : 0; S->done = 1; return; }
+    b1 = sqrt(b1);
+    S->beta1 = b1;
+    S->beta = b1;
+    S->phibar = b1;
+}
+
+__global__ void k_mr_scale_v(int32_t n, const MinresState *S, const double *y, double *v) {
+    if (S->done) return;
+    const double s = 1.0 / S->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = s * y[i];
+}
+
+__global__ void k_mr_y1(int32_t n, const MinresState *S, double *y, const double *r1) {
+    if (S->done || S->itn < 1) return;   // itn counts completed iterations
+    const double f = S->beta / S->oldb;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = y[i] - f * r1[i];
+}
+
+__global__ void k_mr_alfa(MinresState *S) {
+    if (threadIdx.x || S->done) return;
+    S->alfa = S->dotv;
+}
+
+__global__ void k_mr_y2(int32_t n, const MinresState *S, double *y, double *r1, double *r2, const double *cu) {
+    if (S->done) return;
+    const double f = S->alfa / S->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double yi = y[i] - f * r2[i];
+        r1[i] = r2[i];
+        r2[i] = yi;
+        y[i] = (yi * cu[i]) * cu[i];
+    }
+}
+
+__global__ void k_mr_rot(MinresState *S) {
+    if (threadIdx.x || S->done) return;
+    double b2 = S->dotv;
+    if (b2 < 0.0) { S->istop = 9; S->done = 1; return; }
+    S->oldb = S->beta;
+    S->beta = sqrt(b2);
+    S->tnorm2 += S->alfa * S->alfa + S->oldb * S->oldb + S->beta * S->beta;
+    S->oldeps = S->epsln;
+    S->delta = S->cs * S->dbar + S->sn * S->alfa;
+    S->gbar = S->sn * S->dbar - S->cs * S->alfa;
+    S->epsln = S->sn * S->beta;
+    S->dbar = -S->cs * S->beta;
+    S->root = sqrt(S->gbar * S->gbar + S->dbar * S->dbar);
+    double gamma = sqrt(S->gbar * S->gbar + S->beta * S->beta);
+    if (gamma < 2.220446049250313e-16) gamma = 2.220446049250313e-16;
+    S->gamma = gamma;
+    S->cs = S->gbar / gamma;
+    S->sn = S->beta / gamma;
+    S->phi = S->cs * S->phibar;
+    S->phibar = S->sn * S->phibar;
+    S->denom = 1.0 / gamma;
+    S->gmax = fmax(S->gmax, gamma);
+    S->gmin = fmin(S->gmin, gamma);
+}
+
+__global__ void k_mr_w(int32_t n, const MinresState *S, const double *v, double *w, double *w1, double *w2,
+                       double *x) {
+    if (S->done) return;
+    const double oe = S->oldeps, de = S->delta, dn = S->denom, ph = S->phi;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a = w2[i], b = w[i];
+        w1[i] = a;
+        w2[i] = b;
+        const double wn = (v[i] - oe * a - de * b) * dn;
+        w[i] = wn;
+        x[i] = x[i] + ph * wn;
+    }
+}
+
+__global__ void k_mr_test(MinresState *S) {
+    if (threadIdx.x || S->done) return;
+    S->itn += 1;
+    S->Anorm = sqrt(S->tnorm2);
+    S->ynorm = sqrt(S->dotv);
+    S->rnorm = S->phibar;
+    const double test1 = S->rnorm / (S->Anorm * S->ynorm);
+    const double test2 = S->root / S->Anorm;
+    const double Acond = S->gmax / S->gmin;
+    int istop = 0;
+    if (S->itn >= S->itnlim) istop = 6;
+    if (Acond >= 0.1 / 2.220446049250313e-16) istop = 4;
+    if (test2 <= S->rtol) istop = 2;
+    if (test1 <= S->rtol) istop = 1;
+    if (istop) { S->istop = istop; S->done = 1; }
+}
+
+__global__ void k_copy_pad(int32_t n, int32_t ntot, const double *x, double *xa) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * blockDim.x)
+        xa[i] = i < n ? x[i] : 0.0;
+}
+
+__global__ void k_copy_if(int32_t n, const MinresState *S, const double *a, double *b) {
+    if (S && S->done) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = a[i];
+}
+
+__global__ void k_apply_precond(int32_t n, const double *r, const double *cu, double *y) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (r[i] * cu[i]) * cu[i];
+}
+
+__global__ void k_precond(int32_t n, const double *dg, double *cu) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        cu[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
+}
+
+__global__ void k_diag_update(int32_t n, double *dg, const double *v, const double *y, const double *betap) {
+    const double beta = *betap;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dg[i] = dg[i] - 4.0 * v[i] * y[i] + 4.0 * beta * v[i] * v[i];
+}
+
+__global__ void k_sparse_diag(int32_t n, const double *matD, double *dg) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dg[i] = matD[i];
+}
+
+__global__ void k_sub(int32_t n, double *a, const double *b) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = a[i] - b[i];
+}
+
+// ---------------------------------------------------------------- helpers
+struct Solver {
+    mpgpu_ctx *c;
+    DevJob &j;
+    cudaStream_t s;
+    int nsm;
+    SparseBlocks sb;
+    double *part = nullptr;
+    explicit Solver(mpgpu_ctx *cc) : c(cc), j(cc->j), s(cc->stream) {
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    }
+    ~Solver() {
+        dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
+        dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tbuf); dfree(part);
+    }
+    unsigned grid(int64_t n, int per = kThreads) const {
+        int64_t g = (n + per - 1) / per;
+        int64_t m = (int64_t)nsm * 8;
+        if (g > m) g = m;
+        return (unsigned)(g < 1 ? 1 : g);
+    }
+    unsigned wgrid(int64_t nwarp) const { return grid(nwarp * 32); }
+
+    // block table of the sparse storage, built from the host copies
+    int32_t build_blocks() {
+        std::vector<int64_t> off(2 * (j.nG + 1));
+        std::vector<int32_t> col(std::max<int64_t>(j.ncolw, 1));
+        cudaMemcpy(off.data(), j.off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost);
+        if (j.ncolw > 0) cudaMemcpy(col.data(), j.col, sizeof(int32_t) * j.ncolw, cudaMemcpyDeviceToHost);
+        const std::vector<int32_t> &aig = j.hAig;
+        std::vector<int64_t> rowStart(1, 0), boff, tOff;
+        std::vector<int32_t> bcol, bld;
+        int64_t tl = 0;
+        for (int32_t I = 1; I <= j.nG; ++I) {
+            const int32_t np = aig[I] - aig[I - 1];
+            const int64_t kk = off[2 * (I - 1)], ll = off[2 * (I - 1) + 1];
+            const int64_t ku = off[2 * I] - kk;
+            if (ku > 0) {
+                if (col[kk] != 0) {  // uncompressed: one (np x ku) matrix
+                    int64_t k = 0;
+                    while (k < ku) {
+                        const int32_t first = col[kk + k];
+                        // group of this column
+                        int32_t J = (int32_t)(std::upper_bound(aig.begin(), aig.end(), first) - aig.begin());
+                        const int32_t nj = aig[J] - aig[J - 1];
+                        bcol.push_back(J);
+                        boff.push_back(ll + k);
+                        bld.push_back((int32_t)ku);
+                        tOff.push_back(J == I ? -1 : tl);
+                        if (J != I) tl += nj;
+                        k += nj;
+                    }
+                } else {  // compressed: regions (offset, first group) ... (end offset, n+1)
+                    for (int64_t k = 2; k <= ku - 2; k += 2) {
+                        const int32_t g0 = col[kk + k - 1];
+                        const int32_t o0 = col[kk + k - 2];
+                        const int32_t o1 = col[kk + k];
+                        const int32_t width = o1 - o0;
+                        int32_t inreg = 0, J = g0;
+                        while (inreg < width) {
+                            const int32_t nj = aig[J] - aig[J - 1];
+                            bcol.push_back(J);
+                            boff.push_back(ll + (int64_t)o0 * np + inreg);
+                            bld.push_back(width);
+                            tOff.push_back(J == I ? -1 : tl);
+                            if (J != I) tl += nj;
+                            inreg += nj;
+                            J++;
+                        }
+                    }
+                }
+            }
+            rowStart.push_back((int64_t)bcol.size());
+        }
+        // incoming (transposed) blocks per column group, ordered by row group
+        const int64_t nb = (int64_t)bcol.size();
+        std::vector<int64_t> cnt(j.nG + 2, 0);
+        std::vector<int32_t> brow(nb);
+        for (int32_t I = 1; I <= j.nG; ++I)
+            for (int64_t b = rowStart[I - 1]; b < rowStart[I]; ++b) brow[b] = I;
+        for (int64_t b = 0; b < nb; ++b)
+            if (bcol[b] != brow[b]) cnt[bcol[b]]++;
+        std::vector<int64_t> colStart(j.nG + 1, 0);
+        for (int32_t J = 1; J <= j.nG; ++J) colStart[J] = colStart[J - 1] + cnt[J];
+        std::vector<int64_t> fill(colStart.begin(), colStart.end() - 1), colBlk(std::max<int64_t>(colStart[j.nG], 1));
+        for (int64_t b = 0; b < nb; ++b)
+            if (bcol[b] != brow[b]) colBlk[fill[bcol[b] - 1]++] = b;
+        sb.nblk = nb;
+        sb.tlen = tl;
+        auto up = [&](auto *&d, const auto &h) -> cudaError_t {
+            cudaError_t e = cudaMalloc((void **)&d, sizeof(h[0]) * std::max<size_t>(h.size(), 1));
+            if (e != cudaSuccess) return e;
+            return cudaMemcpy(d, h.data(), sizeof(h[0]) * h.size(), cudaMemcpyHostToDevice);
+        };
+        MPG_CUDA(c, up(sb.rowStart, rowStart));
+        MPG_CUDA(c, up(sb.bcol, bcol));
+        MPG_CUDA(c, up(sb.boff, boff));
+        MPG_CUDA(c, up(sb.bld, bld));
+        MPG_CUDA(c, up(sb.tOff, tOff));
+        MPG_CUDA(c, up(sb.colStart, colStart));
+        MPG_CUDA(c, up(sb.colBlk, colBlk));
+        MPG_CUDA(c, cudaMalloc((void **)&sb.tbuf, sizeof(double) * std::max<int64_t>(tl, 1)));
+        return MPGPU_OK;
+    }
+
+    // y = A x (full parameter space)
+    void avprd0(const double *x, double *y) {
+        if (j.matsto == 2) {
+            k_spmv_rows<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.bcol, sb.boff, sb.bld,
+                                                         sb.tOff, j.matD, x, y, sb.tbuf);
+            k_spmv_cols<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.colStart, sb.colBlk, sb.tOff,
+                                                         sb.tbuf, y);
+        } else {
+            k_packed_matvec<<<wgrid(j.nVar), kThreads, 0, s>>>(j.nVar, j.matD, x, y);
+        }
+    }
+    void qlmlq(double *x, int t) {
+        if (j.ncon <= 0) return;
+        if (t) k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, j.nVar, j.ncon, j.ncon, 1, -1);
+        else k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, j.nVar, j.ncon, 1, j.ncon, 1);
+    }
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------- inversion / Cholesky
+// minver / mchdec (pede.f90:7838-8054) on the packed matrix
+int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrOut, double *errs,
+                        mpgpu_solveinfo *info, bool decomposition) {
+    Solver S(c);
+    DevJob &j = c->j;
+    cudaStream_t s = c->stream;
+    const int32_t n = j.nVar, ncon = j.ncon, nfit = n - ncon;
+    double *corr = nullptr, *vbuf = nullptr, *Av = nullptr, *vk = nullptr, *diag = nullptr, *yv = nullptr;
+    int32_t *used = nullptr, *piv = nullptr;
+    MPG_CUDA(c, cudaMalloc(&corr, sizeof(double) * n));
+    MPG_CUDA(c, cudaMalloc(&vbuf, sizeof(double) * n));
+    MPG_CUDA(c, cudaMalloc(&Av, sizeof(double) * n));
+    MPG_CUDA(c, cudaMalloc(&vk, sizeof(double) * n));
+    MPG_CUDA(c, cudaMalloc(&diag, sizeof(double) * n));
+    MPG_CUDA(c, cudaMalloc(&yv, sizeof(double) * (ncon + 1)));
+    MPG_CUDA(c, cudaMalloc(&used, sizeof(int32_t) * n));
+    MPG_CUDA(c, cudaMalloc(&piv, sizeof(int32_t) * 4));
+    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    MPG_CUDA(c, cudaMemcpyAsync(corr, j.gvec, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    double *scal = c->scal + 300;   // device scalars
+    // Q^T A Q (qlssq, reflections k = ncon .. 1)
+    auto qlssq = [&](int t) {
+        for (int jj = 1; jj <= ncon; ++jj) {
+            const int k = t ? ncon + 1 - jj : jj;
+            const int kn = n + k - ncon;
+            const int ilast = j.hR2[k - 1];
+            const double vkv = j.hVk[k - 1];
+            const double *v = j.qlV + (int64_t)(k - 1) * n;
+            k_vec_with_kn<<<S.grid(n), kThreads, 0, s>>>(v, ilast, vkv, kn, n, vbuf);
+            S.avprd0(vbuf, Av);
+            dot(vbuf, Av, n, S.part, scal, s);   // vtAv
+            k_qlssq_update<<<S.wgrid(n), kThreads, 0, s>>>(n, j.matD, v, vkv, Av, scal, ilast, kn);
+        }
+    };
+    std::vector<double> y(ncon > 0 ? ncon : 1, 0.0);
+    if (ncon > 0) {
+        qlssq(1);
+        // qlbsub (mpqldec.f90:991-1014) on the host
+        for (int k = ncon; k >= 1; --k) {
+            double d = 0.0;
+            for (int cc = 1; cc <= ncon - k; ++cc) d = d + j.hL[(size_t)(k - 1) * ncon + k - 1 + cc] * y[k - 1 + cc];
+            y[k - 1] = ((consResiduals ? consResiduals[k - 1] : 0.0) - d) / j.hL[(size_t)(k - 1) * ncon + k - 1];
+        }
+        MPG_CUDA(c, cudaMemcpyAsync(yv, y.data(), sizeof(double) * ncon, cudaMemcpyHostToDevice, s));
+        S.qlmlq(corr, 1);
+        k_cons_rhs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, ncon, j.matD, yv, corr);
+    }
+    int nrank = 0;
+    if (!decomposition) {
+        // sqminl (mpnum.f90:230-355) on the leading nfit x nfit block
+        k_diag_abs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, j.matD, diag);
+        MPG_CUDA(c, cudaMemsetAsync(used, 0, sizeof(int32_t) * nfit, s));
+        MPG_CUDA(c, cudaMemsetAsync(piv, 0, sizeof(int32_t) * 4, s));
+        for (int i = 0; i < nfit; ++i) {
+            k_sqminl_pivot<<<1, 1024, 0, s>>>(nfit, j.matD, corr, diag, used, vk, scal + 8, piv);
+            k_sqminl_elim<<<S.wgrid(nfit), kThreads, 0, s>>>(nfit, j.matD, corr, vk, scal + 8, piv);
+        }
+        k_sqminl_deficit<<<S.grid(nfit, 1), kThreads, 0, s>>>(nfit, j.matD, corr, used, piv);
+        k_negate<<<S.grid((int64_t)nfit * (nfit + 1) / 2), kThreads, 0, s>>>((int64_t)nfit * (nfit + 1) / 2, j.matD);
+        std::vector<int32_t> hu(nfit);
+        MPG_CUDA(c, cudaMemcpyAsync(hu.data(), used, sizeof(int32_t) * nfit, cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        for (int32_t u : hu) nrank += u;
+    } else {
+        // chdec2 + chslv2 (mpnum.f90:891-987)
+        MPG_CUDA(c, cudaMemsetAsync(scal + 16, 0, sizeof(double) * 3, s));
+        for (int64_t i = nfit; i >= 1; --i) {
+            k_chdec_pivot<<<1, 32, 0, s>>>(i, j.matD, scal + 16);
+            if (i > 1) {
+                k_chdec_update<<<S.wgrid(i - 1), kThreads, 0, s>>>(i, j.matD);
+                k_chdec_scale<<<S.grid(i - 1), kThreads, 0, s>>>(i, j.matD);
+            }
+        }
+        k_chslv2<<<1, 1024, 0, s>>>(j.matD, corr, nfit);
+        double st[3];
+        MPG_CUDA(c, cudaMemcpyAsync(st, scal + 16, sizeof(double) * 3, cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        info->evmax = st[0];
+        info->evmin = st[1];
+        nrank = (int)st[2];
+    }
+    info->nrank = nrank;
+    if (ncon > 0) {
+        MPG_CUDA(c, cudaMemcpyAsync(corr + nfit, yv, sizeof(double) * ncon, cudaMemcpyDeviceToDevice, s));
+        S.qlmlq(corr, 0);
+    }
+    if (!decomposition && errs) {
+        // covariance Q A^-1 Q^T with the constraint rows zeroed (xloopn,
+        // pede.f90:9094-9121); its diagonal gives the parameter errors
+        if (ncon > 0) {
+            k_zero_rows<<<S.grid(ncon, 1), kThreads, 0, s>>>(nfit, n, j.matD);
+            qlssq(0);
+        }
+        k_get_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, diag);
+        MPG_CUDA(c, cudaMemcpyAsync(errs, diag, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    }
+    MPG_CUDA(c, cudaMemcpyAsync(corrOut, corr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    cudaEventRecord(e1, s);
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    info->ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
+    cudaFree(used); cudaFree(piv);
+    return MPGPU_OK;
+}
+
+// ---------------------------------------------------------------- MINRES
+// mminrs (pede.f90:8243-8333) with the diagonal preconditioner of the
+// QL-reduced matrix and MINRES (Paige & Saunders 1975) kept on the device.
+int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
+                     double *corrOut, mpgpu_solveinfo *info) {
+    Solver S(c);
+    DevJob &j = c->j;
+    cudaStream_t s = c->stream;
+    const int32_t n = j.nVar, ncon = j.ncon, nfit = n - ncon;
+    if (j.matsto == 2) {
+        int32_t rc = S.build_blocks();
+        if (rc) return rc;
+    }
+    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    std::vector<double *> bufs;
+    auto vec = [&](int64_t len) -> double * {
+        double *p = nullptr;
+        if (cudaMalloc(&p, sizeof(double) * std::max<int64_t>(len, 1)) != cudaSuccess) return nullptr;
+        bufs.push_back(p);
+        return p;
+    };
+    double *rhs = vec(n), *xa = vec(n), *ba = vec(n), *dg = vec(n), *cu = vec(n), *tmp = vec(n), *yk = vec(n);
+    double *r1 = vec(n), *r2 = vec(n), *y = vec(n), *v = vec(n), *w = vec(n), *w1 = vec(n), *w2 = vec(n);
+    double *x = vec(n);
+    MinresState *St = nullptr;
+    MPG_CUDA(c, cudaMalloc(&St, sizeof(MinresState)));
+    for (double *p : bufs)
+        if (!p) return set_err(c, MPGPU_ERR_ALLOC, "MINRES workspace");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    MPG_CUDA(c, cudaMemcpyAsync(rhs, j.gvec, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    std::vector<double> yc(ncon > 0 ? ncon : 1, 0.0);
+    double *dsc = c->scal + 300;
+    if (ncon > 0) {
+        for (int k = ncon; k >= 1; --k) {
+            double d = 0.0;
+            for (int cc = 1; cc <= ncon - k; ++cc) d = d + j.hL[(size_t)(k - 1) * ncon + k - 1 + cc] * yc[k - 1 + cc];
+            yc[k - 1] = ((consResiduals ? consResiduals[k - 1] : 0.0) - d) / j.hL[(size_t)(k - 1) * ncon + k - 1];
+        }
+        // rhs - A Q [0; y], then Q^T
+        MPG_CUDA(c, cudaMemsetAsync(xa, 0, sizeof(double) * n, s));
+        MPG_CUDA(c, cudaMemcpyAsync(xa + nfit, yc.data(), sizeof(double) * ncon, cudaMemcpyHostToDevice, s));
+        S.qlmlq(xa, 0);
+        S.avprd0(xa, ba);
+        k_sub<<<S.grid(n), kThreads, 0, s>>>(n, rhs, ba);
+        S.qlmlq(rhs, 1);
+    }
+    // preconditioner: diagonal of Q^T A Q (the band-width-1 case of qlpssq,
+    // mpqldec.f90:711-950), reflections in the order of qlssq (k = m..1):
+    // y = P^T A P v_k with P = H_m ... H_{k+1}, dg -= 4 v y - 4 (v.y) v^2
+    if (j.matsto == 2) k_sparse_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
+    else k_get_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
+    for (int k = ncon; k >= 1; --k) {
+        const int kn = n + k - ncon;
+        const double *vr = j.qlV + (int64_t)(k - 1) * n;
+        k_vec_with_kn<<<S.grid(n), kThreads, 0, s>>>(vr, j.hR2[k - 1], j.hVk[k - 1], kn, n, v);
+        MPG_CUDA(c, cudaMemcpyAsync(tmp, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(tmp, j.qlV, j.qlVk, j.qlR2, n, ncon, k + 1, ncon, 1);
+        S.avprd0(tmp, yk);
+        if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(yk, j.qlV, j.qlVk, j.qlR2, n, ncon, ncon, k + 1, -1);
+        dot(v, yk, n, S.part, dsc, s);
+        k_diag_update<<<S.grid(n), kThreads, 0, s>>>(n, dg, v, yk, dsc);
+    }
+    k_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, dg, cu);
+    // MINRES state: x = 0, r1 = r2 = b, y = M^-1 r1, beta1 = sqrt(r1.y)
+    MPG_CUDA(c, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMemsetAsync(w, 0, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMemsetAsync(w1, 0, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMemsetAsync(w2, 0, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMemcpyAsync(r1, rhs, sizeof(double) * nfit, cudaMemcpyDeviceToDevice, s));
+    MPG_CUDA(c, cudaMemcpyAsync(r2, rhs, sizeof(double) * nfit, cudaMemcpyDeviceToDevice, s));
+    k_apply_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, r1, cu, y);
+    dot(r1, y, nfit, S.part, &St->dotv, s);
+    k_mr_init<<<1, 32, 0, s>>>(St, rtol, itnlim);
+    MinresState hs;
+    int it = 0;
+    const int batch = 16;
+    for (;;) {
+        for (int q = 0; q < batch; ++q) {
+            k_mr_scale_v<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, v);
+            // y = (Q^T A Q v)(1:nfit)
+            k_copy_pad<<<S.grid(n), kThreads, 0, s>>>(nfit, n, v, xa);
+            S.qlmlq(xa, 0);
+            S.avprd0(xa, ba);
+            S.qlmlq(ba, 1);
+            k_copy_if<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, ba, y);
+            k_mr_y1<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, r1);
+            dot(v, y, nfit, S.part, &St->dotv, s);
+            k_mr_alfa<<<1, 32, 0, s>>>(St);
+            k_mr_y2<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, r1, r2, cu);
+            dot(r2, y, nfit, S.part, &St->dotv, s);
+            k_mr_rot<<<1, 32, 0, s>>>(St);
+            k_mr_w<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, v, w, w1, w2, x);
+            dot(x, x, nfit, S.part, &St->dotv, s);
+            k_mr_test<<<1, 32, 0, s>>>(St);
+        }
+        it += batch;
+        MPG_CUDA(c, cudaMemcpyAsync(&hs, St, sizeof(MinresState), cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        if (hs.done || it > itnlim + batch) break;
+    }
+    info->itn = hs.itn;
+    info->istop = hs.istop;
+    if (ncon > 0) {
+        MPG_CUDA(c, cudaMemcpyAsync(x + nfit, yc.data(), sizeof(double) * ncon, cudaMemcpyHostToDevice, s));
+        S.qlmlq(x, 0);
+    }
+    MPG_CUDA(c, cudaMemcpyAsync(corrOut, x, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    cudaEventRecord(e1, s);
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    info->ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (double *p : bufs) cudaFree(p);
+    cudaFree(St);
+    return MPGPU_OK;
+}
+
+int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b) {
+    Solver S(c);
+    DevJob &j = c->j;
+    cudaStream_t s = c->stream;
+    if (j.matsto == 2) {
+        int32_t rc = S.build_blocks();
+        if (rc) return rc;
+    }
+    double *xa = nullptr, *ba = nullptr;
+    MPG_CUDA(c, cudaMalloc(&xa, sizeof(double) * j.nVar));
+    MPG_CUDA(c, cudaMalloc(&ba, sizeof(double) * j.nVar));
+    MPG_CUDA(c, cudaMemsetAsync(xa, 0, sizeof(double) * j.nVar, s));
+    MPG_CUDA(c, cudaMemcpyAsync(xa, x, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    S.qlmlq(xa, 0);
+    S.avprd0(xa, ba);
+    S.qlmlq(ba, 1);
+    MPG_CUDA(c, cudaMemcpyAsync(b, ba, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    cudaFree(xa);
+    cudaFree(ba);
+    return MPGPU_OK;
+}

@@ -1,0 +1,377 @@
+"""ctypes binding of libmpgpu.so (include/mpgpu.h).
+
+The Python side is a thin caller of the C-ABI, the same entry points the
+Fortran pede host binds through ISO_C_BINDING.  Loading fails loudly when the
+library has not been built: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(HERE, "lib")
+LIBPATH = os.path.join(LIBDIR, "libmpgpu.so")
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+f64p = C.POINTER(C.c_double)
+f32p = C.POINTER(C.c_float)
+
+
+class MpgpuCfg(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_int32), ("staging_bytes", C.c_int64)]
+
+
+class FitOpts(C.Structure):
+    _fields_ = [("icalcm", C.c_int32), ("nloopn", C.c_int32), ("lhuber", C.c_int32),
+                ("lfitbb", C.c_int32), ("chicut", C.c_float), ("chhuge", C.c_float),
+                ("dwcut", C.c_float), ("cndlmx", C.c_float)]
+
+
+class FitStats(C.Structure):
+    _fields_ = [("nrej", C.c_int64 * 6), ("chi2SumI", C.c_int64), ("chi2SumD", C.c_double),
+                ("ndfSum", C.c_int64), ("ndfSumW", C.c_double), ("nbndr", C.c_int32 * 2),
+                ("nbdrx", C.c_int32), ("nbndx", C.c_int32), ("naccepted", C.c_int64)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
+                ("pad", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
+                ("ms", C.c_double)]
+
+
+class Steer(C.Structure):
+    _fields_ = [("metsol", C.c_int32), ("matsto", C.c_int32), ("mitera", C.c_int32),
+                ("lhuber", C.c_int32), ("chicut", C.c_float), ("chirem", C.c_float),
+                ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float),
+                ("lfitbb", C.c_int32), ("mreqenf", C.c_int32), ("mreqena", C.c_int32),
+                ("mreqpe", C.c_int32), ("mrestl", C.c_double), ("itnlim", C.c_int32),
+                ("nthreads", C.c_int32)]
+
+
+class Job(C.Structure):
+    _fields_ = [("nrec", C.c_int64), ("recPtr", i64p), ("inder", i32p), ("glder", f64p),
+                ("recFile", i32p), ("nfiles", C.c_int32), ("fileWeight", f64p),
+                ("npar", C.c_int32), ("parLabel", i32p), ("parValue", f64p),
+                ("parSigma", f64p),
+                ("ncon", C.c_int32), ("conStart", i32p), ("conLabel", i32p),
+                ("conCoef", f64p), ("conRhs", f64p),
+                ("nmeas", C.c_int32), ("msStart", i32p), ("msLabel", i32p),
+                ("msCoef", f64p), ("msRhs", f64p), ("msSigma", f64p)]
+
+
+class Result(C.Structure):
+    _fields_ = [("cap", C.c_int32), ("nTotal", C.c_int32), ("nVar", C.c_int32),
+                ("nVarGroups", C.c_int32), ("nFit", C.c_int32),
+                ("labels", i32p), ("parameter", f64p), ("presigma", f64p), ("error", f64p),
+                ("counts", i64p), ("varIndex", i32p),
+                ("nrej", C.c_int64 * 6), ("fvalue", C.c_double), ("ndf", C.c_int64),
+                ("nrank", C.c_int32), ("minresItn", C.c_int32), ("minresIstop", C.c_int32),
+                ("nloopn", C.c_int32), ("exitCode", C.c_int32),
+                ("msBuild", C.c_double), ("msSolve", C.c_double)]
+
+
+class GenCfg(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nlayers", C.c_int32), ("nmod", C.c_int32),
+                ("minHits", C.c_int32), ("maxHits", C.c_int32), ("ntracks", C.c_int64),
+                ("seed", C.c_uint64), ("sigma1", C.c_double), ("sigma2", C.c_double),
+                ("misal", C.c_double), ("outlierFrac", C.c_double), ("theta0", C.c_double)]
+
+
+def ptr(a, t):
+    """ctypes pointer to a contiguous numpy array (None -> NULL)."""
+    if a is None:
+        return C.cast(None, t)
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(t)
+
+
+_lib = None
+
+
+def lib():
+    """Load libmpgpu.so; raises when it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError(f"libmpgpu.so not built ({LIBPATH}); run __graft_entry__.build()")
+        L = C.CDLL(LIBPATH)
+        if hasattr(L, "mpgpu_last_error"):
+            L.mpgpu_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+EXPORTS = [
+    "mpgpu_create", "mpgpu_destroy", "mpgpu_last_error", "mpgpu_set_layout",
+    "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
+    "mpgpu_mupdat", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
+    "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_host_labels",
+    "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
+    "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
+]
+
+
+# ----------------------------------------------------------------- data
+def gen_config(name, ntracks=None, seed=None):
+    """Named synthetic workloads (sizes of the benchmark configurations)."""
+    if name == "telescope":      # 10 layers x 20 modules, 200 x-shifts
+        c = GenCfg(kind=1, nlayers=10, nmod=20, ntracks=5000, seed=1, sigma1=0.005,
+                   sigma2=0.005, misal=0.01)
+    elif name == "barrel":       # 5000 modules x 6 dof = 30000 globals
+        c = GenCfg(kind=2, nmod=5000, ntracks=2_000_000, seed=2, sigma1=0.002, sigma2=0.008,
+                   misal=0.005)
+    elif name == "brokenlines":  # barrel, 4..40 hits, nloc 8..84
+        c = GenCfg(kind=3, nmod=5000, minHits=4, maxHits=40, ntracks=1_000_000, seed=3,
+                   sigma1=0.002, sigma2=0.008, misal=0.005, theta0=0.001)
+    elif name == "telescope_dense":  # telescope scaled up in module count
+        c = GenCfg(kind=1, nlayers=10, nmod=2000, ntracks=400_000, seed=4, sigma1=0.005,
+                   sigma2=0.005, misal=0.01)
+    else:
+        raise ValueError(name)
+    if ntracks is not None:
+        c.ntracks = ntracks
+    if seed is not None:
+        c.seed = seed
+    return c
+
+
+def generate(cfg):
+    """Mille records (recPtr, inder, glder), true misalignments, constraints."""
+    L = lib()
+    nrec, nw, nlab = C.c_int64(), C.c_int64(), C.c_int32()
+    rc = L.mpgen_count(C.byref(cfg), C.byref(nrec), C.byref(nw), C.byref(nlab))
+    assert rc == 0, rc
+    recPtr = np.zeros(nrec.value + 1, np.int64)
+    inder = np.zeros(nw.value, np.int32)
+    glder = np.zeros(nw.value, np.float64)
+    truth = np.zeros(nlab.value, np.float64)
+    rc = L.mpgen_fill(C.byref(cfg), ptr(recPtr, i64p), ptr(inder, i32p), ptr(glder, f64p),
+                      ptr(truth, f64p))
+    assert rc == 0, rc
+    ncon = C.c_int32()
+    L.mpgen_constraints(C.byref(cfg), C.byref(ncon), None, None, None)
+    nwc = L.mpgen_constraint_words(C.byref(cfg))
+    conStart = np.zeros(ncon.value + 1, np.int32)
+    conLabel = np.zeros(nwc, np.int32)
+    conCoef = np.zeros(nwc, np.float64)
+    L.mpgen_constraints(C.byref(cfg), C.byref(ncon), ptr(conStart, i32p), ptr(conLabel, i32p),
+                        ptr(conCoef, f64p))
+    return dict(recPtr=recPtr, inder=inder, glder=glder, truth=truth, conStart=conStart,
+                conLabel=conLabel, conCoef=conCoef, ncon=ncon.value)
+
+
+def write_mille_c(path, recPtr, inder, glder):
+    """Write records as a C-format double-precision Mille binary file
+    (int32 header -2*w, w doubles, w int32; python/readMilleBinary.py)."""
+    with open(path, "wb") as f:
+        for r in range(len(recPtr) - 1):
+            a, b = recPtr[r], recPtr[r + 1]
+            np.array([-2 * (b - a)], np.int32).tofile(f)
+            glder[a:b].tofile(f)
+            inder[a:b].tofile(f)
+
+
+def read_mille_c(path):
+    """Read a C-format Mille binary file (float or double records)."""
+    data = open(path, "rb").read()
+    pos, ptrs, ints, dbls = 0, [0], [], []
+    while pos < len(data):
+        h = int(np.frombuffer(data, np.int32, 1, pos)[0]); pos += 4
+        w = abs(h) // 2
+        if h < 0:
+            d = np.frombuffer(data, np.float64, w, pos); pos += 8 * w
+        else:
+            d = np.frombuffer(data, np.float32, w, pos).astype(np.float64); pos += 4 * w
+        i = np.frombuffer(data, np.int32, w, pos); pos += 4 * w
+        ints.append(i); dbls.append(d); ptrs.append(ptrs[-1] + w)
+    return (np.array(ptrs, np.int64), np.concatenate(ints).astype(np.int32),
+            np.concatenate(dbls).astype(np.float64))
+
+
+# ----------------------------------------------------------------- host side
+class HostStructure:
+    """loop1/loop2 products computed by the library's host side:
+    sorted labels, entries, variable indices, parameter groups, translated
+    records and (sparse storage) the mpbits row structure."""
+
+    def __init__(self, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True):
+        L = lib()
+        self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
+        inder = np.ascontiguousarray(data["inder"], np.int32)
+        self.glder = np.ascontiguousarray(data["glder"], np.float64)
+        nrec = len(self.recPtr) - 1
+        cap = len(inder) + len(steerLabels) + 16
+        labels = np.zeros(cap, np.int32)
+        counter = np.zeros(cap, np.int64)
+        varIndex = np.zeros(cap, np.int32)
+        totGroup = np.zeros(cap, np.int32)
+        nVar, nG = C.c_int32(), C.c_int32()
+        sl = np.ascontiguousarray(steerLabels, np.int32)
+        pl = np.ascontiguousarray(preLabel, np.int32)
+        ps = np.ascontiguousarray(preSigma, np.float64)
+        n = L.mpgpu_host_labels(C.c_int64(nrec), ptr(self.recPtr, i64p), ptr(inder, i32p),
+                                ptr(self.glder, f64p), C.c_int32(len(sl)), ptr(sl, i32p),
+                                C.c_int32(len(pl)), ptr(pl, i32p), ptr(ps, f64p),
+                                C.c_int32(mreqenf), C.c_int32(cap), ptr(labels, i32p),
+                                ptr(counter, i64p), ptr(varIndex, i32p), ptr(totGroup, i32p),
+                                C.byref(nVar), C.byref(nG))
+        if n < 0:
+            raise RuntimeError(f"mpgpu_host_labels failed ({n})")
+        self.nTotal = n
+        self.labels, self.counter = labels[:n].copy(), counter[:n].copy()
+        self.varIndex, self.totGroup = varIndex[:n].copy(), totGroup[:n].copy()
+        self.nVar, self.nG = nVar.value, nG.value
+        aig = []
+        prev = -1
+        for i in range(n):
+            if self.varIndex[i] <= 0:
+                continue
+            if self.totGroup[i] != prev:
+                aig.append(self.varIndex[i])
+                prev = self.totGroup[i]
+        aig.append(self.nVar + 1)
+        self.aig = np.array(aig, np.int32)
+        self.tinder = np.zeros_like(inder)
+        rc = L.mpgpu_host_translate(C.c_int64(nrec), ptr(self.recPtr, i64p), ptr(inder, i32p),
+                                    ptr(self.glder, f64p), C.c_int32(n), ptr(self.labels, i32p),
+                                    ptr(self.tinder, i32p))
+        if rc:
+            raise RuntimeError(f"mpgpu_host_translate failed ({rc})")
+        self.offsets = np.zeros(2 * (self.nG + 1), np.int64)
+        self.columns = np.zeros(1, np.int32)
+        self.ncolw = 0
+        self.nmatSparse = 0
+        if sparse:
+            capc = 1 << 20
+            while True:
+                cols = np.zeros(capc, np.int32)
+                ncolw, nmat = C.c_int64(), C.c_int64()
+                rc = L.mpgpu_host_mpbits(C.c_int64(nrec), ptr(self.recPtr, i64p),
+                                         ptr(self.tinder, i32p), ptr(self.glder, f64p),
+                                         ptr(self.varIndex, i32p), C.c_int32(self.nVar),
+                                         C.c_int32(self.nG), ptr(self.aig, i32p), C.c_int64(capc),
+                                         ptr(self.offsets, i64p), ptr(cols, i32p),
+                                         C.byref(ncolw), C.byref(nmat))
+                if rc == 0:
+                    break
+                capc *= 4
+            self.columns = cols[:max(ncolw.value, 1)].copy()
+            self.ncolw, self.nmatSparse = ncolw.value, nmat.value
+        self.nmatPacked = self.nVar * (self.nVar + 1) // 2
+
+
+class Context:
+    """One device context with a layout and uploaded records."""
+
+    def __init__(self, device=0, staging_bytes=0):
+        self.L = lib()
+        self.h = C.c_void_p()
+        cfg = MpgpuCfg(device=device, flags=0, staging_bytes=staging_bytes)
+        self.check(self.L.mpgpu_create(C.byref(self.h), C.byref(cfg)))
+
+    def check(self, rc):
+        if rc != 0:
+            msg = self.L.mpgpu_last_error(self.h) if self.h else b""
+            raise RuntimeError(f"mpgpu error {rc}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self.h:
+            self.L.mpgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_layout(self, S, matsto):
+        self.nVar, self.nTotal, self.matsto = S.nVar, S.nTotal, matsto
+        self.nmat = S.nmatSparse if matsto == 2 else S.nmatPacked
+        self.check(self.L.mpgpu_set_layout(
+            self.h, C.c_int32(S.nTotal), ptr(S.varIndex, i32p), C.c_int32(S.nVar),
+            C.c_int32(S.nG), ptr(S.aig, i32p), C.c_int32(matsto),
+            ptr(S.offsets if matsto == 2 else None, i64p),
+            ptr(S.columns if matsto == 2 else None, i32p), C.c_int64(S.ncolw),
+            C.c_int64(self.nmat)))
+
+    def set_constraints(self, A):
+        A = np.ascontiguousarray(A, np.float64)
+        self.ncon = A.shape[0]
+        self.check(self.L.mpgpu_set_constraints(self.h, C.c_int32(A.shape[0]), ptr(A, f64p)))
+
+    def upload(self, S, recFile=None, fileWeight=None):
+        self.nrec = len(S.recPtr) - 1
+        rf = None if recFile is None else np.ascontiguousarray(recFile, np.int32)
+        fw = None if fileWeight is None else np.ascontiguousarray(fileWeight, np.float64)
+        self.nfiles = 1 if fw is None else len(fw)
+        self.check(self.L.mpgpu_upload_records(
+            self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(S.tinder, i32p),
+            ptr(S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
+
+    def loopbf(self, gpar, **kw):
+        o = dict(icalcm=1, nloopn=1, lhuber=0, lfitbb=1, chicut=0.0, chhuge=50.0, dwcut=0.0,
+                 cndlmx=100.0)
+        o.update(kw)
+        fo = FitOpts(**o)
+        st = FitStats()
+        gvec = np.zeros(self.nVar, np.float64)
+        gcnt = np.zeros(self.nVar, np.int64)
+        naccf = np.zeros(self.nfiles, np.int32)
+        chi2f = np.zeros(self.nfiles, np.float32)
+        ndff = np.zeros(self.nfiles, np.int32)
+        gpar = np.ascontiguousarray(gpar, np.float64)
+        self.check(self.L.mpgpu_loopbf(self.h, C.byref(fo), ptr(gpar, f64p), ptr(gvec, f64p),
+                                       ptr(gcnt, i64p), C.byref(st), ptr(naccf, i32p),
+                                       ptr(chi2f, f32p), ptr(ndff, i32p)))
+        return dict(gvec=gvec, gcnt=gcnt, nrej=list(st.nrej), chi2=st.chi2SumD + st.chi2SumI,
+                    ndf=st.ndfSum, naccepted=st.naccepted, nbndr=list(st.nbndr),
+                    nbdrx=st.nbdrx, nbndx=st.nbndx, naccf=naccf, chi2f=chi2f, ndff=ndff)
+
+    def matrix(self):
+        m = np.zeros(self.nmat, np.float64)
+        self.check(self.L.mpgpu_download_matrix(self.h, ptr(m, f64p)))
+        return m
+
+    def status(self):
+        s = np.zeros(self.nrec, np.int32)
+        self.check(self.L.mpgpu_download_record_status(self.h, ptr(s, i32p)))
+        return s
+
+    def mupdat(self, i, j, add):
+        i = np.ascontiguousarray(i, np.int32)
+        j = np.ascontiguousarray(j, np.int32)
+        add = np.ascontiguousarray(add, np.float64)
+        self.check(self.L.mpgpu_mupdat(self.h, C.c_int32(len(i)), ptr(i, i32p), ptr(j, i32p),
+                                       ptr(add, f64p)))
+
+    def solve(self, metsol, consResiduals=None, rtol=1e-10, itnlim=2000, errors=False):
+        corr = np.zeros(self.nVar, np.float64)
+        err = np.zeros(self.nVar, np.float64) if errors else None
+        cr = None if consResiduals is None else np.ascontiguousarray(consResiduals, np.float64)
+        info = SolveInfo()
+        self.check(self.L.mpgpu_solve(self.h, C.c_int32(metsol), ptr(cr, f64p), C.c_double(rtol),
+                                      C.c_int32(itnlim), ptr(corr, f64p), ptr(err, f64p),
+                                      C.byref(info)))
+        return corr, err, info
+
+    def avprod(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        b = np.zeros_like(x)
+        self.check(self.L.mpgpu_avprod(self.h, C.c_int32(len(x)), ptr(x, f64p), ptr(b, f64p)))
+        return b
+
+
+def constraint_matrix(data, S):
+    """Rows of the constraint matrix over the variable parameters."""
+    A = np.zeros((data["ncon"], S.nVar))
+    pos = {int(l): i for i, l in enumerate(S.labels)}
+    cs, cl, cc = data["conStart"], data["conLabel"], data["conCoef"]
+    for c in range(data["ncon"]):
+        for k in range(cs[c], cs[c + 1]):
+            li = pos.get(int(cl[k]))
+            if li is not None and S.varIndex[li] > 0:
+                A[c, S.varIndex[li] - 1] += cc[k]
+    return A

@@ -1,0 +1,579 @@
+/*
+ * mpref_solve.c -- oracle: global solvers.  TEST INFRASTRUCTURE ONLY.
+ *
+ * Packed Gauss-Jordan inversion (sqminl), root-free Cholesky (chdec2/chslv2),
+ * Householder QL elimination of linear constraints (mpqldec.f90, one
+ * parameter block), the sparse/packed matrix-vector product (avprd0) and
+ * preconditioned MINRES written from Paige & Saunders (1975).
+ */
+#include "mpref.h"
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* sqminl, mpnum.f90:230-355 (eps = 1e-10 relative pivot limit) */
+void mpref_sqminl(double *v0, double *b0, int32_t n, int32_t *nrank)
+{
+    double *v = v0 - 1, *b = b0 - 1;
+    double *diag = (double *)malloc(sizeof(double) * ((size_t)n + 1));
+    double *vk = (double *)malloc(sizeof(double) * ((size_t)n + 1));
+    int32_t *next = (int32_t *)malloc(sizeof(int32_t) * ((size_t)n + 1));
+    const double eps = 1.0E-10;
+    int32_t i, j, k, l = 1, last, next0 = 1;
+    double vkk, vjk;
+    for (i = 1; i <= n; i++) {
+        int64_t i8 = i;
+        next[i] = i + 1;
+        diag[i] = fabs(v[(i8 * i8 + i8) / 2]);
+    }
+    next[n] = -1;
+    *nrank = 0;
+    for (i = 1; i <= n; i++) {
+        k = 0;
+        vkk = 0.0;
+        j = next0;
+        last = 0;
+        while (j > 0) {
+            int64_t j8 = j, jj = (j8 * j8 + j8) / 2;
+            double lim = fabs(vkk) > eps * diag[j] ? fabs(vkk) : eps * diag[j];
+            if (fabs(v[jj]) > lim) {
+                vkk = v[jj];
+                k = j;
+                l = last;
+            }
+            last = j;
+            j = next[last];
+        }
+        if (k != 0) {
+            int64_t k8 = k, kk = (k8 * k8 + k8) / 2, kkmk = kk - k8, jk;
+            if (l == 0) next0 = next[k];
+            else next[l] = next[k];
+            next[k] = 0;
+            (*nrank)++;
+            vkk = 1.0 / vkk;
+            v[kk] = -vkk;
+            b[k] = b[k] * vkk;
+            jk = kkmk;
+            for (j = 1; j <= n; j++) {
+                if (j == k) {
+                    jk = kk;
+                    vk[j] = 0.0;
+                } else {
+                    if (j < k) jk = jk + 1;
+                    else jk = jk + j - 1;
+                    v[jk] = v[jk] * vkk;
+                    vk[j] = v[jk];
+                }
+            }
+            for (j = n; j >= 1; j--) {
+                if (j == k) continue;
+                int64_t j8 = j, jl = j8 * (j8 - 1) / 2;
+                vjk = vk[j] / vkk;
+                b[j] = b[j] - b[k] * vjk;
+                for (int32_t c = 1; c <= j; c++) v[jl + c] = v[jl + c] - vk[c] * vjk;
+            }
+        } else {
+            for (k = 1; k <= n; k++) {
+                int64_t k8 = k, kk = (k8 * k8 - k8) / 2;
+                if (next[k] != 0) {
+                    b[k] = 0.0;
+                    for (j = 1; j <= k; j++)
+                        if (next[j] != 0) v[kk + j] = 0.0;
+                }
+            }
+            break;
+        }
+    }
+    for (int64_t jj = 1; jj <= (int64_t)n * (int64_t)(n + 1) / 2; jj++) v[jj] = -v[jj];
+    free(diag);
+    free(vk);
+    free(next);
+}
+
+/* chdec2, mpnum.f90:891-942 (root-free LDLt of the packed lower triangle,
+ * processed from the last row upwards; diagonal replaced by 1/d) */
+void mpref_chdec2(double *g0, int32_t n, int32_t *nrank, double *evmax, double *evmin)
+{
+    double *g = g0 - 1;
+    int64_t ii = ((int64_t)n * (int64_t)(n + 1)) / 2, jj;
+    int32_t i, j;
+    double ratio;
+    *nrank = 0;
+    *evmax = 0.0;
+    *evmin = 0.0;
+    for (i = n; i >= 1; i--) {
+        if (g[ii] > 0.0) {
+            (*nrank)++;
+            if (*nrank == 1) {
+                *evmax = g[ii];
+                *evmin = g[ii];
+            } else {
+                if (g[ii] > *evmax) *evmax = g[ii];
+                if (g[ii] < *evmin) *evmin = g[ii];
+            }
+            g[ii] = 1.0 / g[ii];
+        }
+        ii = ii - i;
+        for (j = 1; j <= i - 1; j++) {
+            ratio = g[ii + j] * g[ii + i];
+            if (ratio == 0.0) continue;
+            jj = ((int64_t)(j - 1) * (int64_t)j) / 2;
+            for (int32_t c = 1; c <= j; c++) g[jj + c] = g[jj + c] - g[ii + c] * ratio;
+        }
+        for (int32_t c = 1; c <= i - 1; c++) g[ii + c] = g[ii + c] * g[ii + i];
+    }
+}
+
+/* chslv2, mpnum.f90:953-987 */
+void mpref_chslv2(const double *g0, double *x0, int32_t n)
+{
+    const double *g = g0 - 1;
+    double *x = x0 - 1;
+    int64_t ii = ((int64_t)n * (int64_t)(n + 1)) / 2, kk;
+    int32_t i, k;
+    double dsum;
+    for (i = n; i >= 1; i--) {
+        dsum = x[i];
+        kk = ii;
+        for (k = i + 1; k <= n; k++) {
+            dsum = dsum - g[kk + i] * x[k];
+            kk = kk + k;
+        }
+        x[i] = dsum;
+        ii = ii - i;
+    }
+    for (i = 1; i <= n; i++) {
+        dsum = x[i] * g[ii + i];
+        for (k = 1; k <= i - 1; k++) dsum = dsum - g[k + ii] * x[k];
+        x[i] = dsum;
+        ii = ii + i;
+    }
+}
+
+/* ------------------------------------------------------------------ QL */
+struct mpref_ql {
+    int32_t npar, ncon;
+    double *V;    /* ncon x npar (1-based flat: V[(k-1)*npar + i]) */
+    double *Vk;   /* [1..ncon] */
+    double *L;    /* ncon x ncon (1-based flat) */
+    int32_t *r1, *r2;  /* irangeParNZ */
+};
+
+/* qldec, mpqldec.f90:125-196 */
+mpref_ql *mpref_ql_create(int32_t npar, int32_t ncon, const double *A)
+{
+    mpref_ql *q = (mpref_ql *)calloc(1, sizeof(mpref_ql));
+    int64_t len = (int64_t)npar * ncon;
+    q->npar = npar;
+    q->ncon = ncon;
+    q->V = (double *)calloc((size_t)len + 1, sizeof(double));
+    q->Vk = (double *)calloc((size_t)ncon + 1, sizeof(double));
+    q->L = (double *)calloc((size_t)ncon * ncon + 1, sizeof(double));
+    q->r1 = (int32_t *)calloc((size_t)ncon + 1, sizeof(int32_t));
+    q->r2 = (int32_t *)calloc((size_t)ncon + 1, sizeof(int32_t));
+    double *vecN = (double *)calloc((size_t)npar + 1, sizeof(double));
+    double *V = q->V;
+    for (int64_t i = 0; i < len; i++) V[i + 1] = A[i];
+    for (int32_t k = ncon; k >= 1; k--) {
+        int32_t kn = npar + k - ncon, i, c;
+        int64_t ioff1 = (int64_t)(k - 1) * npar, ioff2, ioff3;
+        double nrm = 0.0, sp;
+        for (c = 1; c <= kn; c++) vecN[c] = V[ioff1 + c];
+        for (c = 1; c <= kn; c++) nrm = nrm + vecN[c] * vecN[c];
+        nrm = sqrt(nrm);
+        if (nrm == 0.0) continue;
+        if (vecN[kn] >= 0.0) vecN[kn] = vecN[kn] + nrm;
+        else vecN[kn] = vecN[kn] - nrm;
+        nrm = 0.0;
+        for (c = 1; c <= kn; c++) nrm = nrm + vecN[c] * vecN[c];
+        nrm = sqrt(nrm);
+        for (c = 1; c <= kn; c++) vecN[c] = vecN[c] / nrm;
+        ioff2 = 0;
+        for (i = 1; i <= k; i++) {
+            sp = 0.0;
+            for (c = 1; c <= kn; c++) sp = sp + vecN[c] * V[ioff2 + c];
+            for (c = 1; c <= kn; c++) V[ioff2 + c] = V[ioff2 + c] - 2.0 * vecN[c] * sp;
+            ioff2 = ioff2 + npar;
+        }
+        ioff3 = (int64_t)(k - 1) * ncon;
+        for (c = k; c <= ncon; c++) q->L[ioff3 + c] = V[ioff1 + kn + (c - k)];
+        for (c = 1; c <= kn - 1; c++) V[ioff1 + c] = vecN[c];
+        for (c = kn; c <= npar; c++) V[ioff1 + c] = 0.0;
+        q->r1[k] = 1;
+        q->r2[k] = kn - 1;
+        q->Vk[k] = vecN[kn];
+    }
+    free(vecN);
+    return q;
+}
+
+void mpref_ql_destroy(mpref_ql *q)
+{
+    if (!q) return;
+    free(q->V); free(q->Vk); free(q->L); free(q->r1); free(q->r2);
+    free(q);
+}
+
+void mpref_ql_export(const mpref_ql *q, double *V, double *Vk, double *L)
+{
+    int64_t len = (int64_t)q->npar * q->ncon;
+    if (V) for (int64_t i = 0; i < len; i++) V[i] = q->V[i + 1];
+    if (Vk) for (int32_t i = 0; i < q->ncon; i++) Vk[i] = q->Vk[i + 1];
+    if (L) for (int64_t i = 0; i < (int64_t)q->ncon * q->ncon; i++) L[i] = q->L[i + 1];
+}
+
+/* qlmlq, mpqldec.f90:404-454 (m = 1) */
+void mpref_ql_mlq(const mpref_ql *q, double *x0, int32_t t)
+{
+    double *x = x0 - 1;
+    int32_t nconb = q->ncon, nparb = q->npar;
+    for (int32_t j = 1; j <= nconb; j++) {
+        int32_t k = t ? nconb + 1 - j : j;
+        int32_t kn = nparb + k - nconb, ifirst = q->r1[k], ilast = q->r2[k], c;
+        const double *vr = q->V + (int64_t)(k - 1) * nparb;   /* vr[1..] */
+        double vkn = q->Vk[k];
+        if (ifirst <= 0) continue;
+        double sp = 0.0;
+        for (c = ifirst; c <= ilast; c++) sp = sp + vr[1 + c - ifirst] * x[c];
+        sp = sp + vkn * x[kn];
+        for (c = ifirst; c <= ilast; c++) x[c] = x[c] - 2.0 * vr[1 + c - ifirst] * sp;
+        x[kn] = x[kn] - 2.0 * vkn * sp;
+    }
+}
+
+/* qlbsub, mpqldec.f90:991-1014 */
+void mpref_ql_bsub(const mpref_ql *q, const double *d0, double *y0)
+{
+    const double *d = d0 - 1;
+    double *y = y0 - 1;
+    int32_t ncon = q->ncon, nconb = ncon;
+    int64_t idiag = (int64_t)ncon * (ncon - 1) + nconb;
+    for (int32_t k = nconb; k >= 1; k--) {
+        double dot = 0.0;
+        for (int32_t c = 1; c <= nconb - k; c++) dot = dot + q->L[idiag + c] * y[k + c];
+        y[k] = (d[k] - dot) / q->L[idiag];
+        idiag = idiag - ncon - 1;
+    }
+}
+
+/* qlgete, mpqldec.f90:955-981 */
+void mpref_ql_gete(const mpref_ql *q, double *emin, double *emax)
+{
+    int64_t idiag = 1;
+    *emax = q->L[1];
+    *emin = *emax;
+    for (int32_t i = 1; i <= q->ncon; i++) {
+        if (fabs(*emax) < fabs(q->L[idiag])) *emax = q->L[idiag];
+        if (fabs(*emin) > fabs(q->L[idiag])) *emin = q->L[idiag];
+        idiag = idiag + q->ncon + 1;
+    }
+}
+
+/* avprds, pede.f90:4855-4930 (packed part): y += A x using only the
+ * components x(is..ie); lower part first, then the transposed part */
+static void aprod_packed_range(int32_t n, const double *A, const double *x, int32_t is,
+                               int32_t ie, double *y)
+{
+    /* A 1-based packed lower triangle, x, y 1-based */
+    for (int32_t i = 1; i <= n; i++) {
+        int64_t ij = ((int64_t)i * i - i) / 2;
+        int32_t jhi = ie < i ? ie : i;
+        for (int32_t j = is; j <= jhi; j++) y[i] = y[i] + A[ij + j] * x[j];
+    }
+    for (int32_t i = is; i <= ie; i++) {
+        int64_t ij = ((int64_t)i * i - i) / 2;
+        for (int32_t j = 1; j <= i - 1; j++) y[j] = y[j] + A[ij + j] * x[i];
+    }
+}
+
+/* qlssq, mpqldec.f90:573-698, packed storage, one block */
+void mpref_ql_ssq_packed(const mpref_ql *q, double *A0, int32_t t)
+{
+    double *A = A0 - 1;
+    int32_t nconb = q->ncon, nparb = q->npar;
+    double *vecN = (double *)calloc((size_t)nparb + 1, sizeof(double));
+    double *Av = (double *)calloc((size_t)nparb + 1, sizeof(double));
+    for (int32_t j = 1; j <= nconb; j++) {
+        int32_t k = t ? nconb + 1 - j : j;
+        int32_t kn = nparb + k - nconb, ifirst = q->r1[k], ilast = q->r2[k], i, c;
+        const double *vr = q->V + (int64_t)(k - 1) * nparb;
+        double vk = q->Vk[k], vtAv;
+        for (c = 1; c <= nparb; c++) vecN[c] = 0.0;
+        for (c = ifirst; c <= ilast; c++) vecN[c] = vr[1 + c - ifirst];
+        vecN[kn] = vk;
+        for (c = 1; c <= nparb; c++) Av[c] = 0.0;
+        aprod_packed_range(nparb, A, vecN, ifirst, ilast, Av);
+        aprod_packed_range(nparb, A, vecN, kn, kn, Av);
+        vtAv = 0.0;
+        for (c = ifirst; c <= ilast; c++) vtAv = vtAv + vecN[c] * Av[c];
+        vtAv = vtAv + vecN[kn] * Av[kn];
+        for (i = 1; i <= kn; i++) {
+            int64_t ro = ((int64_t)i * i - i) / 2;
+            int32_t ilasti = ilast < i ? ilast : i;
+            double f = 2.0 * vecN[i] * vtAv - Av[i];
+            for (c = ifirst; c <= ilasti; c++) A[ro + c] = A[ro + c] + 2.0 * (f * vecN[c]);
+        }
+        for (i = ifirst; i <= ilast; i++) {
+            int64_t ro = ((int64_t)i * i - i) / 2;
+            for (c = 1; c <= i; c++) A[ro + c] = A[ro + c] - 2.0 * Av[c] * vecN[i];
+        }
+        {
+            int64_t ro = ((int64_t)kn * kn - kn) / 2;
+            A[ro + kn] = A[ro + kn] + 2.0 * ((2.0 * vk * vtAv - Av[kn]) * vk - Av[kn] * vk);
+        }
+        for (i = kn + 1; i <= nparb; i++) {
+            int64_t ro = ((int64_t)i * i - i) / 2;
+            for (c = ifirst; c <= ilast; c++) A[ro + c] = A[ro + c] - 2.0 * vecN[c] * Av[i];
+            A[ro + kn] = A[ro + kn] - 2.0 * vk * Av[i];
+        }
+    }
+    free(vecN);
+    free(Av);
+}
+
+/* avprd0, pede.f90:5069-5232 (nspc = 1, mextnd = 0) */
+void mpref_avprd0(int32_t matsto, int32_t n, const double *x0, double *b0, int32_t nG,
+                  const int32_t *allIndexGroups, const int64_t *offsets,
+                  const int32_t *columns, const double *matD)
+{
+    const double *x = x0 - 1, *A = matD - 1;
+    double *b = b0 - 1;
+    int32_t i, j;
+    if (matsto != 2) {
+        for (i = 1; i <= n; i++) {
+            int64_t ij = ((int64_t)i * i - i) / 2;
+            b[i] = A[ij + i] * x[i];
+            for (j = 1; j <= i - 1; j++) {
+                b[j] = b[j] + A[ij + j] * x[i];
+                b[i] = b[i] + A[ij + j] * x[j];
+            }
+        }
+        return;
+    }
+    const int32_t *npgrp = allIndexGroups - 1;
+    const int32_t *col = columns - 1;
+    for (int32_t ipg = 1; ipg <= nG; ipg++) {
+        int32_t ia = npgrp[ipg], ib = npgrp[ipg + 1] - 1, in = ib - ia + 1;
+        for (i = ia; i <= ib; i++) b[i] = A[i] * x[i];
+        int64_t kk = offsets[2 * (ipg - 1)], ll = offsets[2 * (ipg - 1) + 1];
+        int64_t ku = offsets[2 * ipg] - kk, indid = kk, indij = ll, k;
+        if (ku <= 0) continue;
+        if (col[indid + 1] != 0) {
+            for (i = ia; i <= ib; i++) {
+                for (k = 1; k <= ku; k++) {
+                    j = col[indid + k];
+                    b[j] = b[j] + A[indij + k] * x[i];
+                    b[i] = b[i] + A[indij + k] * x[j];
+                }
+                indij = indij + ku;
+            }
+        } else {
+            for (k = 2; k <= ku - 2; k += 2) {
+                int32_t jg = col[indid + k];
+                int32_t ja = npgrp[jg];
+                int32_t lj = col[indid + k - 1];
+                int32_t jn = col[indid + k + 1] - lj;
+                int32_t jb = ja + jn - 1, l;
+                lj = 1;
+                for (i = ia; i <= ib; i++) {
+                    double s = 0.0;
+                    for (l = 0; l < jn; l++) s = s + A[indij + lj + l] * x[ja + l];
+                    b[i] = b[i] + s;
+                    lj = lj + jn;
+                }
+                lj = 1;
+                for (j = ja; j <= jb; j++) {
+                    double s = 0.0;
+                    for (l = 0; l < in; l++) s = s + A[indij + lj + (int64_t)l * jn] * x[ia + l];
+                    b[j] = b[j] + s;
+                    lj = lj + 1;
+                }
+                indij = indij + (int64_t)in * jn;
+            }
+        }
+    }
+}
+
+/* reduced operator for MINRES: b = (Q^T A Q x)(1:nfit) (avprod) */
+typedef struct {
+    int32_t matsto, nVar, nG, nfit;
+    const int32_t *aig;
+    const int64_t *off;
+    const int32_t *col;
+    const double *matD;
+    const mpref_ql *q;
+    double *xa, *ba;
+} redop;
+
+static void avprod(const redop *o, const double *x, double *b)
+{
+    int32_t n = o->nfit, i;
+    for (i = 0; i < n; i++) o->xa[i] = x[i];
+    for (i = n; i < o->nVar; i++) o->xa[i] = 0.0;
+    if (o->q) mpref_ql_mlq(o->q, o->xa, 0);
+    mpref_avprd0(o->matsto, o->nVar, o->xa, o->ba, o->nG, o->aig, o->off, o->col, o->matD);
+    if (o->q) mpref_ql_mlq(o->q, o->ba, 1);
+    for (i = 0; i < n; i++) b[i] = o->ba[i];
+}
+
+/* diag(Q^T A Q) by explicit reflection tracking (see qlpssq,
+ * mpqldec.f90:711-950, band width 1) */
+static void reduced_diag(const redop *o, double *dg)
+{
+    int32_t nV = o->nVar, i;
+    for (i = 0; i < nV; i++) dg[i] = 0.0;
+    /* start from diag(A) */
+    for (i = 1; i <= nV; i++) {
+        if (o->matsto == 2) dg[i - 1] = o->matD[i - 1];
+        else dg[i - 1] = o->matD[((int64_t)i * i - i) / 2 + i - 1];
+    }
+    if (!o->q) return;
+    const mpref_ql *q = o->q;
+    int32_t m = q->ncon;
+    double *v = (double *)calloc((size_t)nV, sizeof(double));
+    double *y = (double *)calloc((size_t)nV, sizeof(double));
+    double *tmp = (double *)calloc((size_t)nV, sizeof(double));
+    /* transforms applied in the order k = m, m-1, ..., 1 (qlssq t=true) */
+    for (int32_t k = m; k >= 1; k--) {
+        int32_t kn = nV + k - m;
+        const double *vr = q->V + (int64_t)(k - 1) * nV;
+        for (i = 0; i < nV; i++) v[i] = 0.0;
+        for (i = q->r1[k]; i <= q->r2[k]; i++) v[i - 1] = vr[1 + i - q->r1[k]];
+        v[kn - 1] = q->Vk[k];
+        /* P v with P = H_m ... H_{k+1}: apply H_{k+1} first */
+        for (i = 0; i < nV; i++) tmp[i] = v[i];
+        for (int32_t kk = k + 1; kk <= m; kk++) {
+            int32_t knn = nV + kk - m;
+            const double *wr = q->V + (int64_t)(kk - 1) * nV;
+            double sp = 0.0;
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) sp += wr[1 + i - q->r1[kk]] * tmp[i - 1];
+            sp += q->Vk[kk] * tmp[knn - 1];
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) tmp[i - 1] -= 2.0 * wr[1 + i - q->r1[kk]] * sp;
+            tmp[knn - 1] -= 2.0 * q->Vk[kk] * sp;
+        }
+        mpref_avprd0(o->matsto, nV, tmp, y, o->nG, o->aig, o->off, o->col, o->matD);
+        for (int32_t kk = m; kk >= k + 1; kk--) {
+            int32_t knn = nV + kk - m;
+            const double *wr = q->V + (int64_t)(kk - 1) * nV;
+            double sp = 0.0;
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) sp += wr[1 + i - q->r1[kk]] * y[i - 1];
+            sp += q->Vk[kk] * y[knn - 1];
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) y[i - 1] -= 2.0 * wr[1 + i - q->r1[kk]] * sp;
+            y[knn - 1] -= 2.0 * q->Vk[kk] * sp;
+        }
+        double beta = 0.0;
+        for (i = 0; i < nV; i++) beta += v[i] * y[i];
+        for (i = 0; i < nV; i++) dg[i] = dg[i] - 4.0 * v[i] * y[i] + 4.0 * beta * v[i] * v[i];
+    }
+    free(v); free(y); free(tmp);
+}
+
+/* Preconditioned MINRES, Paige & Saunders (1975), SIAM J. Numer. Anal. 12,
+ * 617-629: Lanczos tridiagonalisation of the preconditioned operator,
+ * QR of the tridiagonal by Givens rotations, solution update along the
+ * rotated directions.  Stopping: relative residual rnorm/(Anorm*ynorm) <=
+ * rtol (istop 1), Arnorm/Anorm <= rtol (istop 2), itn >= itnlim (istop 6). */
+static int32_t minres(const redop *o, const double *pc, const double *b, double *x,
+                      double rtol, int32_t itnlim, int32_t *itnout)
+{
+    int32_t n = o->nfit, i, itn = 0, istop = 0;
+    double *r1 = calloc((size_t)n, sizeof(double)), *r2 = calloc((size_t)n, sizeof(double));
+    double *y = calloc((size_t)n, sizeof(double)), *v = calloc((size_t)n, sizeof(double));
+    double *w = calloc((size_t)n, sizeof(double)), *w1 = calloc((size_t)n, sizeof(double));
+    double *w2 = calloc((size_t)n, sizeof(double));
+    const double eps = DBL_EPSILON;
+    double beta1, beta, oldb, alfa, dbar = 0, epsln = 0, oldeps, delta, gbar, root;
+    double gamma, cs = -1, sn = 0, phi, phibar, denom, tnorm2 = 0, gmax = 0, gmin = DBL_MAX;
+    double Anorm = 0, ynorm, rnorm, test1, test2, Acond;
+    for (i = 0; i < n; i++) { x[i] = 0.0; r1[i] = b[i]; }
+    for (i = 0; i < n; i++) y[i] = (r1[i] * pc[i]) * pc[i];
+    beta1 = 0.0;
+    for (i = 0; i < n; i++) beta1 += r1[i] * y[i];
+    if (beta1 <= 0.0) { *itnout = 0; istop = beta1 < 0.0 ? 9 : 0; goto out; }
+    beta1 = sqrt(beta1);
+    beta = beta1;
+    oldb = 0.0;
+    phibar = beta1;
+    for (i = 0; i < n; i++) r2[i] = r1[i];
+    while (itn < itnlim) {
+        itn++;
+        double s = 1.0 / beta;
+        for (i = 0; i < n; i++) v[i] = s * y[i];
+        avprod(o, v, y);
+        if (itn >= 2)
+            for (i = 0; i < n; i++) y[i] = y[i] - (beta / oldb) * r1[i];
+        alfa = 0.0;
+        for (i = 0; i < n; i++) alfa += v[i] * y[i];
+        for (i = 0; i < n; i++) y[i] = y[i] - (alfa / beta) * r2[i];
+        for (i = 0; i < n; i++) { r1[i] = r2[i]; r2[i] = y[i]; }
+        for (i = 0; i < n; i++) y[i] = (r2[i] * pc[i]) * pc[i];
+        oldb = beta;
+        beta = 0.0;
+        for (i = 0; i < n; i++) beta += r2[i] * y[i];
+        if (beta < 0.0) { istop = 9; break; }
+        beta = sqrt(beta);
+        tnorm2 += alfa * alfa + oldb * oldb + beta * beta;
+        oldeps = epsln;
+        delta = cs * dbar + sn * alfa;
+        gbar = sn * dbar - cs * alfa;
+        epsln = sn * beta;
+        dbar = -cs * beta;
+        root = sqrt(gbar * gbar + dbar * dbar);
+        gamma = sqrt(gbar * gbar + beta * beta);
+        if (gamma < eps) gamma = eps;
+        cs = gbar / gamma;
+        sn = beta / gamma;
+        phi = cs * phibar;
+        phibar = sn * phibar;
+        denom = 1.0 / gamma;
+        for (i = 0; i < n; i++) {
+            w1[i] = w2[i];
+            w2[i] = w[i];
+            w[i] = (v[i] - oldeps * w1[i] - delta * w2[i]) * denom;
+            x[i] = x[i] + phi * w[i];
+        }
+        if (gamma > gmax) gmax = gamma;
+        if (gamma < gmin) gmin = gamma;
+        Anorm = sqrt(tnorm2);
+        ynorm = 0.0;
+        for (i = 0; i < n; i++) ynorm += x[i] * x[i];
+        ynorm = sqrt(ynorm);
+        rnorm = phibar;
+        test1 = rnorm / (Anorm * ynorm);
+        test2 = root / Anorm;
+        Acond = gmax / gmin;
+        if (itn >= itnlim) istop = 6;
+        if (Acond >= 0.1 / eps) istop = 4;
+        if (test2 <= rtol) istop = 2;
+        if (test1 <= rtol) istop = 1;
+        if (istop) break;
+    }
+    *itnout = itn;
+out:
+    free(r1); free(r2); free(y); free(v); free(w); free(w1); free(w2);
+    return istop;
+}
+
+int32_t mpref_minres_sparse(int32_t matsto, int32_t nVar, int32_t nG,
+                            const int32_t *allIndexGroups, const int64_t *offsets,
+                            const int32_t *columns, const double *matD,
+                            const mpref_ql *q, const double *rhs, double *x,
+                            double rtol, int32_t itnlim, int32_t *itn)
+{
+    redop o;
+    int32_t ncon = q ? q->ncon : 0, i;
+    o.matsto = matsto; o.nVar = nVar; o.nG = nG; o.nfit = nVar - ncon;
+    o.aig = allIndexGroups; o.off = offsets; o.col = columns; o.matD = matD; o.q = q;
+    o.xa = (double *)calloc((size_t)nVar, sizeof(double));
+    o.ba = (double *)calloc((size_t)nVar, sizeof(double));
+    double *dg = (double *)calloc((size_t)nVar, sizeof(double));
+    double *pc = (double *)calloc((size_t)nVar, sizeof(double));
+    reduced_diag(&o, dg);
+    /* precons/presols with no constraint blocks (mpnum.f90:2881-3060):
+     * cu = 1/sqrt(c); M^-1 y = (y*cu)*cu */
+    for (i = 0; i < o.nfit; i++) pc[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
+    int32_t istop = minres(&o, pc, rhs, x, rtol, itnlim, itn);
+    free(o.xa); free(o.ba); free(dg); free(pc);
+    return istop;
+}

@@ -1,0 +1,116 @@
+"""Global solves on the GPU (mpgpu_solve) against the oracle on the same
+matrix: inversion and decomposition with QL-eliminated constraints,
+sparse MINRES, the avprod product."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def build(mp, name, ntracks, matsto, seed=21):
+    d = mp.generate(mp.gen_config(name, ntracks=ntracks, seed=seed))
+    H = mp.HostStructure(d, mreqenf=5, sparse=(matsto == 2))
+    A = mp.constraint_matrix(d, H)
+    ctx = mp.Context()
+    ctx.set_layout(H, matsto)
+    ctx.set_constraints(A)
+    ctx.upload(H)
+    lb = ctx.loopbf(np.zeros(H.nTotal))
+    return d, H, A, ctx, lb
+
+
+def dense_from_packed(p, n):
+    M = np.zeros((n, n))
+    M[np.tril_indices(n)] = p
+    return M + np.tril(M, -1).T
+
+
+def kkt_solution(M, A, b):
+    n, m = M.shape[0], A.shape[0]
+    K = np.block([[M, A.T], [A, np.zeros((m, m))]])
+    return np.linalg.solve(K, np.concatenate([b, np.zeros(m)]))[:n]
+
+
+@pytest.mark.parametrize("metsol", [1, 3])
+def test_packed_solvers_vs_oracle(mp, orc, metsol):
+    d, H, A, ctx, lb = build(mp, "telescope", 5000, 1)
+    with ctx:
+        M = ctx.matrix()
+        corr, err, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), errors=(metsol == 1))
+    n = H.nVar
+    x = kkt_solution(dense_from_packed(M, n), A, lb["gvec"])
+    assert np.max(np.abs(corr - x)) <= 1e-9 * np.max(np.abs(x))
+    assert info.nrank == n - A.shape[0]
+    # oracle: same elimination and solver on the same matrix
+    L = orc.lib()
+    q = L.mpref_ql_create(n, A.shape[0], orc.ptr(np.ascontiguousarray(A), orc.f64p))
+    Mo = M.copy()
+    bo = lb["gvec"].copy()
+    L.mpref_ql_ssq_packed(C.c_void_p(q), orc.ptr(Mo, orc.f64p), C.c_int32(1))
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(bo, orc.f64p), C.c_int32(1))
+    nfit = n - A.shape[0]
+    nr = C.c_int32()
+    if metsol == 1:
+        L.mpref_sqminl(orc.ptr(Mo, orc.f64p), orc.ptr(bo, orc.f64p), C.c_int32(nfit), C.byref(nr))
+    else:
+        emax, emin = C.c_double(), C.c_double()
+        L.mpref_chdec2(orc.ptr(Mo, orc.f64p), C.c_int32(nfit), C.byref(nr), C.byref(emax), C.byref(emin))
+        L.mpref_chslv2(orc.ptr(Mo, orc.f64p), orc.ptr(bo, orc.f64p), C.c_int32(nfit))
+    bo[nfit:] = 0.0
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(bo, orc.f64p), C.c_int32(0))
+    assert nr.value == info.nrank
+    assert np.max(np.abs(corr - bo)) <= 1e-10 * np.max(np.abs(bo))
+    if metsol == 1:
+        # errors: oracle's literal back-transform of the same inverse
+        Mo2 = M.copy()
+        b2 = lb["gvec"].copy()
+        L.mpref_ql_ssq_packed(C.c_void_p(q), orc.ptr(Mo2, orc.f64p), C.c_int32(1))
+        L.mpref_sqminl(orc.ptr(Mo2, orc.f64p), orc.ptr(b2, orc.f64p), C.c_int32(nfit), C.byref(nr))
+        P = dense_from_packed(Mo2, n)
+        P[nfit:, :] = 0.0
+        P[:, nfit:] = 0.0
+        Mp = P[np.tril_indices(n)].copy()
+        L.mpref_ql_ssq_packed(C.c_void_p(q), orc.ptr(Mp, orc.f64p), C.c_int32(0))
+        diag = dense_from_packed(Mp, n).diagonal()
+        assert np.max(np.abs(err - diag) / np.abs(diag)) <= 1e-9
+    L.mpref_ql_destroy(C.c_void_p(q))
+
+
+def test_minres_sparse(mp, orc):
+    d, H, A, ctx, lb = build(mp, "barrel", 40000, 2)
+    with ctx:
+        M = ctx.matrix()
+        corr, _, info = ctx.solve(4, consResiduals=np.zeros(A.shape[0]), rtol=1e-12, itnlim=4000)
+        # avprod: Q^T A Q on a random reduced vector
+        nfit = H.nVar - A.shape[0]
+        xr = np.random.default_rng(1).normal(size=nfit)
+        bg = ctx.avprod(xr)
+    O = orc.Structure(d, mreqenf=5)
+    xo = np.zeros(H.nVar)
+    itn = C.c_int32()
+    L = orc.lib()
+    q = L.mpref_ql_create(H.nVar, A.shape[0], orc.ptr(np.ascontiguousarray(A), orc.f64p))
+    rhs = lb["gvec"].copy()
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(rhs, orc.f64p), C.c_int32(1))
+    istop = L.mpref_minres_sparse(C.c_int32(2), C.c_int32(H.nVar), C.c_int32(O.nG),
+                                  orc.ptr(O.aig, orc.i32p), orc.ptr(O.offsets, orc.i64p),
+                                  orc.ptr(O.columns, orc.i32p), orc.ptr(M, orc.f64p),
+                                  C.c_void_p(q), orc.ptr(rhs, orc.f64p), orc.ptr(xo, orc.f64p),
+                                  C.c_double(1e-12), C.c_int32(4000), C.byref(itn))
+    xo[nfit:] = 0.0
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xo, orc.f64p), C.c_int32(0))
+    assert info.istop in (1, 2) and istop in (1, 2)
+    assert abs(info.itn - itn.value) <= 2
+    assert np.max(np.abs(corr - xo)) <= 1e-9 * np.max(np.abs(xo))
+    # avprod against the oracle's avprd0 with explicit Q
+    xa = np.concatenate([xr, np.zeros(A.shape[0])])
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xa, orc.f64p), C.c_int32(0))
+    ba = np.zeros(H.nVar)
+    L.mpref_avprd0(C.c_int32(2), C.c_int32(H.nVar), orc.ptr(xa, orc.f64p), orc.ptr(ba, orc.f64p),
+                   C.c_int32(O.nG), orc.ptr(O.aig, orc.i32p), orc.ptr(O.offsets, orc.i64p),
+                   orc.ptr(O.columns, orc.i32p), orc.ptr(M, orc.f64p))
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(ba, orc.f64p), C.c_int32(1))
+    assert np.max(np.abs(bg - ba[:nfit])) <= 1e-12 * np.max(np.abs(ba))
+    L.mpref_ql_destroy(C.c_void_p(q))

@@ -1,0 +1,59 @@
+"""Host-side structure (label table, entries, parameter groups, mpbits
+sparse layout) against the oracle's literal restatement: bit-exact."""
+import numpy as np
+import pytest
+
+
+def _small(mp, name, ntracks, seed=7):
+    return mp.generate(mp.gen_config(name, ntracks=ntracks, seed=seed))
+
+
+@pytest.mark.parametrize("name,ntracks", [("telescope", 3000), ("barrel", 4000)])
+def test_structure_matches_oracle(mp, orc, name, ntracks):
+    d = _small(mp, name, ntracks)
+    H = mp.HostStructure(d, mreqenf=5)
+    O = orc.Structure(d, mreqenf=5)
+    assert H.nTotal == O.nTotal and H.nVar == O.nVar and H.nG == O.nG
+    np.testing.assert_array_equal(H.labels, O.labels)
+    np.testing.assert_array_equal(H.counter, O.counter)
+    np.testing.assert_array_equal(H.varIndex, O.varIndex)
+    np.testing.assert_array_equal(H.totGroup, O.totGroup)
+    np.testing.assert_array_equal(H.aig, O.aig)
+    np.testing.assert_array_equal(H.tinder, O.tinder)
+    np.testing.assert_array_equal(H.offsets, O.offsets)
+    np.testing.assert_array_equal(H.columns[:H.ncolw], O.columns[:O.ncolw])
+    assert H.nmatSparse == O.nmatSparse
+
+
+def test_groups_random_equations(mp, orc):
+    """Random equation structures: parameter groups and entries agree with the
+    literal pargrp restatement."""
+    rng = np.random.default_rng(11)
+    for trial in range(20):
+        nlab = int(rng.integers(5, 40))
+        recs_i, recs_d, ptrs = [], [], [0]
+        for r in range(int(rng.integers(3, 30))):
+            ii, dd = [0], [0.0]
+            for m in range(int(rng.integers(1, 5))):
+                ii += [0, 1]
+                dd += [rng.normal(), 1.0]
+                k = int(rng.integers(1, 6))
+                labs = sorted(set(int(x) for x in rng.integers(1, nlab + 1, k)))
+                ii += [0]
+                dd += [0.1]
+                for lab in labs:
+                    ii.append(lab * 3)
+                    dd.append(0.0 if rng.random() < 0.1 else float(rng.normal()))
+            recs_i += ii
+            recs_d += dd
+            ptrs.append(len(recs_i))
+        d = dict(recPtr=np.array(ptrs, np.int64), inder=np.array(recs_i, np.int32),
+                 glder=np.array(recs_d, np.float64))
+        H = mp.HostStructure(d, mreqenf=1, sparse=True)
+        O = orc.Structure(d, mreqenf=1, sparse=True)
+        np.testing.assert_array_equal(H.labels, O.labels)
+        np.testing.assert_array_equal(H.counter, O.counter)
+        np.testing.assert_array_equal(H.totGroup, O.totGroup)
+        np.testing.assert_array_equal(H.varIndex, O.varIndex)
+        np.testing.assert_array_equal(H.offsets, O.offsets)
+        np.testing.assert_array_equal(H.columns[:H.ncolw], O.columns[:O.ncolw])
