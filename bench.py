@@ -1,0 +1,321 @@
+"""Benchmark: global-matrix build throughput of the pede data loop.
+
+One step = one data loop (local fits of every record, rejection decisions,
+Schur-complement updates accumulated into the mpbits-sparse global matrix
+and the gradient) over the barrel workload: 12-layer barrel, 5000 modules x
+6 rigid-body parameters = 30000 global parameters, 2,000,000 linearised
+helix tracks with 5 local parameters and 12 two-dimensional hits (72 global
+parameters per record), 18 constraints.  Synthetic, seeded data of those
+sizes (there is no public dataset for it).
+
+value  : records/s with the records resident in HBM (device-timed loop)
+e2e    : records/s through the C-ABI from pinned host buffers: every step
+         uploads the records (mpgpu_upload_records) and runs mpgpu_loopbf
+         with the global parameters in and the gradient/counts out
+--impl reference: the CPU oracle (FP64 C restatement of loopbf + the
+         sparse update) on all host cores over a bounded record sample.
+
+Launch: python bench.py [--gpus N --steps K --warmup W]; for N > 1 through
+torchrun, each rank processing its own replica (weak scaling, no exchange).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+
+def _load_pkg():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "millepede_ii_gb300_mpgpu", os.path.join(ROOT, "millepede-ii_gb300", "mpgpu.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["millepede_ii_gb300_mpgpu"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def dist_setup(ngpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        try:
+            import torch
+            torch.cuda.set_device(local)
+        except Exception:
+            backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if sms:
+            out = {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                   "samples": len(sms)}
+        return out
+
+
+def flops_per_record(nmeas, nloc, ng, nalg):
+    """Algorithmic FP64 flops of one record's local fit and update."""
+    c_solve = nloc ** 3
+    return 2 * (nmeas * (nloc + nloc * (nloc + 1) // 2) + c_solve + nmeas * ng * (ng + 1) // 2
+                + nmeas * ng * nloc + nalg * nloc * nloc + nloc * nalg * (nalg + 1) // 2)
+
+
+def record_shape(d):
+    """(nmeas, nloc, ng, nalg) of the uniform barrel records."""
+    a, b = int(d["recPtr"][0]), int(d["recPtr"][1])
+    ii = d["inder"][a:b]
+    zeros = np.flatnonzero(ii == 0)
+    nmeas = (len(zeros) - 1) // 2
+    sl, sg = zeros[1], zeros[2]
+    nloc = int(ii[sl + 1:sg].max())
+    nxt = zeros[3] if len(zeros) > 3 else b - a
+    ng = int(nxt - sg - 1)
+    nalg = 6 * 12
+    return nmeas, nloc, ng, nalg
+
+
+def cpu_reference(d, nsample, nthreads, steps=1):
+    """CPU oracle (loopbf restatement, OpenMP) on the first nsample records."""
+    import oracle_ref as orc
+    rp = d["recPtr"][:nsample + 1]
+    sub = dict(recPtr=rp, inder=d["inder"][:rp[-1]], glder=d["glder"][:rp[-1]])
+    S = orc.Structure(sub, mreqenf=1)
+    gpar = np.zeros(S.nTotal)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o = S.loopbf(gpar, matsto=2, nthreads=nthreads)
+        times.append(time.perf_counter() - t0)
+        assert o["rc"] == 0
+    return nsample / statistics.median(times), times
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--ntracks", type=int, default=2_000_000)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=100_000)
+    ap.add_argument("--profile", action="store_true", help="small run for profilers (no e2e/cpu)")
+    ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
+    args = ap.parse_args()
+    rank, world, local, pg = dist_setup(args.gpus)
+    mp = _load_pkg()
+    cfg = mp.gen_config("barrel", ntracks=args.ntracks, seed=2 + 1000 * rank)
+    t0 = time.time()
+    d = mp.generate(cfg)
+    gen_s = time.time() - t0
+    nrec = len(d["recPtr"]) - 1
+    ncores = os.cpu_count() or 1
+    base_cfg = {"workload": "barrel 12 layers, 5000 modules x 6 dof = 30000 globals, "
+                            f"{args.ntracks} helix tracks x 12 2D hits (72 globals/record), "
+                            "5 local params, 18 constraints, mpbits sparse storage",
+                "records": nrec, "matsto": 2, "l2": "inputs (records, 7.5 GB) larger than L2",
+                "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        nsample = min(args.cpu_sample, nrec)
+        cpu_reference(d, min(nsample, 5000), ncores, steps=1)  # warm-up
+        val, times = cpu_reference(d, nsample, ncores, steps=args.steps)
+        line = {"metric": "records/s build", "value": val, "unit": "records/s", "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * statistics.median(times), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference", "config": dict(base_cfg, sample_records=nsample),
+                "cpu_baseline": {"value": val, "unit": "records/s", "cores": ncores,
+                                 "kind": "port",
+                                 "sample": f"first {nsample} records of the workload, one data "
+                                           "loop with sparse matrix build per step"},
+                "e2e": {"value": val, "unit": "records/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    S = mp.HostStructure(d, mreqenf=25)
+    A = mp.constraint_matrix(d, S)
+    L = mp.lib()
+    # pin the host record buffers (e2e uploads run from page-locked memory)
+    pinned = []
+    for key in ("recPtr", "inder", "glder"):
+        arr = d[key] if key != "inder" else S.tinder
+        if L.mpgpu_host_register(C.c_void_p(arr.ctypes.data), C.c_int64(arr.nbytes)) == 0:
+            pinned.append(arr)
+    ctx = mp.Context(device=local, staging_bytes=args.staging_mb << 20)
+    ctx.set_layout(S, 2)
+    ctx.set_constraints(A)
+    t0 = time.time()
+    ctx.upload(S)
+    upload_s = time.time() - t0
+    gpar = np.zeros(S.nTotal)
+    for _ in range(args.warmup):
+        ctx.loopbf(gpar)
+    clocks = ClockSampler(local)
+    barrier(pg)
+    clocks.start()
+    t0 = time.perf_counter()
+    ms_loop, ms_fit, ms_acc, launches = [], [], [], 0
+    for _ in range(args.steps):
+        r = ctx.loopbf(gpar)
+        ms_loop.append(r["msLoop"])
+        ms_fit.append(r["msFit"])
+        ms_acc.append(r["msAccum"])
+        launches += r["launches"]
+    wall = time.perf_counter() - t0
+    barrier(pg)
+    clk = clocks.stop()
+    dev_s = sum(ms_loop) * 1e-3
+    dev_s_max = max_over_ranks(pg, dev_s)
+    total_rec = sum_over_ranks(pg, float(nrec * args.steps))
+    value = total_rec / dev_s_max
+    ms_per_step = 1e3 * dev_s_max / args.steps
+    nmeas, nloc, ng, nalg = record_shape(d)
+    fpr = flops_per_record(nmeas, nloc, ng, nalg)
+    fp64 = C.c_double()
+    L.mpgpu_probe_fp64(C.c_int32(local), C.byref(fp64))
+    fit_ms = statistics.median(ms_fit)
+    achieved = fpr * nrec / (fit_ms * 1e-3) / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    # accumulation kernel: staging read + block-row read/write of the matrix
+    ngg = nalg * (nalg + 1) // 2
+    acc_bytes = 8.0 * ngg * nrec + 16.0 * ctx.nmat
+    acc_ms = statistics.median(ms_acc)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    roof = {"bound": "fp64", "kernel": "k_fit (local fit + Schur update)",
+            "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
+            "frac": achieved / fp64.value if fp64.value else None, "traffic": None,
+            "flops_per_record": fpr,
+            "peak_source": "FP64 FMA throughput measured in this run (mpgpu_probe_fp64)",
+            "accumulate": {"bound": "hbm", "achieved": acc_bytes / (acc_ms * 1e-3) / 1e9,
+                           "peak": hbm_peak, "unit": "GB/s",
+                           "frac": acc_bytes / (acc_ms * 1e-3) / 1e9 / hbm_peak,
+                           "bytes_per_loop": acc_bytes,
+                           "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback"}}
+    line = {"metric": "records/s build", "value": value, "unit": "records/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": base_cfg, "roofline": roof, "clocks": clk,
+            "gpu_launches": launches,
+            "detail": {"ms_fit": fit_ms, "ms_accumulate": acc_ms, "wall_s": wall,
+                       "nmat": ctx.nmat, "generate_s": gen_s, "upload_s": upload_s}}
+    if not args.profile:
+        # end to end through the C-ABI from pinned host buffers
+        bi = S.tinder.nbytes + d["glder"].nbytes + d["recPtr"].nbytes + 8 * S.nTotal
+        bo = 16 * S.nVar + 256
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ctx.upload(S)
+            ctx.loopbf(gpar)
+        e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+        line["e2e"] = {"value": total_rec / args.steps * args.e2e_steps / e2e_s,
+                       "unit": "records/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
+                       "steps": args.e2e_steps}
+        if rank == 0:
+            nsample = min(args.cpu_sample, nrec)
+            val, times = cpu_reference(d, nsample, ncores, steps=1)
+            line["cpu_baseline"] = {"value": val, "unit": "records/s", "cores": ncores,
+                                    "kind": "port",
+                                    "sample": f"first {nsample} records, one sparse data loop"}
+    ctx.close()
+    for arr in pinned:
+        L.mpgpu_host_unregister(C.c_void_p(arr.ctypes.data))
+    if rank == 0:
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

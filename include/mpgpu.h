@@ -113,6 +113,11 @@ typedef struct mpgpu_fitstats {
     int32_t nbndr[2];   /* records solved as bordered band (left / right) */
     int32_t nbdrx, nbndx;
     int64_t naccepted;
+    double msFit;       /* device time of the local-fit kernels (CUDA events) */
+    double msAccum;     /* device time of the accumulation kernels */
+    double msLoop;      /* device time of the whole data loop */
+    int32_t launches;   /* kernels launched by the loop */
+    int32_t pad;
 } mpgpu_fitstats;
 
 /* One data loop (loopbf): local fits of all records with the given global
@@ -162,6 +167,15 @@ typedef struct mpgpu_solveinfo {
 int32_t mpgpu_solve(mpgpu_ctx *ctx, int32_t metsol, const double *consResiduals,
                     double rtol, int32_t itnlim, double *correction, double *errors,
                     mpgpu_solveinfo *info);
+
+/* Page-lock (register) / release a caller-owned host buffer so that the
+ * uploads from it run at full host-device bandwidth. */
+int32_t mpgpu_host_register(void *ptr, int64_t bytes);
+int32_t mpgpu_host_unregister(void *ptr);
+
+/* Measured FP64 fused-multiply-add throughput of the device (TFLOP/s),
+ * used as the roofline denominator of the FP64-bound local-fit kernel. */
+int32_t mpgpu_probe_fp64(int32_t device, double *tflops);
 
 /* b = Q^T A Q x restricted to the first n = nVar - ncon components
  * (avprod), x and b host arrays of length n. */

@@ -43,6 +43,44 @@ int32_t find_label(const std::vector<int32_t> &lab, int32_t item) {
     return (int32_t)(it - lab.begin());
 }
 
+// label -> 0-based total index: direct table for compact label ranges,
+// binary search otherwise
+struct LabelMap {
+    const std::vector<int32_t> &lab;
+    std::vector<int32_t> direct;
+    int32_t lo = 0;
+    explicit LabelMap(const std::vector<int32_t> &l) : lab(l) {
+        if (lab.empty()) return;
+        const int64_t span = (int64_t)lab.back() - lab.front() + 1;
+        if (span <= (int64_t)64 << 20) {
+            lo = lab.front();
+            direct.assign((size_t)span, -1);
+            for (size_t i = 0; i < lab.size(); ++i) direct[(size_t)(lab[i] - lo)] = (int32_t)i;
+        }
+    }
+    int32_t find(int32_t item) const {
+        if (!direct.empty()) {
+            const int64_t k = (int64_t)item - lo;
+            return (k < 0 || k >= (int64_t)direct.size()) ? -1 : direct[(size_t)k];
+        }
+        return find_label(lab, item);
+    }
+};
+
+int host_threads(int64_t nwork) {
+    int n = (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+    if (nwork < 20000) n = 1;
+    return n;
+}
+
+template <class F>
+void run_threads(int nt, F f) {
+    if (nt <= 1) { f(0); return; }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) th.emplace_back([&f, t] { f(t); });
+    for (auto &x : th) x.join();
+}
+
 }  // namespace
 
 // loop1: labels (ascending order defines the total index), entries per
@@ -59,48 +97,84 @@ extern "C" int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const 
                                      int32_t mreqenf, int32_t cap, int32_t *labels,
                                      int64_t *counter, int32_t *varIndex, int32_t *totGroup,
                                      int32_t *nVar, int32_t *nVarGroups) {
+    const int nt = host_threads(nrec);
+    // distinct labels: per-thread sort/unique of the record labels, merged
+    std::vector<std::vector<int32_t>> part(nt);
+    std::vector<int> bad(nt, 0);
+    run_threads(nt, [&](int t) {
+        std::vector<int32_t> &v = part[t];
+        int32_t last = 0;
+        for (int64_t r = nrec * t / nt; r < nrec * (t + 1) / nt; ++r) {
+            bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
+                                           [&](int64_t, int64_t sg, int64_t lg) {
+                                               for (int64_t w = sg + 1; w <= lg; ++w)
+                                                   if (inder[w] > 0 && inder[w] != last) {
+                                                       v.push_back(inder[w]);
+                                                       last = inder[w];
+                                                   }
+                                           });
+            if (!ok) { bad[t] = 1; return; }
+            if (v.size() > (1u << 22)) {
+                std::sort(v.begin(), v.end());
+                v.erase(std::unique(v.begin(), v.end()), v.end());
+            }
+        }
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+    });
+    for (int t = 0; t < nt; ++t)
+        if (bad[t]) return -20;
     std::vector<int32_t> all;
-    all.reserve((size_t)(recPtr[nrec] - recPtr[0]) / 2 + nsteer);
     for (int32_t i = 0; i < nsteer; ++i)
         if (steerLabels[i] > 0) all.push_back(steerLabels[i]);
-    for (int64_t r = 0; r < nrec; ++r) {
-        bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
-                                       [&](int64_t, int64_t sg, int64_t lg) {
-                                           for (int64_t w = sg + 1; w <= lg; ++w)
-                                               if (inder[w] > 0) all.push_back(inder[w]);
-                                       });
-        if (!ok) return -20;
-    }
+    for (auto &v : part) all.insert(all.end(), v.begin(), v.end());
     std::sort(all.begin(), all.end());
     all.erase(std::unique(all.begin(), all.end()), all.end());
     const int32_t n = (int32_t)all.size();
     if (n > cap) return -1;
-    // cut[i] (0-based): a group boundary between index i and i+1
+    LabelMap lmap(all);
+    // entries and group cuts per equation (non-zero derivatives), per thread
+    // partial arrays merged at the end: cut[i] = boundary between i and i+1
+    std::vector<std::vector<uint8_t>> cutP(nt), seenP(nt);
+    std::vector<std::vector<int64_t>> cntP(nt);
+    run_threads(nt, [&](int t) {
+        std::vector<uint8_t> &cut = cutP[t], &seen = seenP[t];
+        std::vector<int64_t> &cnt = cntP[t];
+        cut.assign(n + 1, 0);
+        seen.assign(n, 0);
+        cnt.assign(n, 0);
+        std::vector<int32_t> list;
+        for (int64_t r = nrec * t / nt; r < nrec * (t + 1) / nt; ++r) {
+            for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
+                list.clear();
+                for (int64_t w = sg + 1; w <= lg; ++w) {
+                    if (glder[w] == 0.0) continue;
+                    list.push_back(lmap.find(inder[w]));
+                }
+                if (list.empty()) return;
+                std::sort(list.begin(), list.end());
+                for (int32_t x : list) { cnt[x]++; seen[x] = 1; }
+                if (list.front() > 0) cut[list.front() - 1] = 1;
+                for (size_t q = 0; q + 1 < list.size(); ++q)
+                    if (list[q + 1] != list[q] + 1) {
+                        cut[list[q]] = 1;
+                        if (list[q + 1] > 0) cut[list[q + 1] - 1] = 1;
+                    }
+                cut[list.back()] = 1;
+            });
+        }
+    });
     std::vector<uint8_t> cut(n + 1, 0), seen(n, 0);
     std::vector<int64_t> cnt(n, 0);
-    std::vector<int32_t> list;
-    for (int64_t r = 0; r < nrec; ++r) {
-        for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
-            list.clear();
-            for (int64_t w = sg + 1; w <= lg; ++w) {
-                if (glder[w] == 0.0) continue;
-                list.push_back(find_label(all, inder[w]));
-            }
-            if (list.empty()) return;
-            std::sort(list.begin(), list.end());
-            for (int32_t x : list) { cnt[x]++; seen[x] = 1; }
-            if (list.front() > 0) cut[list.front() - 1] = 1;
-            for (size_t q = 0; q + 1 < list.size(); ++q)
-                if (list[q + 1] != list[q] + 1) {
-                    cut[list[q]] = 1;
-                    if (list[q + 1] > 0) cut[list[q + 1] - 1] = 1;
-                }
-            cut[list.back()] = 1;
-        });
-    }
+    for (int t = 0; t < nt; ++t)
+        for (int32_t i = 0; i < n; ++i) {
+            cut[i] |= cutP[t][i];
+            seen[i] |= seenP[t][i];
+            cnt[i] += cntP[t][i];
+        }
     std::vector<double> ps(n, 0.0);
     for (int32_t i = 0; i < npre; ++i) {
-        int32_t li = find_label(all, preLabel[i]);
+        int32_t li = lmap.find(preLabel[i]);
         if (li >= 0) ps[li] = preSigma[i];
     }
     int32_t nv = 0, ntg = 0;
@@ -130,15 +204,24 @@ extern "C" int32_t mpgpu_host_translate(int64_t nrec, const int64_t *recPtr, con
                                         const double *glder, int32_t nTotal, const int32_t *labels,
                                         int32_t *outInder) {
     std::vector<int32_t> lab(labels, labels + nTotal);
-    std::memcpy(outInder + recPtr[0], inder + recPtr[0], sizeof(int32_t) * (size_t)(recPtr[nrec] - recPtr[0]));
-    for (int64_t r = 0; r < nrec; ++r) {
-        bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
-                                       [&](int64_t, int64_t sg, int64_t lg) {
-                                           for (int64_t w = sg + 1; w <= lg; ++w)
-                                               outInder[w] = find_label(lab, inder[w]) + 1;
-                                       });
-        if (!ok) return 20;
-    }
+    LabelMap lmap(lab);
+    const int nt = host_threads(nrec);
+    std::vector<int> bad(nt, 0);
+    run_threads(nt, [&](int t) {
+        const int64_t a = nrec * t / nt, b = nrec * (t + 1) / nt;
+        if (b <= a) return;
+        std::memcpy(outInder + recPtr[a], inder + recPtr[a], sizeof(int32_t) * (size_t)(recPtr[b] - recPtr[a]));
+        for (int64_t r = a; r < b; ++r) {
+            bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
+                                           [&](int64_t, int64_t sg, int64_t lg) {
+                                               for (int64_t w = sg + 1; w <= lg; ++w)
+                                                   outInder[w] = lmap.find(inder[w]) + 1;
+                                           });
+            if (!ok) { bad[t] = 1; return; }
+        }
+    });
+    for (int t = 0; t < nt; ++t)
+        if (bad[t]) return 20;
     return 0;
 }
 

@@ -555,14 +555,21 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     ap.aig = j.aig; ap.off = j.off; ap.col = j.col; ap.nG = j.nG; ap.matsto = j.matsto;
     ap.icalcm = opt->icalcm; ap.matD = j.matD; ap.gvec = j.gvec; ap.gcnt = j.gcnt; ap.errFlag = errFlag;
     const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
+    // events bracket every kernel of the loop: fit and accumulation times
+    std::vector<cudaEvent_t> ev(2 * nchunk + 3);
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], s);
+    int32_t launches = 0;
     for (int64_t ch = 0; ch < nchunk; ++ch) {
         fp.r0 = j.chunkRec[ch];
         fp.r1 = j.chunkRec[ch + 1];
-        if (fp.r1 <= fp.r0) continue;
-        MPG_CUDA(c, launch_fit(fp, nsm, s));
+        cudaEventRecord(ev[1 + 2 * ch], s);
+        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, s)); launches++; }
+        cudaEventRecord(ev[2 + 2 * ch], s);
         ap.eStart = j.eStart + ch * (j.nG + 1);
-        MPG_CUDA(c, launch_accumulate(ap, nsm, s));
+        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_accumulate(ap, nsm, s)); launches++; }
     }
+    cudaEventRecord(ev[2 * nchunk + 1], s);
     // statistics
     const int32_t nf = j.nfiles;
     int64_t *iout = (int64_t *)(c->scal + 8);
@@ -574,8 +581,21 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     StatParams sp{j.status, j.chi2add, j.ndfadd, j.chndf, j.rec, j.fileWeight, j.nrec, nf,
                   dout, iout, fout};
     MPG_CUDA(c, launch_stats(sp, s));
+    launches += 2;
+    cudaEventRecord(ev[2 * nchunk + 2], s);
     MPG_CUDA(c, cudaMemcpyAsync(c->hscal, c->scal, 4096, cudaMemcpyDeviceToHost, s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
+    double msFit = 0.0, msAcc = 0.0;
+    float t = 0.0f;
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        cudaEventElapsedTime(&t, ev[1 + 2 * ch], ev[2 + 2 * ch]);
+        msFit += t;
+        cudaEventElapsedTime(&t, ev[2 + 2 * ch], ch + 1 < nchunk ? ev[3 + 2 * ch] : ev[2 * nchunk + 1]);
+        msAcc += t;
+    }
+    cudaEventElapsedTime(&t, ev[0], ev[2 * nchunk + 2]);
+    const double msLoop = t;
+    for (auto &e : ev) cudaEventDestroy(e);
     const int32_t *hflag = (const int32_t *)c->hscal;
     if (hflag[0]) return set_err(c, hflag[0], "device index error in the data loop");
     const int64_t *hi = (const int64_t *)(c->hscal + 8);
@@ -593,6 +613,10 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
             stats->nbdrx = j.nbdrx; stats->nbndx = j.nbndx;
         }
         stats->naccepted = hi[8];
+        stats->msFit = msFit;
+        stats->msAccum = msAcc;
+        stats->msLoop = msLoop;
+        stats->launches = launches;
     }
     c->lastNaccepted = hi[8];
     for (int32_t f = 0; f < nf; ++f) {
@@ -722,4 +746,59 @@ extern "C" int32_t mpgpu_avprod(mpgpu_ctx *c, int32_t n, const double *x, double
     if (n != c->j.nVar - c->j.ncon) return set_err(c, MPGPU_ERR_SIZE, "avprod: vector/matrix size mismatch");
     cudaSetDevice(c->device);
     return avprod_host(c, n, x, b);
+}
+
+// ------------------------------------------------------------------ FP64 peak
+namespace {
+// independent fused multiply-add chains (8 per thread) keep the FP64 pipe busy
+__global__ void k_dfma_chain(double *out, int iters, double a, double b) {
+    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1e-3, x2 = x0 + 2e-3, x3 = x0 + 3e-3;
+    double x4 = x0 + 4e-3, x5 = x0 + 5e-3, x6 = x0 + 6e-3, x7 = x0 + 7e-3;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    const double s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+}  // namespace
+
+extern "C" int32_t mpgpu_probe_fp64(int32_t device, double *tflops) {
+    if (!tflops) return MPGPU_ERR_ARG;
+    *tflops = 0.0;
+    if (cudaSetDevice(device) != cudaSuccess) return MPGPU_ERR_CUDA;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    double *d = nullptr;
+    if (cudaMalloc(&d, 8) != cudaSuccess) return MPGPU_ERR_ALLOC;
+    const int iters = 4096, threads = 256, blocks = nsm * 8;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0);
+        k_dfma_chain<<<blocks, threads>>>(d, iters, 0.999999, 1e-7);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+        if (rep > 0 && ms > 0.0f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    *tflops = best;
+    return cudaGetLastError() == cudaSuccess ? MPGPU_OK : MPGPU_ERR_CUDA;
+}
+
+extern "C" int32_t mpgpu_host_register(void *ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return MPGPU_ERR_ARG;
+    return cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault) == cudaSuccess ? MPGPU_OK : MPGPU_ERR_CUDA;
+}
+
+extern "C" int32_t mpgpu_host_unregister(void *ptr) {
+    if (!ptr) return MPGPU_ERR_ARG;
+    return cudaHostUnregister(ptr) == cudaSuccess ? MPGPU_OK : MPGPU_ERR_CUDA;
 }

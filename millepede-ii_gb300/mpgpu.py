@@ -32,7 +32,9 @@ class FitOpts(C.Structure):
 class FitStats(C.Structure):
     _fields_ = [("nrej", C.c_int64 * 6), ("chi2SumI", C.c_int64), ("chi2SumD", C.c_double),
                 ("ndfSum", C.c_int64), ("ndfSumW", C.c_double), ("nbndr", C.c_int32 * 2),
-                ("nbdrx", C.c_int32), ("nbndx", C.c_int32), ("naccepted", C.c_int64)]
+                ("nbdrx", C.c_int32), ("nbndx", C.c_int32), ("naccepted", C.c_int64),
+                ("msFit", C.c_double), ("msAccum", C.c_double), ("msLoop", C.c_double),
+                ("launches", C.c_int32), ("pad", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -107,7 +109,9 @@ EXPORTS = [
     "mpgpu_create", "mpgpu_destroy", "mpgpu_last_error", "mpgpu_set_layout",
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
     "mpgpu_mupdat", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
-    "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_host_labels",
+    "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
+    "mpgpu_host_register", "mpgpu_host_unregister",
+    "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
 ]
@@ -328,7 +332,8 @@ class Context:
                                        ptr(chi2f, f32p), ptr(ndff, i32p)))
         return dict(gvec=gvec, gcnt=gcnt, nrej=list(st.nrej), chi2=st.chi2SumD + st.chi2SumI,
                     ndf=st.ndfSum, naccepted=st.naccepted, nbndr=list(st.nbndr),
-                    nbdrx=st.nbdrx, nbndx=st.nbndx, naccf=naccf, chi2f=chi2f, ndff=ndff)
+                    nbdrx=st.nbdrx, nbndx=st.nbndx, naccf=naccf, chi2f=chi2f, ndff=ndff,
+                    msFit=st.msFit, msAccum=st.msAccum, msLoop=st.msLoop, launches=st.launches)
 
     def matrix(self):
         m = np.zeros(self.nmat, np.float64)
