@@ -1,12 +1,12 @@
 // mpgpu_accum.cu -- deterministic accumulation of the per-record updates
 // into the global matrix and vector, the per-loop statistics and mupdat.
 //
-// Owner computes: one warp owns one parameter group (a block row of the
-// lower-triangular global matrix and the matching slice of the vector) and
-// walks the records that contain the group in record order.  No two warps
-// write the same element and every element receives its contributions in
-// record order, so the result does not depend on scheduling and no atomics
-// are used on floating-point data.  This replaces the write cache and the
+// Owner computes: the contributions to one parameter group's block row of
+// the lower-triangular global matrix (and its slice of the vector) are
+// summed by fixed work items in record order, then the items of a row are
+// combined in item order.  Every element therefore receives its sum in the
+// same order on every run, independent of scheduling, and no atomics are
+// used on floating-point data.  This replaces the write cache and the
 // row-owner flush of loopbf/mgupdt (pede.f90:4280-4421, 3219-3357).
 #include <cuda_runtime.h>
 
@@ -60,57 +60,68 @@ __device__ int64_t d_ijpgrp(int32_t itema, int32_t itemb, int32_t nG, const int3
 
 namespace {
 
-// Warp per parameter group I.  Entries (record, group position a) of this
-// chunk in record order; for an accepted record the rows of group a of its
-// packed update matrix (one contiguous segment) are subtracted from the
-// block row of I, and its vector slice is added.
-__global__ void __launch_bounds__(256) k_accumulate(AccParams p) {
-    const int ln = threadIdx.x & 31;
-    const int64_t wg = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    __shared__ int64_t s_ij[8][MPG_NGRP_MAX + 1];
-    __shared__ int32_t s_lr[8][MPG_NGRP_MAX + 1];
-    __shared__ int32_t s_off[8][MPG_NGRP_MAX + 2];
-    __shared__ int32_t s_gf[8][MPG_NGRP_MAX + 1];
-    const int wib = threadIdx.x >> 5;
-    for (int64_t I = 1 + wg; I <= p.nG; I += nwarp) {
-        const int32_t ia = p.aig[I - 1];           // first variable index (1-based)
-        const int32_t np = p.aig[I] - ia;
-        const int64_t e0 = p.eStart[I - 1], e1 = p.eStart[I];
-        for (int64_t e = e0; e < e1; ++e) {
+// Work item = (row group I, a record-ordered range of the records that
+// contain I).  One warp sums, in record order, the rows of group I of every
+// accepted record's update into a private partial block row (dense row
+// layout of I: the stored column blocks side by side) and the vector slice.
+// Hot row groups (modules crossed by many tracks) are split into several
+// items, so the work is balanced over the GPU; k_acc_reduce then adds the
+// partials of a row group in item order.  Fixed item boundaries make the
+// result independent of scheduling.
+constexpr int kAccWarps = 8;
+constexpr int kAccSmem = 768;    // doubles of shared-memory partial per warp
+
+__global__ void __launch_bounds__(32 * kAccWarps) k_acc_items(AccParams p) {
+    extern __shared__ __align__(16) double sacc[];
+    __shared__ int32_t s_off[kAccWarps][MPG_NGRP_MAX + 2];
+    __shared__ int32_t s_col[kAccWarps][MPG_NGRP_MAX + 1];
+    const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t w = (int64_t)blockIdx.x * kAccWarps + wib;
+    const int64_t nw = (int64_t)gridDim.x * kAccWarps;
+    double *mine = sacc + (int64_t)wib * kAccSmem;
+    for (int64_t it = p.item0 + w; it < p.item0 + p.nitem; it += nw) {
+        const int32_t I = p.itRow[it];
+        const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
+        const int32_t width = p.rowWidth[I - 1];
+        const int64_t psz = (int64_t)np * width, total = psz + 2 * np;
+        double *P = total <= kAccSmem ? mine : p.partial + p.itPOff[it];
+        for (int64_t q = ln; q < total; q += 32) P[q] = 0.0;
+        __syncwarp();
+        const int64_t kb0 = p.matsto == 2 ? p.rowBlk0[I - 1] : 0;
+        const int64_t kb1 = p.matsto == 2 ? p.rowBlk0[I] : 0;
+        for (int64_t e = p.itE0[it]; e < p.itE1[it]; ++e) {
             const int64_t ent = p.entries[e];
             const int64_t r = ent >> 8;
             const int a = (int)(ent & 0xff);
             if (p.status[r] != 0) continue;
-            const RecInfo ri = p.rec[r];
-            // block locations of (I, J_b) for the record's groups b <= a
+            const int64_t updOff = p.rec[r].updOff, grpOff = p.rec[r].grpOff;
+            const int64_t slotOff = p.rec[r].slotOff;
             for (int b = ln; b <= a; b += 32) {
-                const int32_t J = p.grpId[ri.grpOff + b];
-                s_off[wib][b] = p.grpSlot[ri.grpOff + b];
-                s_gf[wib][b] = p.aig[J - 1];
-                if (p.matsto == 2 && p.icalcm == 1) {
-                    int32_t lr = 0;
-                    int64_t ij = (J == I) ? -1 : d_ijpgrp((int32_t)I, J, p.nG, p.aig, p.off, p.col, &lr);
-                    if (J == I) {  // diagonal block: strictly-lower part stored like others
-                        ij = d_ijpgrp((int32_t)I, (int32_t)I, p.nG, p.aig, p.off, p.col, &lr);
+                const int32_t J = p.grpId[grpOff + b];
+                s_off[wib][b] = p.grpSlot[grpOff + b];
+                int32_t col = -1;
+                if (p.matsto == 2) {
+                    int64_t lo = kb0, hi = kb1 - 1;
+                    while (lo <= hi) {
+                        const int64_t mid = (lo + hi) >> 1;
+                        const int32_t jm = p.blkJ[mid];
+                        if (jm == J) { col = p.blkCol[mid]; break; }
+                        if (jm < J) lo = mid + 1; else hi = mid - 1;
                     }
-                    s_ij[wib][b] = ij;
-                    s_lr[wib][b] = lr;
+                    if (col < 0) *p.errFlag = 23;
+                } else {
+                    col = p.aig[J - 1] - 1;
                 }
+                s_col[wib][b] = col < 0 ? 0 : col;
             }
+            __syncwarp();
             if (ln == 0) s_off[wib][a + 1] = s_off[wib][a] + np;
             __syncwarp();
             const int32_t offa = s_off[wib][a];
-            // vector slice and counts
-            for (int ii = ln; ii < np; ii += 32) {
-                p.gvec[ia - 1 + ii] += p.vstage[ri.slotOff + offa + ii];
-                p.gcnt[ia - 1 + ii] += p.slotCnt[ri.slotOff + offa + ii];
-            }
             if (p.icalcm == 1) {
-                // segment: packed rows offa .. offa+np-1, columns 0 .. row
                 const int64_t s0 = (int64_t)offa * (offa + 1) / 2;
                 const int64_t s1 = (int64_t)(offa + np) * (offa + np + 1) / 2;
-                const double *U = p.stage + ri.updOff;
+                const double *U = p.stage + updOff;
                 int ra = offa, cb = ln;
                 while (cb > ra) { cb -= ra + 1; ra++; }
                 int b = 0;
@@ -118,24 +129,73 @@ __global__ void __launch_bounds__(256) k_accumulate(AccParams p) {
                     while (cb >= s_off[wib][b + 1]) b++;
                     while (cb < s_off[wib][b]) b--;
                     const int ii = ra - offa, jj = cb - s_off[wib][b];
-                    const double u = U[idx];
-                    if (p.matsto == 2) {
-                        if (b == a && jj == ii) {
-                            p.matD[ia - 1 + ii] -= u;
-                        } else {
-                            const int64_t t = s_ij[wib][b] + jj + (int64_t)ii * s_lr[wib][b] - 1;
-                            if (s_ij[wib][b] <= 0) { *p.errFlag = 23; }
-                            else p.matD[t] -= u;
-                        }
-                    } else {
-                        const int64_t gi = ia + ii, gj = s_gf[wib][b] + jj;
-                        p.matD[(gi * gi - gi) / 2 + gj - 1] -= u;
-                    }
+                    P[(int64_t)ii * width + s_col[wib][b] + jj] += U[idx];
                     cb += 32;
                     while (cb > ra) { cb -= ra + 1; ra++; }
                 }
             }
+            for (int ii = ln; ii < np; ii += 32) {
+                P[psz + ii] += p.vstage[slotOff + offa + ii];
+                P[psz + np + ii] += (double)p.slotCnt[slotOff + offa + ii];
+            }
             __syncwarp();
+        }
+        if (total <= kAccSmem) {
+            double *G = p.partial + p.itPOff[it];
+            for (int64_t q = ln; q < total; q += 32) G[q] = P[q];
+        }
+        __syncwarp();
+    }
+}
+
+// Warp per row group: partials of its items in item (= record) order,
+// subtracted from the block row of the global matrix; vector and counts.
+__global__ void __launch_bounds__(256) k_acc_reduce(AccParams p) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t I = 1 + w; I <= p.nG; I += nw) {
+        const int64_t i0 = p.rowItem0[I - 1], i1 = p.rowItem0[I];
+        if (i1 <= i0) continue;
+        const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
+        const int32_t width = p.rowWidth[I - 1];
+        const int64_t psz = (int64_t)np * width;
+        if (p.icalcm == 1) {
+            if (p.matsto == 2) {
+                for (int64_t k = p.rowBlk0[I - 1]; k < p.rowBlk0[I]; ++k) {
+                    const int32_t J = p.blkJ[k];
+                    const int32_t nj = p.aig[J] - p.aig[J - 1];
+                    const int64_t boff = p.blkOff[k];
+                    const int32_t ld = p.blkLd[k], col0 = p.blkCol[k];
+                    for (int q = ln; q < np * nj; q += 32) {
+                        const int ii = q / nj, jj = q - ii * nj;
+                        if (J == I && jj > ii) continue;
+                        double sum = 0.0;
+                        for (int64_t it = i0; it < i1; ++it)
+                            sum += p.partial[p.itPOff[it] + (int64_t)ii * width + col0 + jj];
+                        if (J == I && jj == ii) p.matD[ia + ii] -= sum;
+                        else p.matD[boff + (int64_t)ii * ld + jj] -= sum;
+                    }
+                }
+            } else {
+                for (int64_t q = ln; q < psz; q += 32) {
+                    const int64_t ii = q / width, col = q - ii * width;
+                    const int64_t gi = ia + ii + 1, gj = col + 1;
+                    if (gj > gi) continue;
+                    double sum = 0.0;
+                    for (int64_t it = i0; it < i1; ++it) sum += p.partial[p.itPOff[it] + q];
+                    p.matD[(gi * gi - gi) / 2 + gj - 1] -= sum;
+                }
+            }
+        }
+        for (int ii = ln; ii < np; ii += 32) {
+            double v = 0.0, cn = 0.0;
+            for (int64_t it = i0; it < i1; ++it) {
+                v += p.partial[p.itPOff[it] + psz + ii];
+                cn += p.partial[p.itPOff[it] + psz + np + ii];
+            }
+            p.gvec[ia + ii] += v;
+            p.gcnt[ia + ii] += (int64_t)cn;
         }
     }
 }
@@ -239,12 +299,19 @@ __global__ void k_mupdat(int32_t n, const int32_t *iv, const int32_t *jv, const 
 }  // namespace
 
 cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
-    int64_t warps = p.nG;
-    int64_t blocks = (warps + 7) / 8;
-    int64_t maxb = (int64_t)nsm * 8;
-    if (blocks > maxb) blocks = maxb;
-    if (blocks < 1) blocks = 1;
-    k_accumulate<<<(unsigned)blocks, 256, 0, s>>>(p);
+    const int smem = kAccWarps * kAccSmem * (int)sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(k_acc_items, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    if (p.nitem > 0) {
+        int64_t blocks = (p.nitem + kAccWarps - 1) / kAccWarps;
+        const int64_t maxb = (int64_t)nsm * 4;
+        if (blocks > maxb) blocks = maxb;
+        k_acc_items<<<(unsigned)blocks, 32 * kAccWarps, smem, s>>>(p);
+    }
+    int64_t rb = (p.nG + 7) / 8;
+    if (rb > (int64_t)nsm * 8) rb = (int64_t)nsm * 8;
+    if (rb < 1) rb = 1;
+    k_acc_reduce<<<(unsigned)rb, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

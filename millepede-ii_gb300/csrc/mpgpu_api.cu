@@ -73,13 +73,18 @@ void free_records(DevJob &j) {
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
     dfree(j.fileWeight); dfree(j.status); dfree(j.chi2add); dfree(j.ndfadd); dfree(j.chndf);
     dfree(j.vstage); dfree(j.entries); dfree(j.eStart); dfree(j.stage);
+    dfree(j.itRow); dfree(j.itE0); dfree(j.itE1); dfree(j.itPOff); dfree(j.rowItem0);
+    dfree(j.partial);
     j.chunkRec.clear();
+    j.chunkItem.clear();
     j.nrec = 0;
 }
 
 void free_layout(DevJob &j) {
     dfree(j.varOfTot); dfree(j.aig); dfree(j.p2g); dfree(j.off); dfree(j.col);
     dfree(j.matD); dfree(j.gvec); dfree(j.gcnt); dfree(j.gpar); dfree(j.work);
+    dfree(j.rowBlk0); dfree(j.blkJ); dfree(j.blkOff); dfree(j.blkLd); dfree(j.blkCol);
+    dfree(j.rowWidth);
 }
 
 void free_constraints(DevJob &j) {
@@ -179,6 +184,60 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
     if (matsto == 2) {
         MPG_CUDA(c, dupload(j.off, sparseOffsets, 2 * (int64_t)(nGroups + 1), s));
         MPG_CUDA(c, dupload(j.col, sparseColumns, ncolw, s));
+    }
+    // block rows (dense row layout of each row group; for the sparse storage
+    // the blocks of sparseMatrixOffsets/Columns, ijpgrp pede.f90:5371-5461)
+    {
+        std::vector<int64_t> rowBlk0(nGroups + 1, 0), bOff;
+        std::vector<int32_t> bJ, bLd, bCol, width(nGroups, 0);
+        for (int32_t I = 1; I <= nGroups; ++I) {
+            const int32_t np = allIndexGroups[I] - allIndexGroups[I - 1];
+            if (matsto == 2) {
+                const int64_t kk = sparseOffsets[2 * (I - 1)], ll = sparseOffsets[2 * (I - 1) + 1];
+                const int64_t ku = sparseOffsets[2 * I] - kk;
+                if (ku > 0 && sparseColumns[kk] != 0) {
+                    int64_t k = 0;
+                    while (k < ku) {
+                        const int32_t first = sparseColumns[kk + k];
+                        if (first < 1 || first > nVar) return set_err(c, MPGPU_ERR_SIZE, "bad sparse columns");
+                        const int32_t J = p2g[first - 1];
+                        const int32_t nj = allIndexGroups[J] - allIndexGroups[J - 1];
+                        bJ.push_back(J); bOff.push_back(ll + k); bLd.push_back((int32_t)ku);
+                        bCol.push_back((int32_t)k);
+                        k += nj;
+                    }
+                    width[I - 1] = (int32_t)ku;
+                } else if (ku > 0) {
+                    for (int64_t k = 2; k <= ku - 2; k += 2) {
+                        const int32_t o0 = sparseColumns[kk + k - 2], g0 = sparseColumns[kk + k - 1];
+                        const int32_t o1 = sparseColumns[kk + k];
+                        int32_t inreg = 0, J = g0;
+                        while (inreg < o1 - o0) {
+                            if (J < 1 || J > nGroups) return set_err(c, MPGPU_ERR_SIZE, "bad sparse regions");
+                            const int32_t nj = allIndexGroups[J] - allIndexGroups[J - 1];
+                            bJ.push_back(J); bOff.push_back(ll + (int64_t)o0 * np + inreg);
+                            bLd.push_back(o1 - o0); bCol.push_back(o0 + inreg);
+                            inreg += nj;
+                            J++;
+                        }
+                        width[I - 1] = o1;
+                    }
+                }
+            } else {
+                width[I - 1] = allIndexGroups[I] - 1;
+            }
+            rowBlk0[I] = (int64_t)bJ.size();
+        }
+        j.hRowWidth = width;
+        MPG_CUDA(c, dupload(j.rowWidth, width.data(), nGroups, s));
+        if (matsto == 2) {
+            MPG_CUDA(c, dupload(j.rowBlk0, rowBlk0.data(), nGroups + 1, s));
+            MPG_CUDA(c, dupload(j.blkJ, bJ.data(), (int64_t)bJ.size(), s));
+            MPG_CUDA(c, dupload(j.blkOff, bOff.data(), (int64_t)bOff.size(), s));
+            MPG_CUDA(c, dupload(j.blkLd, bLd.data(), (int64_t)bLd.size(), s));
+            MPG_CUDA(c, dupload(j.blkCol, bCol.data(), (int64_t)bCol.size(), s));
+            MPG_CUDA(c, cudaStreamSynchronize(s));
+        }
     }
     MPG_CUDA(c, dalloc(j.matD, nmat));
     MPG_CUDA(c, cudaMemsetAsync(j.matD, 0, sizeof(double) * (size_t)nmat, s));
@@ -495,6 +554,40 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
                 }
         ebase = es[nG];
     }
+    // work items of the accumulation: each row group's entries cut into
+    // record-ordered ranges of about equal cost; the partial block row of an
+    // item is at most 1/16 of the update data it sums
+    std::vector<int32_t> itRow;
+    std::vector<int64_t> itE0, itE1, itPOff, rowItem0((size_t)nchunk * (nG + 1));
+    j.chunkItem.assign(1, 0);
+    int64_t maxPartial = 1;
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        const int64_t *es = &eStart[(size_t)ch * (nG + 1)];
+        int64_t *ri0 = &rowItem0[(size_t)ch * (nG + 1)];
+        int64_t pOff = 0;
+        for (int32_t I = 1; I <= nG; ++I) {
+            ri0[I - 1] = (int64_t)itRow.size();
+            const int32_t np = aig[I] - aig[I - 1];
+            const int64_t psz = (int64_t)np * j.hRowWidth[I - 1] + 2 * np;
+            const int64_t target = std::max<int64_t>(65536, 16 * psz);
+            int64_t cost = 0, e0 = es[I - 1];
+            for (int64_t e = es[I - 1]; e < es[I]; ++e) {
+                const int64_t r = entries[e] >> 8;
+                const int q = (int)(entries[e] & 0xff);
+                const int64_t offa = grpSlot[rec[r].grpOff + q];
+                cost += 48 + ((offa + np) * (offa + np + 1) - offa * (offa + 1)) / 2;
+                if (cost >= target || e + 1 == es[I]) {
+                    itRow.push_back(I); itE0.push_back(e0); itE1.push_back(e + 1); itPOff.push_back(pOff);
+                    pOff += psz;
+                    e0 = e + 1;
+                    cost = 0;
+                }
+            }
+        }
+        ri0[nG] = (int64_t)itRow.size();
+        j.chunkItem.push_back((int64_t)itRow.size());
+        maxPartial = std::max(maxPartial, pOff);
+    }
 
     // ---- upload
     cudaStream_t s = c->stream;
@@ -510,6 +603,13 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     MPG_CUDA(c, dupload(j.grpSlot, grpSlot.data(), ngrpT, s));
     MPG_CUDA(c, dupload(j.entries, entries.data(), ebase, s));
     MPG_CUDA(c, dupload(j.eStart, eStart.data(), (int64_t)eStart.size(), s));
+    MPG_CUDA(c, dupload(j.itRow, itRow.data(), (int64_t)itRow.size(), s));
+    MPG_CUDA(c, dupload(j.itE0, itE0.data(), (int64_t)itE0.size(), s));
+    MPG_CUDA(c, dupload(j.itE1, itE1.data(), (int64_t)itE1.size(), s));
+    MPG_CUDA(c, dupload(j.itPOff, itPOff.data(), (int64_t)itPOff.size(), s));
+    MPG_CUDA(c, dupload(j.rowItem0, rowItem0.data(), (int64_t)rowItem0.size(), s));
+    j.partialLen = maxPartial;
+    MPG_CUDA(c, dalloc(j.partial, maxPartial));
     std::vector<double> fw(nfiles, 1.0);
     if (fileWeight) fw.assign(fileWeight, fileWeight + nfiles);
     MPG_CUDA(c, dupload(j.fileWeight, fw.data(), nfiles, s));
@@ -550,6 +650,9 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.errFlag = errFlag;
     if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     AccParams ap{};
+    ap.itRow = j.itRow; ap.itE0 = j.itE0; ap.itE1 = j.itE1; ap.itPOff = j.itPOff;
+    ap.rowBlk0 = j.rowBlk0; ap.blkJ = j.blkJ; ap.blkOff = j.blkOff; ap.blkLd = j.blkLd;
+    ap.blkCol = j.blkCol; ap.rowWidth = j.rowWidth; ap.partial = j.partial;
     ap.rec = j.rec; ap.entries = j.entries; ap.grpId = j.grpId; ap.grpSlot = j.grpSlot;
     ap.status = j.status; ap.stage = j.stage; ap.vstage = j.vstage; ap.slotCnt = j.slotCnt;
     ap.aig = j.aig; ap.off = j.off; ap.col = j.col; ap.nG = j.nG; ap.matsto = j.matsto;
@@ -567,6 +670,9 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, s)); launches++; }
         cudaEventRecord(ev[2 + 2 * ch], s);
         ap.eStart = j.eStart + ch * (j.nG + 1);
+        ap.rowItem0 = j.rowItem0 + ch * (j.nG + 1);
+        ap.item0 = j.chunkItem[ch];
+        ap.nitem = j.chunkItem[ch + 1] - j.chunkItem[ch];
         if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_accumulate(ap, nsm, s)); launches++; }
     }
     cudaEventRecord(ev[2 * nchunk + 1], s);

@@ -43,6 +43,16 @@ struct DevJob {
     double *gvec = nullptr;        // [nVar]
     int64_t *gcnt = nullptr;       // [nVar]
     double *gpar = nullptr;        // [nTotal]
+    // block rows of the global matrix: blocks (I, J <= I) of row group I,
+    // ordered by J, with the offset of element (0,0) in globalMatD, the row
+    // stride and the column offset in the dense row layout of I
+    int64_t *rowBlk0 = nullptr;    // [nG+1]
+    int32_t *blkJ = nullptr;
+    int64_t *blkOff = nullptr;
+    int32_t *blkLd = nullptr;
+    int32_t *blkCol = nullptr;
+    int32_t *rowWidth = nullptr;   // [nG] columns of the dense row layout
+    std::vector<int32_t> hRowWidth;
     // records
     int64_t nrec = 0, nw = 0, neqTot = 0, nslotTot = 0, nswTot = 0, ngrpTot = 0;
     int32_t nfiles = 1;
@@ -67,6 +77,14 @@ struct DevJob {
     std::vector<int64_t> chunkRec;     // [nchunk+1] record boundaries
     int64_t *entries = nullptr;        // (record << 8) | group position
     int64_t *eStart = nullptr;         // [nchunk*(nG+1)]
+    // accumulation work items: (row group, record-ordered entry range,
+    // partial-sum offset); items of one row group are consecutive
+    std::vector<int64_t> chunkItem;    // [nchunk+1] item boundaries
+    int32_t *itRow = nullptr;
+    int64_t *itE0 = nullptr, *itE1 = nullptr, *itPOff = nullptr;
+    int64_t *rowItem0 = nullptr;       // [nchunk*(nG+1)] first item of each row group
+    double *partial = nullptr;
+    int64_t partialLen = 0;
     double *stage = nullptr;
     int64_t stageLen = 0;
     // limits over the job (fit kernel shared memory sizing)
@@ -131,6 +149,14 @@ struct AccParams {
     const RecInfo *rec;
     const int64_t *entries;
     const int64_t *eStart;
+    const int32_t *itRow;
+    const int64_t *itE0, *itE1, *itPOff;
+    const int64_t *rowItem0;   // this chunk, [nG+1] (absolute item ids)
+    int64_t item0, nitem;      // item range of this chunk
+    const int64_t *rowBlk0;
+    const int32_t *blkJ, *blkLd, *blkCol, *rowWidth;
+    const int64_t *blkOff;
+    double *partial;
     const int32_t *grpId, *grpSlot;
     const int8_t *status;
     const double *stage;

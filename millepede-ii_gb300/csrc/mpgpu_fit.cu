@@ -445,7 +445,7 @@ __device__ void s_sqmibb(int side, double *v, double *b, int n, int nbdr, int nb
 // ------------------------------------------------------------------------
 // shared-memory carve-up of one warp
 struct WarpMem {
-    double *gl, *rm1, *lcor, *lwgt, *res, *t1, *t2, *clmat, *blvec, *diag, *ocol, *scol;
+    double *gl, *rm1, *lcor, *lwgt, *res, *t1, *t2, *w0, *clmat, *blvec, *diag, *ocol, *scol;
     double *B, *W;
     double *bnd;   // band scratch (may be null)
     int32_t *in, *mq, *slots, *swS, *sw, *used;
@@ -464,7 +464,7 @@ __host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax,
                                               int bandmax, int bdrmax) {
     int64_t d = 0;
     d += wmax;                          // gl
-    d += 6 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2
+    d += 7 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2 w0
     d += (int64_t)nalcmax * (nalcmax + 1) / 2 + 4 * (int64_t)nalcmax;  // clmat blvec diag ocol scol
     d += 2 * (int64_t)nalcmax * nalgmax;  // B W
     d += band_doubles(nalcmax, bandmax, bdrmax);
@@ -488,6 +488,7 @@ __device__ WarpMem carve(char *base, const FitParams &p) {
     m.res = d; d += p.neqmax;
     m.t1 = d; d += p.neqmax;
     m.t2 = d; d += p.neqmax;
+    m.w0 = d; d += p.neqmax;
     m.clmat = d; d += (int64_t)p.nalcmax * (p.nalcmax + 1) / 2;
     m.blvec = d; d += p.nalcmax;
     m.diag = d; d += p.nalcmax;
@@ -556,11 +557,14 @@ k_fit(FitParams p, int perWarp) {
                 }
                 m.rm1[e] = rm;
                 m.lcor[e] = 0.0;
+                const double rerr = m.gl[sg];
+                m.w0[e] = 1.0 / (rerr * rerr);   // weight from the error, same value in every loop
             }
             __syncwarp();
             const int nter = (p.nloopn != 1 && p.lhuber != 0) ? p.lhuber : 1;
             const bool band = ri.mbnd >= 0 && p.lfitbb > 0 && nalc > 5;
             const bool seqNormal = ((ri.mside >> 8) & 1) != 0;
+            const bool needResing = p.lhuber > 1 && p.dwcut != 0.0f;
             const int npk = (nalc * nalc + nalc) / 2;
             int nrank = 0, ndf = 0;
             double summ = 0.0;
@@ -570,7 +574,7 @@ k_fit(FitParams p, int perWarp) {
                 for (int e = ln; e < neq; e += 32) {
                     const int sg = m.mq[3 * e + 1];
                     const double rerr = m.gl[sg];
-                    double wght = 1.0 / (rerr * rerr);
+                    double wght = m.w0[e];
                     const double resid = m.rm1[e] - m.lcor[e];
                     if (down) {
                         if (iter <= 3) {
@@ -659,7 +663,7 @@ k_fit(FitParams p, int perWarp) {
                 for (int e = ln; e < neq; e += 32) {
                     const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                     const double rerr = m.gl[sg];
-                    double wght = 1.0 / (rerr * rerr);
+                    double wght = m.w0[e];
                     double rmloc = 0.0;
                     for (int j = 1; j <= sg - sl - 1; ++j) {
                         const int ij = m.in[sl + j];
@@ -680,15 +684,20 @@ k_fit(FitParams p, int perWarp) {
                             dchi2 = log(1.0 + t * t) * (kCauchy * kCauchy);
                         }
                     }
-                    const double dn = 1.0 / sqrt(wght);
                     m.t1[e] = dchi2;
-                    m.t2[e] = rerr / dn;
+                    if (needResing) {
+                        const double dn = 1.0 / sqrt(wght);
+                        m.t2[e] = rerr / dn;
+                    }
                 }
                 __syncwarp();
                 summ = wsum_serial(m.t1, neq);
-                const double suwt = wsum_serial(m.t2, neq);
                 ndf = neq - nrank;
-                resing = ((float)neq - (float)suwt) / (float)neq;
+                if (needResing) {
+                    // down-weight fraction, used only by the dwcut decision
+                    const double suwt = wsum_serial(m.t2, neq);
+                    resing = ((float)neq - (float)suwt) / (float)neq;
+                }
                 if (nan) { st = 1; break; }
                 if (nrank != nalc) { st = 2; break; }
                 if (cndl10 > p.cndlmx) { st = 3; break; }
@@ -722,7 +731,7 @@ k_fit(FitParams p, int perWarp) {
                     const int sg = m.mq[3 * e + 1];
                     const double rm = m.rm1[e] - m.lcor[e];
                     const double rerr = m.gl[sg];
-                    double wght = 1.0 / (rerr * rerr);
+                    double wght = m.w0[e];
                     double dchi2 = wght * rm * rm;
                     if (p.nloopn != 1 && p.lhuber != 0) {
                         const double resid = fabs(rm);
