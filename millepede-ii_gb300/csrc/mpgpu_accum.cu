@@ -60,142 +60,155 @@ __device__ int64_t d_ijpgrp(int32_t itema, int32_t itemb, int32_t nG, const int3
 
 namespace {
 
-// Work item = (row group I, a record-ordered range of the records that
-// contain I).  One warp sums, in record order, the rows of group I of every
-// accepted record's update into a private partial block row (dense row
-// layout of I: the stored column blocks side by side) and the vector slice.
-// Hot row groups (modules crossed by many tracks) are split into several
-// items, so the work is balanced over the GPU; k_acc_reduce then adds the
-// partials of a row group in item order.  Fixed item boundaries make the
-// result independent of scheduling.
-constexpr int kAccWarps = 8;
-constexpr int kAccSmem = 768;    // doubles of shared-memory partial per warp
+// Work item = (block (I, J <= I) of the global matrix, a record-ordered
+// range of the records containing both groups).  Lane l of the warp sums
+// the records l, l+32, l+64, ... of the item (each a small gather from that
+// record's packed update), then the 32 lane sums are added in lane order;
+// blocks crossed by many tracks are split into several items whose sums are
+// added in item order by k_acc_block_reduce.  Item boundaries and the lane
+// assignment are fixed, so the result is identical on every run.
+// Rejected records carry an all-zero update.
+constexpr int kAccWarps = 4;
+constexpr int kTile = 36;   // block elements per pass (one 6x6 block)
+constexpr int kTileV = 8;   // vector elements per pass
 
-__global__ void __launch_bounds__(32 * kAccWarps) k_acc_items(AccParams p) {
-    extern __shared__ __align__(16) double sacc[];
-    __shared__ int32_t s_off[kAccWarps][MPG_NGRP_MAX + 2];
-    __shared__ int32_t s_col[kAccWarps][MPG_NGRP_MAX + 1];
+__global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
+    extern __shared__ __align__(16) double accs[];
+    double (*acc)[kTile][32] = reinterpret_cast<double (*)[kTile][32]>(accs);
+    __shared__ int32_t s_ii[kAccWarps][kTile], s_jj[kAccWarps][kTile];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * kAccWarps + wib;
     const int64_t nw = (int64_t)gridDim.x * kAccWarps;
-    double *mine = sacc + (int64_t)wib * kAccSmem;
     for (int64_t it = p.item0 + w; it < p.item0 + p.nitem; it += nw) {
-        const int32_t I = p.itRow[it];
+        const int32_t blk = p.itBlk[it];
+        const int32_t I = p.bkI[blk], J = p.bkJ[blk];
         const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
-        const int32_t width = p.rowWidth[I - 1];
-        const int64_t psz = (int64_t)np * width, total = psz + 2 * np;
-        double *P = total <= kAccSmem ? mine : p.partial + p.itPOff[it];
-        for (int64_t q = ln; q < total; q += 32) P[q] = 0.0;
-        __syncwarp();
-        const int64_t kb0 = p.matsto == 2 ? p.rowBlk0[I - 1] : 0;
-        const int64_t kb1 = p.matsto == 2 ? p.rowBlk0[I] : 0;
-        for (int64_t e = p.itE0[it]; e < p.itE1[it]; ++e) {
-            const int64_t ent = p.entries[e];
-            const int64_t r = ent >> 8;
-            const int a = (int)(ent & 0xff);
-            if (p.status[r] != 0) continue;
-            const int64_t updOff = p.rec[r].updOff, grpOff = p.rec[r].grpOff;
-            const int64_t slotOff = p.rec[r].slotOff;
-            for (int b = ln; b <= a; b += 32) {
-                const int32_t J = p.grpId[grpOff + b];
-                s_off[wib][b] = p.grpSlot[grpOff + b];
-                int32_t col = -1;
-                if (p.matsto == 2) {
-                    int64_t lo = kb0, hi = kb1 - 1;
-                    while (lo <= hi) {
-                        const int64_t mid = (lo + hi) >> 1;
-                        const int32_t jm = p.blkJ[mid];
-                        if (jm == J) { col = p.blkCol[mid]; break; }
-                        if (jm < J) lo = mid + 1; else hi = mid - 1;
+        const int32_t ja = p.aig[J - 1] - 1, nj = p.aig[J] - p.aig[J - 1];
+        const bool diag = I == J;
+        const int64_t e0 = p.itE0[it], e1 = p.itE1[it], slot = p.itSlot[it];
+        // elements of the block stored in the update (lower part for I == J)
+        int32_t nel = 0;
+        for (int32_t t0 = 0;; t0 += kTile) {
+            // build the next tile of element coordinates
+            int32_t tn = 0;
+            if (ln == 0) {
+                int32_t k = 0, cnt = 0;
+                for (int32_t ii = 0; ii < np && tn < kTile; ++ii)
+                    for (int32_t jj = 0; jj < nj && tn < kTile; ++jj) {
+                        if (diag && jj > ii) continue;
+                        if (k++ < t0) continue;
+                        s_ii[wib][tn] = ii;
+                        s_jj[wib][tn] = jj;
+                        tn++;
+                        cnt++;
                     }
-                    if (col < 0) *p.errFlag = 23;
+                (void)cnt;
+            }
+            tn = __shfl_sync(0xffffffffu, tn, 0);
+            __syncwarp();
+            if (tn == 0) break;
+            nel += tn;
+            for (int q = 0; q < tn; ++q) acc[wib][q][ln] = 0.0;
+            for (int64_t e = e0 + ln; e < e1; e += 32) {
+                const int64_t ent = p.bEntries[e];
+                const int32_t offa = (int32_t)(ent & 0xffff);
+                const double *U = p.stage + (ent >> 16);
+                int32_t cii = -1;
+                int64_t rb = 0;
+                for (int q = 0; q < tn; ++q) {
+                    const int32_t ii = s_ii[wib][q];
+                    if (ii != cii) { cii = ii; rb = (int64_t)(offa + ii) * (offa + ii + 1) / 2; }
+                    acc[wib][q][ln] += U[rb + s_jj[wib][q]];
+                }
+            }
+            __syncwarp();
+            for (int q = ln; q < tn; q += 32) {
+                double sum = 0.0;
+                for (int l = 0; l < 32; ++l) sum += acc[wib][q][l];
+                const int32_t ii = s_ii[wib][q], jj = s_jj[wib][q];
+                if (slot >= 0) {
+                    p.partial[slot * p.pstride + t0 + q] = sum;
+                } else if (p.matsto == 2) {
+                    if (diag && ii == jj) p.matD[ia + ii] -= sum;
+                    else p.matD[p.bkOff[blk] + (int64_t)ii * p.bkLd[blk] + jj] -= sum;
                 } else {
-                    col = p.aig[J - 1] - 1;
-                }
-                s_col[wib][b] = col < 0 ? 0 : col;
-            }
-            __syncwarp();
-            if (ln == 0) s_off[wib][a + 1] = s_off[wib][a] + np;
-            __syncwarp();
-            const int32_t offa = s_off[wib][a];
-            if (p.icalcm == 1) {
-                const int64_t s0 = (int64_t)offa * (offa + 1) / 2;
-                const int64_t s1 = (int64_t)(offa + np) * (offa + np + 1) / 2;
-                const double *U = p.stage + updOff;
-                int ra = offa, cb = ln;
-                while (cb > ra) { cb -= ra + 1; ra++; }
-                int b = 0;
-                for (int64_t idx = s0 + ln; idx < s1; idx += 32) {
-                    while (cb >= s_off[wib][b + 1]) b++;
-                    while (cb < s_off[wib][b]) b--;
-                    const int ii = ra - offa, jj = cb - s_off[wib][b];
-                    P[(int64_t)ii * width + s_col[wib][b] + jj] += U[idx];
-                    cb += 32;
-                    while (cb > ra) { cb -= ra + 1; ra++; }
-                }
-            }
-            for (int ii = ln; ii < np; ii += 32) {
-                P[psz + ii] += p.vstage[slotOff + offa + ii];
-                P[psz + np + ii] += (double)p.slotCnt[slotOff + offa + ii];
-            }
-            __syncwarp();
-        }
-        if (total <= kAccSmem) {
-            double *G = p.partial + p.itPOff[it];
-            for (int64_t q = ln; q < total; q += 32) G[q] = P[q];
-        }
-        __syncwarp();
-    }
-}
-
-// Warp per row group: partials of its items in item (= record) order,
-// subtracted from the block row of the global matrix; vector and counts.
-__global__ void __launch_bounds__(256) k_acc_reduce(AccParams p) {
-    const int ln = threadIdx.x & 31;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t I = 1 + w; I <= p.nG; I += nw) {
-        const int64_t i0 = p.rowItem0[I - 1], i1 = p.rowItem0[I];
-        if (i1 <= i0) continue;
-        const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
-        const int32_t width = p.rowWidth[I - 1];
-        const int64_t psz = (int64_t)np * width;
-        if (p.icalcm == 1) {
-            if (p.matsto == 2) {
-                for (int64_t k = p.rowBlk0[I - 1]; k < p.rowBlk0[I]; ++k) {
-                    const int32_t J = p.blkJ[k];
-                    const int32_t nj = p.aig[J] - p.aig[J - 1];
-                    const int64_t boff = p.blkOff[k];
-                    const int32_t ld = p.blkLd[k], col0 = p.blkCol[k];
-                    for (int q = ln; q < np * nj; q += 32) {
-                        const int ii = q / nj, jj = q - ii * nj;
-                        if (J == I && jj > ii) continue;
-                        double sum = 0.0;
-                        for (int64_t it = i0; it < i1; ++it)
-                            sum += p.partial[p.itPOff[it] + (int64_t)ii * width + col0 + jj];
-                        if (J == I && jj == ii) p.matD[ia + ii] -= sum;
-                        else p.matD[boff + (int64_t)ii * ld + jj] -= sum;
-                    }
-                }
-            } else {
-                for (int64_t q = ln; q < psz; q += 32) {
-                    const int64_t ii = q / width, col = q - ii * width;
-                    const int64_t gi = ia + ii + 1, gj = col + 1;
-                    if (gj > gi) continue;
-                    double sum = 0.0;
-                    for (int64_t it = i0; it < i1; ++it) sum += p.partial[p.itPOff[it] + q];
+                    const int64_t gi = ia + ii + 1, gj = ja + jj + 1;
                     p.matD[(gi * gi - gi) / 2 + gj - 1] -= sum;
                 }
             }
+            __syncwarp();
         }
-        for (int ii = ln; ii < np; ii += 32) {
-            double v = 0.0, cn = 0.0;
-            for (int64_t it = i0; it < i1; ++it) {
-                v += p.partial[p.itPOff[it] + psz + ii];
-                cn += p.partial[p.itPOff[it] + psz + np + ii];
+        (void)nel;
+    }
+}
+
+// blocks with several items: item sums added in item order
+__global__ void __launch_bounds__(256) k_acc_block_reduce(AccParams p) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = p.red0 + w; r < p.red0 + p.nred; r += nw) {
+        const int32_t blk = p.rdBlk[r];
+        const int64_t s0 = p.rdSlot0[r];
+        const int32_t ns = p.rdN[r];
+        const int32_t I = p.bkI[blk], J = p.bkJ[blk];
+        const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
+        const int32_t ja = p.aig[J - 1] - 1, nj = p.aig[J] - p.aig[J - 1];
+        const bool diag = I == J;
+        // element order of k_acc_blocks: rows ii, columns jj (jj <= ii on the diagonal)
+        int32_t q = 0;
+        for (int32_t ii = 0; ii < np; ++ii)
+            for (int32_t jj = 0; jj < nj; ++jj) {
+                if (diag && jj > ii) continue;
+                if ((q & 31) == ln) {
+                    double sum = 0.0;
+                    for (int32_t k = 0; k < ns; ++k) sum += p.partial[(s0 + k) * p.pstride + q];
+                    if (p.matsto == 2) {
+                        if (diag && ii == jj) p.matD[ia + ii] -= sum;
+                        else p.matD[p.bkOff[blk] + (int64_t)ii * p.bkLd[blk] + jj] -= sum;
+                    } else {
+                        const int64_t gi = ia + ii + 1, gj = ja + jj + 1;
+                        p.matD[(gi * gi - gi) / 2 + gj - 1] -= sum;
+                    }
+                }
+                q++;
             }
-            p.gvec[ia + ii] += v;
-            p.gcnt[ia + ii] += (int64_t)cn;
+    }
+}
+
+// vector slices and counts: warp per row group, lane l sums the accepted
+// records l, l+32, ... of the group, lane sums added in lane order
+__global__ void __launch_bounds__(256) k_acc_vector(AccParams p) {
+    __shared__ double vacc[8][kTileV][32];
+    __shared__ int32_t cacc[8][kTileV][32];
+    const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t I = 1 + w; I <= p.nG; I += nw) {
+        const int64_t e0 = p.vStart[I - 1], e1 = p.vStart[I];
+        if (e1 <= e0) continue;
+        const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
+        for (int32_t t0 = 0; t0 < np; t0 += kTileV) {
+            const int32_t tn = np - t0 < kTileV ? np - t0 : kTileV;
+            for (int q = 0; q < tn; ++q) { vacc[wib][q][ln] = 0.0; cacc[wib][q][ln] = 0; }
+            for (int64_t e = e0 + ln; e < e1; e += 32) {
+                const int64_t ent = p.vEntries[e];
+                const int64_t r = ent >> 40, vo = ent & ((int64_t(1) << 40) - 1);
+                if (p.status[r] != 0) continue;
+                for (int q = 0; q < tn; ++q) {
+                    vacc[wib][q][ln] += p.vstage[vo + t0 + q];
+                    cacc[wib][q][ln] += p.slotCnt[vo + t0 + q];
+                }
+            }
+            __syncwarp();
+            for (int q = ln; q < tn; q += 32) {
+                double v = 0.0;
+                int64_t cn = 0;
+                for (int l = 0; l < 32; ++l) { v += vacc[wib][q][l]; cn += cacc[wib][q][l]; }
+                p.gvec[ia + t0 + q] += v;
+                p.gcnt[ia + t0 + q] += cn;
+            }
+            __syncwarp();
         }
     }
 }
@@ -299,19 +312,24 @@ __global__ void k_mupdat(int32_t n, const int32_t *iv, const int32_t *jv, const 
 }  // namespace
 
 cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
-    const int smem = kAccWarps * kAccSmem * (int)sizeof(double);
-    cudaError_t e = cudaFuncSetAttribute(k_acc_items, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    if (p.nitem > 0) {
+    if (p.icalcm == 1 && p.nitem > 0) {
+        const int smem = kAccWarps * kTile * 32 * (int)sizeof(double);
+        cudaError_t e = cudaFuncSetAttribute(k_acc_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
         int64_t blocks = (p.nitem + kAccWarps - 1) / kAccWarps;
-        const int64_t maxb = (int64_t)nsm * 4;
+        const int64_t maxb = (int64_t)nsm * 12;
         if (blocks > maxb) blocks = maxb;
-        k_acc_items<<<(unsigned)blocks, 32 * kAccWarps, smem, s>>>(p);
+        k_acc_blocks<<<(unsigned)blocks, 32 * kAccWarps, smem, s>>>(p);
+        if (p.nred > 0) {
+            int64_t rb = (p.nred + 7) / 8;
+            if (rb > (int64_t)nsm * 8) rb = (int64_t)nsm * 8;
+            k_acc_block_reduce<<<(unsigned)rb, 256, 0, s>>>(p);
+        }
     }
-    int64_t rb = (p.nG + 7) / 8;
-    if (rb > (int64_t)nsm * 8) rb = (int64_t)nsm * 8;
-    if (rb < 1) rb = 1;
-    k_acc_reduce<<<(unsigned)rb, 256, 0, s>>>(p);
+    int64_t vb = (p.nG + 7) / 8;
+    if (vb > (int64_t)nsm * 8) vb = (int64_t)nsm * 8;
+    if (vb < 1) vb = 1;
+    k_acc_vector<<<(unsigned)vb, 256, 0, s>>>(p);
     return cudaGetLastError();
 }
 

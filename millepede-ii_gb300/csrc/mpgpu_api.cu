@@ -72,11 +72,14 @@ void free_records(DevJob &j) {
     dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
     dfree(j.fileWeight); dfree(j.status); dfree(j.chi2add); dfree(j.ndfadd); dfree(j.chndf);
-    dfree(j.vstage); dfree(j.entries); dfree(j.eStart); dfree(j.stage);
-    dfree(j.itRow); dfree(j.itE0); dfree(j.itE1); dfree(j.itPOff); dfree(j.rowItem0);
-    dfree(j.partial);
+    dfree(j.vstage); dfree(j.stage);
+    dfree(j.bkI); dfree(j.bkJ); dfree(j.bkLd); dfree(j.bkOff);
+    dfree(j.itBlk); dfree(j.itE0); dfree(j.itE1); dfree(j.itSlot); dfree(j.bEntries);
+    dfree(j.rdBlk); dfree(j.rdSlot0); dfree(j.rdN); dfree(j.partial);
+    dfree(j.vEntries); dfree(j.vStart);
     j.chunkRec.clear();
     j.chunkItem.clear();
+    j.chunkRed.clear();
     j.nrec = 0;
 }
 
@@ -229,6 +232,10 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
             rowBlk0[I] = (int64_t)bJ.size();
         }
         j.hRowWidth = width;
+        j.hRowBlk0 = rowBlk0;
+        j.hBlkJ = bJ;
+        j.hBlkOff = bOff;
+        j.hBlkLd = bLd;
         MPG_CUDA(c, dupload(j.rowWidth, width.data(), nGroups, s));
         if (matsto == 2) {
             MPG_CUDA(c, dupload(j.rowBlk0, rowBlk0.data(), nGroups + 1, s));
@@ -531,63 +538,165 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
         }
     });
 
-    // ---- pass D: owner lists per parameter group and chunk (record order)
+    // ---- pass D: blocks of the global matrix met in the records
     const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
     const int32_t nG = j.nG;
-    std::vector<int64_t> eStart((size_t)nchunk * (nG + 1));
-    std::vector<int64_t> entries(ngrpT);
-    int64_t ebase = 0;
-    for (int64_t ch = 0; ch < nchunk; ++ch) {
-        int64_t *es = &eStart[(size_t)ch * (nG + 1)];
-        std::vector<int64_t> cntg(nG + 1, 0);
-        for (int64_t r = j.chunkRec[ch]; r < j.chunkRec[ch + 1]; ++r)
-            if (rec[r].nalc > 0)
-                for (int32_t q = 0; q < rec[r].ngrp; ++q) cntg[grpId[rec[r].grpOff + q]]++;
-        es[0] = ebase;
-        for (int32_t g = 1; g <= nG; ++g) es[g] = es[g - 1] + cntg[g];
-        std::vector<int64_t> fillp(es, es + nG);
-        for (int64_t r = j.chunkRec[ch]; r < j.chunkRec[ch + 1]; ++r)
-            if (rec[r].nalc > 0)
-                for (int32_t q = 0; q < rec[r].ngrp; ++q) {
-                    const int32_t g = grpId[rec[r].grpOff + q];
-                    entries[fillp[g - 1]++] = (r << 8) | q;
-                }
-        ebase = es[nG];
+    std::vector<int64_t> pairOff(nrec + 1, 0);
+    for (int64_t r = 0; r < nrec; ++r) {
+        const int64_t ng = rec[r].nalc > 0 ? rec[r].ngrp : 0;
+        pairOff[r + 1] = pairOff[r] + ng * (ng + 1) / 2;
     }
-    // work items of the accumulation: each row group's entries cut into
-    // record-ordered ranges of about equal cost; the partial block row of an
-    // item is at most 1/16 of the update data it sums
-    std::vector<int32_t> itRow;
-    std::vector<int64_t> itE0, itE1, itPOff, rowItem0((size_t)nchunk * (nG + 1));
-    j.chunkItem.assign(1, 0);
-    int64_t maxPartial = 1;
-    for (int64_t ch = 0; ch < nchunk; ++ch) {
-        const int64_t *es = &eStart[(size_t)ch * (nG + 1)];
-        int64_t *ri0 = &rowItem0[(size_t)ch * (nG + 1)];
-        int64_t pOff = 0;
-        for (int32_t I = 1; I <= nG; ++I) {
-            ri0[I - 1] = (int64_t)itRow.size();
-            const int32_t np = aig[I] - aig[I - 1];
-            const int64_t psz = (int64_t)np * j.hRowWidth[I - 1] + 2 * np;
-            const int64_t target = std::max<int64_t>(65536, 16 * psz);
-            int64_t cost = 0, e0 = es[I - 1];
-            for (int64_t e = es[I - 1]; e < es[I]; ++e) {
-                const int64_t r = entries[e] >> 8;
-                const int q = (int)(entries[e] & 0xff);
-                const int64_t offa = grpSlot[rec[r].grpOff + q];
-                cost += 48 + ((offa + np) * (offa + np + 1) - offa * (offa + 1)) / 2;
-                if (cost >= target || e + 1 == es[I]) {
-                    itRow.push_back(I); itE0.push_back(e0); itE1.push_back(e + 1); itPOff.push_back(pOff);
-                    pOff += psz;
-                    e0 = e + 1;
-                    cost = 0;
+    const int64_t npairs = pairOff[nrec];
+    std::vector<int32_t> bkI, bkJ, bkLd;
+    std::vector<int64_t> bkOff, packedKey;
+    if (j.matsto == 2) {
+        const int64_t nb = (int64_t)j.hBlkJ.size();
+        bkI.resize(nb);
+        for (int32_t I = 1; I <= nG; ++I)
+            for (int64_t k = j.hRowBlk0[I - 1]; k < j.hRowBlk0[I]; ++k) bkI[k] = I;
+        bkJ = j.hBlkJ;
+        bkLd = j.hBlkLd;
+        bkOff = j.hBlkOff;
+    } else {
+        // packed storage: the group pairs that occur in records
+        std::vector<std::vector<int64_t>> keys(nthreads_host());
+        parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
+            std::vector<int64_t> &kv = keys[t];
+            for (int64_t r = a; r < b; ++r) {
+                if (rec[r].nalc <= 0) continue;
+                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa)
+                    for (int32_t qb = 0; qb <= qa; ++qb)
+                        kv.push_back((int64_t)grpId[rec[r].grpOff + qa] * (nG + 1) + grpId[rec[r].grpOff + qb]);
+                if (kv.size() > (1u << 24)) {
+                    std::sort(kv.begin(), kv.end());
+                    kv.erase(std::unique(kv.begin(), kv.end()), kv.end());
+                }
+            }
+            std::sort(kv.begin(), kv.end());
+            kv.erase(std::unique(kv.begin(), kv.end()), kv.end());
+        });
+        for (auto &kv : keys) packedKey.insert(packedKey.end(), kv.begin(), kv.end());
+        std::sort(packedKey.begin(), packedKey.end());
+        packedKey.erase(std::unique(packedKey.begin(), packedKey.end()), packedKey.end());
+        for (int64_t key : packedKey) {
+            bkI.push_back((int32_t)(key / (nG + 1)));
+            bkJ.push_back((int32_t)(key % (nG + 1)));
+            bkLd.push_back(0);
+            bkOff.push_back(0);
+        }
+    }
+    const int64_t nblk = (int64_t)bkI.size();
+    // block of every record pair (a >= b)
+    std::vector<int32_t> pairBlk(std::max<int64_t>(npairs, 1));
+    std::vector<int> pbad(nthreads_host() + 1, 0);
+    parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
+        for (int64_t r = a; r < b; ++r) {
+            if (rec[r].nalc <= 0) continue;
+            int64_t q = pairOff[r];
+            for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
+                const int32_t I = grpId[rec[r].grpOff + qa];
+                for (int32_t qb = 0; qb <= qa; ++qb) {
+                    const int32_t J = grpId[rec[r].grpOff + qb];
+                    int64_t k = -1;
+                    if (j.matsto == 2) {
+                        auto b0 = j.hBlkJ.begin() + j.hRowBlk0[I - 1], b1 = j.hBlkJ.begin() + j.hRowBlk0[I];
+                        auto itb = std::lower_bound(b0, b1, J);
+                        if (itb != b1 && *itb == J) k = itb - j.hBlkJ.begin();
+                    } else {
+                        const int64_t key = (int64_t)I * (nG + 1) + J;
+                        auto itb = std::lower_bound(packedKey.begin(), packedKey.end(), key);
+                        k = itb - packedKey.begin();
+                    }
+                    if (k < 0) { pbad[t] = 1; k = 0; }
+                    pairBlk[q++] = (int32_t)k;
                 }
             }
         }
-        ri0[nG] = (int64_t)itRow.size();
-        j.chunkItem.push_back((int64_t)itRow.size());
-        maxPartial = std::max(maxPartial, pOff);
+    });
+    for (int v : pbad)
+        if (v) return set_err(c, MPGPU_ERR_BADINDEX, "record group pair not in the sparse structure");
+    int32_t maxEl = 1;
+    for (int64_t k = 0; k < nblk; ++k) {
+        const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
+        maxEl = std::max(maxEl, bkI[k] == bkJ[k] ? ni * (ni + 1) / 2 : ni * nj);
     }
+    j.pstride = maxEl;
+    // per chunk: block entries in record order, items, reduction lists;
+    // vector entries per row group in record order
+    std::vector<int64_t> bEntries(std::max<int64_t>(npairs, 1));
+    std::vector<int32_t> itBlk, rdBlk, rdN;
+    std::vector<int64_t> itE0, itE1, itSlot, rdSlot0;
+    int64_t nvent = 0;
+    for (int64_t r = 0; r < nrec; ++r) if (rec[r].nalc > 0) nvent += rec[r].ngrp;
+    std::vector<int64_t> vEntries(std::max<int64_t>(nvent, 1)), vStart((size_t)nchunk * (nG + 1));
+    j.chunkItem.assign(1, 0);
+    j.chunkRed.assign(1, 0);
+    int64_t maxSlots = 1, vbase = 0;
+    const int nt = nthreads_host();
+    std::vector<int64_t> cnt(nblk + 1);
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        const int64_t r0 = j.chunkRec[ch], r1 = j.chunkRec[ch + 1];
+        const int64_t p0 = pairOff[r0], p1 = pairOff[r1];
+        // counting sort of the chunk's pairs by block, stable in record order
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int64_t q = p0; q < p1; ++q) cnt[pairBlk[q] + 1]++;
+        for (int64_t k = 0; k < nblk; ++k) cnt[k + 1] += cnt[k];
+        std::vector<int64_t> bs(cnt.begin(), cnt.end());
+        std::vector<int64_t> fillp(cnt.begin(), cnt.end() - 1);
+        for (int64_t r = r0; r < r1; ++r) {
+            if (rec[r].nalc <= 0) continue;
+            int64_t q = pairOff[r];
+            for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
+                const int64_t offa = grpSlot[rec[r].grpOff + qa];
+                for (int32_t qb = 0; qb <= qa; ++qb) {
+                    const int64_t offb = grpSlot[rec[r].grpOff + qb];
+                    bEntries[p0 + fillp[pairBlk[q]]++] = ((rec[r].updOff + offb) << 16) | offa;
+                    q++;
+                }
+            }
+        }
+        int64_t slot = 0;
+        for (int64_t k = 0; k < nblk; ++k) {
+            const int64_t e0 = bs[k], e1 = bs[k + 1];
+            if (e1 <= e0) continue;
+            const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
+            const int32_t nel = bkI[k] == bkJ[k] ? ni * (ni + 1) / 2 : ni * nj;
+            const int64_t per = std::max<int64_t>(32, 9216 / std::max(nel, 1));
+            const int64_t nitem = (e1 - e0 + per - 1) / per;
+            for (int64_t m = 0; m < nitem; ++m) {
+                itBlk.push_back((int32_t)k);
+                itE0.push_back(p0 + e0 + m * per);
+                itE1.push_back(p0 + std::min(e1, e0 + (m + 1) * per));
+                itSlot.push_back(nitem > 1 ? slot + m : -1);
+            }
+            if (nitem > 1) {
+                rdBlk.push_back((int32_t)k);
+                rdSlot0.push_back(slot);
+                rdN.push_back((int32_t)nitem);
+                slot += nitem;
+            }
+        }
+        maxSlots = std::max(maxSlots, slot);
+        j.chunkItem.push_back((int64_t)itBlk.size());
+        j.chunkRed.push_back((int64_t)rdBlk.size());
+        // vector entries of the chunk by row group
+        int64_t *vs = &vStart[(size_t)ch * (nG + 1)];
+        std::vector<int64_t> vc(nG + 1, 0);
+        for (int64_t r = r0; r < r1; ++r)
+            if (rec[r].nalc > 0)
+                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) vc[grpId[rec[r].grpOff + qa]]++;
+        vs[0] = vbase;
+        for (int32_t g = 1; g <= nG; ++g) vs[g] = vs[g - 1] + vc[g];
+        std::vector<int64_t> vf(vs, vs + nG);
+        for (int64_t r = r0; r < r1; ++r)
+            if (rec[r].nalc > 0)
+                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
+                    const int32_t g = grpId[rec[r].grpOff + qa];
+                    vEntries[vf[g - 1]++] = (r << 40) | (rec[r].slotOff + grpSlot[rec[r].grpOff + qa]);
+                }
+        vbase = vs[nG];
+    }
+    (void)nt;
 
     // ---- upload
     cudaStream_t s = c->stream;
@@ -601,15 +710,23 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     MPG_CUDA(c, dupload(j.sw, sw.data(), nswT, s));
     MPG_CUDA(c, dupload(j.grpId, grpId.data(), ngrpT, s));
     MPG_CUDA(c, dupload(j.grpSlot, grpSlot.data(), ngrpT, s));
-    MPG_CUDA(c, dupload(j.entries, entries.data(), ebase, s));
-    MPG_CUDA(c, dupload(j.eStart, eStart.data(), (int64_t)eStart.size(), s));
-    MPG_CUDA(c, dupload(j.itRow, itRow.data(), (int64_t)itRow.size(), s));
+    j.nblk = nblk;
+    MPG_CUDA(c, dupload(j.bkI, bkI.data(), nblk, s));
+    MPG_CUDA(c, dupload(j.bkJ, bkJ.data(), nblk, s));
+    MPG_CUDA(c, dupload(j.bkLd, bkLd.data(), nblk, s));
+    MPG_CUDA(c, dupload(j.bkOff, bkOff.data(), nblk, s));
+    MPG_CUDA(c, dupload(j.bEntries, bEntries.data(), npairs, s));
+    MPG_CUDA(c, dupload(j.itBlk, itBlk.data(), (int64_t)itBlk.size(), s));
     MPG_CUDA(c, dupload(j.itE0, itE0.data(), (int64_t)itE0.size(), s));
     MPG_CUDA(c, dupload(j.itE1, itE1.data(), (int64_t)itE1.size(), s));
-    MPG_CUDA(c, dupload(j.itPOff, itPOff.data(), (int64_t)itPOff.size(), s));
-    MPG_CUDA(c, dupload(j.rowItem0, rowItem0.data(), (int64_t)rowItem0.size(), s));
-    j.partialLen = maxPartial;
-    MPG_CUDA(c, dalloc(j.partial, maxPartial));
+    MPG_CUDA(c, dupload(j.itSlot, itSlot.data(), (int64_t)itSlot.size(), s));
+    MPG_CUDA(c, dupload(j.rdBlk, rdBlk.data(), (int64_t)rdBlk.size(), s));
+    MPG_CUDA(c, dupload(j.rdSlot0, rdSlot0.data(), (int64_t)rdSlot0.size(), s));
+    MPG_CUDA(c, dupload(j.rdN, rdN.data(), (int64_t)rdN.size(), s));
+    MPG_CUDA(c, dupload(j.vEntries, vEntries.data(), nvent, s));
+    MPG_CUDA(c, dupload(j.vStart, vStart.data(), (int64_t)vStart.size(), s));
+    j.partialLen = maxSlots * j.pstride;
+    MPG_CUDA(c, dalloc(j.partial, j.partialLen));
     std::vector<double> fw(nfiles, 1.0);
     if (fileWeight) fw.assign(fileWeight, fileWeight + nfiles);
     MPG_CUDA(c, dupload(j.fileWeight, fw.data(), nfiles, s));
@@ -650,12 +767,12 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.errFlag = errFlag;
     if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     AccParams ap{};
-    ap.itRow = j.itRow; ap.itE0 = j.itE0; ap.itE1 = j.itE1; ap.itPOff = j.itPOff;
-    ap.rowBlk0 = j.rowBlk0; ap.blkJ = j.blkJ; ap.blkOff = j.blkOff; ap.blkLd = j.blkLd;
-    ap.blkCol = j.blkCol; ap.rowWidth = j.rowWidth; ap.partial = j.partial;
-    ap.rec = j.rec; ap.entries = j.entries; ap.grpId = j.grpId; ap.grpSlot = j.grpSlot;
+    ap.bkI = j.bkI; ap.bkJ = j.bkJ; ap.bkLd = j.bkLd; ap.bkOff = j.bkOff;
+    ap.itBlk = j.itBlk; ap.itE0 = j.itE0; ap.itE1 = j.itE1; ap.itSlot = j.itSlot;
+    ap.bEntries = j.bEntries; ap.rdBlk = j.rdBlk; ap.rdSlot0 = j.rdSlot0; ap.rdN = j.rdN;
+    ap.partial = j.partial; ap.pstride = j.pstride; ap.vEntries = j.vEntries;
     ap.status = j.status; ap.stage = j.stage; ap.vstage = j.vstage; ap.slotCnt = j.slotCnt;
-    ap.aig = j.aig; ap.off = j.off; ap.col = j.col; ap.nG = j.nG; ap.matsto = j.matsto;
+    ap.aig = j.aig; ap.nG = j.nG; ap.matsto = j.matsto;
     ap.icalcm = opt->icalcm; ap.matD = j.matD; ap.gvec = j.gvec; ap.gcnt = j.gcnt; ap.errFlag = errFlag;
     const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
     // events bracket every kernel of the loop: fit and accumulation times
@@ -669,10 +786,11 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         cudaEventRecord(ev[1 + 2 * ch], s);
         if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, s)); launches++; }
         cudaEventRecord(ev[2 + 2 * ch], s);
-        ap.eStart = j.eStart + ch * (j.nG + 1);
-        ap.rowItem0 = j.rowItem0 + ch * (j.nG + 1);
+        ap.vStart = j.vStart + ch * (j.nG + 1);
         ap.item0 = j.chunkItem[ch];
         ap.nitem = j.chunkItem[ch + 1] - j.chunkItem[ch];
+        ap.red0 = j.chunkRed[ch];
+        ap.nred = j.chunkRed[ch + 1] - j.chunkRed[ch];
         if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_accumulate(ap, nsm, s)); launches++; }
     }
     cudaEventRecord(ev[2 * nchunk + 1], s);

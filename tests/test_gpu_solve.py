@@ -103,7 +103,20 @@ def test_minres_sparse(mp, orc):
     L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xo, orc.f64p), C.c_int32(0))
     assert info.istop in (1, 2) and istop in (1, 2)
     assert abs(info.itn - itn.value) <= 0.1 * itn.value  # long Krylov runs drift in rounding
-    assert np.max(np.abs(corr - xo)) <= 1e-9 * np.max(np.abs(xo))
+    # two MINRES runs to rtol 1e-12 on a system this ill-conditioned agree to
+    # a few 1e-9; the GPU solution's own residual is the sharper check
+    assert np.max(np.abs(corr - xo)) <= 1e-8 * np.max(np.abs(xo))
+    xr_sol = np.zeros(H.nVar)
+    xr_sol[:] = corr
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xr_sol, orc.f64p), C.c_int32(1))
+    with mp.Context() as c2:
+        c2.set_layout(H, 2)
+        c2.set_constraints(A)
+        c2.upload(H)
+        c2.loopbf(np.zeros(H.nTotal))
+        Ax = c2.avprod(xr_sol[:nfit])
+    res = np.linalg.norm(Ax - rhs[:nfit]) / np.linalg.norm(rhs[:nfit])
+    assert res <= 1e-9
     # avprod against the oracle's avprd0 with explicit Q
     xa = np.concatenate([xr, np.zeros(A.shape[0])])
     L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xa, orc.f64p), C.c_int32(0))
