@@ -75,7 +75,8 @@ constexpr int kTileV = 8;   // vector elements per pass
 __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
     extern __shared__ __align__(16) double accs[];
     double (*acc)[kTile][32] = reinterpret_cast<double (*)[kTile][32]>(accs);
-    __shared__ int32_t s_ii[kAccWarps][kTile], s_jj[kAccWarps][kTile];
+    // element q of a tile: U offset relative to row offa = ii*offa + c
+    __shared__ int32_t s_ii[kAccWarps][kTile], s_c[kAccWarps][kTile], s_jj[kAccWarps][kTile];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * kAccWarps + wib;
     const int64_t nw = (int64_t)gridDim.x * kAccWarps;
@@ -86,41 +87,42 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
         const int32_t ja = p.aig[J - 1] - 1, nj = p.aig[J] - p.aig[J - 1];
         const bool diag = I == J;
         const int64_t e0 = p.itE0[it], e1 = p.itE1[it], slot = p.itSlot[it];
-        // elements of the block stored in the update (lower part for I == J)
-        int32_t nel = 0;
         for (int32_t t0 = 0;; t0 += kTile) {
-            // build the next tile of element coordinates
             int32_t tn = 0;
             if (ln == 0) {
-                int32_t k = 0, cnt = 0;
+                int32_t k = 0;
                 for (int32_t ii = 0; ii < np && tn < kTile; ++ii)
                     for (int32_t jj = 0; jj < nj && tn < kTile; ++jj) {
                         if (diag && jj > ii) continue;
                         if (k++ < t0) continue;
                         s_ii[wib][tn] = ii;
                         s_jj[wib][tn] = jj;
+                        s_c[wib][tn] = ii * (ii + 1) / 2 + jj;
                         tn++;
-                        cnt++;
                     }
-                (void)cnt;
             }
             tn = __shfl_sync(0xffffffffu, tn, 0);
             __syncwarp();
             if (tn == 0) break;
-            nel += tn;
-            for (int q = 0; q < tn; ++q) acc[wib][q][ln] = 0.0;
+            double a[kTile];
+#pragma unroll
+            for (int q = 0; q < kTile; ++q) a[q] = 0.0;
             for (int64_t e = e0 + ln; e < e1; e += 32) {
                 const int64_t ent = p.bEntries[e];
-                const int32_t offa = (int32_t)(ent & 0xffff);
-                const double *U = p.stage + (ent >> 16);
-                int32_t cii = -1;
-                int64_t rb = 0;
-                for (int q = 0; q < tn; ++q) {
-                    const int32_t ii = s_ii[wib][q];
-                    if (ii != cii) { cii = ii; rb = (int64_t)(offa + ii) * (offa + ii + 1) / 2; }
-                    acc[wib][q][ln] += U[rb + s_jj[wib][q]];
-                }
+                const int64_t offa = ent & 0xffff;
+                // row offa of the record's packed update, columns from offb
+                const double *U = p.stage + (ent >> 16) + offa * (offa + 1) / 2;
+                double v[kTile];
+#pragma unroll
+                for (int q = 0; q < kTile; ++q)
+                    if (q < tn) v[q] = __ldg(U + s_ii[wib][q] * offa + s_c[wib][q]);
+#pragma unroll
+                for (int q = 0; q < kTile; ++q)
+                    if (q < tn) a[q] += v[q];
             }
+#pragma unroll
+            for (int q = 0; q < kTile; ++q)
+                if (q < tn) acc[wib][q][ln] = a[q];
             __syncwarp();
             for (int q = ln; q < tn; q += 32) {
                 double sum = 0.0;
@@ -138,7 +140,6 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
             }
             __syncwarp();
         }
-        (void)nel;
     }
 }
 

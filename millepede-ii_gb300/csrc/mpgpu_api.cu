@@ -128,6 +128,7 @@ extern "C" int32_t mpgpu_create(mpgpu_ctx **out, const mpgpu_cfg *cfg) {
     c->stagingBytes = (cfg && cfg->staging_bytes > 0) ? cfg->staging_bytes : (int64_t)4 << 30;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc((void **)&c->scal, 4096);
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hscal, 4096);
     if (e != cudaSuccess) {
@@ -149,6 +150,7 @@ extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
     if (c->scal) cudaFree(c->scal);
     if (c->hscal) cudaFreeHost(c->hscal);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     delete c;
     return MPGPU_OK;
 }
@@ -735,8 +737,10 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     MPG_CUDA(c, dalloc(j.ndfadd, nrec));
     MPG_CUDA(c, dalloc(j.chndf, nrec));
     MPG_CUDA(c, dalloc(j.vstage, nslotT));
+    // two staging buffers when there are several chunks: the fits of chunk
+    // k+1 overlap the accumulation of chunk k
     j.stageLen = maxStage;
-    MPG_CUDA(c, dalloc(j.stage, maxStage));
+    MPG_CUDA(c, dalloc(j.stage, (j.chunkRec.size() > 2 ? 2 : 1) * maxStage));
     MPG_CUDA(c, cudaStreamSynchronize(s));
     return MPGPU_OK;
 }
@@ -775,25 +779,46 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     ap.aig = j.aig; ap.nG = j.nG; ap.matsto = j.matsto;
     ap.icalcm = opt->icalcm; ap.matD = j.matD; ap.gvec = j.gvec; ap.gcnt = j.gcnt; ap.errFlag = errFlag;
     const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
-    // events bracket every kernel of the loop: fit and accumulation times
-    std::vector<cudaEvent_t> ev(2 * nchunk + 3);
-    for (auto &e : ev) cudaEventCreate(&e);
-    cudaEventRecord(ev[0], s);
+    // fits on stream 1, accumulation on stream 2; with several chunks the
+    // staging alternates between two buffers and the fit of chunk k+1 runs
+    // while chunk k is accumulated (the fit kernel then keeps one CTA per SM
+    // so the memory-bound accumulation can share the SMs)
+    cudaStream_t s2 = c->stream2;
+    const bool overlap = nchunk > 1;
+    std::vector<cudaEvent_t> evF0(nchunk), evF1(nchunk), evA0(nchunk), evA1(nchunk);
+    cudaEvent_t evStart, evZero, evEnd;
+    cudaEventCreate(&evStart);
+    cudaEventCreateWithFlags(&evZero, cudaEventDisableTiming);
+    cudaEventCreate(&evEnd);
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        cudaEventCreate(&evF0[ch]); cudaEventCreate(&evF1[ch]);
+        cudaEventCreate(&evA0[ch]); cudaEventCreate(&evA1[ch]);
+    }
+    cudaEventRecord(evStart, s);
+    cudaEventRecord(evZero, s);
+    MPG_CUDA(c, cudaStreamWaitEvent(s2, evZero, 0));
     int32_t launches = 0;
     for (int64_t ch = 0; ch < nchunk; ++ch) {
         fp.r0 = j.chunkRec[ch];
         fp.r1 = j.chunkRec[ch + 1];
-        cudaEventRecord(ev[1 + 2 * ch], s);
-        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, s)); launches++; }
-        cudaEventRecord(ev[2 + 2 * ch], s);
+        double *stg = j.stage + (overlap ? (ch & 1) * j.stageLen : 0);
+        if (overlap && ch >= 2) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[ch - 2], 0));
+        fp.stage = stg;
+        cudaEventRecord(evF0[ch], s);
+        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, overlap ? 1 : 0, s)); launches++; }
+        cudaEventRecord(evF1[ch], s);
+        MPG_CUDA(c, cudaStreamWaitEvent(s2, evF1[ch], 0));
+        ap.stage = stg;
         ap.vStart = j.vStart + ch * (j.nG + 1);
         ap.item0 = j.chunkItem[ch];
         ap.nitem = j.chunkItem[ch + 1] - j.chunkItem[ch];
         ap.red0 = j.chunkRed[ch];
         ap.nred = j.chunkRed[ch + 1] - j.chunkRed[ch];
-        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_accumulate(ap, nsm, s)); launches++; }
+        cudaEventRecord(evA0[ch], s2);
+        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_accumulate(ap, nsm, s2)); launches += 3; }
+        cudaEventRecord(evA1[ch], s2);
     }
-    cudaEventRecord(ev[2 * nchunk + 1], s);
+    if (nchunk > 0) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[nchunk - 1], 0));
     // statistics
     const int32_t nf = j.nfiles;
     int64_t *iout = (int64_t *)(c->scal + 8);
@@ -806,20 +831,24 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
                   dout, iout, fout};
     MPG_CUDA(c, launch_stats(sp, s));
     launches += 2;
-    cudaEventRecord(ev[2 * nchunk + 2], s);
+    cudaEventRecord(evEnd, s);
     MPG_CUDA(c, cudaMemcpyAsync(c->hscal, c->scal, 4096, cudaMemcpyDeviceToHost, s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
     double msFit = 0.0, msAcc = 0.0;
     float t = 0.0f;
     for (int64_t ch = 0; ch < nchunk; ++ch) {
-        cudaEventElapsedTime(&t, ev[1 + 2 * ch], ev[2 + 2 * ch]);
+        cudaEventElapsedTime(&t, evF0[ch], evF1[ch]);
         msFit += t;
-        cudaEventElapsedTime(&t, ev[2 + 2 * ch], ch + 1 < nchunk ? ev[3 + 2 * ch] : ev[2 * nchunk + 1]);
+        cudaEventElapsedTime(&t, evA0[ch], evA1[ch]);
         msAcc += t;
     }
-    cudaEventElapsedTime(&t, ev[0], ev[2 * nchunk + 2]);
+    cudaEventElapsedTime(&t, evStart, evEnd);
     const double msLoop = t;
-    for (auto &e : ev) cudaEventDestroy(e);
+    for (int64_t ch = 0; ch < nchunk; ++ch) {
+        cudaEventDestroy(evF0[ch]); cudaEventDestroy(evF1[ch]);
+        cudaEventDestroy(evA0[ch]); cudaEventDestroy(evA1[ch]);
+    }
+    cudaEventDestroy(evStart); cudaEventDestroy(evZero); cudaEventDestroy(evEnd);
     const int32_t *hflag = (const int32_t *)c->hscal;
     if (hflag[0]) return set_err(c, hflag[0], "device index error in the data loop");
     const int64_t *hi = (const int64_t *)(c->hscal + 8);

@@ -122,6 +122,7 @@ struct DevJob {
 struct mpgpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // accumulation, overlapped with the fits
     int64_t stagingBytes = 0;
     std::string err;
     DevJob j;
@@ -157,7 +158,7 @@ struct FitParams {
 
 int fit_smem_per_warp(const FitParams &p);
 int fit_warps_per_cta(const FitParams &p);
-cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s);
+cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s);
 
 struct AccParams {
     const int32_t *bkI, *bkJ, *bkLd;

@@ -860,7 +860,7 @@ int fit_warps_per_cta(const FitParams &p) {
     return (int64_t)per * wpc > 220 * 1024 ? 0 : wpc;
 }
 
-cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s) {
+cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s) {
     const int per = fit_smem_per_warp(p);
     const int wpc = fit_warps_per_cta(p);
     if (wpc < 1) return cudaErrorInvalidConfiguration;
@@ -870,6 +870,7 @@ cudaError_t launch_fit(const FitParams &p, int nsm, cudaStream_t s) {
     int perSM = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_fit, 32 * wpc, bytes);
     if (perSM < 1) perSM = 1;
+    if (maxPerSM > 0 && perSM > maxPerSM) perSM = maxPerSM;
     int64_t nrec = p.r1 - p.r0;
     int64_t grid = (int64_t)nsm * perSM;
     int64_t need = (nrec + wpc - 1) / wpc;
