@@ -61,22 +61,55 @@ __device__ int64_t d_ijpgrp(int32_t itema, int32_t itemb, int32_t nG, const int3
 namespace {
 
 // Work item = (block (I, J <= I) of the global matrix, a record-ordered
-// range of the records containing both groups).  Lane l of the warp sums
-// the records l, l+32, l+64, ... of the item (each a small gather from that
-// record's packed update), then the 32 lane sums are added in lane order;
-// blocks crossed by many tracks are split into several items whose sums are
-// added in item order by k_acc_block_reduce.  Item boundaries and the lane
-// assignment are fixed, so the result is identical on every run.
-// Rejected records carry an all-zero update.
-constexpr int kAccWarps = 4;
-constexpr int kTile = 36;   // block elements per pass (one 6x6 block)
-constexpr int kTileV = 8;   // vector elements per pass
+// range of the records containing both groups).  The fit kernel writes the
+// part of each record's update that falls in a block to the staging position
+// base + k * nel, k the record's rank among the block's records of the chunk
+// (elements row-major, lower triangle on diagonal blocks), so an item is one
+// contiguous cnt x nel array.  Blocks of more than kSmallEl elements: lane l
+// owns elements l, l+32, ... and adds the records in record order (coalesced
+// rows).  Smaller blocks: lane l adds the records l, l+32, ... and the 32
+// lane sums are combined by a fixed shuffle tree.  Blocks crossed by many
+// tracks are split into several items whose sums are added in item order by
+// k_acc_block_reduce.  Item boundaries are fixed, so every element receives
+// its sum in the same order on every run.  Rejected records carry zeros.
+constexpr int kAccWarps = 8;
+constexpr int kSmallEl = 8;   // lane-per-record at or below this block size
+constexpr int kLaneEl = 4;    // element accumulators per lane (128 elements per pass)
+constexpr int kUnroll = 4;    // records loaded ahead of the adds
+constexpr int kTileV = 8;     // vector elements per pass
+
+// element t of a block (row-major, lower triangle when diagonal) -> (ii, jj)
+__device__ __forceinline__ void blk_elem(int32_t t, bool diag, int32_t nj, int32_t &ii, int32_t &jj) {
+    if (diag) {
+        int32_t r = (int32_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+        while (r > 0 && r * (r + 1) / 2 > t) r--;
+        while ((r + 1) * (r + 2) / 2 <= t) r++;
+        ii = r;
+        jj = t - r * (r + 1) / 2;
+    } else {
+        ii = t / nj;
+        jj = t - ii * nj;
+    }
+}
+
+__device__ __forceinline__ void blk_store(const AccParams &p, int32_t blk, int64_t slot, int32_t t,
+                                          bool diag, int32_t ia, int32_t ja, int32_t nj, double sum) {
+    if (slot >= 0) {
+        p.partial[slot * p.pstride + t] = sum;
+        return;
+    }
+    int32_t ii, jj;
+    blk_elem(t, diag, nj, ii, jj);
+    if (p.matsto == 2) {
+        if (diag && ii == jj) p.matD[ia + ii] -= sum;
+        else p.matD[p.bkOff[blk] + (int64_t)ii * p.bkLd[blk] + jj] -= sum;
+    } else {
+        const int64_t gi = ia + ii + 1, gj = ja + jj + 1;
+        p.matD[(gi * gi - gi) / 2 + gj - 1] -= sum;
+    }
+}
 
 __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
-    extern __shared__ __align__(16) double accs[];
-    double (*acc)[kTile][32] = reinterpret_cast<double (*)[kTile][32]>(accs);
-    // element q of a tile: U offset relative to row offa = ii*offa + c
-    __shared__ int32_t s_ii[kAccWarps][kTile], s_c[kAccWarps][kTile], s_jj[kAccWarps][kTile];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t w = (int64_t)blockIdx.x * kAccWarps + wib;
     const int64_t nw = (int64_t)gridDim.x * kAccWarps;
@@ -86,64 +119,60 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
         const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
         const int32_t ja = p.aig[J - 1] - 1, nj = p.aig[J] - p.aig[J - 1];
         const bool diag = I == J;
-        const int64_t e0 = p.itE0[it], e1 = p.itE1[it], slot = p.itSlot[it];
-        for (int32_t t0 = 0;; t0 += kTile) {
-            int32_t tn = 0;
-            if (ln == 0) {
-                int32_t k = 0;
-                for (int32_t ii = 0; ii < np && tn < kTile; ++ii)
-                    for (int32_t jj = 0; jj < nj && tn < kTile; ++jj) {
-                        if (diag && jj > ii) continue;
-                        if (k++ < t0) continue;
-                        s_ii[wib][tn] = ii;
-                        s_jj[wib][tn] = jj;
-                        s_c[wib][tn] = ii * (ii + 1) / 2 + jj;
-                        tn++;
-                    }
-            }
-            tn = __shfl_sync(0xffffffffu, tn, 0);
-            __syncwarp();
-            if (tn == 0) break;
-            double a[kTile];
+        const int32_t nel = diag ? np * (np + 1) / 2 : np * nj;
+        const int64_t slot = p.itSlot[it];
+        const int32_t cnt = p.itCnt[it];
+        const double *src = p.stage + p.itBase[it];
+        if (nel <= kSmallEl) {
+            double a[kSmallEl];
 #pragma unroll
-            for (int q = 0; q < kTile; ++q) a[q] = 0.0;
-            for (int64_t e = e0 + ln; e < e1; e += 32) {
-                const int64_t ent = p.bEntries[e];
-                const int64_t offa = ent & 0xffff;
-                // row offa of the record's packed update, columns from offb
-                const double *U = p.stage + (ent >> 16) + offa * (offa + 1) / 2;
-                double v[kTile];
+            for (int q = 0; q < kSmallEl; ++q) a[q] = 0.0;
+            for (int32_t r = ln; r < cnt; r += 32) {
+                const double *row = src + (int64_t)r * nel;
 #pragma unroll
-                for (int q = 0; q < kTile; ++q)
-                    if (q < tn) v[q] = __ldg(U + s_ii[wib][q] * offa + s_c[wib][q]);
-#pragma unroll
-                for (int q = 0; q < kTile; ++q)
-                    if (q < tn) a[q] += v[q];
+                for (int q = 0; q < kSmallEl; ++q)
+                    if (q < nel) a[q] += __ldg(row + q);
             }
 #pragma unroll
-            for (int q = 0; q < kTile; ++q)
-                if (q < tn) acc[wib][q][ln] = a[q];
-            __syncwarp();
-            for (int q = ln; q < tn; q += 32) {
-                double sum = 0.0;
-                for (int l = 0; l < 32; ++l) sum += acc[wib][q][l];
-                const int32_t ii = s_ii[wib][q], jj = s_jj[wib][q];
-                if (slot >= 0) {
-                    p.partial[slot * p.pstride + t0 + q] = sum;
-                } else if (p.matsto == 2) {
-                    if (diag && ii == jj) p.matD[ia + ii] -= sum;
-                    else p.matD[p.bkOff[blk] + (int64_t)ii * p.bkLd[blk] + jj] -= sum;
-                } else {
-                    const int64_t gi = ia + ii + 1, gj = ja + jj + 1;
-                    p.matD[(gi * gi - gi) / 2 + gj - 1] -= sum;
-                }
+            for (int q = 0; q < kSmallEl; ++q) {
+                if (q >= nel) break;
+                double v = a[q];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                if (ln == 0) blk_store(p, blk, slot, q, diag, ia, ja, nj, v);
             }
-            __syncwarp();
+            continue;
+        }
+        for (int32_t t0 = 0; t0 < nel; t0 += 32 * kLaneEl) {
+            const int32_t lim = nel - t0 - ln;  // element q of the lane valid when 32 q < lim
+            const double *col = src + t0 + ln;
+            double a[kLaneEl];
+#pragma unroll
+            for (int q = 0; q < kLaneEl; ++q) a[q] = 0.0;
+            int32_t r = 0;
+            for (; r + kUnroll <= cnt; r += kUnroll) {
+                double v[kUnroll][kLaneEl];
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+                    for (int q = 0; q < kLaneEl; ++q)
+                        v[u][q] = 32 * q < lim ? __ldg(col + (int64_t)(r + u) * nel + 32 * q) : 0.0;
+#pragma unroll
+                for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+                    for (int q = 0; q < kLaneEl; ++q) a[q] += v[u][q];
+            }
+            for (; r < cnt; ++r)
+#pragma unroll
+                for (int q = 0; q < kLaneEl; ++q)
+                    if (32 * q < lim) a[q] += __ldg(col + (int64_t)r * nel + 32 * q);
+#pragma unroll
+            for (int q = 0; q < kLaneEl; ++q)
+                if (32 * q < lim) blk_store(p, blk, slot, t0 + ln + 32 * q, diag, ia, ja, nj, a[q]);
         }
     }
 }
 
-// blocks with several items: item sums added in item order
 __global__ void __launch_bounds__(256) k_acc_block_reduce(AccParams p) {
     const int ln = threadIdx.x & 31;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -314,13 +343,10 @@ __global__ void k_mupdat(int32_t n, const int32_t *iv, const int32_t *jv, const 
 
 cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
     if (p.icalcm == 1 && p.nitem > 0) {
-        const int smem = kAccWarps * kTile * 32 * (int)sizeof(double);
-        cudaError_t e = cudaFuncSetAttribute(k_acc_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
         int64_t blocks = (p.nitem + kAccWarps - 1) / kAccWarps;
-        const int64_t maxb = (int64_t)nsm * 12;
+        const int64_t maxb = (int64_t)nsm * 8;
         if (blocks > maxb) blocks = maxb;
-        k_acc_blocks<<<(unsigned)blocks, 32 * kAccWarps, smem, s>>>(p);
+        k_acc_blocks<<<(unsigned)blocks, 32 * kAccWarps, 0, s>>>(p);
         if (p.nred > 0) {
             int64_t rb = (p.nred + 7) / 8;
             if (rb > (int64_t)nsm * 8) rb = (int64_t)nsm * 8;

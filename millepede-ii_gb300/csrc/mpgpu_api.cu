@@ -74,7 +74,7 @@ void free_records(DevJob &j) {
     dfree(j.fileWeight); dfree(j.status); dfree(j.chi2add); dfree(j.ndfadd); dfree(j.chndf);
     dfree(j.vstage); dfree(j.stage);
     dfree(j.bkI); dfree(j.bkJ); dfree(j.bkLd); dfree(j.bkOff);
-    dfree(j.itBlk); dfree(j.itE0); dfree(j.itE1); dfree(j.itSlot); dfree(j.bEntries);
+    dfree(j.itBlk); dfree(j.itBase); dfree(j.itCnt); dfree(j.itSlot); dfree(j.pairDst);
     dfree(j.rdBlk); dfree(j.rdSlot0); dfree(j.rdN); dfree(j.partial);
     dfree(j.vEntries); dfree(j.vStart);
     j.chunkRec.clear();
@@ -443,7 +443,7 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     // ---- pass B: offsets, maxima, chunks by staging size
     int64_t neqT = 0, nslotT = 0, nswT = 0, ngrpT = 0;
     j.maxNw = j.maxNeq = j.maxNalc = j.maxNalg = 0;
-    j.maxBand = -1; j.maxBdr = 0;
+    j.maxBand = -1; j.maxBdr = 0; j.maxNgrp = 1;
     j.nbndr[0] = j.nbndr[1] = 0; j.nbdrx = j.nbndx = 0;
     const int64_t stageElems = std::max<int64_t>(c->stagingBytes / 8, 1);
     j.chunkRec.assign(1, 0);
@@ -455,11 +455,12 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
         ri.slotOff = nslotT; nslotT += ri.nalg + 1;
         ri.swOff = nswT; nswT += nsw;
         ri.grpOff = ngrpT; ngrpT += ri.ngrp;
-        const int64_t ngg = (int64_t)ri.nalg * (ri.nalg + 1) / 2;
+        // records without local parameters leave no update in the staging
+        const int64_t ngg = ri.nalc > 0 ? (int64_t)ri.nalg * (ri.nalg + 1) / 2 : 0;
         if (ngg > stageElems) return set_err(c, MPGPU_ERR_LIMIT, "record update larger than the staging buffer");
         if (upd + ngg > stageElems) { j.chunkRec.push_back(r); maxStage = std::max(maxStage, upd); upd = 0; }
-        ri.updOff = upd;
         upd += ngg;
+        j.maxNgrp = std::max(j.maxNgrp, ri.ngrp);
         j.maxNw = std::max(j.maxNw, ri.nw);
         j.maxNeq = std::max(j.maxNeq, ri.neq);
         j.maxNalc = std::max(j.maxNalc, ri.nalc);
@@ -546,6 +547,7 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     std::vector<int64_t> pairOff(nrec + 1, 0);
     for (int64_t r = 0; r < nrec; ++r) {
         const int64_t ng = rec[r].nalc > 0 ? rec[r].ngrp : 0;
+        rec[r].pairOff = pairOff[r];
         pairOff[r + 1] = pairOff[r] + ng * (ng + 1) / 2;
     }
     const int64_t npairs = pairOff[nrec];
@@ -623,52 +625,49 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
         maxEl = std::max(maxEl, bkI[k] == bkJ[k] ? ni * (ni + 1) / 2 : ni * nj);
     }
     j.pstride = maxEl;
-    // per chunk: block entries in record order, items, reduction lists;
-    // vector entries per row group in record order
-    std::vector<int64_t> bEntries(std::max<int64_t>(npairs, 1));
-    std::vector<int32_t> itBlk, rdBlk, rdN;
-    std::vector<int64_t> itE0, itE1, itSlot, rdSlot0;
+    // per chunk: staging position of every record block (the records of one
+    // global-matrix block contiguous in record order), work items and
+    // reduction lists; vector entries per row group in record order
+    std::vector<int64_t> nelOf(std::max<int64_t>(nblk, 1));
+    for (int64_t k = 0; k < nblk; ++k) {
+        const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
+        nelOf[k] = bkI[k] == bkJ[k] ? (int64_t)ni * (ni + 1) / 2 : (int64_t)ni * nj;
+    }
+    std::vector<int64_t> pairDst(std::max<int64_t>(npairs, 1));
+    std::vector<int32_t> itBlk, itCnt, rdBlk, rdN;
+    std::vector<int64_t> itBase, itSlot, rdSlot0;
     int64_t nvent = 0;
     for (int64_t r = 0; r < nrec; ++r) if (rec[r].nalc > 0) nvent += rec[r].ngrp;
     std::vector<int64_t> vEntries(std::max<int64_t>(nvent, 1)), vStart((size_t)nchunk * (nG + 1));
     j.chunkItem.assign(1, 0);
     j.chunkRed.assign(1, 0);
     int64_t maxSlots = 1, vbase = 0;
-    const int nt = nthreads_host();
-    std::vector<int64_t> cnt(nblk + 1);
+    std::vector<int64_t> cnt(nblk + 1), bBase(nblk + 1);
     for (int64_t ch = 0; ch < nchunk; ++ch) {
         const int64_t r0 = j.chunkRec[ch], r1 = j.chunkRec[ch + 1];
         const int64_t p0 = pairOff[r0], p1 = pairOff[r1];
-        // counting sort of the chunk's pairs by block, stable in record order
         std::fill(cnt.begin(), cnt.end(), 0);
-        for (int64_t q = p0; q < p1; ++q) cnt[pairBlk[q] + 1]++;
-        for (int64_t k = 0; k < nblk; ++k) cnt[k + 1] += cnt[k];
-        std::vector<int64_t> bs(cnt.begin(), cnt.end());
-        std::vector<int64_t> fillp(cnt.begin(), cnt.end() - 1);
-        for (int64_t r = r0; r < r1; ++r) {
-            if (rec[r].nalc <= 0) continue;
-            int64_t q = pairOff[r];
-            for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
-                const int64_t offa = grpSlot[rec[r].grpOff + qa];
-                for (int32_t qb = 0; qb <= qa; ++qb) {
-                    const int64_t offb = grpSlot[rec[r].grpOff + qb];
-                    bEntries[p0 + fillp[pairBlk[q]]++] = ((rec[r].updOff + offb) << 16) | offa;
-                    q++;
-                }
-            }
+        for (int64_t q = p0; q < p1; ++q) cnt[pairBlk[q]]++;
+        bBase[0] = 0;
+        for (int64_t k = 0; k < nblk; ++k) bBase[k + 1] = bBase[k] + cnt[k] * nelOf[k];
+        if (bBase[nblk] > maxStage) return set_err(c, MPGPU_ERR_LIMIT, "staging layout exceeds the chunk size");
+        std::vector<int64_t> fill(bBase.begin(), bBase.end() - 1);
+        for (int64_t q = p0; q < p1; ++q) {
+            const int32_t k = pairBlk[q];
+            pairDst[q] = fill[k];
+            fill[k] += nelOf[k];
         }
         int64_t slot = 0;
         for (int64_t k = 0; k < nblk; ++k) {
-            const int64_t e0 = bs[k], e1 = bs[k + 1];
-            if (e1 <= e0) continue;
-            const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
-            const int32_t nel = bkI[k] == bkJ[k] ? ni * (ni + 1) / 2 : ni * nj;
-            const int64_t per = std::max<int64_t>(32, 9216 / std::max(nel, 1));
-            const int64_t nitem = (e1 - e0 + per - 1) / per;
+            const int64_t n = cnt[k];
+            if (n <= 0) continue;
+            const int64_t nel = std::max<int64_t>(nelOf[k], 1);
+            const int64_t per = std::max<int64_t>(32, 16384 / nel);
+            const int64_t nitem = (n + per - 1) / per;
             for (int64_t m = 0; m < nitem; ++m) {
                 itBlk.push_back((int32_t)k);
-                itE0.push_back(p0 + e0 + m * per);
-                itE1.push_back(p0 + std::min(e1, e0 + (m + 1) * per));
+                itBase.push_back(bBase[k] + m * per * nelOf[k]);
+                itCnt.push_back((int32_t)std::min(per, n - m * per));
                 itSlot.push_back(nitem > 1 ? slot + m : -1);
             }
             if (nitem > 1) {
@@ -698,7 +697,6 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
                 }
         vbase = vs[nG];
     }
-    (void)nt;
 
     // ---- upload
     cudaStream_t s = c->stream;
@@ -717,10 +715,10 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     MPG_CUDA(c, dupload(j.bkJ, bkJ.data(), nblk, s));
     MPG_CUDA(c, dupload(j.bkLd, bkLd.data(), nblk, s));
     MPG_CUDA(c, dupload(j.bkOff, bkOff.data(), nblk, s));
-    MPG_CUDA(c, dupload(j.bEntries, bEntries.data(), npairs, s));
+    MPG_CUDA(c, dupload(j.pairDst, pairDst.data(), npairs, s));
     MPG_CUDA(c, dupload(j.itBlk, itBlk.data(), (int64_t)itBlk.size(), s));
-    MPG_CUDA(c, dupload(j.itE0, itE0.data(), (int64_t)itE0.size(), s));
-    MPG_CUDA(c, dupload(j.itE1, itE1.data(), (int64_t)itE1.size(), s));
+    MPG_CUDA(c, dupload(j.itBase, itBase.data(), (int64_t)itBase.size(), s));
+    MPG_CUDA(c, dupload(j.itCnt, itCnt.data(), (int64_t)itCnt.size(), s));
     MPG_CUDA(c, dupload(j.itSlot, itSlot.data(), (int64_t)itSlot.size(), s));
     MPG_CUDA(c, dupload(j.rdBlk, rdBlk.data(), (int64_t)rdBlk.size(), s));
     MPG_CUDA(c, dupload(j.rdSlot0, rdSlot0.data(), (int64_t)rdSlot0.size(), s));
@@ -760,6 +758,7 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     FitParams fp{};
     fp.rec = j.rec; fp.inder = j.inder; fp.glder = j.glder; fp.meas = j.meas;
     fp.slots = j.slots; fp.swStart = j.swStart; fp.sw = j.sw; fp.gpar = j.gpar;
+    fp.grpSlot = j.grpSlot; fp.pairDst = j.pairDst;
     fp.varOfTot = j.varOfTot; fp.fileWeight = j.fileWeight;
     fp.icalcm = opt->icalcm; fp.nloopn = opt->nloopn; fp.lhuber = opt->lhuber; fp.lfitbb = opt->lfitbb;
     fp.chicut = opt->chicut; fp.chhuge = opt->chhuge; fp.dwcut = opt->dwcut; fp.cndlmx = opt->cndlmx;
@@ -768,12 +767,13 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.wmax = std::max(j.maxNw, 1); fp.neqmax = std::max(j.maxNeq, 1);
     fp.nalcmax = std::max(j.maxNalc, 1); fp.nalgmax = std::max(j.maxNalg, 1);
     fp.bandmax = opt->lfitbb > 0 ? j.maxBand : -1; fp.bdrmax = j.maxBdr;
+    fp.ngrpmax = std::max(j.maxNgrp, 1);
     fp.errFlag = errFlag;
     if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     AccParams ap{};
     ap.bkI = j.bkI; ap.bkJ = j.bkJ; ap.bkLd = j.bkLd; ap.bkOff = j.bkOff;
-    ap.itBlk = j.itBlk; ap.itE0 = j.itE0; ap.itE1 = j.itE1; ap.itSlot = j.itSlot;
-    ap.bEntries = j.bEntries; ap.rdBlk = j.rdBlk; ap.rdSlot0 = j.rdSlot0; ap.rdN = j.rdN;
+    ap.itBlk = j.itBlk; ap.itBase = j.itBase; ap.itCnt = j.itCnt; ap.itSlot = j.itSlot;
+    ap.rdBlk = j.rdBlk; ap.rdSlot0 = j.rdSlot0; ap.rdN = j.rdN;
     ap.partial = j.partial; ap.pstride = j.pstride; ap.vEntries = j.vEntries;
     ap.status = j.status; ap.stage = j.stage; ap.vstage = j.vstage; ap.slotCnt = j.slotCnt;
     ap.aig = j.aig; ap.nG = j.nG; ap.matsto = j.matsto;

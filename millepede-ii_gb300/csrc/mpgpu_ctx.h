@@ -19,7 +19,7 @@ struct alignas(16) RecInfo {
     int64_t w0;        // first word (error-count word) in the record arrays
     int64_t measOff;   // first equation in the measurement table
     int64_t slotOff;   // first entry of the per-slot arrays (stride nalg+1)
-    int64_t updOff;    // first element of the update matrix in the chunk staging
+    int64_t pairOff;   // first of the record's group pairs in the pair-destination table
     int64_t swOff;     // first entry of the slot-word lists
     int64_t grpOff;    // first entry of the group list
     int32_t nw, neq, nalc, nalg;
@@ -86,9 +86,10 @@ struct DevJob {
     int64_t *bkOff = nullptr;          // sparse: offset of element (0,0)
     std::vector<int64_t> chunkItem;    // [nchunk+1]
     int32_t *itBlk = nullptr;
-    int64_t *itE0 = nullptr, *itE1 = nullptr;
+    int64_t *itBase = nullptr;         // staging offset of the item's first record block
+    int32_t *itCnt = nullptr;          // records in the item
     int64_t *itSlot = nullptr;         // partial slot, -1: write the matrix directly
-    int64_t *bEntries = nullptr;
+    int64_t *pairDst = nullptr;        // per record group pair: staging offset of its block
     std::vector<int64_t> chunkRed;     // [nchunk+1] blocks with several items
     int32_t *rdBlk = nullptr;
     int64_t *rdSlot0 = nullptr;
@@ -102,7 +103,7 @@ struct DevJob {
     double *stage = nullptr;
     int64_t stageLen = 0;
     // limits over the job (fit kernel shared memory sizing)
-    int32_t maxNw = 0, maxNeq = 0, maxNalc = 0, maxNalg = 0, maxBand = -1, maxBdr = 0;
+    int32_t maxNw = 0, maxNeq = 0, maxNalc = 0, maxNalg = 0, maxBand = -1, maxBdr = 0, maxNgrp = 1;
     int32_t nbndr[2] = {0, 0}, nbdrx = 0, nbndx = 0;
     // constraints (QL of the constraint matrix, kept on the device)
     int32_t ncon = 0;
@@ -140,6 +141,8 @@ struct FitParams {
     const int32_t *slots;
     const int32_t *swStart;
     const int32_t *sw;
+    const int32_t *grpSlot;
+    const int64_t *pairDst;
     const double *gpar;
     const int32_t *varOfTot;
     const double *fileWeight;
@@ -152,7 +155,7 @@ struct FitParams {
     double *chi2add;
     int32_t *ndfadd;
     float *chndf;
-    int32_t wmax, neqmax, nalcmax, nalgmax, bandmax, bdrmax;  // shared-memory sizing
+    int32_t wmax, neqmax, nalcmax, nalgmax, bandmax, bdrmax, ngrpmax;  // shared-memory sizing
     int32_t *errFlag;
 };
 
@@ -163,9 +166,8 @@ cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s
 struct AccParams {
     const int32_t *bkI, *bkJ, *bkLd;
     const int64_t *bkOff;
-    const int32_t *itBlk;
-    const int64_t *itE0, *itE1, *itSlot;
-    const int64_t *bEntries;
+    const int32_t *itBlk, *itCnt;
+    const int64_t *itBase, *itSlot;
     int64_t item0, nitem;          // items of this chunk
     const int32_t *rdBlk;
     const int64_t *rdSlot0;

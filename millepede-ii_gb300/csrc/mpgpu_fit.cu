@@ -448,7 +448,7 @@ struct WarpMem {
     double *gl, *rm1, *lcor, *lwgt, *res, *t1, *t2, *w0, *clmat, *blvec, *diag, *ocol, *scol;
     double *B, *W;
     double *bnd;   // band scratch (may be null)
-    int32_t *in, *mq, *slots, *swS, *sw, *used;
+    int32_t *in, *mq, *slots, *swS, *sw, *used, *goff;
 };
 
 __host__ __device__ inline int64_t align8(int64_t x) { return (x + 7) & ~int64_t(7); }
@@ -461,7 +461,7 @@ __host__ __device__ inline int64_t band_doubles(int nalc, int bandmax, int bdrma
 }
 
 __host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax, int nalgmax,
-                                              int bandmax, int bdrmax) {
+                                              int bandmax, int bdrmax, int ngrpmax) {
     int64_t d = 0;
     d += wmax;                          // gl
     d += 7 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2 w0
@@ -475,6 +475,7 @@ __host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax,
     i += nalgmax + 1;     // swS
     i += wmax;            // sw
     i += nalcmax + 2;     // used / scflag
+    i += ngrpmax + 2;     // goff
     return align8(d * 8 + i * 4 + 64);
 }
 
@@ -504,9 +505,63 @@ __device__ WarpMem carve(char *base, const FitParams &p) {
     m.slots = q; q += p.nalgmax;
     m.swS = q; q += p.nalgmax + 1;
     m.sw = q; q += p.wmax;
-    m.used = q;
+    m.used = q; q += p.nalcmax + 2;
+    m.goff = q;
     return m;
 }
+
+// Walk over the update elements of one record in block-major order: group
+// pairs (qa >= qb), inside a pair row-major (ii, jj) with jj <= ii when
+// qa == qb.  goff[q] = first slot of group q, goff[ngrp] = nalg.
+struct BlockWalk {
+    const int32_t *goff;
+    int ngrp;
+    int qa = 0, qb = 0, e = 0;     // current pair and element inside it
+    int ii = 0, jj = 0;
+    __device__ __forceinline__ BlockWalk(const int32_t *g, int n) : goff(g), ngrp(n) {}
+    __device__ __forceinline__ int size(int q) const { return goff[q + 1] - goff[q]; }
+    __device__ __forceinline__ int nel() const {
+        const int na = size(qa);
+        return qa == qb ? na * (na + 1) / 2 : na * size(qb);
+    }
+    // move n elements ahead (n <= 32)
+    __device__ __forceinline__ void advance(int n) {
+        if (qa >= ngrp) return;
+        e += n;
+        if (e < nel()) {  // same block: step the row and column
+            jj += n;
+            if (qa == qb) {
+                while (jj > ii) { jj -= ii + 1; ii++; }
+            } else {
+                const int nj = size(qb);
+                ii += jj / nj;
+                jj -= (jj / nj) * nj;
+            }
+            return;
+        }
+        for (int guard = 0; guard < 1 << 20; ++guard) {
+            const int ne = nel();
+            if (e < ne) break;
+            e -= ne;
+            if (++qb > qa) { qa++; qb = 0; }
+            if (qa >= ngrp) return;
+        }
+        // e < 32 here
+        if (qa == qb) {
+            int r = 0;
+            while ((r + 1) * (r + 2) / 2 <= e) r++;
+            ii = r;
+            jj = e - r * (r + 1) / 2;
+        } else {
+            const int nj = size(qb);
+            ii = e / nj;
+            jj = e - ii * nj;
+        }
+    }
+    __device__ __forceinline__ int a() const { return goff[qa] + ii; }
+    __device__ __forceinline__ int b() const { return goff[qb] + jj; }
+    __device__ __forceinline__ int pair() const { return qa * (qa + 1) / 2 + qb; }
+};
 
 __device__ __forceinline__ double wsum_serial(const double *a, int n) {
     // sequential sum in index order on lane 0, broadcast to the warp
@@ -534,6 +589,12 @@ k_fit(FitParams p, int perWarp) {
         for (int i = ln; i < 3 * neq; i += 32) m.mq[i] = p.meas[3 * ri.measOff + i];
         for (int i = ln; i < nalg; i += 32) m.slots[i] = p.slots[ri.slotOff + i];
         for (int i = ln; i <= nalg; i += 32) m.swS[i] = p.swStart[ri.slotOff + i];
+        const int ngrp = ri.ngrp;
+        const int64_t *pdst = p.pairDst + ri.pairOff;  // staging offset per group pair
+        if (p.icalcm == 1 && nalc > 0) {
+            for (int i = ln; i < ngrp; i += 32) m.goff[i] = p.grpSlot[ri.grpOff + i];
+            if (ln == 0) m.goff[ngrp] = nalg;
+        }
         __syncwarp();
         const int nswr = m.swS[nalg];
         for (int i = ln; i < nswr; i += 32) m.sw[i] = p.sw[ri.swOff + i];
@@ -788,12 +849,15 @@ k_fit(FitParams p, int perWarp) {
                         }
                     }
                     __syncwarp();
-                    // U(a,b) = -sum_eq dw1 w g_a g_b + sum_k W(a,k) B(b,k), a >= b
-                    double *U = p.stage + ri.updOff;
+                    // U(a,b) = -sum_eq dw1 w g_a g_b + sum_k W(a,k) B(b,k), a >= b,
+                    // written block by block (group pairs qa >= qb, rows ii,
+                    // columns jj <= ii on diagonal blocks) to the staging
+                    // position of the block's record list
+                    BlockWalk bw(m.goff, ngrp);
+                    bw.advance(ln);
                     const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
-                    int a = 0, b = ln;
-                    while (b > a) { b -= a + 1; a++; }
                     for (int64_t idx = ln; idx < ngg; idx += 32) {
+                        const int a = bw.a(), b = bw.b();
                         double u = 0.0;
                         // Gt W G: equations shared by slots a and b (merge of the
                         // equation-ordered word lists), pair taken in the
@@ -804,7 +868,6 @@ k_fit(FitParams p, int perWarp) {
                             const int ea = m.sw[qa] >> 16, eb = m.sw[qb] >> 16;
                             if (ea < eb) { qa++; continue; }
                             if (eb < ea) { qb++; continue; }
-                            // same equation: all word pairs of a and b in it
                             int qa2 = qa, qb2 = qb;
                             while (qa2 < qae && (m.sw[qa2] >> 16) == ea) qa2++;
                             while (qb2 < qbe && (m.sw[qb2] >> 16) == ea) qb2++;
@@ -823,18 +886,21 @@ k_fit(FitParams p, int perWarp) {
                         }
                         const double *wa = m.W + a * nalc;
                         for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], m.B[k * nalg + b], u);
-                        U[idx] = u;
-                        b += 32;
-                        while (b > a) { b -= a + 1; a++; }
+                        p.stage[__ldg(pdst + bw.pair()) + bw.e] = u;
+                        bw.advance(32);
                     }
                 }
             }
         }
         if (st != 0 && p.icalcm == 1 && nalc > 0) {
             // a rejected record contributes an all-zero update
-            double *U = p.stage + ri.updOff;
+            BlockWalk bw(m.goff, ngrp);
+            bw.advance(ln);
             const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
-            for (int64_t idx = ln; idx < ngg; idx += 32) U[idx] = 0.0;
+            for (int64_t idx = ln; idx < ngg; idx += 32) {
+                p.stage[__ldg(pdst + bw.pair()) + bw.e] = 0.0;
+                bw.advance(32);
+            }
         }
         if (ln == 0) {
             p.status[r] = (int8_t)st;
@@ -849,7 +915,7 @@ k_fit(FitParams p, int perWarp) {
 }  // namespace
 
 int fit_smem_per_warp(const FitParams &p) {
-    return (int)warp_bytes(p.wmax, p.neqmax, p.nalcmax, p.nalgmax, p.bandmax, p.bdrmax);
+    return (int)warp_bytes(p.wmax, p.neqmax, p.nalcmax, p.nalgmax, p.bandmax, p.bdrmax, p.ngrpmax);
 }
 
 // warps per CTA so that one CTA fits the 227 KB of shared memory
