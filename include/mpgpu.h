@@ -141,6 +141,22 @@ int32_t mpgpu_loopbf_device(mpgpu_ctx *ctx, const mpgpu_fitopts *opt,
  * += vadd) is applied when vidx != NULL. */
 int32_t mpgpu_mupdat(mpgpu_ctx *ctx, int32_t n, const int32_t *i, const int32_t *j,
                      const double *add);
+
+/* mpgpu_mupdat without any device allocation.  This entry point has no
+ * counterpart in the reference (pede's mupdat adds to host memory).  It is
+ * for callers that must not allocate or free device memory during the call:
+ * a host loop that adds terms while other streams keep the device busy
+ * (cudaFree would wait for all of them), or a job whose matrix and staging
+ * fill the device memory.  The triplets are staged in a fixed device area of
+ * MPGPU_MUPDAT_NOALLOC_MAX elements reserved when the library is loaded;
+ * larger n returns MPGPU_ERR_LIMIT and changes nothing.  The area is one per
+ * device and shared by all contexts on it: calls that overlap in time on the
+ * same device race on it, so serialise them.  The first call on a device
+ * looks up the area's address once; make it before any stream capture is
+ * begun on that device.  Same result and error codes as mpgpu_mupdat. */
+#define MPGPU_MUPDAT_NOALLOC_MAX 65536
+int32_t mpgpu_mupdat_noalloc(mpgpu_ctx *ctx, int32_t n, const int32_t *i, const int32_t *j,
+                             const double *add);
 int32_t mpgpu_vector_add(mpgpu_ctx *ctx, int32_t n, const int32_t *vidx, const double *vadd);
 
 int32_t mpgpu_download_matrix(mpgpu_ctx *ctx, double *globalMatD);

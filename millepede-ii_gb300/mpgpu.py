@@ -108,7 +108,7 @@ def lib():
 EXPORTS = [
     "mpgpu_create", "mpgpu_destroy", "mpgpu_last_error", "mpgpu_set_layout",
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
-    "mpgpu_mupdat", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
+    "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
     "mpgpu_host_register", "mpgpu_host_unregister",
     "mpgpu_host_labels",
@@ -351,6 +351,14 @@ class Context:
         add = np.ascontiguousarray(add, np.float64)
         self.check(self.L.mpgpu_mupdat(self.h, C.c_int32(len(i)), ptr(i, i32p), ptr(j, i32p),
                                        ptr(add, f64p)))
+
+    def mupdat_noalloc(self, i, j, add):
+        """mupdat through the entry point that stages in a fixed device area."""
+        i = np.ascontiguousarray(i, np.int32)
+        j = np.ascontiguousarray(j, np.int32)
+        add = np.ascontiguousarray(add, np.float64)
+        self.check(self.L.mpgpu_mupdat_noalloc(self.h, C.c_int32(len(i)), ptr(i, i32p),
+                                               ptr(j, i32p), ptr(add, f64p)))
 
     def solve(self, metsol, consResiduals=None, rtol=1e-10, itnlim=2000, errors=False):
         corr = np.zeros(self.nVar, np.float64)
