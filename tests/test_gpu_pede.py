@@ -9,8 +9,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def gpu_job(mp, orc, d, steer):
-    job, keep = orc.make_job(d)
+def gpu_job(mp, orc, d, steer, **jobkw):
+    job, keep = orc.make_job(d, **jobkw)
     cap = len(d["inder"]) + 16
     res, kr = orc.make_result(cap, cls=mp.Result)
     st = mp.Steer(**{f: getattr(steer, f) for f, _ in mp.Steer._fields_})
