@@ -1,0 +1,182 @@
+"""Known-answer tests of the CPU oracle's numerical kernels against numpy /
+scipy on the same inputs: the local solvers (sqminv, bordered band
+sqmibb/sqmibb2), the global solvers (sqminl, chdec2/chslv2, MINRES), the
+QL constraint elimination and the chindl table.  Tolerances: 1e-11
+relative for direct solvers on well-conditioned matrices, 1e-9 for MINRES
+at rtol 1e-13, 2e-3 for chindl up to 30 degrees of freedom (its table has 4-5
+significant digits) and 5e-2 above (Fisher's approximation)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_ref as O
+
+f64p = C.POINTER(C.c_double)
+i32p = C.POINTER(C.c_int32)
+
+
+def p(a):
+    return a.ctypes.data_as(f64p)
+
+
+def packed(M):
+    """lower triangle by rows, (i*i+i)/2 + j (0-based)"""
+    return np.ascontiguousarray(M[np.tril_indices(len(M))], np.float64)
+
+
+def unpack(v, n):
+    M = np.zeros((n, n))
+    M[np.tril_indices(n)] = v
+    return M + np.tril(M, -1).T
+
+
+def spd(n, rng, pattern=None):
+    A = rng.normal(size=(n, n))
+    A = A + A.T
+    if pattern is not None:
+        A = np.where(pattern, A, 0.0)
+    A += np.diag(np.sum(np.abs(A), axis=1) + 1.0)
+    return A
+
+
+def rel(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("fn,n", [("mpref_sqminv", 5), ("mpref_sqminv", 17), ("mpref_sqminl", 60)])
+def test_gauss_jordan_inverse(orc, fn, n):
+    rng = np.random.default_rng(n)
+    A = spd(n, rng)
+    b = rng.normal(size=n)
+    v, x = packed(A), b.copy()
+    rank = C.c_int32()
+    getattr(O.lib(), fn)(p(v), p(x), C.c_int32(n), C.byref(rank))
+    assert rank.value == n
+    assert rel(unpack(v, n), np.linalg.inv(A)) <= 1e-11
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-11
+
+
+def test_sqminv_rank_deficit(orc):
+    rng = np.random.default_rng(1)
+    B = rng.normal(size=(6, 4))
+    A = B @ B.T  # rank 4
+    v, x = packed(A), rng.normal(size=6)
+    rank = C.c_int32()
+    O.lib().mpref_sqminv(p(v), p(x), C.c_int32(6), C.byref(rank))
+    assert rank.value == 4
+
+
+@pytest.mark.parametrize("side", [1, 2])
+@pytest.mark.parametrize("inv", [1, 2])
+def test_bordered_band(orc, side, inv):
+    n, nbdr, nbnd = 14, 3, 2
+    rng = np.random.default_rng(10 * side + inv)
+    idx = np.arange(n)
+    bdr = idx < nbdr if side == 1 else idx >= n - nbdr
+    band = np.abs(idx[:, None] - idx[None, :]) <= nbnd
+    pattern = band | bdr[:, None] | bdr[None, :]
+    A = spd(n, rng, pattern)
+    b = rng.normal(size=n)
+    v, x = packed(A), b.copy()
+    rank, emin, emax = C.c_int32(), C.c_double(), C.c_double()
+    fn = O.lib().mpref_sqmibb if side == 1 else O.lib().mpref_sqmibb2
+    fn(p(v), p(x), C.c_int32(n), C.c_int32(nbdr), C.c_int32(nbnd), C.c_int32(inv),
+       C.byref(rank), C.byref(emin), C.byref(emax))
+    assert rank.value == n
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-11
+    Ai = np.linalg.inv(A)
+    got = unpack(v, n)
+    if inv == 2:
+        assert rel(got, Ai) <= 1e-11
+    else:  # band part of the inverse and the border rows
+        assert rel(got[pattern], Ai[pattern]) <= 1e-11
+    assert 0 < emin.value <= emax.value
+
+
+def test_cholesky(orc):
+    n = 40
+    rng = np.random.default_rng(7)
+    A = spd(n, rng)
+    b = rng.normal(size=n)
+    g = packed(A)
+    rank, evmax, evmin = C.c_int32(), C.c_double(), C.c_double()
+    O.lib().mpref_chdec2(p(g), C.c_int32(n), C.byref(rank), C.byref(evmax), C.byref(evmin))
+    assert rank.value == n
+    x = b.copy()
+    O.lib().mpref_chslv2(p(g), p(x), C.c_int32(n))
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-11
+
+
+def ql(npar, ncon, rng):
+    A = np.ascontiguousarray(rng.normal(size=(ncon, npar)))
+    L = O.lib()
+    L.mpref_ql_create.restype = C.c_void_p
+    h = L.mpref_ql_create(C.c_int32(npar), C.c_int32(ncon), p(A))
+    return A, h
+
+
+def ql_apply(h, x, t):
+    y = np.ascontiguousarray(x, np.float64).copy()
+    O.lib().mpref_ql_mlq(C.c_void_p(h), p(y), C.c_int32(t))
+    return y
+
+
+def test_ql_elimination(orc):
+    npar, ncon = 30, 4
+    rng = np.random.default_rng(3)
+    A, h = ql(npar, ncon, rng)
+    try:
+        Q = np.stack([ql_apply(h, e, 0) for e in np.eye(npar)], axis=1)
+        assert rel(Q.T @ Q, np.eye(npar)) <= 1e-13
+        # Q^T C^T: the constraints live in the last ncon coordinates only
+        QtCt = np.stack([ql_apply(h, A[k], 1) for k in range(ncon)], axis=1)
+        assert np.max(np.abs(QtCt[: npar - ncon])) <= 1e-13 * np.max(np.abs(A))
+        # qlbsub: y with (Q^T C^T)^T restricted to the last rows times y = d
+        d = rng.normal(size=ncon)
+        y = np.zeros(ncon)
+        O.lib().mpref_ql_bsub(C.c_void_p(h), p(d), p(y))
+        x = np.zeros(npar)
+        x[npar - ncon:] = y
+        assert rel(A @ ql_apply(h, x, 0), d) <= 1e-12
+        # qlssq (t=1) gives Q^T M Q on the block that is kept
+        M = spd(npar, rng)
+        v = packed(M)
+        O.lib().mpref_ql_ssq_packed(C.c_void_p(h), p(v), C.c_int32(1))
+        m = npar - ncon
+        assert rel(unpack(v, npar)[:m, :m], (Q.T @ M @ Q)[:m, :m]) <= 1e-12
+    finally:
+        O.lib().mpref_ql_destroy(C.c_void_p(h))
+
+
+def test_minres_packed(orc):
+    n = 80
+    rng = np.random.default_rng(9)
+    A = spd(n, rng)
+    b = rng.normal(size=n)
+    x = np.zeros(n)
+    itn = C.c_int32()
+    aig = np.arange(1, n + 2, dtype=np.int32)
+    L = O.lib()
+    istop = L.mpref_minres_sparse(C.c_int32(1), C.c_int32(n), C.c_int32(n),
+                                  aig.ctypes.data_as(i32p), None, None, p(packed(A)), None,
+                                  p(b), p(x), C.c_double(1e-13), C.c_int32(1000), C.byref(itn))
+    assert istop in (1, 2, 3)
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-9
+
+
+def test_chindl(orc):
+    from scipy.stats import chi2, norm
+    f = O.lib().mpref_chindl
+    f.restype = C.c_float
+    for m in (1, 2, 3):
+        prob = 2.0 * norm.sf(m)
+        for nd in (1, 2, 5, 10, 30, 31, 60, 200):
+            want = chi2.isf(prob, nd) / nd
+            # above 30 the reference uses Fisher's sqrt(2 chi2) approximation
+            tol = 2e-3 if nd <= 30 else 5e-2
+            assert abs(f(m, nd) - want) <= tol * want, (m, nd, f(m, nd), want)
+            if nd > 30:
+                sn = (0.47523, 1.690140, 2.782170)[m - 1]
+                fisher = np.float32((sn + np.sqrt(np.float32(2 * nd - 1))) ** 2 / (2 * nd))
+                assert abs(f(m, nd) - fisher) <= 1e-6 * fisher
