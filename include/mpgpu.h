@@ -59,7 +59,7 @@ typedef struct mpgpu_ctx mpgpu_ctx;
 typedef struct mpgpu_cfg {
     int32_t device;             /* CUDA device ordinal */
     int32_t flags;              /* reserved, 0 */
-    int64_t staging_bytes;      /* per-record update staging (0: default 4 GiB) */
+    int64_t staging_bytes;      /* update staging per chunk (0: sized per job, one chunk when it fits) */
 } mpgpu_cfg;
 
 int32_t mpgpu_create(mpgpu_ctx **ctx, const mpgpu_cfg *cfg);

@@ -65,18 +65,29 @@ namespace {
 // part of each record's update that falls in a block to the staging position
 // base + k * nel, k the record's rank among the block's records of the chunk
 // (elements row-major, lower triangle on diagonal blocks), so an item is one
-// contiguous cnt x nel array.  Blocks of more than kSmallEl elements: lane l
-// owns elements l, l+32, ... and adds the records in record order (coalesced
-// rows).  Smaller blocks: lane l adds the records l, l+32, ... and the 32
-// lane sums are combined by a fixed shuffle tree.  Blocks crossed by many
-// tracks are split into several items whose sums are added in item order by
-// k_acc_block_reduce.  Item boundaries are fixed, so every element receives
-// its sum in the same order on every run.  Rejected records carry zeros.
+// contiguous cnt x nel array.
+//
+// Flat mode (L = lcm(32, nel) <= kFlatMax): the warp streams the array as
+// flat words f = lane + 32 k; word f belongs to element f mod nel and is
+// added to the shared-memory slot f mod L, which the same lane always owns.
+// Every lane does useful work on every load whatever nel is, and each slot
+// sums its records in record order.  The L / nel slots of an element are
+// then added in slot order.  Larger blocks: lane per element, records in
+// order.  Blocks crossed by many tracks are split into several items whose
+// sums are added in item order by k_acc_block_reduce.  Item boundaries are
+// fixed, so every element receives its sum in the same order on every run.
+// Rejected records carry zeros.
 constexpr int kAccWarps = 8;
-constexpr int kSmallEl = 8;   // lane-per-record at or below this block size
-constexpr int kLaneEl = 4;    // element accumulators per lane (128 elements per pass)
-constexpr int kUnroll = 4;    // records loaded ahead of the adds
-constexpr int kTileV = 8;     // vector elements per pass
+constexpr int kFlatMax = 768;   // slots per warp (6 KB)
+constexpr int kLaneEl = 4;      // element accumulators per lane (128 elements per pass)
+constexpr int kUnroll = 4;      // loads issued ahead of the adds
+constexpr int kTileV = 8;       // vector elements per pass
+
+__host__ __device__ inline int gcd32(int nel) {
+    int g = 32;
+    while ((nel % g) != 0) g >>= 1;
+    return g;
+}
 
 // element t of a block (row-major, lower triangle when diagonal) -> (ii, jj)
 __device__ __forceinline__ void blk_elem(int32_t t, bool diag, int32_t nj, int32_t &ii, int32_t &jj) {
@@ -109,8 +120,41 @@ __device__ __forceinline__ void blk_store(const AccParams &p, int32_t blk, int64
     }
 }
 
+// lane-per-element pass over nq (1..kLaneEl) accumulators per lane
+template <int NQ>
+__device__ __forceinline__ void acc_lane_elements(const AccParams &p, const double *col, int32_t cnt,
+                                                  int32_t nel, int32_t lim, int32_t t, int32_t blk,
+                                                  int64_t slot, bool diag, int32_t ia, int32_t ja,
+                                                  int32_t nj) {
+    double a[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) a[q] = 0.0;
+    int32_t r = 0;
+    for (; r + kUnroll <= cnt; r += kUnroll) {
+        double v[kUnroll][NQ];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q)
+                v[u][q] = 32 * q < lim ? __ldg(col + (int64_t)(r + u) * nel + 32 * q) : 0.0;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) a[q] += v[u][q];
+    }
+    for (; r < cnt; ++r)
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+            if (32 * q < lim) a[q] += __ldg(col + (int64_t)r * nel + 32 * q);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+        if (32 * q < lim) blk_store(p, blk, slot, t + 32 * q, diag, ia, ja, nj, a[q]);
+}
+
 __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
+    extern __shared__ __align__(16) double accs[];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    double *acc = accs + wib * kFlatMax;
     const int64_t w = (int64_t)blockIdx.x * kAccWarps + wib;
     const int64_t nw = (int64_t)gridDim.x * kAccWarps;
     for (int64_t it = p.item0 + w; it < p.item0 + p.nitem; it += nw) {
@@ -123,52 +167,51 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_acc_blocks(AccParams p) {
         const int64_t slot = p.itSlot[it];
         const int32_t cnt = p.itCnt[it];
         const double *src = p.stage + p.itBase[it];
-        if (nel <= kSmallEl) {
-            double a[kSmallEl];
+        const int32_t L = 32 * (nel / gcd32(nel));
+        // FP64 adds issued per warp: flat ~ cnt nel / 32 + L / nel (slot
+        // reduction), lane per element cnt ceil(nel / 32)
+        const int64_t costFlat = ((int64_t)cnt * nel + 31) / 32 + L / nel;
+        const int64_t costLane = (int64_t)cnt * ((nel + 31) / 32);
+        if (L <= kFlatMax && costFlat < costLane) {
+            const int32_t R = L / 32;
+            for (int32_t q = ln; q < L; q += 32) acc[q] = 0.0;
+            __syncwarp();
+            const int64_t total = (int64_t)cnt * nel;
+            double *mine = acc + ln;
+            int32_t kr = 0;
+            int64_t f = ln;
+            for (; f + 32 * (kUnroll - 1) < total; f += 32 * kUnroll) {
+                double v[kUnroll];
 #pragma unroll
-            for (int q = 0; q < kSmallEl; ++q) a[q] = 0.0;
-            for (int32_t r = ln; r < cnt; r += 32) {
-                const double *row = src + (int64_t)r * nel;
+                for (int u = 0; u < kUnroll; ++u) v[u] = __ldg(src + f + 32 * u);
 #pragma unroll
-                for (int q = 0; q < kSmallEl; ++q)
-                    if (q < nel) a[q] += __ldg(row + q);
+                for (int u = 0; u < kUnroll; ++u) {
+                    mine[32 * kr] += v[u];
+                    kr = kr + 1 == R ? 0 : kr + 1;
+                }
             }
-#pragma unroll
-            for (int q = 0; q < kSmallEl; ++q) {
-                if (q >= nel) break;
-                double v = a[q];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-                if (ln == 0) blk_store(p, blk, slot, q, diag, ia, ja, nj, v);
+            for (; f < total; f += 32) {
+                mine[32 * kr] += __ldg(src + f);
+                kr = kr + 1 == R ? 0 : kr + 1;
             }
+            __syncwarp();
+            const int32_t per = L / nel;
+            for (int32_t t = ln; t < nel; t += 32) {
+                double sum = 0.0;
+                for (int32_t m = 0; m < per; ++m) sum += acc[t + nel * m];
+                blk_store(p, blk, slot, t, diag, ia, ja, nj, sum);
+            }
+            __syncwarp();
             continue;
         }
         for (int32_t t0 = 0; t0 < nel; t0 += 32 * kLaneEl) {
             const int32_t lim = nel - t0 - ln;  // element q of the lane valid when 32 q < lim
+            const int32_t nq = min(kLaneEl, (nel - t0 + 31) / 32);
             const double *col = src + t0 + ln;
-            double a[kLaneEl];
-#pragma unroll
-            for (int q = 0; q < kLaneEl; ++q) a[q] = 0.0;
-            int32_t r = 0;
-            for (; r + kUnroll <= cnt; r += kUnroll) {
-                double v[kUnroll][kLaneEl];
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-#pragma unroll
-                    for (int q = 0; q < kLaneEl; ++q)
-                        v[u][q] = 32 * q < lim ? __ldg(col + (int64_t)(r + u) * nel + 32 * q) : 0.0;
-#pragma unroll
-                for (int u = 0; u < kUnroll; ++u)
-#pragma unroll
-                    for (int q = 0; q < kLaneEl; ++q) a[q] += v[u][q];
-            }
-            for (; r < cnt; ++r)
-#pragma unroll
-                for (int q = 0; q < kLaneEl; ++q)
-                    if (32 * q < lim) a[q] += __ldg(col + (int64_t)r * nel + 32 * q);
-#pragma unroll
-            for (int q = 0; q < kLaneEl; ++q)
-                if (32 * q < lim) blk_store(p, blk, slot, t0 + ln + 32 * q, diag, ia, ja, nj, a[q]);
+            if (nq == 1) acc_lane_elements<1>(p, col, cnt, nel, lim, t0 + ln, blk, slot, diag, ia, ja, nj);
+            else if (nq == 2) acc_lane_elements<2>(p, col, cnt, nel, lim, t0 + ln, blk, slot, diag, ia, ja, nj);
+            else if (nq == 3) acc_lane_elements<3>(p, col, cnt, nel, lim, t0 + ln, blk, slot, diag, ia, ja, nj);
+            else acc_lane_elements<4>(p, col, cnt, nel, lim, t0 + ln, blk, slot, diag, ia, ja, nj);
         }
     }
 }
@@ -343,10 +386,13 @@ __global__ void k_mupdat(int32_t n, const int32_t *iv, const int32_t *jv, const 
 
 cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
     if (p.icalcm == 1 && p.nitem > 0) {
+        const int smem = kAccWarps * kFlatMax * (int)sizeof(double);
+        cudaError_t e = cudaFuncSetAttribute(k_acc_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
         int64_t blocks = (p.nitem + kAccWarps - 1) / kAccWarps;
-        const int64_t maxb = (int64_t)nsm * 8;
+        const int64_t maxb = (int64_t)nsm * 4;
         if (blocks > maxb) blocks = maxb;
-        k_acc_blocks<<<(unsigned)blocks, 32 * kAccWarps, 0, s>>>(p);
+        k_acc_blocks<<<(unsigned)blocks, 32 * kAccWarps, smem, s>>>(p);
         if (p.nred > 0) {
             int64_t rb = (p.nred + 7) / 8;
             if (rb > (int64_t)nsm * 8) rb = (int64_t)nsm * 8;

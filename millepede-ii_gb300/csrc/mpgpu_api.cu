@@ -125,7 +125,7 @@ extern "C" int32_t mpgpu_create(mpgpu_ctx **out, const mpgpu_cfg *cfg) {
     *out = nullptr;
     mpgpu_ctx *c = new mpgpu_ctx();
     c->device = cfg ? cfg->device : 0;
-    c->stagingBytes = (cfg && cfg->staging_bytes > 0) ? cfg->staging_bytes : (int64_t)4 << 30;
+    c->stagingBytes = (cfg && cfg->staging_bytes > 0) ? cfg->staging_bytes : 0;  // 0: sized per job
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
@@ -341,7 +341,9 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     std::vector<int64_t> errAt(nthreads_host() + 1, -1);
     parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
         std::vector<Eq> eqs;
-        std::vector<int32_t> stamp(nVar + 1, 0), ibandh;
+        std::vector<int32_t> stamp(nVar + 1, 0), ibandh, eqStamp(nVar + 1, 0);
+        std::vector<int32_t> gStamp(j.nG + 1, 0), gCnt(j.nG + 1, 0), eqGroups;
+        int32_t eqTag = 0;
         std::vector<int32_t> sl;
         for (int64_t r = a; r < b; ++r) {
             RecInfo &ri = rec[r];
@@ -383,6 +385,30 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
             nalg = (int32_t)sl.size();
             ri.nalc = nalc;
             ri.nalg = nalg;
+            // every equation carries the local derivatives 1..nalc in order
+            // (fast normal equations); no variable parameter twice in one
+            // equation (lockstep word lists in the update)
+            bool denseLoc = nalc > 0, simpleWords = true;
+            for (const Eq &e : eqs) {
+                if (e.sg - e.sl - 1 != nalc) denseLoc = false;
+                for (int32_t q = e.sl + 1; denseLoc && q < e.sg; ++q)
+                    if (in[q] != q - e.sl) denseLoc = false;
+                // ... and every group it touches complete (then all slots of a
+                // group have the same equation list)
+                ++eqTag;
+                eqGroups.clear();
+                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
+                    const int32_t v = varOfTot[in[q] - 1];
+                    if (v <= 0) continue;
+                    if (eqStamp[v] == eqTag) simpleWords = false;
+                    eqStamp[v] = eqTag;
+                    const int32_t g = p2g[v - 1];
+                    if (gStamp[g] != eqTag) { gStamp[g] = eqTag; gCnt[g] = 0; eqGroups.push_back(g); }
+                    gCnt[g]++;
+                }
+                for (int32_t g : eqGroups)
+                    if (gCnt[g] != aig[g] - aig[g - 1]) simpleWords = false;
+            }
             // groups of the sorted variable parameters; the record must hold
             // complete groups (loopbf's npar == nalg check, pede.f90:3710-3724)
             std::sort(sl.begin(), sl.end());
@@ -429,7 +455,8 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
                 }
                 if (kx > 0) { ri.mbnd = (int16_t)(kx - 2); ri.mbdr = (int16_t)kbdrx; ri.mside = side; }
             }
-            ri.mside = (ri.mside & 0xff) | (nonmono ? 0x100 : 0);
+            ri.mside = (ri.mside & 0xff) | (nonmono ? 0x100 : 0) | (denseLoc ? 0x200 : 0) |
+                       (simpleWords ? 0x400 : 0);
             ri.measOff = nsw;  // temporarily: number of slot words
         }
     });
@@ -445,7 +472,21 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     j.maxNw = j.maxNeq = j.maxNalc = j.maxNalg = 0;
     j.maxBand = -1; j.maxBdr = 0; j.maxNgrp = 1;
     j.nbndr[0] = j.nbndr[1] = 0; j.nbdrx = j.nbndx = 0;
-    const int64_t stageElems = std::max<int64_t>(c->stagingBytes / 8, 1);
+    int64_t stageElems = std::max<int64_t>(c->stagingBytes / 8, 1);
+    if (c->stagingBytes <= 0) {
+        // sized per job: all updates of the loop in one chunk when that fits
+        // in the free device memory left after the record tables (estimated
+        // generously as twice the record words), else two chunk buffers of
+        // half the room each
+        int64_t need = 0;
+        for (int64_t r = 0; r < nrec; ++r)
+            if (rec[r].nalc > 0) need += (int64_t)rec[r].nalg * (rec[r].nalg + 1) / 2;
+        size_t freeB = 0, totalB = 0;
+        MPG_CUDA(c, cudaMemGetInfo(&freeB, &totalB));
+        const int64_t others = 2 * 12 * j.nw + (int64_t)nrec * 512 + ((int64_t)1 << 30);
+        const int64_t room = std::max<int64_t>(((int64_t)freeB - others) / 10 * 9, (int64_t)256 << 20);
+        stageElems = need * 8 <= room ? std::max<int64_t>(need, 1) : room / 16;
+    }
     j.chunkRec.assign(1, 0);
     int64_t upd = 0, maxStage = 0;
     for (int64_t r = 0; r < nrec; ++r) {
@@ -805,7 +846,7 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         if (overlap && ch >= 2) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[ch - 2], 0));
         fp.stage = stg;
         cudaEventRecord(evF0[ch], s);
-        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, overlap ? 1 : 0, s)); launches++; }
+        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, 0, s)); launches++; }
         cudaEventRecord(evF1[ch], s);
         MPG_CUDA(c, cudaStreamWaitEvent(s2, evF1[ch], 0));
         ap.stage = stg;

@@ -25,7 +25,9 @@ struct alignas(16) RecInfo {
     int32_t nw, neq, nalc, nalg;
     int32_t ngrp;
     int16_t mbnd, mbdr;   // bordered band structure (mbnd < 0: dense)
-    int32_t mside;        // 1 upper/left, 2 lower/right border
+    int32_t mside;        // low byte: 1 upper/left, 2 lower/right border; bit 8 local indices not
+                          // increasing; bit 9 dense locals (1..nalc in every equation);
+                          // bit 10 no variable parameter twice in one equation
     int32_t file;         // 1-based file index
 };
 

@@ -625,6 +625,8 @@ k_fit(FitParams p, int perWarp) {
             const int nter = (p.nloopn != 1 && p.lhuber != 0) ? p.lhuber : 1;
             const bool band = ri.mbnd >= 0 && p.lfitbb > 0 && nalc > 5;
             const bool seqNormal = ((ri.mside >> 8) & 1) != 0;
+            const bool denseLoc = ((ri.mside >> 9) & 1) != 0;
+            const bool simpleWords = ((ri.mside >> 10) & 1) != 0;
             const bool needResing = p.lhuber > 1 && p.dwcut != 0.0f;
             const int npk = (nalc * nalc + nalc) / 2;
             int nrank = 0, ndf = 0;
@@ -647,10 +649,36 @@ k_fit(FitParams p, int perWarp) {
                     }
                     m.lwgt[e] = wght;
                 }
+                // ---- second loop: normal equations
+                if (denseLoc) {
+                    // every equation has the locals 1..nalc: lane per element
+                    // of clmat (row j >= column k) or blvec, equations added in
+                    // order, each term (w g_j) g_k resp. (w r) g_j as in the
+                    // equation-by-equation form
+                    const int nq = npk + nalc;
+                    for (int q = ln; q < nq; q += 32) {
+                        const bool isC = q < npk;
+                        int j = q - npk + 1, k = 1;
+                        if (isC) {
+                            j = 1;
+                            k = q + 1;
+                            while (k > j) { k -= j; j++; }
+                        }
+                        double acc = 0.0;
+                        for (int e = 0; e < neq; ++e) {
+                            const int sl = m.mq[3 * e];
+                            const double x = isC ? m.gl[sl + j] : m.rm1[e];
+                            const double y = isC ? m.gl[sl + k] : m.gl[sl + j];
+                            acc = acc + m.lwgt[e] * x * y;
+                        }
+                        if (isC) m.clmat[q] = acc;
+                        else m.blvec[j - 1] = acc;
+                    }
+                    __syncwarp();
+                } else {
                 for (int i = ln; i < npk; i += 32) m.clmat[i] = 0.0;
                 for (int i = ln; i < nalc; i += 32) m.blvec[i] = 0.0;
                 __syncwarp();
-                // ---- second loop: normal equations, equation by equation
                 for (int e = 0; e < neq; ++e) {
                     const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                     const int nl = sg - sl - 1;
@@ -683,6 +711,7 @@ k_fit(FitParams p, int perWarp) {
                         }
                     }
                     __syncwarp();
+                }
                 }
                 // ---- local solve
                 if (band) {
@@ -810,8 +839,20 @@ k_fit(FitParams p, int perWarp) {
                     m.t1[e] = dchi2;
                 }
                 __syncwarp();
-                chi2add = wsum_serial(m.t1, neq);
+                // without down-weighting in this loop the terms equal those of
+                // the last third-loop pass, so is their ordered sum
+                chi2add = (p.nloopn != 1 && p.lhuber != 0) ? wsum_serial(m.t1, neq) : summ;
                 ndfadd = ndf;
+                // per-equation factors of the vector and B terms, (dw1 w) r and
+                // dw2 w, and of the G^T W G term, dw1 w
+                __syncwarp();
+                for (int e = ln; e < neq; e += 32) {
+                    const double wv = m.lwgt[e];
+                    m.t1[e] = dw1 * wv * m.res[e];
+                    m.t2[e] = dw2 * wv;
+                    m.w0[e] = dw1 * wv;
+                }
+                __syncwarp();
                 // ---- global vector and local-global matrix B, one lane per slot
                 for (int s = ln; s < nalg; s += 32) {
                     double v = 0.0;
@@ -821,10 +862,9 @@ k_fit(FitParams p, int perWarp) {
                         const int ent = m.sw[q];
                         const int e = ent >> 16, wp = ent & 0xffff;
                         const double g = m.gl[wp];
-                        const double wv = m.lwgt[e];
-                        if (g != 0.0) v = v + dw1 * wv * m.res[e] * g;
+                        if (g != 0.0) v = v + m.t1[e] * g;
                         if (p.icalcm == 1) {
-                            const double cb = dw2 * wv * g;
+                            const double cb = m.t2[e] * g;
                             const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                             for (int jj = 1; jj <= sg - sl - 1; ++jj) {
                                 const int k = m.in[sl + jj] - 1;
@@ -864,6 +904,15 @@ k_fit(FitParams p, int perWarp) {
                         // reference's order (later word first)
                         int qa = m.swS[a], qae = m.swS[a + 1];
                         int qb = m.swS[b], qbe = m.swS[b + 1];
+                        if (simpleWords && bw.qa == bw.qb) {
+                            // same group: the same equations, one word each
+                            for (; qa < qae; ++qa, ++qb) {
+                                const int ea = m.sw[qa] >> 16;
+                                const double ca = m.w0[ea] * m.gl[m.sw[qa] & 0xffff];
+                                u = __fma_rn(-ca, m.gl[m.sw[qb] & 0xffff], u);
+                            }
+                            qa = qae;
+                        }
                         while (qa < qae && qb < qbe) {
                             const int ea = m.sw[qa] >> 16, eb = m.sw[qb] >> 16;
                             if (ea < eb) { qa++; continue; }
@@ -871,7 +920,7 @@ k_fit(FitParams p, int perWarp) {
                             int qa2 = qa, qb2 = qb;
                             while (qa2 < qae && (m.sw[qa2] >> 16) == ea) qa2++;
                             while (qb2 < qbe && (m.sw[qb2] >> 16) == ea) qb2++;
-                            const double cw = dw1 * m.lwgt[ea];
+                            const double cw = m.w0[ea];
                             for (int x = qa; x < qa2; ++x)
                                 for (int y = qb; y < qb2; ++y) {
                                     const int wa = m.sw[x] & 0xffff, wb = m.sw[y] & 0xffff;
