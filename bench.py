@@ -295,13 +295,18 @@ def main():
         bo = 16 * S.nVar + 256
         barrier(pg)
         t0 = time.perf_counter()
+        up_s, lp_s = [], []
         for _ in range(args.e2e_steps):
+            ta = time.perf_counter()
             ctx.upload(S)
+            tb = time.perf_counter()
             ctx.loopbf(gpar)
+            up_s.append(tb - ta)
+            lp_s.append(time.perf_counter() - tb)
         e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
         line["e2e"] = {"value": total_rec / args.steps * args.e2e_steps / e2e_s,
                        "unit": "records/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
-                       "steps": args.e2e_steps}
+                       "steps": args.e2e_steps, "upload_s": up_s, "loop_s": lp_s}
         if rank == 0:
             nsample = min(args.cpu_sample, nrec)
             val, times = cpu_reference(d, nsample, ncores, steps=1)

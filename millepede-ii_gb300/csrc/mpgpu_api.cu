@@ -7,7 +7,6 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "mpgpu_ctx.h"
@@ -46,29 +45,12 @@ cudaError_t dupload(T *&p, const T *h, int64_t n, cudaStream_t s) {
     return cudaSuccess;
 }
 
-int nthreads_host() {
-    unsigned n = std::thread::hardware_concurrency();
-    if (n < 1) n = 1;
-    if (n > 64) n = 64;
-    return (int)n;
-}
-
-template <class F>
-void parallel_for(int64_t n, F f) {
-    const int nt = nthreads_host();
-    if (n < 4096 || nt == 1) {
-        f(0, n, 0);
-        return;
-    }
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t) {
-        int64_t a = n * t / nt, b = n * (t + 1) / nt;
-        th.emplace_back([=, &f] { f(a, b, t); });
-    }
-    for (auto &x : th) x.join();
-}
-
 void free_records(DevJob &j) {
+    UpTmp &t = j.tmp;
+    dfree(t.recPtr); dfree(t.recFile); dfree(t.cnt); dfree(t.off); dfree(t.scanTmp); dfree(t.grpRec);
+    dfree(t.k0); dfree(t.k1); dfree(t.v0); dfree(t.v1); dfree(t.pairKey); dfree(t.hist); dfree(t.head);
+    dfree(t.nel); dfree(t.segStart); dfree(t.segEnd); dfree(t.bcnt); dfree(t.bscan); dfree(t.cntG); dfree(t.scal);
+    j.cap.clear();
     dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
     dfree(j.fileWeight); dfree(j.status); dfree(j.chi2add); dfree(j.ndfadd); dfree(j.chndf);
@@ -93,28 +75,6 @@ void free_layout(DevJob &j) {
 void free_constraints(DevJob &j) {
     dfree(j.qlV); dfree(j.qlVk); dfree(j.qlR2);
     j.ncon = 0;
-}
-
-// decodeNextMeasurement (pede.f90:2428-2468) on one record; positions
-// relative to the record start; returns false for a malformed record
-struct Eq { int32_t sl, sg, lg; };
-bool decode_record(const int32_t *in, const double *gl, int32_t nw, std::vector<Eq> &eqs) {
-    eqs.clear();
-    int32_t lg = 0;
-    const int32_t end = nw - 1;
-    for (;;) {
-        if (lg >= end) return true;
-        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
-        const int32_t sl = lg;
-        do { lg++; if (lg > end) return false; } while (in[lg] != 0);
-        const int32_t sg = lg;
-        if (sl + 1 == sg && gl[sg] < 0.0) {
-            lg = lg + (int32_t)(-gl[sg] + 0.5);  // special data block
-            continue;
-        }
-        while (lg < end && in[lg + 1] != 0) lg++;
-        eqs.push_back({sl, sg, lg});
-    }
 }
 
 }  // namespace
@@ -321,467 +281,12 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     if (!c || nrec < 0 || !recPtr || !inder || !glder) return MPGPU_ERR_ARG;
     DevJob &j = c->j;
     if (j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the records");
-    cudaSetDevice(c->device);
-    free_records(j);
     if (nfiles < 1) nfiles = 1;
-    j.nfiles = nfiles;
-    j.nrec = nrec;
-    j.nw = recPtr[nrec] - recPtr[0];
-    const int32_t nVar = j.nVar, nTotal = j.nTotal;
-    std::vector<int32_t> varOfTot(nTotal);
-    MPG_CUDA(c, cudaMemcpy(varOfTot.data(), j.varOfTot, sizeof(int32_t) * nTotal, cudaMemcpyDeviceToHost));
-    const std::vector<int32_t> &aig = j.hAig;
-    std::vector<int32_t> p2g(nVar);
-    for (int32_t g = 1; g <= j.nG; ++g)
-        for (int32_t v = aig[g - 1]; v < aig[g]; ++v) p2g[v - 1] = g;
-
-    // ---- pass A: sizes and structure per record
-    std::vector<RecInfo> rec(nrec);
-    std::vector<int32_t> errRec(nthreads_host() + 1, 0);
-    std::vector<int64_t> errAt(nthreads_host() + 1, -1);
-    parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
-        std::vector<Eq> eqs;
-        std::vector<int32_t> stamp(nVar + 1, 0), ibandh, eqStamp(nVar + 1, 0);
-        std::vector<int32_t> gStamp(j.nG + 1, 0), gCnt(j.nG + 1, 0), eqGroups;
-        int32_t eqTag = 0;
-        std::vector<int32_t> sl;
-        for (int64_t r = a; r < b; ++r) {
-            RecInfo &ri = rec[r];
-            memset(&ri, 0, sizeof(ri));
-            const int64_t w0 = recPtr[r];
-            const int64_t nw64 = recPtr[r + 1] - w0;
-            const int32_t *in = inder + w0;
-            const double *gl = glder + w0;
-            ri.w0 = w0 - recPtr[0];
-            ri.file = recFile ? recFile[r] : 1;
-            if (nw64 < 1 || nw64 > MPG_WORDS_MAX || ri.file < 1 || ri.file > nfiles ||
-                !decode_record(in, gl, (int32_t)nw64, eqs)) {
-                errRec[t] = MPGPU_ERR_BADRECORD; errAt[t] = r; return;
-            }
-            ri.nw = (int32_t)nw64;
-            ri.neq = (int32_t)eqs.size();
-            int32_t nalc = 0, nalg = 0, nsw = 0;
-            bool nonmono = false;
-            sl.clear();
-            for (const Eq &e : eqs) {
-                int32_t prev = 0;
-                for (int32_t q = e.sl + 1; q < e.sg; ++q) {
-                    const int32_t li = in[q];
-                    if (li <= 0) { errRec[t] = MPGPU_ERR_BADRECORD; errAt[t] = r; return; }
-                    if (li > nalc) nalc = li;
-                    if (li <= prev) nonmono = true;
-                    prev = li;
-                }
-                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
-                    const int32_t ti = in[q];
-                    if (ti < 1 || ti > nTotal) { errRec[t] = MPGPU_ERR_BADINDEX; errAt[t] = r; return; }
-                    const int32_t v = varOfTot[ti - 1];
-                    if (v > 0) {
-                        nsw++;
-                        if (stamp[v] != (int32_t)(r - a + 1)) { stamp[v] = (int32_t)(r - a + 1); sl.push_back(v); }
-                    }
-                }
-            }
-            nalg = (int32_t)sl.size();
-            ri.nalc = nalc;
-            ri.nalg = nalg;
-            // every equation carries the local derivatives 1..nalc in order
-            // (fast normal equations); no variable parameter twice in one
-            // equation (lockstep word lists in the update)
-            bool denseLoc = nalc > 0, simpleWords = true;
-            for (const Eq &e : eqs) {
-                if (e.sg - e.sl - 1 != nalc) denseLoc = false;
-                for (int32_t q = e.sl + 1; denseLoc && q < e.sg; ++q)
-                    if (in[q] != q - e.sl) denseLoc = false;
-                // ... and every group it touches complete (then all slots of a
-                // group have the same equation list)
-                ++eqTag;
-                eqGroups.clear();
-                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
-                    const int32_t v = varOfTot[in[q] - 1];
-                    if (v <= 0) continue;
-                    if (eqStamp[v] == eqTag) simpleWords = false;
-                    eqStamp[v] = eqTag;
-                    const int32_t g = p2g[v - 1];
-                    if (gStamp[g] != eqTag) { gStamp[g] = eqTag; gCnt[g] = 0; eqGroups.push_back(g); }
-                    gCnt[g]++;
-                }
-                for (int32_t g : eqGroups)
-                    if (gCnt[g] != aig[g] - aig[g - 1]) simpleWords = false;
-            }
-            // groups of the sorted variable parameters; the record must hold
-            // complete groups (loopbf's npar == nalg check, pede.f90:3710-3724)
-            std::sort(sl.begin(), sl.end());
-            int32_t ngrp = 0, prevg = -1, npar = 0;
-            for (int32_t v : sl) {
-                const int32_t g = p2g[v - 1];
-                if (g != prevg) { ngrp++; prevg = g; npar += aig[g] - aig[g - 1]; }
-            }
-            if (nalc > 0 && npar != nalg) { errRec[t] = MPGPU_ERR_GROUPS; errAt[t] = r; return; }
-            if (ngrp > MPG_NGRP_MAX) { errRec[t] = MPGPU_ERR_LIMIT; errAt[t] = r; return; }
-            ri.ngrp = ngrp;
-            // bordered band structure of the local matrix (pede.f90:3812-3874)
-            ri.mbnd = -1; ri.mbdr = (int16_t)nalc; ri.mside = -1;
-            if (nalc > 5) {
-                ibandh.assign(2 * nalc + 2, 0);
-                for (const Eq &e : eqs)
-                    for (int32_t jq = e.sl + 1; jq < e.sg; ++jq)
-                        for (int32_t kq = e.sl + 1; kq <= jq; ++kq) {
-                            const int32_t ij = in[jq], ik = in[kq];
-                            const int32_t id = std::abs(ij - ik) + 1;
-                            int32_t im = std::min(ij, ik);
-                            ibandh[id] = std::max(ibandh[id], im);
-                            im = std::min(nalc + 1 - ij, nalc + 1 - ik);
-                            ibandh[nalc + id] = std::max(ibandh[nalc + id], im);
-                        }
-                int32_t kx = -1, kbdrx = 0, kbdr = 0, side = -1;
-                int64_t icmn = (int64_t)nalc * nalc * nalc;
-                for (int32_t k = nalc; k >= 2; --k) {
-                    const int32_t kbnd = k - 2;
-                    kbdr = std::max(kbdr, ibandh[k]);
-                    const int64_t w = kbnd + kbdr + 1;
-                    const int64_t icost = 6 * (int64_t)(nalc - kbdr) * w * w + 2 * (int64_t)kbdr * kbdr * kbdr;
-                    if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 1; }
-                }
-                if (kx < 0) {
-                    kbdr = 0;
-                    for (int32_t k = nalc; k >= 2; --k) {
-                        const int32_t kbnd = k - 2;
-                        kbdr = std::max(kbdr, ibandh[k + nalc]);
-                        const int64_t w = kbnd + kbdr + 1;
-                        const int64_t icost = 6 * (int64_t)(nalc - kbdr) * w * w + 2 * (int64_t)kbdr * kbdr * kbdr;
-                        if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 2; }
-                    }
-                }
-                if (kx > 0) { ri.mbnd = (int16_t)(kx - 2); ri.mbdr = (int16_t)kbdrx; ri.mside = side; }
-            }
-            ri.mside = (ri.mside & 0xff) | (nonmono ? 0x100 : 0) | (denseLoc ? 0x200 : 0) |
-                       (simpleWords ? 0x400 : 0);
-            ri.measOff = nsw;  // temporarily: number of slot words
-        }
-    });
-    for (size_t t = 0; t < errRec.size(); ++t)
-        if (errRec[t]) {
-            char buf[128];
-            snprintf(buf, sizeof buf, "record %lld rejected at upload (code %d)", (long long)errAt[t], errRec[t]);
-            return set_err(c, errRec[t], buf);
-        }
-
-    // ---- pass B: offsets, maxima, chunks by staging size
-    int64_t neqT = 0, nslotT = 0, nswT = 0, ngrpT = 0;
-    j.maxNw = j.maxNeq = j.maxNalc = j.maxNalg = 0;
-    j.maxBand = -1; j.maxBdr = 0; j.maxNgrp = 1;
-    j.nbndr[0] = j.nbndr[1] = 0; j.nbdrx = j.nbndx = 0;
-    int64_t stageElems = std::max<int64_t>(c->stagingBytes / 8, 1);
-    if (c->stagingBytes <= 0) {
-        // sized per job: all updates of the loop in one chunk when that fits
-        // in the free device memory left after the record tables (estimated
-        // generously as twice the record words), else two chunk buffers of
-        // half the room each
-        int64_t need = 0;
-        for (int64_t r = 0; r < nrec; ++r)
-            if (rec[r].nalc > 0) need += (int64_t)rec[r].nalg * (rec[r].nalg + 1) / 2;
-        size_t freeB = 0, totalB = 0;
-        MPG_CUDA(c, cudaMemGetInfo(&freeB, &totalB));
-        const int64_t others = 2 * 12 * j.nw + (int64_t)nrec * 512 + ((int64_t)1 << 30);
-        const int64_t room = std::max<int64_t>(((int64_t)freeB - others) / 10 * 9, (int64_t)256 << 20);
-        stageElems = need * 8 <= room ? std::max<int64_t>(need, 1) : room / 16;
-    }
-    j.chunkRec.assign(1, 0);
-    int64_t upd = 0, maxStage = 0;
-    for (int64_t r = 0; r < nrec; ++r) {
-        RecInfo &ri = rec[r];
-        const int64_t nsw = ri.measOff;
-        ri.measOff = neqT; neqT += ri.neq;
-        ri.slotOff = nslotT; nslotT += ri.nalg + 1;
-        ri.swOff = nswT; nswT += nsw;
-        ri.grpOff = ngrpT; ngrpT += ri.ngrp;
-        // records without local parameters leave no update in the staging
-        const int64_t ngg = ri.nalc > 0 ? (int64_t)ri.nalg * (ri.nalg + 1) / 2 : 0;
-        if (ngg > stageElems) return set_err(c, MPGPU_ERR_LIMIT, "record update larger than the staging buffer");
-        if (upd + ngg > stageElems) { j.chunkRec.push_back(r); maxStage = std::max(maxStage, upd); upd = 0; }
-        upd += ngg;
-        j.maxNgrp = std::max(j.maxNgrp, ri.ngrp);
-        j.maxNw = std::max(j.maxNw, ri.nw);
-        j.maxNeq = std::max(j.maxNeq, ri.neq);
-        j.maxNalc = std::max(j.maxNalc, ri.nalc);
-        j.maxNalg = std::max(j.maxNalg, ri.nalg);
-        if (ri.mbnd >= 0) {
-            j.maxBand = std::max<int32_t>(j.maxBand, ri.mbnd);
-            j.maxBdr = std::max<int32_t>(j.maxBdr, ri.mbdr);
-            j.nbndr[(ri.mside & 0xff) - 1]++;
-            j.nbdrx = std::max<int32_t>(j.nbdrx, ri.mbdr);
-            j.nbndx = std::max<int32_t>(j.nbndx, ri.mbnd);
-        }
-    }
-    j.chunkRec.push_back(nrec);
-    maxStage = std::max(maxStage, upd);
-    j.neqTot = neqT; j.nslotTot = nslotT; j.nswTot = nswT; j.ngrpTot = ngrpT;
-    if (j.maxNalc > MPG_NALC_MAX) return set_err(c, MPGPU_ERR_LIMIT, "local system larger than the fit kernel limit");
-
-    // ---- pass C: fill the tables
-    std::vector<int32_t> meas(3 * neqT), slots(nslotT), slotCnt(nslotT), swStart(nslotT), sw(nswT);
-    std::vector<int32_t> grpId(ngrpT), grpSlot(ngrpT);
-    parallel_for(nrec, [&](int64_t a, int64_t b, int) {
-        std::vector<Eq> eqs;
-        std::vector<int32_t> pos(nVar + 1, -1), cnt;
-        for (int64_t r = a; r < b; ++r) {
-            const RecInfo &ri = rec[r];
-            const int32_t *in = inder + recPtr[r];
-            const double *gl = glder + recPtr[r];
-            decode_record(in, gl, ri.nw, eqs);
-            for (int32_t e = 0; e < ri.neq; ++e) {
-                meas[3 * (ri.measOff + e)] = eqs[e].sl;
-                meas[3 * (ri.measOff + e) + 1] = eqs[e].sg;
-                meas[3 * (ri.measOff + e) + 2] = eqs[e].lg;
-            }
-            // sorted slots
-            int32_t *sl = &slots[ri.slotOff];
-            int32_t n = 0;
-            for (const Eq &e : eqs)
-                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
-                    const int32_t v = varOfTot[in[q] - 1];
-                    if (v > 0 && pos[v] < 0) { pos[v] = 0; sl[n++] = v; }
-                }
-            std::sort(sl, sl + n);
-            sl[n] = 0;
-            for (int32_t s = 0; s < n; ++s) pos[sl[s]] = s;
-            // word lists per slot, in equation order (counting sort)
-            cnt.assign(n + 1, 0);
-            int32_t *cs = &slotCnt[ri.slotOff];
-            for (int32_t s = 0; s <= n; ++s) cs[s] = 0;
-            for (const Eq &e : eqs)
-                for (int32_t q = e.sg + 1; q <= e.lg; ++q) {
-                    const int32_t v = varOfTot[in[q] - 1];
-                    if (v > 0) {
-                        cnt[pos[v] + 1]++;
-                        if (gl[q] != 0.0) cs[pos[v]]++;
-                    }
-                }
-            int32_t *ss = &swStart[ri.slotOff];
-            ss[0] = 0;
-            for (int32_t s = 0; s < n; ++s) ss[s + 1] = ss[s] + cnt[s + 1];
-            std::vector<int32_t> fillp(ss, ss + n);
-            for (int32_t e = 0; e < ri.neq; ++e)
-                for (int32_t q = eqs[e].sg + 1; q <= eqs[e].lg; ++q) {
-                    const int32_t v = varOfTot[in[q] - 1];
-                    if (v > 0) sw[ri.swOff + fillp[pos[v]]++] = (e << 16) | q;
-                }
-            // groups
-            int32_t g = 0, prevg = -1;
-            for (int32_t s = 0; s < n; ++s) {
-                const int32_t gg = p2g[sl[s] - 1];
-                if (gg != prevg) {
-                    grpId[ri.grpOff + g] = gg;
-                    grpSlot[ri.grpOff + g] = s;
-                    g++;
-                    prevg = gg;
-                }
-            }
-            for (int32_t s = 0; s < n; ++s) pos[sl[s]] = -1;
-        }
-    });
-
-    // ---- pass D: blocks of the global matrix met in the records
-    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
-    const int32_t nG = j.nG;
-    std::vector<int64_t> pairOff(nrec + 1, 0);
-    for (int64_t r = 0; r < nrec; ++r) {
-        const int64_t ng = rec[r].nalc > 0 ? rec[r].ngrp : 0;
-        rec[r].pairOff = pairOff[r];
-        pairOff[r + 1] = pairOff[r] + ng * (ng + 1) / 2;
-    }
-    const int64_t npairs = pairOff[nrec];
-    std::vector<int32_t> bkI, bkJ, bkLd;
-    std::vector<int64_t> bkOff, packedKey;
-    if (j.matsto == 2) {
-        const int64_t nb = (int64_t)j.hBlkJ.size();
-        bkI.resize(nb);
-        for (int32_t I = 1; I <= nG; ++I)
-            for (int64_t k = j.hRowBlk0[I - 1]; k < j.hRowBlk0[I]; ++k) bkI[k] = I;
-        bkJ = j.hBlkJ;
-        bkLd = j.hBlkLd;
-        bkOff = j.hBlkOff;
-    } else {
-        // packed storage: the group pairs that occur in records
-        std::vector<std::vector<int64_t>> keys(nthreads_host());
-        parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
-            std::vector<int64_t> &kv = keys[t];
-            for (int64_t r = a; r < b; ++r) {
-                if (rec[r].nalc <= 0) continue;
-                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa)
-                    for (int32_t qb = 0; qb <= qa; ++qb)
-                        kv.push_back((int64_t)grpId[rec[r].grpOff + qa] * (nG + 1) + grpId[rec[r].grpOff + qb]);
-                if (kv.size() > (1u << 24)) {
-                    std::sort(kv.begin(), kv.end());
-                    kv.erase(std::unique(kv.begin(), kv.end()), kv.end());
-                }
-            }
-            std::sort(kv.begin(), kv.end());
-            kv.erase(std::unique(kv.begin(), kv.end()), kv.end());
-        });
-        for (auto &kv : keys) packedKey.insert(packedKey.end(), kv.begin(), kv.end());
-        std::sort(packedKey.begin(), packedKey.end());
-        packedKey.erase(std::unique(packedKey.begin(), packedKey.end()), packedKey.end());
-        for (int64_t key : packedKey) {
-            bkI.push_back((int32_t)(key / (nG + 1)));
-            bkJ.push_back((int32_t)(key % (nG + 1)));
-            bkLd.push_back(0);
-            bkOff.push_back(0);
-        }
-    }
-    const int64_t nblk = (int64_t)bkI.size();
-    // block of every record pair (a >= b)
-    std::vector<int32_t> pairBlk(std::max<int64_t>(npairs, 1));
-    std::vector<int> pbad(nthreads_host() + 1, 0);
-    parallel_for(nrec, [&](int64_t a, int64_t b, int t) {
-        for (int64_t r = a; r < b; ++r) {
-            if (rec[r].nalc <= 0) continue;
-            int64_t q = pairOff[r];
-            for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
-                const int32_t I = grpId[rec[r].grpOff + qa];
-                for (int32_t qb = 0; qb <= qa; ++qb) {
-                    const int32_t J = grpId[rec[r].grpOff + qb];
-                    int64_t k = -1;
-                    if (j.matsto == 2) {
-                        auto b0 = j.hBlkJ.begin() + j.hRowBlk0[I - 1], b1 = j.hBlkJ.begin() + j.hRowBlk0[I];
-                        auto itb = std::lower_bound(b0, b1, J);
-                        if (itb != b1 && *itb == J) k = itb - j.hBlkJ.begin();
-                    } else {
-                        const int64_t key = (int64_t)I * (nG + 1) + J;
-                        auto itb = std::lower_bound(packedKey.begin(), packedKey.end(), key);
-                        k = itb - packedKey.begin();
-                    }
-                    if (k < 0) { pbad[t] = 1; k = 0; }
-                    pairBlk[q++] = (int32_t)k;
-                }
-            }
-        }
-    });
-    for (int v : pbad)
-        if (v) return set_err(c, MPGPU_ERR_BADINDEX, "record group pair not in the sparse structure");
-    int32_t maxEl = 1;
-    for (int64_t k = 0; k < nblk; ++k) {
-        const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
-        maxEl = std::max(maxEl, bkI[k] == bkJ[k] ? ni * (ni + 1) / 2 : ni * nj);
-    }
-    j.pstride = maxEl;
-    // per chunk: staging position of every record block (the records of one
-    // global-matrix block contiguous in record order), work items and
-    // reduction lists; vector entries per row group in record order
-    std::vector<int64_t> nelOf(std::max<int64_t>(nblk, 1));
-    for (int64_t k = 0; k < nblk; ++k) {
-        const int32_t ni = aig[bkI[k]] - aig[bkI[k] - 1], nj = aig[bkJ[k]] - aig[bkJ[k] - 1];
-        nelOf[k] = bkI[k] == bkJ[k] ? (int64_t)ni * (ni + 1) / 2 : (int64_t)ni * nj;
-    }
-    std::vector<int64_t> pairDst(std::max<int64_t>(npairs, 1));
-    std::vector<int32_t> itBlk, itCnt, rdBlk, rdN;
-    std::vector<int64_t> itBase, itSlot, rdSlot0;
-    int64_t nvent = 0;
-    for (int64_t r = 0; r < nrec; ++r) if (rec[r].nalc > 0) nvent += rec[r].ngrp;
-    std::vector<int64_t> vEntries(std::max<int64_t>(nvent, 1)), vStart((size_t)nchunk * (nG + 1));
-    j.chunkItem.assign(1, 0);
-    j.chunkRed.assign(1, 0);
-    int64_t maxSlots = 1, vbase = 0;
-    std::vector<int64_t> cnt(nblk + 1), bBase(nblk + 1);
-    for (int64_t ch = 0; ch < nchunk; ++ch) {
-        const int64_t r0 = j.chunkRec[ch], r1 = j.chunkRec[ch + 1];
-        const int64_t p0 = pairOff[r0], p1 = pairOff[r1];
-        std::fill(cnt.begin(), cnt.end(), 0);
-        for (int64_t q = p0; q < p1; ++q) cnt[pairBlk[q]]++;
-        bBase[0] = 0;
-        for (int64_t k = 0; k < nblk; ++k) bBase[k + 1] = bBase[k] + cnt[k] * nelOf[k];
-        if (bBase[nblk] > maxStage) return set_err(c, MPGPU_ERR_LIMIT, "staging layout exceeds the chunk size");
-        std::vector<int64_t> fill(bBase.begin(), bBase.end() - 1);
-        for (int64_t q = p0; q < p1; ++q) {
-            const int32_t k = pairBlk[q];
-            pairDst[q] = fill[k];
-            fill[k] += nelOf[k];
-        }
-        int64_t slot = 0;
-        for (int64_t k = 0; k < nblk; ++k) {
-            const int64_t n = cnt[k];
-            if (n <= 0) continue;
-            const int64_t nel = std::max<int64_t>(nelOf[k], 1);
-            const int64_t per = std::max<int64_t>(32, 16384 / nel);
-            const int64_t nitem = (n + per - 1) / per;
-            for (int64_t m = 0; m < nitem; ++m) {
-                itBlk.push_back((int32_t)k);
-                itBase.push_back(bBase[k] + m * per * nelOf[k]);
-                itCnt.push_back((int32_t)std::min(per, n - m * per));
-                itSlot.push_back(nitem > 1 ? slot + m : -1);
-            }
-            if (nitem > 1) {
-                rdBlk.push_back((int32_t)k);
-                rdSlot0.push_back(slot);
-                rdN.push_back((int32_t)nitem);
-                slot += nitem;
-            }
-        }
-        maxSlots = std::max(maxSlots, slot);
-        j.chunkItem.push_back((int64_t)itBlk.size());
-        j.chunkRed.push_back((int64_t)rdBlk.size());
-        // vector entries of the chunk by row group
-        int64_t *vs = &vStart[(size_t)ch * (nG + 1)];
-        std::vector<int64_t> vc(nG + 1, 0);
-        for (int64_t r = r0; r < r1; ++r)
-            if (rec[r].nalc > 0)
-                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) vc[grpId[rec[r].grpOff + qa]]++;
-        vs[0] = vbase;
-        for (int32_t g = 1; g <= nG; ++g) vs[g] = vs[g - 1] + vc[g];
-        std::vector<int64_t> vf(vs, vs + nG);
-        for (int64_t r = r0; r < r1; ++r)
-            if (rec[r].nalc > 0)
-                for (int32_t qa = 0; qa < rec[r].ngrp; ++qa) {
-                    const int32_t g = grpId[rec[r].grpOff + qa];
-                    vEntries[vf[g - 1]++] = (r << 40) | (rec[r].slotOff + grpSlot[rec[r].grpOff + qa]);
-                }
-        vbase = vs[nG];
-    }
-
-    // ---- upload
-    cudaStream_t s = c->stream;
-    MPG_CUDA(c, dupload(j.inder, inder + recPtr[0], j.nw, s));
-    MPG_CUDA(c, dupload(j.glder, glder + recPtr[0], j.nw, s));
-    MPG_CUDA(c, dupload(j.rec, rec.data(), nrec, s));
-    MPG_CUDA(c, dupload(j.meas, meas.data(), 3 * neqT, s));
-    MPG_CUDA(c, dupload(j.slots, slots.data(), nslotT, s));
-    MPG_CUDA(c, dupload(j.slotCnt, slotCnt.data(), nslotT, s));
-    MPG_CUDA(c, dupload(j.swStart, swStart.data(), nslotT, s));
-    MPG_CUDA(c, dupload(j.sw, sw.data(), nswT, s));
-    MPG_CUDA(c, dupload(j.grpId, grpId.data(), ngrpT, s));
-    MPG_CUDA(c, dupload(j.grpSlot, grpSlot.data(), ngrpT, s));
-    j.nblk = nblk;
-    MPG_CUDA(c, dupload(j.bkI, bkI.data(), nblk, s));
-    MPG_CUDA(c, dupload(j.bkJ, bkJ.data(), nblk, s));
-    MPG_CUDA(c, dupload(j.bkLd, bkLd.data(), nblk, s));
-    MPG_CUDA(c, dupload(j.bkOff, bkOff.data(), nblk, s));
-    MPG_CUDA(c, dupload(j.pairDst, pairDst.data(), npairs, s));
-    MPG_CUDA(c, dupload(j.itBlk, itBlk.data(), (int64_t)itBlk.size(), s));
-    MPG_CUDA(c, dupload(j.itBase, itBase.data(), (int64_t)itBase.size(), s));
-    MPG_CUDA(c, dupload(j.itCnt, itCnt.data(), (int64_t)itCnt.size(), s));
-    MPG_CUDA(c, dupload(j.itSlot, itSlot.data(), (int64_t)itSlot.size(), s));
-    MPG_CUDA(c, dupload(j.rdBlk, rdBlk.data(), (int64_t)rdBlk.size(), s));
-    MPG_CUDA(c, dupload(j.rdSlot0, rdSlot0.data(), (int64_t)rdSlot0.size(), s));
-    MPG_CUDA(c, dupload(j.rdN, rdN.data(), (int64_t)rdN.size(), s));
-    MPG_CUDA(c, dupload(j.vEntries, vEntries.data(), nvent, s));
-    MPG_CUDA(c, dupload(j.vStart, vStart.data(), (int64_t)vStart.size(), s));
-    j.partialLen = maxSlots * j.pstride;
-    MPG_CUDA(c, dalloc(j.partial, j.partialLen));
-    std::vector<double> fw(nfiles, 1.0);
-    if (fileWeight) fw.assign(fileWeight, fileWeight + nfiles);
-    MPG_CUDA(c, dupload(j.fileWeight, fw.data(), nfiles, s));
-    MPG_CUDA(c, dalloc(j.status, nrec));
-    MPG_CUDA(c, dalloc(j.chi2add, nrec));
-    MPG_CUDA(c, dalloc(j.ndfadd, nrec));
-    MPG_CUDA(c, dalloc(j.chndf, nrec));
-    MPG_CUDA(c, dalloc(j.vstage, nslotT));
-    // two staging buffers when there are several chunks: the fits of chunk
-    // k+1 overlap the accumulation of chunk k
-    j.stageLen = maxStage;
-    MPG_CUDA(c, dalloc(j.stage, (j.chunkRec.size() > 2 ? 2 : 1) * maxStage));
-    MPG_CUDA(c, cudaStreamSynchronize(s));
-    return MPGPU_OK;
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    j.nrec = 0;  // no records until the upload succeeds
+    const int32_t rc = upload_records_device(c, nrec, recPtr, inder, glder, recFile, nfiles, fileWeight);
+    if (rc != MPGPU_OK) j.nrec = 0;
+    return rc;
 }
 
 // ------------------------------------------------------------------ data loop

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/mpgpu.h"
@@ -29,6 +30,22 @@ struct alignas(16) RecInfo {
                           // increasing; bit 9 dense locals (1..nalc in every equation);
                           // bit 10 no variable parameter twice in one equation
     int32_t file;         // 1-based file index
+};
+
+// Work arrays of the device-side record preparation (kept between uploads).
+struct UpTmp {
+    int64_t *recPtr = nullptr;
+    int32_t *recFile = nullptr;
+    int64_t *cnt = nullptr, *off = nullptr;   // 6 x (nrec + 1) counts and offsets
+    int64_t *scanTmp = nullptr;
+    int32_t *grpRec = nullptr;                // record of each group entry
+    uint64_t *k0 = nullptr, *k1 = nullptr;    // radix-sort keys
+    uint32_t *v0 = nullptr, *v1 = nullptr;    // radix-sort values
+    uint64_t *pairKey = nullptr;              // block of each record group pair
+    int64_t *hist = nullptr, *head = nullptr;
+    int64_t *nel = nullptr, *segStart = nullptr, *segEnd = nullptr;
+    int64_t *bcnt = nullptr, *bscan = nullptr, *cntG = nullptr;
+    int64_t *scal = nullptr;                  // error word and maxima
 };
 
 // Device arrays of one job.  Every pointer is owned by the context.
@@ -104,6 +121,8 @@ struct DevJob {
     int64_t *vStart = nullptr;         // [nchunk*(nG+1)]
     double *stage = nullptr;
     int64_t stageLen = 0;
+    UpTmp tmp;
+    std::unordered_map<const void *, int64_t> cap;   // capacities of the arrays kept between uploads
     // limits over the job (fit kernel shared memory sizing)
     int32_t maxNw = 0, maxNeq = 0, maxNalc = 0, maxNalg = 0, maxBand = -1, maxBdr = 0, maxNgrp = 1;
     int32_t nbndr[2] = {0, 0}, nbdrx = 0, nbndx = 0;
@@ -223,6 +242,11 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corr,
 int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
                      double *corr, mpgpu_solveinfo *info);
 int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b);
+
+// record preparation on the device (mpgpu_upload.cu)
+int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                              const double *glder, const int32_t *recFile, int32_t nfiles,
+                              const double *fileWeight);
 
 // error helpers
 int32_t set_err(mpgpu_ctx *c, int32_t code, const std::string &msg);
