@@ -193,6 +193,16 @@ int32_t mpgpu_host_unregister(void *ptr);
  * used as the roofline denominator of the FP64-bound local-fit kernel. */
 int32_t mpgpu_probe_fp64(int32_t device, double *tflops);
 
+/* Dense Cholesky factor L (L L^T = A) of a symmetric positive definite
+ * n x n matrix (row-major, lower triangle read; L written row-major, lower
+ * triangle), blocked in 128 x 128 tiles (the dense form of chdec2,
+ * mpnum.f90:891-987).  mode 0: FP64 throughout; mode 1: trailing updates on
+ * the tensor cores in 3xTF32 (about 1e-6 relative accuracy of the factor,
+ * used as the preconditioner of the refined solve).  *ms receives the device
+ * time.  Returns MPGPU_ERR_FACTOR on a non-positive pivot. */
+int32_t mpgpu_dense_cholesky(mpgpu_ctx *ctx, int32_t n, const double *A, double *L, int32_t mode,
+                             double *ms);
+
 /* b = Q^T A Q x restricted to the first n = nVar - ncon components
  * (avprod), x and b host arrays of length n. */
 int32_t mpgpu_avprod(mpgpu_ctx *ctx, int32_t n, const double *x, double *b);

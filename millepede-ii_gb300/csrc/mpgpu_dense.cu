@@ -1,0 +1,407 @@
+// mpgpu_dense.cu -- blocked dense Cholesky of the global matrix (the dense
+// solve of `method cholesky`, pede.f90:7951-8054 / chdec2 mpnum.f90:891-987,
+// re-blocked for the GPU) in two forms:
+//   mode 0: FP64 throughout (panel, triangular solve, trailing update on the
+//           FP64 CUDA cores);
+//   mode 1: FP64 panel factorisation and triangular solve; the trailing
+//           update A22 -= L21 L21^T, which carries the N^3/3 work, on the
+//           tcgen05 tensor cores in 3xTF32 (x = hi + lo, products
+//           hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory) and
+//           subtracted from the FP64 matrix.
+// The matrix is dense row-major (lower triangle used), padded to a multiple
+// of 128 with identity rows.  The factor of mode 1 is accurate to about the
+// TF32x3 product precision; solves refine it in FP64 (mpgpu_solve,
+// metsol 31).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "mpgpu_ctx.h"
+
+namespace {
+
+constexpr int kNB = 128;   // panel width = tile size
+
+// ------------------------------------------------------------ panel kernels
+// Cholesky of the 128 x 128 diagonal block at (k0, k0), in shared memory.
+__global__ void __launch_bounds__(512) k_potrf128(double *A, int64_t ld, int64_t k0, int32_t *err) {
+    extern __shared__ __align__(16) double sa[];   // 128 x 129
+    constexpr int S = kNB + 1;
+    __shared__ int bad;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) bad = 0;
+    for (int e = tid; e < kNB * kNB; e += nt) {
+        const int i = e / kNB, j = e % kNB;
+        sa[i * S + j] = j <= i ? A[(k0 + i) * ld + k0 + j] : 0.0;
+    }
+    __syncthreads();
+    for (int j = 0; j < kNB; ++j) {
+        if (tid == 0) {
+            const double d = sa[j * S + j];
+            if (!(d > 0.0)) { bad = 1; sa[j * S + j] = 1.0; }
+            else sa[j * S + j] = sqrt(d);
+        }
+        __syncthreads();
+        const double inv = 1.0 / sa[j * S + j];
+        for (int i = j + 1 + tid; i < kNB; i += nt) sa[i * S + j] *= inv;
+        __syncthreads();
+        const int m = kNB - 1 - j;
+        for (int e = tid; e < m * m; e += nt) {
+            const int i = j + 1 + e / m, k = j + 1 + e % m;
+            if (k <= i) sa[i * S + k] -= sa[i * S + j] * sa[k * S + j];
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < kNB * kNB; e += nt) {
+        const int i = e / kNB, j = e % kNB;
+        if (j <= i) A[(k0 + i) * ld + k0 + j] = sa[i * S + j];
+    }
+    if (tid == 0 && bad) atomicExch(err, (int)(k0 / kNB) + 1);
+}
+
+// L21 = A21 L11^-T: one warp per row below the diagonal block; L11 held
+// transposed in shared memory so that a column of L11 is contiguous.
+__global__ void __launch_bounds__(256) k_trsm128(double *A, int64_t ld, int64_t k0, int64_t nrows) {
+    extern __shared__ __align__(16) double lt[];   // 128 x 128 (lt[j * 128 + c] = L11[c][j]) + 128 inverse diagonal
+    double *dinv = lt + kNB * kNB;
+    const int tid = threadIdx.x, ln = tid & 31, wib = tid >> 5;
+    for (int e = tid; e < kNB * kNB; e += blockDim.x) {
+        const int c = e / kNB, j = e % kNB;
+        lt[j * kNB + c] = j <= c ? A[(k0 + c) * ld + k0 + j] : 0.0;
+    }
+    __syncthreads();
+    for (int j = tid; j < kNB; j += blockDim.x) dinv[j] = 1.0 / lt[j * kNB + j];
+    __syncthreads();
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib; r < nrows; r += nw) {
+        double *row = A + (k0 + kNB + r) * ld + k0;
+        double a[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = row[q * 32 + ln];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            for (int l = 0; l < 32; ++l) {
+                const int j = q * 32 + l;
+                const double xj = __shfl_sync(0xffffffffu, a[q], l) * dinv[j];
+                if (ln == l) a[q] = xj;
+#pragma unroll
+                for (int q2 = 0; q2 < 4; ++q2) {
+                    if (q2 < q) continue;
+                    const int c = q2 * 32 + ln;
+                    if (c > j) a[q2] -= xj * lt[j * kNB + c];
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) row[q * 32 + ln] = a[q];
+    }
+}
+
+// L21 rows as TF32 pairs (hi, lo), row-major with 128 columns
+__global__ void k_split_tf32(const double *A, int64_t ld, int64_t k0, int64_t nrows, float *hi, float *lo) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nrows * kNB) return;
+    const int64_t r = e / kNB;
+    const int k = (int)(e % kNB);
+    const double x = A[(k0 + kNB + r) * ld + k0 + k];
+    uint32_t h, l;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
+    const double rest = x - (double)__uint_as_float(h);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"((float)rest));
+    hi[e] = __uint_as_float(h);
+    lo[e] = __uint_as_float(l);
+}
+
+// --------------------------------------------- tcgen05 3xTF32 trailing update
+// One CTA per 128 x 128 tile (bi >= bj) of the trailing matrix:
+// C -= L_i L_j^T with K = 128, fed in chunks of 32 (128 bytes per row).
+// Shared-memory operand layout: K-major, no swizzle, core matrices of
+// 8 rows x 16 bytes; core (row group g, k group c) at (g * 8 + c) * 128
+// bytes, i.e. leading (K) byte offset 128 and stride (row) byte offset 1024.
+constexpr int kTK = 32;                         // K per chunk
+constexpr int kOpBytes = kNB * kTK * 4;         // 16 KB per operand chunk
+constexpr int kTcThreads = 128;
+constexpr int kWaitLimit = 1 << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, N = 128, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kNB >> 3) << 17) |
+                            ((uint32_t)(kNB >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+    for (int i = 0; i < kWaitLimit; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// copy a 128 x 32 fp32 chunk (rows of length 128 in global) into the core
+// matrix layout
+__device__ __forceinline__ void load_chunk(const float *g, int kc0, char *s) {
+    for (int idx = threadIdx.x; idx < kNB * (kTK / 4); idx += kTcThreads) {
+        const int row = idx >> 3, k4 = idx & 7;
+        const float4 v = *reinterpret_cast<const float4 *>(g + (int64_t)row * kNB + kc0 + k4 * 4);
+        *reinterpret_cast<float4 *>(s + ((row >> 3) * 8 + k4) * 128 + (row & 7) * 16) = v;
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_syrk_tc(double *A, int64_t ld, int64_t r0, int32_t T,
+                                                        const float *hi, const float *lo, int32_t *err) {
+    extern __shared__ __align__(1024) char tsm[];   // Ahi Alo Bhi Blo chunks
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, wib = tid >> 5, ln = tid & 31;
+    // tile (bi, bj), bj <= bi, from the triangular index
+    const int64_t t = blockIdx.x;
+    int bi = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((int64_t)bi * (bi + 1) / 2 > t) bi--;
+    while ((int64_t)(bi + 1) * (bi + 2) / 2 <= t) bi++;
+    const int bj = (int)(t - (int64_t)bi * (bi + 1) / 2);
+    if (bi >= T) return;
+    char *sAhi = tsm, *sAlo = tsm + kOpBytes, *sBhi = tsm + 2 * kOpBytes, *sBlo = tsm + 3 * kOpBytes;
+    if (wib == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tbase)),
+                     "r"(kNB));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tbase;
+    const uint32_t mb = smem_u32(&mbar);
+    const float *ahi = hi + (int64_t)bi * kNB * kNB, *alo = lo + (int64_t)bi * kNB * kNB;
+    const float *bhi = hi + (int64_t)bj * kNB * kNB, *blo = lo + (int64_t)bj * kNB * kNB;
+    uint32_t parity = 0;
+    bool ok = true;
+    for (int c = 0; c < kNB / kTK; ++c) {
+        load_chunk(ahi, c * kTK, sAhi);
+        load_chunk(alo, c * kTK, sAlo);
+        load_chunk(bhi, c * kTK, sBhi);
+        load_chunk(blo, c * kTK, sBlo);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int kk = 0; kk < kTK / 8; ++kk) {
+                const uint32_t off = kk * 256;   // 8 tf32 = 2 core matrices along K
+                const uint64_t dah = umma_desc(smem_u32(sAhi) + off), dal = umma_desc(smem_u32(sAlo) + off);
+                const uint64_t dbh = umma_desc(smem_u32(sBhi) + off), dbl = umma_desc(smem_u32(sBlo) + off);
+                mma_tf32(tmem, dah, dbh, (c > 0 || kk > 0) ? 1u : 0u);
+                mma_tf32(tmem, dah, dbl, 1u);
+                mma_tf32(tmem, dal, dbh, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+                         : "memory");
+        }
+        if (!mbar_wait(mb, parity)) {
+            // give the tensor core one more bounded wait before the tensor
+            // memory is released
+            mbar_wait(mb, parity);
+            ok = false;
+            break;
+        }
+        parity ^= 1;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (ok) {
+        // rows of warp w = tensor-memory lanes 32w .. 32w+31
+        const int row = wib * 32 + ln;
+        double *crow = A + (r0 + (int64_t)bi * kNB + row) * ld + r0 + (int64_t)bj * kNB;
+        for (int cb = 0; cb < kNB / 32; ++cb) {
+            uint32_t v[32];
+            tmem_ld32(tmem + ((uint32_t)(wib * 32) << 16) + (uint32_t)(cb * 32), v);
+#pragma unroll
+            for (int q = 0; q < 32; ++q) crow[cb * 32 + q] -= (double)__uint_as_float(v[q]);
+        }
+    } else if (tid == 0) {
+        atomicExch(err, -1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (wib == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kNB));
+}
+
+// ------------------------------------------------ FP64 trailing update
+// 64 x 64 tiles (bi >= bj), 256 threads with 4 x 4 outputs each, K = 128
+// in chunks of 16 from the FP64 panel.
+__global__ void __launch_bounds__(256) k_syrk_fp64(double *A, int64_t ld, int64_t k0, int64_t r0, int32_t T) {
+    __shared__ double sa[16][64 + 1], sb[16][64 + 1];
+    const int64_t t = blockIdx.x;
+    int bi = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((int64_t)bi * (bi + 1) / 2 > t) bi--;
+    while ((int64_t)(bi + 1) * (bi + 2) / 2 <= t) bi++;
+    const int bj = (int)(t - (int64_t)bi * (bi + 1) / 2);
+    if (bi >= T) return;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    const int64_t i0 = r0 + (int64_t)bi * 64, j0 = r0 + (int64_t)bj * 64;
+    double acc[4][4] = {};
+    for (int kc = 0; kc < kNB; kc += 16) {
+        for (int e = tid; e < 64 * 16; e += 256) {
+            const int r = e >> 4, k = e & 15;
+            sa[k][r] = A[(i0 + r) * ld + k0 + kc + k];
+            sb[k][r] = A[(j0 + r) * ld + k0 + kc + k];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            double a[4], b[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) { a[q] = sa[k][ty * 4 + q]; b[q] = sb[k][tx * 4 + q]; }
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) A[(i0 + ty * 4 + p) * ld + j0 + tx * 4 + q] -= acc[p][q];
+}
+
+__global__ void k_pad_identity(double *A, int64_t ld, int64_t n, int64_t npad) {
+    const int64_t i = n + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < npad) A[i * ld + i] = 1.0;
+}
+
+}  // namespace
+
+// Factorise the dense padded matrix A (npad x npad, row-major, lower
+// triangle) in place.  Returns 0, MPGPU_ERR_FACTOR (non-positive pivot in
+// panel *badPanel) or a CUDA/timeout error.
+int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, float *hiBuf, float *loBuf,
+                              int32_t *dErr, int32_t *badPanel) {
+    cudaStream_t s = c->stream;
+    const int64_t ld = npad;
+    const int64_t np = npad / kNB;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
+    const int potrfSmem = kNB * (kNB + 1) * (int)sizeof(double);
+    const int trsmSmem = (kNB * kNB + kNB) * (int)sizeof(double);
+    const int tcSmem = 4 * kOpBytes;
+    MPG_CUDA(c, cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, potrfSmem));
+    MPG_CUDA(c, cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize, trsmSmem));
+    MPG_CUDA(c, cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcSmem));
+    MPG_CUDA(c, cudaMemsetAsync(dErr, 0, sizeof(int32_t), s));
+    for (int64_t p = 0; p < np; ++p) {
+        const int64_t k0 = p * kNB;
+        k_potrf128<<<1, 512, potrfSmem, s>>>(A, ld, k0, dErr);
+        const int64_t rows = npad - k0 - kNB;
+        if (rows <= 0) break;
+        const int64_t tb = std::min<int64_t>((rows + 7) / 8, (int64_t)nsm);
+        k_trsm128<<<(unsigned)tb, 256, trsmSmem, s>>>(A, ld, k0, rows);
+        const int64_t r0 = k0 + kNB;
+        if (mode == 1) {
+            k_split_tf32<<<(unsigned)((rows * kNB + 255) / 256), 256, 0, s>>>(A, ld, k0, rows, hiBuf, loBuf);
+            const int32_t T = (int32_t)(rows / kNB);
+            const int64_t ntile = (int64_t)T * (T + 1) / 2;
+            k_syrk_tc<<<(unsigned)ntile, kTcThreads, tcSmem, s>>>(A, ld, r0, T, hiBuf, loBuf, dErr);
+        } else {
+            const int32_t T = (int32_t)(rows / 64);
+            const int64_t ntile = (int64_t)T * (T + 1) / 2;
+            k_syrk_fp64<<<(unsigned)ntile, 256, 0, s>>>(A, ld, k0, r0, T);
+        }
+        MPG_CUDA(c, cudaGetLastError());
+    }
+    int32_t h = 0;
+    MPG_CUDA(c, cudaMemcpyAsync(&h, dErr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    if (h < 0) return set_err(c, MPGPU_ERR_TIMEOUT, "tensor-core update: barrier wait ran out");
+    if (h > 0) {
+        if (badPanel) *badPanel = h - 1;
+        return set_err(c, MPGPU_ERR_FACTOR, "non-positive pivot in the dense Cholesky");
+    }
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_dense_cholesky(mpgpu_ctx *c, int32_t n, const double *A, double *L, int32_t mode,
+                                        double *ms) {
+    if (!c || n <= 0 || !A || !L || (mode != 0 && mode != 1)) return MPGPU_ERR_ARG;
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    const int64_t npad = ((int64_t)n + kNB - 1) / kNB * kNB;
+    double *dA = nullptr;
+    float *hi = nullptr, *lo = nullptr;
+    int32_t *dErr = nullptr;
+    int32_t rc = MPGPU_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto fail = [&](cudaError_t e, const char *w) { rc = cuda_err(c, e, w); };
+    cudaError_t e = cudaMalloc(&dA, sizeof(double) * npad * npad);
+    if (e == cudaSuccess) e = cudaMalloc(&hi, sizeof(float) * npad * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&lo, sizeof(float) * npad * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&dErr, sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemsetAsync(dA, 0, sizeof(double) * npad * npad, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(dA, sizeof(double) * npad, A, sizeof(double) * n, sizeof(double) * n, n,
+                              cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && npad > n)
+        k_pad_identity<<<(unsigned)((npad - n + 255) / 256), 256, 0, s>>>(dA, npad, n, npad);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) fail(e, "mpgpu_dense_cholesky setup");
+    if (rc == MPGPU_OK) {
+        cudaEventRecord(e0, s);
+        int32_t bad = -1;
+        rc = dense_cholesky_device(c, dA, npad, mode, hi, lo, dErr, &bad);
+        cudaEventRecord(e1, s);
+        cudaEventSynchronize(e1);
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (ms) *ms = t;
+    }
+    if (rc == MPGPU_OK) {
+        e = cudaMemcpy2DAsync(L, sizeof(double) * n, dA, sizeof(double) * npad, sizeof(double) * n, n,
+                              cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) fail(e, "mpgpu_dense_cholesky download");
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(dA);
+    cudaFree(hi);
+    cudaFree(lo);
+    cudaFree(dErr);
+    return rc;
+}

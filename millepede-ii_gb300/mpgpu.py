@@ -110,6 +110,7 @@ EXPORTS = [
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
     "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
+    "mpgpu_dense_cholesky",
     "mpgpu_host_register", "mpgpu_host_unregister",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
@@ -351,6 +352,17 @@ class Context:
         add = np.ascontiguousarray(add, np.float64)
         self.check(self.L.mpgpu_mupdat(self.h, C.c_int32(len(i)), ptr(i, i32p), ptr(j, i32p),
                                        ptr(add, f64p)))
+
+    def dense_cholesky(self, A, mode):
+        """Cholesky factor of a dense SPD matrix on the device (mode 0 FP64,
+        mode 1 tensor-core 3xTF32 trailing updates); returns (L, ms)."""
+        A = np.ascontiguousarray(A, np.float64)
+        n = A.shape[0]
+        L = np.zeros_like(A)
+        ms = C.c_double()
+        self.check(self.L.mpgpu_dense_cholesky(self.h, C.c_int32(n), ptr(A, f64p), ptr(L, f64p),
+                                               C.c_int32(mode), C.byref(ms)))
+        return np.tril(L), ms.value
 
     def mupdat_noalloc(self, i, j, add):
         """mupdat through the entry point that stages in a fixed device area."""
