@@ -176,6 +176,13 @@ typedef struct mpgpu_solveinfo {
 
 /* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES)
  * of the matrix built by the last mpgpu_loopbf plus mupdat calls.
+ * Decomposition also in blocked dense form (no counterpart in the
+ * reference, same solution): metsol 32 FP64 blocked Cholesky, metsol 31
+ * Cholesky with tensor-core 3xTF32 trailing updates; both refine the
+ * solution by preconditioned CG in FP64 until the residual is below rtol
+ * (info->itn iterations, info->istop 1 converged / 3 limit, info->evmin the
+ * diagonal shift the low-precision factor needed, info->evmax the final
+ * relative residual).
  * consResiduals[ncon] = d - C p (addcst); correction[nVar] receives the
  * step; errors[nVar] (metsol 1, may be NULL) the diagonal of the covariance
  * (sqrt gives the parameter errors).  rtol/itnlim: MINRES tolerance and

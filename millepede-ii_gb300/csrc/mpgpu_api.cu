@@ -532,9 +532,10 @@ extern "C" int32_t mpgpu_solve(mpgpu_ctx *c, int32_t metsol, const double *consR
     mpgpu_solveinfo tmp;
     if (!info) info = &tmp;
     memset(info, 0, sizeof(*info));
-    if (metsol == 1 || metsol == 3) {
+    if (metsol == 1 || metsol == 3 || metsol == 31 || metsol == 32) {
         if (c->j.matsto != 1) return set_err(c, MPGPU_ERR_ARG, "inversion/decomposition need packed storage");
-        return solve_inversion(c, consResiduals, correction, errors, info, metsol == 3);
+        const int dense = metsol == 31 ? 1 : (metsol == 32 ? 0 : -1);
+        return solve_inversion(c, consResiduals, correction, errors, info, metsol != 1, dense, rtol, itnlim);
     }
     if (metsol == 4) return solve_minres(c, consResiduals, rtol, itnlim, correction, info);
     return set_err(c, MPGPU_ERR_ARG, "unsupported solution method");

@@ -238,7 +238,14 @@ __device__ int64_t d_ijpgrp(int32_t itema, int32_t itemb, int32_t nG, const int3
 
 // ---------------------------------------------------------------- solvers
 int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corr, double *errs,
-                        mpgpu_solveinfo *info, bool decomposition);
+                        mpgpu_solveinfo *info, bool decomposition, int dense = -1, double rtol = 1e-13,
+                        int32_t itnlim = 2000);
+// dense blocked Cholesky (mpgpu_dense.cu): mode 0 FP64, mode 1 tensor-core 3xTF32 trailing updates
+int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, float *hiBuf, float *loBuf,
+                              int32_t *dErr, int32_t *badPanel);
+// packed SPD solve refined by preconditioned CG in FP64 (b in, x out, device)
+int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
+                        int32_t itnlim, mpgpu_solveinfo *info);
 int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
                      double *corr, mpgpu_solveinfo *info);
 int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b);

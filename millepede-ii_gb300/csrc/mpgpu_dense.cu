@@ -405,3 +405,338 @@ extern "C" int32_t mpgpu_dense_cholesky(mpgpu_ctx *c, int32_t n, const double *A
     cudaFree(dErr);
     return rc;
 }
+
+// ======================================================================
+// Refined dense solve: the factor of dense_cholesky_device (FP64 or
+// tensor-core 3xTF32) preconditions conjugate gradients in FP64 on the
+// original matrix, so the solution reaches the FP64 residual whatever the
+// precision of the factor.
+namespace {
+
+constexpr int kDotBlk = 304;   // fixed reduction shape: deterministic sums
+
+// packed lower triangle (n) -> dense lower (factor) and dense full (for the
+// matrix-vector products), both npad x npad row-major; scaled diagonal
+__global__ void k_packed_to_dense(const double *Ap, int64_t n, int64_t npad, double *Lo, double *F) {
+    const int64_t nn = n * (n + 1) / 2;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = (int64_t)((sqrt(8.0 * (double)e + 1.0) - 1.0) * 0.5);
+        while (i * (i + 1) / 2 > e) i--;
+        while ((i + 1) * (i + 2) / 2 <= e) i++;
+        const int64_t j = e - i * (i + 1) / 2;
+        const double v = Ap[e];
+        Lo[i * npad + j] = v;
+        F[i * npad + j] = v;
+        F[j * npad + i] = v;
+    }
+}
+
+__global__ void k_copy_lower_shift(const double *F, double *Lo, int64_t npad, double shift) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < npad * npad;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / npad, j = e % npad;
+        Lo[e] = j < i ? F[e] : (j == i ? F[e] * (1.0 + shift) : 0.0);
+    }
+}
+
+// inverses of the 128 x 128 diagonal blocks of L, stored transposed:
+// DinvT[p][r][*] = column r of L_pp^-1 (one CTA per block, one warp per r)
+__global__ void __launch_bounds__(256) k_trtri_blocks(const double *A, int64_t ld, double *DinvT) {
+    extern __shared__ __align__(16) double lt[];   // lt[j * 128 + c] = L_pp[c][j], then 1 / diagonal
+    double *dinv = lt + kNB * kNB;
+    const int64_t k0 = (int64_t)blockIdx.x * kNB;
+    const int tid = threadIdx.x, ln = tid & 31, wib = tid >> 5;
+    for (int e = tid; e < kNB * kNB; e += blockDim.x) {
+        const int c = e / kNB, j = e % kNB;
+        lt[j * kNB + c] = j <= c ? A[(k0 + c) * ld + k0 + j] : 0.0;
+    }
+    __syncthreads();
+    for (int j = tid; j < kNB; j += blockDim.x) dinv[j] = 1.0 / lt[j * kNB + j];
+    __syncthreads();
+    double *out = DinvT + (int64_t)blockIdx.x * kNB * kNB;
+    for (int r = wib; r < kNB; r += blockDim.x >> 5) {
+        double a[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = (q * 32 + ln == r) ? 1.0 : 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            for (int l = 0; l < 32; ++l) {
+                const int j = q * 32 + l;
+                const double xj = __shfl_sync(0xffffffffu, a[q], l) * dinv[j];
+                if (ln == l) a[q] = xj;
+#pragma unroll
+                for (int q2 = 0; q2 < 4; ++q2) {
+                    if (q2 < q) continue;
+                    const int c = q2 * 32 + ln;
+                    if (c > j) a[q2] -= xj * lt[j * kNB + c];
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) out[(int64_t)r * kNB + q * 32 + ln] = a[q];
+    }
+}
+
+// forward solve, block p: y_p <- L_pp^-1 y_p
+__global__ void k_fwd_diag(const double *DinvT, int64_t p, double *y) {
+    __shared__ double yp[kNB];
+    const int i = threadIdx.x;
+    double *yb = y + p * kNB;
+    yp[i] = yb[i];
+    __syncthreads();
+    const double *D = DinvT + p * kNB * kNB;
+    double s = 0.0;
+    for (int m = 0; m <= i; ++m) s += D[(int64_t)m * kNB + i] * yp[m];
+    yb[i] = s;
+}
+
+// forward solve, rows below block p: y_R -= L[R][block p] y_p (warp per row)
+__global__ void k_fwd_upd(const double *L, int64_t ld, int64_t p, int64_t npad, double *y) {
+    __shared__ double yp[kNB];
+    const int ln = threadIdx.x & 31;
+    if (threadIdx.x < kNB) yp[threadIdx.x] = y[p * kNB + threadIdx.x];
+    __syncthreads();
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t R = (p + 1) * kNB + w; R < npad; R += nw) {
+        const double *row = L + R * ld + p * kNB;
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s += row[q * 32 + ln] * yp[q * 32 + ln];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (ln == 0) y[R] -= s;
+    }
+}
+
+// backward solve, block p: y_p <- L_pp^-T y_p
+__global__ void k_bwd_diag(const double *DinvT, int64_t p, double *y) {
+    __shared__ double yp[kNB];
+    const int i = threadIdx.x;
+    double *yb = y + p * kNB;
+    yp[i] = yb[i];
+    __syncthreads();
+    const double *D = DinvT + p * kNB * kNB + (int64_t)i * kNB;
+    double s = 0.0;
+    for (int m = i; m < kNB; ++m) s += D[m] * yp[m];
+    yb[i] = s;
+}
+
+// backward solve, columns left of block p: y_c -= sum_m L[p*128+m][c] x_p[m]
+__global__ void k_bwd_upd(const double *L, int64_t ld, int64_t p, double *y) {
+    __shared__ double xp[kNB];
+    if (threadIdx.x < kNB) xp[threadIdx.x] = y[p * kNB + threadIdx.x];
+    __syncthreads();
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= p * kNB) return;
+    const double *col = L + p * kNB * ld + c;
+    double s = 0.0;
+    for (int m = 0; m < kNB; ++m) s += col[(int64_t)m * ld] * xp[m];
+    y[c] -= s;
+}
+
+// y = F x, dense full matrix, one warp per row
+__global__ void k_gemv(const double *F, int64_t ld, int64_t npad, const double *x, double *y) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = w; r < npad; r += nw) {
+        const double *row = F + r * ld;
+        double s = 0.0;
+        for (int64_t j = ln; j < npad; j += 32) s += row[j] * x[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (ln == 0) y[r] = s;
+    }
+}
+
+__global__ void k_dotp(int64_t n, const double *a, const double *b, double *part) {
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        s += a[i] * b[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void k_dotf(const double *part, double *out) {
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < kDotBlk; i += blockDim.x) s += part[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// scalars: [0] rz, [1] pq, [2] rz new, [3] rr, [4] bb
+__global__ void k_cg_step(int64_t n, double *x, double *r, const double *p, const double *q, const double *sc) {
+    const double alpha = sc[1] != 0.0 ? sc[0] / sc[1] : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += alpha * p[i];
+        r[i] -= alpha * q[i];
+    }
+}
+
+__global__ void k_cg_dir(int64_t n, double *p, const double *z, double *sc) {
+    const double beta = sc[0] != 0.0 ? sc[2] / sc[0] : 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = z[i] + beta * p[i];
+}
+
+__global__ void k_cg_roll(double *sc) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) sc[0] = sc[2];
+}
+
+__global__ void k_sub_vec(int64_t n, const double *b, const double *ax, double *r) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = b[i] - ax[i];
+}
+
+struct DenseWork {
+    int64_t npad = 0, np = 0;
+    double *L = nullptr, *F = nullptr, *DinvT = nullptr;
+    float *hi = nullptr, *lo = nullptr;
+    double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+    double *part = nullptr, *sc = nullptr;
+    int32_t *err = nullptr;
+    void release() {
+        cudaFree(L); cudaFree(F); cudaFree(DinvT); cudaFree(hi); cudaFree(lo);
+        cudaFree(b); cudaFree(x); cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q);
+        cudaFree(part); cudaFree(sc); cudaFree(err);
+    }
+};
+
+void precond(const DenseWork &w, const double *in, double *out, cudaStream_t s) {
+    cudaMemcpyAsync(out, in, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
+    for (int64_t p = 0; p < w.np; ++p) {
+        k_fwd_diag<<<1, kNB, 0, s>>>(w.DinvT, p, out);
+        const int64_t rows = w.npad - (p + 1) * kNB;
+        if (rows > 0)
+            k_fwd_upd<<<(unsigned)std::min<int64_t>((rows + 7) / 8, 1216), 256, 0, s>>>(w.L, w.npad, p, w.npad, out);
+    }
+    for (int64_t p = w.np - 1; p >= 0; --p) {
+        k_bwd_diag<<<1, kNB, 0, s>>>(w.DinvT, p, out);
+        if (p > 0) k_bwd_upd<<<(unsigned)((p * kNB + 255) / 256), 256, 0, s>>>(w.L, w.npad, p, out);
+    }
+}
+
+void dotv(const DenseWork &w, const double *a, const double *b, double *out, cudaStream_t s) {
+    k_dotp<<<kDotBlk, 256, 0, s>>>(w.npad, a, b, w.part);
+    k_dotf<<<1, 256, 0, s>>>(w.part, out);
+}
+
+}  // namespace
+
+// Solve A x = b for the packed SPD matrix Ap (n, device) and the device
+// vector bx (b in, x out).  mode 0: FP64 factor, mode 1: tensor-core
+// factor; both refined by preconditioned CG in FP64 to rtol.
+int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
+                        int32_t itnlim, mpgpu_solveinfo *info) {
+    cudaStream_t s = c->stream;
+    DenseWork w;
+    w.npad = ((int64_t)n + kNB - 1) / kNB * kNB;
+    w.np = w.npad / kNB;
+    const int64_t nn = w.npad * w.npad;
+    int32_t rc = MPGPU_OK;
+    cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&w.DinvT, sizeof(double) * w.np * kNB * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB);
+    for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
+        if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
+    if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
+    if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w.err, sizeof(int32_t));
+    if (e != cudaSuccess) { w.release(); return cuda_err(c, e, "dense solve allocation"); }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    cudaMemsetAsync(w.F, 0, sizeof(double) * nn, s);
+    k_packed_to_dense<<<4096, 256, 0, s>>>(Ap, n, w.npad, w.L, w.F);
+    if (w.npad > n) k_pad_identity<<<(unsigned)((w.npad - n + 255) / 256), 256, 0, s>>>(w.F, w.npad, n, w.npad);
+    cudaMemsetAsync(w.b, 0, sizeof(double) * w.npad, s);
+    cudaMemcpyAsync(w.b, bx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    // factorisation; a non-positive pivot of the low-precision factor is
+    // cured by a growing diagonal shift (the CG iterations remove it)
+    double shift = 0.0;
+    int tries = 0;
+    for (;; ++tries) {
+        k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, shift);
+        int32_t bad = -1;
+        rc = dense_cholesky_device(c, w.L, w.npad, mode, w.hi, w.lo, w.err, &bad);
+        if (rc != MPGPU_ERR_FACTOR || tries >= 6) break;
+        shift = shift == 0.0 ? 1e-7 : shift * 10.0;
+    }
+    if (rc != MPGPU_OK) { w.release(); return rc; }
+    const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
+    MPG_CUDA(c, cudaFuncSetAttribute(k_trtri_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, trtriSmem));
+    k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
+    // x0 = M^-1 b, r = b - A x0, z = M^-1 r, p = z
+    precond(w, w.b, w.x, s);
+    const unsigned gv = (unsigned)std::min<int64_t>((w.npad + 7) / 8, 4096);
+    k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, w.x, w.q);
+    k_sub_vec<<<(unsigned)((w.npad + 255) / 256), 256, 0, s>>>(w.npad, w.b, w.q, w.r);
+    precond(w, w.r, w.z, s);
+    cudaMemcpyAsync(w.p, w.z, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
+    dotv(w, w.r, w.z, w.sc + 0, s);
+    dotv(w, w.b, w.b, w.sc + 4, s);
+    // one CG iteration as a CUDA graph (its ~600 launches replayed cheaply)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    const unsigned ge = (unsigned)std::min<int64_t>((w.npad + 255) / 256, 4096);
+    MPG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, w.p, w.q);
+    dotv(w, w.p, w.q, w.sc + 1, s);
+    k_cg_step<<<ge, 256, 0, s>>>(w.npad, w.x, w.r, w.p, w.q, w.sc);
+    precond(w, w.r, w.z, s);
+    dotv(w, w.r, w.z, w.sc + 2, s);
+    k_cg_dir<<<ge, 256, 0, s>>>(w.npad, w.p, w.z, w.sc);
+    k_cg_roll<<<1, 32, 0, s>>>(w.sc);
+    dotv(w, w.r, w.r, w.sc + 3, s);
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec, graph, 0);
+    if (ce != cudaSuccess) { w.release(); return cuda_err(c, ce, "CG graph"); }
+    int itn = 0, istop = 0;
+    double hs[5];
+    const double tol2 = rtol * rtol;
+    while (itn < itnlim) {
+        const int batch = std::min(4, itnlim - itn);
+        for (int k = 0; k < batch; ++k) cudaGraphLaunch(gexec, s);
+        itn += batch;
+        MPG_CUDA(c, cudaMemcpyAsync(hs, w.sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        if (!(hs[3] == hs[3])) { istop = 9; break; }
+        if (hs[3] <= tol2 * hs[4]) { istop = 1; break; }
+    }
+    if (istop == 0) istop = 3;
+    cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    cudaEventRecord(e1, s);
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (info) {
+        info->itn = itn;
+        info->istop = istop;
+        info->nrank = n;
+        info->evmin = shift;
+        info->evmax = hs[4] > 0.0 ? std::sqrt(hs[3] / hs[4]) : 0.0;
+        info->ms = ms;
+    }
+    cudaGraphExecDestroy(gexec);
+    cudaGraphDestroy(graph);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    w.release();
+    return istop == 9 ? set_err(c, MPGPU_ERR_NAN, "NaN in the refined dense solve") : MPGPU_OK;
+}

@@ -653,7 +653,7 @@ struct Solver {
 // ---------------------------------------------------------------- inversion / Cholesky
 // minver / mchdec (pede.f90:7838-8054) on the packed matrix
 int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrOut, double *errs,
-                        mpgpu_solveinfo *info, bool decomposition) {
+                        mpgpu_solveinfo *info, bool decomposition, int dense, double rtol, int32_t itnlim) {
     Solver S(c);
     DevJob &j = c->j;
     cudaStream_t s = c->stream;
@@ -718,6 +718,17 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
         MPG_CUDA(c, cudaMemcpyAsync(hu.data(), used, sizeof(int32_t) * nfit, cudaMemcpyDeviceToHost, s));
         MPG_CUDA(c, cudaStreamSynchronize(s));
         for (int32_t u : hu) nrank += u;
+    } else if (dense >= 0) {
+        // blocked dense Cholesky (FP64, or tensor-core 3xTF32) refined by
+        // preconditioned CG in FP64
+        const double tol = rtol > 0.0 ? rtol : 1e-13;
+        const int32_t rcd = dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000, info);
+        if (rcd != MPGPU_OK) {
+            cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
+            cudaFree(used); cudaFree(piv);
+            return rcd;
+        }
+        nrank = info->nrank;
     } else {
         // chdec2 + chslv2 (mpnum.f90:891-987)
         MPG_CUDA(c, cudaMemsetAsync(scal + 16, 0, sizeof(double) * 3, s));

@@ -127,3 +127,19 @@ def test_minres_sparse(mp, orc):
     L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(ba, orc.f64p), C.c_int32(1))
     assert np.max(np.abs(bg - ba[:nfit])) <= 1e-12 * np.max(np.abs(ba))
     L.mpref_ql_destroy(C.c_void_p(q))
+
+
+@pytest.mark.parametrize("metsol", [31, 32])
+def test_dense_refined_solvers(mp, metsol):
+    """Blocked dense Cholesky (32: FP64, 31: tensor-core 3xTF32) refined by
+    FP64 conjugate gradients: the constrained solution agrees with the KKT
+    solution of the same matrix within 1e-9 relative (the telescope matrix
+    has condition ~1e6 after the elimination)."""
+    d, H, A, ctx, lb = build(mp, "telescope", 5000, 1)
+    with ctx:
+        M = ctx.matrix()
+        corr, _, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-14, itnlim=500)
+    n = H.nVar
+    x = kkt_solution(dense_from_packed(M, n), A, lb["gvec"])
+    assert info.istop == 1, (info.istop, info.itn)
+    assert np.max(np.abs(corr - x)) <= 1e-9 * np.max(np.abs(x))
