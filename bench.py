@@ -157,6 +157,52 @@ def record_shape(d):
     return nmeas, nloc, ng, nalg
 
 
+def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000):
+    """Dense solve of the scaled telescope (10 layers x nmod modules = 20,000
+    globals, packed FP64 matrix from the data loop, ncon constraints: the
+    generator's 2 weak-mode constraints plus seeded sparse random ones, all
+    eliminated by QL in FP64): the reference-structured FP64 Cholesky
+    (metsol 3), the blocked FP64 Cholesky (32) and the tensor-core 3xTF32
+    Cholesky (31), the latter two refined by FP64 CG to a relative residual
+    of 1e-13."""
+    cfg = mp.gen_config("telescope_dense", ntracks=ntracks, seed=4)
+    cfg.nmod = nmod
+    d = mp.generate(cfg)
+    H = mp.HostStructure(d, mreqenf=5, sparse=False)
+    A0 = mp.constraint_matrix(d, H)
+    rng = np.random.default_rng(11)
+    extra = np.zeros((ncon - A0.shape[0], H.nVar))
+    for k in range(extra.shape[0]):
+        idx = rng.choice(H.nVar, 64, replace=False)
+        extra[k, idx] = rng.normal(size=64)
+    A = np.vstack([A0, extra])
+    res = {}
+    for metsol in (32, 31, 3):
+        ctx = mp.Context(device=local)
+        ctx.set_layout(H, 1)
+        ctx.set_constraints(A)
+        ctx.upload(H)
+        ctx.loopbf(np.zeros(H.nTotal))
+        corr, _, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-13, itnlim=2000)
+        res[metsol] = (corr, info.ms, info.itn, info.istop, info.msFactor, info.msRefine)
+        ctx.close()
+    ref = res[32][0]
+
+    def rel(x):
+        return float(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+    return {"n": int(H.nVar), "ncon": int(A.shape[0]), "nfit": int(H.nVar - A.shape[0]),
+            "matrix": "scaled telescope, packed FP64 from the data loop",
+            "ms_fp64_chdec2": res[3][1], "ms_fp64_blocked": res[32][1], "ms_mixed_tf32x3": res[31][1],
+            "speedup_mixed_vs_fp64_blocked": res[32][1] / res[31][1],
+            "speedup_mixed_vs_fp64_chdec2": res[3][1] / res[31][1],
+            "ms_factor_fp64_blocked": res[32][4], "ms_factor_mixed": res[31][4],
+            "ms_refine_fp64_blocked": res[32][5], "ms_refine_mixed": res[31][5],
+            "factor_speedup_mixed_vs_fp64_blocked": res[32][4] / max(res[31][4], 1e-9),
+            "cg_iterations_mixed": res[31][2], "cg_iterations_fp64": res[32][2],
+            "rel_err_mixed_vs_fp64": rel(res[31][0]), "rel_err_chdec2_vs_fp64_blocked": rel(res[3][0]),
+            "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
+
+
 def cpu_reference(d, nsample, nthreads, steps=1):
     """CPU oracle (loopbf restatement, OpenMP) on the first nsample records."""
     import oracle_ref as orc
@@ -184,6 +230,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=100_000)
     ap.add_argument("--profile", action="store_true", help="small run for profilers (no e2e/cpu)")
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
+    ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     mp = _load_pkg()
@@ -295,18 +342,20 @@ def main():
         bo = 16 * S.nVar + 256
         barrier(pg)
         t0 = time.perf_counter()
-        up_s, lp_s = [], []
+        up_s, lp_s, up_dev = [], [], []
         for _ in range(args.e2e_steps):
             ta = time.perf_counter()
             ctx.upload(S)
             tb = time.perf_counter()
             ctx.loopbf(gpar)
             up_s.append(tb - ta)
+            up_dev.append(ctx.upload_timing())
             lp_s.append(time.perf_counter() - tb)
         e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
         line["e2e"] = {"value": total_rec / args.steps * args.e2e_steps / e2e_s,
                        "unit": "records/s", "h2d_bytes_per_step": bi, "d2h_bytes_per_step": bo,
-                       "steps": args.e2e_steps, "upload_s": up_s, "loop_s": lp_s}
+                       "steps": args.e2e_steps, "upload_s": up_s, "loop_s": lp_s,
+                       "upload_device_ms": up_dev, "pinned_buffers": len(pinned)}
         if rank == 0:
             nsample = min(args.cpu_sample, nrec)
             val, times = cpu_reference(d, nsample, ncores, steps=1)
@@ -314,6 +363,9 @@ def main():
                                     "kind": "port",
                                     "sample": f"first {nsample} records, one sparse data loop"}
     ctx.close()
+    if args.dense_n > 0 and rank == 0:
+        line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
+                                                  ntracks=20 * args.dense_n)
     for arr in pinned:
         L.mpgpu_host_unregister(C.c_void_p(arr.ctypes.data))
     if rank == 0:

@@ -93,6 +93,11 @@ int32_t mpgpu_upload_records(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr
                              const int32_t *recFile, int32_t nfiles,
                              const double *fileWeight);
 
+/* Device time of the last mpgpu_upload_records: the host-to-device copy of
+ * the records and the record preparation on the device, and the number of
+ * chunks the loop will run in (no counterpart in the reference). */
+int32_t mpgpu_upload_timing(const mpgpu_ctx *ctx, double *msCopy, double *msPrepare, int32_t *nchunk);
+
 typedef struct mpgpu_fitopts {
     int32_t icalcm;    /* 1: build the global matrix */
     int32_t nloopn;    /* data-loop counter (1 = first) */
@@ -172,6 +177,8 @@ typedef struct mpgpu_solveinfo {
     int32_t pad;
     double evmin, evmax;  /* decomposition pivot range */
     double ms;          /* device time of the solve */
+    double msFactor;    /* dense solves: device time of the factorisation */
+    double msRefine;    /* dense solves: device time of the CG refinement */
 } mpgpu_solveinfo;
 
 /* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES)

@@ -289,6 +289,15 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
     return rc;
 }
 
+extern "C" int32_t mpgpu_upload_timing(const mpgpu_ctx *c, double *msCopy, double *msPrepare,
+                                       int32_t *nchunk) {
+    if (!c) return MPGPU_ERR_ARG;
+    if (msCopy) *msCopy = c->j.msUploadCopy;
+    if (msPrepare) *msPrepare = c->j.msUploadPrepare;
+    if (nchunk) *nchunk = c->j.uploadChunks;
+    return MPGPU_OK;
+}
+
 // ------------------------------------------------------------------ data loop
 static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *stats,
                         int32_t *naccf, float *chi2f, int32_t *ndff) {

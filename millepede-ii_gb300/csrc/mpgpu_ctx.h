@@ -122,6 +122,8 @@ struct DevJob {
     double *stage = nullptr;
     int64_t stageLen = 0;
     UpTmp tmp;
+    double msUploadCopy = 0.0, msUploadPrepare = 0.0;   // device time of the last upload
+    int32_t uploadChunks = 0;
     std::unordered_map<const void *, int64_t> cap;   // capacities of the arrays kept between uploads
     // limits over the job (fit kernel shared memory sizing)
     int32_t maxNw = 0, maxNeq = 0, maxNalc = 0, maxNalg = 0, maxBand = -1, maxBdr = 0, maxNgrp = 1;

@@ -116,12 +116,18 @@ __global__ void k_split_tf32(const double *A, int64_t ld, int64_t k0, int64_t nr
 
 // --------------------------------------------- tcgen05 3xTF32 trailing update
 // One CTA per 128 x 128 tile (bi >= bj) of the trailing matrix:
-// C -= L_i L_j^T with K = 128, fed in chunks of 32 (128 bytes per row).
+// C -= L_i L_j^T with K = 128, streamed in chunks of 16 through a 3-stage
+// cp.async pipeline; one thread issues the tcgen05.mma of a chunk
+// (hi*hi, hi*lo, lo*hi for two K = 8 steps) and commits them to the
+// stage's mbarrier, which frees the stage for the chunk three ahead.
 // Shared-memory operand layout: K-major, no swizzle, core matrices of
-// 8 rows x 16 bytes; core (row group g, k group c) at (g * 8 + c) * 128
-// bytes, i.e. leading (K) byte offset 128 and stride (row) byte offset 1024.
-constexpr int kTK = 32;                         // K per chunk
-constexpr int kOpBytes = kNB * kTK * 4;         // 16 KB per operand chunk
+// 8 rows x 16 bytes; core (row group g, k group c) at (g * 4 + c) * 128
+// bytes: leading (K) byte offset 128, stride (row) byte offset 512.
+constexpr int kTK = 16;                          // K per chunk
+constexpr int kStages = 3;
+constexpr int kOpBytes = kNB * kTK * 4;          // 8 KB per operand chunk
+constexpr int kStageBytes = 4 * kOpBytes;        // hi/lo of both operands
+constexpr int kTcSmem = kStages * kStageBytes;  // the epilogue transposes reuse stage 0
 constexpr int kTcThreads = 128;
 constexpr int kWaitLimit = 1 << 22;
 
@@ -130,7 +136,7 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 }
 
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(512 >> 4) << 32) |
            (1ull << 46);
 }
 
@@ -170,88 +176,125 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-// copy a 128 x 32 fp32 chunk (rows of length 128 in global) into the core
-// matrix layout
-__device__ __forceinline__ void load_chunk(const float *g, int kc0, char *s) {
-    for (int idx = threadIdx.x; idx < kNB * (kTK / 4); idx += kTcThreads) {
-        const int row = idx >> 3, k4 = idx & 7;
-        const float4 v = *reinterpret_cast<const float4 *>(g + (int64_t)row * kNB + kc0 + k4 * 4);
-        *reinterpret_cast<float4 *>(s + ((row >> 3) * 8 + k4) * 128 + (row & 7) * 16) = v;
+// asynchronous copy of a 128 x 16 fp32 chunk (rows of 128 in global) into
+// the core-matrix layout; 4 x 16-byte copies per thread
+__device__ __forceinline__ void load_chunk_async(const float *g, int kc0, uint32_t s) {
+#pragma unroll
+    for (int i = 0; i < kNB * (kTK / 4) / kTcThreads; ++i) {
+        const int idx = threadIdx.x + i * kTcThreads;
+        const int row = idx >> 2, k4 = idx & 3;
+        const float *src = g + (int64_t)row * kNB + kc0 + k4 * 4;
+        const uint32_t dst = s + ((row >> 3) * 4 + k4) * 128 + (row & 7) * 16;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
     }
 }
 
 __global__ void __launch_bounds__(kTcThreads) k_syrk_tc(double *A, int64_t ld, int64_t r0, int32_t T,
                                                         const float *hi, const float *lo, int32_t *err) {
-    extern __shared__ __align__(1024) char tsm[];   // Ahi Alo Bhi Blo chunks
-    __shared__ uint64_t mbar;
+    extern __shared__ __align__(128) char tsm[];
+    __shared__ uint64_t mbar[kStages];
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, wib = tid >> 5, ln = tid & 31;
-    // tile (bi, bj), bj <= bi, from the triangular index
     const int64_t t = blockIdx.x;
     int bi = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
     while ((int64_t)bi * (bi + 1) / 2 > t) bi--;
     while ((int64_t)(bi + 1) * (bi + 2) / 2 <= t) bi++;
     const int bj = (int)(t - (int64_t)bi * (bi + 1) / 2);
     if (bi >= T) return;
-    char *sAhi = tsm, *sAlo = tsm + kOpBytes, *sBhi = tsm + 2 * kOpBytes, *sBlo = tsm + 3 * kOpBytes;
+    const uint32_t sbase = smem_u32(tsm);
+    float *epi = reinterpret_cast<float *>(tsm) + wib * 32 * 33;   // after the last MMA only
     if (wib == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tbase)),
                      "r"(kNB));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar)));
+        for (int st = 0; st < kStages; ++st)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[st])));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tbase;
-    const uint32_t mb = smem_u32(&mbar);
-    const float *ahi = hi + (int64_t)bi * kNB * kNB, *alo = lo + (int64_t)bi * kNB * kNB;
-    const float *bhi = hi + (int64_t)bj * kNB * kNB, *blo = lo + (int64_t)bj * kNB * kNB;
-    uint32_t parity = 0;
+    const float *ops[4] = {hi + (int64_t)bi * kNB * kNB, lo + (int64_t)bi * kNB * kNB,
+                           hi + (int64_t)bj * kNB * kNB, lo + (int64_t)bj * kNB * kNB};
+    constexpr int nch = kNB / kTK;
+    uint32_t ph = 0;   // bit st: parity of the next completion of stage st's barrier
     bool ok = true;
-    for (int c = 0; c < kNB / kTK; ++c) {
-        load_chunk(ahi, c * kTK, sAhi);
-        load_chunk(alo, c * kTK, sAlo);
-        load_chunk(bhi, c * kTK, sBhi);
-        load_chunk(blo, c * kTK, sBlo);
+    for (int c = 0; c < kStages - 1; ++c) {
+#pragma unroll
+        for (int o = 0; o < 4; ++o) load_chunk_async(ops[o], c * kTK, sbase + c * kStageBytes + o * kOpBytes);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    }
+    for (int c = 0; c < nch; ++c) {
+        const int st = c % kStages;
+        asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 2) : "memory");
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sb = sbase + st * kStageBytes;
 #pragma unroll
             for (int kk = 0; kk < kTK / 8; ++kk) {
                 const uint32_t off = kk * 256;   // 8 tf32 = 2 core matrices along K
-                const uint64_t dah = umma_desc(smem_u32(sAhi) + off), dal = umma_desc(smem_u32(sAlo) + off);
-                const uint64_t dbh = umma_desc(smem_u32(sBhi) + off), dbl = umma_desc(smem_u32(sBlo) + off);
+                const uint64_t dah = umma_desc(sb + off), dal = umma_desc(sb + kOpBytes + off);
+                const uint64_t dbh = umma_desc(sb + 2 * kOpBytes + off), dbl = umma_desc(sb + 3 * kOpBytes + off);
                 mma_tf32(tmem, dah, dbh, (c > 0 || kk > 0) ? 1u : 0u);
                 mma_tf32(tmem, dah, dbl, 1u);
                 mma_tf32(tmem, dal, dbh, 1u);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mb)
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&mbar[st]))
                          : "memory");
         }
-        if (!mbar_wait(mb, parity)) {
-            // give the tensor core one more bounded wait before the tensor
-            // memory is released
-            mbar_wait(mb, parity);
-            ok = false;
-            break;
+        // the stage of chunk c + kStages - 1 held chunk c - 1: wait for its MMAs
+        const int cn = c + kStages - 1;
+        if (cn < nch) {
+            const int sn = cn % kStages;
+            if (c >= 1) {
+                if (!mbar_wait(smem_u32(&mbar[sn]), (ph >> sn) & 1)) { ok = false; }
+                ph ^= 1u << sn;
+            }
+            if (ok)
+#pragma unroll
+                for (int o = 0; o < 4; ++o)
+                    load_chunk_async(ops[o], cn * kTK, sbase + sn * kStageBytes + o * kOpBytes);
         }
-        parity ^= 1;
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        if (!__syncthreads_and(ok)) { ok = false; break; }
     }
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    // wait for the MMAs of the chunks not yet waited for (the last kStages-1)
     if (ok) {
-        // rows of warp w = tensor-memory lanes 32w .. 32w+31
-        const int row = wib * 32 + ln;
-        double *crow = A + (r0 + (int64_t)bi * kNB + row) * ld + r0 + (int64_t)bj * kNB;
+        for (int c = (nch > kStages - 1 ? nch - (kStages - 1) : 0); c < nch; ++c) {
+            const int st = c % kStages;
+            if (!mbar_wait(smem_u32(&mbar[st]), (ph >> st) & 1)) ok = false;
+            ph ^= 1u << st;
+        }
+    } else {
+        for (int st = 0; st < kStages; ++st) mbar_wait(smem_u32(&mbar[st]), (ph >> st) & 1);
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (__syncthreads_and(ok)) {   // every MMA done: the stages are free for the transposes
+        // rows of warp w = tensor-memory lanes 32w .. 32w+31; transpose each
+        // 32 x 32 block through shared memory so the FP64 update is coalesced
+        const int64_t rowBase = r0 + (int64_t)bi * kNB + wib * 32;
+        const int64_t colBase = r0 + (int64_t)bj * kNB;
         for (int cb = 0; cb < kNB / 32; ++cb) {
             uint32_t v[32];
             tmem_ld32(tmem + ((uint32_t)(wib * 32) << 16) + (uint32_t)(cb * 32), v);
 #pragma unroll
-            for (int q = 0; q < 32; ++q) crow[cb * 32 + q] -= (double)__uint_as_float(v[q]);
+            for (int q = 0; q < 32; ++q) epi[ln * 33 + q] = __uint_as_float(v[q]);
+            __syncwarp();
+            // all 32 loads in flight before the subtractions
+            double cv[32];
+            double *cp = A + rowBase * ld + colBase + cb * 32 + ln;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) cv[r] = cp[r * ld];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) cp[r * ld] = cv[r] - (double)epi[r * 33 + ln];
+            __syncwarp();
         }
     } else if (tid == 0) {
         atomicExch(err, -1);
@@ -320,7 +363,7 @@ int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, f
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
     const int potrfSmem = kNB * (kNB + 1) * (int)sizeof(double);
     const int trsmSmem = (kNB * kNB + kNB) * (int)sizeof(double);
-    const int tcSmem = 4 * kOpBytes;
+    const int tcSmem = kTcSmem;
     MPG_CUDA(c, cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, potrfSmem));
     MPG_CUDA(c, cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize, trsmSmem));
     MPG_CUDA(c, cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcSmem));
@@ -679,6 +722,9 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         shift = shift == 0.0 ? 1e-7 : shift * 10.0;
     }
     if (rc != MPGPU_OK) { w.release(); return rc; }
+    cudaEvent_t eF;
+    cudaEventCreate(&eF);
+    cudaEventRecord(eF, s);
     const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
     MPG_CUDA(c, cudaFuncSetAttribute(k_trtri_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, trtriSmem));
     k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
@@ -723,9 +769,13 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
     cudaEventRecord(e1, s);
     MPG_CUDA(c, cudaStreamSynchronize(s));
-    float ms = 0.0f;
+    float ms = 0.0f, msF = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventElapsedTime(&msF, e0, eF);
+    cudaEventDestroy(eF);
     if (info) {
+        info->msFactor = msF;
+        info->msRefine = ms - msF;
         info->itn = itn;
         info->istop = istop;
         info->nrank = n;

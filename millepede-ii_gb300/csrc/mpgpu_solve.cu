@@ -83,20 +83,47 @@ __global__ void k_qlapply(double *x, const double *V, const double *Vk, const in
 }
 
 // ---------------------------------------------------------------- packed products
-// y = A x for the packed symmetric matrix, one warp per row: lower part of
-// row i (contiguous) plus the column part below the diagonal.
-__global__ void k_packed_matvec(int32_t n, const double *A, const double *x, double *y) {
-    const int ln = threadIdx.x & 31;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = w; i < n; i += nw) {
-        const int64_t ro = i * (i + 1) / 2;  // 0-based row i start
+// y = A x for the packed symmetric matrix in two deterministic passes.
+// Pass 1, one CTA per block of 64 rows: the lower part of each row (one
+// warp per row, contiguous) and, per column j left of the block's last row,
+// the partial column sum over the block's rows (one thread per column,
+// contiguous across threads).  Pass 2 adds, per j, the row part and the
+// partial column sums of the blocks below j in block order.
+constexpr int kMvRows = 16;
+
+__global__ void __launch_bounds__(256) k_pmv_blocks(int32_t n, const double *A, const double *x, double *yrow,
+                                                     double *part) {
+    const int64_t b = blockIdx.x;
+    const int64_t i0 = b * kMvRows, i1 = min((int64_t)n, i0 + kMvRows);
+    const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    __shared__ double xs[kMvRows];
+    if (threadIdx.x < kMvRows) xs[threadIdx.x] = i0 + threadIdx.x < n ? x[i0 + threadIdx.x] : 0.0;
+    __syncthreads();
+    for (int64_t i = i0 + wib; i < i1; i += 8) {
+        const double *row = A + i * (i + 1) / 2;
         double s = 0.0;
-        for (int64_t j = ln; j <= i; j += 32) s += A[ro + j] * x[j];
-        for (int64_t r = i + 1 + ln; r < n; r += 32) s += A[r * (r + 1) / 2 + i] * x[r];
+        for (int64_t j = ln; j <= i; j += 32) s += row[j] * x[j];
+#pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (ln == 0) y[i] = s;
+        if (ln == 0) yrow[i] = s;
     }
+    for (int64_t j = threadIdx.x; j < i1 - 1; j += blockDim.x) {
+        double s = 0.0;
+        const int64_t ifirst = j + 1 > i0 ? j + 1 : i0;
+        for (int64_t i = ifirst; i < i1; ++i) s += A[i * (i + 1) / 2 + j] * xs[i - i0];
+        part[b * (int64_t)n + j] = s;
+    }
+}
+
+__global__ void k_pmv_final(int32_t n, int64_t nb, const double *yrow, const double *part, double *y) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s = yrow[j];
+    for (int64_t b = (j + 1) / kMvRows; b < nb; ++b) {
+        const int64_t i1 = min((int64_t)n, (b + 1) * kMvRows);
+        if (j < i1 - 1) s += part[b * (int64_t)n + j];
+    }
+    y[j] = s;
 }
 
 // qlssq update of one reflection on the packed matrix (mpqldec.f90:
@@ -112,13 +139,14 @@ __global__ void k_qlssq_update(int32_t n, double *A, const double *v, double vk,
     for (int64_t i1 = 1 + w; i1 <= n; i1 += nw) {   // 1-based row
         double *row = A + (i1 * i1 - i1) / 2 - 1;     // row[c] = A(i1, c), c 1-based
         const double vi = (i1 <= ilast) ? v[i1 - 1] : (i1 == kn ? vk : 0.0);
-        if (i1 <= kn) {
-            const int64_t il = ilast < i1 ? ilast : i1;
-            const double f = 2.0 * vi * vtAv - Av[i1 - 1];
-            for (int64_t cc = 1 + ln; cc <= il; cc += 32) row[cc] = row[cc] + 2.0 * (f * v[cc - 1]);
-        }
         if (i1 <= ilast) {
-            for (int64_t cc = 1 + ln; cc <= i1; cc += 32) row[cc] = row[cc] - 2.0 * Av[cc - 1] * vi;
+            // both corrections of the reference, in its order, in one pass
+            const double f = 2.0 * vi * vtAv - Av[i1 - 1];
+            for (int64_t cc = 1 + ln; cc <= i1; cc += 32)
+                row[cc] = (row[cc] + 2.0 * (f * v[cc - 1])) - 2.0 * Av[cc - 1] * vi;
+        } else if (i1 <= kn) {
+            const double f = 2.0 * vi * vtAv - Av[i1 - 1];
+            for (int64_t cc = 1 + ln; cc <= ilast; cc += 32) row[cc] = row[cc] + 2.0 * (f * v[cc - 1]);
         }
         if (i1 == kn && ln == 0) row[kn] = row[kn] + 2.0 * ((2.0 * vk * vtAv - Av[kn - 1]) * vk - Av[kn - 1] * vk);
         if (i1 > kn) {
@@ -539,6 +567,7 @@ struct Solver {
     ~Solver() {
         dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
         dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tbuf); dfree(part);
+        dfree(pmvRow); dfree(pmvPart);
     }
     unsigned grid(int64_t n, int per = kThreads) const {
         int64_t g = (n + per - 1) / per;
@@ -547,6 +576,22 @@ struct Solver {
         return (unsigned)(g < 1 ? 1 : g);
     }
     unsigned wgrid(int64_t nwarp) const { return grid(nwarp * 32); }
+
+    // packed symmetric product (two passes; buffers kept for the solve)
+    double *pmvRow = nullptr, *pmvPart = nullptr;
+    int64_t pmvN = 0;
+    void packed_matvec(int32_t n, const double *A, const double *x, double *y) {
+        const int64_t nb = ((int64_t)n + kMvRows - 1) / kMvRows;
+        if (pmvN != n) {
+            dfree(pmvRow);
+            dfree(pmvPart);
+            cudaMalloc(&pmvRow, sizeof(double) * std::max<int64_t>(n, 1));
+            cudaMalloc(&pmvPart, sizeof(double) * std::max<int64_t>(nb * n, 1));
+            pmvN = n;
+        }
+        k_pmv_blocks<<<(unsigned)nb, 256, 0, s>>>(n, A, x, pmvRow, pmvPart);
+        k_pmv_final<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nb, pmvRow, pmvPart, y);
+    }
 
     // block table of the sparse storage, built from the host copies
     int32_t build_blocks() {
@@ -638,7 +683,7 @@ struct Solver {
             k_spmv_cols<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.colStart, sb.colBlk, sb.tOff,
                                                          sb.tbuf, y);
         } else {
-            k_packed_matvec<<<wgrid(j.nVar), kThreads, 0, s>>>(j.nVar, j.matD, x, y);
+            packed_matvec(j.nVar, j.matD, x, y);
         }
     }
     void qlmlq(double *x, int t) {

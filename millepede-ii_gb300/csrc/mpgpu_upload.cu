@@ -798,6 +798,9 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     MPG_CUDA(c, dgrow(j, j.inder, j.nw));
     MPG_CUDA(c, dgrow(j, j.glder, j.nw));
     MPG_CUDA(c, dgrow(j, t.recPtr, n1));
+    cudaEvent_t ev[3];
+    for (auto &x : ev) cudaEventCreate(&x);
+    cudaEventRecord(ev[0], s);
     MPG_CUDA(c, cudaMemcpyAsync(j.inder, inder + recPtr[0], sizeof(int32_t) * j.nw, cudaMemcpyHostToDevice, s));
     MPG_CUDA(c, cudaMemcpyAsync(j.glder, glder + recPtr[0], sizeof(double) * j.nw, cudaMemcpyHostToDevice, s));
     MPG_CUDA(c, cudaMemcpyAsync(t.recPtr, recPtr, sizeof(int64_t) * n1, cudaMemcpyHostToDevice, s));
@@ -807,6 +810,7 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
         MPG_CUDA(c, cudaMemcpyAsync(t.recFile, recFile, sizeof(int32_t) * nrec, cudaMemcpyHostToDevice, s));
         dRecFile = t.recFile;
     }
+    cudaEventRecord(ev[1], s);
     MPG_CUDA(c, dgrow(j, j.rec, nrec));
     MPG_CUDA(c, dgrow(j, t.cnt, 6 * n1));
     MPG_CUDA(c, dgrow(j, t.scanTmp, scan_tmp_len(std::max<int64_t>(n1, 256 * 8))));
@@ -1065,6 +1069,14 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     MPG_CUDA(c, dgrow(j, j.partial, j.partialLen));
     j.stageLen = std::max<int64_t>(maxStage, 1);
     MPG_CUDA(c, dgrow(j, j.stage, (nchunk > 1 ? 2 : 1) * j.stageLen));
+    cudaEventRecord(ev[2], s);
     MPG_CUDA(c, cudaStreamSynchronize(s));
+    float t01 = 0.0f, t12 = 0.0f;
+    cudaEventElapsedTime(&t01, ev[0], ev[1]);
+    cudaEventElapsedTime(&t12, ev[1], ev[2]);
+    j.msUploadCopy = t01;
+    j.msUploadPrepare = t12;
+    j.uploadChunks = (int32_t)nchunk;
+    for (auto &x : ev) cudaEventDestroy(x);
     return MPGPU_OK;
 }

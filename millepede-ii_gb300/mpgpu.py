@@ -40,7 +40,7 @@ class FitStats(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
                 ("pad", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
-                ("ms", C.c_double)]
+                ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double)]
 
 
 class Steer(C.Structure):
@@ -110,7 +110,7 @@ EXPORTS = [
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
     "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
-    "mpgpu_dense_cholesky",
+    "mpgpu_dense_cholesky", "mpgpu_upload_timing",
     "mpgpu_host_register", "mpgpu_host_unregister",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
@@ -315,6 +315,12 @@ class Context:
         self.check(self.L.mpgpu_upload_records(
             self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(S.tinder, i32p),
             ptr(S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
+
+    def upload_timing(self):
+        """(ms copy, ms prepare, chunks) of the last upload."""
+        a, b, n = C.c_double(), C.c_double(), C.c_int32()
+        self.check(self.L.mpgpu_upload_timing(self.h, C.byref(a), C.byref(b), C.byref(n)))
+        return a.value, b.value, n.value
 
     def loopbf(self, gpar, **kw):
         o = dict(icalcm=1, nloopn=1, lhuber=0, lfitbb=1, chicut=0.0, chhuge=50.0, dwcut=0.0,
