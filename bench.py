@@ -203,6 +203,48 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000):
             "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
 
 
+def serve_measure(mp, local, njobs=24, rate=8.0, nmin=500, nmax=20000, rmin=10_000, rmax=200_000):
+    """Stream of alignment jobs through the serving loop: Poisson arrivals at
+    `rate` per second; per job (seed 1000 + job) a telescope with globals
+    log-uniform in [nmin, nmax] and records log-uniform in [rmin, rmax],
+    3 iterations with outlier down-weighting, dense solve (tensor-core
+    factor + FP64 CG).  The same jobs, same arrivals, one at a time with the
+    FP64 blocked dense solve, give the plain-form comparison."""
+    rng = np.random.default_rng(7)
+    specs = []
+    for k in range(njobs):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        nrec = int(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
+        cfg = mp.gen_config("telescope", ntracks=nrec, seed=1000 + k)
+        cfg.nmod = max(n // 10, 5)
+        specs.append(mp.generate(cfg))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, njobs))
+
+    def run(metsol, active):
+        jds = [mp.JobData(d, metsol=metsol, matsto=1, mitera=3, lhuber=2, chicut=30.0, chirem=6.0,
+                          mreqenf=5) for d in specs]
+        with mp.Server(device=local, max_active=active) as srv:
+            t0 = time.perf_counter()
+            tickets = []
+            for jd, ta in zip(jds, arrivals):
+                dt = ta - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets.append(srv.submit(jd))
+            out = [srv.wait(t, timeout_ms=1.8e6) for t in tickets]
+            span = time.perf_counter() - t0
+        lat = np.array([o[1] for o in out])
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "jobs_per_s": njobs / span, "ok": all(o[0] == 0 for o in out)}, jds
+    served, jds = run(31, 4)
+    plain, jdp = run(32, 1)
+    diff = max(float(np.max(np.abs(a.parameters()[1] - b.parameters()[1])) /
+                     max(float(np.max(np.abs(b.parameters()[1]))), 1e-300)) for a, b in zip(jds, jdp))
+    return {"jobs": njobs, "arrival_rate_per_s": rate, "globals": [nmin, nmax], "records": [rmin, rmax],
+            "iterations": 3, "served_concurrent_mixed": served, "one_at_a_time_fp64": plain,
+            "max_rel_diff_parameters": diff}
+
+
 def cpu_reference(d, nsample, nthreads, steps=1):
     """CPU oracle (loopbf restatement, OpenMP) on the first nsample records."""
     import oracle_ref as orc
@@ -231,6 +273,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="small run for profilers (no e2e/cpu)")
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
+    ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     mp = _load_pkg()
@@ -363,6 +406,8 @@ def main():
                                     "kind": "port",
                                     "sample": f"first {nsample} records, one sparse data loop"}
     ctx.close()
+    if args.serve_jobs > 0 and rank == 0:
+        line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
     if args.dense_n > 0 and rank == 0:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n)

@@ -287,6 +287,32 @@ int32_t mpgpu_pede_run(mpgpu_ctx *ctx, const mpgpu_steer *st, const mpgpu_job *j
 int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors);
 
 /* ------------------------------------------------------------------
+ * Serving: a resident loop that runs alignment jobs as they arrive (no
+ * counterpart in the reference, which runs one job per process).  maxActive
+ * worker contexts run jobs concurrently on the device; a job is admitted
+ * when its device footprint fits in budgetBytes next to the running jobs,
+ * in submission order.  A job's result does not depend on the other jobs.
+ * ---------------------------------------------------------------- */
+typedef struct mpgpu_server mpgpu_server;
+typedef struct mpgpu_server_cfg {
+    int32_t device;
+    int32_t maxActive;      /* jobs on the device at once (0: 4) */
+    int64_t budgetBytes;    /* device memory budget for admitted jobs (0: 150 GB) */
+} mpgpu_server_cfg;
+int32_t mpgpu_server_create(mpgpu_server **srv, const mpgpu_server_cfg *cfg);
+/* Queue a job (as mpgpu_pede_run); st, job, res and all arrays they point
+ * to must stay valid until mpgpu_server_wait has returned for the ticket. */
+int32_t mpgpu_server_submit(mpgpu_server *srv, const mpgpu_steer *st, const mpgpu_job *job,
+                            mpgpu_result *res, int64_t *ticket);
+/* Wait for a job (timeoutMs <= 0: no limit; MPGPU_ERR_TIMEOUT when it ran
+ * out); returns the job's status and its latency (submission to end), its
+ * wait for a worker and its admitted device footprint. */
+int32_t mpgpu_server_wait(mpgpu_server *srv, int64_t ticket, double timeoutMs, double *msLatency,
+                          double *msQueue, int64_t *bytes);
+/* Runs the queued jobs to the end, then releases the workers. */
+int32_t mpgpu_server_destroy(mpgpu_server *srv);
+
+/* ------------------------------------------------------------------
  * Synthetic Mille data (role of pede -t / mptest1 / mptest2)
  * ---------------------------------------------------------------- */
 typedef struct mpgen_cfg {

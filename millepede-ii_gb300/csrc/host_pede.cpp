@@ -10,6 +10,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <functional>
 #include <vector>
 
 #include "../../include/mpgpu.h"
@@ -325,23 +326,19 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
 }
 
 // ------------------------------------------------------------------ job
-namespace {
-
-struct Timer {
-    double ms = 0.0;
-};
-
-int32_t qlbsub_host(int32_t ncon, const std::vector<double> &, const double *, double *) { return ncon; }
-
-}  // namespace
 
 // Whole alignment job: structure on the host, data loops and solves on the
 // device.  Iteration control of xloopn (pede.f90:8501-9334) without line
 // search and function-value loops: every iteration rebuilds the matrix,
 // solves and adds the correction; chi2-cut factors per loop as in loopn
 // (pede.f90:2583-2593).
-extern "C" int32_t mpgpu_pede_run(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job,
-                                  mpgpu_result *res) {
+// Whole job; `admit`, when given, is asked for the job's device footprint
+// after the host structure passes and before any device allocation of the
+// job, and may block until that much of the device budget is free (the
+// serving loop, mpgpu_serve.cpp); it returns false when the job can never
+// fit.
+int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job, mpgpu_result *res,
+                          const std::function<bool(int64_t)> &admit) {
     if (!st || !job || !res) return MPGPU_ERR_ARG;
     mpgpu_ctx *ctx = ctxIn;
     if (!ctx) {
@@ -391,6 +388,26 @@ extern "C" int32_t mpgpu_pede_run(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const
                                   aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat) == 0)
                 break;
             capc *= 4;
+        }
+    }
+    if (admit) {
+        // device footprint: records and their tables, update staging
+        // (bounded by the squared words per record), matrix, dense solve
+        int64_t stage = 0;
+        for (int64_t r = 0; r < job->nrec; ++r) {
+            const int64_t w = job->recPtr[r + 1] - job->recPtr[r];
+            stage += (w / 2) * (w / 2 + 1) / 2;
+        }
+        const int64_t nm = st->matsto == 2 ? nmat : (int64_t)nVar * (nVar + 1) / 2;
+        const int64_t npad = ((int64_t)nVar + 127) / 128 * 128;
+        const int64_t dense = (st->metsol == 31 || st->metsol == 32) ? 2 * npad * npad : 0;
+        const int64_t stageCap = (int64_t)2 << 30;   // 2 x 8 GiB staging buffers at most (in doubles)
+        const int64_t bytes = 40 * nw + 8 * (std::min(stage, stageCap) + nm + dense) + 64 * (int64_t)nVar +
+                              ((int64_t)64 << 20);
+        if (!admit(bytes)) {
+            res->exitCode = MPGPU_ERR_BUDGET;
+            if (!ctxIn) mpgpu_destroy(ctx);
+            return MPGPU_ERR_BUDGET;
         }
     }
     rc = mpgpu_set_layout(ctx, ntot, res->varIndex, nVar, nG, aig.data(), st->matsto,
@@ -538,8 +555,12 @@ extern "C" int32_t mpgpu_pede_run(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const
     }
     res->exitCode = rc;
     if (!ctxIn) mpgpu_destroy(ctx);
-    (void)qlbsub_host;
     return rc;
+}
+
+extern "C" int32_t mpgpu_pede_run(mpgpu_ctx *ctx, const mpgpu_steer *st, const mpgpu_job *job,
+                                  mpgpu_result *res) {
+    return pede_run_admitted(ctx, st, job, res, nullptr);
 }
 
 namespace {

@@ -111,6 +111,7 @@ EXPORTS = [
     "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
     "mpgpu_dense_cholesky", "mpgpu_upload_timing",
+    "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
     "mpgpu_host_register", "mpgpu_host_unregister",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
@@ -406,3 +407,98 @@ def constraint_matrix(data, S):
             if li is not None and S.varIndex[li] > 0:
                 A[c, S.varIndex[li] - 1] += cc[k]
     return A
+
+
+# ----------------------------------------------------------------- whole jobs
+class JobData:
+    """A job's C structures (mpgpu_steer, mpgpu_job, mpgpu_result) with the
+    numpy arrays they point to kept alive."""
+
+    def __init__(self, data, constraints=None, **steer):
+        st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
+                  dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
+                  mrestl=1e-10, itnlim=2000, nthreads=0)
+        st.update(steer)
+        self.steer = Steer(**st)
+        self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
+        self.inder = np.ascontiguousarray(data["inder"], np.int32)
+        self.glder = np.ascontiguousarray(data["glder"], np.float64)
+        j = Job()
+        j.nrec = len(self.recPtr) - 1
+        j.recPtr, j.inder, j.glder = ptr(self.recPtr, i64p), ptr(self.inder, i32p), ptr(self.glder, f64p)
+        j.nfiles = 1
+        if constraints is None and data.get("ncon", 0) > 0:
+            constraints = (data["conStart"], data["conLabel"], data["conCoef"])
+        if constraints is not None:
+            self.conStart = np.ascontiguousarray(constraints[0], np.int32)
+            self.conLabel = np.ascontiguousarray(constraints[1], np.int32)
+            self.conCoef = np.ascontiguousarray(constraints[2], np.float64)
+            self.conRhs = np.zeros(len(self.conStart) - 1)
+            j.ncon = len(self.conStart) - 1
+            j.conStart, j.conLabel = ptr(self.conStart, i32p), ptr(self.conLabel, i32p)
+            j.conCoef, j.conRhs = ptr(self.conCoef, f64p), ptr(self.conRhs, f64p)
+        self.job = j
+        cap = len(self.inder) + 16
+        self.labels = np.zeros(cap, np.int32)
+        self.parameter = np.zeros(cap)
+        self.presigma = np.zeros(cap)
+        self.error = np.zeros(cap)
+        self.counts = np.zeros(cap, np.int64)
+        self.varIndex = np.zeros(cap, np.int32)
+        r = Result()
+        r.cap = cap
+        r.labels, r.parameter = ptr(self.labels, i32p), ptr(self.parameter, f64p)
+        r.presigma, r.error = ptr(self.presigma, f64p), ptr(self.error, f64p)
+        r.counts, r.varIndex = ptr(self.counts, i64p), ptr(self.varIndex, i32p)
+        self.res = r
+
+    def parameters(self):
+        n = self.res.nTotal
+        return self.labels[:n].copy(), self.parameter[:n].copy()
+
+
+class ServerCfg(C.Structure):
+    _fields_ = [("device", C.c_int32), ("maxActive", C.c_int32), ("budgetBytes", C.c_int64)]
+
+
+class Server:
+    """Resident request loop (mpgpu_server_*): submit JobData, wait by ticket."""
+
+    def __init__(self, device=0, max_active=4, budget_bytes=0):
+        self.L = lib()
+        self.h = C.c_void_p()
+        cfg = ServerCfg(device=device, maxActive=max_active, budgetBytes=budget_bytes)
+        rc = self.L.mpgpu_server_create(C.byref(self.h), C.byref(cfg))
+        if rc != 0:
+            raise RuntimeError(f"mpgpu_server_create: {rc}")
+
+    def submit(self, jd):
+        t = C.c_int64()
+        rc = self.L.mpgpu_server_submit(self.h, C.byref(jd.steer), C.byref(jd.job), C.byref(jd.res),
+                                        C.byref(t))
+        if rc != 0:
+            raise RuntimeError(f"mpgpu_server_submit: {rc}")
+        return t.value
+
+    def wait(self, ticket, timeout_ms=0.0):
+        lat, q, b = C.c_double(), C.c_double(), C.c_int64()
+        rc = self.L.mpgpu_server_wait(self.h, C.c_int64(ticket), C.c_double(timeout_ms), C.byref(lat),
+                                      C.byref(q), C.byref(b))
+        return rc, lat.value, q.value, b.value
+
+    def close(self):
+        if self.h:
+            self.L.mpgpu_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run_job(jd, ctx=None):
+    """Whole job through mpgpu_pede_run (private context when ctx is None)."""
+    return lib().mpgpu_pede_run(ctx.h if ctx is not None else None, C.byref(jd.steer), C.byref(jd.job),
+                                C.byref(jd.res))
