@@ -280,6 +280,18 @@ int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *in
                           int32_t nG, const int32_t *allIndexGroups, int64_t cap,
                           int64_t *offsets, int32_t *columns, int64_t *ncolw, int64_t *nmat);
 
+/* Mille binary files (C or Fortran record framing, float or double words;
+ * recognised per file) into record arrays, the file part of readFromBinary
+ * (pede.f90:1714-2075).  First call with inder == NULL: *nrec and *nw
+ * receive the sizes.  Second call: recPtr[nrec+1], inder[nw], glder[nw]
+ * (float words widened to double) and recFile[nrec] (1-based file index,
+ * may be NULL) are filled; cap is the length of inder/glder.  maxRec > 0
+ * limits the records read per file.  Status 20 on a damaged record. */
+#define MPGPU_FILE_WORDS_MAX 16777216
+int32_t mpgpu_read_mille(int32_t nfiles, const char *const *files, int64_t maxRec, int64_t cap,
+                         int64_t *nrec, int64_t *nw, int64_t *recPtr, int32_t *inder, double *glder,
+                         int32_t *recFile);
+
 /* Whole alignment job on the GPU (iteration control of xloopn without line
  * search); ctx may be NULL (a private context is created). */
 int32_t mpgpu_pede_run(mpgpu_ctx *ctx, const mpgpu_steer *st, const mpgpu_job *job,

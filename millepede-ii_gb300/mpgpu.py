@@ -112,6 +112,7 @@ EXPORTS = [
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
     "mpgpu_dense_cholesky", "mpgpu_upload_timing",
     "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
+    "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
@@ -177,6 +178,28 @@ def write_mille_c(path, recPtr, inder, glder):
             np.array([-2 * (b - a)], np.int32).tofile(f)
             glder[a:b].tofile(f)
             inder[a:b].tofile(f)
+
+
+def read_mille(paths, max_rec=0):
+    """Records of Mille binary files through mpgpu_read_mille (C or Fortran
+    framing, float or double): (recPtr, inder, glder, recFile)."""
+    L = lib()
+    arr = (C.c_char_p * len(paths))(*[p.encode() for p in paths])
+    nrec, nw = C.c_int64(), C.c_int64()
+    rc = L.mpgpu_read_mille(C.c_int32(len(paths)), arr, C.c_int64(max_rec), C.c_int64(0), C.byref(nrec),
+                            C.byref(nw), None, None, None, None)
+    if rc != 0:
+        raise RuntimeError(f"mpgpu_read_mille: {rc}")
+    recPtr = np.zeros(nrec.value + 1, np.int64)
+    inder = np.zeros(nw.value, np.int32)
+    glder = np.zeros(nw.value, np.float64)
+    recFile = np.zeros(nrec.value, np.int32)
+    rc = L.mpgpu_read_mille(C.c_int32(len(paths)), arr, C.c_int64(max_rec), C.c_int64(nw.value),
+                            C.byref(nrec), C.byref(nw), ptr(recPtr, i64p), ptr(inder, i32p),
+                            ptr(glder, f64p), ptr(recFile, i32p))
+    if rc != 0:
+        raise RuntimeError(f"mpgpu_read_mille: {rc}")
+    return recPtr, inder, glder, recFile
 
 
 def read_mille_c(path):
