@@ -56,9 +56,14 @@ extern "C" {
 
 typedef struct mpgpu_ctx mpgpu_ctx;
 
+/* cfg flags: run every record through the large-record path (B and W of a
+ * record in global memory, W B^T by a tiled kernel), which is otherwise
+ * chosen only when the records are too large for the per-warp form */
+#define MPGPU_FLAG_LARGE_RECORDS 1
+
 typedef struct mpgpu_cfg {
     int32_t device;             /* CUDA device ordinal */
-    int32_t flags;              /* reserved, 0 */
+    int32_t flags;              /* MPGPU_FLAG_* */
     int64_t staging_bytes;      /* update staging per chunk (0: sized per job, one chunk when it fits) */
 } mpgpu_cfg;
 

@@ -86,6 +86,7 @@ extern "C" int32_t mpgpu_create(mpgpu_ctx **out, const mpgpu_cfg *cfg) {
     mpgpu_ctx *c = new mpgpu_ctx();
     c->device = cfg ? cfg->device : 0;
     c->stagingBytes = (cfg && cfg->staging_bytes > 0) ? cfg->staging_bytes : 0;  // 0: sized per job
+    c->flags = cfg ? cfg->flags : 0;
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
@@ -324,6 +325,17 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.bandmax = opt->lfitbb > 0 ? j.maxBand : -1; fp.bdrmax = j.maxBdr;
     fp.ngrpmax = std::max(j.maxNgrp, 1);
     fp.errFlag = errFlag;
+    // records too large for B and W in each warp's shared memory (fewer than
+    // four warps per CTA) take the large-record path
+    fp.bigMode = (c->flags & MPGPU_FLAG_LARGE_RECORDS) || fit_warps_per_cta(fp) < 4 ? 1 : 0;
+    int64_t sub = 0;
+    if (fp.bigMode) {
+        fp.bwStride = 2 * (int64_t)fp.nalgmax * fp.nalcmax;
+        // records per fit launch: their B and W within 2 GiB
+        sub = std::max<int64_t>(1, ((int64_t)2 << 30) / (8 * std::max<int64_t>(fp.bwStride, 1)));
+        MPG_CUDA(c, dgrow(j, j.bw, sub * fp.bwStride));
+        fp.bw = j.bw;
+    }
     if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     AccParams ap{};
     ap.bkI = j.bkI; ap.bkJ = j.bkJ; ap.bkLd = j.bkLd; ap.bkOff = j.bkOff;
@@ -360,7 +372,21 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         if (overlap && ch >= 2) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[ch - 2], 0));
         fp.stage = stg;
         cudaEventRecord(evF0[ch], s);
-        if (fp.r1 > fp.r0) { MPG_CUDA(c, launch_fit(fp, nsm, 0, s)); launches++; }
+        if (fp.bigMode) {
+            const int64_t c0 = fp.r0, c1 = fp.r1;
+            for (int64_t a = c0; a < c1; a += sub) {
+                fp.r0 = a;
+                fp.r1 = std::min(c1, a + sub);
+                MPG_CUDA(c, launch_fit(fp, nsm, 0, s));
+                MPG_CUDA(c, launch_update_big(fp, s));
+                launches += 2;
+            }
+            fp.r0 = c0;
+            fp.r1 = c1;
+        } else if (fp.r1 > fp.r0) {
+            MPG_CUDA(c, launch_fit(fp, nsm, 0, s));
+            launches++;
+        }
         cudaEventRecord(evF1[ch], s);
         MPG_CUDA(c, cudaStreamWaitEvent(s2, evF1[ch], 0));
         ap.stage = stg;

@@ -122,6 +122,7 @@ struct DevJob {
     double *stage = nullptr;
     int64_t stageLen = 0;
     UpTmp tmp;
+    double *bw = nullptr;              // large-record mode: B and W of a record range
     double msUploadCopy = 0.0, msUploadPrepare = 0.0;   // device time of the last upload
     int32_t uploadChunks = 0;
     std::unordered_map<const void *, int64_t> cap;   // capacities of the arrays kept between uploads
@@ -145,6 +146,7 @@ struct DevJob {
 
 struct mpgpu_ctx {
     int device = 0;
+    int32_t flags = 0;                 // mpgpu_cfg.flags
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;   // accumulation, overlapped with the fits
     int64_t stagingBytes = 0;
@@ -154,6 +156,22 @@ struct mpgpu_ctx {
     double *hscal = nullptr;     // pinned mirror
     int64_t lastNaccepted = 0;
 };
+
+// Device allocation that keeps its capacity between uploads and loops (no
+// free / alloc when the next request fits).
+template <class T>
+inline cudaError_t dgrow(DevJob &j, T *&p, int64_t n) {
+    const void *key = (const void *)&p;
+    if (n <= 0) n = 1;
+    auto it = j.cap.find(key);
+    if (p && it != j.cap.end() && it->second >= n) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * (size_t)n);
+    if (e != cudaSuccess) { j.cap.erase(key); return e; }
+    j.cap[key] = n;
+    return cudaSuccess;
+}
 
 // ---------------------------------------------------------------- kernels
 struct FitParams {
@@ -179,12 +197,20 @@ struct FitParams {
     int32_t *ndfadd;
     float *chndf;
     int32_t wmax, neqmax, nalcmax, nalgmax, bandmax, bdrmax, ngrpmax;  // shared-memory sizing
+    // large records: B and W of each record of the range in global memory
+    // (stride bwStride doubles per record); the update kernel adds W B^T
+    int32_t bigMode;
+    double *bw;
+    int64_t bwStride;
     int32_t *errFlag;
 };
 
 int fit_smem_per_warp(const FitParams &p);
 int fit_warps_per_cta(const FitParams &p);
 cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s);
+// W B^T of the accepted records r0..r1 added to their block-major staging
+// (large-record mode, one CTA per record, 64 x 64 FP64 tiles)
+cudaError_t launch_update_big(const FitParams &p, cudaStream_t s);
 
 struct AccParams {
     const int32_t *bkI, *bkJ, *bkLd;

@@ -12,6 +12,8 @@
 // the record's sorted variable parameters) for the deterministic owner-
 // computes accumulation (mpgpu_accum.cu).
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "mpgpu_ctx.h"
@@ -461,12 +463,12 @@ __host__ __device__ inline int64_t band_doubles(int nalc, int bandmax, int bdrma
 }
 
 __host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax, int nalgmax,
-                                              int bandmax, int bdrmax, int ngrpmax) {
+                                              int bandmax, int bdrmax, int ngrpmax, bool big = false) {
     int64_t d = 0;
     d += wmax;                          // gl
     d += 7 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2 w0
     d += (int64_t)nalcmax * (nalcmax + 1) / 2 + 4 * (int64_t)nalcmax;  // clmat blvec diag ocol scol
-    d += 2 * (int64_t)nalcmax * nalgmax;  // B W
+    if (!big) d += 2 * (int64_t)nalcmax * nalgmax;  // B W (global memory for large records)
     d += band_doubles(nalcmax, bandmax, bdrmax);
     int64_t i = 0;
     i += wmax;            // in
@@ -495,8 +497,12 @@ __device__ WarpMem carve(char *base, const FitParams &p) {
     m.diag = d; d += p.nalcmax;
     m.ocol = d; d += p.nalcmax;
     m.scol = d; d += p.nalcmax;
-    m.B = d; d += (int64_t)p.nalcmax * p.nalgmax;
-    m.W = d; d += (int64_t)p.nalcmax * p.nalgmax;
+    if (!p.bigMode) {
+        m.B = d; d += (int64_t)p.nalcmax * p.nalgmax;
+        m.W = d; d += (int64_t)p.nalcmax * p.nalgmax;
+    } else {
+        m.B = m.W = nullptr;   // per record in global memory
+    }
     m.bnd = p.bandmax >= 0 ? d : nullptr;
     d += band_doubles(p.nalcmax, p.bandmax, p.bdrmax);
     int32_t *q = (int32_t *)d;
@@ -591,6 +597,11 @@ k_fit(FitParams p, int perWarp) {
         for (int i = ln; i <= nalg; i += 32) m.swS[i] = p.swStart[ri.slotOff + i];
         const int ngrp = ri.ngrp;
         const int64_t *pdst = p.pairDst + ri.pairOff;  // staging offset per group pair
+        double *mB = m.B, *mW = m.W;   // large records: this record's slot in global memory
+        if (p.bigMode) {
+            mB = p.bw + (r - p.r0) * p.bwStride;
+            mW = mB + (int64_t)nalc * nalg;
+        }
         if (p.icalcm == 1 && nalc > 0) {
             for (int i = ln; i < ngrp; i += 32) m.goff[i] = p.grpSlot[ri.grpOff + i];
             if (ln == 0) m.goff[ngrp] = nalg;
@@ -857,7 +868,7 @@ k_fit(FitParams p, int perWarp) {
                 for (int s = ln; s < nalg; s += 32) {
                     double v = 0.0;
                     if (p.icalcm == 1)
-                        for (int k = 0; k < nalc; ++k) m.B[k * nalg + s] = 0.0;
+                        for (int k = 0; k < nalc; ++k) mB[k * nalg + s] = 0.0;
                     for (int q = m.swS[s]; q < m.swS[s + 1]; ++q) {
                         const int ent = m.sw[q];
                         const int e = ent >> 16, wp = ent & 0xffff;
@@ -868,7 +879,7 @@ k_fit(FitParams p, int perWarp) {
                             const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                             for (int jj = 1; jj <= sg - sl - 1; ++jj) {
                                 const int k = m.in[sl + jj] - 1;
-                                m.B[k * nalg + s] = __fma_rn(cb, m.gl[sl + jj], m.B[k * nalg + s]);
+                                mB[k * nalg + s] = __fma_rn(cb, m.gl[sl + jj], mB[k * nalg + s]);
                             }
                         }
                     }
@@ -882,10 +893,10 @@ k_fit(FitParams p, int perWarp) {
                             double cik = 0.0;
                             const int lkl = (k * k - k) / 2;
                             for (int l = 1; l <= k; ++l)
-                                cik = __fma_rn(m.B[(l - 1) * nalg + s], m.clmat[lkl + l - 1], cik);
+                                cik = __fma_rn(mB[(l - 1) * nalg + s], m.clmat[lkl + l - 1], cik);
                             for (int l = k + 1; l <= nalc; ++l)
-                                cik = __fma_rn(m.B[(l - 1) * nalg + s], m.clmat[(l * l - l) / 2 + k - 1], cik);
-                            m.W[s * nalc + k - 1] = cik;
+                                cik = __fma_rn(mB[(l - 1) * nalg + s], m.clmat[(l * l - l) / 2 + k - 1], cik);
+                            mW[s * nalc + k - 1] = cik;
                         }
                     }
                     __syncwarp();
@@ -933,8 +944,10 @@ k_fit(FitParams p, int perWarp) {
                             qa = qa2;
                             qb = qb2;
                         }
-                        const double *wa = m.W + a * nalc;
-                        for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], m.B[k * nalg + b], u);
+                        if (!p.bigMode) {   // large records: W B^T added by k_update_big
+                            const double *wa = mW + a * nalc;
+                            for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], mB[k * nalg + b], u);
+                        }
                         p.stage[__ldg(pdst + bw.pair()) + bw.e] = u;
                         bw.advance(32);
                     }
@@ -963,8 +976,85 @@ k_fit(FitParams p, int perWarp) {
 
 }  // namespace
 
+// W B^T of one accepted large record per CTA, in 64 x 64 tiles of the
+// lower triangle (256 threads, 4 x 4 elements each, K in chunks of 16
+// through shared memory), added to the record's block-major staging, which
+// already holds its G^T W G part.
+namespace {
+constexpr int kUbT = 64, kUbK = 16;
+__global__ void __launch_bounds__(256) k_update_big(FitParams p) {
+    __shared__ double ws[kUbK][kUbT + 1], bs[kUbK][kUbT + 1];
+    __shared__ int32_t goffs[MPG_NGRP_MAX + 2];
+    extern __shared__ int32_t gidx[];   // group of each slot
+    const int64_t r = p.r0 + blockIdx.x;
+    const RecInfo ri = p.rec[r];
+    if (ri.nalc <= 0 || p.status[r] != 0) return;
+    const int nalg = ri.nalg, nalc = ri.nalc, ngrp = ri.ngrp;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int g = tid; g < ngrp; g += blockDim.x) goffs[g] = p.grpSlot[ri.grpOff + g];
+    if (tid == 0) goffs[ngrp] = nalg;
+    __syncthreads();
+    for (int sl = tid; sl < nalg; sl += blockDim.x) {
+        int g = 0;
+        while (g + 1 < ngrp && goffs[g + 1] <= sl) g++;
+        gidx[sl] = g;
+    }
+    __syncthreads();
+    const double *B = p.bw + (r - p.r0) * p.bwStride;   // B[k * nalg + s]
+    const double *W = B + (int64_t)nalc * nalg;          // W[s * nalc + k]
+    const int64_t *pdst = p.pairDst + ri.pairOff;
+    const int T = (nalg + kUbT - 1) / kUbT;
+    for (int ti = 0; ti < T; ++ti)
+        for (int tj = 0; tj <= ti; ++tj) {
+            double acc[4][4] = {};
+            for (int k0 = 0; k0 < nalc; k0 += kUbK) {
+                for (int e = tid; e < kUbT * kUbK; e += blockDim.x) {
+                    const int rr = e / kUbK, kk = e % kUbK;
+                    const int a = ti * kUbT + rr, k = k0 + kk;
+                    ws[kk][rr] = (a < nalg && k < nalc) ? W[(int64_t)a * nalc + k] : 0.0;
+                    const int kb = e / kUbT, cb = e % kUbT;
+                    const int b = tj * kUbT + cb, k2 = k0 + kb;
+                    bs[kb][cb] = (b < nalg && k2 < nalc) ? B[(int64_t)k2 * nalg + b] : 0.0;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int kk = 0; kk < kUbK; ++kk) {
+                    double av[4], bv[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) { av[q] = ws[kk][ty * 4 + q]; bv[q] = bs[kk][tx * 4 + q]; }
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) acc[i][j] = __fma_rn(av[i], bv[j], acc[i][j]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int a = ti * kUbT + ty * 4 + i, b = tj * kUbT + tx * 4 + j;
+                    if (a >= nalg || b > a) continue;
+                    const int qa = gidx[a], qb = gidx[b];
+                    const int ii = a - goffs[qa], jj = b - goffs[qb];
+                    const int64_t e = qa == qb ? (int64_t)ii * (ii + 1) / 2 + jj
+                                               : (int64_t)ii * (goffs[qb + 1] - goffs[qb]) + jj;
+                    p.stage[pdst[qa * (qa + 1) / 2 + qb] + e] += acc[i][j];
+                }
+        }
+}
+}  // namespace
+
+cudaError_t launch_update_big(const FitParams &p, cudaStream_t s) {
+    const int64_t n = p.r1 - p.r0;
+    if (n <= 0) return cudaSuccess;
+    k_update_big<<<(unsigned)n, 256, sizeof(int32_t) * std::max(p.nalgmax, 1), s>>>(p);
+    return cudaGetLastError();
+}
+
 int fit_smem_per_warp(const FitParams &p) {
-    return (int)warp_bytes(p.wmax, p.neqmax, p.nalcmax, p.nalgmax, p.bandmax, p.bdrmax, p.ngrpmax);
+    return (int)warp_bytes(p.wmax, p.neqmax, p.nalcmax, p.nalgmax, p.bandmax, p.bdrmax, p.ngrpmax,
+                           p.bigMode != 0);
 }
 
 // warps per CTA so that one CTA fits the 227 KB of shared memory

@@ -766,22 +766,6 @@ unsigned blocks_for(int64_t n, int t = 256) { return (unsigned)std::max<int64_t>
 
 }  // namespace
 
-// Allocation that keeps its capacity across uploads (no free/alloc when the
-// next job fits).
-template <class T>
-static cudaError_t dgrow(DevJob &j, T *&p, int64_t n) {
-    const void *key = (const void *)&p;
-    if (n <= 0) n = 1;
-    auto it = j.cap.find(key);
-    if (p && it != j.cap.end() && it->second >= n) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * (size_t)n);
-    if (e != cudaSuccess) { j.cap.erase(key); return e; }
-    j.cap[key] = n;
-    return cudaSuccess;
-}
-
 int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const int32_t *inder,
                               const double *glder, const int32_t *recFile, int32_t nfiles,
                               const double *fileWeight) {

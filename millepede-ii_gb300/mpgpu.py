@@ -294,10 +294,10 @@ class HostStructure:
 class Context:
     """One device context with a layout and uploaded records."""
 
-    def __init__(self, device=0, staging_bytes=0):
+    def __init__(self, device=0, staging_bytes=0, flags=0):
         self.L = lib()
         self.h = C.c_void_p()
-        cfg = MpgpuCfg(device=device, flags=0, staging_bytes=staging_bytes)
+        cfg = MpgpuCfg(device=device, flags=flags, staging_bytes=staging_bytes)
         self.check(self.L.mpgpu_create(C.byref(self.h), C.byref(cfg)))
 
     def check(self, rc):

@@ -106,3 +106,32 @@ def test_chunking_consistent(mp):
             ctx.loopbf(np.zeros(H.nTotal))
             out.append(ctx.matrix())
     close(out[0], out[1])
+
+
+@pytest.mark.parametrize("name,matsto,ntracks", [("barrel", 2, 8000), ("telescope", 1, 3000)])
+def test_large_record_path(mp, orc, name, matsto, ntracks):
+    """The large-record path (B and W in global memory, W B^T by the tiled
+    update kernel), forced on records that also fit the per-warp form:
+    same decisions, matrix and vector as the oracle."""
+    d = mp.generate(mp.gen_config(name, ntracks=ntracks, seed=12))
+    H = mp.HostStructure(d, mreqenf=5, sparse=(matsto == 2))
+    O = orc.Structure(d, mreqenf=5, sparse=(matsto == 2))
+    gpar = np.zeros(H.nTotal)
+    o = O.loopbf(gpar, matsto=matsto)
+    with mp.Context(flags=1) as ctx:
+        ctx.set_layout(H, matsto)
+        ctx.upload(H)
+        g = ctx.loopbf(gpar)
+        g["matD"] = ctx.matrix()
+        g["status"] = ctx.status()
+    check(g, o)
+
+
+def test_brokenlines_large(mp, orc):
+    """Broken-line records with up to 40 hits (nloc up to 80, up to 240
+    globals): band local fits and the large-record path, against the
+    oracle."""
+    cfg = mp.gen_config("brokenlines", ntracks=1500, seed=13)
+    d = mp.generate(cfg)
+    g, o, _ = run_pair(mp, orc, d, 2)
+    check(g, o)
