@@ -337,6 +337,12 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         fp.bw = j.bw;
     }
     if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
+    if (fp.bandmax >= 0 && opt->icalcm == 1) {
+        // every warp that can be resident: 64 per SM
+        fp.bscrStride = 32 * (int64_t)fp.nalcmax + (int64_t)fp.nalcmax * (fp.nalcmax + 1) / 2 + 2;
+        MPG_CUDA(c, dgrow(j, j.bscr, (int64_t)nsm * 64 * fp.bscrStride));
+        fp.bscr = j.bscr;
+    }
     AccParams ap{};
     ap.bkI = j.bkI; ap.bkJ = j.bkJ; ap.bkLd = j.bkLd; ap.bkOff = j.bkOff;
     ap.itBlk = j.itBlk; ap.itBase = j.itBase; ap.itCnt = j.itCnt; ap.itSlot = j.itSlot;

@@ -123,6 +123,7 @@ struct DevJob {
     int64_t stageLen = 0;
     UpTmp tmp;
     double *bw = nullptr;              // large-record mode: B and W of a record range
+    double *bscr = nullptr;            // band records: per-warp inverse scratch
     double msUploadCopy = 0.0, msUploadPrepare = 0.0;   // device time of the last upload
     int32_t uploadChunks = 0;
     std::unordered_map<const void *, int64_t> cap;   // capacities of the arrays kept between uploads
@@ -202,6 +203,9 @@ struct FitParams {
     int32_t bigMode;
     double *bw;
     int64_t bwStride;
+    // band records: per-warp scratch of the warp-parallel band inverse
+    double *bscr;
+    int64_t bscrStride;
     int32_t *errFlag;
 };
 

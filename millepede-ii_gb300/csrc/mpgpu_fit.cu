@@ -569,12 +569,98 @@ struct BlockWalk {
     __device__ __forceinline__ int pair() const { return qa * (qa + 1) / 2 + qb; }
 };
 
+// Full inverse of the bordered band matrix factorised by s_sqmibb (called
+// with inv = 0), warp-parallel; the same matrix as s_sqmibb's inv = 2 path
+// (dbcinv plus the border terms, mpnum.f90:3118-3600) up to rounding.  The
+// inverse enters only the Schur complement, not the fit decisions.
+// (1) lane per column c: band inverse column by (L D L^T) x = e_c with the
+//     factored band; (2) lane per packed element: band inverse plus the
+//     border terms, border rows from vbk and aux.  v: 0-based packed n x n;
+//     X: 32 x nalcmax per-lane vectors, Vs: nmb (nmb+1) / 2 (global scratch).
+#define WB(r, c) w[((c) - 1) * mp1 + (r)]
+__device__ void w_band_inverse(int side, double *v, int n, int nbdr, int nbnd, const BandWork &wk, double *X,
+                               int xstride, double *Vs) {
+    const int ln = threadIdx.x & 31;
+    const int mp1 = nbnd + 1, nmb = n - nbdr;
+    const double *w = wk.vbnd, *aux = wk.aux, *vbk = wk.vbk;
+    for (int c0 = 1; c0 <= nmb; c0 += 32) {
+        const int c = c0 + ln;
+        if (c <= nmb) {
+            double *x = X + ln * xstride - 1;   // 1-based
+            for (int i = 1; i <= nmb; ++i) x[i] = i == c ? 1.0 : 0.0;
+            for (int i = c; i <= nmb; ++i) {
+                const int mj = (mp1 - 1 < nmb - i) ? mp1 - 1 : nmb - i;
+                const double xi = x[i];
+                for (int j = 1; j <= mj; ++j) x[j + i] = x[j + i] - WB(j + 1, i) * xi;
+            }
+            for (int i = nmb; i >= 1; --i) {
+                double rxw = x[i] * WB(1, i);
+                const int mj = (mp1 - 1 < nmb - i) ? mp1 - 1 : nmb - i;
+                for (int j = 1; j <= mj; ++j) rxw = rxw - WB(j + 1, i) * x[j + i];
+                x[i] = rxw;
+            }
+            for (int r = c; r <= nmb; ++r) Vs[(r * (r - 1)) / 2 + c] = x[r];   // Vs 1-based packed
+        }
+    }
+    __syncwarp();
+    const int total = n * (n + 1) / 2;
+    const int ab = side == 1 ? nbdr + 1 : 1;   // aux position of band index 0
+    for (int e = ln; e < total; e += 32) {
+        int R = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+        while (R > 0 && R * (R + 1) / 2 > e) R--;
+        while ((R + 1) * (R + 2) / 2 <= e) R++;
+        const int C = e - R * (R + 1) / 2 + 1;
+        R += 1;                                   // 1-based (R, C), C <= R
+        const bool rB = side == 1 ? R <= nbdr : R > nmb;
+        const bool cB = side == 1 ? C <= nbdr : C > nmb;
+        double val;
+        if (rB && cB) {
+            const int ib = side == 1 ? R : R - nmb, jb = side == 1 ? C : C - nmb;
+            val = vbk[(ib * (ib - 1)) / 2 + jb];
+        } else if (rB || cB) {
+            const int ib = rB ? (side == 1 ? R : R - nmb) : (side == 1 ? C : C - nmb);
+            const int i = (rB ? C : R) - (side == 1 ? nbdr + 1 : 1);   // band index, 0-based
+            val = 0.0;
+            for (int jb = 1; jb <= nbdr; ++jb) {
+                const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
+                val = val - vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (jb - 1) * n + i];
+            }
+        } else {
+            const int i = R - (side == 1 ? nbdr + 1 : 1), j = C - (side == 1 ? nbdr + 1 : 1);
+            val = Vs[((i + 1) * i) / 2 + j + 1];
+            for (int ib = 1; ib <= nbdr; ++ib)
+                for (int jb = 1; jb <= nbdr; ++jb) {
+                    const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
+                    val = val + vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (ib - 1) * n + i] * aux[ab + (jb - 1) * n + j];
+                }
+        }
+        v[e] = val;
+    }
+    __syncwarp();
+}
+#undef WB
+
 __device__ __forceinline__ double wsum_serial(const double *a, int n) {
     // sequential sum in index order on lane 0, broadcast to the warp
     double s = 0.0;
     if (lane_id() == 0)
         for (int e = 0; e < n; ++e) s = s + a[e];
     return __shfl_sync(0xffffffffu, s, 0);
+}
+
+// shared-memory work areas of the bordered band solver (1-based views)
+__device__ __forceinline__ BandWork band_work(const WarpMem &m, const RecInfo &ri, int n) {
+    const int nb = ri.mbdr, nbd = ri.mbnd;
+    BandWork wk;
+    double *q = m.bnd;
+    wk.vbnd = q - 1; q += (int64_t)n * (nbd + 1) + 1;
+    wk.vbdr = q - 1; q += (int64_t)n * nb + 1;
+    wk.aux = q - 1; q += (int64_t)n * nb + n + 1;
+    wk.vbk = q - 1; q += (int64_t)nb * nb + 1;
+    wk.vzru = q - 1; q += n + 1;
+    wk.scdiag = q - 1; q += n + 1;
+    wk.scflag = m.used - 1;
+    return wk;
 }
 
 __global__ void __launch_bounds__(32 * MPG_WARPS_FIT)
@@ -729,21 +815,12 @@ k_fit(FitParams p, int perWarp) {
                     double evdmin = 0.0, evdmax = 0.0;
                     int nr = 0;
                     if (ln == 0) {
-                        int inv = 0;
-                        if (iter == 1) inv = 1;
-                        if (p.icalcm == 1) inv = 2;
-                        const int nb = ri.mbdr, nbd = ri.mbnd, n = nalc;
-                        BandWork wk;
-                        double *q = m.bnd;
-                        wk.vbnd = q - 1; q += (int64_t)n * (nbd + 1) + 1;
-                        wk.vbdr = q - 1; q += (int64_t)n * nb + 1;
-                        wk.aux = q - 1; q += (int64_t)n * nb + n + 1;
-                        wk.vbk = q - 1; q += (int64_t)nb * nb + 1;
-                        wk.vzru = q - 1; q += n + 1;
-                        wk.scdiag = q - 1; q += n + 1;
-                        wk.scflag = m.used - 1;
-                        s_sqmibb(ri.mside & 0xff, m.clmat - 1, m.blvec - 1, n, nb, nbd, inv, &nr,
-                                 &evdmin, &evdmax, wk);
+                        // the solution and the factors on one lane (the arithmetic of
+                        // the decisions); the inverse, needed for the update only, is
+                        // formed warp-parallel after the iterations
+                        const BandWork wk = band_work(m, ri, nalc);
+                        s_sqmibb(ri.mside & 0xff, m.clmat - 1, m.blvec - 1, nalc, ri.mbdr, ri.mbnd, 0, &nr,
+                                 &evdmin, &evdmax, const_cast<BandWork &>(wk));
                         if (evdmin > 0.0) cndl10 = log10f((float)(evdmax / evdmin));
                         else cndl10 = 0.0f;
                     }
@@ -886,6 +963,13 @@ k_fit(FitParams p, int perWarp) {
                     p.vstage[ri.slotOff + s] = v;
                 }
                 __syncwarp();
+                if (p.icalcm == 1 && band) {
+                    const BandWork wk = band_work(m, ri, nalc);
+                    const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+                    double *X = p.bscr + wid * p.bscrStride;
+                    w_band_inverse(ri.mside & 0xff, m.clmat, nalc, ri.mbdr, ri.mbnd, wk, X, p.nalcmax,
+                                   X + 32 * (int64_t)p.nalcmax);
+                }
                 if (p.icalcm == 1) {
                     // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432)
                     for (int s = ln; s < nalg; s += 32) {
