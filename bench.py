@@ -312,12 +312,11 @@ def main():
     S = mp.HostStructure(d, mreqenf=25)
     A = mp.constraint_matrix(d, S)
     L = mp.lib()
-    # pin the host record buffers (e2e uploads run from page-locked memory)
-    pinned = []
-    for key in ("recPtr", "inder", "glder"):
-        arr = d[key] if key != "inder" else S.tinder
-        if L.mpgpu_host_register(C.c_void_p(arr.ctypes.data), C.c_int64(arr.nbytes)) == 0:
-            pinned.append(arr)
+    # the host record buffers in page-locked memory from the runtime (e2e
+    # uploads read them); registering the numpy buffers instead gave uploads
+    # that slowed down to pageable speed on some boxes after other GPU work
+    pinned = [mp.PinnedArray(S.recPtr), mp.PinnedArray(S.tinder), mp.PinnedArray(S.glder)]
+    S.recPtr, S.tinder, S.glder = pinned[0].a, pinned[1].a, pinned[2].a
     ctx = mp.Context(device=local, staging_bytes=args.staging_mb << 20)
     ctx.set_layout(S, 2)
     ctx.set_constraints(A)
@@ -412,7 +411,7 @@ def main():
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n)
     for arr in pinned:
-        L.mpgpu_host_unregister(C.c_void_p(arr.ctypes.data))
+        arr.free()
     if rank == 0:
         print(json.dumps(line))
     if pg is not None:

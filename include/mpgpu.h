@@ -207,6 +207,10 @@ int32_t mpgpu_solve(mpgpu_ctx *ctx, int32_t metsol, const double *consResiduals,
  * uploads from it run at full host-device bandwidth. */
 int32_t mpgpu_host_register(void *ptr, int64_t bytes);
 int32_t mpgpu_host_unregister(void *ptr);
+/* Page-locked host memory allocated by the runtime, for record buffers
+ * that are uploaded repeatedly (released with mpgpu_host_free). */
+int32_t mpgpu_host_alloc(void **ptr, int64_t bytes);
+int32_t mpgpu_host_free(void *ptr);
 
 /* Measured FP64 fused-multiply-add throughput of the device (TFLOP/s),
  * used as the roofline denominator of the FP64-bound local-fit kernel. */

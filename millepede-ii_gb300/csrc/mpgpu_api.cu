@@ -643,3 +643,14 @@ extern "C" int32_t mpgpu_host_unregister(void *ptr) {
     if (!ptr) return MPGPU_ERR_ARG;
     return cudaHostUnregister(ptr) == cudaSuccess ? MPGPU_OK : MPGPU_ERR_CUDA;
 }
+
+extern "C" int32_t mpgpu_host_alloc(void **ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return MPGPU_ERR_ARG;
+    *ptr = nullptr;
+    return cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocPortable) == cudaSuccess ? MPGPU_OK : MPGPU_ERR_ALLOC;
+}
+
+extern "C" int32_t mpgpu_host_free(void *ptr) {
+    if (!ptr) return MPGPU_ERR_ARG;
+    return cudaFreeHost(ptr) == cudaSuccess ? MPGPU_OK : MPGPU_ERR_CUDA;
+}

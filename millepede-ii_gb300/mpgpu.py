@@ -113,7 +113,7 @@ EXPORTS = [
     "mpgpu_dense_cholesky", "mpgpu_upload_timing",
     "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
     "mpgpu_read_mille",
-    "mpgpu_host_register", "mpgpu_host_unregister",
+    "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
@@ -525,3 +525,24 @@ def run_job(jd, ctx=None):
     """Whole job through mpgpu_pede_run (private context when ctx is None)."""
     return lib().mpgpu_pede_run(ctx.h if ctx is not None else None, C.byref(jd.steer), C.byref(jd.job),
                                 C.byref(jd.res))
+
+
+class PinnedArray:
+    """numpy array in page-locked memory from mpgpu_host_alloc."""
+
+    def __init__(self, src):
+        src = np.ascontiguousarray(src)
+        self.L = lib()
+        self.p = C.c_void_p()
+        rc = self.L.mpgpu_host_alloc(C.byref(self.p), C.c_int64(max(src.nbytes, 1)))
+        if rc != 0:
+            raise RuntimeError(f"mpgpu_host_alloc: {rc}")
+        buf = (C.c_char * max(src.nbytes, 1)).from_address(self.p.value)
+        self.a = np.frombuffer(buf, dtype=src.dtype, count=src.size).reshape(src.shape)
+        self.a[...] = src
+
+    def free(self):
+        if self.p:
+            self.a = None
+            self.L.mpgpu_host_free(self.p)
+            self.p = C.c_void_p()
