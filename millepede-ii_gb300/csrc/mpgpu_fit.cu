@@ -663,6 +663,7 @@ __device__ __forceinline__ BandWork band_work(const WarpMem &m, const RecInfo &r
     return wk;
 }
 
+template <bool BIG>
 __global__ void __launch_bounds__(32 * MPG_WARPS_FIT)
 k_fit(FitParams p, int perWarp) {
     extern __shared__ __align__(16) char smem[];
@@ -684,7 +685,7 @@ k_fit(FitParams p, int perWarp) {
         const int ngrp = ri.ngrp;
         const int64_t *pdst = p.pairDst + ri.pairOff;  // staging offset per group pair
         double *mB = m.B, *mW = m.W;   // large records: this record's slot in global memory
-        if (p.bigMode) {
+        if (BIG) {
             mB = p.bw + (r - p.r0) * p.bwStride;
             mW = mB + (int64_t)nalc * nalg;
         }
@@ -1028,7 +1029,7 @@ k_fit(FitParams p, int perWarp) {
                             qa = qa2;
                             qb = qb2;
                         }
-                        if (!p.bigMode) {   // large records: W B^T added by k_update_big
+                        if (!BIG) {   // large records: W B^T added by k_update_big
                             const double *wa = mW + a * nalc;
                             for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], mB[k * nalg + b], u);
                         }
@@ -1151,13 +1152,14 @@ int fit_warps_per_cta(const FitParams &p) {
 
 cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s) {
     const int per = fit_smem_per_warp(p);
+    void (*kern)(FitParams, int) = p.bigMode ? k_fit<true> : k_fit<false>;
     const int wpc = fit_warps_per_cta(p);
     if (wpc < 1) return cudaErrorInvalidConfiguration;
     const int bytes = per * wpc;
-    cudaError_t e = cudaFuncSetAttribute(k_fit, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e != cudaSuccess) return e;
     int perSM = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k_fit, 32 * wpc, bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 32 * wpc, bytes);
     if (perSM < 1) perSM = 1;
     if (maxPerSM > 0 && perSM > maxPerSM) perSM = maxPerSM;
     int64_t nrec = p.r1 - p.r0;
@@ -1165,6 +1167,6 @@ cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s
     int64_t need = (nrec + wpc - 1) / wpc;
     if (grid > need) grid = need;
     if (grid < 1) grid = 1;
-    k_fit<<<(unsigned)grid, 32 * wpc, bytes, s>>>(p, per);
+    kern<<<(unsigned)grid, 32 * wpc, bytes, s>>>(p, per);
     return cudaGetLastError();
 }

@@ -34,7 +34,8 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kUpWarps = 4;          // warps per CTA of the record kernels
 constexpr int kEqMax = 512;          // measurements per record
-constexpr int kSwMax = 1024;         // variable global words per record
+constexpr int kSwMax = 512;          // variable global words per record
+constexpr int kWordsMax = 2048;      // records up to this length are decoded from shared memory
 
 // ------------------------------------------------------------ exclusive scan
 constexpr int kScanThreads = 256, kScanItems = 16, kScanTile = kScanThreads * kScanItems;
@@ -219,6 +220,7 @@ struct UpParams {
 };
 
 struct UpWarp {
+    int32_t words[kWordsMax];
     int32_t eq[3 * kEqMax];
     uint64_t key[kSwMax];
     int32_t slotStart[kSwMax + 1];
@@ -267,6 +269,13 @@ __device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks
     if (nw64 < 1 || nw64 > MPG_WORDS_MAX) { R.code = MPGPU_ERR_BADRECORD; return R; }
     const int nw = (int)nw64, end = nw - 1;
     R.nw = nw;
+    // the record's index words in shared memory (one coalesced pass) when
+    // they fit; the decode then reads shared memory only
+    if (nw <= kWordsMax) {
+        for (int i = ln; i < nw; i += 32) W.words[i] = in[i];
+        __syncwarp();
+        in = W.words;
+    }
     // decodeNextMeasurement over the whole record
     int lg = 0, neq = 0;
     for (int guard = 0; guard < MPG_WORDS_MAX + 2; ++guard) {
@@ -423,7 +432,7 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
         if (R.code == 0 && R.nalc > 5) {
             // bordered band structure of the local matrix (pede.f90:3812-3874)
             const int nalc = R.nalc;
-            const int32_t *in = P.inder + (P.recPtr[r] - P.recPtr[0]);
+            const int32_t *in = R.nw <= kWordsMax ? W.words : P.inder + (P.recPtr[r] - P.recPtr[0]);
             for (int i = ln; i < 2 * nalc + 2; i += 32) W.band[i] = 0;
             __syncwarp();
             for (int e = ln; e < R.neq; e += 32) {
