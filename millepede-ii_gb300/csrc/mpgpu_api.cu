@@ -50,6 +50,7 @@ void free_records(DevJob &j) {
     dfree(t.recPtr); dfree(t.recFile); dfree(t.cnt); dfree(t.off); dfree(t.scanTmp); dfree(t.grpRec);
     dfree(t.k0); dfree(t.k1); dfree(t.v0); dfree(t.v1); dfree(t.pairKey); dfree(t.hist); dfree(t.head);
     dfree(t.nel); dfree(t.segStart); dfree(t.segEnd); dfree(t.bcnt); dfree(t.bscan); dfree(t.cntG); dfree(t.scal);
+    dfree(t.ovList);
     j.cap.clear();
     dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);

@@ -46,6 +46,7 @@ struct UpTmp {
     int64_t *nel = nullptr, *segStart = nullptr, *segEnd = nullptr;
     int64_t *bcnt = nullptr, *bscan = nullptr, *cntG = nullptr;
     int64_t *scal = nullptr;                  // error word and maxima
+    int64_t *ovList = nullptr;                // records handed to the large record kernels
 };
 
 // Device arrays of one job.  Every pointer is owned by the context.

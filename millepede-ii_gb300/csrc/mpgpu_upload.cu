@@ -5,7 +5,8 @@
 // The records arrive as the Mille words (inder/glder, labels already
 // translated to total indices).  Everything the data loop needs is derived
 // on the GPU:
-//   1. k_up_scan (one warp per record): decode the measurements, count the
+//   1. k_up_scan (one warp per record; a compact variant for typical
+//      records and a large one for the records it hands over): decode the measurements, count the
 //      locals, the variable global words and the distinct variable
 //      parameters (sorted), form the parameter groups, check the record
 //      (codes as the host checks: 20 malformed, 23 bad index, 35 incomplete
@@ -214,19 +215,40 @@ struct UpParams {
     int64_t *cnt;              // 6 arrays of nrec + 1: eq, slot, sw, grp, pair, stage
     unsigned long long *err;   // min over (record << 8 | code)
     int32_t *maxv;             // nw neq nalc nalg ngrp band bdr nbndr1 nbndr2
+    int64_t *ovList;           // records beyond the compact capacity (filled by k_up_scan<false>)
+    int32_t *ovCount;
     // tables (fill)
     const int64_t *off;        // 6 scanned arrays of nrec + 1
     int32_t *meas, *slots, *slotCnt, *swStart, *sw, *grpId, *grpSlot, *grpRec;
 };
 
-struct UpWarp {
-    int32_t words[kWordsMax];
-    int32_t eq[3 * kEqMax];
-    uint64_t key[kSwMax];
-    int32_t slotStart[kSwMax + 1];
-    int32_t band[2 * MPG_NALC_MAX + 4];
+// Two variants of the record kernels.  The compact one keeps the shared
+// memory of a warp small enough for 32 warps per SM (records of up to 512
+// words, 128 measurements, 256 variable global words: tracks of a few tens
+// of hits); the large one takes records up to the global limits at 8 warps
+// per SM.  The compact kernels hand every record beyond their capacity to
+// the large ones through an overflow list.  Both run the same analysis, so
+// a record's tables and status do not depend on the variant.
+template <bool BIG> struct UpCap;
+template <> struct UpCap<false> {
+    static constexpr int kWords = 512, kEq = 128, kSw = 256, kMinBlocks = 8;
+};
+template <> struct UpCap<true> {
+    static constexpr int kWords = kWordsMax, kEq = kEqMax, kSw = kSwMax, kMinBlocks = 1;
+};
+constexpr int kOverflow = -1;   // analysis result: beyond the compact capacity
+
+template <bool BIG> struct UpWarp {
+    int32_t words[UpCap<BIG>::kWords];
+    int32_t eq[3 * UpCap<BIG>::kEq];
+    uint64_t key[UpCap<BIG>::kSw];     // after the analysis: band table of k_up_scan
+    int32_t slotStart[UpCap<BIG>::kSw + 1];
     int32_t misc[4];
 };
+static_assert(sizeof(uint64_t) * 256 >= sizeof(int32_t) * (2 * MPG_NALC_MAX + 4), "band table in the key array");
+
+// the large kernels reject what exceeds their capacity, the compact ones defer it
+template <bool BIG> __device__ __forceinline__ int cap_code() { return BIG ? MPGPU_ERR_LIMIT : kOverflow; }
 
 __device__ __forceinline__ int warp_max(int v) {
 #pragma unroll
@@ -250,8 +272,147 @@ __device__ int next_zero(const int32_t *in, int from, int end) {
     return -1;
 }
 
+// decodeNextMeasurement (pede.f90:2428-2468) over the whole record: the
+// measurements as (sl, sg, lg) word triples in W.eq.  The zero index words delimit the
+// blocks; without special data blocks they alternate local start, global
+// start, so one ballot pass over the record gives every triple.  A record
+// with a possible special block (two adjacent zero words, the second with a
+// negative value), an odd number of zero words or none takes the sequential
+// decode, which also reports malformed records.
+template <bool BIG>
+__device__ int decode_measurements(const int32_t *in, const double *gl, int end, UpWarp<BIG> &W,
+                                   int &neqOut) {
+    constexpr int CAP = UpCap<BIG>::kEq;
+    const int ln = threadIdx.x & 31;
+    const unsigned lt = (1u << ln) - 1u;
+    int nz = 0, cand = 0;
+    for (int b = 1; b <= end; b += 32) {
+        const int p = b + ln;
+        const bool z = p <= end && in[p] == 0;
+        const unsigned m = __ballot_sync(kFull, z);
+        if (z) {
+            const int idx = nz + __popc(m & lt), e = idx >> 1;
+            if (e < CAP) W.eq[3 * e + (idx & 1)] = p;
+            // a local start closes the previous measurement
+            if ((idx & 1) == 0 && e >= 1 && e <= CAP) W.eq[3 * (e - 1) + 2] = p - 1;
+            if (p >= 2 && in[p - 1] == 0 && gl[p] < 0.0) cand = 1;
+        }
+        nz += __popc(m);
+    }
+    cand = __any_sync(kFull, cand);
+    if (!cand && (nz & 1) == 0 && (nz > 0 || end <= 0)) {
+        const int neq = nz >> 1;
+        if (neq > CAP) return cap_code<BIG>();
+        if (ln == 0 && neq > 0) W.eq[3 * (neq - 1) + 2] = end;
+        __syncwarp();
+        neqOut = neq;
+        return 0;
+    }
+    __syncwarp();
+    int lg = 0, neq = 0;
+    for (int guard = 0; guard < MPG_WORDS_MAX + 2; ++guard) {
+        if (lg >= end) break;
+        const int sl = next_zero(in, lg + 1, end);
+        if (sl < 0) return MPGPU_ERR_BADRECORD;
+        const int sg = next_zero(in, sl + 1, end);
+        if (sg < 0) return MPGPU_ERR_BADRECORD;
+        if (sl + 1 == sg && gl[sg] < 0.0) {  // special data block
+            lg = sg + (int)(-gl[sg] + 0.5);
+            continue;
+        }
+        const int nzp = next_zero(in, sg + 1, end);
+        lg = nzp < 0 ? end : nzp - 1;
+        if (neq >= CAP) return cap_code<BIG>();
+        if (ln == 0) {
+            W.eq[3 * neq] = sl;
+            W.eq[3 * neq + 1] = sg;
+            W.eq[3 * neq + 2] = lg;
+        }
+        neq++;
+    }
+    __syncwarp();
+    neqOut = neq;
+    return 0;
+}
+
+// ascending bitonic sort of 32 * PER keys held in registers, element
+// lane * PER + k in a[k]: strides below PER inside a lane, the others by
+// shuffles between lanes
+template <int PER>
+__device__ __forceinline__ void sort_regs(uint64_t (&a)[PER]) {
+    const int ln = threadIdx.x & 31;
+#pragma unroll
+    for (int kk = 2; kk <= 32 * PER; kk <<= 1) {
+#pragma unroll
+        for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+            if (jj >= PER) {
+                const int lm = jj / PER;
+                const bool lower = (ln & lm) == 0;
+#pragma unroll
+                for (int k = 0; k < PER; ++k) {
+                    const bool up = ((ln * PER + k) & kk) == 0;
+                    const uint64_t b = __shfl_xor_sync(kFull, a[k], lm);
+                    const bool takeMin = lower == up;
+                    const bool bSmaller = b < a[k];
+                    a[k] = (takeMin == bSmaller) ? b : a[k];
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < PER; ++k) {
+                    const int k2 = k ^ jj;
+                    if (k2 > k) {
+                        const bool up = ((ln * PER + k) & kk) == 0;
+                        const uint64_t x = a[k], y = a[k2];
+                        const bool sw = (x > y) == up;
+                        a[k] = sw ? y : x;
+                        a[k2] = sw ? x : y;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <int PER, bool BIG>
+__device__ __forceinline__ void sort_keys_regs(UpWarp<BIG> &W, int nsw) {
+    const int ln = threadIdx.x & 31;
+    uint64_t a[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        const int i = ln * PER + k;
+        a[k] = i < nsw ? W.key[i] : ~0ull;
+    }
+    sort_regs<PER>(a);
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < PER; ++k) W.key[ln * PER + k] = a[k];
+    __syncwarp();
+}
+
+// bitonic sort in shared memory (large records beyond 256 keys)
+template <bool BIG>
+__device__ void sort_keys_smem(UpWarp<BIG> &W, int nsw) {
+    const int ln = threadIdx.x & 31;
+    int P2 = 32;
+    while (P2 < nsw) P2 <<= 1;
+    for (int i = nsw + ln; i < P2; i += 32) W.key[i] = ~0ull;
+    __syncwarp();
+    for (int k = 2; k <= P2; k <<= 1)
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            for (int i = ln; i < P2; i += 32) {
+                const int ixj = i ^ jj;
+                if (ixj > i) {
+                    const uint64_t a = W.key[i], b = W.key[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) { W.key[i] = b; W.key[ixj] = a; }
+                }
+            }
+            __syncwarp();
+        }
+}
+
 struct RecShape {
-    int code;          // 0 or status code
+    int code;          // 0, a status code or kOverflow
     int nw, neq, nalc, nsw, nalg, ngrp;
     bool nonmono, denseLoc, simpleWords;
 };
@@ -259,8 +420,11 @@ struct RecShape {
 // decode + sorted variable words + slots + groups of record r (warp-wide);
 // the SMEM of the warp holds the equations, the sorted keys and the slot
 // starts afterwards
-__device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks) {
+template <bool BIG>
+__device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp<BIG> &W, bool checks) {
+    constexpr int CAPW = UpCap<BIG>::kWords, CAPSW = UpCap<BIG>::kSw;
     const int ln = threadIdx.x & 31;
+    const unsigned lt = (1u << ln) - 1u;
     RecShape R{};
     const int64_t w0 = P.recPtr[r] - P.recPtr[0];
     const int64_t nw64 = P.recPtr[r + 1] - P.recPtr[r];
@@ -271,34 +435,14 @@ __device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks
     R.nw = nw;
     // the record's index words in shared memory (one coalesced pass) when
     // they fit; the decode then reads shared memory only
-    if (nw <= kWordsMax) {
+    if (nw <= CAPW) {
         for (int i = ln; i < nw; i += 32) W.words[i] = in[i];
         __syncwarp();
         in = W.words;
     }
-    // decodeNextMeasurement over the whole record
-    int lg = 0, neq = 0;
-    for (int guard = 0; guard < MPG_WORDS_MAX + 2; ++guard) {
-        if (lg >= end) break;
-        const int sl = next_zero(in, lg + 1, end);
-        if (sl < 0) { R.code = MPGPU_ERR_BADRECORD; return R; }
-        const int sg = next_zero(in, sl + 1, end);
-        if (sg < 0) { R.code = MPGPU_ERR_BADRECORD; return R; }
-        if (sl + 1 == sg && gl[sg] < 0.0) {  // special data block
-            lg = sg + (int)(-gl[sg] + 0.5);
-            continue;
-        }
-        const int nz = next_zero(in, sg + 1, end);
-        lg = nz < 0 ? end : nz - 1;
-        if (neq >= kEqMax) { R.code = MPGPU_ERR_LIMIT; return R; }
-        if (ln == 0) {
-            W.eq[3 * neq] = sl;
-            W.eq[3 * neq + 1] = sg;
-            W.eq[3 * neq + 2] = lg;
-        }
-        neq++;
-    }
-    __syncwarp();
+    int neq = 0;
+    R.code = decode_measurements<BIG>(in, gl, end, W, neq);
+    if (R.code != 0) return R;
     R.neq = neq;
     // locals
     int nalc = 0, nonmono = 0, badl = 0;
@@ -325,44 +469,51 @@ __device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks
             if (in[q] != q - sl) notDense = 1;
     }
     R.denseLoc = !__any_sync(kFull, notDense);
-    // variable global words as sort keys (var, equation, word)
-    if (ln == 0) W.misc[0] = 0;
-    __syncwarp();
-    int badg = 0;
-    for (int e = ln; e < neq; e += 32) {
-        const int sg = W.eq[3 * e + 1], lgq = W.eq[3 * e + 2];
-        for (int q = sg + 1; q <= lgq; ++q) {
-            const int ti = in[q];
-            if (ti < 1 || ti > P.nTotal) { badg = 1; continue; }
-            const int v = P.varOfTot[ti - 1];
-            if (v > 0) {
-                const int k = atomicAdd(&W.misc[0], 1);
-                if (k < kSwMax) W.key[k] = ((uint64_t)v << 40) | ((uint64_t)e << 16) | (uint64_t)q;
+    // variable global words as sort keys (var, equation, word), placed by
+    // ballots (lane = measurement, step = word of the measurement); the
+    // loads of eight words are issued together
+    int nsw = 0, badg = 0;
+    for (int e0 = 0; e0 < neq; e0 += 32) {
+        const int e = e0 + ln;
+        int q0 = 0, len = 0;
+        if (e < neq) {
+            q0 = W.eq[3 * e + 1] + 1;
+            len = W.eq[3 * e + 2] - q0 + 1;
+        }
+        const int lmax = warp_max(len);
+        for (int t0 = 0; t0 < lmax; t0 += 8) {
+            int v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                v[u] = 0;
+                if (t0 + u < len) {
+                    const int ti = in[q0 + t0 + u];
+                    if (ti < 1 || ti > P.nTotal) badg = 1;
+                    else v[u] = P.varOfTot[ti - 1];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const unsigned m = __ballot_sync(kFull, v[u] > 0);
+                if (v[u] > 0) {
+                    const int k = nsw + __popc(m & lt);
+                    if (k < CAPSW)
+                        W.key[k] = ((uint64_t)v[u] << 40) | ((uint64_t)e << 16) | (uint64_t)(q0 + t0 + u);
+                }
+                nsw += __popc(m);
             }
         }
     }
     __syncwarp();
     if (__any_sync(kFull, badg)) { R.code = MPGPU_ERR_BADINDEX; return R; }
-    const int nsw = W.misc[0];
-    if (nsw > kSwMax) { R.code = MPGPU_ERR_LIMIT; return R; }
+    if (nsw > CAPSW) { R.code = cap_code<BIG>(); return R; }
     R.nsw = nsw;
-    // bitonic sort of the keys
-    int P2 = 32;
-    while (P2 < nsw) P2 <<= 1;
-    for (int i = nsw + ln; i < P2; i += 32) W.key[i] = ~0ull;
-    __syncwarp();
-    for (int k = 2; k <= P2; k <<= 1)
-        for (int jj = k >> 1; jj > 0; jj >>= 1) {
-            for (int i = ln; i < P2; i += 32) {
-                const int ixj = i ^ jj;
-                if (ixj > i) {
-                    const uint64_t a = W.key[i], b = W.key[ixj];
-                    const bool up = (i & k) == 0;
-                    if ((a > b) == up) { W.key[i] = b; W.key[ixj] = a; }
-                }
-            }
-            __syncwarp();
-        }
+    // sort of the keys (they are distinct: the word position is part of them)
+    if (nsw <= 32) sort_keys_regs<1>(W, nsw);
+    else if (nsw <= 64) sort_keys_regs<2>(W, nsw);
+    else if (nsw <= 128) sort_keys_regs<4>(W, nsw);
+    else if (nsw <= 256) sort_keys_regs<8>(W, nsw);
+    else if constexpr (BIG) sort_keys_smem<BIG>(W, nsw);
     // distinct variables (slots) and their word-list starts
     int nalg = 0, dup = 0;
     for (int base = 0; base < nsw; base += 32) {
@@ -373,7 +524,7 @@ __device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks
             if (!head && key_eq(W.key[i]) == key_eq(W.key[i - 1])) dup = 1;
         }
         const unsigned m = __ballot_sync(kFull, head);
-        if (head) W.slotStart[nalg + __popc(m & ((1u << ln) - 1))] = i;
+        if (head) W.slotStart[nalg + __popc(m & lt)] = i;
         nalg += __popc(m);
     }
     if (ln == 0) W.slotStart[nalg] = nsw;
@@ -418,13 +569,27 @@ __device__ RecShape analyze(const UpParams &P, int64_t r, UpWarp &W, bool checks
     return R;
 }
 
-__global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
+// record index of work step `it`: all records (compact) or the overflow list (large)
+template <bool BIG>
+__device__ __forceinline__ int64_t up_steps(const UpParams &P) {
+    return BIG ? (int64_t)*P.ovCount : P.nrec;
+}
+
+template <bool BIG>
+__global__ void __launch_bounds__(32 * kUpWarps, UpCap<BIG>::kMinBlocks) k_up_scan(UpParams P) {
     extern __shared__ __align__(16) char upsm[];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    UpWarp &W = reinterpret_cast<UpWarp *>(upsm)[wib];
+    UpWarp<BIG> &W = reinterpret_cast<UpWarp<BIG> *>(upsm)[wib];
     const int64_t nwarps = (int64_t)gridDim.x * kUpWarps;
-    for (int64_t r = (int64_t)blockIdx.x * kUpWarps + wib; r < P.nrec; r += nwarps) {
-        RecShape R = analyze(P, r, W, true);
+    const int64_t nsteps = up_steps<BIG>(P);
+    for (int64_t it = (int64_t)blockIdx.x * kUpWarps + wib; it < nsteps; it += nwarps) {
+        const int64_t r = BIG ? P.ovList[it] : it;
+        RecShape R = analyze<BIG>(P, r, W, true);
+        if (!BIG && R.code == kOverflow) {
+            if (ln == 0) P.ovList[atomicAdd(P.ovCount, 1)] = r;
+            __syncwarp();
+            continue;
+        }
         const int file = P.recFile ? P.recFile[r] : 1;
         if (R.code == 0 && (file < 1 || file > P.nfiles)) R.code = MPGPU_ERR_BADRECORD;
         if (R.code == 0 && R.nalc > MPG_NALC_MAX) R.code = MPGPU_ERR_LIMIT;
@@ -432,8 +597,11 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
         if (R.code == 0 && R.nalc > 5) {
             // bordered band structure of the local matrix (pede.f90:3812-3874)
             const int nalc = R.nalc;
-            const int32_t *in = R.nw <= kWordsMax ? W.words : P.inder + (P.recPtr[r] - P.recPtr[0]);
-            for (int i = ln; i < 2 * nalc + 2; i += 32) W.band[i] = 0;
+            const int32_t *in =
+                R.nw <= UpCap<BIG>::kWords ? W.words : P.inder + (P.recPtr[r] - P.recPtr[0]);
+            int32_t *band = reinterpret_cast<int32_t *>(W.key);
+            __syncwarp();
+            for (int i = ln; i < 2 * nalc + 2; i += 32) band[i] = 0;
             __syncwarp();
             for (int e = ln; e < R.neq; e += 32) {
                 const int sl = W.eq[3 * e], sg = W.eq[3 * e + 1];
@@ -441,8 +609,8 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
                     for (int kq = sl + 1; kq <= jq; ++kq) {
                         const int ij = in[jq], ik = in[kq];
                         const int id = abs(ij - ik) + 1;
-                        atomicMax(&W.band[id], min(ij, ik));
-                        atomicMax(&W.band[nalc + id], min(nalc + 1 - ij, nalc + 1 - ik));
+                        atomicMax(&band[id], min(ij, ik));
+                        atomicMax(&band[nalc + id], min(nalc + 1 - ij, nalc + 1 - ik));
                     }
             }
             __syncwarp();
@@ -451,7 +619,7 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
                 int64_t icmn = (int64_t)nalc * nalc * nalc;
                 for (int k = nalc; k >= 2; --k) {
                     const int kbnd = k - 2;
-                    kbdr = max(kbdr, W.band[k]);
+                    kbdr = max(kbdr, band[k]);
                     const int64_t wd = kbnd + kbdr + 1;
                     const int64_t icost = 6 * (int64_t)(nalc - kbdr) * wd * wd + 2 * (int64_t)kbdr * kbdr * kbdr;
                     if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 1; }
@@ -460,7 +628,7 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
                     kbdr = 0;
                     for (int k = nalc; k >= 2; --k) {
                         const int kbnd = k - 2;
-                        kbdr = max(kbdr, W.band[k + nalc]);
+                        kbdr = max(kbdr, band[k + nalc]);
                         const int64_t wd = kbnd + kbdr + 1;
                         const int64_t icost = 6 * (int64_t)(nalc - kbdr) * wd * wd + 2 * (int64_t)kbdr * kbdr * kbdr;
                         if (icost < icmn) { icmn = icost; kx = k; kbdrx = kbdr; side = 2; }
@@ -511,14 +679,22 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_scan(UpParams P) {
     }
 }
 
-__global__ void __launch_bounds__(32 * kUpWarps) k_up_fill(UpParams P) {
+template <bool BIG>
+__global__ void __launch_bounds__(32 * kUpWarps, UpCap<BIG>::kMinBlocks) k_up_fill(UpParams P) {
     extern __shared__ __align__(16) char upsm[];
     const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    UpWarp &W = reinterpret_cast<UpWarp *>(upsm)[wib];
+    const unsigned lt = (1u << ln) - 1u;
+    UpWarp<BIG> &W = reinterpret_cast<UpWarp<BIG> *>(upsm)[wib];
     const int64_t nwarps = (int64_t)gridDim.x * kUpWarps;
     const int64_t n1 = P.nrec + 1;
-    for (int64_t r = (int64_t)blockIdx.x * kUpWarps + wib; r < P.nrec; r += nwarps) {
-        const RecShape R = analyze(P, r, W, false);
+    const int64_t nsteps = up_steps<BIG>(P);
+    for (int64_t it = (int64_t)blockIdx.x * kUpWarps + wib; it < nsteps; it += nwarps) {
+        const int64_t r = BIG ? P.ovList[it] : it;
+        const RecShape R = analyze<BIG>(P, r, W, false);
+        if (!BIG && R.code == kOverflow) {  // the large kernel fills it
+            __syncwarp();
+            continue;
+        }
         const int64_t oEq = P.off[0 * n1 + r], oSlot = P.off[1 * n1 + r], oSw = P.off[2 * n1 + r];
         const int64_t oGrp = P.off[3 * n1 + r], oPair = P.off[4 * n1 + r];
         if (ln == 0) {
@@ -557,7 +733,7 @@ __global__ void __launch_bounds__(32 * kUpWarps) k_up_fill(UpParams P) {
             }
             const unsigned m = __ballot_sync(kFull, head);
             if (head) {
-                const int gi = g0 + __popc(m & ((1u << ln) - 1));
+                const int gi = g0 + __popc(m & lt);
                 P.grpId[oGrp + gi] = g;
                 P.grpSlot[oGrp + gi] = s;
                 P.grpRec[oGrp + gi] = (int32_t)r;
@@ -814,16 +990,32 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     MPG_CUDA(c, cudaMemsetAsync(dErr, 0xff, 8, s));
     MPG_CUDA(c, cudaMemsetAsync(dMax, 0, 16 * sizeof(int32_t), s));
     MPG_CUDA(c, cudaMemsetAsync(t.cnt, 0, sizeof(int64_t) * 6 * n1, s));
+    // records beyond the compact kernels' capacity: list and count
+    MPG_CUDA(c, dgrow(j, t.ovList, nrec));
+    int32_t *dOvN = (int32_t *)(t.scal + 12);
+    MPG_CUDA(c, cudaMemsetAsync(dOvN, 0, sizeof(int32_t), s));
     UpParams P{};
     P.nrec = nrec; P.recPtr = t.recPtr; P.inder = j.inder; P.glder = j.glder; P.recFile = dRecFile;
     P.nfiles = nfiles; P.varOfTot = j.varOfTot; P.nTotal = j.nTotal; P.p2g = j.p2g; P.aig = j.aig;
     P.nVar = j.nVar; P.nG = j.nG; P.rec = j.rec; P.cnt = t.cnt; P.err = dErr; P.maxv = dMax;
-    const int smem = kUpWarps * (int)sizeof(UpWarp);
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    const unsigned upBlocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nrec + kUpWarps - 1) / kUpWarps,
-                                                                                (int64_t)nsm * 16));
-    if (nrec > 0) k_up_scan<<<upBlocks, 32 * kUpWarps, smem, s>>>(P);
+    P.ovList = t.ovList; P.ovCount = dOvN;
+    // compact kernels: one wave of persistent CTAs at their occupancy;
+    // large kernels: two CTAs per SM over the overflow list
+    const int smemS = kUpWarps * (int)sizeof(UpWarp<false>);
+    const int smemB = kUpWarps * (int)sizeof(UpWarp<true>);
+    MPG_CUDA(c, cudaFuncSetAttribute(k_up_scan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
+    MPG_CUDA(c, cudaFuncSetAttribute(k_up_fill<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
+    MPG_CUDA(c, cudaFuncSetAttribute(k_up_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
+    MPG_CUDA(c, cudaFuncSetAttribute(k_up_fill<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
+    int perSm = 0;
+    MPG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_up_scan<false>, 32 * kUpWarps, smemS));
+    const unsigned upBlocks = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((nrec + kUpWarps - 1) / kUpWarps, (int64_t)nsm * std::max(perSm, 1)));
+    const unsigned upBlocksBig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nrec, (int64_t)nsm * 2));
+    if (nrec > 0) {
+        k_up_scan<false><<<upBlocks, 32 * kUpWarps, smemS, s>>>(P);
+        k_up_scan<true><<<upBlocksBig, 32 * kUpWarps, smemB, s>>>(P);
+    }
     MPG_CUDA(c, cudaGetLastError());
     // offsets: exclusive scans of the six count arrays (the spare last
     // element of each receives the total)
@@ -866,7 +1058,10 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     MPG_CUDA(c, dgrow(j, t.grpRec, ngrpT));
     P.off = t.off; P.meas = j.meas; P.slots = j.slots; P.slotCnt = j.slotCnt; P.swStart = j.swStart;
     P.sw = j.sw; P.grpId = j.grpId; P.grpSlot = j.grpSlot; P.grpRec = t.grpRec;
-    if (nrec > 0) k_up_fill<<<upBlocks, 32 * kUpWarps, smem, s>>>(P);
+    if (nrec > 0) {
+        k_up_fill<false><<<upBlocks, 32 * kUpWarps, smemS, s>>>(P);
+        k_up_fill<true><<<upBlocksBig, 32 * kUpWarps, smemB, s>>>(P);
+    }
     MPG_CUDA(c, cudaGetLastError());
     // ---- blocks of the record pairs
     const int64_t nsort = std::max<int64_t>(std::max(npairs, ngrpT), 1);

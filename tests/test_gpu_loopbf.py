@@ -135,3 +135,39 @@ def test_brokenlines_large(mp, orc):
     d = mp.generate(cfg)
     g, o, _ = run_pair(mp, orc, d, 2)
     check(g, o)
+
+
+def with_special_blocks(d, every_special=3, every_extra=4):
+    """The records of d with (a) a special data block of two words, one of
+    them a zero index word, after the header of every `every_special`-th
+    record, and (b) two more measurements with one local and no global
+    words, the second with a negative measured value, at the end of every
+    `every_extra`-th record.  Both make the device decode take its
+    sequential path (adjacent zero words); (a) is skipped by the decode as
+    pede skips special data (pede.f90:2123-2128)."""
+    rp, ind, gl = d["recPtr"], d["inder"], d["glder"]
+    rp2, ind2, gl2 = [0], [], []
+    for r in range(len(rp) - 1):
+        a, b = int(rp[r]), int(rp[r + 1])
+        wi, wg = list(ind[a:b]), list(gl[a:b])
+        if r % every_special == 0:
+            wi[1:1] = [0, 0, 3, 0]
+            wg[1:1] = [0.0, -2.0, 1.5, 2.5]
+        if r % every_extra == 1:
+            wi += [0, 1, 0, 0, 1, 0]
+            wg += [-0.4, 0.3, 0.2, -0.6, 0.5, 0.2]
+        ind2 += wi
+        gl2 += wg
+        rp2.append(rp2[-1] + len(wi))
+    out = dict(d)
+    out["recPtr"] = np.array(rp2, np.int64)
+    out["inder"] = np.array(ind2, np.int32)
+    out["glder"] = np.array(gl2, np.float64)
+    return out
+
+
+@pytest.mark.parametrize("name,matsto", [("barrel", 2), ("telescope", 1)])
+def test_special_blocks_sequential_decode(mp, orc, name, matsto):
+    d = with_special_blocks(mp.generate(mp.gen_config(name, ntracks=3000, seed=21)))
+    g, o, _ = run_pair(mp, orc, d, matsto)
+    check(g, o)
