@@ -14,6 +14,11 @@
  * One host thread per context; several contexts may run concurrently.
  *
  * The seams replaced (file:line in the Millepede-II sources):
+ *   mpgpu_loop1_device    loop1 label passes, pargrp, prepareRecords(1)
+ *                         translation (mppar.f90:117-321, pede.f90:2311-2404,
+ *                         5958-5971)
+ *   mpgpu_loop2_device    loop2 mpbits structure (pede.f90:6889-6908,
+ *                         mpbits.f90:305-566, 1220-1350)
  *   mpgpu_set_layout      loop2 results: globalAllIndexGroups,
  *                         sparseMatrixOffsets/Columns (pede.f90:6509-6545,
  *                         7174, 7426)
@@ -92,7 +97,10 @@ int32_t mpgpu_set_constraints(mpgpu_ctx *ctx, int32_t ncon, const double *A);
  * translated to total parameter indices (prepareRecords(1)).  Record r
  * occupies words [recPtr[r], recPtr[r+1]); recFile[nrec] holds the 1-based
  * file of each record (NULL: all file 1), fileWeight[nfiles] the file
- * weights (NULL: 1).  Replaces any previously uploaded records. */
+ * weights (NULL: 1).  Replaces any previously uploaded records.  With
+ * inder = glder = NULL the records kept (translated) by mpgpu_loop1_device
+ * are taken over without a copy; recPtr must be the one given there and the
+ * layout must use loop1's label table. */
 int32_t mpgpu_upload_records(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr,
                              const int32_t *inder, const double *glder,
                              const int32_t *recFile, int32_t nfiles,
@@ -271,7 +279,8 @@ typedef struct mpgpu_result {
 } mpgpu_result;
 
 /* loop1 equivalent: label table (sorted), entries per label, parameter
- * groups and variable indices.  Returns nTotal or <0. */
+ * groups and variable indices.  Returns nTotal or <0: -1 more labels than
+ * cap, -20 malformed record, -23 a global word with a label <= 0. */
 int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
                           const double *glder, int32_t nsteer, const int32_t *steerLabels,
                           int32_t npre, const int32_t *preLabel, const double *preSigma,
@@ -288,6 +297,32 @@ int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *in
                           const double *glder, const int32_t *varIndexOfTotal, int32_t nVar,
                           int32_t nG, const int32_t *allIndexGroups, int64_t cap,
                           int64_t *offsets, int32_t *columns, int64_t *ncolw, int64_t *nmat);
+
+/* loop1 on the device: the tables of mpgpu_host_labels (same arguments,
+ * outputs and results) for the label passes of pede's loop1 (label table
+ * mppar.f90:117-252, entries cut pede.f90:5958-5971, pargrp
+ * pede.f90:2311-2404, variable groups pede.f90:6509-6545).  The records are
+ * copied to the device once and kept there, translated to total indices in
+ * place (prepareRecords(1), mppar.f90:282-321; the words of
+ * mpgpu_host_translate), for mpgpu_loop2_device and for the next
+ * mpgpu_upload_records called with inder = glder = NULL.  Records follow the
+ * device limits (at most 65535 words and 512 measurements).  Returns nTotal
+ * or <0: -1 more labels than cap, -20 malformed record, -23 a global word
+ * with a label <= 0, -30 device memory, -43 CUDA, -44 arguments, -45 a
+ * record beyond the device limits. */
+int32_t mpgpu_loop1_device(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                           const double *glder, int32_t nsteer, const int32_t *steerLabels,
+                           int32_t npre, const int32_t *preLabel, const double *preSigma,
+                           int32_t mreqenf, int32_t cap, int32_t *labels, int64_t *counter,
+                           int32_t *varIndex, int32_t *totGroup, int32_t *nVar, int32_t *nVarGroups);
+/* loop2 on the device: sparseMatrixOffsets/Columns of mpgpu_host_mpbits
+ * (pede.f90:6889-6908, mpbits.f90:305-566, 1220-1350) from the records kept
+ * by mpgpu_loop1_device.  Returns 0, -1 when the columns need more than cap
+ * words (offsets, *ncolw and *nmat are set; call again with a larger
+ * array), or a status. */
+int32_t mpgpu_loop2_device(mpgpu_ctx *ctx, const int32_t *varIndexOfTotal, int32_t nVar, int32_t nG,
+                           const int32_t *allIndexGroups, int64_t cap, int64_t *offsets,
+                           int32_t *columns, int64_t *ncolw, int64_t *nmat);
 
 /* Mille binary files (C or Fortran record framing, float or double words;
  * recognised per file) into record arrays, the file part of readFromBinary

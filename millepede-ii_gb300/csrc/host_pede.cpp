@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/mpgpu.h"
+#include "host_struct.h"
 
 namespace {
 
@@ -148,6 +149,8 @@ extern "C" int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const 
         for (int64_t r = nrec * t / nt; r < nrec * (t + 1) / nt; ++r) {
             for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
                 list.clear();
+                for (int64_t w = sg + 1; w <= lg; ++w) if (inder[w] <= 0) bad[t] = 1;
+                if (bad[t]) return;
                 for (int64_t w = sg + 1; w <= lg; ++w) {
                     if (glder[w] == 0.0) continue;
                     list.push_back(lmap.find(inder[w]));
@@ -165,6 +168,8 @@ extern "C" int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const 
             });
         }
     });
+    for (int t = 0; t < nt; ++t)
+        if (bad[t]) return -23;
     std::vector<uint8_t> cut(n + 1, 0), seen(n, 0);
     std::vector<int64_t> cnt(n, 0);
     for (int t = 0; t < nt; ++t)
@@ -173,6 +178,17 @@ extern "C" int32_t mpgpu_host_labels(int64_t nrec, const int64_t *recPtr, const 
             seen[i] |= seenP[t][i];
             cnt[i] += cntP[t][i];
         }
+    return labels_finish(all, cnt, cut, seen, npre, preLabel, preSigma, mreqenf, labels, counter, varIndex,
+                         totGroup, nVar, nVarGroups);
+}
+
+int32_t labels_finish(const std::vector<int32_t> &all, const std::vector<int64_t> &cnt,
+                      const std::vector<uint8_t> &cut, const std::vector<uint8_t> &seen, int32_t npre,
+                      const int32_t *preLabel, const double *preSigma, int32_t mreqenf, int32_t *labels,
+                      int64_t *counter, int32_t *varIndex, int32_t *totGroup, int32_t *nVar,
+                      int32_t *nVarGroups) {
+    const int32_t n = (int32_t)all.size();
+    LabelMap lmap(all);
     std::vector<double> ps(n, 0.0);
     for (int32_t i = 0; i < npre; ++i) {
         int32_t li = lmap.find(preLabel[i]);

@@ -109,6 +109,7 @@ extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
     free_records(c->j);
     free_layout(c->j);
     free_constraints(c->j);
+    free_resident(c->res);
     if (c->scal) cudaFree(c->scal);
     if (c->hscal) cudaFreeHost(c->hscal);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -280,15 +281,58 @@ extern "C" int32_t mpgpu_upload_records(mpgpu_ctx *c, int64_t nrec, const int64_
                                         const int32_t *inder, const double *glder,
                                         const int32_t *recFile, int32_t nfiles,
                                         const double *fileWeight) {
-    if (!c || nrec < 0 || !recPtr || !inder || !glder) return MPGPU_ERR_ARG;
+    if (!c || nrec < 0 || !recPtr || (!inder) != (!glder)) return MPGPU_ERR_ARG;
     DevJob &j = c->j;
     if (j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the records");
     if (nfiles < 1) nfiles = 1;
     MPG_CUDA(c, cudaSetDevice(c->device));
     j.nrec = 0;  // no records until the upload succeeds
+    if (!inder) {
+        // the records kept by mpgpu_loop1_device become the job's records
+        ResidentRecords &R = c->res;
+        if (!R.translated || R.nrec != nrec || R.w0 != recPtr[0] || R.nw != recPtr[nrec] - recPtr[0])
+            return set_err(c, MPGPU_ERR_ARG, "no matching records kept by mpgpu_loop1_device");
+        if (R.nTotal != j.nTotal) return set_err(c, MPGPU_ERR_SIZE, "layout and loop1 label tables differ");
+        dfree(j.inder);
+        dfree(j.glder);
+        j.inder = R.inder;
+        j.glder = R.glder;
+        j.cap[(const void *)&j.inder] = std::max<int64_t>(R.nw, 1);
+        j.cap[(const void *)&j.glder] = std::max<int64_t>(R.nw, 1);
+        R.inder = nullptr;
+        R.glder = nullptr;
+        free_resident(R);
+    }
     const int32_t rc = upload_records_device(c, nrec, recPtr, inder, glder, recFile, nfiles, fileWeight);
     if (rc != MPGPU_OK) j.nrec = 0;
     return rc;
+}
+
+// ------------------------------------------------------------ structure passes
+extern "C" int32_t mpgpu_loop1_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                      const double *glder, int32_t nsteer, const int32_t *steerLabels,
+                                      int32_t npre, const int32_t *preLabel, const double *preSigma,
+                                      int32_t mreqenf, int32_t cap, int32_t *labels, int64_t *counter,
+                                      int32_t *varIndex, int32_t *totGroup, int32_t *nVar,
+                                      int32_t *nVarGroups) {
+    if (!c || nrec < 0 || !recPtr || (nrec > 0 && (!inder || !glder)) || (nsteer > 0 && !steerLabels) ||
+        (npre > 0 && (!preLabel || !preSigma)) || !labels || !counter || !varIndex || !totGroup || !nVar ||
+        !nVarGroups)
+        return -44;
+    if (cudaSetDevice(c->device) != cudaSuccess) return -43;
+    return loop1_device(c, nrec, recPtr, inder, glder, nsteer, steerLabels, npre, preLabel, preSigma, mreqenf,
+                        cap, labels, counter, varIndex, totGroup, nVar, nVarGroups);
+}
+
+extern "C" int32_t mpgpu_loop2_device(mpgpu_ctx *c, const int32_t *varIndexOfTotal, int32_t nVar, int32_t nG,
+                                      const int32_t *allIndexGroups, int64_t cap, int64_t *offsets,
+                                      int32_t *columns, int64_t *ncolw, int64_t *nmat) {
+    if (!c || !varIndexOfTotal || nVar <= 0 || nG <= 0 || !allIndexGroups || !offsets || !ncolw || !nmat ||
+        (cap > 0 && !columns))
+        return MPGPU_ERR_ARG;
+    if (allIndexGroups[nG] != nVar + 1) return set_err(c, MPGPU_ERR_SIZE, "groups do not end at nVar+1");
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    return loop2_device(c, varIndexOfTotal, nVar, nG, allIndexGroups, cap, offsets, columns, ncolw, nmat);
 }
 
 extern "C" int32_t mpgpu_upload_timing(const mpgpu_ctx *c, double *msCopy, double *msPrepare,

@@ -146,6 +146,19 @@ struct DevJob {
     int64_t workLen = 0;
 };
 
+// Records kept on the device by mpgpu_loop1_device: copied once,
+// translated to total indices in place, used by mpgpu_loop2_device and
+// taken over by the next mpgpu_upload_records called with inder = glder =
+// NULL.  Not released by mpgpu_set_layout.
+struct ResidentRecords {
+    int64_t nrec = -1, nw = 0, w0 = 0;   // w0: recPtr[0] of the loop1 call
+    int64_t *recPtr = nullptr;           // [nrec + 1], as passed to loop1
+    int32_t *inder = nullptr;            // [nw]
+    double *glder = nullptr;             // [nw]
+    int32_t nTotal = 0;                  // labels of the loop1 table
+    bool translated = false;
+};
+
 struct mpgpu_ctx {
     int device = 0;
     int32_t flags = 0;                 // mpgpu_cfg.flags
@@ -154,6 +167,7 @@ struct mpgpu_ctx {
     int64_t stagingBytes = 0;
     std::string err;
     DevJob j;
+    ResidentRecords res;
     double *scal = nullptr;      // small device scalar area
     double *hscal = nullptr;     // pinned mirror
     int64_t lastNaccepted = 0;
@@ -290,6 +304,14 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
 
 // error helpers
 int32_t set_err(mpgpu_ctx *c, int32_t code, const std::string &msg);
+void free_resident(ResidentRecords &R);
+int32_t loop1_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const int32_t *inder, const double *glder,
+                     int32_t nsteer, const int32_t *steerLabels, int32_t npre, const int32_t *preLabel,
+                     const double *preSigma, int32_t mreqenf, int32_t cap, int32_t *labels, int64_t *counter,
+                     int32_t *varIndex, int32_t *totGroup, int32_t *nVar, int32_t *nVarGroups);
+int32_t loop2_device(mpgpu_ctx *c, const int32_t *varIndexOfTotal, int32_t nVar, int32_t nG,
+                     const int32_t *allIndexGroups, int64_t cap, int64_t *offsets, int32_t *columns,
+                     int64_t *ncolw, int64_t *nmat);
 int32_t cuda_err(mpgpu_ctx *c, cudaError_t e, const char *where);
 #define MPG_CUDA(c, call)                                      \
     do {                                                       \

@@ -115,7 +115,7 @@ EXPORTS = [
     "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
     "mpgpu_host_labels",
-    "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_pede_run", "mpgpu_write_res",
+    "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_loop1_device", "mpgpu_loop2_device", "mpgpu_pede_run", "mpgpu_write_res",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
 ]
 
@@ -248,20 +248,7 @@ class HostStructure:
                                 C.byref(nVar), C.byref(nG))
         if n < 0:
             raise RuntimeError(f"mpgpu_host_labels failed ({n})")
-        self.nTotal = n
-        self.labels, self.counter = labels[:n].copy(), counter[:n].copy()
-        self.varIndex, self.totGroup = varIndex[:n].copy(), totGroup[:n].copy()
-        self.nVar, self.nG = nVar.value, nG.value
-        aig = []
-        prev = -1
-        for i in range(n):
-            if self.varIndex[i] <= 0:
-                continue
-            if self.totGroup[i] != prev:
-                aig.append(self.varIndex[i])
-                prev = self.totGroup[i]
-        aig.append(self.nVar + 1)
-        self.aig = np.array(aig, np.int32)
+        self._tables(n, labels, counter, varIndex, totGroup, nVar.value, nG.value)
         self.tinder = np.zeros_like(inder)
         rc = L.mpgpu_host_translate(C.c_int64(nrec), ptr(self.recPtr, i64p), ptr(inder, i32p),
                                     ptr(self.glder, f64p), C.c_int32(n), ptr(self.labels, i32p),
@@ -291,6 +278,72 @@ class HostStructure:
         self.nmatPacked = self.nVar * (self.nVar + 1) // 2
 
 
+    def _tables(self, n, labels, counter, varIndex, totGroup, nVar, nG):
+        self.nTotal = n
+        self.labels, self.counter = labels[:n].copy(), counter[:n].copy()
+        self.varIndex, self.totGroup = varIndex[:n].copy(), totGroup[:n].copy()
+        self.nVar, self.nG = nVar, nG
+        var = self.varIndex > 0
+        tg = self.totGroup[var]
+        heads = np.ones(len(tg), bool)
+        heads[1:] = tg[1:] != tg[:-1]
+        self.aig = np.append(self.varIndex[var][heads], self.nVar + 1).astype(np.int32)
+
+
+class DeviceStructure(HostStructure):
+    """The tables of HostStructure computed on the device
+    (mpgpu_loop1_device, mpgpu_loop2_device).  The translated records stay
+    on the context's device; ctx.upload(S) takes them over without a copy
+    (once)."""
+
+    def __init__(self, ctx, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True):
+        L = lib()
+        self.resident = True
+        self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
+        inder = np.ascontiguousarray(data["inder"], np.int32)
+        self.glder = np.ascontiguousarray(data["glder"], np.float64)
+        nrec = len(self.recPtr) - 1
+        cap = len(inder) + len(steerLabels) + 16
+        labels = np.zeros(cap, np.int32)
+        counter = np.zeros(cap, np.int64)
+        varIndex = np.zeros(cap, np.int32)
+        totGroup = np.zeros(cap, np.int32)
+        nVar, nG = C.c_int32(), C.c_int32()
+        sl = np.ascontiguousarray(steerLabels, np.int32)
+        pl = np.ascontiguousarray(preLabel, np.int32)
+        ps = np.ascontiguousarray(preSigma, np.float64)
+        n = L.mpgpu_loop1_device(ctx.h, C.c_int64(nrec), ptr(self.recPtr, i64p), ptr(inder, i32p),
+                                 ptr(self.glder, f64p), C.c_int32(len(sl)), ptr(sl, i32p),
+                                 C.c_int32(len(pl)), ptr(pl, i32p), ptr(ps, f64p),
+                                 C.c_int32(mreqenf), C.c_int32(cap), ptr(labels, i32p),
+                                 ptr(counter, i64p), ptr(varIndex, i32p), ptr(totGroup, i32p),
+                                 C.byref(nVar), C.byref(nG))
+        if n < 0:
+            raise RuntimeError(f"mpgpu_loop1_device failed ({n}): {ctx.last_error()}")
+        self._tables(n, labels, counter, varIndex, totGroup, nVar.value, nG.value)
+        self.tinder = None
+        self.offsets = np.zeros(2 * (self.nG + 1), np.int64)
+        self.columns = np.zeros(1, np.int32)
+        self.ncolw = 0
+        self.nmatSparse = 0
+        if sparse:
+            ncolw, nmat = C.c_int64(), C.c_int64()
+            cols = np.zeros(1 << 20, np.int32)
+            for _ in range(2):
+                rc = L.mpgpu_loop2_device(ctx.h, ptr(self.varIndex, i32p), C.c_int32(self.nVar),
+                                          C.c_int32(self.nG), ptr(self.aig, i32p),
+                                          C.c_int64(len(cols)), ptr(self.offsets, i64p),
+                                          ptr(cols, i32p), C.byref(ncolw), C.byref(nmat))
+                if rc != -1:
+                    break
+                cols = np.zeros(max(ncolw.value, 1), np.int32)
+            if rc != 0:
+                raise RuntimeError(f"mpgpu_loop2_device failed ({rc}): {ctx.last_error()}")
+            self.columns = cols[:max(ncolw.value, 1)].copy()
+            self.ncolw, self.nmatSparse = ncolw.value, nmat.value
+        self.nmatPacked = self.nVar * (self.nVar + 1) // 2
+
+
 class Context:
     """One device context with a layout and uploaded records."""
 
@@ -299,6 +352,10 @@ class Context:
         self.h = C.c_void_p()
         cfg = MpgpuCfg(device=device, flags=flags, staging_bytes=staging_bytes)
         self.check(self.L.mpgpu_create(C.byref(self.h), C.byref(cfg)))
+
+    def last_error(self):
+        msg = self.L.mpgpu_last_error(self.h) if self.h else b""
+        return msg.decode() if msg else ""
 
     def check(self, rc):
         if rc != 0:
@@ -336,9 +393,10 @@ class Context:
         rf = None if recFile is None else np.ascontiguousarray(recFile, np.int32)
         fw = None if fileWeight is None else np.ascontiguousarray(fileWeight, np.float64)
         self.nfiles = 1 if fw is None else len(fw)
+        resident = getattr(S, "resident", False)
         self.check(self.L.mpgpu_upload_records(
-            self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(S.tinder, i32p),
-            ptr(S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
+            self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(None if resident else S.tinder, i32p),
+            ptr(None if resident else S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
 
     def upload_timing(self):
         """(ms copy, ms prepare, chunks) of the last upload."""

@@ -57,3 +57,29 @@ def test_groups_random_equations(mp, orc):
         np.testing.assert_array_equal(H.varIndex, O.varIndex)
         np.testing.assert_array_equal(H.offsets, O.offsets)
         np.testing.assert_array_equal(H.columns[:H.ncolw], O.columns[:O.ncolw])
+
+
+def test_labels_status_codes(mp):
+    """mpgpu_host_labels: -20 for a measurement without its second marker,
+    -23 for a label <= 0 among the global words, -1 beyond the capacity."""
+    d = mp.generate(mp.gen_config("telescope", ntracks=50, seed=8))
+    zeros = [q for q in range(int(d["recPtr"][3]) + 1, int(d["recPtr"][4])) if d["inder"][q] == 0]
+    bad = dict(d, inder=d["inder"].copy())
+    bad["inder"][zeros[-1]] = 3
+    neg = dict(d, inder=d["inder"].copy())
+    neg["inder"][zeros[-1] + 1] = -4
+    for data, code in ((bad, "-20"), (neg, "-23")):
+        with pytest.raises(RuntimeError, match=f"failed \\({code}\\)"):
+            mp.HostStructure(data, mreqenf=1, sparse=False)
+    import ctypes as C
+    L = mp.lib()
+    i32p, i64p, f64p = C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_double)
+    a = [np.zeros(4, np.int32) for _ in range(3)]
+    cnt = np.zeros(4, np.int64)
+    nv, ng = C.c_int32(), C.c_int32()
+    rc = L.mpgpu_host_labels(C.c_int64(len(d["recPtr"]) - 1), d["recPtr"].ctypes.data_as(i64p),
+                             d["inder"].ctypes.data_as(i32p), d["glder"].ctypes.data_as(f64p),
+                             C.c_int32(0), None, C.c_int32(0), None, None, C.c_int32(1), C.c_int32(4),
+                             a[0].ctypes.data_as(i32p), cnt.ctypes.data_as(i64p), a[1].ctypes.data_as(i32p),
+                             a[2].ctypes.data_as(i32p), C.byref(nv), C.byref(ng))
+    assert rc == -1
