@@ -261,6 +261,30 @@ def cpu_reference(d, nsample, nthreads, steps=1):
     return nsample / statistics.median(times), times
 
 
+def structure_measure(mp, S, pinned, device, host_s, ncores):
+    """loop1 + loop2 (label table, translation, entries, groups, mpbits) on
+    the host (mpgpu_host_labels/translate/mpbits, all host threads) and on
+    the device (mpgpu_loop1_device/loop2_device, the copy of the records from
+    page-locked buffers included); the tables must be identical."""
+    data = {"recPtr": pinned[0].a, "glder": pinned[2].a}
+    # the raw (untranslated) words in the page-locked buffer for the device passes
+    raw = mp.PinnedArray(np.asarray(S.rawInder))
+    data["inder"] = raw.a
+    times, same = [], True
+    with mp.Context(device=device) as ctx:
+        for _ in range(3):
+            t0 = time.perf_counter()
+            D = mp.DeviceStructure(ctx, data, mreqenf=25)
+            times.append(time.perf_counter() - t0)
+    for k in ("labels", "counter", "varIndex", "totGroup", "aig", "offsets"):
+        same &= bool(np.array_equal(getattr(S, k), getattr(D, k)))
+    same &= bool(np.array_equal(S.columns[:S.ncolw], D.columns[:D.ncolw]))
+    raw.free()
+    return {"records": len(S.recPtr) - 1, "host_s": host_s, "host_threads": ncores,
+            "device_s": times, "device_s_median": statistics.median(times),
+            "speedup": host_s / statistics.median(times), "tables_identical": same}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -309,7 +333,9 @@ def main():
         print(json.dumps(line))
         return
 
+    t0 = time.perf_counter()
     S = mp.HostStructure(d, mreqenf=25)
+    host_struct_s = time.perf_counter() - t0
     A = mp.constraint_matrix(d, S)
     L = mp.lib()
     # the host record buffers in page-locked memory from the runtime (e2e
@@ -405,6 +431,8 @@ def main():
                                     "kind": "port",
                                     "sample": f"first {nsample} records, one sparse data loop"}
     ctx.close()
+    if not args.profile:
+        line["structure"] = structure_measure(mp, S, pinned, local, host_struct_s, ncores)
     if args.serve_jobs > 0 and rank == 0:
         line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
     if args.dense_n > 0 and rank == 0:

@@ -253,6 +253,9 @@ typedef struct mpgpu_steer {
     double mrestl;
     int32_t itnlim;
     int32_t nthreads;   /* host threads for the structure passes */
+    int32_t structDevice; /* 1: structure passes on the device (mpgpu_loop1_device,
+                             mpgpu_loop2_device) when mpgpu_pede_run is called
+                             directly; 0: on the host */
 } mpgpu_steer;
 
 typedef struct mpgpu_job {

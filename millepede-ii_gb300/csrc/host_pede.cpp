@@ -371,11 +371,25 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     std::vector<int64_t> counter(cap);
     std::vector<int32_t> totGroup(cap);
     int32_t nVar = 0, nG = 0;
-    int32_t ntot = mpgpu_host_labels(job->nrec, job->recPtr, job->inder, job->glder, (int32_t)steer.size(),
-                                     steer.data(), job->npar, job->parLabel, job->parSigma, st->mreqenf,
-                                     cap, res->labels, counter.data(), res->varIndex, totGroup.data(),
-                                     &nVar, &nG);
-    if (ntot < 0) { res->exitCode = 20; if (!ctxIn) mpgpu_destroy(ctx); return 20; }
+    // structure passes on the device: the records are copied once and stay
+    // there translated (not under an admission hook, which must see the
+    // footprint before any device allocation of the job)
+    const bool onDevice = st->structDevice != 0 && !admit;
+    int32_t ntot = onDevice
+                       ? mpgpu_loop1_device(ctx, job->nrec, job->recPtr, job->inder, job->glder,
+                                            (int32_t)steer.size(), steer.data(), job->npar, job->parLabel,
+                                            job->parSigma, st->mreqenf, cap, res->labels, counter.data(),
+                                            res->varIndex, totGroup.data(), &nVar, &nG)
+                       : mpgpu_host_labels(job->nrec, job->recPtr, job->inder, job->glder, (int32_t)steer.size(),
+                                           steer.data(), job->npar, job->parLabel, job->parSigma, st->mreqenf,
+                                           cap, res->labels, counter.data(), res->varIndex, totGroup.data(),
+                                           &nVar, &nG);
+    if (ntot < 0) {
+        const int32_t code = ntot == -23 ? MPGPU_ERR_BADINDEX : ntot <= -30 ? -ntot : 20;
+        res->exitCode = code;
+        if (!ctxIn) mpgpu_destroy(ctx);
+        return code;
+    }
     res->nTotal = ntot;
     res->nVar = nVar;
     res->nVarGroups = nG;
@@ -390,8 +404,11 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         aig[nG] = nVar + 1;
     }
     const int64_t nw = job->recPtr[job->nrec];
-    std::vector<int32_t> tinder(nw);
-    mpgpu_host_translate(job->nrec, job->recPtr, job->inder, job->glder, ntot, res->labels, tinder.data());
+    std::vector<int32_t> tinder;
+    if (!onDevice) {
+        tinder.resize(nw);
+        mpgpu_host_translate(job->nrec, job->recPtr, job->inder, job->glder, ntot, res->labels, tinder.data());
+    }
     std::vector<int64_t> offsets;
     std::vector<int32_t> columns;
     int64_t ncolw = 0, nmat = 0;
@@ -400,10 +417,18 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         int64_t capc = 1 << 20;
         for (;;) {
             columns.assign(capc, 0);
-            if (mpgpu_host_mpbits(job->nrec, job->recPtr, tinder.data(), job->glder, res->varIndex, nVar, nG,
-                                  aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat) == 0)
-                break;
-            capc *= 4;
+            const int32_t r2 =
+                onDevice ? mpgpu_loop2_device(ctx, res->varIndex, nVar, nG, aig.data(), capc, offsets.data(),
+                                              columns.data(), &ncolw, &nmat)
+                         : mpgpu_host_mpbits(job->nrec, job->recPtr, tinder.data(), job->glder, res->varIndex, nVar,
+                                             nG, aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat);
+            if (r2 == 0) break;
+            if (r2 != -1) {
+                res->exitCode = r2;
+                if (!ctxIn) mpgpu_destroy(ctx);
+                return r2;
+            }
+            capc = onDevice ? std::max<int64_t>(ncolw, 1) : capc * 4;
         }
     }
     if (admit) {
@@ -441,8 +466,9 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             }
         rc = mpgpu_set_constraints(ctx, ncon, A.data());
     }
-    if (!rc) rc = mpgpu_upload_records(ctx, job->nrec, job->recPtr, tinder.data(), job->glder, job->recFile,
-                                       job->nfiles, job->fileWeight);
+    if (!rc)
+        rc = mpgpu_upload_records(ctx, job->nrec, job->recPtr, onDevice ? nullptr : tinder.data(),
+                                  onDevice ? nullptr : job->glder, job->recFile, job->nfiles, job->fileWeight);
     const int32_t nfit = nVar - ncon;
     res->nFit = nfit;
     std::vector<double> gpar(ntot, 0.0), psig(ntot, 0.0);

@@ -49,7 +49,7 @@ class Steer(C.Structure):
                 ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float),
                 ("lfitbb", C.c_int32), ("mreqenf", C.c_int32), ("mreqena", C.c_int32),
                 ("mreqpe", C.c_int32), ("mrestl", C.c_double), ("itnlim", C.c_int32),
-                ("nthreads", C.c_int32)]
+                ("nthreads", C.c_int32), ("structDevice", C.c_int32)]
 
 
 class Job(C.Structure):
@@ -249,6 +249,7 @@ class HostStructure:
         if n < 0:
             raise RuntimeError(f"mpgpu_host_labels failed ({n})")
         self._tables(n, labels, counter, varIndex, totGroup, nVar.value, nG.value)
+        self.rawInder = inder
         self.tinder = np.zeros_like(inder)
         rc = L.mpgpu_host_translate(C.c_int64(nrec), ptr(self.recPtr, i64p), ptr(inder, i32p),
                                     ptr(self.glder, f64p), C.c_int32(n), ptr(self.labels, i32p),
@@ -498,7 +499,7 @@ class JobData:
     def __init__(self, data, constraints=None, **steer):
         st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
                   dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
-                  mrestl=1e-10, itnlim=2000, nthreads=0)
+                  mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0)
         st.update(steer)
         self.steer = Steer(**st)
         self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)

@@ -9,11 +9,12 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def gpu_job(mp, orc, d, steer, **jobkw):
+def gpu_job(mp, orc, d, steer, struct_device=0, **jobkw):
     job, keep = orc.make_job(d, **jobkw)
     cap = len(d["inder"]) + 16
     res, kr = orc.make_result(cap, cls=mp.Result)
-    st = mp.Steer(**{f: getattr(steer, f) for f, _ in mp.Steer._fields_})
+    st = mp.Steer(**{f: getattr(steer, f) for f, _ in mp.Steer._fields_ if f != "structDevice"})
+    st.structDevice = struct_device
     jb = mp.Job(**{f: getattr(job, f) for f, _ in mp.Job._fields_})
     rc = mp.lib().mpgpu_pede_run(None, C.byref(st), C.byref(jb), C.byref(res))
     n = res.nTotal
@@ -62,3 +63,18 @@ def test_barrel_sparse_minres(mp, orc):
     assert g["nrej"] == o["nrej"]
     scale = np.max(np.abs(o["parameter"]))
     assert np.max(np.abs(g["parameter"] - o["parameter"])) <= 1e-8 * scale
+
+
+@pytest.mark.parametrize("kind,metsol,matsto", [("barrel", 4, 2), ("telescope", 1, 1)])
+def test_structure_on_device_same_job(mp, orc, kind, metsol, matsto):
+    """The job with its structure passes on the device (steer structDevice)
+    gives the results of the job with host passes, bit for bit."""
+    d = mp.generate(mp.gen_config(kind, ntracks=20000 if kind == "barrel" else 5000, seed=5))
+    st = orc.make_steer(metsol=metsol, matsto=matsto, mitera=2, lhuber=2, mrestl=1e-12, itnlim=3000,
+                        mreqenf=5)
+    h = gpu_job(mp, orc, d, st, struct_device=0)
+    g = gpu_job(mp, orc, d, st, struct_device=1)
+    assert h["rc"] == 0 and g["rc"] == 0
+    for k in ("labels", "varIndex", "counts", "parameter", "error"):
+        np.testing.assert_array_equal(g[k], h[k], err_msg=k)
+    assert g["nrej"] == h["nrej"] and g["ndf"] == h["ndf"] and g["fvalue"] == h["fvalue"]
