@@ -261,6 +261,44 @@ def cpu_reference(d, nsample, nthreads, steps=1):
     return nsample / statistics.median(times), times
 
 
+def brokenlines_measure(mp, device, nrec, ncores, steps=2):
+    """The uneven-record workload (broken-line tracks on the barrel, 4-40
+    hits, nloc 8-84, nalg 24-240; sparse storage): device data loops with
+    the records in fit size classes (tuned warps per CTA), with one launch
+    sized for the largest record, and with one record per CTA; the CPU
+    oracle on a sample."""
+    d = mp.generate(mp.gen_config("brokenlines", ntracks=nrec, seed=3))
+    H = mp.HostStructure(d, mreqenf=25)
+    gpar = np.zeros(H.nTotal)
+    out = {"records": nrec, "hits": [4, 40], "nloc": [8, 84]}
+    forms = (("size_classes", 0), ("one_launch_largest_record", mp.FLAG_NO_BUCKETS),
+             ("one_record_per_block", mp.FLAG_ONE_RECORD_PER_BLOCK))
+    for name, flags in forms:
+        with mp.Context(device=device, flags=flags) as ctx:
+            ctx.set_layout(H, 2)
+            ctx.upload(H)
+            ctx.loopbf(gpar)
+            ms, fit = [], []
+            for _ in range(steps):
+                r = ctx.loopbf(gpar)
+                ms.append(r["msLoop"])
+                fit.append(r["msFit"])
+            cnt, wpc, tms = ctx.fit_buckets()
+        e = {"records_per_s": nrec / (statistics.median(ms) * 1e-3), "ms_loop": ms, "ms_fit": fit}
+        if flags == 0:
+            e["class_records"] = cnt.tolist()
+            e["class_warps_per_cta"] = wpc.tolist()
+            e["class_tune_ms_1_2_4_8_warps"] = [[round(x, 3) for x in row] for row in tms.tolist()]
+        out[name] = e
+    base = out["one_record_per_block"]["records_per_s"]
+    out["speedup_size_classes_vs_one_record_per_block"] = out["size_classes"]["records_per_s"] / base
+    nsample = min(5000, nrec)
+    val, _ = cpu_reference(d, nsample, ncores, steps=1)
+    out["cpu_baseline"] = {"value": val, "unit": "records/s", "cores": ncores, "kind": "port",
+                           "sample": f"first {nsample} records, one sparse data loop"}
+    return out
+
+
 def structure_measure(mp, S, pinned, device, host_s, ncores):
     """loop1 + loop2 (label table, translation, entries, groups, mpbits) on
     the host (mpgpu_host_labels/translate/mpbits, all host threads) and on
@@ -298,6 +336,8 @@ def main():
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--brokenlines", type=int, default=200_000,
+                    help="records of the uneven-record (broken-line) measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     mp = _load_pkg()
@@ -433,6 +473,8 @@ def main():
     ctx.close()
     if not args.profile:
         line["structure"] = structure_measure(mp, S, pinned, local, host_struct_s, ncores)
+    if args.brokenlines > 0 and rank == 0 and not args.profile:
+        line["brokenlines"] = brokenlines_measure(mp, local, args.brokenlines, ncores)
     if args.serve_jobs > 0 and rank == 0:
         line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
     if args.dense_n > 0 and rank == 0:

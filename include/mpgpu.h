@@ -65,6 +65,14 @@ typedef struct mpgpu_ctx mpgpu_ctx;
  * record in global memory, W B^T by a tiled kernel), which is otherwise
  * chosen only when the records are too large for the per-warp form */
 #define MPGPU_FLAG_LARGE_RECORDS 1
+/* one fit launch per chunk with the shared memory sized for the job's
+ * largest record (no size classes); for comparison */
+#define MPGPU_FLAG_NO_BUCKETS 2
+/* one record per CTA of one warp (no persistent loop), no size classes: the
+ * plain launch form, for comparison */
+#define MPGPU_FLAG_ONE_RECORD_PER_BLOCK 4
+/* no timing of warps-per-CTA candidates on the first data loop */
+#define MPGPU_FLAG_NO_AUTOTUNE 8
 
 typedef struct mpgpu_cfg {
     int32_t device;             /* CUDA device ordinal */
@@ -105,6 +113,15 @@ int32_t mpgpu_upload_records(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr
                              const int32_t *inder, const double *glder,
                              const int32_t *recFile, int32_t nfiles,
                              const double *fileWeight);
+
+/* Fit size classes of the uploaded records (the shared memory each fit
+ * needs: class k < 7 up to 4 KB << k, class 7 beyond one CTA): records per
+ * class, warps per CTA chosen by the tuner on the first data loop (0: not
+ * yet tuned, -1: no candidate fitted) and the sample times (ms) of 1, 2, 4
+ * and 8 warps per CTA; arrays of MPGPU_FIT_BUCKETS (and 4x that for
+ * tuneMs).  No counterpart in the reference. */
+#define MPGPU_FIT_BUCKETS 8
+int32_t mpgpu_fit_buckets(const mpgpu_ctx *ctx, int64_t *count, int32_t *wpc, double *tuneMs);
 
 /* Device time of the last mpgpu_upload_records: the host-to-device copy of
  * the records and the record preparation on the device, and the number of

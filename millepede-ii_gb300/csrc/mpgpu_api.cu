@@ -50,7 +50,7 @@ void free_records(DevJob &j) {
     dfree(t.recPtr); dfree(t.recFile); dfree(t.cnt); dfree(t.off); dfree(t.scanTmp); dfree(t.grpRec);
     dfree(t.k0); dfree(t.k1); dfree(t.v0); dfree(t.v1); dfree(t.pairKey); dfree(t.hist); dfree(t.head);
     dfree(t.nel); dfree(t.segStart); dfree(t.segEnd); dfree(t.bcnt); dfree(t.bscan); dfree(t.cntG); dfree(t.scal);
-    dfree(t.ovList);
+    dfree(t.ovList); dfree(t.chunkB); dfree(t.keyEnd); dfree(t.bmax); dfree(j.recList);
     j.cap.clear();
     dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
@@ -335,6 +335,24 @@ extern "C" int32_t mpgpu_loop2_device(mpgpu_ctx *c, const int32_t *varIndexOfTot
     return loop2_device(c, varIndexOfTotal, nVar, nG, allIndexGroups, cap, offsets, columns, ncolw, nmat);
 }
 
+extern "C" int32_t mpgpu_fit_buckets(const mpgpu_ctx *c, int64_t *count, int32_t *wpc, double *tuneMs) {
+    static_assert(MPGPU_FIT_BUCKETS == MPG_FIT_BUCKETS, "bucket count of the ABI");
+    if (!c) return MPGPU_ERR_ARG;
+    const DevJob &j = c->j;
+    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
+    for (int b = 0; b < MPG_FIT_BUCKETS; ++b) {
+        int64_t n = 0;
+        if (!j.bucketOff.empty())
+            for (int64_t ch = 0; ch < nchunk; ++ch)
+                n += j.bucketOff[ch * MPG_FIT_BUCKETS + b + 1] - j.bucketOff[ch * MPG_FIT_BUCKETS + b];
+        if (count) count[b] = n;
+        if (wpc) wpc[b] = j.bucketWpc.empty() ? 0 : j.bucketWpc[b];
+        if (tuneMs)
+            for (int k = 0; k < 4; ++k) tuneMs[4 * b + k] = j.bucketTuneMs.empty() ? 0.0 : j.bucketTuneMs[4 * b + k];
+    }
+    return MPGPU_OK;
+}
+
 extern "C" int32_t mpgpu_upload_timing(const mpgpu_ctx *c, double *msCopy, double *msPrepare,
                                        int32_t *nchunk) {
     if (!c) return MPGPU_ERR_ARG;
@@ -370,23 +388,101 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.bandmax = opt->lfitbb > 0 ? j.maxBand : -1; fp.bdrmax = j.maxBdr;
     fp.ngrpmax = std::max(j.maxNgrp, 1);
     fp.errFlag = errFlag;
-    // records too large for B and W in each warp's shared memory (fewer than
-    // four warps per CTA) take the large-record path
-    fp.bigMode = (c->flags & MPGPU_FLAG_LARGE_RECORDS) || fit_warps_per_cta(fp) < 4 ? 1 : 0;
-    int64_t sub = 0;
-    if (fp.bigMode) {
-        fp.bwStride = 2 * (int64_t)fp.nalgmax * fp.nalcmax;
-        // records per fit launch: their B and W within 2 GiB
-        sub = std::max<int64_t>(1, ((int64_t)2 << 30) / (8 * std::max<int64_t>(fp.bwStride, 1)));
-        MPG_CUDA(c, dgrow(j, j.bw, sub * fp.bwStride));
-        fp.bw = j.bw;
+    // fit launches per size class of records (fit buckets, ordered at
+    // upload): each class gets shared memory for its own largest record;
+    // classes whose B and W do not fit a warp's shared memory with four
+    // warps per CTA take the large-record path
+    const bool onePer = (c->flags & MPGPU_FLAG_ONE_RECORD_PER_BLOCK) != 0;
+    const bool bucketed = !onePer && !(c->flags & MPGPU_FLAG_NO_BUCKETS) && !j.bucketOff.empty();
+    const int nb = bucketed ? MPG_FIT_BUCKETS : 1;
+    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
+    std::vector<FitParams> bfp(nb, fp);
+    std::vector<int64_t> bsub(nb, 0);
+    int64_t bwNeed = 0;
+    for (int b = 0; b < nb; ++b) {
+        FitParams &q = bfp[b];
+        if (bucketed) {
+            if (j.bucketOff[nchunk * nb] == 0) continue;
+            int64_t cnt = 0;
+            for (int64_t ch = 0; ch < nchunk; ++ch) cnt += j.bucketOff[ch * nb + b + 1] - j.bucketOff[ch * nb + b];
+            if (cnt == 0) continue;
+            const int32_t *m = &j.bucketMax[7 * b];
+            q.wmax = std::max(m[0], 1); q.neqmax = std::max(m[1], 1);
+            q.nalcmax = std::max(m[2], 1); q.nalgmax = std::max(m[3], 1);
+            q.bandmax = opt->lfitbb > 0 ? m[4] - 1 : -1; q.bdrmax = m[5];
+            q.ngrpmax = std::max(m[6], 1);
+            q.recList = j.recList;
+        }
+        q.onePerBlock = onePer ? 1 : 0;
+        // the path is chosen by the arena's capacity (not by a tuned warp
+        // count), so that every loop of a job takes the same path
+        q.bigMode = 0;
+        q.wpc = 0;
+        FitParams cap = q;
+        cap.onePerBlock = 0;
+        q.bigMode = (c->flags & MPGPU_FLAG_LARGE_RECORDS) || fit_warps_per_cta(cap) < 4 ? 1 : 0;
+        if (bucketed && !j.bucketWpc.empty() && j.bucketWpc[b] > 0) q.wpc = j.bucketWpc[b];
+        if (q.bigMode) {
+            q.bwStride = 2 * (int64_t)q.nalgmax * q.nalcmax;
+            // records per fit launch: their B and W within 2 GiB
+            bsub[b] = std::max<int64_t>(1, ((int64_t)2 << 30) / (8 * std::max<int64_t>(q.bwStride, 1)));
+            bwNeed = std::max(bwNeed, bsub[b] * q.bwStride);
+        }
+        if (fit_warps_per_cta(q) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     }
-    if (fit_warps_per_cta(fp) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
+    if (bwNeed > 0) {
+        MPG_CUDA(c, dgrow(j, j.bw, bwNeed));
+        for (auto &q : bfp) q.bw = j.bw;
+    }
     if (fp.bandmax >= 0 && opt->icalcm == 1) {
-        // every warp that can be resident: 64 per SM
-        fp.bscrStride = 32 * (int64_t)fp.nalcmax + (int64_t)fp.nalcmax * (fp.nalcmax + 1) / 2 + 2;
-        MPG_CUDA(c, dgrow(j, j.bscr, (int64_t)nsm * 64 * fp.bscrStride));
-        fp.bscr = j.bscr;
+        // every warp that can be resident: 64 per SM (one-record-per-block
+        // launches take at most that many records)
+        const int64_t stride = 32 * (int64_t)fp.nalcmax + (int64_t)fp.nalcmax * (fp.nalcmax + 1) / 2 + 2;
+        MPG_CUDA(c, dgrow(j, j.bscr, (int64_t)nsm * 64 * stride));
+        for (auto &q : bfp) { q.bscr = j.bscr; q.bscrStride = stride; }
+    }
+    // warps per CTA of each class, timed once per upload on a sample of the
+    // class (first loop with matrix); the records' results do not depend on it
+    if (bucketed && opt->icalcm == 1 && !(c->flags & MPGPU_FLAG_NO_AUTOTUNE) && nchunk > 0) {
+        for (int b = 0; b < nb; ++b) {
+            if (j.bucketWpc[b] != 0 || bfp[b].recList == nullptr) continue;
+            // sample: four waves of the most warps an SM holds
+            const int64_t sample = bfp[b].bigMode ? std::min<int64_t>(bsub[b], (int64_t)nsm * 64)
+                                                  : (int64_t)nsm * 64 * 4;
+            const int64_t i0 = j.bucketOff[b], i1 = std::min(j.bucketOff[b + 1], i0 + sample);
+            if (i1 <= i0) continue;
+            FitParams q = bfp[b];
+            q.stage = j.stage;
+            q.r0 = i0;
+            q.r1 = i1;
+            const int cand[4] = {1, 2, 4, 8};
+            float best = 0.0f;
+            int bestW = 0;
+            // more warps per CTA are kept unless fewer are at least 3 % faster
+            cudaEvent_t t0, t1;
+            cudaEventCreate(&t0);
+            cudaEventCreate(&t1);
+            for (int k = 0; k < 4; ++k) {
+                q.wpc = cand[k];
+                if (fit_warps_per_cta(q) != cand[k]) continue;
+                MPG_CUDA(c, launch_fit(q, nsm, 0, s));   // warm
+                cudaEventRecord(t0, s);
+                MPG_CUDA(c, launch_fit(q, nsm, 0, s));
+                cudaEventRecord(t1, s);
+                MPG_CUDA(c, cudaEventSynchronize(t1));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, t0, t1);
+                j.bucketTuneMs[4 * b + k] = ms;
+                if (bestW == 0 || ms <= best * 1.03f) {
+                    if (bestW == 0 || ms < best) best = ms;
+                    bestW = cand[k];
+                }
+            }
+            cudaEventDestroy(t0);
+            cudaEventDestroy(t1);
+            j.bucketWpc[b] = bestW > 0 ? bestW : -1;
+            bfp[b].wpc = bestW > 0 ? bestW : 0;
+        }
     }
     AccParams ap{};
     ap.bkI = j.bkI; ap.bkJ = j.bkJ; ap.bkLd = j.bkLd; ap.bkOff = j.bkOff;
@@ -396,7 +492,6 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     ap.status = j.status; ap.stage = j.stage; ap.vstage = j.vstage; ap.slotCnt = j.slotCnt;
     ap.aig = j.aig; ap.nG = j.nG; ap.matsto = j.matsto;
     ap.icalcm = opt->icalcm; ap.matD = j.matD; ap.gvec = j.gvec; ap.gcnt = j.gcnt; ap.errFlag = errFlag;
-    const int64_t nchunk = (int64_t)j.chunkRec.size() - 1;
     // fits on stream 1, accumulation on stream 2; with several chunks the
     // staging alternates between two buffers and the fit of chunk k+1 runs
     // while chunk k is accumulated (the fit kernel then keeps one CTA per SM
@@ -423,20 +518,24 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         if (overlap && ch >= 2) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[ch - 2], 0));
         fp.stage = stg;
         cudaEventRecord(evF0[ch], s);
-        if (fp.bigMode) {
-            const int64_t c0 = fp.r0, c1 = fp.r1;
-            for (int64_t a = c0; a < c1; a += sub) {
-                fp.r0 = a;
-                fp.r1 = std::min(c1, a + sub);
-                MPG_CUDA(c, launch_fit(fp, nsm, 0, s));
-                MPG_CUDA(c, launch_update_big(fp, s));
-                launches += 2;
+        for (int b = 0; b < nb; ++b) {
+            FitParams q = bfp[b];
+            const int64_t i0 = bucketed ? j.bucketOff[ch * nb + b] : fp.r0;
+            const int64_t i1 = bucketed ? j.bucketOff[ch * nb + b + 1] : fp.r1;
+            if (i1 <= i0) continue;
+            q.stage = stg;
+            int64_t step = q.bigMode ? bsub[b] : i1 - i0;
+            if (onePer) step = std::min<int64_t>(step, (int64_t)nsm * 64);
+            for (int64_t a = i0; a < i1; a += step) {
+                q.r0 = a;
+                q.r1 = std::min(i1, a + step);
+                MPG_CUDA(c, launch_fit(q, nsm, 0, s));
+                launches++;
+                if (q.bigMode) {
+                    MPG_CUDA(c, launch_update_big(q, s));
+                    launches++;
+                }
             }
-            fp.r0 = c0;
-            fp.r1 = c1;
-        } else if (fp.r1 > fp.r0) {
-            MPG_CUDA(c, launch_fit(fp, nsm, 0, s));
-            launches++;
         }
         cudaEventRecord(evF1[ch], s);
         MPG_CUDA(c, cudaStreamWaitEvent(s2, evF1[ch], 0));

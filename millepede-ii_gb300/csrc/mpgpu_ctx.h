@@ -11,6 +11,7 @@
 #include "../../include/mpgpu.h"
 
 #define MPG_WARPS_FIT 8        // warps per CTA of the local-fit kernel
+#define MPG_FIT_BUCKETS 8      // size classes of records for the fit launches
 #define MPG_NALC_MAX 96        // largest local system handled by the fit kernel
 #define MPG_NGRP_MAX 255       // parameter groups per record (entry encoding)
 #define MPG_WORDS_MAX 65535    // words per record (16-bit word positions)
@@ -47,6 +48,8 @@ struct UpTmp {
     int64_t *bcnt = nullptr, *bscan = nullptr, *cntG = nullptr;
     int64_t *scal = nullptr;                  // error word and maxima
     int64_t *ovList = nullptr;                // records handed to the large record kernels
+    int64_t *chunkB = nullptr, *keyEnd = nullptr;  // chunk boundaries, fit-bucket ends
+    int32_t *bmax = nullptr;                  // maxima per fit bucket
 };
 
 // Device arrays of one job.  Every pointer is owned by the context.
@@ -97,6 +100,14 @@ struct DevJob {
     double *vstage = nullptr;      // per-slot vector contributions
     // chunks of records sharing one update staging buffer
     std::vector<int64_t> chunkRec;     // [nchunk+1] record boundaries
+    // fit buckets: records classed by the shared memory their fit needs
+    // (power-of-two classes from 4 KB; the last class for records beyond one
+    // CTA), ordered by (chunk, class, record) in recList
+    uint32_t *recList = nullptr;
+    std::vector<int64_t> bucketOff;    // [nchunk * MPG_FIT_BUCKETS + 1] positions in recList
+    std::vector<int32_t> bucketMax;    // [MPG_FIT_BUCKETS * 7] nw neq nalc nalg band bdr ngrp
+    std::vector<int32_t> bucketWpc;    // [MPG_FIT_BUCKETS] tuned warps per CTA (0: not tuned)
+    std::vector<double> bucketTuneMs;  // [MPG_FIT_BUCKETS * 4] sample times of wpc 1, 2, 4, 8
     // matrix accumulation: the group-pair blocks (I, J <= I) met in records,
     // per chunk the records of each block (packed U offset << 16 | row slot)
     // cut into work items; items of a block share partial sums when a block
@@ -189,6 +200,36 @@ inline cudaError_t dgrow(DevJob &j, T *&p, int64_t n) {
     return cudaSuccess;
 }
 
+// shared memory of one fit warp for records up to the given sizes (the
+// carve-up of mpgpu_fit.cu); also used to class records by size
+__host__ __device__ inline int64_t align8(int64_t x) { return (x + 7) & ~int64_t(7); }
+
+__host__ __device__ inline int64_t band_doubles(int nalc, int bandmax, int bdrmax) {
+    if (bandmax < 0) return 0;
+    int64_t n = nalc, b = bandmax, d = bdrmax;
+    // vbnd n*(b+1), vbdr n*d, aux n*d+n, vbk d*d, vzru n, scdiag n (+1 each)
+    return n * (b + 1) + 2 * n * d + 3 * n + d * d + 16;
+}
+
+__host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax, int nalgmax,
+                                              int bandmax, int bdrmax, int ngrpmax, bool big = false) {
+    int64_t d = 0;
+    d += wmax;                          // gl
+    d += 7 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2 w0
+    d += (int64_t)nalcmax * (nalcmax + 1) / 2 + 4 * (int64_t)nalcmax;  // clmat blvec diag ocol scol
+    if (!big) d += 2 * (int64_t)nalcmax * nalgmax;  // B W (global memory for large records)
+    d += band_doubles(nalcmax, bandmax, bdrmax);
+    int64_t i = 0;
+    i += wmax;            // in
+    i += 3 * (int64_t)neqmax;
+    i += nalgmax;         // slots
+    i += nalgmax + 1;     // swS
+    i += wmax;            // sw
+    i += nalcmax + 2;     // used / scflag
+    i += ngrpmax + 2;     // goff
+    return align8(d * 8 + i * 4 + 64);
+}
+
 // ---------------------------------------------------------------- kernels
 struct FitParams {
     const RecInfo *rec;
@@ -203,7 +244,10 @@ struct FitParams {
     const double *gpar;
     const int32_t *varOfTot;
     const double *fileWeight;
-    int64_t r0, r1;           // record range
+    int64_t r0, r1;           // record range, or positions r0..r1 of recList
+    const uint32_t *recList;  // records in fit order (null: r0..r1 are records)
+    int32_t wpc;              // warps per CTA (0: as many as the shared memory allows)
+    int32_t onePerBlock;      // one record per CTA of one warp, no persistent loop
     int32_t icalcm, nloopn, lhuber, lfitbb;
     float chicut, chhuge, dwcut, cndlmx;
     double *stage;            // update staging of this chunk

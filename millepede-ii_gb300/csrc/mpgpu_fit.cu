@@ -453,34 +453,6 @@ struct WarpMem {
     int32_t *in, *mq, *slots, *swS, *sw, *used, *goff;
 };
 
-__host__ __device__ inline int64_t align8(int64_t x) { return (x + 7) & ~int64_t(7); }
-
-__host__ __device__ inline int64_t band_doubles(int nalc, int bandmax, int bdrmax) {
-    if (bandmax < 0) return 0;
-    int64_t n = nalc, b = bandmax, d = bdrmax;
-    // vbnd n*(b+1), vbdr n*d, aux n*d+n, vbk d*d, vzru n, scdiag n (+1 each)
-    return n * (b + 1) + 2 * n * d + 3 * n + d * d + 16;
-}
-
-__host__ __device__ inline int64_t warp_bytes(int wmax, int neqmax, int nalcmax, int nalgmax,
-                                              int bandmax, int bdrmax, int ngrpmax, bool big = false) {
-    int64_t d = 0;
-    d += wmax;                          // gl
-    d += 7 * (int64_t)neqmax;           // rm1 lcor lwgt res t1 t2 w0
-    d += (int64_t)nalcmax * (nalcmax + 1) / 2 + 4 * (int64_t)nalcmax;  // clmat blvec diag ocol scol
-    if (!big) d += 2 * (int64_t)nalcmax * nalgmax;  // B W (global memory for large records)
-    d += band_doubles(nalcmax, bandmax, bdrmax);
-    int64_t i = 0;
-    i += wmax;            // in
-    i += 3 * (int64_t)neqmax;
-    i += nalgmax;         // slots
-    i += nalgmax + 1;     // swS
-    i += wmax;            // sw
-    i += nalcmax + 2;     // used / scflag
-    i += ngrpmax + 2;     // goff
-    return align8(d * 8 + i * 4 + 64);
-}
-
 __device__ WarpMem carve(char *base, const FitParams &p) {
     WarpMem m;
     double *d = (double *)base;
@@ -672,7 +644,8 @@ k_fit(FitParams p, int perWarp) {
     WarpMem m = carve(smem + (int64_t)wib * perWarp, p);
     const int64_t nwarps = (int64_t)gridDim.x * wpc;
 
-    for (int64_t r = p.r0 + (int64_t)blockIdx.x * wpc + wib; r < p.r1; r += nwarps) {
+    for (int64_t it = p.r0 + (int64_t)blockIdx.x * wpc + wib; it < p.r1; it += nwarps) {
+        const int64_t r = p.recList ? (int64_t)p.recList[it] : it;
         const RecInfo ri = p.rec[r];
         const int nw = ri.nw, neq = ri.neq, nalc = ri.nalc, nalg = ri.nalg;
         for (int i = ln; i < nw; i += 32) {
@@ -686,7 +659,7 @@ k_fit(FitParams p, int perWarp) {
         const int64_t *pdst = p.pairDst + ri.pairOff;  // staging offset per group pair
         double *mB = m.B, *mW = m.W;   // large records: this record's slot in global memory
         if (BIG) {
-            mB = p.bw + (r - p.r0) * p.bwStride;
+            mB = p.bw + (it - p.r0) * p.bwStride;
             mW = mB + (int64_t)nalc * nalg;
         }
         if (p.icalcm == 1 && nalc > 0) {
@@ -1071,7 +1044,8 @@ __global__ void __launch_bounds__(256) k_update_big(FitParams p) {
     __shared__ double ws[kUbK][kUbT + 1], bs[kUbK][kUbT + 1];
     __shared__ int32_t goffs[MPG_NGRP_MAX + 2];
     extern __shared__ int32_t gidx[];   // group of each slot
-    const int64_t r = p.r0 + blockIdx.x;
+    const int64_t it = p.r0 + blockIdx.x;
+    const int64_t r = p.recList ? (int64_t)p.recList[it] : it;
     const RecInfo ri = p.rec[r];
     if (ri.nalc <= 0 || p.status[r] != 0) return;
     const int nalg = ri.nalg, nalc = ri.nalc, ngrp = ri.ngrp;
@@ -1085,7 +1059,7 @@ __global__ void __launch_bounds__(256) k_update_big(FitParams p) {
         gidx[sl] = g;
     }
     __syncthreads();
-    const double *B = p.bw + (r - p.r0) * p.bwStride;   // B[k * nalg + s]
+    const double *B = p.bw + (it - p.r0) * p.bwStride;  // B[k * nalg + s]
     const double *W = B + (int64_t)nalc * nalg;          // W[s * nalc + k]
     const int64_t *pdst = p.pairDst + ri.pairOff;
     const int T = (nalg + kUbT - 1) / kUbT;
@@ -1142,10 +1116,11 @@ int fit_smem_per_warp(const FitParams &p) {
                            p.bigMode != 0);
 }
 
-// warps per CTA so that one CTA fits the 227 KB of shared memory
+// warps per CTA so that one CTA fits the 227 KB of shared memory (at most
+// p.wpc when that is set; one for the one-record-per-block form)
 int fit_warps_per_cta(const FitParams &p) {
     const int per = fit_smem_per_warp(p);
-    int wpc = MPG_WARPS_FIT;
+    int wpc = p.onePerBlock ? 1 : (p.wpc > 0 ? std::min(p.wpc, MPG_WARPS_FIT) : MPG_WARPS_FIT);
     while (wpc > 1 && (int64_t)per * wpc > 220 * 1024) wpc--;
     return (int64_t)per * wpc > 220 * 1024 ? 0 : wpc;
 }
@@ -1165,7 +1140,7 @@ cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s
     int64_t nrec = p.r1 - p.r0;
     int64_t grid = (int64_t)nsm * perSM;
     int64_t need = (nrec + wpc - 1) / wpc;
-    if (grid > need) grid = need;
+    if (grid > need || p.onePerBlock) grid = need;
     if (grid < 1) grid = 1;
     kern<<<(unsigned)grid, 32 * wpc, bytes, s>>>(p, per);
     return cudaGetLastError();

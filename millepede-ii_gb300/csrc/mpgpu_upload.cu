@@ -405,6 +405,58 @@ __global__ void k_ventries(const uint64_t *key, const uint32_t *val, int64_t n, 
 }
 
 
+// fit size class of every record (the shared memory of its fit: power-of-two
+// classes from 4 KB, the last for records beyond one CTA), sort key (chunk,
+// class) and the maxima of each class (reduced per block in shared memory)
+__global__ void k_fit_bucket(const RecInfo *rec, int64_t nrec, const int64_t *chunkB, int nchunk, uint64_t *key,
+                             uint32_t *val, int32_t *bmax) {
+    __shared__ int32_t sm[MPG_FIT_BUCKETS * 7];
+    for (int i = threadIdx.x; i < MPG_FIT_BUCKETS * 7; i += blockDim.x) sm[i] = 0;
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < nrec; r += stride) {
+        const RecInfo ri = rec[r];
+        int lo = 0, hi = nchunk - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (chunkB[mid] <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        const bool band = ri.mbnd >= 0;
+        const int64_t bytes = warp_bytes(max(ri.nw, 1), max(ri.neq, 1), max(ri.nalc, 1), max(ri.nalg, 1),
+                                         band ? ri.mbnd : -1, band ? ri.mbdr : 0, max(ri.ngrp, 1), false);
+        int b = 0;
+        if (bytes > 220 * 1024) b = MPG_FIT_BUCKETS - 1;
+        else
+            while (b < MPG_FIT_BUCKETS - 2 && ((int64_t)4096 << b) < bytes) b++;
+        key[r] = (uint64_t)lo * MPG_FIT_BUCKETS + (uint64_t)b;
+        val[r] = (uint32_t)r;
+        int32_t *m = sm + 7 * b;
+        atomicMax(&m[0], ri.nw);
+        atomicMax(&m[1], ri.neq);
+        atomicMax(&m[2], ri.nalc);
+        atomicMax(&m[3], ri.nalg);
+        if (band) {
+            atomicMax(&m[4], ri.mbnd + 1);
+            atomicMax(&m[5], ri.mbdr);
+        }
+        atomicMax(&m[6], ri.ngrp);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < MPG_FIT_BUCKETS * 7; i += blockDim.x)
+        if (sm[i] > 0) atomicMax(&bmax[i], sm[i]);
+}
+
+__global__ void k_key_ends(const uint64_t *k, int64_t n, int64_t *ends) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && (i == n - 1 || k[i] != k[i + 1])) ends[k[i]] = i + 1;
+}
+
+__global__ void k_u32_copy(const uint32_t *src, uint32_t *dst, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
 }  // namespace
 
 int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const int32_t *inder,
@@ -522,7 +574,7 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     }
     MPG_CUDA(c, cudaGetLastError());
     // ---- blocks of the record pairs
-    const int64_t nsort = std::max<int64_t>(std::max(npairs, ngrpT), 1);
+    const int64_t nsort = std::max<int64_t>({npairs, ngrpT, nrec, 1});
     MPG_CUDA(c, dgrow(j, t.k0, nsort));
     MPG_CUDA(c, dgrow(j, t.k1, nsort));
     MPG_CUDA(c, dgrow(j, t.v0, nsort));
@@ -702,6 +754,35 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
         vbase = vend;
     }
     MPG_CUDA(c, cudaGetLastError());
+    // ---- fit buckets: records ordered by (chunk, size class, record)
+    {
+        const int64_t nkey = nchunk * MPG_FIT_BUCKETS;
+        MPG_CUDA(c, dgrow(j, t.chunkB, nchunk + 1));
+        MPG_CUDA(c, dgrow(j, t.bmax, MPG_FIT_BUCKETS * 7));
+        MPG_CUDA(c, dgrow(j, t.keyEnd, nkey));
+        MPG_CUDA(c, dgrow(j, j.recList, nrec));
+        MPG_CUDA(c, cudaMemcpyAsync(t.chunkB, j.chunkRec.data(), sizeof(int64_t) * (nchunk + 1),
+                                    cudaMemcpyHostToDevice, s));
+        MPG_CUDA(c, cudaMemsetAsync(t.bmax, 0, sizeof(int32_t) * MPG_FIT_BUCKETS * 7, s));
+        MPG_CUDA(c, cudaMemsetAsync(t.keyEnd, 0, sizeof(int64_t) * nkey, s));
+        if (nrec > 0) {
+            k_fit_bucket<<<(unsigned)std::min<int64_t>(blocks_for(nrec), (int64_t)nsm * 4), 256, 0, s>>>(
+                j.rec, nrec, t.chunkB, (int)nchunk, sb.k0, sb.v0, t.bmax);
+            MPG_CUDA(c, radix_sort(sb, nrec, bits_for((uint64_t)std::max<int64_t>(nkey - 1, 1)), s));
+            k_key_ends<<<blocks_for(nrec), 256, 0, s>>>(sb.k0, nrec, t.keyEnd);
+            k_u32_copy<<<blocks_for(nrec), 256, 0, s>>>(sb.v0, j.recList, nrec);
+        }
+        std::vector<int64_t> ends(nkey);
+        j.bucketMax.assign(MPG_FIT_BUCKETS * 7, 0);
+        MPG_CUDA(c, cudaMemcpyAsync(ends.data(), t.keyEnd, sizeof(int64_t) * nkey, cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaMemcpyAsync(j.bucketMax.data(), t.bmax, sizeof(int32_t) * MPG_FIT_BUCKETS * 7,
+                                    cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        j.bucketOff.assign(nkey + 1, 0);
+        for (int64_t k = 0; k < nkey; ++k) j.bucketOff[k + 1] = ends[k] > 0 ? ends[k] : j.bucketOff[k];
+        j.bucketWpc.assign(MPG_FIT_BUCKETS, 0);
+        j.bucketTuneMs.assign(MPG_FIT_BUCKETS * 4, 0.0);
+    }
     // ---- per-loop outputs, file weights, staging and partial sums
     std::vector<double> fw(nfiles, 1.0);
     if (fileWeight) fw.assign(fileWeight, fileWeight + nfiles);

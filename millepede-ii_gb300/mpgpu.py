@@ -19,6 +19,13 @@ f64p = C.POINTER(C.c_double)
 f32p = C.POINTER(C.c_float)
 
 
+# mpgpu_cfg flags (include/mpgpu.h)
+FLAG_LARGE_RECORDS = 1
+FLAG_NO_BUCKETS = 2
+FLAG_ONE_RECORD_PER_BLOCK = 4
+FLAG_NO_AUTOTUNE = 8
+
+
 class MpgpuCfg(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32), ("staging_bytes", C.c_int64)]
 
@@ -110,7 +117,7 @@ EXPORTS = [
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
     "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
-    "mpgpu_dense_cholesky", "mpgpu_upload_timing",
+    "mpgpu_dense_cholesky", "mpgpu_upload_timing", "mpgpu_fit_buckets",
     "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
     "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
@@ -398,6 +405,14 @@ class Context:
         self.check(self.L.mpgpu_upload_records(
             self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(None if resident else S.tinder, i32p),
             ptr(None if resident else S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
+
+    def fit_buckets(self):
+        """(records, tuned warps per CTA, sample ms [k][1,2,4,8 warps]) per fit size class."""
+        cnt = np.zeros(8, np.int64)
+        wpc = np.zeros(8, np.int32)
+        tms = np.zeros(32, np.float64)
+        self.check(self.L.mpgpu_fit_buckets(self.h, ptr(cnt, i64p), ptr(wpc, i32p), ptr(tms, f64p)))
+        return cnt, wpc, tms.reshape(8, 4)
 
     def upload_timing(self):
         """(ms copy, ms prepare, chunks) of the last upload."""

@@ -171,3 +171,40 @@ def test_special_blocks_sequential_decode(mp, orc, name, matsto):
     d = with_special_blocks(mp.generate(mp.gen_config(name, ntracks=3000, seed=21)))
     g, o, _ = run_pair(mp, orc, d, matsto)
     check(g, o)
+
+
+def loop_with_flags(mp, d, flags, matsto=2):
+    H = mp.HostStructure(d, mreqenf=5, sparse=(matsto == 2))
+    with mp.Context(flags=flags) as ctx:
+        ctx.set_layout(H, matsto)
+        ctx.upload(H)
+        gpar = np.zeros(H.nTotal)
+        ctx.loopbf(gpar)                     # first loop: the tuner runs here
+        g = ctx.loopbf(gpar)
+        g["matD"] = ctx.matrix()
+        g["status"] = ctx.status()
+        g["buckets"] = ctx.fit_buckets()
+    return g
+
+
+def test_fit_buckets_same_loop(mp, orc):
+    """Broken-line records of 4-40 hits (nloc 8-84) fall into several size
+    classes with their own fit launches (and tuned warps per CTA); the loop
+    agrees with the single-launch form, with the one-record-per-block form
+    and with the oracle: decisions exactly, sums within 1e-12."""
+    cfg = mp.gen_config("brokenlines", ntracks=3000, seed=41)
+    d = mp.generate(cfg)
+    gb = loop_with_flags(mp, d, 0)
+    cnt, wpc, tms = gb["buckets"]
+    assert np.count_nonzero(cnt) >= 3 and cnt.sum() == len(d["recPtr"]) - 1
+    assert np.all(wpc[cnt > 0] != 0)
+    for flags in (mp.FLAG_NO_BUCKETS, mp.FLAG_ONE_RECORD_PER_BLOCK):
+        g = loop_with_flags(mp, d, flags)
+        np.testing.assert_array_equal(g["status"], gb["status"])
+        assert g["nrej"] == gb["nrej"] and g["ndf"] == gb["ndf"]
+        close(g["gvec"], gb["gvec"])
+        close(g["matD"], gb["matD"])
+    O = orc.Structure(d, mreqenf=5, sparse=True)
+    H = mp.HostStructure(d, mreqenf=5, sparse=True)
+    o = O.loopbf(np.zeros(H.nTotal), matsto=2)
+    check(gb, o)
