@@ -143,51 +143,6 @@ __device__ void warp_sqminv(double *v, double *b, int n, int *nrank_out, double 
 }
 
 // ------------------------------------------------------------------------
-// Sequential bordered-band solvers (one lane), Dbandmatrix.f90:459-638 and
-// mpnum.f90:3118-3600.  All arrays 1-based.
-#define WB(r, c) w[((c) - 1) * mp1 + (r)]
-__device__ void s_dbcdec(double *w, int mp1, int n, double *aux) {
-    for (int i = 1; i <= n; i++) aux[i] = 16.0 * WB(1, i);
-    for (int i = 1; i <= n; i++) {
-        if (WB(1, i) + aux[i] != aux[i]) WB(1, i) = 1.0 / WB(1, i);
-        else WB(1, i) = 0.0;
-        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
-        for (int j = 1; j <= mj; j++) {
-            double rxw = WB(j + 1, i) * WB(1, i);
-            for (int k = 1; k <= mj + 1 - j; k++) WB(k, i + j) = WB(k, i + j) - WB(k + j, i) * rxw;
-            WB(j + 1, i) = rxw;
-        }
-    }
-}
-__device__ void s_dbcslv(const double *w, int mp1, int n, const double *b, double *x) {
-    for (int i = 1; i <= n; i++) x[i] = b[i];
-    for (int i = 1; i <= n; i++) {
-        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
-        for (int j = 1; j <= mj; j++) x[j + i] = x[j + i] - WB(j + 1, i) * x[i];
-    }
-    for (int i = n; i >= 1; i--) {
-        double rxw = x[i] * WB(1, i);
-        int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
-        for (int j = 1; j <= mj; j++) rxw = rxw - WB(j + 1, i) * x[j + i];
-        x[i] = rxw;
-    }
-}
-__device__ void s_dbcinv(const double *w, int mp1, int n, double *vs, bool bandOnly) {
-    for (int i = n; i >= 1; i--) {
-        double rxw = WB(1, i);
-        int jlo = bandOnly ? ((1 > i - mp1 + 1) ? 1 : i - mp1 + 1) : 1;
-        for (int j = i; j >= jlo; j--) {
-            int khi = (n < j + mp1 - 1) ? n : j + mp1 - 1;
-            for (int k = j + 1; k <= khi; k++) {
-                int a = i > k ? i : k, c = i > k ? k : i;
-                rxw = rxw - vs[(a * (a - 1)) / 2 + c] * WB(1 + k - j, j);
-            }
-            vs[(i * i - i) / 2 + j] = rxw;
-            rxw = 0.0;
-        }
-    }
-}
-#undef WB
 
 // sequential sqminv for the border part (1-based)
 __device__ void s_sqminv(double *v, double *b, int n, int *nrank, double *diag, int *next) {
@@ -245,204 +200,6 @@ struct BandWork {
     double *vbnd, *vbdr, *aux, *vbk, *vzru, *scdiag;
     int *scflag;
 };
-
-// sqmibb (side 1, upper/left border) and sqmibb2 (side 2) in one routine;
-// v, b 1-based.
-__device__ void s_sqmibb(int side, double *v, double *b, int n, int nbdr, int nbnd, int inv,
-                         int *nrank, double *evdmin, double *evdmax, BandWork &wk) {
-    double *vbnd = wk.vbnd, *vbdr = wk.vbdr, *aux = wk.aux, *vbk = wk.vbk, *vzru = wk.vzru;
-    int mp1 = nbnd + 1, nmb = n - nbdr, ip, is, ioff, joff, ij, nrankb;
-    *nrank = 0;
-    if (side == 1) {
-        int nb1 = nbdr + 1;
-        for (int i = nb1; i <= n; i++) {
-            ip = (i * (i + 1)) / 2; is = 0;
-            int jhi = (n < i + nbnd) ? n : i + nbnd;
-            for (int j = i; j <= jhi; j++) { ip += is; is = j; vbnd[j - i + 1 + (i - nb1) * mp1] = v[ip]; }
-        }
-        ioff = 0;
-        for (int i = 1; i <= nbdr; i++) {
-            ip = (i * (i + 1)) / 2; is = 0;
-            for (int j = i; j <= n; j++) { ip += is; is = j; vbdr[ioff + j] = v[ip]; }
-            ioff += n;
-        }
-    } else {
-        int nb1 = nmb + 1;
-        for (int i = 1; i <= nmb; i++) {
-            ip = (i * (i + 1)) / 2; is = 0;
-            int jhi = (nmb < i + nbnd) ? nmb : i + nbnd;
-            for (int j = i; j <= jhi; j++) { ip += is; is = j; vbnd[j - i + 1 + (i - 1) * mp1] = v[ip]; }
-        }
-        ioff = 0;
-        for (int i = nb1; i <= n; i++) {
-            ip = (i * (i - 1)) / 2;
-            for (int j = 1; j <= i; j++) vbdr[ioff + j] = v[ip + j];
-            ioff += n;
-        }
-    }
-    s_dbcdec(vbnd, mp1, nmb, aux);
-    ip = 1;
-    *evdmin = 0.0; *evdmax = 0.0;
-    for (int i = 1; i <= nmb; i++) {
-        if (vbnd[ip] <= 0.0) {
-            for (int q = 1; q <= n; q++) b[q] = 0.0;
-            for (int q = 1; q <= (n * n + n) / 2; q++) v[q] = 0.0;
-            *nrank = 0;
-            return;
-        }
-        (*nrank)++;
-        if (*nrank == 1) { *evdmin = vbnd[ip]; *evdmax = vbnd[ip]; }
-        else { if (vbnd[ip] < *evdmin) *evdmin = vbnd[ip]; if (vbnd[ip] > *evdmax) *evdmax = vbnd[ip]; }
-        ip += mp1;
-    }
-    if (nbdr == 0) {
-        s_dbcslv(vbnd, mp1, nmb, b, b);
-        if (inv > 0) s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
-        return;
-    }
-    if (side == 1) {
-        int nb1 = nbdr + 1;
-        ioff = nb1;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            s_dbcslv(vbnd, mp1, nmb, vbdr + ioff - 1, aux + ioff - 1);
-            vzru[ib] = b[ib];
-            for (int i = 0; i <= nmb - 1; i++) vzru[ib] = vzru[ib] - b[nb1 + i] * aux[ioff + i];
-            ioff += n;
-        }
-        s_dbcslv(vbnd, mp1, nmb, b + nb1 - 1, b + nb1 - 1);
-        ip = 0; ioff = nb1;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            joff = nb1;
-            for (int jb = 1; jb <= ib; jb++) {
-                ip++;
-                vbk[ip] = v[ip];
-                for (int i = 0; i <= nmb - 1; i++) vbk[ip] = vbk[ip] - vbdr[ioff + i] * aux[joff + i];
-                joff += n;
-            }
-            ioff += n;
-        }
-        s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
-        if (nrankb == nbdr) *nrank += nbdr;
-        else {
-            for (int ib = 1; ib <= nbdr; ib++) vzru[ib] = 0.0;
-            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) vbk[q] = 0.0;
-        }
-        ioff = nb1;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            b[ib] = vzru[ib];
-            for (int i = 0; i <= nmb - 1; i++) b[nb1 + i] = b[nb1 + i] - b[ib] * aux[ioff + i];
-            ioff += n;
-        }
-        if (inv > 0) {
-            s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
-            int ip1 = (nmb * nmb + nmb) / 2, ip2 = (n * n + n) / 2;
-            for (int i = nmb - 1; i >= 0; i--) {
-                int j0 = 0;
-                if (inv == 1) j0 = (0 > i - nbnd) ? 0 : i - nbnd;
-                for (int j = i; j >= j0; j--) {
-                    v[ip2] = v[ip1];
-                    ioff = nb1;
-                    for (int ib = 1; ib <= nbdr; ib++) {
-                        joff = nb1;
-                        for (int jb = 1; jb <= nbdr; jb++) {
-                            ij = ib > jb ? ib : jb;
-                            ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
-                            v[ip2] = v[ip2] + vbk[ij] * aux[ioff + i] * aux[joff + j];
-                            joff += n;
-                        }
-                        ioff += n;
-                    }
-                    ip1--; ip2--;
-                }
-                ip1 -= j0; ip2 -= j0;
-                for (int ib = nbdr; ib >= 1; ib--) {
-                    v[ip2] = 0.0;
-                    joff = nb1;
-                    for (int jb = 1; jb <= nbdr; jb++) {
-                        ij = ib > jb ? ib : jb;
-                        ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
-                        v[ip2] = v[ip2] - vbk[ij] * aux[i + joff];
-                        joff += n;
-                    }
-                    ip2--;
-                }
-            }
-            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) { v[ip2] = vbk[q]; ip2--; }
-        }
-    } else {
-        ioff = 0;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            s_dbcslv(vbnd, mp1, nmb, vbdr + ioff, aux + ioff);
-            vzru[ib] = b[nmb + ib];
-            for (int i = 1; i <= nmb; i++) vzru[ib] = vzru[ib] - b[i] * aux[ioff + i];
-            ioff += n;
-        }
-        s_dbcslv(vbnd, mp1, nmb, b, b);
-        ip = 0; ioff = 0;
-        int koff = nmb;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            joff = 0;
-            for (int jb = 1; jb <= ib; jb++) {
-                ip++;
-                vbk[ip] = vbdr[koff + jb];
-                for (int i = 1; i <= nmb; i++) vbk[ip] = vbk[ip] - vbdr[ioff + i] * aux[joff + i];
-                joff += n;
-            }
-            ioff += n; koff += n;
-        }
-        s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
-        if (nrankb == nbdr) *nrank += nbdr;
-        else {
-            for (int ib = 1; ib <= nbdr; ib++) vzru[ib] = 0.0;
-            for (int q = (nbdr * nbdr + nbdr) / 2; q >= 1; q--) vbk[q] = 0.0;
-        }
-        ioff = 0;
-        for (int ib = 1; ib <= nbdr; ib++) {
-            for (int i = 1; i <= nmb; i++) b[i] = b[i] - vzru[ib] * aux[ioff + i];
-            ioff += n;
-            b[nmb + ib] = vzru[ib];
-        }
-        if (inv > 0) {
-            s_dbcinv(vbnd, mp1, nmb, v, inv == 1);
-            int ip1 = (nmb * nmb + nmb) / 2;
-            for (int i = nmb - 1; i >= 0; i--) {
-                int j0 = 0;
-                if (inv == 1) j0 = (0 > i - nbnd) ? 0 : i - nbnd;
-                for (int j = i; j >= j0; j--) {
-                    ioff = 1;
-                    for (int ib = 1; ib <= nbdr; ib++) {
-                        joff = 1;
-                        for (int jb = 1; jb <= nbdr; jb++) {
-                            ij = ib > jb ? ib : jb;
-                            ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
-                            v[ip1] = v[ip1] + vbk[ij] * aux[ioff + i] * aux[joff + j];
-                            joff += n;
-                        }
-                        ioff += n;
-                    }
-                    ip1--;
-                }
-                ip1 -= j0;
-            }
-            ip1 = (nmb * nmb + nmb) / 2;
-            ip = 0;
-            for (int ib = 1; ib <= nbdr; ib++) {
-                for (int i = 1; i <= nmb; i++) {
-                    ip1++;
-                    v[ip1] = 0.0;
-                    joff = 0;
-                    for (int jb = 1; jb <= nbdr; jb++) {
-                        ij = ib > jb ? ib : jb;
-                        ij = (ij * ij - ij) / 2 + (ib > jb ? jb : ib);
-                        v[ip1] = v[ip1] - vbk[ij] * aux[i + joff];
-                        joff += n;
-                    }
-                }
-                for (int jb = 1; jb <= ib; jb++) { ip1++; ip++; v[ip1] = vbk[ip]; }
-            }
-        }
-    }
-}
 
 // ------------------------------------------------------------------------
 // shared-memory carve-up of one warp
@@ -541,8 +298,232 @@ struct BlockWalk {
     __device__ __forceinline__ int pair() const { return qa * (qa + 1) / 2 + qb; }
 };
 
-// Full inverse of the bordered band matrix factorised by s_sqmibb (called
-// with inv = 0), warp-parallel; the same matrix as s_sqmibb's inv = 2 path
+
+// ------------------------------------------------------------------------
+// Warp-cooperative sqmibb / sqmibb2 (mpnum.f90:3118-3600) with inv = 0
+// (solution, rank and
+// eigenvalue bounds; factors left in the band work areas).  Every element
+// receives the same operations in the same order as in the reference's
+// sequential routine, so the results are bit-identical to it; the lanes take the operations that are
+// independent: the updates of one column step of the band LDL^T, the
+// forward substitutions, the right-hand sides (border columns and b) of the
+// backward substitutions, the border Schur products and the final updates.
+#define WB2(r, c) w[((c) - 1) * mp1 + (r)]
+__device__ void w_dbcdec(double *w, int mp1, int n, double *aux, double *rx) {
+    const int ln = lane_id();
+    for (int i = 1 + ln; i <= n; i += 32) aux[i] = 16.0 * WB2(1, i);
+    __syncwarp();
+    for (int i = 1; i <= n; i++) {
+        const int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+        if (ln == 0) {
+            if (WB2(1, i) + aux[i] != aux[i]) WB2(1, i) = 1.0 / WB2(1, i);
+            else WB2(1, i) = 0.0;
+        }
+        __syncwarp();
+        const double piv = WB2(1, i);
+        for (int j = 1 + ln; j <= mj; j += 32) rx[j] = WB2(j + 1, i) * piv;
+        __syncwarp();
+        // pair (j, k), k = 1..mj+1-j, updates WB(k, i+j) from column i
+        const int npair = mj * (mj + 1) / 2;
+        for (int q = ln; q < npair; q += 32) {
+            int j = 1, rem = q, cnt = mj;
+            while (rem >= cnt) { rem -= cnt; cnt--; j++; }
+            const int k = rem + 1;
+            WB2(k, i + j) = WB2(k, i + j) - WB2(k + j, i) * rx[j];
+        }
+        __syncwarp();
+        for (int j = 1 + ln; j <= mj; j += 32) WB2(j + 1, i) = rx[j];
+        __syncwarp();
+    }
+}
+
+// nrhs right-hand sides: r < nrhs - extra from inBase + r * stride into
+// outBase + r * stride, and (extra = 1) one more from bIn into bOut;
+// x = b, then the forward and backward substitutions of s_dbcslv
+__device__ void w_dbcslv_multi(const double *w, int mp1, int n, int nrhs, int extra, const double *inBase,
+                               double *outBase, int64_t stride, const double *bIn, double *bOut) {
+    const int ln = lane_id();
+    const int nb = nrhs - extra;
+    auto in_of = [&](int r) { return r < nb ? inBase + r * stride : bIn; };
+    auto out_of = [&](int r) { return r < nb ? outBase + r * stride : bOut; };
+    for (int q = ln; q < nrhs * n; q += 32) {
+        const int r = q / n, i = 1 + q % n;
+        out_of(r)[i] = in_of(r)[i];
+    }
+    __syncwarp();
+    for (int i = 1; i <= n; i++) {
+        const int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+        for (int q = ln; q < nrhs * mj; q += 32) {
+            const int r = q / mj, j = 1 + q % mj;
+            double *x = out_of(r);
+            x[j + i] = x[j + i] - WB2(j + 1, i) * x[i];
+        }
+        __syncwarp();
+    }
+    for (int r = ln; r < nrhs; r += 32) {
+        double *x = out_of(r);
+        for (int i = n; i >= 1; i--) {
+            double rxw = x[i] * WB2(1, i);
+            const int mj = (mp1 - 1 < n - i) ? mp1 - 1 : n - i;
+            for (int j = 1; j <= mj; j++) rxw = rxw - WB2(j + 1, i) * x[j + i];
+            x[i] = rxw;
+        }
+    }
+    __syncwarp();
+}
+#undef WB2
+
+__device__ void w_sqmibb0(int side, double *v, double *b, int n, int nbdr, int nbnd, int *nrank, double *evdmin,
+                          double *evdmax, const BandWork &wk) {
+    const int ln = lane_id();
+    double *vbnd = wk.vbnd, *vbdr = wk.vbdr, *aux = wk.aux, *vbk = wk.vbk, *vzru = wk.vzru;
+    const int mp1 = nbnd + 1, nmb = n - nbdr;
+    if (side == 1) {
+        const int nb1 = nbdr + 1;
+        for (int q = ln; q < nmb * mp1; q += 32) {
+            const int i = nb1 + q / mp1, d = q % mp1, j = i + d;
+            if (j <= n) vbnd[d + 1 + (i - nb1) * mp1] = v[(j * j - j) / 2 + i];
+        }
+        for (int q = ln; q < nbdr * n; q += 32) {
+            const int i = 1 + q / n, j = 1 + q % n;
+            if (j >= i) vbdr[(i - 1) * n + j] = v[(j * j - j) / 2 + i];
+        }
+    } else {
+        const int nb1 = nmb + 1;
+        for (int q = ln; q < nmb * mp1; q += 32) {
+            const int i = 1 + q / mp1, d = q % mp1, j = i + d;
+            if (j <= nmb) vbnd[d + 1 + (i - 1) * mp1] = v[(j * j - j) / 2 + i];
+        }
+        for (int q = ln; q < nbdr * n; q += 32) {
+            const int i = nb1 + q / n, j = 1 + q % n;
+            if (j <= i) vbdr[(i - nb1) * n + j] = v[(i * i - i) / 2 + j];
+        }
+    }
+    __syncwarp();
+    w_dbcdec(vbnd, mp1, nmb, aux, wk.scdiag);
+    // pivots: all positive, else rank 0 and everything zeroed
+    int bad = 0;
+    double lo = 0.0, hi = 0.0;
+    for (int i = 1 + ln; i <= nmb; i += 32) {
+        const double d = vbnd[(i - 1) * mp1 + 1];
+        if (d <= 0.0) bad = 1;
+        if (i == 1 + ln) { lo = d; hi = d; }
+        else { if (d < lo) lo = d; if (d > hi) hi = d; }
+    }
+    const bool any = nmb > 0;
+    const bool have = 1 + ln <= nmb;
+    // exact min / max over the lanes that hold pivots
+    double mn = 0.0, mx = 0.0;
+    {
+        double l0 = have ? lo : 1.0e308, h0 = have ? hi : -1.0e308;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double a = __shfl_xor_sync(0xffffffffu, l0, o), c = __shfl_xor_sync(0xffffffffu, h0, o);
+            l0 = a < l0 ? a : l0;
+            h0 = c > h0 ? c : h0;
+        }
+        mn = any ? l0 : 0.0;
+        mx = any ? h0 : 0.0;
+    }
+    if (__any_sync(0xffffffffu, bad)) {
+        for (int q = 1 + ln; q <= n; q += 32) b[q] = 0.0;
+        for (int q = 1 + ln; q <= (n * n + n) / 2; q += 32) v[q] = 0.0;
+        __syncwarp();
+        *nrank = 0;
+        *evdmin = 0.0;
+        *evdmax = 0.0;
+        return;
+    }
+    *nrank = nmb;
+    *evdmin = mn;
+    *evdmax = mx;
+    if (nbdr == 0) {
+        w_dbcslv_multi(vbnd, mp1, nmb, 1, 1, nullptr, nullptr, 0, b, b);
+        return;
+    }
+    double *xb = wk.scdiag;   // solution of the band part of b (b itself is still needed)
+    int nrankb = 0;
+    if (side == 1) {
+        const int nb1 = nbdr + 1;
+        w_dbcslv_multi(vbnd, mp1, nmb, nbdr + 1, 1, vbdr + nb1 - 1, aux + nb1 - 1, n, b + nb1 - 1, xb);
+        for (int ib = 1 + ln; ib <= nbdr; ib += 32) {
+            const int ioff = nb1 + (ib - 1) * n;
+            double z = b[ib];
+            for (int i = 0; i <= nmb - 1; i++) z = z - b[nb1 + i] * aux[ioff + i];
+            vzru[ib] = z;
+        }
+        __syncwarp();
+        for (int i = 1 + ln; i <= nmb; i += 32) b[nb1 + i - 1] = xb[i];
+        const int np = nbdr * (nbdr + 1) / 2;
+        for (int q = ln; q < np; q += 32) {
+            int ib = 1, rem = q;
+            while (rem >= ib) { rem -= ib; ib++; }
+            const int jb = rem + 1, ip = q + 1;
+            const int ioff = nb1 + (ib - 1) * n, joff = nb1 + (jb - 1) * n;
+            double t = v[ip];
+            for (int i = 0; i <= nmb - 1; i++) t = t - vbdr[ioff + i] * aux[joff + i];
+            vbk[ip] = t;
+        }
+        __syncwarp();
+        if (ln == 0) s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
+        nrankb = __shfl_sync(0xffffffffu, nrankb, 0);
+        __syncwarp();
+        if (nrankb == nbdr) *nrank += nbdr;
+        else {
+            for (int ib = 1 + ln; ib <= nbdr; ib += 32) vzru[ib] = 0.0;
+            for (int q = 1 + ln; q <= (nbdr * nbdr + nbdr) / 2; q += 32) vbk[q] = 0.0;
+        }
+        __syncwarp();
+        for (int ib = 1 + ln; ib <= nbdr; ib += 32) b[ib] = vzru[ib];
+        __syncwarp();
+        for (int i = ln; i <= nmb - 1; i += 32) {
+            double t = b[nb1 + i];
+            for (int ib = 1; ib <= nbdr; ib++) t = t - b[ib] * aux[nb1 + (ib - 1) * n + i];
+            b[nb1 + i] = t;
+        }
+        __syncwarp();
+    } else {
+        w_dbcslv_multi(vbnd, mp1, nmb, nbdr + 1, 1, vbdr, aux, n, b, xb);
+        for (int ib = 1 + ln; ib <= nbdr; ib += 32) {
+            const int ioff = (ib - 1) * n;
+            double z = b[nmb + ib];
+            for (int i = 1; i <= nmb; i++) z = z - b[i] * aux[ioff + i];
+            vzru[ib] = z;
+        }
+        __syncwarp();
+        for (int i = 1 + ln; i <= nmb; i += 32) b[i] = xb[i];
+        const int np = nbdr * (nbdr + 1) / 2;
+        for (int q = ln; q < np; q += 32) {
+            int ib = 1, rem = q;
+            while (rem >= ib) { rem -= ib; ib++; }
+            const int jb = rem + 1, ip = q + 1;
+            const int ioff = (ib - 1) * n, joff = (jb - 1) * n, koff = nmb + (ib - 1) * n;
+            double t = vbdr[koff + jb];
+            for (int i = 1; i <= nmb; i++) t = t - vbdr[ioff + i] * aux[joff + i];
+            vbk[ip] = t;
+        }
+        __syncwarp();
+        if (ln == 0) s_sqminv(vbk, vzru, nbdr, &nrankb, wk.scdiag, wk.scflag);
+        nrankb = __shfl_sync(0xffffffffu, nrankb, 0);
+        __syncwarp();
+        if (nrankb == nbdr) *nrank += nbdr;
+        else {
+            for (int ib = 1 + ln; ib <= nbdr; ib += 32) vzru[ib] = 0.0;
+            for (int q = 1 + ln; q <= (nbdr * nbdr + nbdr) / 2; q += 32) vbk[q] = 0.0;
+        }
+        __syncwarp();
+        for (int i = 1 + ln; i <= nmb; i += 32) {
+            double t = b[i];
+            for (int ib = 1; ib <= nbdr; ib++) t = t - vzru[ib] * aux[(ib - 1) * n + i];
+            b[i] = t;
+        }
+        for (int ib = 1 + ln; ib <= nbdr; ib += 32) b[nmb + ib] = vzru[ib];
+        __syncwarp();
+    }
+}
+
+// Full inverse of the bordered band matrix factorised by w_sqmibb0,
+// warp-parallel; the same matrix as sqmibb's inv = 2 path
 // (dbcinv plus the border terms, mpnum.f90:3118-3600) up to rounding.  The
 // inverse enters only the Schur complement, not the fit decisions.
 // (1) lane per column c: band inverse column by (L D L^T) x = e_c with the
@@ -636,7 +617,7 @@ __device__ __forceinline__ BandWork band_work(const WarpMem &m, const RecInfo &r
 }
 
 template <bool BIG>
-__global__ void __launch_bounds__(32 * MPG_WARPS_FIT)
+__global__ void __launch_bounds__(32 * MPG_WARPS_FIT, 2)
 k_fit(FitParams p, int perWarp) {
     extern __shared__ __align__(16) char smem[];
     const int ln = lane_id();
@@ -786,21 +767,17 @@ k_fit(FitParams p, int perWarp) {
                 }
                 // ---- local solve
                 if (band) {
+                    // the solution and the factors (the arithmetic of the
+                    // decisions, bit-identical to the one-lane form); the
+                    // inverse, needed for the update only, is formed
+                    // warp-parallel after the iterations
                     double evdmin = 0.0, evdmax = 0.0;
                     int nr = 0;
-                    if (ln == 0) {
-                        // the solution and the factors on one lane (the arithmetic of
-                        // the decisions); the inverse, needed for the update only, is
-                        // formed warp-parallel after the iterations
-                        const BandWork wk = band_work(m, ri, nalc);
-                        s_sqmibb(ri.mside & 0xff, m.clmat - 1, m.blvec - 1, nalc, ri.mbdr, ri.mbnd, 0, &nr,
-                                 &evdmin, &evdmax, const_cast<BandWork &>(wk));
-                        if (evdmin > 0.0) cndl10 = log10f((float)(evdmax / evdmin));
-                        else cndl10 = 0.0f;
-                    }
-                    __syncwarp();
-                    nrank = __shfl_sync(0xffffffffu, nr, 0);
-                    cndl10 = __shfl_sync(0xffffffffu, cndl10, 0);
+                    const BandWork wk = band_work(m, ri, nalc);
+                    w_sqmibb0(ri.mside & 0xff, m.clmat - 1, m.blvec - 1, nalc, ri.mbdr, ri.mbnd, &nr, &evdmin,
+                              &evdmax, wk);
+                    cndl10 = evdmin > 0.0 ? log10f((float)(evdmax / evdmin)) : 0.0f;
+                    nrank = nr;
                 } else {
                     cndl10 = 0.0f;
                     warp_sqminv(m.clmat, m.blvec, nalc, &nrank, m.diag, m.ocol, m.scol, m.used);
@@ -945,16 +922,30 @@ k_fit(FitParams p, int perWarp) {
                                    X + 32 * (int64_t)p.nalcmax);
                 }
                 if (p.icalcm == 1) {
-                    // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432)
+                    // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432):
+                    // eight k at a time, each c_ik summed over l = 1..nalc in
+                    // order, every B(l, s) loaded once per eight products
+                    constexpr int KB = 8;
                     for (int s = ln; s < nalg; s += 32) {
-                        for (int k = 1; k <= nalc; ++k) {
-                            double cik = 0.0;
-                            const int lkl = (k * k - k) / 2;
-                            for (int l = 1; l <= k; ++l)
-                                cik = __fma_rn(mB[(l - 1) * nalg + s], m.clmat[lkl + l - 1], cik);
-                            for (int l = k + 1; l <= nalc; ++l)
-                                cik = __fma_rn(mB[(l - 1) * nalg + s], m.clmat[(l * l - l) / 2 + k - 1], cik);
-                            mW[s * nalc + k - 1] = cik;
+                        for (int k0 = 1; k0 <= nalc; k0 += KB) {
+                            double cik[KB];
+#pragma unroll
+                            for (int t = 0; t < KB; ++t) cik[t] = 0.0;
+                            for (int l = 1; l <= nalc; ++l) {
+                                const double bl = mB[(l - 1) * nalg + s];
+                                const int ll = (l * l - l) / 2;
+#pragma unroll
+                                for (int t = 0; t < KB; ++t) {
+                                    const int k = k0 + t;
+                                    if (k > nalc) break;
+                                    // Gamma^-1(l, k) of the packed lower triangle
+                                    const double g = l <= k ? m.clmat[(k * k - k) / 2 + l - 1] : m.clmat[ll + k - 1];
+                                    cik[t] = __fma_rn(bl, g, cik[t]);
+                                }
+                            }
+#pragma unroll
+                            for (int t = 0; t < KB; ++t)
+                                if (k0 + t <= nalc) mW[s * nalc + k0 + t - 1] = cik[t];
                         }
                     }
                     __syncwarp();
