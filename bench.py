@@ -323,6 +323,33 @@ def structure_measure(mp, S, pinned, device, host_s, ncores):
             "speedup": host_s / statistics.median(times), "tables_identical": same}
 
 
+def profile_part(mp, part, ntracks, device, steps):
+    """One part of the path on a small case, for profilers: the record
+    upload (barrel), the device structure passes (barrel) or the data loop
+    of broken-line records (size classes, no tuning).  Each repeats `steps`
+    times after one untimed pass."""
+    kind = "brokenlines" if part == "brokenlines" else "barrel"
+    d = mp.generate(mp.gen_config(kind, ntracks=ntracks, seed=3 if kind == "brokenlines" else 2))
+    flags = mp.FLAG_NO_AUTOTUNE if part == "brokenlines" else 0
+    out = {"part": part, "records": ntracks, "ms": []}
+    with mp.Context(device=device, flags=flags) as ctx:
+        if part == "structure":
+            for k in range(steps + 1):
+                t0 = time.perf_counter()
+                mp.DeviceStructure(ctx, d, mreqenf=25)
+                out["ms"].append(1e3 * (time.perf_counter() - t0))
+        else:
+            H = mp.HostStructure(d, mreqenf=25)
+            ctx.set_layout(H, 2)
+            for k in range(steps + 1):
+                ctx.upload(H)
+                if part == "upload":
+                    out["ms"].append(ctx.upload_timing()[1])
+                else:
+                    out["ms"].append(ctx.loopbf(np.zeros(H.nTotal))["msLoop"])
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -336,11 +363,16 @@ def main():
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
+    ap.add_argument("--part", default="loop", choices=["loop", "upload", "structure", "brokenlines"],
+                    help="with --profile: the part to run on --ntracks records (for profilers)")
     ap.add_argument("--brokenlines", type=int, default=200_000,
                     help="records of the uneven-record (broken-line) measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)
     mp = _load_pkg()
+    if args.profile and args.part != "loop":
+        profile_part(mp, args.part, args.ntracks, local, args.steps)
+        return
     cfg = mp.gen_config("barrel", ntracks=args.ntracks, seed=2 + 1000 * rank)
     t0 = time.time()
     d = mp.generate(cfg)
