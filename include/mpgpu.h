@@ -211,8 +211,13 @@ typedef struct mpgpu_solveinfo {
     double msRefine;    /* dense solves: device time of the CG refinement */
 } mpgpu_solveinfo;
 
-/* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES)
- * of the matrix built by the last mpgpu_loopbf plus mupdat calls.
+/* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES,
+ * 5 MINRES-QLP) of the matrix built by the last mpgpu_loopbf plus mupdat
+ * calls.  MINRES-QLP (mminrsqlp, pede.f90 method 5) takes QLP steps from
+ * the first iteration (pede's mrmode 2) with maxxnorm = nfit / sqrt(eps);
+ * info->istop 1 residual test, 2 least-squares test, 4 condition limit,
+ * 5 iterate longer than maxxnorm (the previous one is returned), 6
+ * iteration limit.
  * Decomposition also in blocked dense form (no counterpart in the
  * reference, same solution): metsol 32 FP64 blocked Cholesky, metsol 31
  * Cholesky with tensor-core 3xTF32 trailing updates; both refine the
@@ -222,7 +227,7 @@ typedef struct mpgpu_solveinfo {
  * relative residual).
  * consResiduals[ncon] = d - C p (addcst); correction[nVar] receives the
  * step; errors[nVar] (metsol 1, may be NULL) the diagonal of the covariance
- * (sqrt gives the parameter errors).  rtol/itnlim: MINRES tolerance and
+ * (sqrt gives the parameter errors).  rtol/itnlim: MINRES(-QLP) tolerance and
  * iteration limit.  The matrix is consumed (factorised in place). */
 int32_t mpgpu_solve(mpgpu_ctx *ctx, int32_t metsol, const double *consResiduals,
                     double rtol, int32_t itnlim, double *correction, double *errors,
@@ -260,7 +265,7 @@ int32_t mpgpu_avprod(mpgpu_ctx *ctx, int32_t n, const double *x, double *b);
  * sparse structure, iteration control and millepede.res.
  * ---------------------------------------------------------------- */
 typedef struct mpgpu_steer {
-    int32_t metsol;     /* 1 inversion, 3 decomposition, 4 MINRES */
+    int32_t metsol;     /* 1 inversion, 3 decomposition, 4 MINRES, 5 MINRES-QLP, 31/32 dense */
     int32_t matsto;     /* 1 packed, 2 sparse */
     int32_t mitera;     /* number of iterations (solutions) */
     int32_t lhuber;     /* outlierdownweighting */

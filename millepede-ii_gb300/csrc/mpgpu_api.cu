@@ -722,7 +722,8 @@ extern "C" int32_t mpgpu_solve(mpgpu_ctx *c, int32_t metsol, const double *consR
         const int dense = metsol == 31 ? 1 : (metsol == 32 ? 0 : -1);
         return solve_inversion(c, consResiduals, correction, errors, info, metsol != 1, dense, rtol, itnlim);
     }
-    if (metsol == 4) return solve_minres(c, consResiduals, rtol, itnlim, correction, info);
+    if (metsol == 4 || metsol == 5)
+        return solve_minres(c, consResiduals, rtol, itnlim, correction, info, metsol == 5);
     return set_err(c, MPGPU_ERR_ARG, "unsupported solution method");
 }
 

@@ -338,7 +338,7 @@ int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, f
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
                         int32_t itnlim, mpgpu_solveinfo *info);
 int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
-                     double *corr, mpgpu_solveinfo *info);
+                     double *corr, mpgpu_solveinfo *info, bool qlp = false);
 int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b);
 
 // record preparation on the device (mpgpu_upload.cu)

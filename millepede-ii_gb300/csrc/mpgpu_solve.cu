@@ -516,6 +516,137 @@ __global__ void k_mr_test(MinresState *S) {
     if (istop) { S->istop = istop; S->done = 1; }
 }
 
+// MINRES-QLP (Choi, Paige & Saunders 2011; minresqlpModule.f90:411-1333 in
+// the reference): the Lanczos scalars of MinresState plus the rows of the
+// lower-triangular L = R P not yet final, the final u values and the
+// rotations of the current iteration for the vector kernel
+struct QlpState {
+    double etaA, thA, gA, tauA, etaB, thB, gB, tauB, uF1, uF2;
+    double c1, s1, c2, s2, uA, uB, uC;
+    int k, commit;
+};
+
+__device__ __forceinline__ void d_sym_ortho(double a, double b, double *c, double *s, double *r) {
+    *r = sqrt(a * a + b * b);
+    if (*r == 0.0) { *c = 1.0; *s = 0.0; return; }
+    *c = a / *r;
+    *s = b / *r;
+}
+
+__global__ void k_qlp_init(QlpState *Q) {
+    if (threadIdx.x) return;
+    memset(Q, 0, sizeof(QlpState));
+}
+
+// beta_{k+1}, the left reflection (column k of R, tau_k), the right
+// reflections P(k-2,k), P(k-1,k) and u; the same arithmetic as the oracle
+__global__ void k_qlp_rot(MinresState *S, QlpState *Q) {
+    if (threadIdx.x || S->done) return;
+    double b2 = S->dotv;
+    if (b2 < 0.0) { S->istop = 9; S->done = 1; return; }
+    const int k = S->itn + 1;
+    Q->k = k;
+    S->oldb = S->beta;
+    S->beta = sqrt(b2);
+    S->tnorm2 += S->alfa * S->alfa + S->oldb * S->oldb + S->beta * S->beta;
+    S->Anorm = sqrt(S->tnorm2);
+    const double epsk = S->epsln;
+    const double delta = S->cs * S->dbar + S->sn * S->alfa;
+    const double gbar = S->sn * S->dbar - S->cs * S->alfa;
+    S->epsln = S->sn * S->beta;
+    S->dbar = -S->cs * S->beta;
+    S->root = sqrt(gbar * gbar + S->dbar * S->dbar);
+    double cs, sn, gamma;
+    d_sym_ortho(gbar, S->beta, &cs, &sn, &gamma);
+    S->cs = cs;
+    S->sn = sn;
+    const double tau = cs * S->phibar;
+    S->phibar = sn * S->phibar;
+    S->gmax = fmax(S->gmax, gamma);
+    S->gmin = fmin(S->gmin, gamma);
+    double c1 = 1, s1 = 0, c2 = 1, s2 = 0, etaC = 0, thC = 0, gC, dk = delta, gk = gamma;
+    if (k >= 3) {
+        double r;
+        d_sym_ortho(Q->gA, epsk, &c1, &s1, &r);
+        Q->gA = r;
+        const double th = c1 * Q->thB + s1 * dk;
+        dk = s1 * Q->thB - c1 * dk;
+        Q->thB = th;
+        etaC = s1 * gk;
+        gk = -c1 * gk;
+    }
+    if (k >= 2) {
+        double r;
+        d_sym_ortho(Q->gB, dk, &c2, &s2, &r);
+        Q->gB = r;
+        thC = s2 * gk;
+        gC = -c2 * gk;
+    } else {
+        gC = gk;
+    }
+    const double tiny = 2.220446049250313e-16 * S->Anorm;
+    double uA = 0.0, uB = 0.0, uC;
+    if (k >= 3) uA = fabs(Q->gA) > tiny ? (Q->tauA - Q->etaA * Q->uF2 - Q->thA * Q->uF1) / Q->gA : 0.0;
+    if (k >= 2) uB = fabs(Q->gB) > tiny ? (Q->tauB - Q->etaB * Q->uF1 - Q->thB * uA) / Q->gB : 0.0;
+    uC = fabs(gC) > tiny ? (tau - etaC * uA - thC * uB) / gC : 0.0;
+    Q->c1 = c1; Q->s1 = s1; Q->c2 = c2; Q->s2 = s2;
+    Q->uA = uA; Q->uB = uB; Q->uC = uC;
+    if (k >= 3) { Q->uF2 = Q->uF1; Q->uF1 = uA; }
+    Q->etaA = Q->etaB; Q->thA = Q->thB; Q->gA = Q->gB; Q->tauA = Q->tauB;
+    Q->etaB = etaC; Q->thB = thC; Q->gB = gC; Q->tauB = tau;
+}
+
+// W = V P (w_{k-2} final into xp) and the candidate iterate xc
+__global__ void k_qlp_w(int32_t n, const MinresState *S, const QlpState *Q, const double *v, double *wa,
+                        double *wb, double *xp, double *xc) {
+    if (S->done) return;
+    const int k = Q->k;
+    const double c1 = Q->c1, s1 = Q->s1, c2 = Q->c2, s2 = Q->s2, uA = Q->uA, uB = Q->uB, uC = Q->uC;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a = wa[i], bb = wb[i], c = v[i];
+        if (k >= 3) {
+            const double a2 = c1 * a + s1 * c;
+            c = s1 * a - c1 * c;
+            a = a2;
+            xp[i] = xp[i] + uA * a;
+        }
+        if (k >= 2) {
+            const double b2 = c2 * bb + s2 * c;
+            c = s2 * bb - c2 * c;
+            bb = b2;
+        }
+        wa[i] = bb;
+        wb[i] = c;
+        xc[i] = xp[i] + uB * bb + uC * c;
+    }
+}
+
+__global__ void k_qlp_test(MinresState *S, QlpState *Q, double maxxnorm) {
+    if (threadIdx.x || S->done) return;
+    Q->commit = 0;
+    const double xnorm = sqrt(S->dotv);
+    if (xnorm > maxxnorm) { S->istop = 5; S->done = 1; S->itn += 1; return; }
+    Q->commit = 1;
+    S->itn += 1;
+    S->ynorm = xnorm;
+    S->rnorm = S->phibar;
+    const double test1 = S->rnorm / (S->Anorm * xnorm);
+    const double test2 = S->root / S->Anorm;
+    const double Acond = S->gmax / S->gmin;
+    int istop = 0;
+    if (S->itn >= S->itnlim) istop = 6;
+    if (Acond >= 0.1 / 2.220446049250313e-16) istop = 4;
+    if (test2 <= S->rtol) istop = 2;
+    if (test1 <= S->rtol) istop = 1;
+    if (istop) { S->istop = istop; S->done = 1; }
+}
+
+__global__ void k_qlp_commit(int32_t n, const QlpState *Q, const double *xc, double *x) {
+    if (!Q->commit) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] = xc[i];
+}
+
 __global__ void k_copy_pad(int32_t n, int32_t ntot, const double *x, double *xa) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * blockDim.x)
         xa[i] = i < n ? x[i] : 0.0;
@@ -822,9 +953,12 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
 
 // ---------------------------------------------------------------- MINRES
 // mminrs (pede.f90:8243-8333) with the diagonal preconditioner of the
-// QL-reduced matrix and MINRES (Paige & Saunders 1975) kept on the device.
+// QL-reduced matrix and MINRES (Paige & Saunders 1975) kept on the device;
+// with qlp, MINRES-QLP on the same Lanczos process (mminrsqlp, the method's
+// QLP steps from the first iteration, maxxnorm = nfit / sqrt(eps) as
+// pede.f90:626 sets it).
 int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int32_t itnlim,
-                     double *corrOut, mpgpu_solveinfo *info) {
+                     double *corrOut, mpgpu_solveinfo *info, bool qlp) {
     Solver S(c);
     DevJob &j = c->j;
     cudaStream_t s = c->stream;
@@ -844,8 +978,12 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     double *rhs = vec(n), *xa = vec(n), *ba = vec(n), *dg = vec(n), *cu = vec(n), *tmp = vec(n), *yk = vec(n);
     double *r1 = vec(n), *r2 = vec(n), *y = vec(n), *v = vec(n), *w = vec(n), *w1 = vec(n), *w2 = vec(n);
     double *x = vec(n);
+    double *wa = nullptr, *wb = nullptr, *xp = nullptr, *xc = nullptr;
+    if (qlp) { wa = vec(n); wb = vec(n); xp = vec(n); xc = vec(n); }
     MinresState *St = nullptr;
+    QlpState *Qs = nullptr;
     MPG_CUDA(c, cudaMalloc(&St, sizeof(MinresState)));
+    if (qlp) MPG_CUDA(c, cudaMalloc(&Qs, sizeof(QlpState)));
     for (double *p : bufs)
         if (!p) return set_err(c, MPGPU_ERR_ALLOC, "MINRES workspace");
     cudaEvent_t e0, e1;
@@ -896,6 +1034,13 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     k_apply_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, r1, cu, y);
     dot(r1, y, nfit, S.part, &St->dotv, s);
     k_mr_init<<<1, 32, 0, s>>>(St, rtol, itnlim);
+    const double maxxnorm = (double)nfit / sqrt(2.220446049250313e-16);
+    if (qlp) {
+        k_qlp_init<<<1, 32, 0, s>>>(Qs);
+        MPG_CUDA(c, cudaMemsetAsync(wa, 0, sizeof(double) * n, s));
+        MPG_CUDA(c, cudaMemsetAsync(wb, 0, sizeof(double) * n, s));
+        MPG_CUDA(c, cudaMemsetAsync(xp, 0, sizeof(double) * n, s));
+    }
     MinresState hs;
     int it = 0;
     const int batch = 16;
@@ -913,10 +1058,18 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
             k_mr_alfa<<<1, 32, 0, s>>>(St);
             k_mr_y2<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, r1, r2, cu);
             dot(r2, y, nfit, S.part, &St->dotv, s);
-            k_mr_rot<<<1, 32, 0, s>>>(St);
-            k_mr_w<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, v, w, w1, w2, x);
-            dot(x, x, nfit, S.part, &St->dotv, s);
-            k_mr_test<<<1, 32, 0, s>>>(St);
+            if (!qlp) {
+                k_mr_rot<<<1, 32, 0, s>>>(St);
+                k_mr_w<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, v, w, w1, w2, x);
+                dot(x, x, nfit, S.part, &St->dotv, s);
+                k_mr_test<<<1, 32, 0, s>>>(St);
+            } else {
+                k_qlp_rot<<<1, 32, 0, s>>>(St, Qs);
+                k_qlp_w<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, Qs, v, wa, wb, xp, xc);
+                dot(xc, xc, nfit, S.part, &St->dotv, s);
+                k_qlp_test<<<1, 32, 0, s>>>(St, Qs, maxxnorm);
+                k_qlp_commit<<<S.grid(nfit), kThreads, 0, s>>>(nfit, Qs, xc, x);
+            }
         }
         it += batch;
         MPG_CUDA(c, cudaMemcpyAsync(&hs, St, sizeof(MinresState), cudaMemcpyDeviceToHost, s));
@@ -939,6 +1092,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     cudaEventDestroy(e1);
     for (double *p : bufs) cudaFree(p);
     cudaFree(St);
+    if (Qs) cudaFree(Qs);
     return MPGPU_OK;
 }
 

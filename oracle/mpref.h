@@ -202,6 +202,15 @@ int32_t mpref_minres_sparse(int32_t matsto, int32_t nVar, int32_t nG,
                             const mpref_ql *q, const double *rhs, double *x,
                             double rtol, int32_t itnlim, int32_t *itn);
 
+/* MINRES-QLP (the published method; the reference vendors
+ * minresqlpModule.f90:411-1333) on the same preconditioned reduced system:
+ * minimum-length solution of singular systems.  Returns istop. */
+int32_t mpref_minresqlp_sparse(int32_t matsto, int32_t nVar, int32_t nG,
+                               const int32_t *allIndexGroups, const int64_t *offsets,
+                               const int32_t *columns, const double *matD,
+                               const mpref_ql *q, const double *rhs, double *x,
+                               double rtol, int32_t itnlim, int32_t *itn);
+
 /* ---------------------------------------------------------------------
  * Whole job (xloopn/loopn/addcst control without line search) and
  * millepede.res writer (prtglo, pede.f90:4477-4651).

@@ -243,7 +243,7 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
                 for (int64_t r = 1; r <= nVar; r++) err[r - 1] = matD[(r * r - r) / 2 + r - 1];
                 haveErr = 1;
             }
-        } else if (st->metsol == 4) {
+        } else if (st->metsol == 4 || st->metsol == 5) {
             double *rhs = (double *)malloc(sizeof(double) * (size_t)nVar);
             for (i = 0; i < nVar; i++) rhs[i] = corr[i];
             if (ncon > 0) {
@@ -259,9 +259,11 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
                 free(bav);
             }
             int32_t itn = 0;
-            res->minresIstop = mpref_minres_sparse(st->matsto, nVar, nG, aig, offsets, columns,
-                                                   matD, q, rhs, corr, st->mrestl, st->itnlim,
-                                                   &itn);
+            res->minresIstop = st->metsol == 4
+                ? mpref_minres_sparse(st->matsto, nVar, nG, aig, offsets, columns, matD, q, rhs, corr,
+                                      st->mrestl, st->itnlim, &itn)
+                : mpref_minresqlp_sparse(st->matsto, nVar, nG, aig, offsets, columns, matD, q, rhs,
+                                         corr, st->mrestl, st->itnlim, &itn);
             res->minresItn = itn;
             if (ncon > 0) {
                 for (j = 0; j < ncon; j++) corr[nfit + j] = csol[j];

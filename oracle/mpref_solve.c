@@ -555,6 +555,185 @@ out:
     return istop;
 }
 
+/* MINRES-QLP (Choi, Paige & Saunders, SIAM J. Sci. Comput. 33 (2011)
+ * 1810-1836; the reference vendors it as minresqlpModule.f90:411-1333),
+ * restated from the method: the preconditioned Lanczos process and the left
+ * reflections of MINRES give the upper-triangular R_k (column k: eps_k in
+ * row k-2, delta_k in row k-1, gamma_k in row k) and the right-hand side
+ * tau_k; two right reflections per iteration (columns k-2,k then k-1,k) turn
+ * R_k into the lower-triangular L_k = R_k P_k (diagonal g, sub-diagonals
+ * theta and eta).  With L u = tau and W = V P, x_k = W u: the first k-2
+ * components of u and columns of W are final and accumulate in xp, the
+ * last two are recomputed each iteration.  A diagonal of L at the rounding
+ * level of |T| gives a zero component, which leaves the minimum-length
+ * solution of a singular system.  An iterate longer than maxxnorm is not
+ * taken (x keeps the previous one).  QLP steps are taken from the first
+ * iteration (the reference's mode 2; in exact arithmetic the iterates equal
+ * those of MINRES where the system is nonsingular).  istop: 1 residual
+ * test, 2 least-squares test, 4 condition limit, 5 |x| above maxxnorm,
+ * 6 iteration limit, 9 indefinite preconditioner. */
+static void sym_ortho(double a, double b, double *c, double *s, double *r)
+{
+    *r = sqrt(a * a + b * b);
+    if (*r == 0.0) { *c = 1.0; *s = 0.0; return; }
+    *c = a / *r;
+    *s = b / *r;
+}
+
+static int32_t minresqlp(const redop *o, const double *pc, const double *b, double *x,
+                         double rtol, int32_t itnlim, double maxxnorm, int32_t *itnout)
+{
+    int32_t n = o->nfit, i, itn = 0, istop = 0;
+    double *r1 = calloc((size_t)n, sizeof(double)), *r2 = calloc((size_t)n, sizeof(double));
+    double *y = calloc((size_t)n, sizeof(double)), *v = calloc((size_t)n, sizeof(double));
+    double *wa = calloc((size_t)n, sizeof(double)), *wb = calloc((size_t)n, sizeof(double));
+    double *xp = calloc((size_t)n, sizeof(double)), *xc = calloc((size_t)n, sizeof(double));
+    const double eps = DBL_EPSILON;
+    double beta1, beta, oldb, alfa, dbar = 0, epsln = 0, epsk, delta, gbar, root;
+    double gamma, cs = -1, sn = 0, tau, phibar, tnorm2 = 0, gmax = 0, gmin = DBL_MAX;
+    double Anorm = 0, xnorm, test1, test2, Acond;
+    /* rows k-2 (A) and k-1 (B) of L: eta, theta, diagonal, tau */
+    double etaA = 0, thA = 0, gA = 0, tauA = 0, etaB = 0, thB = 0, gB = 0, tauB = 0;
+    double uF1 = 0, uF2 = 0;   /* final u_{k-3}, u_{k-4} */
+    for (i = 0; i < n; i++) { x[i] = 0.0; r1[i] = b[i]; }
+    for (i = 0; i < n; i++) y[i] = (r1[i] * pc[i]) * pc[i];
+    beta1 = 0.0;
+    for (i = 0; i < n; i++) beta1 += r1[i] * y[i];
+    if (beta1 <= 0.0) { *itnout = 0; istop = beta1 < 0.0 ? 9 : 0; goto out; }
+    beta1 = sqrt(beta1);
+    beta = beta1;
+    oldb = 0.0;
+    phibar = beta1;
+    for (i = 0; i < n; i++) r2[i] = r1[i];
+    while (itn < itnlim) {
+        itn++;
+        /* Lanczos step (as MINRES) */
+        double s = 1.0 / beta;
+        for (i = 0; i < n; i++) v[i] = s * y[i];
+        avprod(o, v, y);
+        if (itn >= 2)
+            for (i = 0; i < n; i++) y[i] = y[i] - (beta / oldb) * r1[i];
+        alfa = 0.0;
+        for (i = 0; i < n; i++) alfa += v[i] * y[i];
+        for (i = 0; i < n; i++) y[i] = y[i] - (alfa / beta) * r2[i];
+        for (i = 0; i < n; i++) { r1[i] = r2[i]; r2[i] = y[i]; }
+        for (i = 0; i < n; i++) y[i] = (r2[i] * pc[i]) * pc[i];
+        oldb = beta;
+        beta = 0.0;
+        for (i = 0; i < n; i++) beta += r2[i] * y[i];
+        if (beta < 0.0) { istop = 9; break; }
+        beta = sqrt(beta);
+        tnorm2 += alfa * alfa + oldb * oldb + beta * beta;
+        Anorm = sqrt(tnorm2);
+        /* left reflection: column k of R and tau_k */
+        epsk = epsln;
+        delta = cs * dbar + sn * alfa;
+        gbar = sn * dbar - cs * alfa;
+        epsln = sn * beta;
+        dbar = -cs * beta;
+        root = sqrt(gbar * gbar + dbar * dbar);
+        sym_ortho(gbar, beta, &cs, &sn, &gamma);
+        tau = cs * phibar;
+        phibar = sn * phibar;
+        if (gamma > gmax) gmax = gamma;
+        if (gamma < gmin) gmin = gamma;
+        /* right reflections: P(k-2,k) zeroes eps_k in row k-2, P(k-1,k)
+         * the updated delta in row k-1; row k gets eta, theta, g */
+        double c1 = 1, s1 = 0, c2 = 1, s2 = 0, etaC = 0, thC = 0, gC, dk = delta, gk = gamma;
+        if (itn >= 3) {
+            double r;
+            sym_ortho(gA, epsk, &c1, &s1, &r);
+            gA = r;
+            const double th = c1 * thB + s1 * dk;
+            dk = s1 * thB - c1 * dk;
+            thB = th;
+            etaC = s1 * gk;
+            gk = -c1 * gk;
+        }
+        if (itn >= 2) {
+            double r;
+            sym_ortho(gB, dk, &c2, &s2, &r);
+            gB = r;
+            thC = s2 * gk;
+            gC = -c2 * gk;
+        } else {
+            gC = gk;
+        }
+        /* u: row k-2 final, rows k-1 and k provisional */
+        const double tiny = eps * Anorm;
+        double uA = 0, uB, uC;
+        if (itn >= 3) {
+            uA = fabs(gA) > tiny ? (tauA - etaA * uF2 - thA * uF1) / gA : 0.0;
+        }
+        if (itn >= 2) uB = fabs(gB) > tiny ? (tauB - etaB * uF1 - thB * uA) / gB : 0.0;
+        else uB = 0.0;
+        uC = fabs(gC) > tiny ? (tau - etaC * uA - thC * uB) / gC : 0.0;
+        /* W = V P: w_{k-2} final (into xp), w_{k-1}, w_k provisional */
+        for (i = 0; i < n; i++) {
+            double a = wa[i], bb = wb[i], c = v[i];
+            if (itn >= 3) {
+                const double a2 = c1 * a + s1 * c;
+                c = s1 * a - c1 * c;
+                a = a2;
+                xp[i] = xp[i] + uA * a;
+            }
+            if (itn >= 2) {
+                const double b2 = c2 * bb + s2 * c;
+                c = s2 * bb - c2 * c;
+                bb = b2;
+            }
+            wa[i] = bb;
+            wb[i] = c;
+            xc[i] = xp[i] + uB * bb + uC * c;
+        }
+        /* shift the rows: B becomes A, row k becomes B */
+        if (itn >= 3) { uF2 = uF1; uF1 = uA; }
+        etaA = etaB; thA = thB; gA = gB; tauA = tauB;
+        etaB = etaC; thB = thC; gB = gC; tauB = tau;
+        xnorm = 0.0;
+        for (i = 0; i < n; i++) xnorm += xc[i] * xc[i];
+        xnorm = sqrt(xnorm);
+        /* an iterate longer than maxxnorm is not taken: x keeps the last one */
+        if (xnorm > maxxnorm) { istop = 5; break; }
+        for (i = 0; i < n; i++) x[i] = xc[i];
+        test1 = phibar / (Anorm * xnorm);
+        test2 = root / Anorm;
+        Acond = gmax / gmin;
+        if (itn >= itnlim) istop = 6;
+        if (Acond >= 0.1 / eps) istop = 4;
+        if (test2 <= rtol) istop = 2;
+        if (test1 <= rtol) istop = 1;
+        if (istop) break;
+    }
+    *itnout = itn;
+out:
+    free(r1); free(r2); free(y); free(v); free(wa); free(wb); free(xp); free(xc);
+    return istop;
+}
+
+int32_t mpref_minresqlp_sparse(int32_t matsto, int32_t nVar, int32_t nG,
+                               const int32_t *allIndexGroups, const int64_t *offsets,
+                               const int32_t *columns, const double *matD,
+                               const mpref_ql *q, const double *rhs, double *x,
+                               double rtol, int32_t itnlim, int32_t *itn)
+{
+    redop o;
+    int32_t ncon = q ? q->ncon : 0, i;
+    o.matsto = matsto; o.nVar = nVar; o.nG = nG; o.nfit = nVar - ncon;
+    o.aig = allIndexGroups; o.off = offsets; o.col = columns; o.matD = matD; o.q = q;
+    o.xa = (double *)calloc((size_t)nVar, sizeof(double));
+    o.ba = (double *)calloc((size_t)nVar, sizeof(double));
+    double *dg = (double *)calloc((size_t)nVar, sizeof(double));
+    double *pc = (double *)calloc((size_t)nVar, sizeof(double));
+    reduced_diag(&o, dg);
+    for (i = 0; i < o.nfit; i++) pc[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
+    /* maxxnorm as pede sets it (pede.f90:626) */
+    const double maxxnorm = (double)o.nfit / sqrt(DBL_EPSILON);
+    int32_t istop = minresqlp(&o, pc, rhs, x, rtol, itnlim, maxxnorm, itn);
+    free(o.xa); free(o.ba); free(dg); free(pc);
+    return istop;
+}
+
 int32_t mpref_minres_sparse(int32_t matsto, int32_t nVar, int32_t nG,
                             const int32_t *allIndexGroups, const int64_t *offsets,
                             const int32_t *columns, const double *matD,

@@ -78,3 +78,17 @@ def test_structure_on_device_same_job(mp, orc, kind, metsol, matsto):
     for k in ("labels", "varIndex", "counts", "parameter", "error"):
         np.testing.assert_array_equal(g[k], h[k], err_msg=k)
     assert g["nrej"] == h["nrej"] and g["ndf"] == h["ndf"] and g["fvalue"] == h["fvalue"]
+
+
+def test_barrel_sparse_minresqlp(mp, orc):
+    """Whole job with MINRES-QLP (metsol 5) against the oracle's job driver."""
+    d = mp.generate(mp.gen_config("barrel", ntracks=30000, seed=4))
+    st = orc.make_steer(metsol=5, matsto=2, mitera=2, lhuber=2, mrestl=1e-12, itnlim=3000,
+                        mreqenf=5)
+    g = gpu_job(mp, orc, d, st)
+    o = orc.run(d, st)
+    assert g["rc"] == 0 and o["rc"] == 0
+    np.testing.assert_array_equal(g["counts"], o["counts"])
+    assert g["nrej"] == o["nrej"]
+    scale = np.max(np.abs(o["parameter"]))
+    assert np.max(np.abs(g["parameter"] - o["parameter"])) <= 1e-8 * scale

@@ -143,3 +143,72 @@ def test_dense_refined_solvers(mp, metsol):
     x = kkt_solution(dense_from_packed(M, n), A, lb["gvec"])
     assert info.istop == 1, (info.istop, info.itn)
     assert np.max(np.abs(corr - x)) <= 1e-9 * np.max(np.abs(x))
+
+
+def test_minresqlp_sparse_vs_minres_and_oracle(mp, orc):
+    """MINRES-QLP (metsol 5) on the constrained barrel system: the MINRES
+    solution and the oracle's MINRES-QLP within 1e-8 relative, and a
+    relative residual of the reduced system below 1e-9."""
+    out = {}
+    for metsol in (4, 5):
+        d, H, A, ctx, lb = build(mp, "barrel", 40000, 2)
+        with ctx:
+            M = ctx.matrix()
+            corr, _, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-12, itnlim=4000)
+        out[metsol] = (corr, info.istop, info.itn)
+    corr, istop, itn = out[5]
+    assert istop in (1, 2)
+    scale = np.max(np.abs(out[4][0]))
+    assert np.max(np.abs(corr - out[4][0])) <= 1e-8 * scale
+    O = orc.Structure(d, mreqenf=5)
+    nfit = H.nVar - A.shape[0]
+    L = orc.lib()
+    q = L.mpref_ql_create(H.nVar, A.shape[0], orc.ptr(np.ascontiguousarray(A), orc.f64p))
+    rhs = lb["gvec"].copy()
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(rhs, orc.f64p), C.c_int32(1))
+    xo = np.zeros(H.nVar)
+    it = C.c_int32()
+    so = L.mpref_minresqlp_sparse(C.c_int32(2), C.c_int32(H.nVar), C.c_int32(O.nG),
+                                  orc.ptr(O.aig, orc.i32p), orc.ptr(O.offsets, orc.i64p),
+                                  orc.ptr(O.columns, orc.i32p), orc.ptr(M, orc.f64p),
+                                  C.c_void_p(q), orc.ptr(rhs, orc.f64p), orc.ptr(xo, orc.f64p),
+                                  C.c_double(1e-12), C.c_int32(4000), C.byref(it))
+    xo[nfit:] = 0.0
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xo, orc.f64p), C.c_int32(0))
+    assert so in (1, 2)
+    assert np.max(np.abs(corr - xo)) <= 1e-8 * np.max(np.abs(xo))
+    xr = corr.copy()
+    L.mpref_ql_mlq(C.c_void_p(q), orc.ptr(xr, orc.f64p), C.c_int32(1))
+    with mp.Context() as c2:
+        c2.set_layout(H, 2)
+        c2.set_constraints(A)
+        c2.upload(H)
+        c2.loopbf(np.zeros(H.nTotal))
+        Ax = c2.avprod(xr[:nfit])
+    assert np.linalg.norm(Ax - rhs[:nfit]) / np.linalg.norm(rhs[:nfit]) <= 1e-9
+    L.mpref_ql_destroy(C.c_void_p(q))
+
+
+def test_minresqlp_singular_minimum_length(mp):
+    """Telescope without constraints: the global shift and shear are free,
+    the matrix is singular and the normal equations consistent up to
+    rounding (b's null-space part is at the 1e-16 level, which bounds the
+    attainable relative residual near 1e-11).  At a tolerance above that
+    floor MINRES-QLP returns the minimum-length solution of the diagonally
+    preconditioned system, D pinv(D M D) D b (D = 1/sqrt(diag M)), within
+    1e-7; a tolerance below it lets the iterations continue into the null
+    space."""
+    d = mp.generate(mp.gen_config("telescope", ntracks=3000, seed=31))
+    H = mp.HostStructure(d, mreqenf=5, sparse=False)
+    with mp.Context() as ctx:
+        ctx.set_layout(H, 1)
+        ctx.upload(H)
+        lb = ctx.loopbf(np.zeros(H.nTotal))
+        M = dense_from_packed(ctx.matrix(), H.nVar)
+        corr, _, info = ctx.solve(5, rtol=1e-10, itnlim=2000)
+    b = lb["gvec"]
+    Dm = np.diag(1.0 / np.sqrt(np.diag(M)))
+    want = Dm @ np.linalg.pinv(Dm @ M @ Dm, rcond=1e-10) @ Dm @ b
+    assert np.linalg.matrix_rank(M, tol=1e-9 * np.max(np.abs(M))) <= H.nVar - 2
+    assert info.istop in (1, 2, 4)
+    assert np.max(np.abs(corr - want)) <= 1e-7 * np.max(np.abs(want))

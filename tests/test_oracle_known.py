@@ -180,3 +180,60 @@ def test_chindl(orc):
                 sn = (0.47523, 1.690140, 2.782170)[m - 1]
                 fisher = np.float32((sn + np.sqrt(np.float32(2 * nd - 1))) ** 2 / (2 * nd))
                 assert abs(f(m, nd) - fisher) <= 1e-6 * fisher
+
+
+def minres_call(fn, A, b, rtol=1e-13, itnlim=2000):
+    n = len(b)
+    x = np.zeros(n)
+    itn = C.c_int32()
+    aig = np.arange(1, n + 2, dtype=np.int32)
+    istop = getattr(O.lib(), fn)(C.c_int32(1), C.c_int32(n), C.c_int32(n), aig.ctypes.data_as(i32p), None,
+                                 None, p(packed(A)), None, p(np.ascontiguousarray(b)), p(x),
+                                 C.c_double(rtol), C.c_int32(itnlim), C.byref(itn))
+    return x, istop, itn.value
+
+
+def test_minresqlp_nonsingular(orc):
+    """MINRES-QLP on an SPD system: the solution of numpy within 1e-9, and
+    the MINRES solution within 1e-9 (same Krylov iterates)."""
+    n = 80
+    rng = np.random.default_rng(19)
+    A = spd(n, rng)
+    b = rng.normal(size=n)
+    x, istop, itn = minres_call("mpref_minresqlp_sparse", A, b)
+    assert istop in (1, 2) and itn > 0
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-9
+    xm, _, _ = minres_call("mpref_minres_sparse", A, b)
+    assert rel(x, xm) <= 1e-9
+
+
+def test_minresqlp_singular_minimum_length(orc):
+    """Singular consistent system (rank 40 of 60): MINRES-QLP gives the
+    minimum-length solution of the diagonally preconditioned system,
+    x = D pinv(D A D) D b with D the preconditioner's 1/sqrt(diag A), within
+    1e-8."""
+    n, r = 60, 40
+    rng = np.random.default_rng(23)
+    B = rng.normal(size=(n, r))
+    A = B @ B.T
+    b = A @ rng.normal(size=n)
+    x, istop, itn = minres_call("mpref_minresqlp_sparse", A, b, rtol=1e-12, itnlim=500)
+    D = np.diag(1.0 / np.sqrt(np.diag(A)))
+    want = D @ np.linalg.pinv(D @ A @ D, rcond=1e-10) @ D @ b
+    assert istop in (1, 2), istop
+    assert rel(x, want) <= 1e-8, (rel(x, want), istop, itn)
+
+
+def test_minresqlp_maxxnorm_keeps_last_iterate(orc):
+    """An inconsistent singular system drives the iterates' length up; the
+    solver stops before taking an iterate longer than its limit
+    (n / sqrt(eps)) and returns a finite solution."""
+    n, r = 60, 40
+    rng = np.random.default_rng(29)
+    B = rng.normal(size=(n, r))
+    A = B @ B.T
+    null = np.linalg.svd(B.T)[2][r:].T
+    b = A @ rng.normal(size=n) + null @ rng.normal(size=n - r)
+    x, istop, itn = minres_call("mpref_minresqlp_sparse", A, b, rtol=1e-14, itnlim=400)
+    assert np.all(np.isfinite(x))
+    assert np.linalg.norm(x) <= n / np.sqrt(np.finfo(float).eps)
