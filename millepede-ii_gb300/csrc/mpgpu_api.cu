@@ -441,8 +441,9 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         MPG_CUDA(c, dgrow(j, j.bscr, (int64_t)nsm * 64 * stride));
         for (auto &q : bfp) { q.bscr = j.bscr; q.bscrStride = stride; }
     }
-    // warps per CTA of each class, timed once per upload on a sample of the
-    // class (first loop with matrix); the records' results do not depend on it
+    // warps per CTA of each class, timed on a sample of the class on the
+    // first loop with matrix after an upload that changed the class's
+    // maxima; the records' results do not depend on it
     if (bucketed && opt->icalcm == 1 && !(c->flags & MPGPU_FLAG_NO_AUTOTUNE) && nchunk > 0) {
         for (int b = 0; b < nb; ++b) {
             if (j.bucketWpc[b] != 0 || bfp[b].recList == nullptr) continue;
@@ -462,10 +463,12 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
             cudaEvent_t t0, t1;
             cudaEventCreate(&t0);
             cudaEventCreate(&t1);
+            bool warm = false;
             for (int k = 0; k < 4; ++k) {
                 q.wpc = cand[k];
                 if (fit_warps_per_cta(q) != cand[k]) continue;
-                MPG_CUDA(c, launch_fit(q, nsm, 0, s));   // warm
+                if (!warm) MPG_CUDA(c, launch_fit(q, nsm, 0, s));   // caches and first-launch costs
+                warm = true;
                 cudaEventRecord(t0, s);
                 MPG_CUDA(c, launch_fit(q, nsm, 0, s));
                 cudaEventRecord(t1, s);

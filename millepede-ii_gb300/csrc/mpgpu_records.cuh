@@ -199,6 +199,7 @@ struct UpParams {
     unsigned long long *err;   // min over (record << 8 | code)
     int32_t *maxv;             // nw neq nalc nalg ngrp band bdr nbndr1 nbndr2
     int64_t *ovList;           // records beyond the compact capacity (filled by k_up_scan<false>)
+    int64_t rBegin, rEnd;      // records of a compact-kernel launch
     int32_t *ovCount;
     // tables (fill)
     const int64_t *off;        // 6 scanned arrays of nrec + 1

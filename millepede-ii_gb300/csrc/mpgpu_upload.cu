@@ -29,7 +29,7 @@ namespace {
 // record index of work step `it`: all records (compact) or the overflow list (large)
 template <bool BIG>
 __device__ __forceinline__ int64_t up_steps(const UpParams &P) {
-    return BIG ? (int64_t)*P.ovCount : P.nrec;
+    return BIG ? (int64_t)*P.ovCount : P.rEnd - P.rBegin;
 }
 
 template <bool BIG>
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(32 * kUpWarps, UpCap<BIG>::kMinBlocks) k_up_sc
     const int64_t nwarps = (int64_t)gridDim.x * kUpWarps;
     const int64_t nsteps = up_steps<BIG>(P);
     for (int64_t it = (int64_t)blockIdx.x * kUpWarps + wib; it < nsteps; it += nwarps) {
-        const int64_t r = BIG ? P.ovList[it] : it;
+        const int64_t r = BIG ? P.ovList[it] : P.rBegin + it;
         RecShape R = analyze<BIG>(P, r, W, true);
         if (!BIG && R.code == kOverflow) {
             if (ln == 0) P.ovList[atomicAdd(P.ovCount, 1)] = r;
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(32 * kUpWarps, UpCap<BIG>::kMinBlocks) k_up_fi
     const int64_t n1 = P.nrec + 1;
     const int64_t nsteps = up_steps<BIG>(P);
     for (int64_t it = (int64_t)blockIdx.x * kUpWarps + wib; it < nsteps; it += nwarps) {
-        const int64_t r = BIG ? P.ovList[it] : it;
+        const int64_t r = BIG ? P.ovList[it] : P.rBegin + it;
         const RecShape R = analyze<BIG>(P, r, W, false);
         if (!BIG && R.code == kOverflow) {  // the large kernel fills it
             __syncwarp();
@@ -478,18 +478,40 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     cudaEvent_t ev[3];
     for (auto &x : ev) cudaEventCreate(&x);
     cudaEventRecord(ev[0], s);
-    if (inder) {  // else the records are already on the device (mpgpu_loop1_device)
-        MPG_CUDA(c, cudaMemcpyAsync(j.inder, inder + recPtr[0], sizeof(int32_t) * j.nw, cudaMemcpyHostToDevice, s));
-        MPG_CUDA(c, cudaMemcpyAsync(j.glder, glder + recPtr[0], sizeof(double) * j.nw, cudaMemcpyHostToDevice, s));
-    }
     MPG_CUDA(c, cudaMemcpyAsync(t.recPtr, recPtr, sizeof(int64_t) * n1, cudaMemcpyHostToDevice, s));
+    // the words in chunks of records on the second stream; the scan of a
+    // chunk starts as soon as its copy is done (the link, not the decode,
+    // bounds the upload)
+    const int nchunkCopy = (inder && j.nw > ((int64_t)64 << 20)) ? 8 : 1;
+    std::vector<int64_t> cr(nchunkCopy + 1);
+    for (int k = 0; k <= nchunkCopy; ++k) cr[k] = nrec * k / nchunkCopy;
+    std::vector<cudaEvent_t> evc(nchunkCopy);
+    for (auto &x : evc) cudaEventCreateWithFlags(&x, cudaEventDisableTiming);
+    struct EvFree {
+        std::vector<cudaEvent_t> &e;
+        ~EvFree() {
+            for (auto x : e) cudaEventDestroy(x);
+        }
+    } evFree{evc};
+    cudaStream_t sc = inder ? c->stream2 : s;
+    MPG_CUDA(c, cudaEventRecord(ev[1], s));
+    MPG_CUDA(c, cudaStreamWaitEvent(sc, ev[1], 0));
+    for (int k = 0; k < nchunkCopy; ++k) {
+        const int64_t a = recPtr[cr[k]], b = recPtr[cr[k + 1]];
+        if (inder && b > a) {
+            MPG_CUDA(c, cudaMemcpyAsync(j.inder + (a - recPtr[0]), inder + a, sizeof(int32_t) * (b - a),
+                                        cudaMemcpyHostToDevice, sc));
+            MPG_CUDA(c, cudaMemcpyAsync(j.glder + (a - recPtr[0]), glder + a, sizeof(double) * (b - a),
+                                        cudaMemcpyHostToDevice, sc));
+        }
+        MPG_CUDA(c, cudaEventRecord(evc[k], sc));
+    }
     int32_t *dRecFile = nullptr;
     if (recFile) {
         MPG_CUDA(c, dgrow(j, t.recFile, nrec));
         MPG_CUDA(c, cudaMemcpyAsync(t.recFile, recFile, sizeof(int32_t) * nrec, cudaMemcpyHostToDevice, s));
         dRecFile = t.recFile;
     }
-    cudaEventRecord(ev[1], s);
     MPG_CUDA(c, dgrow(j, j.rec, nrec));
     MPG_CUDA(c, dgrow(j, t.cnt, 6 * n1));
     MPG_CUDA(c, dgrow(j, t.scanTmp, scan_tmp_len(std::max<int64_t>(n1, 256 * 8))));
@@ -522,10 +544,19 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     const unsigned upBlocks = (unsigned)std::max<int64_t>(
         1, std::min<int64_t>((nrec + kUpWarps - 1) / kUpWarps, (int64_t)nsm * std::max(perSm, 1)));
     const unsigned upBlocksBig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nrec, (int64_t)nsm * 2));
-    if (nrec > 0) {
-        k_up_scan<false><<<upBlocks, 32 * kUpWarps, smemS, s>>>(P);
-        k_up_scan<true><<<upBlocksBig, 32 * kUpWarps, smemB, s>>>(P);
+    for (int k = 0; k < nchunkCopy; ++k) {
+        MPG_CUDA(c, cudaStreamWaitEvent(s, evc[k], 0));
+        P.rBegin = cr[k];
+        P.rEnd = cr[k + 1];
+        const unsigned g = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>((P.rEnd - P.rBegin + kUpWarps - 1) / kUpWarps, (int64_t)upBlocks));
+        if (P.rEnd > P.rBegin) k_up_scan<false><<<g, 32 * kUpWarps, smemS, s>>>(P);
     }
+    // copy time: until the last chunk has arrived
+    cudaEventRecord(ev[1], sc);
+    if (nrec > 0) k_up_scan<true><<<upBlocksBig, 32 * kUpWarps, smemB, s>>>(P);
+    P.rBegin = 0;
+    P.rEnd = nrec;
     MPG_CUDA(c, cudaGetLastError());
     // offsets: exclusive scans of the six count arrays (the spare last
     // element of each receives the total)
@@ -773,6 +804,7 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
             k_u32_copy<<<blocks_for(nrec), 256, 0, s>>>(sb.v0, j.recList, nrec);
         }
         std::vector<int64_t> ends(nkey);
+        std::vector<int32_t> prevMax = j.bucketMax;
         j.bucketMax.assign(MPG_FIT_BUCKETS * 7, 0);
         MPG_CUDA(c, cudaMemcpyAsync(ends.data(), t.keyEnd, sizeof(int64_t) * nkey, cudaMemcpyDeviceToHost, s));
         MPG_CUDA(c, cudaMemcpyAsync(j.bucketMax.data(), t.bmax, sizeof(int32_t) * MPG_FIT_BUCKETS * 7,
@@ -780,8 +812,18 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
         MPG_CUDA(c, cudaStreamSynchronize(s));
         j.bucketOff.assign(nkey + 1, 0);
         for (int64_t k = 0; k < nkey; ++k) j.bucketOff[k + 1] = ends[k] > 0 ? ends[k] : j.bucketOff[k];
-        j.bucketWpc.assign(MPG_FIT_BUCKETS, 0);
-        j.bucketTuneMs.assign(MPG_FIT_BUCKETS * 4, 0.0);
+        // tuned warps per CTA stay valid for a class whose maxima (and so
+        // its shared-memory arena) did not change
+        if (j.bucketWpc.size() != MPG_FIT_BUCKETS || prevMax.size() != j.bucketMax.size()) {
+            j.bucketWpc.assign(MPG_FIT_BUCKETS, 0);
+            j.bucketTuneMs.assign(MPG_FIT_BUCKETS * 4, 0.0);
+        } else {
+            for (int b = 0; b < MPG_FIT_BUCKETS; ++b)
+                if (!std::equal(prevMax.begin() + 7 * b, prevMax.begin() + 7 * b + 7, j.bucketMax.begin() + 7 * b)) {
+                    j.bucketWpc[b] = 0;
+                    for (int k = 0; k < 4; ++k) j.bucketTuneMs[4 * b + k] = 0.0;
+                }
+        }
     }
     // ---- per-loop outputs, file weights, staging and partial sums
     std::vector<double> fw(nfiles, 1.0);
