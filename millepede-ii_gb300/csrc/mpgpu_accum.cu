@@ -249,39 +249,67 @@ __global__ void __launch_bounds__(256) k_acc_block_reduce(AccParams p) {
     }
 }
 
-// vector slices and counts: warp per row group, lane l sums the accepted
-// records l, l+32, ... of the group, lane sums added in lane order
-__global__ void __launch_bounds__(256) k_acc_vector(AccParams p) {
-    __shared__ double vacc[8][kTileV][32];
-    __shared__ int32_t cacc[8][kTileV][32];
-    const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t I = 1 + w; I <= p.nG; I += nw) {
+// vector slices and counts: one CTA of 256 threads per row group; thread t
+// sums the accepted records t, t+256, ... of the group in registers (loads
+// of four entries issued together), then the threads' sums are added by a
+// fixed tree (warp shuffles, then the eight warp sums in order), so every
+// loop adds in the same order
+constexpr int kVecThreads = 256;
+__global__ void __launch_bounds__(kVecThreads) k_acc_vector(AccParams p) {
+    __shared__ double wsum[kVecThreads / 32][kTileV];
+    __shared__ long long wcnt[kVecThreads / 32][kTileV];
+    const int tid = threadIdx.x, ln = tid & 31, wib = tid >> 5;
+    for (int64_t I = 1 + blockIdx.x; I <= p.nG; I += gridDim.x) {
         const int64_t e0 = p.vStart[I - 1], e1 = p.vStart[I];
         if (e1 <= e0) continue;
         const int32_t ia = p.aig[I - 1] - 1, np = p.aig[I] - p.aig[I - 1];
         for (int32_t t0 = 0; t0 < np; t0 += kTileV) {
             const int32_t tn = np - t0 < kTileV ? np - t0 : kTileV;
-            for (int q = 0; q < tn; ++q) { vacc[wib][q][ln] = 0.0; cacc[wib][q][ln] = 0; }
-            for (int64_t e = e0 + ln; e < e1; e += 32) {
-                const int64_t ent = p.vEntries[e];
-                const int64_t r = ent >> 40, vo = ent & ((int64_t(1) << 40) - 1);
-                if (p.status[r] != 0) continue;
-                for (int q = 0; q < tn; ++q) {
-                    vacc[wib][q][ln] += p.vstage[vo + t0 + q];
-                    cacc[wib][q][ln] += p.slotCnt[vo + t0 + q];
+            double acc[kTileV];
+            long long cn[kTileV];
+#pragma unroll
+            for (int q = 0; q < kTileV; ++q) { acc[q] = 0.0; cn[q] = 0; }
+            for (int64_t e = e0 + tid; e < e1; e += 4 * kVecThreads) {
+                int64_t vo[4];
+                bool ok[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t eu = e + (int64_t)u * kVecThreads;
+                    const int64_t ent = eu < e1 ? p.vEntries[eu] : -1;
+                    vo[u] = ent & ((int64_t(1) << 40) - 1);
+                    ok[u] = ent >= 0 && p.status[ent >> 40] == 0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (!ok[u]) continue;
+#pragma unroll
+                    for (int q = 0; q < kTileV; ++q) {
+                        if (q >= tn) break;
+                        acc[q] += p.vstage[vo[u] + t0 + q];
+                        cn[q] += p.slotCnt[vo[u] + t0 + q];
+                    }
                 }
             }
-            __syncwarp();
-            for (int q = ln; q < tn; q += 32) {
-                double v = 0.0;
-                int64_t cn = 0;
-                for (int l = 0; l < 32; ++l) { v += vacc[wib][q][l]; cn += cacc[wib][q][l]; }
-                p.gvec[ia + t0 + q] += v;
-                p.gcnt[ia + t0 + q] += cn;
+#pragma unroll
+            for (int q = 0; q < kTileV; ++q) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+                    cn[q] += __shfl_xor_sync(0xffffffffu, cn[q], o);
+                }
             }
-            __syncwarp();
+            if (ln == 0)
+#pragma unroll
+                for (int q = 0; q < kTileV; ++q) { wsum[wib][q] = acc[q]; wcnt[wib][q] = cn[q]; }
+            __syncthreads();
+            if (tid < tn) {
+                double v = 0.0;
+                long long c = 0;
+                for (int w = 0; w < kVecThreads / 32; ++w) { v += wsum[w][tid]; c += wcnt[w][tid]; }
+                p.gvec[ia + t0 + tid] += v;
+                p.gcnt[ia + t0 + tid] += c;
+            }
+            __syncthreads();
         }
     }
 }
@@ -291,31 +319,43 @@ __global__ void __launch_bounds__(256) k_acc_vector(AccParams p) {
 // tree (block partials in a fixed order, then one block).
 __global__ void k_stats_partial(StatParams p, double *part, float *fpart) {
     __shared__ double sf[256], sw[256];
+    // integer counters of the block (exact), one global atomic each at the end
+    __shared__ unsigned long long ic[9];
+    extern __shared__ unsigned long long fc[];   // 2 * nfiles: accepted, ndf per file
+    for (int k = threadIdx.x; k < 9; k += blockDim.x) ic[k] = 0;
+    for (int k = threadIdx.x; k < 2 * p.nfiles; k += blockDim.x) fc[k] = 0;
+    __syncthreads();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double frac = 0.0, wndf = 0.0;
+    int st = -1, file = 0;
     if (i < p.nrec) {
-        const int st = p.status[i];
-        const RecInfo ri = p.rec[i];
-        const double dw = p.fileWeight ? p.fileWeight[ri.file - 1] : 1.0;
-        if (st >= 1 && st <= 6) atomicAdd((unsigned long long *)&p.iout[1 + st], 1ull);
+        st = p.status[i];
+        file = p.rec[i].file;
+        const double dw = p.fileWeight ? p.fileWeight[file - 1] : 1.0;
+        const int ndfa = p.ndfadd[i];
+        const double c2 = p.chi2add[i];
+        if (st >= 1 && st <= 6) atomicAdd(&ic[1 + st], 1ull);
         if (st == 0) {
-            atomicAdd((unsigned long long *)&p.iout[8], 1ull);
-            atomicAdd((unsigned long long *)&p.iout[9 + ri.file - 1], 1ull);
-            atomicAdd((unsigned long long *)&p.iout[9 + p.nfiles + ri.file - 1],
-                      (unsigned long long)(long long)p.ndfadd[i]);
+            atomicAdd(&ic[8], 1ull);
+            atomicAdd(&fc[file - 1], 1ull);
+            atomicAdd(&fc[p.nfiles + file - 1], (unsigned long long)(long long)ndfa);
         }
-        if (p.ndfadd[i] > 0 || p.chi2add[i] != 0.0) {
-            const double add = p.chi2add[i] * dw;
+        if (ndfa > 0 || c2 != 0.0) {
+            const double add = c2 * dw;
             const long long nadd = (long long)add;
-            atomicAdd((unsigned long long *)&p.iout[0], (unsigned long long)nadd);
-            atomicAdd((unsigned long long *)&p.iout[1], (unsigned long long)(long long)p.ndfadd[i]);
+            atomicAdd(&ic[0], (unsigned long long)nadd);
+            atomicAdd(&ic[1], (unsigned long long)(long long)ndfa);
             frac = add - (double)nadd;
-            wndf = (double)p.ndfadd[i] * dw;
+            wndf = (double)ndfa * dw;
         }
     }
     sf[threadIdx.x] = frac;
     sw[threadIdx.x] = wndf;
     __syncthreads();
+    for (int k = threadIdx.x; k < 9; k += blockDim.x)
+        if (ic[k]) atomicAdd((unsigned long long *)&p.iout[k], ic[k]);
+    for (int k = threadIdx.x; k < 2 * p.nfiles; k += blockDim.x)
+        if (fc[k]) atomicAdd((unsigned long long *)&p.iout[9 + k], fc[k]);
     for (int s = 128; s > 0; s >>= 1) {
         if (threadIdx.x < s) {
             sf[threadIdx.x] += sf[threadIdx.x + s];
@@ -331,7 +371,7 @@ __global__ void k_stats_partial(StatParams p, double *part, float *fpart) {
     for (int f = 0; f < p.nfiles; ++f) {
         __syncthreads();
         float v = 0.0f;
-        if (i < p.nrec && p.status[i] == 0 && p.rec[i].file == f + 1) v = p.chndf[i];
+        if (st == 0 && file == f + 1) v = p.chndf[i];
         sf[threadIdx.x] = (double)v;
         __syncthreads();
         for (int s = 128; s > 0; s >>= 1) {
@@ -342,19 +382,44 @@ __global__ void k_stats_partial(StatParams p, double *part, float *fpart) {
     }
 }
 
-__global__ void k_stats_final(StatParams p, const double *part, const float *fpart, int nblk) {
-    if (threadIdx.x != 0) return;
+// block partials summed by 256 threads: thread t adds partials t, t+256,
+// ... in order, then a fixed tree (warp shuffles, warp sums in order)
+__global__ void __launch_bounds__(256) k_stats_final(StatParams p, const double *part, const float *fpart,
+                                                     int nblk) {
+    __shared__ double ws[8][2];
+    __shared__ float wf[8];
+    const int tid = threadIdx.x, ln = tid & 31, wib = tid >> 5;
     double f = 0.0, w = 0.0;
-    for (int b = 0; b < nblk; ++b) {
+    for (int b = tid; b < nblk; b += 256) {
         f += part[2 * b];
         w += part[2 * b + 1];
     }
-    p.out[0] = f;
-    p.out[1] = w;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        f += __shfl_xor_sync(0xffffffffu, f, o);
+        w += __shfl_xor_sync(0xffffffffu, w, o);
+    }
+    if (ln == 0) { ws[wib][0] = f; ws[wib][1] = w; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, c = 0.0;
+        for (int q = 0; q < 8; ++q) { a += ws[q][0]; c += ws[q][1]; }
+        p.out[0] = a;
+        p.out[1] = c;
+    }
     for (int fi = 0; fi < p.nfiles; ++fi) {
-        float s = 0.0f;
-        for (int b = 0; b < nblk; ++b) s += fpart[(int64_t)fi * nblk + b];
-        p.fout[fi] = s;
+        __syncthreads();
+        float sfl = 0.0f;
+        for (int b = tid; b < nblk; b += 256) sfl += fpart[(int64_t)fi * nblk + b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sfl += __shfl_xor_sync(0xffffffffu, sfl, o);
+        if (ln == 0) wf[wib] = sfl;
+        __syncthreads();
+        if (tid == 0) {
+            float a = 0.0f;
+            for (int q = 0; q < 8; ++q) a += wf[q];
+            p.fout[fi] = a;
+        }
     }
 }
 
@@ -399,10 +464,10 @@ cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
             k_acc_block_reduce<<<(unsigned)rb, 256, 0, s>>>(p);
         }
     }
-    int64_t vb = (p.nG + 7) / 8;
-    if (vb > (int64_t)nsm * 8) vb = (int64_t)nsm * 8;
+    int64_t vb = p.nG;
+    if (vb > (int64_t)nsm * 16) vb = (int64_t)nsm * 16;
     if (vb < 1) vb = 1;
-    k_acc_vector<<<(unsigned)vb, 256, 0, s>>>(p);
+    k_acc_vector<<<(unsigned)vb, kVecThreads, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -414,8 +479,9 @@ cudaError_t launch_stats(const StatParams &p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     e = cudaMallocAsync(&fpart, sizeof(float) * (size_t)(p.nfiles > 0 ? p.nfiles : 1) * (nblk + 1), s);
     if (e != cudaSuccess) return e;
-    if (nblk > 0) k_stats_partial<<<nblk, 256, 0, s>>>(p, part, fpart);
-    k_stats_final<<<1, 32, 0, s>>>(p, part, fpart, nblk);
+    const size_t fsm = sizeof(unsigned long long) * 2 * (size_t)(p.nfiles > 0 ? p.nfiles : 1);
+    if (nblk > 0) k_stats_partial<<<nblk, 256, fsm, s>>>(p, part, fpart);
+    k_stats_final<<<1, 256, 0, s>>>(p, part, fpart, nblk);
     cudaFreeAsync(part, s);
     cudaFreeAsync(fpart, s);
     return cudaGetLastError();
