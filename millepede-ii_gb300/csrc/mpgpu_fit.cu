@@ -616,6 +616,76 @@ __device__ __forceinline__ BandWork band_work(const WarpMem &m, const RecInfo &r
     return wk;
 }
 
+// -sum over the equations shared by slots a and b of dw1 w g_a g_b (the
+// G^T W G part of one update element): merge of the equation-ordered word
+// lists, the pair taken in the reference's order (later word first); for
+// two slots of one group with simple word lists one word per equation
+__device__ __forceinline__ double gtwg_element(const WarpMem &m, int a, int b, bool sameGroupSimple) {
+    double u = 0.0;
+    int qa = m.swS[a], qae = m.swS[a + 1];
+    int qb = m.swS[b], qbe = m.swS[b + 1];
+    if (sameGroupSimple) {
+        for (; qa < qae; ++qa, ++qb) {
+            const int ea = m.sw[qa] >> 16;
+            const double ca = m.w0[ea] * m.gl[m.sw[qa] & 0xffff];
+            u = __fma_rn(-ca, m.gl[m.sw[qb] & 0xffff], u);
+        }
+        return u;
+    }
+    while (qa < qae && qb < qbe) {
+        const int ea = m.sw[qa] >> 16, eb = m.sw[qb] >> 16;
+        if (ea < eb) { qa++; continue; }
+        if (eb < ea) { qb++; continue; }
+        int qa2 = qa, qb2 = qb;
+        while (qa2 < qae && (m.sw[qa2] >> 16) == ea) qa2++;
+        while (qb2 < qbe && (m.sw[qb2] >> 16) == ea) qb2++;
+        const double cw = m.w0[ea];
+        for (int x = qa; x < qa2; ++x)
+            for (int y = qb; y < qb2; ++y) {
+                const int wa = m.sw[x] & 0xffff, wb = m.sw[y] & 0xffff;
+                if (a == b && wb > wa) continue;  // pair once
+                const int wj = wa > wb ? wa : wb, wk = wa > wb ? wb : wa;
+                const double gj = m.gl[wj];
+                if (gj == 0.0) continue;
+                u = u - cw * gj * m.gl[wk];
+            }
+        qa = qa2;
+        qb = qb2;
+    }
+    return u;
+}
+
+constexpr int kSformMaxEq = 4;   // equations per group of the S-form update
+
+// one S-form task: row a of block (pg, q) with MQ equations in group q
+template <int MQ>
+__device__ __forceinline__ void sform_task(const WarpMem &m, const double *S, int neq, int a, int pg, int q,
+                                           const int64_t *pdst, double *stage) {
+    const int c0 = m.goff[q], c1 = (q == pg) ? a + 1 : m.goff[q + 1];
+    const int qa0 = m.swS[a], ma = m.swS[a + 1] - qa0, qc0 = m.swS[c0];
+    double Z[MQ];
+#pragma unroll
+    for (int f = 0; f < MQ; ++f) {
+        const int ef = m.sw[qc0 + f] >> 16;
+        double z = 0.0;
+        for (int i = 0; i < ma; ++i) {
+            const int ent = m.sw[qa0 + i];
+            z = __fma_rn(m.gl[ent & 0xffff], S[(ent >> 16) * neq + ef], z);
+        }
+        Z[f] = z;
+    }
+    const int ii = a - m.goff[pg];
+    const int64_t base = __ldg(pdst + pg * (pg + 1) / 2 + q) +
+                         (q == pg ? (int64_t)ii * (ii + 1) / 2 : (int64_t)ii * (m.goff[q + 1] - c0));
+    for (int b = c0; b < c1; ++b) {
+        double u = gtwg_element(m, a, b, q == pg);
+        const int qb0 = m.swS[b];
+#pragma unroll
+        for (int f = 0; f < MQ; ++f) u = __fma_rn(Z[f], m.gl[m.sw[qb0 + f] & 0xffff], u);
+        stage[base + (b - c0)] = u;
+    }
+}
+
 template <bool BIG>
 __global__ void __launch_bounds__(32 * MPG_WARPS_FIT, 2)
 k_fit(FitParams p, int perWarp) {
@@ -892,17 +962,50 @@ k_fit(FitParams p, int perWarp) {
                     m.w0[e] = dw1 * wv;
                 }
                 __syncwarp();
+                // ---- form of the Schur term B Gamma^-1 B^T.  With T_ek = t2_e
+                // l_ek (weighted local derivatives) B = G T, so the term is
+                // G S G^T with S = T Gamma^-1 T^T (neq x neq), and the block of
+                // groups (p, q) is G_p S(E_p, E_q) G_q^T over the equations
+                // E_p, E_q of the two groups: cheaper than the rank-nalc form
+                // when groups sit in few equations (one hit: two).  Taken for
+                // records with simple word lists, at most four equations per
+                // group, room for Y and S in the B/W area and a lower count.
+                bool sform = false;
+                if (!BIG && p.icalcm == 1 && simpleWords) {
+                    int mmax = 0, nnz = 0;
+                    for (int g = ln; g < ngrp; g += 32) {
+                        const int c0 = m.goff[g];
+                        mmax = max(mmax, m.swS[c0 + 1] - m.swS[c0]);
+                    }
+                    for (int e = ln; e < neq; e += 32) nnz += m.mq[3 * e + 1] - m.mq[3 * e] - 1;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        mmax = max(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+                        nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
+                    }
+                    const int64_t room = 2 * (int64_t)p.nalcmax * p.nalgmax;
+                    const int64_t need = (int64_t)neq * nalc + (int64_t)neq * neq + (ngrp + 2) / 2 + 1;
+                    if (mmax >= 1 && mmax <= kSformMaxEq && need <= room) {
+                        const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
+                        const int64_t costB = (int64_t)nalg * nalc * (nalc + 1) + ngg * nalc;
+                        // tasks (slot a, group q <= group of a): about nalg * ngrp / 2
+                        const int64_t ntask = (int64_t)nalg * (ngrp + 1) / 2;
+                        const int64_t costS = (int64_t)nnz * nalc + (int64_t)neq * (neq + 1) / 2 * (nnz / neq + 1) +
+                                              ngg * mmax + ntask * mmax * mmax;
+                        sform = costS < costB;
+                    }
+                }
                 // ---- global vector and local-global matrix B, one lane per slot
                 for (int s = ln; s < nalg; s += 32) {
                     double v = 0.0;
-                    if (p.icalcm == 1)
+                    if (p.icalcm == 1 && !sform)
                         for (int k = 0; k < nalc; ++k) mB[k * nalg + s] = 0.0;
                     for (int q = m.swS[s]; q < m.swS[s + 1]; ++q) {
                         const int ent = m.sw[q];
                         const int e = ent >> 16, wp = ent & 0xffff;
                         const double g = m.gl[wp];
                         if (g != 0.0) v = v + m.t1[e] * g;
-                        if (p.icalcm == 1) {
+                        if (p.icalcm == 1 && !sform) {
                             const double cb = m.t2[e] * g;
                             const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                             for (int jj = 1; jj <= sg - sl - 1; ++jj) {
@@ -921,7 +1024,70 @@ k_fit(FitParams p, int perWarp) {
                     w_band_inverse(ri.mside & 0xff, m.clmat, nalc, ri.mbdr, ri.mbnd, wk, X, p.nalcmax,
                                    X + 32 * (int64_t)p.nalcmax);
                 }
-                if (p.icalcm == 1) {
+                if (p.icalcm == 1 && sform) {
+                    double *Y = mB;                               // neq x nalc: L Gamma^-1
+                    double *S = mB + (int64_t)neq * nalc;         // neq x neq
+                    int32_t *tpre = reinterpret_cast<int32_t *>(S + (int64_t)neq * neq);   // ngrp + 1
+                    // Y_ek = sum over the locals j of equation e of l_ej Gamma^-1_jk
+                    for (int t = ln; t < neq * nalc; t += 32) {
+                        const int e = t / nalc, k = t - e * nalc + 1;
+                        const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
+                        double y = 0.0;
+                        for (int jj = 1; jj <= sg - sl - 1; ++jj) {
+                            const int l = m.in[sl + jj];
+                            const double g = l <= k ? m.clmat[(k * k - k) / 2 + l - 1] : m.clmat[(l * l - l) / 2 + k - 1];
+                            y = __fma_rn(m.gl[sl + jj], g, y);
+                        }
+                        Y[t] = y;
+                    }
+                    // task prefix over groups: group g has (rows of g) x (g + 1) tasks
+                    if (ln == 0) {
+                        int acc = 0;
+                        for (int g = 0; g < ngrp; ++g) {
+                            tpre[g] = acc;
+                            acc += (m.goff[g + 1] - m.goff[g]) * (g + 1);
+                        }
+                        tpre[ngrp] = acc;
+                    }
+                    __syncwarp();
+                    // S_ef = t2_e t2_f sum over the locals k of equation f of Y_ek l_fk
+                    const int ns = neq * (neq + 1) / 2;
+                    for (int t = ln; t < ns; t += 32) {
+                        int e = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+                        while (e > 0 && e * (e + 1) / 2 > t) e--;
+                        while ((e + 1) * (e + 2) / 2 <= t) e++;
+                        const int f = t - e * (e + 1) / 2;
+                        const int sl = m.mq[3 * f], sg = m.mq[3 * f + 1];
+                        double acc = 0.0;
+                        for (int jj = 1; jj <= sg - sl - 1; ++jj)
+                            acc = __fma_rn(Y[e * nalc + m.in[sl + jj] - 1], m.gl[sl + jj], acc);
+                        const double v = m.t2[e] * m.t2[f] * acc;
+                        S[e * neq + f] = v;
+                        S[f * neq + e] = v;
+                    }
+                    __syncwarp();
+                    // tasks (slot a, group q): Z_f = sum_{e in E_p} g_ae S_ef over the
+                    // equations f of q, then the row of a in block (p, q):
+                    // U(a, b) = G^T W G part + sum_f Z_f g_bf
+                    const int ntask = tpre[ngrp];
+                    for (int t = ln; t < ntask; t += 32) {
+                        int lo = 0, hi = ngrp - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (tpre[mid] <= t) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        const int pg = lo, loc = t - tpre[pg];
+                        const int a = m.goff[pg] + loc / (pg + 1), q = loc % (pg + 1);
+                        const int c0 = m.goff[q];
+                        switch (m.swS[c0 + 1] - m.swS[c0]) {
+                            case 1: sform_task<1>(m, S, neq, a, pg, q, pdst, p.stage); break;
+                            case 2: sform_task<2>(m, S, neq, a, pg, q, pdst, p.stage); break;
+                            case 3: sform_task<3>(m, S, neq, a, pg, q, pdst, p.stage); break;
+                            default: sform_task<4>(m, S, neq, a, pg, q, pdst, p.stage); break;
+                        }
+                    }
+                } else if (p.icalcm == 1) {
                     // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432):
                     // eight k at a time, each c_ik summed over l = 1..nalc in
                     // order, every B(l, s) loaded once per eight products
@@ -958,41 +1124,7 @@ k_fit(FitParams p, int perWarp) {
                     const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
                     for (int64_t idx = ln; idx < ngg; idx += 32) {
                         const int a = bw.a(), b = bw.b();
-                        double u = 0.0;
-                        // Gt W G: equations shared by slots a and b (merge of the
-                        // equation-ordered word lists), pair taken in the
-                        // reference's order (later word first)
-                        int qa = m.swS[a], qae = m.swS[a + 1];
-                        int qb = m.swS[b], qbe = m.swS[b + 1];
-                        if (simpleWords && bw.qa == bw.qb) {
-                            // same group: the same equations, one word each
-                            for (; qa < qae; ++qa, ++qb) {
-                                const int ea = m.sw[qa] >> 16;
-                                const double ca = m.w0[ea] * m.gl[m.sw[qa] & 0xffff];
-                                u = __fma_rn(-ca, m.gl[m.sw[qb] & 0xffff], u);
-                            }
-                            qa = qae;
-                        }
-                        while (qa < qae && qb < qbe) {
-                            const int ea = m.sw[qa] >> 16, eb = m.sw[qb] >> 16;
-                            if (ea < eb) { qa++; continue; }
-                            if (eb < ea) { qb++; continue; }
-                            int qa2 = qa, qb2 = qb;
-                            while (qa2 < qae && (m.sw[qa2] >> 16) == ea) qa2++;
-                            while (qb2 < qbe && (m.sw[qb2] >> 16) == ea) qb2++;
-                            const double cw = m.w0[ea];
-                            for (int x = qa; x < qa2; ++x)
-                                for (int y = qb; y < qb2; ++y) {
-                                    const int wa = m.sw[x] & 0xffff, wb = m.sw[y] & 0xffff;
-                                    if (a == b && wb > wa) continue;  // pair once
-                                    const int wj = wa > wb ? wa : wb, wk = wa > wb ? wb : wa;
-                                    const double gj = m.gl[wj];
-                                    if (gj == 0.0) continue;
-                                    u = u - cw * gj * m.gl[wk];
-                                }
-                            qa = qa2;
-                            qb = qb2;
-                        }
+                        double u = gtwg_element(m, a, b, simpleWords && bw.qa == bw.qb);
                         if (!BIG) {   // large records: W B^T added by k_update_big
                             const double *wa = mW + a * nalc;
                             for (int k = 0; k < nalc; ++k) u = __fma_rn(wa[k], mB[k * nalg + b], u);
