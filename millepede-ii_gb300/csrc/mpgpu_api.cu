@@ -51,6 +51,7 @@ void free_records(DevJob &j) {
     dfree(t.k0); dfree(t.k1); dfree(t.v0); dfree(t.v1); dfree(t.pairKey); dfree(t.hist); dfree(t.head);
     dfree(t.nel); dfree(t.segStart); dfree(t.segEnd); dfree(t.bcnt); dfree(t.bscan); dfree(t.cntG); dfree(t.scal);
     dfree(t.ovList); dfree(t.chunkB); dfree(t.keyEnd); dfree(t.bmax); dfree(j.recList);
+    dfree(j.bigDone);
     j.cap.clear();
     dfree(j.inder); dfree(j.glder); dfree(j.rec); dfree(j.meas); dfree(j.slots);
     dfree(j.slotCnt); dfree(j.swStart); dfree(j.sw); dfree(j.grpId); dfree(j.grpSlot);
@@ -431,8 +432,11 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         if (fit_warps_per_cta(q) < 1) return set_err(c, MPGPU_ERR_LIMIT, "records too large for the fit kernel");
     }
     if (bwNeed > 0) {
+        int64_t subMax = 1;
+        for (int b = 0; b < nb; ++b) subMax = std::max(subMax, bsub[b]);
         MPG_CUDA(c, dgrow(j, j.bw, bwNeed));
-        for (auto &q : bfp) q.bw = j.bw;
+        MPG_CUDA(c, dgrow(j, j.bigDone, subMax));
+        for (auto &q : bfp) { q.bw = j.bw; q.bigDone = j.bigDone; }
     }
     if (fp.bandmax >= 0 && opt->icalcm == 1) {
         // every warp that can be resident: 64 per SM (one-record-per-block

@@ -135,6 +135,7 @@ struct DevJob {
     int64_t stageLen = 0;
     UpTmp tmp;
     double *bw = nullptr;              // large-record mode: B and W of a record range
+    uint8_t *bigDone = nullptr;        // large-record mode: records whose fit wrote the whole update
     double *bscr = nullptr;            // band records: per-warp inverse scratch
     double msUploadCopy = 0.0, msUploadPrepare = 0.0;   // device time of the last upload
     int32_t uploadChunks = 0;
@@ -262,6 +263,7 @@ struct FitParams {
     int32_t bigMode;
     double *bw;
     int64_t bwStride;
+    uint8_t *bigDone;         // per position of the launch: update fully written by the fit
     // band records: per-warp scratch of the warp-parallel band inverse
     double *bscr;
     int64_t bscrStride;

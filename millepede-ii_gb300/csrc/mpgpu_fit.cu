@@ -971,7 +971,7 @@ k_fit(FitParams p, int perWarp) {
                 // records with simple word lists, at most four equations per
                 // group, room for Y and S in the B/W area and a lower count.
                 bool sform = false;
-                if (!BIG && p.icalcm == 1 && simpleWords) {
+                if (p.icalcm == 1 && simpleWords) {
                     int mmax = 0, nnz = 0;
                     for (int g = ln; g < ngrp; g += 32) {
                         const int c0 = m.goff[g];
@@ -983,7 +983,9 @@ k_fit(FitParams p, int perWarp) {
                         mmax = max(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
                         nnz += __shfl_xor_sync(0xffffffffu, nnz, o);
                     }
-                    const int64_t room = 2 * (int64_t)p.nalcmax * p.nalgmax;
+                    // Y, S and the task prefix in the B/W area (large records:
+                    // the record's slot in global memory)
+                    const int64_t room = BIG ? p.bwStride : 2 * (int64_t)p.nalcmax * p.nalgmax;
                     const int64_t need = (int64_t)neq * nalc + (int64_t)neq * neq + (ngrp + 2) / 2 + 1;
                     if (mmax >= 1 && mmax <= kSformMaxEq && need <= room) {
                         const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
@@ -1133,6 +1135,9 @@ k_fit(FitParams p, int perWarp) {
                         bw.advance(32);
                     }
                 }
+                // large records: the update kernel adds W B^T unless the
+                // fit wrote the whole update here
+                if (BIG && p.icalcm == 1 && ln == 0) p.bigDone[it - p.r0] = sform ? 1 : 0;
             }
         }
         if (st != 0 && p.icalcm == 1 && nalc > 0) {
@@ -1170,7 +1175,7 @@ __global__ void __launch_bounds__(256) k_update_big(FitParams p) {
     const int64_t it = p.r0 + blockIdx.x;
     const int64_t r = p.recList ? (int64_t)p.recList[it] : it;
     const RecInfo ri = p.rec[r];
-    if (ri.nalc <= 0 || p.status[r] != 0) return;
+    if (ri.nalc <= 0 || p.status[r] != 0 || p.bigDone[blockIdx.x]) return;
     const int nalg = ri.nalg, nalc = ri.nalc, ngrp = ri.ngrp;
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     for (int g = tid; g < ngrp; g += blockDim.x) goffs[g] = p.grpSlot[ri.grpOff + g];
