@@ -349,9 +349,10 @@ int32_t mpgpu_loop2_device(mpgpu_ctx *ctx, const int32_t *varIndexOfTotal, int32
                            const int32_t *allIndexGroups, int64_t cap, int64_t *offsets,
                            int32_t *columns, int64_t *ncolw, int64_t *nmat);
 
-/* Mille binary files (C or Fortran record framing, float or double words;
- * recognised per file) into record arrays, the file part of readFromBinary
- * (pede.f90:1714-2075).  First call with inder == NULL: *nrec and *nw
+/* Mille binary files (C or Fortran record framing, float or double words,
+ * plain or gzip-compressed; recognised per file, compressed files through
+ * the zlib runtime library libz.so.1) into record arrays, the file part of
+ * readFromBinary (pede.f90:1714-2075).  First call with inder == NULL: *nrec and *nw
  * receive the sizes.  Second call: recPtr[nrec+1], inder[nw], glder[nw]
  * (float words widened to double) and recFile[nrec] (1-based file index,
  * may be NULL) are filled; cap is the length of inder/glder.  maxRec > 0

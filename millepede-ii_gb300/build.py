@@ -53,7 +53,7 @@ def build_lib(verbose=False):
         list(ex.map(_run, jobs))
     objs = [j[-1] for j in jobs]
     out = os.path.join(LIBDIR, "libmpgpu.so")
-    _run([nvcc] + ARCH + ["-shared", "-o", out] + objs + ["-lpthread"])
+    _run([nvcc] + ARCH + ["-shared", "-o", out] + objs + ["-lpthread", "-ldl"])
     if verbose:
         print("built", out)
     return out

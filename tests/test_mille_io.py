@@ -1,6 +1,10 @@
 """Mille binary files through mpgpu_read_mille (no device): C and Fortran
-framing, double and float words, several files with the file index per
-record, a record limit per file, and a damaged file (status 20)."""
+framing, double and float words, gzip-compressed files, several files with
+the file index per record, a record limit per file, and a damaged file
+(status 20)."""
+import gzip
+import shutil
+
 import numpy as np
 import pytest
 
@@ -54,5 +58,38 @@ def test_damaged_file(mp, tmp_path):
     write(p, d["recPtr"], d["inder"], d["glder"], False, True)
     raw = open(p, "rb").read()
     open(p, "wb").write(raw[:-10])
+    with pytest.raises(RuntimeError, match="20"):
+        mp.read_mille([p])
+
+
+@pytest.mark.parametrize("fortran", [False, True])
+def test_read_gzip(mp, tmp_path, fortran):
+    """A gzip-compressed file (recognised by its first bytes) reads like the
+    plain one, also mixed with a plain file."""
+    d = mp.generate(mp.gen_config("barrel", ntracks=200, seed=4))
+    plain = str(tmp_path / "p.bin")
+    write(plain, d["recPtr"], d["inder"], d["glder"], fortran, True)
+    packed = str(tmp_path / "p.bin.gz")
+    with open(plain, "rb") as src, gzip.open(packed, "wb") as dst:
+        shutil.copyfileobj(src, dst)
+    a = mp.read_mille([plain])
+    b = mp.read_mille([packed])
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+    recPtr, inder, glder, recFile = mp.read_mille([packed, plain], max_rec=50)
+    assert len(recPtr) - 1 == 100
+    np.testing.assert_array_equal(recFile, [1] * 50 + [2] * 50)
+    n = d["recPtr"][50]
+    np.testing.assert_array_equal(inder[:n], d["inder"][:n])
+    np.testing.assert_array_equal(inder[n:], d["inder"][:n])
+
+
+def test_damaged_gzip(mp, tmp_path):
+    d = mp.generate(mp.gen_config("telescope", ntracks=20, seed=3))
+    plain = str(tmp_path / "t.bin")
+    write(plain, d["recPtr"], d["inder"], d["glder"], False, True)
+    raw = gzip.compress(open(plain, "rb").read()[:-10])
+    p = str(tmp_path / "t.bin.gz")
+    open(p, "wb").write(raw)
     with pytest.raises(RuntimeError, match="20"):
         mp.read_mille([p])
