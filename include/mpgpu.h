@@ -114,6 +114,48 @@ int32_t mpgpu_upload_records(mpgpu_ctx *ctx, int64_t nrec, const int64_t *recPtr
                              const int32_t *recFile, int32_t nfiles,
                              const double *fileWeight);
 
+/* Monitoring of the data loop (pede's histograms 3, 12, 13, 14 and its
+ * measurement monitor, pede.f90:3938-3980, 4025-4032, 7533-7633), filled
+ * by the device fit in the first local-fit iteration of every record:
+ * normalized residuals r/sigma and pulls r/sqrt(sigma^2 - l^T C l) (where
+ * variance is left), each for measurements with and without global
+ * derivatives, and per monitored group (the first global label of the
+ * measurement, mpgpu_monitor_groups) the pulls (mode 1, monitorpulls) or
+ * the residuals scaled by the group's mean error (mode 0,
+ * monitorresiduals) in measBins bins of 0.1.  Pulls are formed in loops
+ * nloopn <= lfitnp (0: all).  The histograms are reset by every
+ * mpgpu_loopbf.  No counterpart as a C-ABI in the reference. */
+typedef struct mpgpu_monitor_cfg {
+    int32_t nbins;      /* bins of the four histograms, over [-range, range) */
+    float range;
+    int32_t measBins;   /* bins per monitored group (pede's measBins, 100) */
+    int32_t mode;       /* 0 scaled residuals, 1 pulls */
+    int32_t lfitnp;
+} mpgpu_monitor_cfg;
+/* cfg NULL switches monitoring off.  measIndex[nTotal]: group 1..numMeas
+ * of each total parameter index as first global label (0: none); measRes
+ * [numMeas] the groups' mean errors (both from mpgpu_monitor_groups). */
+int32_t mpgpu_set_monitor(mpgpu_ctx *ctx, const mpgpu_monitor_cfg *cfg, const int32_t *measIndex,
+                          const double *measRes, int32_t numMeas);
+/* hist[4 * (nbins + 2)]: residuals with globals, residuals without,
+ * pulls with globals, pulls without; each underflow, bins, overflow.
+ * measHists[numMeas * measBins] (may be NULL). */
+int32_t mpgpu_get_monitor(mpgpu_ctx *ctx, int64_t *hist, int64_t *measHists);
+/* loop2's grouping of the monitor (pede.f90:6700-6710, 7075-7081): the
+ * measurements with local and global derivatives of the (translated)
+ * records by their first global label, counted and their errors averaged
+ * in record order; measIndex[nTotal] numbers the groups in index order.
+ * Returns 0 or a status. */
+int32_t mpgpu_monitor_groups(int64_t nrec, const int64_t *recPtr, const int32_t *inder, const double *glder,
+                             int32_t nTotal, int32_t *measIndex, double *measRes, int32_t *numMeas);
+/* monres (pede.f90:7533-7633): one line per group with the loop number,
+ * its label, entries, median and 1.4826 x median absolute deviation of the
+ * binned values, and the group's mean error, appended to path (header
+ * lines when header != 0). */
+int32_t mpgpu_write_mon(const char *path, int32_t header, int32_t mode, int32_t nloopn, int32_t numMeas,
+                        const int32_t *groupLabel, const int64_t *measHists, int32_t measBins,
+                        const double *measRes);
+
 /* Fit size classes of the uploaded records (the shared memory each fit
  * needs: class k < 7 up to 4 KB << k, class 7 beyond one CTA): records per
  * class, warps per CTA chosen by the tuner on the first data loop (0: not
@@ -278,6 +320,11 @@ typedef struct mpgpu_steer {
     int32_t structDevice; /* 1: structure passes on the device (mpgpu_loop1_device,
                              mpgpu_loop2_device) when mpgpu_pede_run is called
                              directly; 0: on the host */
+    int32_t monitor;      /* imonit of monitorresiduals / monitorpulls: bit 0 writes the
+                             millepede.mon lines (job->monPath) after the first data loop,
+                             bit 1 after the last, < 0 after every loop; 0 off */
+    int32_t monitorPulls; /* imonmd: 1 pulls (monitorpulls), 0 normalised residuals */
+    int32_t monitorBins;  /* measBins, bins of 0.1 per group histogram (>= 2, pede's 100) */
 } mpgpu_steer;
 
 typedef struct mpgpu_job {
@@ -288,6 +335,7 @@ typedef struct mpgpu_job {
     const double *conRhs;
     int32_t nmeas; const int32_t *msStart; const int32_t *msLabel; const double *msCoef;
     const double *msRhs; const double *msSigma;
+    const char *monPath;  /* millepede.mon of the monitor (steer monitor != 0), NULL: none */
 } mpgpu_job;
 
 typedef struct mpgpu_result {

@@ -487,6 +487,42 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         const double s = psig[v2t[i]];
         if (s > 0.0) { pi.push_back(i + 1); pj.push_back(i + 1); pa.push_back(1.0 / (s * s)); }
     }
+    // monitorresiduals / monitorpulls (pede.f90:6571-6579, 2879, 9011):
+    // groups of the first global labels from the translated records; the
+    // group histograms of one data loop are written as millepede.mon lines
+    // after the first loop (bit 0), the last (bit 1) or every loop (< 0)
+    const bool monitor = !rc && st->monitor != 0 && job->monPath;
+    const int32_t monBins = std::max<int32_t>(st->monitorBins, 2);
+    std::vector<int32_t> measIndex, groupLabel;
+    std::vector<double> measRes;
+    int32_t numMeas = 0;
+    bool monHeader = true;
+    if (monitor) {
+        std::vector<int32_t> tr;
+        const int32_t *tin = tinder.data();
+        if (onDevice) {
+            tr.resize(nw);
+            mpgpu_host_translate(job->nrec, job->recPtr, job->inder, job->glder, ntot, res->labels, tr.data());
+            tin = tr.data();
+        }
+        measIndex.assign(ntot, 0);
+        measRes.assign(ntot, 0.0);
+        rc = mpgpu_monitor_groups(job->nrec, job->recPtr, tin, job->glder, ntot, measIndex.data(), measRes.data(),
+                                  &numMeas);
+        groupLabel.assign(std::max(numMeas, 1), 0);
+        for (int32_t i = 0; i < ntot; ++i)
+            if (measIndex[i] > 0) groupLabel[measIndex[i] - 1] = res->labels[i];
+        mpgpu_monitor_cfg mc{100, 5.0f, monBins, st->monitorPulls ? 1 : 0, 0};
+        if (!rc) rc = mpgpu_set_monitor(ctx, &mc, measIndex.data(), measRes.data(), numMeas);
+    }
+    std::vector<int64_t> monHist(4 * 102), monMeas((size_t)std::max(numMeas, 1) * monBins);
+    int32_t monLoop = 0;
+    auto writeMon = [&](int32_t loop) {
+        const int32_t r = mpgpu_write_mon(job->monPath, monHeader ? 1 : 0, st->monitorPulls ? 1 : 0, loop, numMeas,
+                                          groupLabel.data(), monMeas.data(), monBins, measRes.data());
+        monHeader = false;
+        return r;
+    };
     std::vector<double> gvec(nVar), corr(nVar), err(nVar, 0.0), cres(ncon > 0 ? ncon : 1, 0.0);
     std::vector<int64_t> gcnt(nVar);
     bool haveErr = false;
@@ -508,6 +544,12 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         mpgpu_fitstats fs;
         rc = mpgpu_loopbf(ctx, &fo, gpar.data(), nullptr, nullptr, &fs, nullptr, nullptr, nullptr);
         if (rc) break;
+        if (monitor) {
+            rc = mpgpu_get_monitor(ctx, monHist.data(), monMeas.data());
+            monLoop = nloopn;
+            if (!rc && (st->monitor < 0 || (nloopn == 1 && (st->monitor & 1)))) rc = writeMon(nloopn);
+            if (rc) break;
+        }
         nrejTot = 0;
         for (int k = 0; k < 6; ++k) { res->nrej[k] = fs.nrej[k]; nrejTot += fs.nrej[k]; }
         if (3 * nrejTot > job->nrec) { rc = MPGPU_ERR_TOOMANYREJ; break; }
@@ -581,6 +623,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         }
         res->nloopn = nloopn;
     }
+    if (!rc && monitor && st->monitor > 0 && (st->monitor & 2) && monLoop > 0) rc = writeMon(monLoop);
     for (int32_t i = 0; i < ntot; ++i) {
         res->parameter[i] = gpar[i];
         res->presigma[i] = psig[i];
@@ -654,4 +697,89 @@ extern "C" int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, in
     }
     std::fclose(f);
     return 0;
+}
+
+// ------------------------------------------------------------------ monitor
+extern "C" int32_t mpgpu_monitor_groups(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                        const double *glder, int32_t nTotal, int32_t *measIndex, double *measRes,
+                                        int32_t *numMeas) {
+    if (nrec < 0 || !recPtr || !inder || !glder || nTotal <= 0 || !measIndex || !measRes || !numMeas)
+        return MPGPU_ERR_ARG;
+    std::vector<int64_t> cnt(nTotal, 0);
+    std::vector<double> sum(nTotal, 0.0);
+    int32_t bad = 0;
+    for (int64_t r = 0; r < nrec && !bad; ++r) {
+        const bool ok = for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1],
+                                             [&](int64_t, int64_t sg, int64_t lg) {
+                                                 if (lg <= sg) return;   // no global derivative
+                                                 const int32_t ij = inder[sg + 1];
+                                                 if (ij < 1 || ij > nTotal) { bad = 1; return; }
+                                                 cnt[ij - 1]++;
+                                                 sum[ij - 1] = sum[ij - 1] + glder[sg];
+                                             });
+        if (!ok) return MPGPU_ERR_BADRECORD;
+    }
+    if (bad) return MPGPU_ERR_BADINDEX;
+    int32_t n = 0;
+    for (int32_t i = 0; i < nTotal; ++i) {
+        measIndex[i] = 0;
+        if (cnt[i] > 0) {
+            measRes[n] = sum[i] / (double)cnt[i];
+            measIndex[i] = ++n;
+        }
+    }
+    *numMeas = n;
+    return MPGPU_OK;
+}
+
+// location (median) and scale (1.4826 x median absolute deviation) of one
+// group's binned values as monres computes them: medians of the cumulative
+// bin counts with linear interpolation inside the bin, the deviations by
+// folding the bins around the median bin; single precision
+extern "C" int32_t mpgpu_write_mon(const char *path, int32_t header, int32_t mode, int32_t nloopn, int32_t numMeas,
+                                   const int32_t *groupLabel, const int64_t *measHists, int32_t measBins,
+                                   const double *measRes) {
+    if (!path || numMeas < 0 || measBins < 2 || (numMeas > 0 && (!groupLabel || !measHists || !measRes)))
+        return MPGPU_ERR_ARG;
+    FILE *f = std::fopen(path, "a");
+    if (!f) return MPGPU_ERR_ARG;
+    if (header) {
+        std::fprintf(f, "%s\n", mode == 0 ? "*** Normalized residuals grouped by first global label (per local fit cycle) ***"
+                                          : "*** Pulls grouped by first global label (per local fit cycle) ***");
+        std::fprintf(f, "%s\n", "! LFC     Label   Entries        Median  RMS(MAD)          <error>");
+    }
+    const float binSize = 0.1f;
+    std::vector<int64_t> isuml(measBins + 2), isums(measBins + 2);
+    for (int32_t g = 0; g < numMeas; ++g) {
+        const int64_t *h = measHists + (int64_t)g * measBins;   // h[j - 1]: bin j
+        float amed = 0.0f, amad = 0.0f;
+        isuml[1] = h[0];
+        for (int32_t j = 2; j <= measBins; ++j) isuml[j] = isuml[j - 1] + h[j - 1];
+        const int64_t nent = isuml[measBins];
+        if (nent > 0) {
+            int32_t j = 2;
+            for (; j <= measBins; ++j)
+                if (2 * isuml[j] > nent) break;
+            const int32_t imed = j;
+            amed = (float)j;
+            if (j <= measBins && isuml[j] > isuml[j - 1])
+                amed = amed + (float)(nent - 2 * isuml[j - 1]) / (float)(2 * isuml[j] - 2 * isuml[j - 1]);
+            amed = binSize * (amed - (float)(measBins / 2));
+            for (int32_t k = 0; k <= measBins; ++k) isums[k] = 0;
+            for (int32_t jj = imed; jj <= measBins; ++jj) isums[jj - imed + 1] += h[jj - 1];
+            for (int32_t jj = imed - 1; jj >= 1; --jj) isums[imed - jj] += h[jj - 1];
+            for (int32_t k = 2; k <= measBins; ++k) isums[k] = isums[k] + isums[k - 1];
+            for (j = 2; j <= measBins; ++j)
+                if (2 * isums[j] > nent) break;
+            amad = (float)(j - 1);
+            if (j <= measBins && isums[j] > isums[j - 1])
+                amad = amad + (float)(nent - 2 * isums[j - 1]) / (float)(2 * isums[j] - 2 * isums[j - 1]);
+            amad = binSize * amad;
+        }
+        std::fprintf(f, "%5d%10d%10lld%s%s%s\n", nloopn, groupLabel[g], (long long)nent,
+                     fmt_g145((double)amed).c_str(), fmt_g145((double)(amad * 1.4826f)).c_str(),
+                     fmt_g145((double)(float)measRes[g]).c_str());
+    }
+    std::fclose(f);
+    return MPGPU_OK;
 }

@@ -111,6 +111,10 @@ extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
     free_layout(c->j);
     free_constraints(c->j);
     free_resident(c->res);
+    if (c->mon.measIndex) cudaFree(c->mon.measIndex);
+    if (c->mon.measRes) cudaFree(c->mon.measRes);
+    if (c->mon.hist) cudaFree(c->mon.hist);
+    if (c->mon.meas) cudaFree(c->mon.meas);
     if (c->scal) cudaFree(c->scal);
     if (c->hscal) cudaFreeHost(c->hscal);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -336,6 +340,54 @@ extern "C" int32_t mpgpu_loop2_device(mpgpu_ctx *c, const int32_t *varIndexOfTot
     return loop2_device(c, varIndexOfTotal, nVar, nG, allIndexGroups, cap, offsets, columns, ncolw, nmat);
 }
 
+extern "C" int32_t mpgpu_set_monitor(mpgpu_ctx *c, const mpgpu_monitor_cfg *cfg, const int32_t *measIndex,
+                                     const double *measRes, int32_t numMeas) {
+    if (!c) return MPGPU_ERR_ARG;
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    Monitor &M = c->mon;
+    if (M.measIndex) cudaFree(M.measIndex);
+    if (M.measRes) cudaFree(M.measRes);
+    if (M.hist) cudaFree(M.hist);
+    if (M.meas) cudaFree(M.meas);
+    M = Monitor{};
+    if (!cfg) return MPGPU_OK;   // monitoring off
+    if (cfg->nbins < 1 || cfg->nbins > (1 << 20) || !(cfg->range > 0.0f) || cfg->measBins < 1 ||
+        cfg->measBins > (1 << 20) || numMeas < 0 || (numMeas > 0 && (!measIndex || !measRes)))
+        return set_err(c, MPGPU_ERR_ARG, "mpgpu_set_monitor: bad configuration");
+    DevJob &j = c->j;
+    if (numMeas > 0 && j.nTotal <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the monitor groups");
+    M.nbins = cfg->nbins;
+    M.range = cfg->range;
+    M.measBins = cfg->measBins;
+    M.mode = cfg->mode;
+    M.lfitnp = cfg->lfitnp > 0 ? cfg->lfitnp : (1 << 30);
+    M.numMeas = numMeas;
+    MPG_CUDA(c, cudaMalloc(&M.hist, sizeof(unsigned long long) * 4 * (M.nbins + 2)));
+    if (numMeas > 0) {
+        for (int32_t i = 0; i < j.nTotal; ++i)
+            if (measIndex[i] < 0 || measIndex[i] > numMeas) return set_err(c, MPGPU_ERR_ARG, "bad monitor group");
+        MPG_CUDA(c, cudaMalloc(&M.measIndex, sizeof(int32_t) * j.nTotal));
+        MPG_CUDA(c, cudaMalloc(&M.measRes, sizeof(double) * numMeas));
+        MPG_CUDA(c, cudaMalloc(&M.meas, sizeof(unsigned long long) * (size_t)numMeas * M.measBins));
+        MPG_CUDA(c, cudaMemcpy(M.measIndex, measIndex, sizeof(int32_t) * j.nTotal, cudaMemcpyHostToDevice));
+        MPG_CUDA(c, cudaMemcpy(M.measRes, measRes, sizeof(double) * numMeas, cudaMemcpyHostToDevice));
+    }
+    M.on = true;
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_get_monitor(mpgpu_ctx *c, int64_t *hist, int64_t *measHists) {
+    if (!c || !c->mon.on) return c ? set_err(c, MPGPU_ERR_ARG, "monitoring is off") : MPGPU_ERR_ARG;
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    const Monitor &M = c->mon;
+    if (hist)
+        MPG_CUDA(c, cudaMemcpy(hist, M.hist, sizeof(int64_t) * 4 * (M.nbins + 2), cudaMemcpyDeviceToHost));
+    if (measHists && M.numMeas > 0)
+        MPG_CUDA(c, cudaMemcpy(measHists, M.meas, sizeof(int64_t) * (size_t)M.numMeas * M.measBins,
+                               cudaMemcpyDeviceToHost));
+    return MPGPU_OK;
+}
+
 extern "C" int32_t mpgpu_fit_buckets(const mpgpu_ctx *c, int64_t *count, int32_t *wpc, double *tuneMs) {
     static_assert(MPGPU_FIT_BUCKETS == MPG_FIT_BUCKETS, "bucket count of the ABI");
     if (!c) return MPGPU_ERR_ARG;
@@ -389,6 +441,23 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     fp.bandmax = opt->lfitbb > 0 ? j.maxBand : -1; fp.bdrmax = j.maxBdr;
     fp.ngrpmax = std::max(j.maxNgrp, 1);
     fp.errFlag = errFlag;
+    const Monitor &mon = c->mon;
+    if (mon.on) {
+        fp.monOn = 1;
+        fp.monPull = opt->nloopn <= mon.lfitnp ? 1 : 0;
+        fp.monBins = mon.nbins;
+        fp.monMeasBins = mon.measBins;
+        fp.monMode = mon.mode;
+        fp.monRange = mon.range;
+        fp.measIndex = mon.numMeas > 0 ? mon.measIndex : nullptr;
+        fp.measRes = mon.measRes;
+        fp.monHist = mon.hist;
+        fp.measHists = mon.meas;
+        MPG_CUDA(c, cudaMemsetAsync(mon.hist, 0, sizeof(unsigned long long) * 4 * (mon.nbins + 2), s));
+        if (mon.numMeas > 0)
+            MPG_CUDA(c, cudaMemsetAsync(mon.meas, 0, sizeof(unsigned long long) * (size_t)mon.numMeas * mon.measBins,
+                                        s));
+    }
     // fit launches per size class of records (fit buckets, ordered at
     // upload): each class gets shared memory for its own largest record;
     // classes whose B and W do not fit a warp's shared memory with four
@@ -438,7 +507,7 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         MPG_CUDA(c, dgrow(j, j.bigDone, subMax));
         for (auto &q : bfp) { q.bw = j.bw; q.bigDone = j.bigDone; }
     }
-    if (fp.bandmax >= 0 && opt->icalcm == 1) {
+    if (fp.bandmax >= 0 && (opt->icalcm == 1 || mon.on)) {
         // every warp that can be resident: 64 per SM (one-record-per-block
         // launches take at most that many records)
         const int64_t stride = 32 * (int64_t)fp.nalcmax + (int64_t)fp.nalcmax * (fp.nalcmax + 1) / 2 + 2;
@@ -460,6 +529,7 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
             q.stage = j.stage;
             q.r0 = i0;
             q.r1 = i1;
+            q.monOn = 0;   // sample fits leave the monitor alone
             const int cand[4] = {1, 2, 4, 8};
             float best = 0.0f;
             int bestW = 0;

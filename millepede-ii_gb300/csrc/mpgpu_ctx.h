@@ -171,6 +171,17 @@ struct ResidentRecords {
     bool translated = false;
 };
 
+// monitoring of the data loop (mpgpu_set_monitor)
+struct Monitor {
+    bool on = false;
+    int32_t nbins = 100, measBins = 100, mode = 0, lfitnp = 1 << 30, numMeas = 0;
+    float range = 5.0f;
+    int32_t *measIndex = nullptr;        // device [nTotal]
+    double *measRes = nullptr;           // device [numMeas]
+    unsigned long long *hist = nullptr;  // device [4 * (nbins + 2)]
+    unsigned long long *meas = nullptr;  // device [numMeas * measBins]
+};
+
 struct mpgpu_ctx {
     int device = 0;
     int32_t flags = 0;                 // mpgpu_cfg.flags
@@ -180,6 +191,7 @@ struct mpgpu_ctx {
     std::string err;
     DevJob j;
     ResidentRecords res;
+    Monitor mon;
     double *scal = nullptr;      // small device scalar area
     double *hscal = nullptr;     // pinned mirror
     int64_t lastNaccepted = 0;
@@ -264,6 +276,15 @@ struct FitParams {
     double *bw;
     int64_t bwStride;
     uint8_t *bigDone;         // per position of the launch: update fully written by the fit
+    // monitoring (first local-fit iteration): normalized residuals and pulls
+    // with/without global derivatives (4 histograms of monBins + 2 bins:
+    // underflow, bins, overflow) and the pulls or scaled residuals of the
+    // monitored measurement groups (measBins per group)
+    int32_t monOn, monPull, monBins, monMeasBins, monMode;
+    float monRange;
+    const int32_t *measIndex;       // [nTotal] group (1-based) of the first global label, 0: none
+    const double *measRes;          // [numMeas] mean error of the group
+    unsigned long long *monHist, *measHists;
     // band records: per-warp scratch of the warp-parallel band inverse
     double *bscr;
     int64_t bscrStride;

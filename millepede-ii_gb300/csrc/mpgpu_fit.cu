@@ -616,6 +616,20 @@ __device__ __forceinline__ BandWork band_work(const WarpMem &m, const RecInfo &r
     return wk;
 }
 
+// one entry of monitoring histogram h: bins 1..nbins cover [-range, range),
+// bin 0 and nbins + 1 take what falls below and above; NaN is not entered
+__device__ __forceinline__ void mon_hist(const FitParams &p, int h, float x) {
+    if (!(x == x)) return;
+    int b;
+    if (x < -p.monRange) b = 0;
+    else if (x >= p.monRange) b = p.monBins + 1;
+    else {
+        b = 1 + (int)((x + p.monRange) * ((float)p.monBins / (2.0f * p.monRange)));
+        if (b > p.monBins) b = p.monBins;
+    }
+    atomicAdd(&p.monHist[h * (p.monBins + 2) + b], 1ull);
+}
+
 // -sum over the equations shared by slots a and b of dw1 w g_a g_b (the
 // G^T W G part of one update element): merge of the equation-ordered word
 // lists, the pair taken in the reference's order (later word first); for
@@ -848,6 +862,14 @@ k_fit(FitParams p, int perWarp) {
                               &evdmax, wk);
                     cndl10 = evdmin > 0.0 ? log10f((float)(evdmax / evdmin)) : 0.0f;
                     nrank = nr;
+                    if (p.monOn && p.monPull && iter == 1 && nr == nalc) {
+                        // the local covariance for the pulls (rebuilt from the
+                        // normal equations in later iterations)
+                        const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+                        double *X = p.bscr + wid * p.bscrStride;
+                        w_band_inverse(ri.mside & 0xff, m.clmat, nalc, ri.mbdr, ri.mbnd, wk, X, p.nalcmax,
+                                       X + 32 * (int64_t)p.nalcmax);
+                    }
                 } else {
                     cndl10 = 0.0f;
                     warp_sqminv(m.clmat, m.blvec, nalc, &nrank, m.diag, m.ocol, m.scol, m.used);
@@ -870,6 +892,40 @@ k_fit(FitParams p, int perWarp) {
                     }
                     m.lcor[e] = rmloc;
                     const double rm = m.rm1[e] - rmloc;
+                    if (p.monOn && iter == 1) {
+                        // monitoring (pede.f90:3938-3980, 4025-4032): normalized
+                        // residual; pull rm / sqrt(1/w - l^T C l) where variance is
+                        // left, binned per group of the first global label
+                        const bool withGlobal = sg < m.mq[3 * e + 2];
+                        mon_hist(p, withGlobal ? 0 : 1, (float)(rm / rerr));
+                        if (p.monPull && (!band || nrank == nalc)) {
+                            double dvar = 0.0;
+                            for (int j = 1; j <= sg - sl - 1; ++j) {
+                                const int ij = m.in[sl + j];
+                                const int jk = (ij * ij - ij) / 2;
+                                for (int k = 1; k <= j - 1; ++k) {
+                                    const int ik = m.in[sl + k];
+                                    dvar = dvar + m.clmat[jk + ik - 1] * m.gl[sl + j] * m.gl[sl + k] * 2.0;
+                                }
+                                dvar = dvar + m.clmat[jk + ij - 1] * m.gl[sl + j] * m.gl[sl + j];
+                            }
+                            if (0.999999 / wght > dvar) {
+                                const double pull = rm / sqrt(1.0 / wght - dvar);
+                                mon_hist(p, withGlobal ? 2 : 3, (float)pull);
+                                if (withGlobal && p.measIndex) {
+                                    const int g = p.measIndex[m.in[sg + 1] - 1];
+                                    if (g > 0) {
+                                        const double half = 0.5 * (double)p.monMeasBins;
+                                        const double x = p.monMode == 0 ? pull * rerr / p.measRes[g - 1] / 0.1 + half
+                                                                        : pull / 0.1 + half;
+                                        int irbin = x == x ? (int)x : 1;
+                                        irbin = irbin < 1 ? 1 : (irbin > p.monMeasBins ? p.monMeasBins : irbin);
+                                        atomicAdd(&p.measHists[(int64_t)(g - 1) * p.monMeasBins + irbin - 1], 1ull);
+                                    }
+                                }
+                            }
+                        }
+                    }
                     double dchi2 = wght * rm * rm;
                     if (down) {
                         if (iter <= 3) {

@@ -26,6 +26,36 @@ FLAG_ONE_RECORD_PER_BLOCK = 4
 FLAG_NO_AUTOTUNE = 8
 
 
+class MonitorCfg(C.Structure):
+    _fields_ = [("nbins", C.c_int32), ("range", C.c_float), ("measBins", C.c_int32),
+                ("mode", C.c_int32), ("lfitnp", C.c_int32)]
+
+
+def monitor_groups(S):
+    """Monitor groups of a HostStructure's translated records:
+    (measIndex[nTotal], measRes[numMeas])."""
+    mi = np.zeros(S.nTotal, np.int32)
+    mr = np.zeros(max(S.nTotal, 1), np.float64)
+    n = C.c_int32()
+    rc = lib().mpgpu_monitor_groups(C.c_int64(len(S.recPtr) - 1), ptr(S.recPtr, i64p), ptr(S.tinder, i32p),
+                                    ptr(S.glder, f64p), C.c_int32(S.nTotal), ptr(mi, i32p), ptr(mr, f64p),
+                                    C.byref(n))
+    if rc:
+        raise RuntimeError(f"mpgpu_monitor_groups failed ({rc})")
+    return mi, mr[:n.value].copy()
+
+
+def write_mon(path, header, mode, nloopn, group_labels, meas_hists, meas_res):
+    gl = np.ascontiguousarray(group_labels, np.int32)
+    mh = np.ascontiguousarray(meas_hists, np.int64)
+    mr = np.ascontiguousarray(meas_res, np.float64)
+    rc = lib().mpgpu_write_mon(str(path).encode(), C.c_int32(header), C.c_int32(mode), C.c_int32(nloopn),
+                               C.c_int32(len(gl)), ptr(gl, i32p), ptr(mh.reshape(-1), i64p),
+                               C.c_int32(mh.shape[1] if mh.ndim == 2 else 100), ptr(mr, f64p))
+    if rc:
+        raise RuntimeError(f"mpgpu_write_mon failed ({rc})")
+
+
 class MpgpuCfg(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32), ("staging_bytes", C.c_int64)]
 
@@ -56,7 +86,8 @@ class Steer(C.Structure):
                 ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float),
                 ("lfitbb", C.c_int32), ("mreqenf", C.c_int32), ("mreqena", C.c_int32),
                 ("mreqpe", C.c_int32), ("mrestl", C.c_double), ("itnlim", C.c_int32),
-                ("nthreads", C.c_int32), ("structDevice", C.c_int32)]
+                ("nthreads", C.c_int32), ("structDevice", C.c_int32), ("monitor", C.c_int32),
+                ("monitorPulls", C.c_int32), ("monitorBins", C.c_int32)]
 
 
 class Job(C.Structure):
@@ -67,7 +98,7 @@ class Job(C.Structure):
                 ("ncon", C.c_int32), ("conStart", i32p), ("conLabel", i32p),
                 ("conCoef", f64p), ("conRhs", f64p),
                 ("nmeas", C.c_int32), ("msStart", i32p), ("msLabel", i32p),
-                ("msCoef", f64p), ("msRhs", f64p), ("msSigma", f64p)]
+                ("msCoef", f64p), ("msRhs", f64p), ("msSigma", f64p), ("monPath", C.c_char_p)]
 
 
 class Result(C.Structure):
@@ -118,6 +149,7 @@ EXPORTS = [
     "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
     "mpgpu_dense_cholesky", "mpgpu_upload_timing", "mpgpu_fit_buckets",
+    "mpgpu_set_monitor", "mpgpu_get_monitor", "mpgpu_monitor_groups", "mpgpu_write_mon",
     "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
     "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
@@ -406,6 +438,29 @@ class Context:
             self.h, C.c_int64(self.nrec), ptr(S.recPtr, i64p), ptr(None if resident else S.tinder, i32p),
             ptr(None if resident else S.glder, f64p), ptr(rf, i32p), C.c_int32(self.nfiles), ptr(fw, f64p)))
 
+    def set_monitor(self, nbins=100, rng=5.0, meas_bins=100, mode=1, lfitnp=0, meas_index=None,
+                    meas_res=None):
+        """Monitoring of the following data loops (None as nbins: off)."""
+        if nbins is None:
+            self.check(self.L.mpgpu_set_monitor(self.h, None, None, None, C.c_int32(0)))
+            self.mon = None
+            return
+        cfg = MonitorCfg(nbins=nbins, range=rng, measBins=meas_bins, mode=mode, lfitnp=lfitnp)
+        mi = None if meas_index is None else np.ascontiguousarray(meas_index, np.int32)
+        mr = None if meas_res is None else np.ascontiguousarray(meas_res, np.float64)
+        nmeas = 0 if mr is None else len(mr)
+        self.check(self.L.mpgpu_set_monitor(self.h, C.byref(cfg), ptr(mi, i32p), ptr(mr, f64p),
+                                            C.c_int32(nmeas)))
+        self.mon = (nbins, meas_bins, nmeas)
+
+    def get_monitor(self):
+        """(hist[4, nbins + 2], measHists[numMeas, measBins]) of the last loop."""
+        nbins, mb, nmeas = self.mon
+        h = np.zeros(4 * (nbins + 2), np.int64)
+        mh = np.zeros(max(nmeas * mb, 1), np.int64)
+        self.check(self.L.mpgpu_get_monitor(self.h, ptr(h, i64p), ptr(mh, i64p)))
+        return h.reshape(4, nbins + 2), mh[:nmeas * mb].reshape(nmeas, mb)
+
     def fit_buckets(self):
         """(records, tuned warps per CTA, sample ms [k][1,2,4,8 warps]) per fit size class."""
         cnt = np.zeros(8, np.int64)
@@ -514,7 +569,8 @@ class JobData:
     def __init__(self, data, constraints=None, **steer):
         st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
                   dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
-                  mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0)
+                  mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0, monitor=0,
+                  monitorPulls=0, monitorBins=100)
         st.update(steer)
         self.steer = Steer(**st)
         self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)

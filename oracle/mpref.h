@@ -193,6 +193,13 @@ void mpref_avprd0(int32_t matsto, int32_t n, const double *x, double *b, int32_t
                   const int32_t *allIndexGroups, const int64_t *offsets,
                   const int32_t *columns, const double *matD);
 
+/* Monitoring of the first local-fit iteration (pede.f90:3938-3980,
+ * 4025-4032) for the following loopbf calls: hist[4 * (nbins + 2)]
+ * (residuals with/without globals, pulls with/without globals) and
+ * meas[numMeas * measBins] are incremented (caller zeroes them). */
+void mpref_set_monitor(int32_t on, int32_t pull, int32_t nbins, float range, int32_t measBins, int32_t mode,
+                       const int32_t *measIndex, const double *measRes, int64_t *hist, int64_t *meas);
+
 /* MINRES (Paige & Saunders 1975) with a diagonal preconditioner (precons
  * with no constraint blocks, mpnum.f90:2881-3080) on the QL-reduced sparse
  * system (avprod, pede.f90:5331-5358).  Returns istop; *itn iterations. */

@@ -46,6 +46,38 @@ float mpref_chindl(int32_t n, int32_t nd)
 }
 
 /* addsums, pede.f90:11666-11697 (single accumulator) */
+/* monitoring of the first local-fit iteration (pede.f90:3938-3980,
+ * 4025-4032): the histograms of the device monitor, filled with the same
+ * arithmetic; set by mpref_set_monitor (tests only) */
+static struct {
+    int32_t on, pull, nbins, measBins, mode;
+    float range;
+    const int32_t *measIndex;
+    const double *measRes;
+    int64_t *hist, *meas;
+} g_mon;
+
+void mpref_set_monitor(int32_t on, int32_t pull, int32_t nbins, float range, int32_t measBins, int32_t mode,
+                       const int32_t *measIndex, const double *measRes, int64_t *hist, int64_t *meas)
+{
+    g_mon.on = on; g_mon.pull = pull; g_mon.nbins = nbins; g_mon.range = range;
+    g_mon.measBins = measBins; g_mon.mode = mode; g_mon.measIndex = measIndex;
+    g_mon.measRes = measRes; g_mon.hist = hist; g_mon.meas = meas;
+}
+
+static void mon_hist(int h, float x)
+{
+    int b;
+    if (!(x == x)) return;
+    if (x < -g_mon.range) b = 0;
+    else if (x >= g_mon.range) b = g_mon.nbins + 1;
+    else {
+        b = 1 + (int)((x + g_mon.range) * ((float)g_mon.nbins / (2.0f * g_mon.range)));
+        if (b > g_mon.nbins) b = g_mon.nbins;
+    }
+    __atomic_fetch_add(&g_mon.hist[h * (g_mon.nbins + 2) + b], 1, __ATOMIC_RELAXED);
+}
+
 static void addsums(mpref_fitout *o, double chi2, int32_t ndf, double dw)
 {
     double add = chi2 * dw;
@@ -438,6 +470,38 @@ static int fit_record(const ctx_t *c, int64_t r, scratch *s, double *gvec, int64
             }
             s->lcor[ieq] = rmloc;
             rmeas = rmeas - rmloc;
+            if (g_mon.on && iter == 1) {
+                const int withGlobal = startGlobal < s->eqE[ieq];
+                mon_hist(withGlobal ? 0 : 1, (float)(rmeas / rerr));
+                if (g_mon.pull && (mbnd < 0 || nrank == nalc)) {
+                    double dvar = 0.0;
+                    for (j = 1; j <= startGlobal - startLocal - 1; j++) {
+                        int32_t ij = inder[startLocal + j];
+                        int32_t jk = (ij * ij - ij) / 2;
+                        for (k = 1; k <= j - 1; k++) {
+                            int32_t ik = inder[startLocal + k];
+                            dvar = dvar + clmat[jk + ik] * glder[startLocal + j] * glder[startLocal + k] * 2.0;
+                        }
+                        dvar = dvar + clmat[jk + ij] * glder[startLocal + j] * glder[startLocal + j];
+                    }
+                    if (0.999999 / wght > dvar) {
+                        double pull = rmeas / sqrt(1.0 / wght - dvar);
+                        mon_hist(withGlobal ? 2 : 3, (float)pull);
+                        if (withGlobal && g_mon.measIndex) {
+                            int32_t g = g_mon.measIndex[inder[startGlobal + 1] - 1];
+                            if (g > 0) {
+                                double half = 0.5 * (double)g_mon.measBins;
+                                double x = g_mon.mode == 0 ? pull * rerr / g_mon.measRes[g - 1] / 0.1 + half
+                                                           : pull / 0.1 + half;
+                                int irbin = x == x ? (int)x : 1;
+                                irbin = irbin < 1 ? 1 : (irbin > g_mon.measBins ? g_mon.measBins : irbin);
+                                __atomic_fetch_add(&g_mon.meas[(int64_t)(g - 1) * g_mon.measBins + irbin - 1], 1,
+                                                   __ATOMIC_RELAXED);
+                            }
+                        }
+                    }
+                }
+            }
             double dchi2 = wght * rmeas * rmeas;
             double resid = rmeas;
             if (o->nloopn != 1 && iter != 1 && o->lhuber != 0) {

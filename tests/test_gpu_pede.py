@@ -13,9 +13,9 @@ def gpu_job(mp, orc, d, steer, struct_device=0, **jobkw):
     job, keep = orc.make_job(d, **jobkw)
     cap = len(d["inder"]) + 16
     res, kr = orc.make_result(cap, cls=mp.Result)
-    st = mp.Steer(**{f: getattr(steer, f) for f, _ in mp.Steer._fields_ if f != "structDevice"})
+    st = mp.Steer(**{f: getattr(steer, f) for f, _ in mp.Steer._fields_ if f not in ("structDevice", "monitor", "monitorPulls", "monitorBins")})
     st.structDevice = struct_device
-    jb = mp.Job(**{f: getattr(job, f) for f, _ in mp.Job._fields_})
+    jb = mp.Job(**{f: getattr(job, f) for f, _ in mp.Job._fields_ if f != "monPath"})
     rc = mp.lib().mpgpu_pede_run(None, C.byref(st), C.byref(jb), C.byref(res))
     n = res.nTotal
     return dict(rc=rc, labels=kr.labels[:n].copy(), parameter=kr.parameter[:n].copy(),
