@@ -246,10 +246,11 @@ typedef struct mpgpu_solveinfo {
     int32_t nrank;      /* rank found by inversion / decomposition */
     int32_t itn;        /* MINRES iterations */
     int32_t istop;      /* MINRES stop reason */
-    int32_t pad;
+    int32_t nrkd;       /* band preconditioner: lltdec's rank-deficit code */
     double evmin, evmax;  /* decomposition pivot range */
     double ms;          /* device time of the solve */
-    double msFactor;    /* dense solves: device time of the factorisation */
+    double msFactor;    /* dense solves: device time of the factorisation; MINRES: of the
+                           preconditioner set-up */
     double msRefine;    /* dense solves: device time of the CG refinement */
 } mpgpu_solveinfo;
 
@@ -274,6 +275,25 @@ typedef struct mpgpu_solveinfo {
 int32_t mpgpu_solve(mpgpu_ctx *ctx, int32_t metsol, const double *consResiduals,
                     double rtol, int32_t itnlim, double *correction, double *errors,
                     mpgpu_solveinfo *info);
+
+/* Preconditioner of MINRES / MINRES-QLP (pede's "bandwidth mbandw lprecm",
+ * pede.f90:10495-10503, used in mminrs/mminrsqlp 8292-8316): mbandw < 0
+ * none, 0 the diagonal (default, precons), 1..MPGPU_BAND_WIDTH_MAX the
+ * variable-band Cholesky factor of the band of Q^T A Q (equdecs/equslvs with
+ * the constraints eliminated, mpnum.f90:2486-2678); lprecm > 0 is lltdec's
+ * skyline option (a dependent row keeps the root of its own diagonal).
+ * Kept by the context for the following solves; wider bands return
+ * MPGPU_ERR_LIMIT from the solve. */
+#define MPGPU_BAND_WIDTH_MAX 32
+int32_t mpgpu_set_preconditioner(mpgpu_ctx *ctx, int32_t mbandw, int32_t lprecm);
+
+/* The band preconditioner alone (equdecs on matPreCond): the band of
+ * width mbandw > 0 of Q^T A Q of the current matrix factorised by lltdec,
+ * written to c in pede's variable-band layout (indPreCond, pede.f90:
+ * 7705-7717: rows 1..mbandw triangular, then mbandw per row, the diagonal
+ * last in each row and replaced by 1/sqrt) for the nVar - ncon fit
+ * parameters; *nrkd receives lltdec's rank-deficit code. */
+int32_t mpgpu_band_factor(mpgpu_ctx *ctx, int32_t mbandw, int32_t lprecm, double *c, int32_t *nrkd);
 
 /* Page-lock (register) / release a caller-owned host buffer so that the
  * uploads from it run at full host-device bandwidth. */
@@ -325,6 +345,9 @@ typedef struct mpgpu_steer {
                              bit 1 after the last, < 0 after every loop; 0 off */
     int32_t monitorPulls; /* imonmd: 1 pulls (monitorpulls), 0 normalised residuals */
     int32_t monitorBins;  /* measBins, bins of 0.1 per group histogram (>= 2, pede's 100) */
+    int32_t mbandw;       /* MINRES preconditioner (mpgpu_set_preconditioner): < 0 none,
+                             0 diagonal, > 0 band width */
+    int32_t lprecm;       /* lltdec skyline option of the band preconditioner */
 } mpgpu_steer;
 
 typedef struct mpgpu_job {

@@ -17,9 +17,10 @@ ORACLE_BUILD = os.path.join(ORACLE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-ffp-contract=off"]
-# the local-fit unit keeps the reference's separate multiply and add so that
-# record decisions are bit-identical; fused products are requested explicitly
-PER_FILE = {"mpgpu_fit.cu": ["-fmad=false"]}
+# the local-fit and preconditioner units keep the reference's separate
+# multiply and add so that record decisions and the band factor are
+# bit-identical; fused products are requested explicitly
+PER_FILE = {"mpgpu_fit.cu": ["-fmad=false"], "mpgpu_precond.cu": ["-fmad=false"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread"]
 
 

@@ -530,6 +530,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     int64_t nrejTot = 0;
     std::memset(res->nrej, 0, sizeof(res->nrej));
     res->msBuild = res->msSolve = 0.0;
+    if (!rc && (st->metsol == 4 || st->metsol == 5)) rc = mpgpu_set_preconditioner(ctx, st->mbandw, st->lprecm);
     for (int32_t iter = 1; !rc && iter <= st->mitera; ++iter) {
         const int32_t nloopn = iter;
         if (nloopn > 1) {

@@ -75,7 +75,7 @@ void free_layout(DevJob &j) {
 }
 
 void free_constraints(DevJob &j) {
-    dfree(j.qlV); dfree(j.qlVk); dfree(j.qlR2);
+    dfree(j.qlV); dfree(j.qlVk); dfree(j.qlR2); dfree(j.qlT);
     j.ncon = 0;
 }
 
@@ -269,7 +269,33 @@ extern "C" int32_t mpgpu_set_constraints(mpgpu_ctx *c, int32_t ncon, const doubl
         if (L[(size_t)k * ncon + k] == 0.0) return set_err(c, MPGPU_ERR_QL, "singular constraints");
     j.ncon = ncon;
     j.hV = V; j.hVk = Vk; j.hL = L; j.hR1 = r1; j.hR2 = r2;
+    // compact WY form of the reflections (Schreiber & Van Loan 1989):
+    // H_1 H_2 ... H_m = I - U T U^T with u_k = (V_k, Vk_k at kn_k), T upper
+    // triangular, T_kk = 2, T(0:k, k) = -2 T(0:k, 0:k) U(:, 0:k)^T u_k; the
+    // Gram matrix U^T U from the vectors' common support
+    std::vector<double> G((size_t)ncon * ncon), T((size_t)ncon * ncon, 0.0);
+    auto kn0 = [&](int32_t k) { return npar - ncon + k; };  // 0-based position of Vk_k
+    for (int32_t a = 0; a < ncon; ++a)
+        for (int32_t b = a; b < ncon; ++b) {
+            const double *va = &V[(size_t)a * npar], *vb = &V[(size_t)b * npar];
+            double g = 0.0;
+            const int32_t lim = std::min(kn0(a), kn0(b));
+            for (int32_t q = 0; q < lim; ++q) g += va[q] * vb[q];
+            // the Vk entries: u_a at kn0(a) meets u_b there (V row of b or Vk_b)
+            g += Vk[a] * (kn0(a) == kn0(b) ? Vk[b] : (kn0(a) < kn0(b) ? vb[kn0(a)] : 0.0));
+            if (kn0(b) < kn0(a)) g += Vk[b] * va[kn0(b)];
+            G[(size_t)a * ncon + b] = G[(size_t)b * ncon + a] = g;
+        }
+    for (int32_t k = 0; k < ncon; ++k) {
+        T[(size_t)k * ncon + k] = 2.0;
+        for (int32_t r = 0; r < k; ++r) {
+            double acc = 0.0;
+            for (int32_t cc = r; cc < k; ++cc) acc += T[(size_t)r * ncon + cc] * G[(size_t)cc * ncon + k];
+            T[(size_t)r * ncon + k] = -2.0 * acc;
+        }
+    }
     cudaStream_t s = c->stream;
+    MPG_CUDA(c, dupload(j.qlT, T.data(), (int64_t)ncon * ncon, s));
     MPG_CUDA(c, dupload(j.qlV, V.data(), (int64_t)ncon * npar, s));
     MPG_CUDA(c, dupload(j.qlVk, Vk.data(), ncon, s));
     MPG_CUDA(c, dupload(j.qlR2, r2.data(), ncon, s));
@@ -802,6 +828,23 @@ extern "C" int32_t mpgpu_solve(mpgpu_ctx *c, int32_t metsol, const double *consR
     if (metsol == 4 || metsol == 5)
         return solve_minres(c, consResiduals, rtol, itnlim, correction, info, metsol == 5);
     return set_err(c, MPGPU_ERR_ARG, "unsupported solution method");
+}
+
+extern "C" int32_t mpgpu_set_preconditioner(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm) {
+    if (!c) return MPGPU_ERR_ARG;
+    if (mbandw > MPGPU_BAND_WIDTH_MAX) return set_err(c, MPGPU_ERR_LIMIT, "band preconditioner wider than 32");
+    c->mbandw = mbandw < 0 ? -1 : mbandw;
+    c->lprecm = lprecm;
+    return MPGPU_OK;
+}
+
+extern "C" int32_t mpgpu_band_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double *cOut, int32_t *nrkd) {
+    if (!c || !cOut || !nrkd) return MPGPU_ERR_ARG;
+    if (mbandw <= 0 || mbandw > MPGPU_BAND_WIDTH_MAX)
+        return set_err(c, MPGPU_ERR_LIMIT, "band width outside 1..32");
+    if (!c->j.matD) return set_err(c, MPGPU_ERR_ARG, "no matrix");
+    cudaSetDevice(c->device);
+    return band_precond_factor(c, mbandw, lprecm, cOut, nrkd);
 }
 
 extern "C" int32_t mpgpu_avprod(mpgpu_ctx *c, int32_t n, const double *x, double *b) {

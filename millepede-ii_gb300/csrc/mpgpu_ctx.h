@@ -148,6 +148,7 @@ struct DevJob {
     double *qlV = nullptr;         // [ncon*nVar] Householder vectors (row k)
     double *qlVk = nullptr;        // [ncon]
     int32_t *qlR2 = nullptr;       // [ncon] last non-zero index of each vector
+    double *qlT = nullptr;         // [ncon*ncon] compact WY factor: H_1 ... H_m = I - U T U^T
     std::vector<double> hL;        // [ncon*ncon] lower triangle L (host)
     std::vector<double> hV, hVk;
     std::vector<int32_t> hR1, hR2;
@@ -195,7 +196,31 @@ struct mpgpu_ctx {
     double *scal = nullptr;      // small device scalar area
     double *hscal = nullptr;     // pinned mirror
     int64_t lastNaccepted = 0;
+    int32_t mbandw = 0;          // MINRES preconditioner: < 0 none, 0 diagonal, > 0 band width
+    int32_t lprecm = 0;          // lltdec option of the band preconditioner
 };
+
+// variable-band preconditioner of MINRES (mpgpu_precond.cu): band of
+// Q^T A Q over nVar rows (B), its lltdec factor over the nfit rows (F by
+// rows, Fc by columns), the block spikes (G, H: nfit x w) and the
+// per-block coupling values (T, Hd)
+#define MPGPU_BAND_MAX 32
+struct BandPre {
+    int32_t n = 0, w = 0, s = 0, p = 0;  // rows, lower width, rows per block, blocks
+    double *B = nullptr, *F = nullptr, *Fc = nullptr, *G = nullptr, *H = nullptr, *T = nullptr, *Hd = nullptr;
+    int32_t *nrkd = nullptr;
+};
+int32_t band_alloc(BandPre &P, int32_t nVar, int32_t nfit, int32_t w);
+void band_free(BandPre &P);
+cudaError_t band_fill(const BandPre &P, int32_t nVar, int32_t matsto, const double *matD, const int32_t *aig,
+                      const int32_t *p2g, const int64_t *rowStart, const int32_t *bcol, const int64_t *boff,
+                      const int32_t *bld, cudaStream_t s);
+cudaError_t band_reflect(const BandPre &P, int32_t nVar, const double *v, const double *y, const double *beta,
+                         cudaStream_t s);
+cudaError_t band_factor(const BandPre &P, int32_t lprecm, cudaStream_t s);
+// y := (L L^T)^-1 y on the nfit rows; nothing when *done is set
+cudaError_t band_solve(const BandPre &P, const int *done, double *y, cudaStream_t s);
+int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double *cOut, int32_t *nrkd);
 
 // Device allocation that keeps its capacity between uploads and loops (no
 // free / alloc when the next request fits).

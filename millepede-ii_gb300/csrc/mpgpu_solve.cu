@@ -82,6 +82,76 @@ __global__ void k_qlapply(double *x, const double *V, const double *Vk, const in
     }
 }
 
+// qlmlq in the compact WY form: Q^T x = x - U T (U^T x), Q x = x - U T^T
+// (U^T x), U = the reflection vectors (rows of V with Vk at position
+// npar - ncon + k).  Pass 1: per CTA the partial products of eight vectors
+// at a time over a fixed row partition; pass 2 (one CTA): the sums in CTA
+// order plus the Vk terms, then t = T s or T^T s; pass 3: x -= U t.
+constexpr int kWyBlocks = 304;
+
+__global__ void __launch_bounds__(256) k_wy_dots(int32_t n, int32_t m, const double *V, const double *x,
+                                                  double *part) {
+    __shared__ double sh[8][8];
+    const int ln = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int32_t k0 = 0; k0 < m; k0 += 8) {
+        const int kc = min(8, m - k0);
+        double acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            const double xi = x[i];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q < kc) acc[q] += V[(int64_t)(k0 + q) * n + i] * xi;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            double v = acc[q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (ln == 0) sh[q][wib] = v;
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < kc) {
+            double v = 0.0;
+            for (int w8 = 0; w8 < (int)(blockDim.x >> 5); ++w8) v += sh[threadIdx.x][w8];
+            part[(int64_t)blockIdx.x * m + k0 + threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_wy_coef(int32_t n, int32_t m, int32_t nblk, const double *part, const double *Vk,
+                          const double *T, const double *x, int transT, double *tv) {
+    extern __shared__ double sv[];
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nblk; ++b) s += part[(int64_t)b * m + k];
+        sv[k] = s + Vk[k] * x[n - m + k];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        double t = 0.0;
+        if (transT)
+            for (int c = 0; c <= k; ++c) t += T[(int64_t)c * m + k] * sv[c];
+        else
+            for (int c = k; c < m; ++c) t += T[(int64_t)k * m + c] * sv[c];
+        tv[k] = t;
+    }
+}
+
+__global__ void k_wy_apply(int32_t n, int32_t m, const double *V, const double *Vk, const double *tv, double *x) {
+    extern __shared__ double st[];
+    for (int k = threadIdx.x; k < m; k += blockDim.x) st[k] = tv[k];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double a = 0.0;
+        for (int k = 0; k < m; ++k) a += V[(int64_t)k * n + i] * st[k];
+        const int64_t kk = i - (n - m);
+        if (kk >= 0) a += Vk[kk] * st[kk];
+        x[i] -= a;
+    }
+}
+
 // ---------------------------------------------------------------- packed products
 // y = A x for the packed symmetric matrix in two deterministic passes.
 // Pass 1, one CTA per block of 64 rows: the lower part of each row (one
@@ -343,8 +413,20 @@ struct SparseBlocks {
     int64_t *tOff = nullptr;       // transposed-product buffer offset (off-diagonal blocks)
     int64_t *colStart = nullptr;   // [nG+1] incoming blocks of column group J
     int64_t *colBlk = nullptr;     // block ids ordered by (J, I)
+    int64_t *tBase = nullptr;      // [nG] first transposed product of column group J
     double *tbuf = nullptr;
     int64_t tlen = 0;
+    bool smallGroups = false;     // every group has at most kSmallGroup parameters
+    // small groups: the blocks of a row group in work items of at most
+    // kItemBlocks blocks (one warp each, partial row sums in rowPart), the
+    // transposed products of column group J stored parameter-major (stride
+    // = its incoming block count, tStr per block)
+    int64_t nItem = 0;
+    int32_t *itemGroup = nullptr;  // [nItem] row group
+    int64_t *itemB0 = nullptr;     // [nItem+1] first block (items of a group are consecutive)
+    int64_t *itemBeg = nullptr;    // [nG+1] first item of row group I
+    int32_t *tStr = nullptr;       // [nblk] stride of the block's transposed products
+    double *rowPart = nullptr;     // [nItem * kSmallGroup]
 };
 
 // phase 1: warp per row group I: y_I = D_I x_I + sum_J A_IJ x_J, the
@@ -402,6 +484,124 @@ __global__ void k_spmv_cols(int32_t nG, const int32_t *aig, const int64_t *colSt
             double s = y[ja + jj];
             for (int64_t q = colStart[J - 1]; q < colStart[J]; ++q) s += tbuf[tOff[colBlk[q]] + jj];
             y[ja + jj] = s;
+        }
+    }
+}
+
+// the same two phases for row groups of at most 8 parameters.  Phase 1, one
+// warp per work item (at most kItemBlocks blocks of one row group): one lane
+// per block with its rows and columns in registers; the item's partial row
+// sums reduced over the lanes by a fixed shuffle tree into rowPart, the
+// transposed products of each block into tbuf (parameter-major per column
+// group).  Phase 2, one warp per group: y = D x + the row parts of the
+// group's items in item order + the transposed products summed over its
+// incoming blocks (lanes over blocks, fixed tree).
+constexpr int kSmallGroup = 8;
+constexpr int kItemBlocks = 64;
+
+__global__ void __launch_bounds__(256) k_spmv_items(int64_t nItem, const int32_t *itemGroup, const int64_t *itemB0,
+                                                    const int32_t *aig, const int32_t *bcol, const int64_t *boff,
+                                                    const int32_t *bld, const int64_t *tOff, const int32_t *tStr,
+                                                    const double *matD, const double *x, double *tbuf,
+                                                    double *rowPart) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t it = w; it < nItem; it += nw) {
+        const int32_t I = itemGroup[it];
+        const int32_t ia = aig[I - 1] - 1, np = aig[I] - 1 - ia;
+        double xi[kSmallGroup], sr[kSmallGroup];
+#pragma unroll
+        for (int ii = 0; ii < kSmallGroup; ++ii) {
+            xi[ii] = ii < np ? x[ia + ii] : 0.0;
+            sr[ii] = 0.0;
+        }
+        const int64_t b0 = itemB0[it], b1 = itemB0[it + 1];
+        int64_t bdiag = -1;
+        for (int64_t bl = b0 + ln; bl < b1; bl += 32) {
+            const int32_t J = bcol[bl];
+            if (J == I) { bdiag = bl; continue; }
+            const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
+            const double *blk = matD + boff[bl];
+            const int32_t ld = bld[bl];
+            double xj[kSmallGroup], tc[kSmallGroup];
+#pragma unroll
+            for (int jj = 0; jj < kSmallGroup; ++jj) {
+                xj[jj] = jj < nj ? x[ja + jj] : 0.0;
+                tc[jj] = 0.0;
+            }
+#pragma unroll
+            for (int ii = 0; ii < kSmallGroup; ++ii) {
+                if (ii < np) {
+#pragma unroll
+                    for (int jj = 0; jj < kSmallGroup; ++jj) {
+                        if (jj < nj) {
+                            const double a = blk[(int64_t)ii * ld + jj];
+                            sr[ii] += a * xj[jj];
+                            tc[jj] += a * xi[ii];
+                        }
+                    }
+                }
+            }
+            double *tb = tbuf + tOff[bl];
+            const int32_t st = tStr[bl];
+#pragma unroll
+            for (int jj = 0; jj < kSmallGroup; ++jj)
+                if (jj < nj) tb[(int64_t)jj * st] = tc[jj];
+        }
+        // the diagonal block's strictly-lower elements, both triangles
+        const int64_t bd = (int64_t)__reduce_max_sync(0xffffffffu, bdiag >= 0 ? (unsigned)(bdiag - b0 + 1) : 0u) - 1;
+        if (bd >= 0) {
+            const double *blk = matD + boff[b0 + bd];
+            const int32_t ld = bld[b0 + bd];
+            const int ne = np * (np - 1) / 2;
+            for (int e = ln; e < ne; e += 32) {
+                int ii = 1, base = 0;
+                while (base + ii <= e) { base += ii; ++ii; }
+                const int jj = e - base;
+                const double a = blk[(int64_t)ii * ld + jj];
+                double xa = 0.0, xb = 0.0;
+#pragma unroll
+                for (int q = 0; q < kSmallGroup; ++q) {
+                    if (q == jj) xa = xi[q];
+                    if (q == ii) xb = xi[q];
+                }
+#pragma unroll
+                for (int q = 0; q < kSmallGroup; ++q) {
+                    if (q == ii) sr[q] += a * xa;
+                    if (q == jj) sr[q] += a * xb;
+                }
+            }
+        }
+#pragma unroll
+        for (int ii = 0; ii < kSmallGroup; ++ii) {
+            double v = sr[ii];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (ln == 0) rowPart[it * kSmallGroup + ii] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_spmv_groups(int32_t nG, const int32_t *aig, const int64_t *itemBeg,
+                                                     const double *rowPart, const int64_t *colStart,
+                                                     const int64_t *tBase, const double *tbuf,
+                                                     const double *matD, const double *x, double *y) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t J = 1 + w; J <= nG; J += nw) {
+        const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
+        const int64_t cnt = colStart[J] - colStart[J - 1];
+        const double *t = tbuf + tBase[J - 1];
+        for (int jj = 0; jj < nj; ++jj) {
+            double v = 0.0;
+            for (int64_t q = ln; q < cnt; q += 32) v += t[(int64_t)jj * cnt + q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (ln == 0) {
+                double r = matD[ja + jj] * x[ja + jj];
+                for (int64_t it = itemBeg[J - 1]; it < itemBeg[J]; ++it) r += rowPart[it * kSmallGroup + jj];
+                y[ja + jj] = r + v;
+            }
         }
     }
 }
@@ -679,6 +879,11 @@ __global__ void k_sparse_diag(int32_t n, const double *matD, double *dg) {
         dg[i] = matD[i];
 }
 
+__global__ void k_fill(int32_t n, double v, double *a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
 __global__ void k_sub(int32_t n, double *a, const double *b) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         a[i] = a[i] - b[i];
@@ -696,8 +901,10 @@ struct Solver {
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
     }
     ~Solver() {
+        dfree(wyPart); dfree(wyT);
         dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
-        dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tbuf); dfree(part);
+        dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tBase); dfree(sb.tbuf); dfree(part);
+        dfree(sb.tStr); dfree(sb.itemGroup); dfree(sb.itemB0); dfree(sb.itemBeg); dfree(sb.rowPart);
         dfree(pmvRow); dfree(pmvPart);
     }
     unsigned grid(int64_t n, int per = kThreads) const {
@@ -711,15 +918,18 @@ struct Solver {
     // packed symmetric product (two passes; buffers kept for the solve)
     double *pmvRow = nullptr, *pmvPart = nullptr;
     int64_t pmvN = 0;
+    void alloc_pmv(int32_t n) {
+        if (pmvN == n) return;
+        const int64_t nb = ((int64_t)n + kMvRows - 1) / kMvRows;
+        dfree(pmvRow);
+        dfree(pmvPart);
+        cudaMalloc(&pmvRow, sizeof(double) * std::max<int64_t>(n, 1));
+        cudaMalloc(&pmvPart, sizeof(double) * std::max<int64_t>(nb * n, 1));
+        pmvN = n;
+    }
     void packed_matvec(int32_t n, const double *A, const double *x, double *y) {
         const int64_t nb = ((int64_t)n + kMvRows - 1) / kMvRows;
-        if (pmvN != n) {
-            dfree(pmvRow);
-            dfree(pmvPart);
-            cudaMalloc(&pmvRow, sizeof(double) * std::max<int64_t>(n, 1));
-            cudaMalloc(&pmvPart, sizeof(double) * std::max<int64_t>(nb * n, 1));
-            pmvN = n;
-        }
+        alloc_pmv(n);
         k_pmv_blocks<<<(unsigned)nb, 256, 0, s>>>(n, A, x, pmvRow, pmvPart);
         k_pmv_final<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nb, pmvRow, pmvPart, y);
     }
@@ -788,6 +998,45 @@ struct Solver {
         std::vector<int64_t> fill(colStart.begin(), colStart.end() - 1), colBlk(std::max<int64_t>(colStart[j.nG], 1));
         for (int64_t b = 0; b < nb; ++b)
             if (bcol[b] != brow[b]) colBlk[fill[bcol[b] - 1]++] = b;
+        int32_t maxnp = 0;
+        for (int32_t I = 1; I <= j.nG; ++I) maxnp = std::max(maxnp, aig[I] - aig[I - 1]);
+        sb.smallGroups = maxnp <= kSmallGroup && nb < (int64_t)0xffffffff;
+        // transposed products stored by column group, incoming blocks in row
+        // group order: block after block (general kernels) or parameter-major
+        // with the group's block count as stride (small groups)
+        std::vector<int64_t> tBase(std::max(j.nG, 1));
+        std::vector<int32_t> tStr(std::max<int64_t>(nb, 1), 1);
+        {
+            int64_t off = 0;
+            for (int32_t J = 1; J <= j.nG; ++J) {
+                tBase[J - 1] = off;
+                const int32_t nj = aig[J] - aig[J - 1];
+                const int64_t cnt = colStart[J] - colStart[J - 1];
+                for (int64_t q = colStart[J - 1]; q < colStart[J]; ++q) {
+                    const int64_t r = q - colStart[J - 1];
+                    tOff[colBlk[q]] = sb.smallGroups ? off + r : off + r * nj;
+                    tStr[colBlk[q]] = (int32_t)cnt;
+                }
+                off += cnt * nj;
+            }
+        }
+        // work items of at most kItemBlocks blocks per row group
+        std::vector<int32_t> itemGroup;
+        std::vector<int64_t> itemB0, itemBeg(j.nG + 1, 0);
+        for (int32_t I = 1; I <= j.nG; ++I) {
+            itemBeg[I - 1] = (int64_t)itemGroup.size();
+            for (int64_t b = rowStart[I - 1]; b < rowStart[I] || b == rowStart[I - 1]; b += kItemBlocks) {
+                itemGroup.push_back(I);
+                itemB0.push_back(b);
+                if (rowStart[I] == rowStart[I - 1]) break;
+            }
+        }
+        itemBeg[j.nG] = (int64_t)itemGroup.size();
+        // item ends: the next item's start, or the group's end
+        std::vector<int64_t> itemB(itemB0.size() + 1);
+        for (size_t q = 0; q < itemB0.size(); ++q) itemB[q] = itemB0[q];
+        itemB[itemB0.size()] = nb;
+        sb.nItem = (int64_t)itemGroup.size();
         sb.nblk = nb;
         sb.tlen = tl;
         auto up = [&](auto *&d, const auto &h) -> cudaError_t {
@@ -802,13 +1051,27 @@ struct Solver {
         MPG_CUDA(c, up(sb.tOff, tOff));
         MPG_CUDA(c, up(sb.colStart, colStart));
         MPG_CUDA(c, up(sb.colBlk, colBlk));
+        MPG_CUDA(c, up(sb.tBase, tBase));
+        if (sb.smallGroups) {
+            MPG_CUDA(c, up(sb.tStr, tStr));
+            MPG_CUDA(c, up(sb.itemGroup, itemGroup));
+            MPG_CUDA(c, up(sb.itemB0, itemB));
+            MPG_CUDA(c, up(sb.itemBeg, itemBeg));
+            MPG_CUDA(c, cudaMalloc((void **)&sb.rowPart, sizeof(double) * std::max<int64_t>(sb.nItem, 1) * kSmallGroup));
+        }
         MPG_CUDA(c, cudaMalloc((void **)&sb.tbuf, sizeof(double) * std::max<int64_t>(tl, 1)));
         return MPGPU_OK;
     }
 
     // y = A x (full parameter space)
     void avprd0(const double *x, double *y) {
-        if (j.matsto == 2) {
+        if (j.matsto == 2 && sb.smallGroups) {
+            k_spmv_items<<<wgrid(sb.nItem), kThreads, 0, s>>>(sb.nItem, sb.itemGroup, sb.itemB0, j.aig, sb.bcol,
+                                                              sb.boff, sb.bld, sb.tOff, sb.tStr, j.matD, x,
+                                                              sb.tbuf, sb.rowPart);
+            k_spmv_groups<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.itemBeg, sb.rowPart, sb.colStart,
+                                                           sb.tBase, sb.tbuf, j.matD, x, y);
+        } else if (j.matsto == 2) {
             k_spmv_rows<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.bcol, sb.boff, sb.bld,
                                                          sb.tOff, j.matD, x, y, sb.tbuf);
             k_spmv_cols<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.colStart, sb.colBlk, sb.tOff,
@@ -817,10 +1080,58 @@ struct Solver {
             packed_matvec(j.nVar, j.matD, x, y);
         }
     }
+    // the reflections of qlssq in its order (k = m..1): v = v_k, yk =
+    // P^T A P v_k with P = H_m ... H_{k+1}, *dsc = v.yk; apply() after each
+    template <class Fn>
+    void reflections(double *v, double *tmp, double *yk, double *dsc, Fn &&apply) {
+        const int32_t n = j.nVar, ncon = j.ncon;
+        for (int k = ncon; k >= 1; --k) {
+            const int kn = n + k - ncon;
+            const double *vr = j.qlV + (int64_t)(k - 1) * n;
+            k_vec_with_kn<<<grid(n), kThreads, 0, s>>>(vr, j.hR2[k - 1], j.hVk[k - 1], kn, n, v);
+            cudaMemcpyAsync(tmp, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+            if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(tmp, j.qlV, j.qlVk, j.qlR2, n, ncon, k + 1, ncon, 1);
+            avprd0(tmp, yk);
+            if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(yk, j.qlV, j.qlVk, j.qlR2, n, ncon, ncon, k + 1, -1);
+            dot(v, yk, n, part, dsc, s);
+            apply();
+        }
+    }
+    // band of Q^T A Q (pede's preconditioner fill and qlpssq with band
+    // width mbandw) and its lltdec factor with the block spikes
+    int32_t band_build(BandPre &P, int32_t mbandw, int32_t lprecm, double *v, double *tmp, double *yk,
+                       double *dsc) {
+        const int32_t n = j.nVar, nfit = j.nVar - j.ncon;
+        if (mbandw > MPGPU_BAND_MAX) return set_err(c, MPGPU_ERR_LIMIT, "band preconditioner wider than 32");
+        if (band_alloc(P, n, nfit, mbandw - 1)) return set_err(c, MPGPU_ERR_ALLOC, "band preconditioner");
+        MPG_CUDA(c, band_fill(P, n, j.matsto, j.matD, j.aig, j.p2g, sb.rowStart, sb.bcol, sb.boff, sb.bld, s));
+        cudaError_t e = cudaSuccess;
+        reflections(v, tmp, yk, dsc, [&] {
+            if (e == cudaSuccess) e = band_reflect(P, n, v, yk, dsc, s);
+        });
+        MPG_CUDA(c, e);
+        MPG_CUDA(c, band_factor(P, lprecm, s));
+        return MPGPU_OK;
+    }
+    // qlmlq (mpqldec.f90:404-454): t = 1 Q^T x (reflections ncon..1), t = 0
+    // Q x (1..ncon), in the compact WY form
+    double *wyPart = nullptr, *wyT = nullptr;
     void qlmlq(double *x, int t) {
         if (j.ncon <= 0) return;
-        if (t) k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, j.nVar, j.ncon, j.ncon, 1, -1);
-        else k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, j.nVar, j.ncon, 1, j.ncon, 1);
+        const int32_t m = j.ncon, n = j.nVar;
+        if (m > 4096) {  // coefficients beyond the shared memory of one CTA
+            if (t) k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, n, m, m, 1, -1);
+            else k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, n, m, 1, m, 1);
+            return;
+        }
+        if (!wyPart) {
+            cudaMalloc(&wyPart, sizeof(double) * (size_t)kWyBlocks * m);
+            cudaMalloc(&wyT, sizeof(double) * m);
+        }
+        const int nb = (int)std::min<int64_t>(kWyBlocks, std::max<int64_t>(1, n / 512));
+        k_wy_dots<<<nb, 256, 0, s>>>(n, m, j.qlV, x, wyPart);
+        k_wy_coef<<<1, 256, sizeof(double) * m, s>>>(n, m, nb, wyPart, j.qlVk, j.qlT, x, t ? 0 : 1, wyT);
+        k_wy_apply<<<grid(n), kThreads, sizeof(double) * m, s>>>(n, m, j.qlV, j.qlVk, wyT, x);
     }
 };
 
@@ -1007,23 +1318,29 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
         k_sub<<<S.grid(n), kThreads, 0, s>>>(n, rhs, ba);
         S.qlmlq(rhs, 1);
     }
-    // preconditioner: diagonal of Q^T A Q (the band-width-1 case of qlpssq,
-    // mpqldec.f90:711-950), reflections in the order of qlssq (k = m..1):
-    // y = P^T A P v_k with P = H_m ... H_{k+1}, dg -= 4 v y - 4 (v.y) v^2
-    if (j.matsto == 2) k_sparse_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
-    else k_get_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
-    for (int k = ncon; k >= 1; --k) {
-        const int kn = n + k - ncon;
-        const double *vr = j.qlV + (int64_t)(k - 1) * n;
-        k_vec_with_kn<<<S.grid(n), kThreads, 0, s>>>(vr, j.hR2[k - 1], j.hVk[k - 1], kn, n, v);
-        MPG_CUDA(c, cudaMemcpyAsync(tmp, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-        if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(tmp, j.qlV, j.qlVk, j.qlR2, n, ncon, k + 1, ncon, 1);
-        S.avprd0(tmp, yk);
-        if (k < ncon) k_qlapply<<<1, 1024, 0, s>>>(yk, j.qlV, j.qlVk, j.qlR2, n, ncon, ncon, k + 1, -1);
-        dot(v, yk, n, S.part, dsc, s);
-        k_diag_update<<<S.grid(n), kThreads, 0, s>>>(n, dg, v, yk, dsc);
+    // preconditioner (pede.f90:8292-8316 by mbandw): < 0 none (M = I), 0
+    // the diagonal of Q^T A Q (the band-width-1 case of qlpssq,
+    // mpqldec.f90:711-950: dg -= 4 v y - 4 (v.y) v^2 per reflection), > 0
+    // the variable-band Cholesky factor of its band (equdecs/equslvs)
+    const int32_t mbandw = c->mbandw;
+    BandPre P;
+    struct BandGuard { BandPre &p; ~BandGuard() { band_free(p); } } bandGuard{P};
+    cudaEvent_t ep;
+    cudaEventCreate(&ep);
+    if (mbandw == 0) {
+        if (j.matsto == 2) k_sparse_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
+        else k_get_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
+        S.reflections(v, tmp, yk, dsc, [&] { k_diag_update<<<S.grid(n), kThreads, 0, s>>>(n, dg, v, yk, dsc); });
+        k_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, dg, cu);
+    } else {
+        k_fill<<<S.grid(nfit), kThreads, 0, s>>>(nfit, 1.0, cu);
+        if (mbandw > 0) {
+            int32_t rc = S.band_build(P, mbandw, c->lprecm, v, tmp, yk, dsc);
+            if (rc) { cudaEventDestroy(ep); return rc; }
+        }
     }
-    k_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, dg, cu);
+    cudaEventRecord(ep, s);
+    const int *doneFlag = &St->done;
     // MINRES state: x = 0, r1 = r2 = b, y = M^-1 r1, beta1 = sqrt(r1.y)
     MPG_CUDA(c, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
     MPG_CUDA(c, cudaMemsetAsync(w, 0, sizeof(double) * n, s));
@@ -1032,6 +1349,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     MPG_CUDA(c, cudaMemcpyAsync(r1, rhs, sizeof(double) * nfit, cudaMemcpyDeviceToDevice, s));
     MPG_CUDA(c, cudaMemcpyAsync(r2, rhs, sizeof(double) * nfit, cudaMemcpyDeviceToDevice, s));
     k_apply_precond<<<S.grid(nfit), kThreads, 0, s>>>(nfit, r1, cu, y);
+    if (mbandw > 0) MPG_CUDA(c, band_solve(P, nullptr, y, s));
     dot(r1, y, nfit, S.part, &St->dotv, s);
     k_mr_init<<<1, 32, 0, s>>>(St, rtol, itnlim);
     const double maxxnorm = (double)nfit / sqrt(2.220446049250313e-16);
@@ -1044,7 +1362,10 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     MinresState hs;
     int it = 0;
     const int batch = 16;
-    for (;;) {
+    // the iterations of one batch are recorded once as a CUDA graph and
+    // replayed (all scalars live on the device); direct launches if the
+    // capture is refused
+    auto batchBody = [&] {
         for (int q = 0; q < batch; ++q) {
             k_mr_scale_v<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, v);
             // y = (Q^T A Q v)(1:nfit)
@@ -1057,6 +1378,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
             dot(v, y, nfit, S.part, &St->dotv, s);
             k_mr_alfa<<<1, 32, 0, s>>>(St);
             k_mr_y2<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, r1, r2, cu);
+            if (mbandw > 0) band_solve(P, doneFlag, y, s);
             dot(r2, y, nfit, S.part, &St->dotv, s);
             if (!qlp) {
                 k_mr_rot<<<1, 32, 0, s>>>(St);
@@ -1071,6 +1393,25 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
                 k_qlp_commit<<<S.grid(nfit), kThreads, 0, s>>>(nfit, Qs, xc, x);
             }
         }
+    };
+    if (j.matsto != 2) S.alloc_pmv(n);  // no allocation while the graph is recorded
+    struct GraphGuard {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t e = nullptr;
+        ~GraphGuard() {
+            if (e) cudaGraphExecDestroy(e);
+            if (g) cudaGraphDestroy(g);
+        }
+    } gg;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        batchBody();
+        if (cudaStreamEndCapture(s, &gg.g) != cudaSuccess || cudaGraphInstantiate(&gg.e, gg.g, 0) != cudaSuccess)
+            gg.e = nullptr;
+        cudaGetLastError();
+    }
+    for (;;) {
+        if (gg.e) MPG_CUDA(c, cudaGraphLaunch(gg.e, s));
+        else batchBody();
         it += batch;
         MPG_CUDA(c, cudaMemcpyAsync(&hs, St, sizeof(MinresState), cudaMemcpyDeviceToHost, s));
         MPG_CUDA(c, cudaStreamSynchronize(s));
@@ -1088,8 +1429,12 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
     info->ms = ms;
+    cudaEventElapsedTime(&ms, e0, ep);
+    info->msFactor = ms;
+    if (mbandw > 0) cudaMemcpy(&info->nrkd, P.nrkd, sizeof(int32_t), cudaMemcpyDeviceToHost);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    cudaEventDestroy(ep);
     for (double *p : bufs) cudaFree(p);
     cudaFree(St);
     if (Qs) cudaFree(Qs);
@@ -1117,4 +1462,39 @@ int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b) {
     cudaFree(xa);
     cudaFree(ba);
     return MPGPU_OK;
+}
+
+// the band preconditioner alone (equdecs on pede's matPreCond): band of
+// Q^T A Q and its lltdec factor, returned in the variable-band layout of
+// indPreCond (pede.f90:7705-7717) for the nfit rows
+int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double *cOut, int32_t *nrkd) {
+    Solver S(c);
+    DevJob &j = c->j;
+    cudaStream_t s = c->stream;
+    const int32_t n = j.nVar, nfit = n - j.ncon;
+    if (mbandw <= 0) return set_err(c, MPGPU_ERR_ARG, "band width must be positive");
+    if (j.matsto == 2) {
+        int32_t rc = S.build_blocks();
+        if (rc) return rc;
+    }
+    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    double *v = nullptr, *tmp = nullptr, *yk = nullptr;
+    MPG_CUDA(c, cudaMalloc(&v, sizeof(double) * std::max(n, 1)));
+    MPG_CUDA(c, cudaMalloc(&tmp, sizeof(double) * std::max(n, 1)));
+    MPG_CUDA(c, cudaMalloc(&yk, sizeof(double) * std::max(n, 1)));
+    BandPre P;
+    int32_t rc = S.band_build(P, mbandw, lprecm, v, tmp, yk, c->scal + 300);
+    if (!rc) {
+        const int W1 = P.w + 1;
+        std::vector<double> F((size_t)std::max(nfit, 1) * W1);
+        cudaMemcpyAsync(F.data(), P.F, sizeof(double) * F.size(), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(nrkd, P.nrkd, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) rc = cuda_err(c, cudaGetLastError(), "band factor");
+        int64_t pos = 0;  // india(i) - i + j, 0-based running position
+        for (int32_t i = 0; !rc && i < nfit; ++i)
+            for (int32_t t = std::max(0, P.w - i); t <= P.w; ++t) cOut[pos++] = F[(size_t)i * W1 + t];
+    }
+    band_free(P);
+    cudaFree(v); cudaFree(tmp); cudaFree(yk);
+    return rc;
 }

@@ -76,7 +76,7 @@ class FitStats(C.Structure):
 
 class SolveInfo(C.Structure):
     _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
-                ("pad", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
+                ("nrkd", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
                 ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double)]
 
 
@@ -87,7 +87,8 @@ class Steer(C.Structure):
                 ("lfitbb", C.c_int32), ("mreqenf", C.c_int32), ("mreqena", C.c_int32),
                 ("mreqpe", C.c_int32), ("mrestl", C.c_double), ("itnlim", C.c_int32),
                 ("nthreads", C.c_int32), ("structDevice", C.c_int32), ("monitor", C.c_int32),
-                ("monitorPulls", C.c_int32), ("monitorBins", C.c_int32)]
+                ("monitorPulls", C.c_int32), ("monitorBins", C.c_int32),
+                ("mbandw", C.c_int32), ("lprecm", C.c_int32)]
 
 
 class Job(C.Structure):
@@ -146,7 +147,7 @@ def lib():
 EXPORTS = [
     "mpgpu_create", "mpgpu_destroy", "mpgpu_last_error", "mpgpu_set_layout",
     "mpgpu_set_constraints", "mpgpu_upload_records", "mpgpu_loopbf", "mpgpu_loopbf_device",
-    "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
+    "mpgpu_mupdat", "mpgpu_mupdat_noalloc", "mpgpu_set_preconditioner", "mpgpu_band_factor", "mpgpu_vector_add", "mpgpu_download_matrix", "mpgpu_download_vector",
     "mpgpu_download_record_status", "mpgpu_solve", "mpgpu_avprod", "mpgpu_probe_fp64",
     "mpgpu_dense_cholesky", "mpgpu_upload_timing", "mpgpu_fit_buckets",
     "mpgpu_set_monitor", "mpgpu_get_monitor", "mpgpu_monitor_groups", "mpgpu_write_mon",
@@ -415,6 +416,7 @@ class Context:
 
     def set_layout(self, S, matsto):
         self.nVar, self.nTotal, self.matsto = S.nVar, S.nTotal, matsto
+        self.ncon = 0
         self.nmat = S.nmatSparse if matsto == 2 else S.nmatPacked
         self.check(self.L.mpgpu_set_layout(
             self.h, C.c_int32(S.nTotal), ptr(S.varIndex, i32p), C.c_int32(S.nVar),
@@ -541,6 +543,21 @@ class Context:
                                       C.byref(info)))
         return corr, err, info
 
+    def set_preconditioner(self, mbandw, lprecm=0):
+        self.check(self.L.mpgpu_set_preconditioner(self.h, C.c_int32(mbandw), C.c_int32(lprecm)))
+
+    def band_factor(self, mbandw, lprecm=0):
+        """lltdec factor of the band of Q^T A Q in pede's variable-band layout
+        (rows 1..mbandw triangular, then mbandw per row) and nrkd."""
+        nfit = self.nVar - self.ncon
+        k = min(mbandw, nfit)
+        size = k * (k + 1) // 2 + max(nfit - k, 0) * mbandw
+        c = np.zeros(max(size, 1), np.float64)
+        nrkd = C.c_int32()
+        self.check(self.L.mpgpu_band_factor(self.h, C.c_int32(mbandw), C.c_int32(lprecm), ptr(c, f64p),
+                                            C.byref(nrkd)))
+        return c[:size], nrkd.value
+
     def avprod(self, x):
         x = np.ascontiguousarray(x, np.float64)
         b = np.zeros_like(x)
@@ -570,7 +587,7 @@ class JobData:
         st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
                   dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
                   mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0, monitor=0,
-                  monitorPulls=0, monitorBins=100)
+                  monitorPulls=0, monitorBins=100, mbandw=0, lprecm=0)
         st.update(steer)
         self.steer = Steer(**st)
         self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)

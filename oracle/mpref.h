@@ -218,6 +218,27 @@ int32_t mpref_minresqlp_sparse(int32_t matsto, int32_t nVar, int32_t nG,
                                const mpref_ql *q, const double *rhs, double *x,
                                double rtol, int32_t itnlim, int32_t *itn);
 
+/* MINRES (qlp 0) or MINRES-QLP (qlp 1) with the preconditioner chosen by
+ * mbandw as pede's "bandwidth" option (pede.f90:8292-8316): < 0 none, 0 the
+ * diagonal, > 0 the variable-band Cholesky factor of the band of Q^T A Q
+ * (equdecs/equslvs with constraints eliminated, lltdec option lprecm).
+ * *nrkd receives lltdec's rank-deficit code (may be NULL). */
+int32_t mpref_minres_precond(int32_t qlp, int32_t matsto, int32_t nVar, int32_t nG,
+                             const int32_t *allIndexGroups, const int64_t *offsets,
+                             const int32_t *columns, const double *matD, const mpref_ql *q,
+                             const double *rhs, double *x, double rtol, int32_t itnlim,
+                             int32_t mbandw, int32_t lprecm, int32_t *itn, int32_t *nrkd);
+
+/* The band preconditioner alone: band of Q^T A Q (mbandw > 0) factorised by
+ * lltdec; c receives the first nfit rows in the variable-band layout of
+ * mpref_band_index (india[nfit-1] doubles). */
+int32_t mpref_band_precond(int32_t matsto, int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
+                           const int64_t *offsets, const int32_t *columns, const double *matD,
+                           const mpref_ql *q, int32_t mbandw, int32_t lprecm, double *c, int32_t *nrkd);
+void mpref_band_index(int32_t n, int32_t mbandw, int64_t *india);
+int32_t mpref_lltdec(int32_t n, double *c, const int64_t *india, int32_t iopt);
+void mpref_lltslv(int32_t n, const double *c, const int64_t *india, double *x);
+
 /* ---------------------------------------------------------------------
  * Whole job (xloopn/loopn/addcst control without line search) and
  * millepede.res writer (prtglo, pede.f90:4477-4651).
@@ -233,6 +254,8 @@ typedef struct mpref_steer {
     double mrestl;
     int32_t itnlim;
     int32_t nthreads;   /* OpenMP threads for the data loop (1 = literal) */
+    int32_t mbandw;     /* MINRES preconditioner: < 0 none, 0 diagonal, > 0 band width */
+    int32_t lprecm;     /* lltdec option of the band preconditioner (skyline) */
 } mpref_steer;
 
 typedef struct mpref_job {

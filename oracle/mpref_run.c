@@ -259,11 +259,9 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
                 free(bav);
             }
             int32_t itn = 0;
-            res->minresIstop = st->metsol == 4
-                ? mpref_minres_sparse(st->matsto, nVar, nG, aig, offsets, columns, matD, q, rhs, corr,
-                                      st->mrestl, st->itnlim, &itn)
-                : mpref_minresqlp_sparse(st->matsto, nVar, nG, aig, offsets, columns, matD, q, rhs,
-                                         corr, st->mrestl, st->itnlim, &itn);
+            res->minresIstop = mpref_minres_precond(st->metsol == 5, st->matsto, nVar, nG, aig, offsets,
+                                                    columns, matD, q, rhs, corr, st->mrestl, st->itnlim,
+                                                    st->mbandw, st->lprecm, &itn, NULL);
             res->minresItn = itn;
             if (ncon > 0) {
                 for (j = 0; j < ncon; j++) corr[nfit + j] = csol[j];

@@ -395,6 +395,118 @@ void mpref_avprd0(int32_t matsto, int32_t n, const double *x0, double *b0, int32
     }
 }
 
+/* ------------------------------------------------------------------
+ * Preconditioners of MINRES: none (mbandw < 0), the diagonal of precons
+ * (mbandw = 0, no constraint blocks, mpnum.f90:2881-3060: cu = 1/sqrt(c),
+ * M^-1 y = (y*cu)*cu) or the variable-band Cholesky factor of equdecs /
+ * equslvs with no Lagrange multipliers (mbandw > 0, mpnum.f90:2486-2678:
+ * lltdec 2155-2209, lltfwd 2222-2240, lltbwd 2300-2318).
+ * ---------------------------------------------------------------- */
+typedef struct {
+    int32_t kind;          /* -1 none, 0 diagonal, 1 band */
+    int32_t n;
+    const double *pc;      /* kind 0: cu */
+    const double *c;       /* kind 1: factor in the variable-band layout */
+    const int64_t *india;  /* kind 1: position of each row's diagonal (1-based) */
+} precond;
+
+/* indPreCond (pede.f90:7705-7717): rows 1..mbandw triangular, then a
+ * fixed width of mbandw; india[i-1] = 1-based position of c(i,i). */
+void mpref_band_index(int32_t n, int32_t mbandw, int64_t *india)
+{
+    int32_t i;
+    for (i = 1; i <= n; i++)
+        india[i - 1] = i <= mbandw ? (int64_t)i * (i + 1) / 2 : india[i - 2] + mbandw;
+}
+
+/* lltdec (mpnum.f90:2155-2209): c = L L^T of the variable band in place,
+ * the diagonal replaced by 1/sqrt; a row whose reduced diagonal is not
+ * above 16 eps times its original is reset (iopt > 0: diagonal from the
+ * original value, "skyline").  Returns nrkd as lltdec. */
+int32_t mpref_lltdec(int32_t n, double *c, const int64_t *india, int32_t iopt)
+{
+    const double eps = 16.0 * DBL_EPSILON;
+    int32_t nrkd = 0, i, j, k;
+    double diag = 0.0;
+    if (n <= 0) return 0;
+#define C_(q) c[(q) - 1]
+#define IN_(q) india[(q) - 1]
+    if (C_(IN_(1)) > 0.0) {
+        C_(IN_(1)) = 1.0 / sqrt(C_(IN_(1)));
+    } else {
+        C_(IN_(1)) = 0.0;
+        nrkd = -1;
+    }
+    for (k = 2; k <= n; k++) {
+        const int32_t mk = (int32_t)(k - IN_(k) + IN_(k - 1) + 1);
+        for (j = mk; j <= k; j++) {
+            int32_t mj = 1;
+            if (j > 1) mj = (int32_t)(j - IN_(j) + IN_(j - 1) + 1);
+            const int64_t kj = IN_(k) - k + j;
+            diag = C_(IN_(j));
+            for (i = (mj > mk ? mj : mk); i <= j - 1; i++) {
+                const double prod = C_(IN_(k) - k + i) * C_(IN_(j) - j + i);
+                C_(kj) = C_(kj) - prod;
+            }
+            if (j != k) C_(kj) = C_(kj) * diag;
+        }
+        if (C_(IN_(k)) > eps * diag) {
+            C_(IN_(k)) = 1.0 / sqrt(C_(IN_(k)));
+        } else {
+            for (j = mk; j <= k; j++) C_(IN_(k) - k + j) = 0.0;
+            if (iopt > 0 && diag > 0.0) {
+                C_(IN_(k)) = 1.0 / sqrt(diag);
+            } else {
+                if (nrkd == 0) {
+                    nrkd = -k;
+                } else {
+                    if (nrkd < 0) nrkd = 1;
+                    nrkd = nrkd + 1;
+                }
+            }
+        }
+    }
+    return nrkd;
+}
+
+/* lltfwd + lltbwd (mpnum.f90:2222-2240, 2300-2318): x := (L L^T)^-1 x */
+void mpref_lltslv(int32_t n, const double *c, const int64_t *india, double *x)
+{
+    int32_t j, k;
+    if (n <= 0) return;
+    x[0] = x[0] * C_(IN_(1));
+    for (k = 2; k <= n; k++) {
+        for (j = (int32_t)(k - IN_(k) + IN_(k - 1) + 1); j <= k - 1; j++) {
+            const double prod = C_(IN_(k) - k + j) * x[j - 1];
+            x[k - 1] = x[k - 1] - prod;
+        }
+        x[k - 1] = x[k - 1] * C_(IN_(k));
+    }
+    for (k = n; k >= 2; k--) {
+        x[k - 1] = x[k - 1] * C_(IN_(k));
+        for (j = (int32_t)(k - IN_(k) + IN_(k - 1) + 1); j <= k - 1; j++) {
+            const double prod = C_(IN_(k) - k + j) * x[k - 1];
+            x[j - 1] = x[j - 1] - prod;
+        }
+    }
+    x[0] = x[0] * C_(IN_(1));
+#undef C_
+#undef IN_
+}
+
+static void msolve(const precond *P, const double *r, double *y)
+{
+    int32_t i, n = P->n;
+    if (P->kind < 0) {
+        for (i = 0; i < n; i++) y[i] = r[i];
+    } else if (P->kind == 0) {
+        for (i = 0; i < n; i++) y[i] = (r[i] * P->pc[i]) * P->pc[i];
+    } else {
+        for (i = 0; i < n; i++) y[i] = r[i];
+        mpref_lltslv(n, P->c, P->india, y);
+    }
+}
+
 /* reduced operator for MINRES: b = (Q^T A Q x)(1:nfit) (avprod) */
 typedef struct {
     int32_t matsto, nVar, nG, nfit;
@@ -469,12 +581,88 @@ static void reduced_diag(const redop *o, double *dg)
     free(v); free(y); free(tmp);
 }
 
+/* Band of Q^T A Q over all nVar rows in the variable-band layout (the
+ * preconditioner fill of pede.f90:2639-2651 followed by qlpssq with band
+ * width mbandw, mpqldec.f90:711-945).  The reference tracks the products
+ * of the reflections through coefficient tables; here each reflection
+ * k = m..1 is applied explicitly: with P = H_m ... H_{k+1}, y = P^T A P v
+ * and beta = v.y, H A' H changes element (i,j) by
+ * -2 (v_i y_j + y_i v_j) + 4 beta v_i v_j.  Same matrix up to rounding. */
+static void reduced_band(const redop *o, int32_t mbandw, const int64_t *india, double *c)
+{
+    int32_t nV = o->nVar, i, j;
+    int32_t *p2g = NULL;
+    if (o->matsto == 2) {
+        p2g = (int32_t *)calloc((size_t)(nV > 0 ? nV : 1), sizeof(int32_t));
+        for (int32_t g = 1; g <= o->nG; g++)
+            for (int32_t q = o->aig[g - 1]; q < o->aig[g]; q++) p2g[q - 1] = g;
+    }
+    for (i = 1; i <= nV; i++) {
+        const int64_t ia = india[i - 1];
+        for (j = (i - mbandw + 1 > 1 ? i - mbandw + 1 : 1); j <= i; j++) {
+            double a = 0.0;
+            if (o->matsto == 2) {
+                const int64_t ij = mpref_ijadd(i, j, o->nG, o->aig, p2g, o->off, o->col);
+                if (ij > 0) a = o->matD[ij - 1];
+            } else {
+                a = o->matD[((int64_t)i * i - i) / 2 + j - 1];
+            }
+            c[ia - i + j - 1] = a;
+        }
+    }
+    free(p2g);
+    if (!o->q) return;
+    const mpref_ql *q = o->q;
+    int32_t m = q->ncon;
+    double *v = (double *)calloc((size_t)nV, sizeof(double));
+    double *y = (double *)calloc((size_t)nV, sizeof(double));
+    double *tmp = (double *)calloc((size_t)nV, sizeof(double));
+    for (int32_t k = m; k >= 1; k--) {
+        int32_t kn = nV + k - m;
+        const double *vr = q->V + (int64_t)(k - 1) * nV;
+        for (i = 0; i < nV; i++) v[i] = 0.0;
+        for (i = q->r1[k]; i <= q->r2[k]; i++) v[i - 1] = vr[1 + i - q->r1[k]];
+        v[kn - 1] = q->Vk[k];
+        for (i = 0; i < nV; i++) tmp[i] = v[i];
+        for (int32_t kk = k + 1; kk <= m; kk++) {
+            int32_t knn = nV + kk - m;
+            const double *wr = q->V + (int64_t)(kk - 1) * nV;
+            double sp = 0.0;
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) sp += wr[1 + i - q->r1[kk]] * tmp[i - 1];
+            sp += q->Vk[kk] * tmp[knn - 1];
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) tmp[i - 1] -= 2.0 * wr[1 + i - q->r1[kk]] * sp;
+            tmp[knn - 1] -= 2.0 * q->Vk[kk] * sp;
+        }
+        mpref_avprd0(o->matsto, nV, tmp, y, o->nG, o->aig, o->off, o->col, o->matD);
+        for (int32_t kk = m; kk >= k + 1; kk--) {
+            int32_t knn = nV + kk - m;
+            const double *wr = q->V + (int64_t)(kk - 1) * nV;
+            double sp = 0.0;
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) sp += wr[1 + i - q->r1[kk]] * y[i - 1];
+            sp += q->Vk[kk] * y[knn - 1];
+            for (i = q->r1[kk]; i <= q->r2[kk]; i++) y[i - 1] -= 2.0 * wr[1 + i - q->r1[kk]] * sp;
+            y[knn - 1] -= 2.0 * q->Vk[kk] * sp;
+        }
+        double beta = 0.0;
+        for (i = 0; i < nV; i++) beta += v[i] * y[i];
+        for (i = 1; i <= nV; i++) {
+            const int64_t ia = india[i - 1];
+            for (j = (i - mbandw + 1 > 1 ? i - mbandw + 1 : 1); j <= i; j++) {
+                const double vi = v[i - 1], vj = v[j - 1];
+                if (vi == 0.0 && vj == 0.0) continue;
+                c[ia - i + j - 1] += -2.0 * (vi * y[j - 1] + y[i - 1] * vj) + 4.0 * beta * (vi * vj);
+            }
+        }
+    }
+    free(v); free(y); free(tmp);
+}
+
 /* Preconditioned MINRES, Paige & Saunders (1975), SIAM J. Numer. Anal. 12,
  * 617-629: Lanczos tridiagonalisation of the preconditioned operator,
  * QR of the tridiagonal by Givens rotations, solution update along the
  * rotated directions.  Stopping: relative residual rnorm/(Anorm*ynorm) <=
  * rtol (istop 1), Arnorm/Anorm <= rtol (istop 2), itn >= itnlim (istop 6). */
-static int32_t minres(const redop *o, const double *pc, const double *b, double *x,
+static int32_t minres(const redop *o, const precond *pc, const double *b, double *x,
                       double rtol, int32_t itnlim, int32_t *itnout)
 {
     int32_t n = o->nfit, i, itn = 0, istop = 0;
@@ -487,7 +675,7 @@ static int32_t minres(const redop *o, const double *pc, const double *b, double 
     double gamma, cs = -1, sn = 0, phi, phibar, denom, tnorm2 = 0, gmax = 0, gmin = DBL_MAX;
     double Anorm = 0, ynorm, rnorm, test1, test2, Acond;
     for (i = 0; i < n; i++) { x[i] = 0.0; r1[i] = b[i]; }
-    for (i = 0; i < n; i++) y[i] = (r1[i] * pc[i]) * pc[i];
+    msolve(pc, r1, y);
     beta1 = 0.0;
     for (i = 0; i < n; i++) beta1 += r1[i] * y[i];
     if (beta1 <= 0.0) { *itnout = 0; istop = beta1 < 0.0 ? 9 : 0; goto out; }
@@ -507,7 +695,7 @@ static int32_t minres(const redop *o, const double *pc, const double *b, double 
         for (i = 0; i < n; i++) alfa += v[i] * y[i];
         for (i = 0; i < n; i++) y[i] = y[i] - (alfa / beta) * r2[i];
         for (i = 0; i < n; i++) { r1[i] = r2[i]; r2[i] = y[i]; }
-        for (i = 0; i < n; i++) y[i] = (r2[i] * pc[i]) * pc[i];
+        msolve(pc, r2, y);
         oldb = beta;
         beta = 0.0;
         for (i = 0; i < n; i++) beta += r2[i] * y[i];
@@ -580,7 +768,7 @@ static void sym_ortho(double a, double b, double *c, double *s, double *r)
     *s = b / *r;
 }
 
-static int32_t minresqlp(const redop *o, const double *pc, const double *b, double *x,
+static int32_t minresqlp(const redop *o, const precond *pc, const double *b, double *x,
                          double rtol, int32_t itnlim, double maxxnorm, int32_t *itnout)
 {
     int32_t n = o->nfit, i, itn = 0, istop = 0;
@@ -596,7 +784,7 @@ static int32_t minresqlp(const redop *o, const double *pc, const double *b, doub
     double etaA = 0, thA = 0, gA = 0, tauA = 0, etaB = 0, thB = 0, gB = 0, tauB = 0;
     double uF1 = 0, uF2 = 0;   /* final u_{k-3}, u_{k-4} */
     for (i = 0; i < n; i++) { x[i] = 0.0; r1[i] = b[i]; }
-    for (i = 0; i < n; i++) y[i] = (r1[i] * pc[i]) * pc[i];
+    msolve(pc, r1, y);
     beta1 = 0.0;
     for (i = 0; i < n; i++) beta1 += r1[i] * y[i];
     if (beta1 <= 0.0) { *itnout = 0; istop = beta1 < 0.0 ? 9 : 0; goto out; }
@@ -617,7 +805,7 @@ static int32_t minresqlp(const redop *o, const double *pc, const double *b, doub
         for (i = 0; i < n; i++) alfa += v[i] * y[i];
         for (i = 0; i < n; i++) y[i] = y[i] - (alfa / beta) * r2[i];
         for (i = 0; i < n; i++) { r1[i] = r2[i]; r2[i] = y[i]; }
-        for (i = 0; i < n; i++) y[i] = (r2[i] * pc[i]) * pc[i];
+        msolve(pc, r2, y);
         oldb = beta;
         beta = 0.0;
         for (i = 0; i < n; i++) beta += r2[i] * y[i];
@@ -711,27 +899,84 @@ out:
     return istop;
 }
 
+static void redop_init(redop *o, int32_t matsto, int32_t nVar, int32_t nG, const int32_t *aig,
+                       const int64_t *offsets, const int32_t *columns, const double *matD, const mpref_ql *q)
+{
+    int32_t ncon = q ? q->ncon : 0;
+    o->matsto = matsto; o->nVar = nVar; o->nG = nG; o->nfit = nVar - ncon;
+    o->aig = aig; o->off = offsets; o->col = columns; o->matD = matD; o->q = q;
+    o->xa = (double *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(double));
+    o->ba = (double *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(double));
+}
+
+int32_t mpref_band_precond(int32_t matsto, int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
+                           const int64_t *offsets, const int32_t *columns, const double *matD,
+                           const mpref_ql *q, int32_t mbandw, int32_t lprecm, double *c, int32_t *nrkd)
+{
+    redop o;
+    if (mbandw <= 0) return -1;
+    redop_init(&o, matsto, nVar, nG, allIndexGroups, offsets, columns, matD, q);
+    int64_t *india = (int64_t *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(int64_t));
+    mpref_band_index(nVar, mbandw, india);
+    double *cf = (double *)calloc((size_t)(nVar > 0 ? india[nVar - 1] : 1), sizeof(double));
+    reduced_band(&o, mbandw, india, cf);
+    *nrkd = mpref_lltdec(o.nfit, cf, india, lprecm);
+    if (o.nfit > 0) memcpy(c, cf, sizeof(double) * (size_t)india[o.nfit - 1]);
+    free(cf); free(india); free(o.xa); free(o.ba);
+    return 0;
+}
+
+int32_t mpref_minres_precond(int32_t qlp, int32_t matsto, int32_t nVar, int32_t nG,
+                             const int32_t *allIndexGroups, const int64_t *offsets,
+                             const int32_t *columns, const double *matD, const mpref_ql *q,
+                             const double *rhs, double *x, double rtol, int32_t itnlim,
+                             int32_t mbandw, int32_t lprecm, int32_t *itn, int32_t *nrkd)
+{
+    redop o;
+    int32_t i;
+    redop_init(&o, matsto, nVar, nG, allIndexGroups, offsets, columns, matD, q);
+    precond P;
+    P.kind = mbandw < 0 ? -1 : (mbandw == 0 ? 0 : 1);
+    P.n = o.nfit;
+    P.pc = NULL; P.c = NULL; P.india = NULL;
+    double *pc = NULL, *cf = NULL, *dg = NULL;
+    int64_t *india = NULL;
+    if (nrkd) *nrkd = 0;
+    if (P.kind == 0) {
+        dg = (double *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(double));
+        pc = (double *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(double));
+        reduced_diag(&o, dg);
+        for (i = 0; i < o.nfit; i++) pc[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
+        P.pc = pc;
+    } else if (P.kind == 1) {
+        india = (int64_t *)calloc((size_t)(nVar > 0 ? nVar : 1), sizeof(int64_t));
+        mpref_band_index(nVar, mbandw, india);
+        cf = (double *)calloc((size_t)(nVar > 0 ? india[nVar - 1] : 1), sizeof(double));
+        reduced_band(&o, mbandw, india, cf);
+        const int32_t r = mpref_lltdec(o.nfit, cf, india, lprecm);
+        if (nrkd) *nrkd = r;
+        P.c = cf; P.india = india;
+    }
+    int32_t istop;
+    if (qlp) {
+        /* maxxnorm as pede sets it (pede.f90:626) */
+        const double maxxnorm = (double)o.nfit / sqrt(DBL_EPSILON);
+        istop = minresqlp(&o, &P, rhs, x, rtol, itnlim, maxxnorm, itn);
+    } else {
+        istop = minres(&o, &P, rhs, x, rtol, itnlim, itn);
+    }
+    free(o.xa); free(o.ba); free(dg); free(pc); free(cf); free(india);
+    return istop;
+}
+
 int32_t mpref_minresqlp_sparse(int32_t matsto, int32_t nVar, int32_t nG,
                                const int32_t *allIndexGroups, const int64_t *offsets,
                                const int32_t *columns, const double *matD,
                                const mpref_ql *q, const double *rhs, double *x,
                                double rtol, int32_t itnlim, int32_t *itn)
 {
-    redop o;
-    int32_t ncon = q ? q->ncon : 0, i;
-    o.matsto = matsto; o.nVar = nVar; o.nG = nG; o.nfit = nVar - ncon;
-    o.aig = allIndexGroups; o.off = offsets; o.col = columns; o.matD = matD; o.q = q;
-    o.xa = (double *)calloc((size_t)nVar, sizeof(double));
-    o.ba = (double *)calloc((size_t)nVar, sizeof(double));
-    double *dg = (double *)calloc((size_t)nVar, sizeof(double));
-    double *pc = (double *)calloc((size_t)nVar, sizeof(double));
-    reduced_diag(&o, dg);
-    for (i = 0; i < o.nfit; i++) pc[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
-    /* maxxnorm as pede sets it (pede.f90:626) */
-    const double maxxnorm = (double)o.nfit / sqrt(DBL_EPSILON);
-    int32_t istop = minresqlp(&o, pc, rhs, x, rtol, itnlim, maxxnorm, itn);
-    free(o.xa); free(o.ba); free(dg); free(pc);
-    return istop;
+    return mpref_minres_precond(1, matsto, nVar, nG, allIndexGroups, offsets, columns, matD, q, rhs, x,
+                                rtol, itnlim, 0, 0, itn, NULL);
 }
 
 int32_t mpref_minres_sparse(int32_t matsto, int32_t nVar, int32_t nG,
@@ -740,19 +985,6 @@ int32_t mpref_minres_sparse(int32_t matsto, int32_t nVar, int32_t nG,
                             const mpref_ql *q, const double *rhs, double *x,
                             double rtol, int32_t itnlim, int32_t *itn)
 {
-    redop o;
-    int32_t ncon = q ? q->ncon : 0, i;
-    o.matsto = matsto; o.nVar = nVar; o.nG = nG; o.nfit = nVar - ncon;
-    o.aig = allIndexGroups; o.off = offsets; o.col = columns; o.matD = matD; o.q = q;
-    o.xa = (double *)calloc((size_t)nVar, sizeof(double));
-    o.ba = (double *)calloc((size_t)nVar, sizeof(double));
-    double *dg = (double *)calloc((size_t)nVar, sizeof(double));
-    double *pc = (double *)calloc((size_t)nVar, sizeof(double));
-    reduced_diag(&o, dg);
-    /* precons/presols with no constraint blocks (mpnum.f90:2881-3060):
-     * cu = 1/sqrt(c); M^-1 y = (y*cu)*cu */
-    for (i = 0; i < o.nfit; i++) pc[i] = dg[i] > 0.0 ? 1.0 / sqrt(dg[i]) : 0.0;
-    int32_t istop = minres(&o, pc, rhs, x, rtol, itnlim, itn);
-    free(o.xa); free(o.ba); free(dg); free(pc);
-    return istop;
+    return mpref_minres_precond(0, matsto, nVar, nG, allIndexGroups, offsets, columns, matD, q, rhs, x,
+                                rtol, itnlim, 0, 0, itn, NULL);
 }

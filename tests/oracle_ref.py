@@ -35,7 +35,7 @@ class Steer(C.Structure):
                 ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float),
                 ("lfitbb", C.c_int32), ("mreqenf", C.c_int32), ("mreqena", C.c_int32),
                 ("mreqpe", C.c_int32), ("mrestl", C.c_double), ("itnlim", C.c_int32),
-                ("nthreads", C.c_int32)]
+                ("nthreads", C.c_int32), ("mbandw", C.c_int32), ("lprecm", C.c_int32)]
 
 
 class Job(C.Structure):

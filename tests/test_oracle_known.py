@@ -237,3 +237,129 @@ def test_minresqlp_maxxnorm_keeps_last_iterate(orc):
     x, istop, itn = minres_call("mpref_minresqlp_sparse", A, b, rtol=1e-14, itnlim=400)
     assert np.all(np.isfinite(x))
     assert np.linalg.norm(x) <= n / np.sqrt(np.finfo(float).eps)
+
+
+# ---- band preconditioner (equdecs/equslvs with constraints eliminated)
+i64p = C.POINTER(C.c_int64)
+
+
+def band_index(n, mb):
+    india = np.zeros(n, np.int64)
+    O.lib().mpref_band_index(C.c_int32(n), C.c_int32(mb), india.ctypes.data_as(i64p))
+    return india
+
+
+def band_fill(A, mb):
+    n = len(A)
+    india = band_index(n, mb)
+    c = np.zeros(int(india[-1]))
+    for k in range(n):
+        for j in range(max(0, k - mb + 1), k + 1):
+            c[india[k] - 1 - k + j] = A[k, j]
+    return c, india
+
+
+def band_factor(c, india, mb):
+    """dense L from lltdec's band: off-diagonals as stored, diagonal 1/c"""
+    n = len(india)
+    L = np.zeros((n, n))
+    for k in range(n):
+        for j in range(max(0, k - mb + 1), k):
+            L[k, j] = c[india[k] - 1 - k + j]
+        d = c[india[k] - 1]
+        L[k, k] = 1.0 / d if d != 0.0 else 0.0
+    return L
+
+
+def band_of(A, mb):
+    n = len(A)
+    i, j = np.indices((n, n))
+    return np.where((i - j < mb) & (j - i < mb), A, 0.0)
+
+
+def test_lltdec_band_solve(orc):
+    """lltdec on an SPD band: L L^T reproduces the band within 1e-13;
+    lltfwd + lltbwd solve it within 1e-11."""
+    n, mb = 50, 6
+    rng = np.random.default_rng(41)
+    A = band_of(spd(n, rng), mb)
+    c, india = band_fill(A, mb)
+    nrkd = O.lib().mpref_lltdec(C.c_int32(n), p(c), india.ctypes.data_as(i64p), C.c_int32(0))
+    assert nrkd == 0
+    L = band_factor(c, india, mb)
+    assert rel(L @ L.T, A) <= 1e-13
+    b = rng.normal(size=n)
+    x = b.copy()
+    O.lib().mpref_lltslv(C.c_int32(n), p(c), india.ctypes.data_as(i64p), p(x))
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-11
+
+
+@pytest.mark.parametrize("iopt", [0, 1])
+def test_lltdec_dependent_row(orc, iopt):
+    """A row equal to the one before it (an exact 2x2 block [[4,4],[4,4]]):
+    its reduced diagonal is exactly 0, the row is reset; without the skyline
+    option its diagonal is 0 and nrkd = -row, with it the diagonal is
+    1/sqrt(4) and nrkd = 0."""
+    n, mb, k = 20, 4, 9
+    rng = np.random.default_rng(43)
+    A = band_of(spd(n, rng), mb)
+    A[k - 1:k + 1, :] = 0.0
+    A[:, k - 1:k + 1] = 0.0
+    A[k - 1:k + 1, k - 1:k + 1] = 4.0
+    c, india = band_fill(A, mb)
+    nrkd = O.lib().mpref_lltdec(C.c_int32(n), p(c), india.ctypes.data_as(i64p), C.c_int32(iopt))
+    row = c[india[k] - 1 - (min(k, mb - 1)):india[k] - 1]
+    assert np.all(row == 0.0)
+    if iopt:
+        assert nrkd == 0 and c[india[k] - 1] == 0.5
+    else:
+        assert nrkd == -(k + 1) and c[india[k] - 1] == 0.0
+
+
+def test_band_precond_of_reduced_matrix(orc):
+    """With constraints eliminated, the factor's L L^T is the band of
+    (Q^T M Q) restricted to the fit parameters, within 1e-12."""
+    npar, ncon, mb = 40, 3, 5
+    rng = np.random.default_rng(47)
+    Cm, h = ql(npar, ncon, rng)
+    try:
+        Q = np.stack([ql_apply(h, e, 0) for e in np.eye(npar)], axis=1)
+        M = spd(npar, rng)
+        m = npar - ncon
+        want = band_of((Q.T @ M @ Q)[:m, :m], mb)
+        india = band_index(npar, mb)
+        c = np.zeros(int(india[m - 1]))
+        nrkd = C.c_int32()
+        aig = np.arange(1, npar + 2, dtype=np.int32)
+        rc = O.lib().mpref_band_precond(C.c_int32(1), C.c_int32(npar), C.c_int32(npar), aig.ctypes.data_as(i32p),
+                                        None, None, p(packed(M)), C.c_void_p(h), C.c_int32(mb), C.c_int32(0),
+                                        p(c), C.byref(nrkd))
+        assert rc == 0 and nrkd.value == 0
+        L = band_factor(c, india[:m], mb)
+        assert rel(L @ L.T, want) <= 1e-12
+    finally:
+        O.lib().mpref_ql_destroy(C.c_void_p(h))
+
+
+@pytest.mark.parametrize("qlp", [0, 1])
+@pytest.mark.parametrize("mbandw", [-1, 0, 4, 80])
+def test_minres_preconditioners(orc, qlp, mbandw):
+    """MINRES and MINRES-QLP with no, diagonal and band preconditioners
+    reach numpy's solution within 1e-9; the band as wide as the matrix is
+    its exact factor, so one or two iterations suffice."""
+    n = 80
+    rng = np.random.default_rng(53)
+    pat = rng.random((n, n)) < 0.1
+    A = spd(n, rng, pattern=pat | pat.T)
+    b = rng.normal(size=n)
+    x = np.zeros(n)
+    itn, nrkd = C.c_int32(), C.c_int32()
+    aig = np.arange(1, n + 2, dtype=np.int32)
+    istop = O.lib().mpref_minres_precond(C.c_int32(qlp), C.c_int32(1), C.c_int32(n), C.c_int32(n),
+                                         aig.ctypes.data_as(i32p), None, None, p(packed(A)), None, p(b), p(x),
+                                         C.c_double(1e-13), C.c_int32(1000), C.c_int32(mbandw), C.c_int32(0),
+                                         C.byref(itn), C.byref(nrkd))
+    assert istop in (1, 2), istop
+    assert rel(x, np.linalg.solve(A, b)) <= 1e-9
+    if mbandw >= n:
+        assert itn.value <= 2
