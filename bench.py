@@ -203,6 +203,62 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000):
             "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
 
 
+def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
+    """MINRES on the sparse barrel (30,000 tracks: 30,000 globals, 6.1M
+    stored elements, 18 constraints eliminated by QL): device time per
+    iteration (a fixed number of iterations, rtol below reach) with the
+    diagonal and the band-6 preconditioner, set-up time apart; the FP64
+    bound of the sparse product (2 FMAs per stored off-diagonal element, 2
+    FMAs per SM per clock on 152 SMs); and the oracle's MINRES on the host
+    cores for cpu_iters iterations on the same matrix."""
+    import ctypes as C
+    import oracle_ref as orc
+    d = mp.generate(mp.gen_config("barrel", ntracks=30000, seed=4))
+    H = mp.HostStructure(d, mreqenf=5, sparse=True)
+    A = mp.constraint_matrix(d, H)
+    ctx = mp.Context(device=local)
+    ctx.set_layout(H, 2)
+    ctx.set_constraints(A)
+    ctx.upload(H)
+    lb = ctx.loopbf(np.zeros(H.nTotal))
+    M = ctx.matrix()
+    out = {"n": int(H.nVar), "ncon": int(A.shape[0]), "nmat": int(len(M)), "iterations": iters}
+    for mb in (0, 6):
+        ctx.set_preconditioner(mb)
+        ctx.solve(4, consResiduals=np.zeros(A.shape[0]), rtol=1e-30, itnlim=16)
+        _, _, info = ctx.solve(4, consResiduals=np.zeros(A.shape[0]), rtol=1e-30, itnlim=iters)
+        key = "diagonal" if mb == 0 else "band6"
+        out[f"ms_per_iteration_{key}"] = (info.ms - info.msFactor) / max(info.itn, 1)
+        out[f"ms_setup_{key}"] = info.msFactor
+    ctx.close()
+    fmas = 2 * (len(M) - H.nVar) + H.nVar
+    out["spmv_fp64_bound_us"] = fmas / (2 * 152 * 2.07e9) * 1e6
+    # the oracle's MINRES (diagonal) on one host core, same matrix and rhs
+    L = orc.lib()
+    f64p, i32p, i64p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+    L.mpref_ql_create.restype = C.c_void_p
+    Ac = np.ascontiguousarray(A)
+    q = L.mpref_ql_create(C.c_int32(H.nVar), C.c_int32(A.shape[0]), Ac.ctypes.data_as(f64p))
+    b = lb["gvec"].copy()
+    L.mpref_ql_mlq(C.c_void_p(q), b.ctypes.data_as(f64p), C.c_int32(1))
+    x = np.zeros(H.nVar)
+    itn, nrkd = C.c_int32(), C.c_int32()
+    off = np.ascontiguousarray(H.offsets, np.int64)
+    col = np.ascontiguousarray(H.columns, np.int32)
+    t0 = time.perf_counter()
+    L.mpref_minres_precond(C.c_int32(0), C.c_int32(2), C.c_int32(H.nVar), C.c_int32(H.nG),
+                           H.aig.ctypes.data_as(i32p), off.ctypes.data_as(i64p), col.ctypes.data_as(i32p),
+                           M.ctypes.data_as(f64p), C.c_void_p(q), b.ctypes.data_as(f64p), x.ctypes.data_as(f64p),
+                           C.c_double(1e-30), C.c_int32(cpu_iters), C.c_int32(0), C.c_int32(0), C.byref(itn),
+                           C.byref(nrkd))
+    cpu_s = time.perf_counter() - t0
+    L.mpref_ql_destroy(C.c_void_p(q))
+    out["cpu_baseline"] = {"ms_per_iteration": cpu_s * 1e3 / max(itn.value, 1), "cores": 1, "kind": "port",
+                           "sample": f"{itn.value} iterations including the preconditioner set-up"}
+    out["speedup_vs_cpu_diagonal"] = out["cpu_baseline"]["ms_per_iteration"] / out["ms_per_iteration_diagonal"]
+    return out
+
+
 def serve_measure(mp, local, njobs=24, rate=8.0, nmin=500, nmax=20000, rmin=10_000, rmax=200_000):
     """Stream of alignment jobs through the serving loop: Poisson arrivals at
     `rate` per second; per job (seed 1000 + job) a telescope with globals
@@ -362,6 +418,7 @@ def main():
     ap.add_argument("--profile", action="store_true", help="small run for profilers (no e2e/cpu)")
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
+    ap.add_argument("--minres-iters", type=int, default=300, help="iterations of the MINRES measurement (0: skip)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--part", default="loop", choices=["loop", "upload", "structure", "brokenlines"],
                     help="with --profile: the part to run on --ntracks records (for profilers)")
@@ -509,6 +566,8 @@ def main():
         line["brokenlines"] = brokenlines_measure(mp, local, args.brokenlines, ncores)
     if args.serve_jobs > 0 and rank == 0:
         line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
+    if args.minres_iters > 0 and rank == 0 and not args.profile:
+        line["minres"] = minres_measure(mp, local, iters=args.minres_iters)
     if args.dense_n > 0 and rank == 0:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n)
