@@ -417,16 +417,13 @@ struct SparseBlocks {
     double *tbuf = nullptr;
     int64_t tlen = 0;
     bool smallGroups = false;     // every group has at most kSmallGroup parameters
-    // small groups: the blocks of a row group in work items of at most
-    // kItemBlocks blocks (one warp each, partial row sums in rowPart), the
-    // transposed products of column group J stored parameter-major (stride
-    // = its incoming block count, tStr per block)
-    int64_t nItem = 0;
-    int32_t *itemGroup = nullptr;  // [nItem] row group
-    int64_t *itemB0 = nullptr;     // [nItem+1] first block (items of a group are consecutive)
-    int64_t *itemBeg = nullptr;    // [nG+1] first item of row group I
-    int32_t *tStr = nullptr;       // [nblk] stride of the block's transposed products
-    double *rowPart = nullptr;     // [nItem * kSmallGroup]
+    // small groups: per block its row group (brow), its partial row sums
+    // (rowPart, kSmallGroup each) and the stride of its transposed products
+    // (tStr: the column group's incoming block count, parameter-major)
+    int32_t *brow = nullptr;       // [nblk]
+    int32_t *tStr = nullptr;       // [nblk]
+    double *rowPart = nullptr;     // [nblk * kSmallGroup]
+    int uniform = 0;               // every group has this many parameters (0: mixed)
 };
 
 // phase 1: warp per row group I: y_I = D_I x_I + sum_J A_IJ x_J, the
@@ -488,53 +485,52 @@ __global__ void k_spmv_cols(int32_t nG, const int32_t *aig, const int64_t *colSt
     }
 }
 
-// the same two phases for row groups of at most 8 parameters.  Phase 1, one
-// warp per work item (at most kItemBlocks blocks of one row group): one lane
-// per block with its rows and columns in registers; the item's partial row
-// sums reduced over the lanes by a fixed shuffle tree into rowPart, the
-// transposed products of each block into tbuf (parameter-major per column
-// group).  Phase 2, one warp per group: y = D x + the row parts of the
-// group's items in item order + the transposed products summed over its
-// incoming blocks (lanes over blocks, fixed tree).
+// the same two phases for row groups of at most 8 parameters.  Phase 1,
+// one thread per stored block (all blocks of all row groups, so the lanes
+// stay full whatever the row lengths): the block's rows times x_J into its
+// partial row sums (rowPart, 8 per block; the diagonal block adds both
+// triangles of its strictly-lower part there) and its columns times x_I
+// into tbuf (parameter-major per column group).  G > 0: every group has G
+// parameters (loops fully unrolled); G = 0: at most 8, predicated.  Phase
+// 2, one warp per group: y = D x + the partial row sums of the group's
+// blocks + the transposed products of its incoming blocks, the lanes over
+// both lists with four independent partial sums each, then a fixed shuffle
+// tree; no atomics, the sums are reproducible.
 constexpr int kSmallGroup = 8;
-constexpr int kItemBlocks = 64;
 
-__global__ void __launch_bounds__(256) k_spmv_items(int64_t nItem, const int32_t *itemGroup, const int64_t *itemB0,
-                                                    const int32_t *aig, const int32_t *bcol, const int64_t *boff,
-                                                    const int32_t *bld, const int64_t *tOff, const int32_t *tStr,
-                                                    const double *matD, const double *x, double *tbuf,
-                                                    double *rowPart) {
-    const int ln = threadIdx.x & 31;
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t it = w; it < nItem; it += nw) {
-        const int32_t I = itemGroup[it];
-        const int32_t ia = aig[I - 1] - 1, np = aig[I] - 1 - ia;
-        double xi[kSmallGroup], sr[kSmallGroup];
+template <int G>
+__global__ void __launch_bounds__(256) k_spmv_blocks(int64_t nb, const int32_t *brow, const int32_t *aig,
+                                                     const int32_t *bcol, const int64_t *boff, const int32_t *bld,
+                                                     const int64_t *tOff, const int32_t *tStr,
+                                                     const double *matD, const double *x, double *tbuf,
+                                                     double *rowPart) {
+    constexpr int M = G > 0 ? G : kSmallGroup;
+    for (int64_t bl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; bl < nb;
+         bl += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t I = brow[bl], J = bcol[bl];
+        const int32_t ia = aig[I - 1] - 1, ja = aig[J - 1] - 1;
+        const int np = G > 0 ? G : aig[I] - 1 - ia;
+        const int nj = G > 0 ? G : aig[J] - 1 - ja;
+        const double *blk = matD + boff[bl];
+        const int32_t ld = bld[bl];
+        double xi[M], sr[M];
 #pragma unroll
-        for (int ii = 0; ii < kSmallGroup; ++ii) {
+        for (int ii = 0; ii < M; ++ii) {
             xi[ii] = ii < np ? x[ia + ii] : 0.0;
             sr[ii] = 0.0;
         }
-        const int64_t b0 = itemB0[it], b1 = itemB0[it + 1];
-        int64_t bdiag = -1;
-        for (int64_t bl = b0 + ln; bl < b1; bl += 32) {
-            const int32_t J = bcol[bl];
-            if (J == I) { bdiag = bl; continue; }
-            const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
-            const double *blk = matD + boff[bl];
-            const int32_t ld = bld[bl];
-            double xj[kSmallGroup], tc[kSmallGroup];
+        if (J != I) {
+            double xj[M], tc[M];
 #pragma unroll
-            for (int jj = 0; jj < kSmallGroup; ++jj) {
+            for (int jj = 0; jj < M; ++jj) {
                 xj[jj] = jj < nj ? x[ja + jj] : 0.0;
                 tc[jj] = 0.0;
             }
 #pragma unroll
-            for (int ii = 0; ii < kSmallGroup; ++ii) {
+            for (int ii = 0; ii < M; ++ii) {
                 if (ii < np) {
 #pragma unroll
-                    for (int jj = 0; jj < kSmallGroup; ++jj) {
+                    for (int jj = 0; jj < M; ++jj) {
                         if (jj < nj) {
                             const double a = blk[(int64_t)ii * ld + jj];
                             sr[ii] += a * xj[jj];
@@ -546,43 +542,28 @@ __global__ void __launch_bounds__(256) k_spmv_items(int64_t nItem, const int32_t
             double *tb = tbuf + tOff[bl];
             const int32_t st = tStr[bl];
 #pragma unroll
-            for (int jj = 0; jj < kSmallGroup; ++jj)
+            for (int jj = 0; jj < M; ++jj)
                 if (jj < nj) tb[(int64_t)jj * st] = tc[jj];
-        }
-        // the diagonal block's strictly-lower elements, both triangles
-        const int64_t bd = (int64_t)__reduce_max_sync(0xffffffffu, bdiag >= 0 ? (unsigned)(bdiag - b0 + 1) : 0u) - 1;
-        if (bd >= 0) {
-            const double *blk = matD + boff[b0 + bd];
-            const int32_t ld = bld[b0 + bd];
-            const int ne = np * (np - 1) / 2;
-            for (int e = ln; e < ne; e += 32) {
-                int ii = 1, base = 0;
-                while (base + ii <= e) { base += ii; ++ii; }
-                const int jj = e - base;
-                const double a = blk[(int64_t)ii * ld + jj];
-                double xa = 0.0, xb = 0.0;
+        } else {
 #pragma unroll
-                for (int q = 0; q < kSmallGroup; ++q) {
-                    if (q == jj) xa = xi[q];
-                    if (q == ii) xb = xi[q];
-                }
+            for (int ii = 1; ii < M; ++ii) {
+                if (ii < np) {
 #pragma unroll
-                for (int q = 0; q < kSmallGroup; ++q) {
-                    if (q == ii) sr[q] += a * xa;
-                    if (q == jj) sr[q] += a * xb;
+                    for (int jj = 0; jj < ii; ++jj) {
+                        const double a = blk[(int64_t)ii * ld + jj];
+                        sr[ii] += a * xi[jj];
+                        sr[jj] += a * xi[ii];
+                    }
                 }
             }
         }
+        double *rp = rowPart + bl * kSmallGroup;
 #pragma unroll
-        for (int ii = 0; ii < kSmallGroup; ++ii) {
-            double v = sr[ii];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (ln == 0) rowPart[it * kSmallGroup + ii] = v;
-        }
+        for (int ii = 0; ii < M; ++ii) rp[ii] = sr[ii];
     }
 }
 
-__global__ void __launch_bounds__(256) k_spmv_groups(int32_t nG, const int32_t *aig, const int64_t *itemBeg,
+__global__ void __launch_bounds__(256) k_spmv_groups(int32_t nG, const int32_t *aig, const int64_t *rowStart,
                                                      const double *rowPart, const int64_t *colStart,
                                                      const int64_t *tBase, const double *tbuf,
                                                      const double *matD, const double *x, double *y) {
@@ -591,17 +572,24 @@ __global__ void __launch_bounds__(256) k_spmv_groups(int32_t nG, const int32_t *
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t J = 1 + w; J <= nG; J += nw) {
         const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
+        const int64_t r0 = rowStart[J - 1], nr = rowStart[J] - r0;
         const int64_t cnt = colStart[J] - colStart[J - 1];
         const double *t = tbuf + tBase[J - 1];
         for (int jj = 0; jj < nj; ++jj) {
-            double v = 0.0;
-            for (int64_t q = ln; q < cnt; q += 32) v += t[(int64_t)jj * cnt + q];
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (ln == 0) {
-                double r = matD[ja + jj] * x[ja + jj];
-                for (int64_t it = itemBeg[J - 1]; it < itemBeg[J]; ++it) r += rowPart[it * kSmallGroup + jj];
-                y[ja + jj] = r + v;
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+            for (int64_t q = ln; q < nr; q += 32) v0 += rowPart[(r0 + q) * kSmallGroup + jj];
+            const double *tj = t + (int64_t)jj * cnt;
+            int64_t q = ln;
+            for (; q + 96 < cnt; q += 128) {
+                v0 += tj[q];
+                v1 += tj[q + 32];
+                v2 += tj[q + 64];
+                v3 += tj[q + 96];
             }
+            for (; q < cnt; q += 32) v1 += tj[q];
+            double v = (v0 + v1) + (v2 + v3);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (ln == 0) y[ja + jj] = matD[ja + jj] * x[ja + jj] + v;
         }
     }
 }
@@ -904,7 +892,7 @@ struct Solver {
         dfree(wyPart); dfree(wyT);
         dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
         dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tBase); dfree(sb.tbuf); dfree(part);
-        dfree(sb.tStr); dfree(sb.itemGroup); dfree(sb.itemB0); dfree(sb.itemBeg); dfree(sb.rowPart);
+        dfree(sb.tStr); dfree(sb.brow); dfree(sb.rowPart);
         dfree(pmvRow); dfree(pmvPart);
     }
     unsigned grid(int64_t n, int per = kThreads) const {
@@ -1020,23 +1008,9 @@ struct Solver {
                 off += cnt * nj;
             }
         }
-        // work items of at most kItemBlocks blocks per row group
-        std::vector<int32_t> itemGroup;
-        std::vector<int64_t> itemB0, itemBeg(j.nG + 1, 0);
-        for (int32_t I = 1; I <= j.nG; ++I) {
-            itemBeg[I - 1] = (int64_t)itemGroup.size();
-            for (int64_t b = rowStart[I - 1]; b < rowStart[I] || b == rowStart[I - 1]; b += kItemBlocks) {
-                itemGroup.push_back(I);
-                itemB0.push_back(b);
-                if (rowStart[I] == rowStart[I - 1]) break;
-            }
-        }
-        itemBeg[j.nG] = (int64_t)itemGroup.size();
-        // item ends: the next item's start, or the group's end
-        std::vector<int64_t> itemB(itemB0.size() + 1);
-        for (size_t q = 0; q < itemB0.size(); ++q) itemB[q] = itemB0[q];
-        itemB[itemB0.size()] = nb;
-        sb.nItem = (int64_t)itemGroup.size();
+        int32_t minnp = maxnp;
+        for (int32_t I = 1; I <= j.nG; ++I) minnp = std::min(minnp, aig[I] - aig[I - 1]);
+        sb.uniform = (sb.smallGroups && minnp == maxnp) ? maxnp : 0;
         sb.nblk = nb;
         sb.tlen = tl;
         auto up = [&](auto *&d, const auto &h) -> cudaError_t {
@@ -1054,10 +1028,8 @@ struct Solver {
         MPG_CUDA(c, up(sb.tBase, tBase));
         if (sb.smallGroups) {
             MPG_CUDA(c, up(sb.tStr, tStr));
-            MPG_CUDA(c, up(sb.itemGroup, itemGroup));
-            MPG_CUDA(c, up(sb.itemB0, itemB));
-            MPG_CUDA(c, up(sb.itemBeg, itemBeg));
-            MPG_CUDA(c, cudaMalloc((void **)&sb.rowPart, sizeof(double) * std::max<int64_t>(sb.nItem, 1) * kSmallGroup));
+            MPG_CUDA(c, up(sb.brow, brow));
+            MPG_CUDA(c, cudaMalloc((void **)&sb.rowPart, sizeof(double) * std::max<int64_t>(nb, 1) * kSmallGroup));
         }
         MPG_CUDA(c, cudaMalloc((void **)&sb.tbuf, sizeof(double) * std::max<int64_t>(tl, 1)));
         return MPGPU_OK;
@@ -1066,10 +1038,23 @@ struct Solver {
     // y = A x (full parameter space)
     void avprd0(const double *x, double *y) {
         if (j.matsto == 2 && sb.smallGroups) {
-            k_spmv_items<<<wgrid(sb.nItem), kThreads, 0, s>>>(sb.nItem, sb.itemGroup, sb.itemB0, j.aig, sb.bcol,
-                                                              sb.boff, sb.bld, sb.tOff, sb.tStr, j.matD, x,
-                                                              sb.tbuf, sb.rowPart);
-            k_spmv_groups<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.itemBeg, sb.rowPart, sb.colStart,
+            const unsigned gb = grid(sb.nblk);
+#define MPG_SPMV_BLOCKS(G)                                                                                  \
+    k_spmv_blocks<G><<<gb, kThreads, 0, s>>>(sb.nblk, sb.brow, j.aig, sb.bcol, sb.boff, sb.bld, sb.tOff, sb.tStr, \
+                                             j.matD, x, sb.tbuf, sb.rowPart)
+            switch (sb.uniform) {
+            case 1: MPG_SPMV_BLOCKS(1); break;
+            case 2: MPG_SPMV_BLOCKS(2); break;
+            case 3: MPG_SPMV_BLOCKS(3); break;
+            case 4: MPG_SPMV_BLOCKS(4); break;
+            case 5: MPG_SPMV_BLOCKS(5); break;
+            case 6: MPG_SPMV_BLOCKS(6); break;
+            case 7: MPG_SPMV_BLOCKS(7); break;
+            case 8: MPG_SPMV_BLOCKS(8); break;
+            default: MPG_SPMV_BLOCKS(0); break;
+            }
+#undef MPG_SPMV_BLOCKS
+            k_spmv_groups<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.rowPart, sb.colStart,
                                                            sb.tBase, sb.tbuf, j.matD, x, y);
         } else if (j.matsto == 2) {
             k_spmv_rows<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.bcol, sb.boff, sb.bld,
