@@ -96,8 +96,6 @@ __global__ void __launch_bounds__(32) k_lltdec(int32_t n, int32_t w, const doubl
     extern __shared__ double win[];
     const int W1 = w + 1;
     uint16_t *pairs = reinterpret_cast<uint16_t *>(win + W1 * W1);
-    __shared__ double sd;
-    __shared__ int sreset;
     const int ln = threadIdx.x;
     const int npair = w * (w + 1) / 2;
     // pairs (qm, ql), 1 <= ql <= qm <= w, row-major
@@ -121,10 +119,10 @@ __global__ void __launch_bounds__(32) k_lltdec(int32_t n, int32_t w, const doubl
         if (mn < n && ln < W1) nxt = B[(int64_t)mn * W1 + ln];
         const double orig = origNext;
         if (ln == 0 && k + 1 < n) origNext = B[(int64_t)(k + 1) * W1 + w];
+        double d = 0.0;
+        int reset = 0;
         if (ln == 0) {
             const double a = win[sk * W1 + w];
-            double d = 0.0;
-            int reset = 0;
             if (k == 0) {
                 if (a > 0.0) d = 1.0 / sqrt(a);
                 else nrkd = -1;
@@ -141,37 +139,34 @@ __global__ void __launch_bounds__(32) k_lltdec(int32_t n, int32_t w, const doubl
                     nrkd = nrkd + 1;
                 }
             }
-            sd = d;
-            sreset = reset;
             F[(int64_t)k * W1 + w] = d;
         }
-        __syncwarp();
-        const double d = sd;
-        const int reset = sreset;
+        d = __shfl_sync(kFull, d, 0);
+        reset = __shfl_sync(kFull, reset, 0);
         if (reset)
             for (int t = ln; t < w; t += 32) F[(int64_t)k * W1 + t] = 0.0;
-        // column k of rows k+1 .. k+mmax; a reset row k leaves them
-        // (a_mk - 0) * d with the original a_mk
+        // column k of rows k+1 .. k+mmax goes to F only (later steps use
+        // columns right of k); each lane forms the column entries it needs
+        // for the trailing update again, the same product; a reset row k
+        // leaves them (a_mk - 0) * d with the original a_mk
         const int mmax = min(w, n - 1 - k);
         for (int q = 1 + ln; q <= mmax; q += 32) {
             const int32_t m = k + q;
-            const int idx = (m % W1) * W1 + (w - q);
-            const double a = reset ? B[(int64_t)m * W1 + (w - q)] : win[idx];
-            const double cv = __dmul_rn(a, d);
-            win[idx] = cv;
-            F[(int64_t)m * W1 + (w - q)] = cv;
+            const double a = reset ? B[(int64_t)m * W1 + (w - q)] : win[(m % W1) * W1 + (w - q)];
+            F[(int64_t)m * W1 + (w - q)] = __dmul_rn(a, d);
         }
-        __syncwarp();
         // trailing update of the window: (m, l) -= c_mk c_lk, k < l <= m
         for (int e = ln; e < npair; e += 32) {
             const int qm = pairs[e] >> 8, ql = pairs[e] & 0xff;
             if (qm > mmax) continue;
             const int rm = ((k + qm) % W1) * W1, rl = ((k + ql) % W1) * W1;
-            const double cm = win[rm + (w - qm)], cl = win[rl + (w - ql)];
+            const double am = reset ? B[(int64_t)(k + qm) * W1 + (w - qm)] : win[rm + (w - qm)];
+            const double al = reset ? B[(int64_t)(k + ql) * W1 + (w - ql)] : win[rl + (w - ql)];
+            const double cm = __dmul_rn(am, d), cl = __dmul_rn(al, d);
             double &x = win[rm + (w - qm + ql)];
             x = __dsub_rn(x, __dmul_rn(cm, cl));
         }
-        __syncwarp();
+        // row k's slot takes row k + w + 1 (no lane reads it in this step)
         if (mn < n && ln < W1) win[sk * W1 + ln] = nxt;
         __syncwarp();
     }
