@@ -1264,11 +1264,24 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
         if (rc) return rc;
     }
     MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
-    std::vector<double *> bufs;
+    // workspace released on every return
+    struct Scratch {
+        std::vector<double *> bufs;
+        MinresState *St = nullptr;
+        QlpState *Qs = nullptr;
+        cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+        ~Scratch() {
+            for (double *p : bufs) cudaFree(p);
+            if (St) cudaFree(St);
+            if (Qs) cudaFree(Qs);
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
+        }
+    } W;
     auto vec = [&](int64_t len) -> double * {
         double *p = nullptr;
         if (cudaMalloc(&p, sizeof(double) * std::max<int64_t>(len, 1)) != cudaSuccess) return nullptr;
-        bufs.push_back(p);
+        W.bufs.push_back(p);
         return p;
     };
     double *rhs = vec(n), *xa = vec(n), *ba = vec(n), *dg = vec(n), *cu = vec(n), *tmp = vec(n), *yk = vec(n);
@@ -1276,13 +1289,13 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     double *x = vec(n);
     double *wa = nullptr, *wb = nullptr, *xp = nullptr, *xc = nullptr;
     if (qlp) { wa = vec(n); wb = vec(n); xp = vec(n); xc = vec(n); }
-    MinresState *St = nullptr;
-    QlpState *Qs = nullptr;
+    MinresState *&St = W.St;
+    QlpState *&Qs = W.Qs;
     MPG_CUDA(c, cudaMalloc(&St, sizeof(MinresState)));
     if (qlp) MPG_CUDA(c, cudaMalloc(&Qs, sizeof(QlpState)));
-    for (double *p : bufs)
+    for (double *p : W.bufs)
         if (!p) return set_err(c, MPGPU_ERR_ALLOC, "MINRES workspace");
-    cudaEvent_t e0, e1;
+    cudaEvent_t &e0 = W.ev[0], &e1 = W.ev[1], &ep = W.ev[2];
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, s);
@@ -1310,7 +1323,6 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     const int32_t mbandw = c->mbandw;
     BandPre P;
     struct BandGuard { BandPre &p; ~BandGuard() { band_free(p); } } bandGuard{P};
-    cudaEvent_t ep;
     cudaEventCreate(&ep);
     if (mbandw == 0) {
         if (j.matsto == 2) k_sparse_diag<<<S.grid(n), kThreads, 0, s>>>(n, j.matD, dg);
@@ -1321,7 +1333,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
         k_fill<<<S.grid(nfit), kThreads, 0, s>>>(nfit, 1.0, cu);
         if (mbandw > 0) {
             int32_t rc = S.band_build(P, mbandw, c->lprecm, v, tmp, yk, dsc);
-            if (rc) { cudaEventDestroy(ep); return rc; }
+            if (rc) return rc;
         }
     }
     cudaEventRecord(ep, s);
@@ -1417,12 +1429,6 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     cudaEventElapsedTime(&ms, e0, ep);
     info->msFactor = ms;
     if (mbandw > 0) cudaMemcpy(&info->nrkd, P.nrkd, sizeof(int32_t), cudaMemcpyDeviceToHost);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaEventDestroy(ep);
-    for (double *p : bufs) cudaFree(p);
-    cudaFree(St);
-    if (Qs) cudaFree(Qs);
     return MPGPU_OK;
 }
 
@@ -1463,11 +1469,19 @@ int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double
         if (rc) return rc;
     }
     MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
-    double *v = nullptr, *tmp = nullptr, *yk = nullptr;
+    struct Bufs {
+        double *v = nullptr, *tmp = nullptr, *yk = nullptr;
+        BandPre P;
+        ~Bufs() {
+            cudaFree(v); cudaFree(tmp); cudaFree(yk);
+            band_free(P);
+        }
+    } bb;
+    double *&v = bb.v, *&tmp = bb.tmp, *&yk = bb.yk;
     MPG_CUDA(c, cudaMalloc(&v, sizeof(double) * std::max(n, 1)));
     MPG_CUDA(c, cudaMalloc(&tmp, sizeof(double) * std::max(n, 1)));
     MPG_CUDA(c, cudaMalloc(&yk, sizeof(double) * std::max(n, 1)));
-    BandPre P;
+    BandPre &P = bb.P;
     int32_t rc = S.band_build(P, mbandw, lprecm, v, tmp, yk, c->scal + 300);
     if (!rc) {
         const int W1 = P.w + 1;
@@ -1479,7 +1493,5 @@ int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double
         for (int32_t i = 0; !rc && i < nfit; ++i)
             for (int32_t t = std::max(0, P.w - i); t <= P.w; ++t) cOut[pos++] = F[(size_t)i * W1 + t];
     }
-    band_free(P);
-    cudaFree(v); cudaFree(tmp); cudaFree(yk);
     return rc;
 }
