@@ -30,9 +30,19 @@
  *                         (pede.f90:2613; routine at 3387-4442) with the
  *                         mgupdt flush (pede.f90:3219-3357)
  *   mpgpu_mupdat          CALL mupdat(i,j,add) (pede.f90:3134-3204)
- *   mpgpu_solve           CALL minver / mchdec / mminrs (pede.f90:8832-8855)
+ *   mpgpu_solve           CALL minver / mchdec / mminrs / mminrsqlp
+ *                         (pede.f90:8832-8855)
+ *   mpgpu_set_preconditioner  steering "bandwidth mbandw lprecm"
+ *                         (pede.f90:10495-10503), used by mminrs 8292-8316
+ *   mpgpu_band_factor     CALL equdecs on matPreCond (pede.f90:8309,
+ *                         mpnum.f90:2486-2592)
  *   mpgpu_avprod          SUBROUTINE avprod(n,x,b) (pede.f90:5331-5358)
  *   mpgpu_download_matrix globalMatD after the data loop
+ *   mpgpu_set_monitor /   measIndex/measRes and measHists of
+ *   mpgpu_get_monitor     monitorresiduals/monitorpulls (pede.f90:6571-6579,
+ *                         3967-3990); mpgpu_write_mon: monres (7533-7633)
+ *   mpgpu_read_mille      readC / readF of the binary files (pede.f90:1714-2075)
+ *   mpgpu_write_res       prtglo (pede.f90:4477-4651)
  */
 #ifndef MPGPU_H
 #define MPGPU_H
