@@ -423,6 +423,13 @@ struct SparseBlocks {
     int32_t *brow = nullptr;       // [nblk]
     int32_t *tStr = nullptr;       // [nblk]
     double *rowPart = nullptr;     // [nblk * kSmallGroup]
+    // column items: at most kColItem incoming blocks of one column group
+    int64_t nColItem = 0;
+    int32_t *colItemJ = nullptr;   // [nColItem]
+    int64_t *colItemQ0 = nullptr;  // [nColItem] first incoming block (0-based within the group)
+    int64_t *colItemQ1 = nullptr;  // [nColItem] end
+    int64_t *colItemBeg = nullptr; // [nG+1] first item of column group J
+    double *colPart = nullptr;     // [nColItem * kSmallGroup]
     int uniform = 0;               // every group has this many parameters (0: mixed)
 };
 
@@ -492,10 +499,10 @@ __global__ void k_spmv_cols(int32_t nG, const int32_t *aig, const int64_t *colSt
 // triangles of its strictly-lower part there) and its columns times x_I
 // into tbuf (parameter-major per column group).  G > 0: every group has G
 // parameters (loops fully unrolled); G = 0: at most 8, predicated.  Phase
-// 2, one warp per group: y = D x + the partial row sums of the group's
-// blocks + the transposed products of its incoming blocks, the lanes over
-// both lists with four independent partial sums each, then a fixed shuffle
-// tree; no atomics, the sums are reproducible.
+// 2: the partial row sums of a group's blocks and the transposed products
+// of its incoming blocks summed by column items (long columns split over
+// several warps), then y = D x + the group's items in item order; no
+// atomics, the sums are reproducible.
 constexpr int kSmallGroup = 8;
 
 template <int G>
@@ -563,34 +570,60 @@ __global__ void __launch_bounds__(256) k_spmv_blocks(int64_t nb, const int32_t *
     }
 }
 
-__global__ void __launch_bounds__(256) k_spmv_groups(int32_t nG, const int32_t *aig, const int64_t *rowStart,
-                                                     const double *rowPart, const int64_t *colStart,
-                                                     const int64_t *tBase, const double *tbuf,
-                                                     const double *matD, const double *x, double *y) {
+// phase 2a, one warp per column item (at most kColItem incoming blocks of
+// one column group; the first item of a group also takes the partial row
+// sums of the group's own blocks): lanes with four independent partial
+// sums, a fixed shuffle tree, into colPart (8 per item)
+constexpr int kColItem = 128;
+
+__global__ void __launch_bounds__(256) k_spmv_colitems(int64_t nItem, const int32_t *itemJ, const int64_t *itemQ0,
+                                                       const int64_t *itemQ1, const int32_t *aig,
+                                                       const int64_t *rowStart, const double *rowPart,
+                                                       const int64_t *colStart, const int64_t *tBase,
+                                                       const double *tbuf, double *colPart) {
     const int ln = threadIdx.x & 31;
     const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t J = 1 + w; J <= nG; J += nw) {
-        const int32_t ja = aig[J - 1] - 1, nj = aig[J] - 1 - ja;
-        const int64_t r0 = rowStart[J - 1], nr = rowStart[J] - r0;
+    for (int64_t it = w; it < nItem; it += nw) {
+        const int32_t J = itemJ[it];
+        const int32_t nj = aig[J] - aig[J - 1];
+        const int64_t q0 = itemQ0[it], q1 = itemQ1[it];
+        const bool first = q0 == 0;
+        const int64_t r0 = rowStart[J - 1], nr = first ? rowStart[J] - r0 : 0;
         const int64_t cnt = colStart[J] - colStart[J - 1];
         const double *t = tbuf + tBase[J - 1];
-        for (int jj = 0; jj < nj; ++jj) {
-            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
-            for (int64_t q = ln; q < nr; q += 32) v0 += rowPart[(r0 + q) * kSmallGroup + jj];
-            const double *tj = t + (int64_t)jj * cnt;
-            int64_t q = ln;
-            for (; q + 96 < cnt; q += 128) {
-                v0 += tj[q];
-                v1 += tj[q + 32];
-                v2 += tj[q + 64];
-                v3 += tj[q + 96];
+        for (int jj = 0; jj < kSmallGroup; ++jj) {
+            double v = 0.0;
+            if (jj < nj) {
+                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+                for (int64_t q = ln; q < nr; q += 32) v0 += rowPart[(r0 + q) * kSmallGroup + jj];
+                const double *tj = t + (int64_t)jj * cnt;
+                int64_t q = q0 + ln;
+                for (; q + 96 < q1; q += 128) {
+                    v0 += tj[q];
+                    v1 += tj[q + 32];
+                    v2 += tj[q + 64];
+                    v3 += tj[q + 96];
+                }
+                for (; q < q1; q += 32) v1 += tj[q];
+                v = (v0 + v1) + (v2 + v3);
             }
-            for (; q < cnt; q += 32) v1 += tj[q];
-            double v = (v0 + v1) + (v2 + v3);
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (ln == 0) y[ja + jj] = matD[ja + jj] * x[ja + jj] + v;
+            if (ln == 0) colPart[it * kSmallGroup + jj] = v;
         }
+    }
+}
+
+// phase 2b, one thread per parameter: y = D x + the column items of its
+// group in item order
+__global__ void k_spmv_final(int32_t n, const int32_t *aig, const int32_t *p2g, const int64_t *colItemBeg,
+                             const double *colPart, const double *matD, const double *x, double *y) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t J = p2g[j];
+        const int32_t jj = (int32_t)j - (aig[J - 1] - 1);
+        double r = matD[j] * x[j];
+        for (int64_t it = colItemBeg[J - 1]; it < colItemBeg[J]; ++it) r += colPart[it * kSmallGroup + jj];
+        y[j] = r;
     }
 }
 
@@ -893,6 +926,7 @@ struct Solver {
         dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
         dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tBase); dfree(sb.tbuf); dfree(part);
         dfree(sb.tStr); dfree(sb.brow); dfree(sb.rowPart);
+        dfree(sb.colItemJ); dfree(sb.colItemQ0); dfree(sb.colItemQ1); dfree(sb.colItemBeg); dfree(sb.colPart);
         dfree(pmvRow); dfree(pmvPart);
     }
     unsigned grid(int64_t n, int per = kThreads) const {
@@ -1008,6 +1042,21 @@ struct Solver {
                 off += cnt * nj;
             }
         }
+        std::vector<int32_t> ciJ;
+        std::vector<int64_t> ciQ0, ciQ1, ciBeg(j.nG + 1, 0);
+        for (int32_t J = 1; J <= j.nG; ++J) {
+            ciBeg[J - 1] = (int64_t)ciJ.size();
+            const int64_t cnt = colStart[J] - colStart[J - 1];
+            int64_t q = 0;
+            do {
+                ciJ.push_back(J);
+                ciQ0.push_back(q);
+                ciQ1.push_back(std::min<int64_t>(cnt, q + kColItem));
+                q += kColItem;
+            } while (q < cnt);
+        }
+        ciBeg[j.nG] = (int64_t)ciJ.size();
+        sb.nColItem = (int64_t)ciJ.size();
         int32_t minnp = maxnp;
         for (int32_t I = 1; I <= j.nG; ++I) minnp = std::min(minnp, aig[I] - aig[I - 1]);
         sb.uniform = (sb.smallGroups && minnp == maxnp) ? maxnp : 0;
@@ -1030,6 +1079,11 @@ struct Solver {
             MPG_CUDA(c, up(sb.tStr, tStr));
             MPG_CUDA(c, up(sb.brow, brow));
             MPG_CUDA(c, cudaMalloc((void **)&sb.rowPart, sizeof(double) * std::max<int64_t>(nb, 1) * kSmallGroup));
+            MPG_CUDA(c, up(sb.colItemJ, ciJ));
+            MPG_CUDA(c, up(sb.colItemQ0, ciQ0));
+            MPG_CUDA(c, up(sb.colItemQ1, ciQ1));
+            MPG_CUDA(c, up(sb.colItemBeg, ciBeg));
+            MPG_CUDA(c, cudaMalloc((void **)&sb.colPart, sizeof(double) * std::max<int64_t>(sb.nColItem, 1) * kSmallGroup));
         }
         MPG_CUDA(c, cudaMalloc((void **)&sb.tbuf, sizeof(double) * std::max<int64_t>(tl, 1)));
         return MPGPU_OK;
@@ -1054,8 +1108,11 @@ struct Solver {
             default: MPG_SPMV_BLOCKS(0); break;
             }
 #undef MPG_SPMV_BLOCKS
-            k_spmv_groups<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.rowPart, sb.colStart,
-                                                           sb.tBase, sb.tbuf, j.matD, x, y);
+            k_spmv_colitems<<<wgrid(sb.nColItem), kThreads, 0, s>>>(sb.nColItem, sb.colItemJ, sb.colItemQ0,
+                                                                    sb.colItemQ1, j.aig, sb.rowStart, sb.rowPart,
+                                                                    sb.colStart, sb.tBase, sb.tbuf, sb.colPart);
+            k_spmv_final<<<grid(j.nVar), kThreads, 0, s>>>(j.nVar, j.aig, j.p2g, sb.colItemBeg, sb.colPart, j.matD,
+                                                           x, y);
         } else if (j.matsto == 2) {
             k_spmv_rows<<<wgrid(j.nG), kThreads, 0, s>>>(j.nG, j.aig, sb.rowStart, sb.bcol, sb.boff, sb.bld,
                                                          sb.tOff, j.matD, x, y, sb.tbuf);
