@@ -24,6 +24,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -93,7 +94,10 @@ class ClockSampler:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples in MPGPU_CLOCK_DIR when given (kept for inspection),
+        # else in the temporary directory; the summary goes into the line
+        base = os.environ.get("MPGPU_CLOCK_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(base, f"clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
