@@ -383,11 +383,31 @@ def structure_measure(mp, S, pinned, device, host_s, ncores):
             "speedup": host_s / statistics.median(times), "tables_identical": same}
 
 
-def profile_part(mp, part, ntracks, device, steps):
+def profile_part(mp, part, ntracks, device, steps, mbandw=0):
     """One part of the path on a small case, for profilers: the record
     upload (barrel), the device structure passes (barrel) or the data loop
     of broken-line records (size classes, no tuning).  Each repeats `steps`
-    times after one untimed pass."""
+    times after one untimed pass.  `minres`: the barrel (seed 4) with its
+    constraints, sparse matrix from one data loop, then two MINRES solves
+    of `steps` iterations each (rtol below reach) with preconditioner
+    `mbandw` (0 diagonal, > 0 band width)."""
+    if part == "minres":
+        d = mp.generate(mp.gen_config("barrel", ntracks=ntracks, seed=4))
+        H = mp.HostStructure(d, mreqenf=5, sparse=True)
+        A = mp.constraint_matrix(d, H)
+        out = {"part": part, "n": int(H.nVar), "ncon": int(A.shape[0]), "mbandw": mbandw, "solves": []}
+        with mp.Context(device=device) as ctx:
+            ctx.set_layout(H, 2)
+            ctx.set_constraints(A)
+            ctx.upload(H)
+            ctx.loopbf(np.zeros(H.nTotal))
+            ctx.set_preconditioner(mbandw)
+            for _ in range(2):
+                _, _, info = ctx.solve(4, consResiduals=np.zeros(A.shape[0]), rtol=1e-30, itnlim=steps)
+                out["solves"].append({"itn": info.itn, "ms": info.ms, "ms_setup": info.msFactor,
+                                      "ms_per_iteration": (info.ms - info.msFactor) / max(info.itn, 1)})
+        print(json.dumps(out))
+        return
     kind = "brokenlines" if part == "brokenlines" else "barrel"
     d = mp.generate(mp.gen_config(kind, ntracks=ntracks, seed=3 if kind == "brokenlines" else 2))
     flags = mp.FLAG_NO_AUTOTUNE if part == "brokenlines" else 0
@@ -423,8 +443,9 @@ def main():
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
     ap.add_argument("--minres-iters", type=int, default=300, help="iterations of the MINRES measurement (0: skip)")
+    ap.add_argument("--mbandw", type=int, default=0, help="--part minres: preconditioner (0 diagonal, > 0 band width)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
-    ap.add_argument("--part", default="loop", choices=["loop", "upload", "structure", "brokenlines"],
+    ap.add_argument("--part", default="loop", choices=["loop", "upload", "structure", "brokenlines", "minres"],
                     help="with --profile: the part to run on --ntracks records (for profilers)")
     ap.add_argument("--brokenlines", type=int, default=200_000,
                     help="records of the uneven-record (broken-line) measurement (0: skip)")
@@ -432,7 +453,7 @@ def main():
     rank, world, local, pg = dist_setup(args.gpus)
     mp = _load_pkg()
     if args.profile and args.part != "loop":
-        profile_part(mp, args.part, args.ntracks, local, args.steps)
+        profile_part(mp, args.part, args.ntracks, local, args.steps, args.mbandw)
         return
     cfg = mp.gen_config("barrel", ntracks=args.ntracks, seed=2 + 1000 * rank)
     t0 = time.time()
