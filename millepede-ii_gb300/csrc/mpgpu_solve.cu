@@ -1161,14 +1161,20 @@ struct Solver {
     void qlmlq(double *x, int t) {
         if (j.ncon <= 0) return;
         const int32_t m = j.ncon, n = j.nVar;
-        if (m > 4096) {  // coefficients beyond the shared memory of one CTA
+        if (!wyPart && m <= 4096) {
+            if (cudaMalloc(&wyPart, sizeof(double) * (size_t)kWyBlocks * m) != cudaSuccess ||
+                cudaMalloc(&wyT, sizeof(double) * m) != cudaSuccess) {
+                dfree(wyPart);
+                dfree(wyT);
+                cudaGetLastError();
+            }
+        }
+        // coefficients beyond the shared memory of one CTA, or no workspace:
+        // the reflections one after the other in one CTA
+        if (m > 4096 || !wyPart || !wyT) {
             if (t) k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, n, m, m, 1, -1);
             else k_qlapply<<<1, 1024, 0, s>>>(x, j.qlV, j.qlVk, j.qlR2, n, m, 1, m, 1);
             return;
-        }
-        if (!wyPart) {
-            cudaMalloc(&wyPart, sizeof(double) * (size_t)kWyBlocks * m);
-            cudaMalloc(&wyT, sizeof(double) * m);
         }
         const int nb = (int)std::min<int64_t>(kWyBlocks, std::max<int64_t>(1, n / 512));
         k_wy_dots<<<nb, 256, 0, s>>>(n, m, j.qlV, x, wyPart);
