@@ -237,6 +237,19 @@ def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
     ctx.close()
     fmas = 2 * (len(M) - H.nVar) + H.nVar
     out["spmv_fp64_bound_us"] = fmas / (2 * 152 * 2.07e9) * 1e6
+    # algorithmic bytes per iteration: the stored matrix and its column
+    # words once, about ten vectors of N doubles
+    try:
+        hbm = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs", 6800.0))
+        src = "MEASURED_PEAKS.json hbm_gbs"
+    except (OSError, ValueError):
+        hbm, src = 6800.0, "fallback"
+    nbytes = 8 * len(M) + 4 * int(H.ncolw) + 80 * H.nVar
+    gbs = nbytes / (out["ms_per_iteration_diagonal"] * 1e-3) / 1e9
+    out["roofline_diagonal"] = {"bytes_per_iteration": nbytes, "achieved_gbs": gbs, "peak_gbs": hbm,
+                                "frac": gbs / hbm, "peak_source": src,
+                                "hbm_bound_us": nbytes / (hbm * 1e9) * 1e6,
+                                "binding": "fp64" if out["spmv_fp64_bound_us"] > nbytes / (hbm * 1e3) else "hbm"}
     # the oracle's MINRES (diagonal) on one host core, same matrix and rhs
     L = orc.lib()
     f64p, i32p, i64p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
