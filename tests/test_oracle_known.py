@@ -363,3 +363,18 @@ def test_minres_preconditioners(orc, qlp, mbandw):
     assert rel(x, np.linalg.solve(A, b)) <= 1e-9
     if mbandw >= n:
         assert itn.value <= 2
+
+
+def test_job_band_preconditioner_same_solution(mp):
+    """The oracle's job driver with MINRES and pede's "bandwidth 6" reaches
+    the parameters of the diagonal preconditioner (well-determined
+    telescope with its constraints) within 1e-8."""
+    d = mp.generate(mp.gen_config("telescope", ntracks=3000, seed=7))
+    out = {}
+    for mb in (0, 6, -1):
+        st = O.make_steer(metsol=4, matsto=2, mitera=1, mrestl=1e-13, itnlim=3000, mreqenf=5, mbandw=mb)
+        out[mb] = O.run(d, st)
+        assert out[mb]["rc"] == 0
+    scale = np.max(np.abs(out[0]["parameter"]))
+    for mb in (6, -1):
+        assert np.max(np.abs(out[mb]["parameter"] - out[0]["parameter"])) <= 1e-8 * scale
