@@ -236,6 +236,10 @@ int32_t mpref_band_precond(int32_t matsto, int32_t nVar, int32_t nG, const int32
                            const int64_t *offsets, const int32_t *columns, const double *matD,
                            const mpref_ql *q, int32_t mbandw, int32_t lprecm, double *c, int32_t *nrkd);
 void mpref_band_index(int32_t n, int32_t mbandw, int64_t *india);
+/* 1: form the preconditioner of the QL-reduced system (diagonal and band)
+ * by qlpssq's own route (mpqldec.f90:711-945) instead of the exact band of
+ * Q^T A Q; 0 (default): exact band, as the device does. */
+void mpref_set_qlpssq_literal(int32_t on);
 int32_t mpref_lltdec(int32_t n, double *c, const int64_t *india, int32_t iopt);
 void mpref_lltslv(int32_t n, const double *c, const int64_t *india, double *x);
 

@@ -529,6 +529,15 @@ static void avprod(const redop *o, const double *x, double *b)
     for (i = 0; i < n; i++) b[i] = o->ba[i];
 }
 
+static int g_qlpssq_literal;
+static void qlpssq_literal(const redop *o, int32_t mbandw, const int64_t *india, double *c);
+static double dotn(const double *a, const double *b, int32_t n)
+{
+    double s = 0.0;
+    for (int32_t i = 0; i < n; i++) s += a[i] * b[i];
+    return s;
+}
+
 /* diag(Q^T A Q) by explicit reflection tracking (see qlpssq,
  * mpqldec.f90:711-950, band width 1) */
 static void reduced_diag(const redop *o, double *dg)
@@ -541,6 +550,13 @@ static void reduced_diag(const redop *o, double *dg)
         else dg[i - 1] = o->matD[((int64_t)i * i - i) / 2 + i - 1];
     }
     if (!o->q) return;
+    if (g_qlpssq_literal) {  /* qlpssq with band width 1 (pede.f90:8295) */
+        int64_t *ind = (int64_t *)calloc((size_t)nV, sizeof(int64_t));
+        for (i = 0; i < nV; i++) ind[i] = i + 1;
+        qlpssq_literal(o, 1, ind, dg);
+        free(ind);
+        return;
+    }
     const mpref_ql *q = o->q;
     int32_t m = q->ncon;
     double *v = (double *)calloc((size_t)nV, sizeof(double));
@@ -612,6 +628,10 @@ static void reduced_band(const redop *o, int32_t mbandw, const int64_t *india, d
     }
     free(p2g);
     if (!o->q) return;
+    if (g_qlpssq_literal) {
+        qlpssq_literal(o, mbandw, india, c);
+        return;
+    }
     const mpref_ql *q = o->q;
     int32_t m = q->ncon;
     double *v = (double *)calloc((size_t)nV, sizeof(double));
@@ -655,6 +675,99 @@ static void reduced_band(const redop *o, int32_t mbandw, const int64_t *india, d
         }
     }
     free(v); free(y); free(tmp);
+}
+
+/* qlpssq (mpqldec.f90:711-945, t = .true.) literally: the band of width
+ * mbandw (variable-band layout india, all nVar rows) updated for the
+ * reflections through products of the untransformed matrix (first pass)
+ * and tables of the vectors' mutual products and coefficients (second
+ * pass), as the reference forms the preconditioner of the reduced system.
+ * Used when mpref_set_qlpssq_literal(1) is in force. */
+static int g_qlpssq_literal = 0;
+void mpref_set_qlpssq_literal(int32_t on) { g_qlpssq_literal = on; }
+
+static void qlpssq_literal(const redop *o, int32_t mbandw, const int64_t *india, double *c)
+{
+    const mpref_ql *q = o->q;
+    const int32_t npar = o->nVar, ncon = q->ncon, mbnd = mbandw - 1 > 0 ? mbandw - 1 : 0;
+    const double eps16 = 16.0 * DBL_EPSILON;
+    double *vtvp = (double *)calloc((size_t)ncon * ncon, sizeof(double));
+    double *vtAvp = (double *)calloc((size_t)ncon * ncon, sizeof(double));
+    double *coef = (double *)calloc((size_t)ncon * ncon, sizeof(double));
+    int32_t *rlo = (int32_t *)calloc((size_t)ncon + 1, sizeof(int32_t));
+    int32_t *rhi = (int32_t *)calloc((size_t)ncon + 1, sizeof(int32_t));
+    double *vN = (double *)calloc((size_t)npar, sizeof(double));
+    double *v2 = (double *)calloc((size_t)npar, sizeof(double));
+    double *vAv = (double *)calloc((size_t)npar, sizeof(double));
+    int32_t i, l, j, j2;
+#define V_(k, vec) do { int32_t ii_; for (ii_ = 0; ii_ < npar; ii_++) (vec)[ii_] = 0.0; \
+        for (ii_ = q->r1[k]; ii_ <= q->r2[k]; ii_++) (vec)[ii_ - 1] = q->V[(int64_t)((k) - 1) * npar + 1 + ii_ - q->r1[k]]; \
+        (vec)[npar + (k) - ncon - 1] = q->Vk[k]; } while (0)
+    /* the band update of mpqldec.f90:838-854 (and 883-898) */
+#define BAND_(vtAv, kn) do { int64_t q_ = 0; \
+        for (i = 1; i <= npar; i++) { const int64_t ia_ = india[i - 1]; \
+            for (l = (i - mbnd > 1 ? i - mbnd : 1); l <= i; l++) { q_ = ia_ - i + l - 1; \
+                if (i <= (kn)) c[q_] += 2.0 * ((2.0 * vN[i - 1] * (vtAv) - vAv[i - 1]) * vN[l - 1] - vAv[l - 1] * vN[i - 1]); \
+                else c[q_] -= 2.0 * vAv[i - 1] * vN[l - 1]; } } } while (0)
+    for (j = 1; j <= ncon; j++) {
+        const int32_t k = ncon + 1 - j, kn = npar + k - ncon;
+        rlo[k] = ncon;
+        rhi[k] = 1;
+        V_(k, vN);
+        mpref_avprd0(o->matsto, npar, vN, vAv, o->nG, o->aig, o->off, o->col, o->matD);
+        for (j2 = j + 1; j2 <= ncon; j2++) {
+            const int32_t k2 = ncon + 1 - j2;
+            V_(k2, v2);
+            const double x = dotn(vN, v2, npar);
+            if (fabs(x) > eps16) {
+                vtvp[(int64_t)(k - 1) * ncon + k2 - 1] = x;
+                vtvp[(int64_t)(k2 - 1) * ncon + k - 1] = x;
+            }
+        }
+        vtvp[(int64_t)(k - 1) * ncon + k - 1] = 1.0;
+        for (j2 = 1; j2 <= j; j2++) {
+            const int32_t k2 = ncon + 1 - j2;
+            V_(k2, v2);
+            vtAvp[(int64_t)(k - 1) * ncon + k2 - 1] = dotn(v2, vAv, npar);
+        }
+        BAND_(vtAvp[(int64_t)(k - 1) * ncon + k - 1], kn);
+    }
+    for (j = 1; j <= ncon; j++) {
+        const int32_t k = ncon + 1 - j, kn = npar + k - ncon;
+        const double *ck = coef + (int64_t)(k - 1) * ncon, *vk = vtvp + (int64_t)(k - 1) * ncon;
+        int32_t l1 = rlo[k], l2 = rhi[k], k2;
+        double vtAv = vtAvp[(int64_t)(k - 1) * ncon + k - 1];
+        for (k2 = l1; k2 <= l2; k2++) vtAv += ck[k2 - 1] * vk[k2 - 1];
+        V_(k, vN);
+        for (i = 0; i < npar; i++) vAv[i] = 0.0;
+        for (k2 = l1; k2 <= l2; k2++) {
+            if (ck[k2 - 1] == 0.0) continue;
+            V_(k2, v2);
+            for (i = 0; i < npar; i++) vAv[i] += ck[k2 - 1] * v2[i];
+        }
+        BAND_(vtAv, kn);
+        for (j2 = j + 1; j2 <= ncon; j2++) {
+            const int32_t kk2 = ncon + 1 - j2;
+            double *c2 = coef + (int64_t)(kk2 - 1) * ncon;
+            const double x = vk[kk2 - 1];
+            int32_t m1 = rlo[kk2], m2 = rhi[kk2], q2;
+            double va = vtAvp[(int64_t)(kk2 - 1) * ncon + k - 1];
+            for (q2 = m1; q2 <= m2; q2++) va += c2[q2 - 1] * vk[q2 - 1];
+            if (k < m1) m1 = k;
+            if (k > m2) m2 = k;
+            c2[k - 1] += 2.0 * (2.0 * vtAv * x - va);
+            if (x != 0.0) {
+                if (rlo[k] < m1) m1 = rlo[k];
+                if (rhi[k] > m2) m2 = rhi[k];
+                for (q2 = m1; q2 <= m2; q2++) c2[q2 - 1] -= 2.0 * ck[q2 - 1] * x;
+            }
+            rlo[kk2] = m1;
+            rhi[kk2] = m2;
+        }
+    }
+#undef V_
+#undef BAND_
+    free(vtvp); free(vtAvp); free(coef); free(rlo); free(rhi); free(vN); free(v2); free(vAv);
 }
 
 /* Preconditioned MINRES, Paige & Saunders (1975), SIAM J. Numer. Anal. 12,

@@ -5,8 +5,10 @@ update with vtAv = v^T A v again while no coefficient has been formed yet,
 so the restated route gives band(H A H) + 4 (v^T A v) band(v v^T): the
 reference's preconditioner (diagonal, mbandw 0, and band) carries that term
 once per reflection.  The preconditioners here use the exact band of
-Q^T A Q (tests/test_oracle_known.py); the MINRES solution does not depend
-on the preconditioner, its iteration count can."""
+Q^T A Q (tests/test_oracle_known.py); the oracle also carries the literal
+route (mpref_set_qlpssq_literal), checked here against the restatement.
+The MINRES solution does not depend on the preconditioner, its iteration
+count can."""
 import numpy as np
 
 
@@ -122,3 +124,66 @@ def test_one_reflection_adds_four_beta_vvT():
     extra = 4.0 * (u @ M @ u) * np.outer(u, u)
     assert np.max(np.abs((got - H @ M @ H - extra)[band])) <= 1e-12 * np.max(np.abs(M))
     assert np.max(np.abs((got - H @ M @ H)[band])) > 1e-3 * np.max(np.abs(M))
+
+
+def test_oracle_literal_route_matches_restatement(orc):
+    """The oracle's literal qlpssq route (mpref_set_qlpssq_literal) gives the
+    band of the step-by-step restatement above (three constraints, packed
+    matrix), compared through lltdec's factor of the fit rows."""
+    import ctypes as C
+    f64p, i32p, i64p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+    npar, ncon, mb = 30, 3, 4
+    rng = np.random.default_rng(5)
+    A = np.ascontiguousarray(rng.normal(size=(ncon, npar)))
+    V, Vk, r2 = qldec(A)
+    M = rng.normal(size=(npar, npar))
+    M = M + M.T + 4 * npar * np.eye(npar)
+    want_band = qlpssq_band(M, V, Vk, r2, mb)
+    L = orc.lib()
+    nfit = npar - ncon
+    india = np.zeros(npar, np.int64)
+    L.mpref_band_index(C.c_int32(npar), C.c_int32(mb), india.ctypes.data_as(i64p))
+    cw = np.zeros(int(india[nfit - 1]))
+    for k in range(nfit):
+        for jj in range(max(0, k - mb + 1), k + 1):
+            cw[india[k] - 1 - k + jj] = want_band[k, jj]
+    L.mpref_lltdec(C.c_int32(nfit), cw.ctypes.data_as(f64p), india.ctypes.data_as(i64p), C.c_int32(0))
+    L.mpref_ql_create.restype = C.c_void_p
+    q = L.mpref_ql_create(C.c_int32(npar), C.c_int32(ncon), A.ctypes.data_as(f64p))
+    packed = np.ascontiguousarray(M[np.tril_indices(npar)], np.float64)
+    aig = np.arange(1, npar + 2, dtype=np.int32)
+    cg = np.zeros_like(cw)
+    nrkd = C.c_int32()
+    L.mpref_set_qlpssq_literal(C.c_int32(1))
+    try:
+        rc = L.mpref_band_precond(C.c_int32(1), C.c_int32(npar), C.c_int32(npar), aig.ctypes.data_as(i32p), None,
+                                  None, packed.ctypes.data_as(f64p), C.c_void_p(q), C.c_int32(mb), C.c_int32(0),
+                                  cg.ctypes.data_as(f64p), C.byref(nrkd))
+    finally:
+        L.mpref_set_qlpssq_literal(C.c_int32(0))
+        L.mpref_ql_destroy(C.c_void_p(q))
+    assert rc == 0 and nrkd.value == 0
+    assert np.max(np.abs(cg - cw)) <= 1e-10 * np.max(np.abs(cw))
+
+
+def test_literal_route_same_solution(mp):
+    """MINRES on a job's QL-reduced system with the literal route's
+    preconditioners (diagonal and band 6) reaches the solution of the exact
+    preconditioners within 1e-8; only the iteration counts may differ."""
+    import oracle_ref as O
+    d = mp.generate(mp.gen_config("telescope", ntracks=3000, seed=9))
+    L = O.lib()
+    out = {}
+    for literal in (0, 1):
+        L.mpref_set_qlpssq_literal(literal)
+        try:
+            for mb in (0, 6):
+                st = O.make_steer(metsol=4, matsto=2, mitera=1, mrestl=1e-13, itnlim=3000, mreqenf=5, mbandw=mb)
+                r = O.run(d, st)
+                assert r["rc"] == 0
+                out[(literal, mb)] = r["parameter"]
+        finally:
+            L.mpref_set_qlpssq_literal(0)
+    scale = np.max(np.abs(out[(0, 0)]))
+    for key in ((1, 0), (1, 6), (0, 6)):
+        assert np.max(np.abs(out[key] - out[(0, 0)])) <= 1e-8 * scale
