@@ -235,18 +235,23 @@ int32_t mpgpu_mupdat(mpgpu_ctx *ctx, int32_t n, const int32_t *i, const int32_t 
  * a host loop that adds terms while other streams keep the device busy
  * (cudaFree would wait for all of them), or a job whose matrix and staging
  * fill the device memory.  The triplets are staged in a fixed device area of
- * MPGPU_MUPDAT_NOALLOC_MAX elements reserved when the library is loaded;
- * larger n returns MPGPU_ERR_LIMIT and changes nothing.  The area is one per
- * device and shared by all contexts on it: calls that overlap in time on the
- * same device race on it, so serialise them.  The first call on a device
- * looks up the area's address once; make it before any stream capture is
- * begun on that device.  Same result and error codes as mpgpu_mupdat. */
+ * MPGPU_MUPDAT_NOALLOC_MAX elements, one per device; CUDA reserves it when it
+ * loads the library's module holding it, which mpgpu_create forces on its
+ * device (the area is in place before the job's large allocations, and
+ * mpgpu_mupdat_noalloc itself never loads a module or reserves memory).
+ * Larger n returns MPGPU_ERR_LIMIT and changes nothing.  The area is shared
+ * by all contexts on a device: calls that overlap in time on the same device
+ * race on it, so serialise them.  Same result and error codes as
+ * mpgpu_mupdat. */
 #define MPGPU_MUPDAT_NOALLOC_MAX 65536
 int32_t mpgpu_mupdat_noalloc(mpgpu_ctx *ctx, int32_t n, const int32_t *i, const int32_t *j,
                              const double *add);
 int32_t mpgpu_vector_add(mpgpu_ctx *ctx, int32_t n, const int32_t *vidx, const double *vadd);
 
 int32_t mpgpu_download_matrix(mpgpu_ctx *ctx, double *globalMatD);
+/* diagonal[nVar] of the current global matrix (matij(i,i), the diagonal
+ * minver saves before the inversion, pede.f90:7864-7866) */
+int32_t mpgpu_matrix_diagonal(mpgpu_ctx *ctx, double *diagonal);
 int32_t mpgpu_download_vector(mpgpu_ctx *ctx, double *globalVector, int64_t *globalCounter);
 /* per-record outcome of the last loop: 0 accepted, 1..6 rejection class
  * (nrej index + 1), -1 no local parameters */
@@ -262,6 +267,8 @@ typedef struct mpgpu_solveinfo {
     double msFactor;    /* dense solves: device time of the factorisation; MINRES: of the
                            preconditioner set-up */
     double msRefine;    /* dense solves: device time of the CG refinement */
+    double dxRel;       /* dense solves: size of the last CG correction relative to the
+                           solution (|alpha p| / |x|) */
 } mpgpu_solveinfo;
 
 /* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES,
@@ -274,10 +281,12 @@ typedef struct mpgpu_solveinfo {
  * Decomposition also in blocked dense form (no counterpart in the
  * reference, same solution): metsol 32 FP64 blocked Cholesky, metsol 31
  * Cholesky with tensor-core 3xTF32 trailing updates; both refine the
- * solution by preconditioned CG in FP64 until the residual is below rtol
+ * solution by preconditioned CG in FP64 until the relative residual is
+ * below rtol and the last correction is below 1e-13 of the solution, so
+ * that factors of either precision reach the same FP64 solution
  * (info->itn iterations, info->istop 1 converged / 3 limit, info->evmin the
  * diagonal shift the low-precision factor needed, info->evmax the final
- * relative residual).
+ * relative residual, info->dxRel the last relative correction).
  * consResiduals[ncon] = d - C p (addcst); correction[nVar] receives the
  * step; errors[nVar] (metsol 1, may be NULL) the diagonal of the covariance
  * (sqrt gives the parameter errors).  rtol/itnlim: MINRES(-QLP) tolerance and
@@ -382,6 +391,16 @@ typedef struct mpgpu_result {
     int32_t nloopn;
     int32_t exitCode;
     double msBuild, msSolve;   /* device time of the last build / solve */
+    /* optional per-label outputs of mpgpu_pede_run (NULL: not written):
+     * start values (globalParStart: the steering's values, set in loop1,
+     * pede.f90:5916-5930, before feasib), the global correlation of each variable
+     * parameter after an inversion (sqrt(1 - 1/(C_ii A_ii)) with the saved
+     * diagonal A_ii of the matrix, prtglo pede.f90:4537-4544; -1 where it
+     * is not defined) and the entries of each label in the records
+     * (globalParLabelCounter, counted in loop1, pede.f90:2334) */
+    double *start;
+    double *gcor;
+    int64_t *fileCounts;
 } mpgpu_result;
 
 /* loop1 equivalent: label table (sorted), entries per label, parameter
@@ -447,7 +466,26 @@ int32_t mpgpu_read_mille(int32_t nfiles, const char *const *files, int64_t maxRe
  * search); ctx may be NULL (a private context is created). */
 int32_t mpgpu_pede_run(mpgpu_ctx *ctx, const mpgpu_steer *st, const mpgpu_job *job,
                        mpgpu_result *res);
+/* millepede.res (prtglo, pede.f90:4477-4651): label, value and pre-sigma
+ * of every parameter, and for variable ones the difference to the start
+ * value (res->start; the value itself when start is NULL), the error
+ * (errors != 0) in pede's G14.5 layout (format 102). */
 int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors);
+/* The same with pede's printing options: ipcntr (steering "printcounts n",
+ * pede.f90:10592-10596) 0 no counts, 1 the entries of the last local fits
+ * (res->counts), > 1 the entries in the records (res->fileCounts); counts
+ * of variable parameters below mreqena are written as -(count+1), pede's
+ * lowstat flag (formats 110-112, pede.f90:4546-4590).  igcorr (steering
+ * "globalcorr") adds the global correlation column res->gcor (F8.3,
+ * format 102) when errors are written and ipcntr is 0.  ipcntr < 0 (the
+ * counts of zero derivatives) is not kept by this library: status 44. */
+typedef struct mpgpu_res_opts {
+    int32_t errors;
+    int32_t ipcntr;
+    int32_t igcorr;
+    int32_t mreqena;
+} mpgpu_res_opts;
+int32_t mpgpu_write_res_opts(const char *path, const mpgpu_result *res, const mpgpu_res_opts *opts);
 
 /* ------------------------------------------------------------------
  * Serving: a resident loop that runs alignment jobs as they arrive (no

@@ -343,6 +343,51 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
 
 // ------------------------------------------------------------------ job
 
+namespace {
+// feasib (pede.f90:1553-1680), one constraint group: residuals r = rhs - C p
+// over all labels; when their rms is at least concut (first of two
+// iterations), p_var += C^T (C C^T)^-1 r.  cinv holds the Cholesky factor
+// of the product matrix C C^T (rows of ncon); pede inverts that matrix with
+// sqminv (feasma, pede.f90:1466-1478) and multiplies with dbsvx, the same
+// solution up to rounding.
+void feasib(const mpgpu_job *job, const std::vector<int32_t> &lab, const int32_t *varIndex,
+            const std::vector<double> &cfac, std::vector<double> &gpar, float concut) {
+    const int32_t ncon = job->ncon;
+    if (ncon <= 0) return;
+    std::vector<double> r(ncon), lam(ncon);
+    for (int iter = 1; iter <= 2; ++iter) {
+        double sum1 = 0.0;
+        for (int32_t c = 0; c < ncon; ++c) {
+            double rhs = job->conRhs ? job->conRhs[c] : 0.0;
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; ++k) {
+                const int32_t li = find_label(lab, job->conLabel[k]);
+                if (li >= 0) rhs = rhs - job->conCoef[k] * gpar[li];
+            }
+            r[c] = rhs;
+            sum1 = sum1 + rhs * rhs;
+        }
+        sum1 = std::sqrt(sum1 / (double)ncon);
+        if (iter == 1 && sum1 < concut) return;
+        // (L L^T) lam = r
+        for (int32_t a = 0; a < ncon; ++a) {
+            double t = r[a];
+            for (int32_t b = 0; b < a; ++b) t -= cfac[(size_t)a * ncon + b] * lam[b];
+            lam[a] = t / cfac[(size_t)a * ncon + a];
+        }
+        for (int32_t a = ncon - 1; a >= 0; --a) {
+            double t = lam[a];
+            for (int32_t b = a + 1; b < ncon; ++b) t -= cfac[(size_t)b * ncon + a] * lam[b];
+            lam[a] = t / cfac[(size_t)a * ncon + a];
+        }
+        for (int32_t c = 0; c < ncon; ++c)
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; ++k) {
+                const int32_t li = find_label(lab, job->conLabel[k]);
+                if (li >= 0 && varIndex[li] > 0) gpar[li] = gpar[li] + lam[c] * job->conCoef[k];
+            }
+    }
+}
+}  // namespace
+
 // Whole alignment job: structure on the host, data loops and solves on the
 // device.  Iteration control of xloopn (pede.f90:8501-9334) without line
 // search and function-value loops: every iteration rebuilds the matrix,
@@ -478,6 +523,32 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         if (job->parValue) gpar[li] = job->parValue[i];
         if (job->parSigma) psig[li] = job->parSigma[i];
     }
+    const std::vector<double> gstart(gpar);   // globalParStart (loop1, pede.f90:5916-5930)
+    // product matrix C C^T of the constraints over the variable parameters
+    // (feasma, pede.f90:1466-1476) and its Cholesky factor for feasib; the
+    // start values are made feasible before the first data loop (cut 1e-12,
+    // xloopn pede.f90:8693, 8730)
+    std::vector<double> cfac;
+    if (!rc && ncon > 0) {
+        cfac.assign((size_t)ncon * ncon, 0.0);
+        for (int32_t l = 0; l < nVar; ++l)
+            for (int32_t a = 0; a < ncon; ++a)
+                for (int32_t b = 0; b <= a; ++b)
+                    cfac[(size_t)a * ncon + b] = cfac[(size_t)a * ncon + b] + A[(size_t)a * nVar + l] * A[(size_t)b * nVar + l];
+        for (int32_t a = 0; a < ncon && !rc; ++a) {
+            for (int32_t b = 0; b <= a; ++b) {
+                double t = cfac[(size_t)a * ncon + b];
+                for (int32_t k = 0; k < b; ++k) t -= cfac[(size_t)a * ncon + k] * cfac[(size_t)b * ncon + k];
+                if (a == b) {
+                    if (!(t > 0.0)) { rc = MPGPU_ERR_QL; break; }
+                    cfac[(size_t)a * ncon + a] = std::sqrt(t);
+                } else {
+                    cfac[(size_t)a * ncon + b] = t / cfac[(size_t)b * ncon + b];
+                }
+            }
+        }
+        if (!rc) feasib(job, lab, res->varIndex, cfac, gpar, 1.0e-12f);
+    }
     std::vector<int32_t> v2t(nVar);
     for (int32_t i = 0; i < ntot; ++i)
         if (res->varIndex[i] > 0) v2t[res->varIndex[i] - 1] = i;
@@ -523,7 +594,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         monHeader = false;
         return r;
     };
-    std::vector<double> gvec(nVar), corr(nVar), err(nVar, 0.0), cres(ncon > 0 ? ncon : 1, 0.0);
+    std::vector<double> gvec(nVar), corr(nVar), err(nVar, 0.0), diag0(nVar, 0.0), cres(ncon > 0 ? ncon : 1, 0.0);
     std::vector<int64_t> gcnt(nVar);
     bool haveErr = false;
     float chicut = st->chicut;
@@ -610,6 +681,11 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         }
         mpgpu_solveinfo si;
         const bool wantErr = (st->metsol == 1 && iter == st->mitera);
+        // minver saves the diagonal for the global correlations (pede.f90:7864-7866)
+        if (wantErr && res->gcor) {
+            rc = mpgpu_matrix_diagonal(ctx, diag0.data());
+            if (rc) break;
+        }
         rc = mpgpu_solve(ctx, st->metsol, cres.data(), st->mrestl, st->itnlim, corr.data(),
                          wantErr ? err.data() : nullptr, &si);
         if (rc) break;
@@ -623,6 +699,8 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             gpar[v2t[i]] += corr[i];
         }
         res->nloopn = nloopn;
+        // the corrected parameters made feasible (cut 1e-6, pede.f90:8865-8866)
+        if (!rc && ncon > 0) feasib(job, lab, res->varIndex, cfac, gpar, 1.0e-6f);
     }
     if (!rc && monitor && st->monitor > 0 && (st->monitor & 2) && monLoop > 0) rc = writeMon(monLoop);
     for (int32_t i = 0; i < ntot; ++i) {
@@ -630,9 +708,20 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         res->presigma[i] = psig[i];
         res->error[i] = 0.0;
         res->counts[i] = 0;
+        if (res->start) res->start[i] = gstart[i];
+        if (res->fileCounts) res->fileCounts[i] = counter[i];
+        if (res->gcor) res->gcor[i] = -1.0;
         const int32_t iv = res->varIndex[i];
         if (iv > 0) {
             res->counts[i] = gcnt[iv - 1];
+            if (haveErr && res->gcor) {
+                // global correlation (prtglo, pede.f90:4537-4544)
+                const double gmati = err[iv - 1], dg = diag0[iv - 1];
+                if (gmati * dg > 0.0) {
+                    const double gcor2 = 1.0 - 1.0 / (gmati * dg);
+                    if (gcor2 >= 0.0 && gcor2 <= 1.0) res->gcor[i] = (double)(float)std::sqrt(gcor2);
+                }
+            }
             if (haveErr) {
                 const double e = std::sqrt(std::fabs(err[iv - 1]));
                 res->error[i] = err[iv - 1] < 0.0 ? -e : e;
@@ -674,30 +763,65 @@ std::string fmt_g145(double v) {
 }
 }  // namespace
 
-// millepede.res in the layout of prtglo (pede.f90:4477-4651): label,
-// value, pre-sigma and, for variable parameters, the difference to the
-// start value and (inversion) the error, in single precision.
-extern "C" int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors) {
+// millepede.res in the layout of prtglo (pede.f90:4477-4651, formats
+// 102 and 110-112 at 4643-4650): label, value, pre-sigma and, for variable
+// parameters, the difference to the start value and (inversion) the error,
+// in single precision; optionally the entries (printcounts) or the global
+// correlation (globalcorr).
+extern "C" int32_t mpgpu_write_res_opts(const char *path, const mpgpu_result *res, const mpgpu_res_opts *o) {
+    if (!path || !res || !o) return MPGPU_ERR_ARG;
+    if (o->ipcntr < 0) return MPGPU_ERR_ARG;   // zero-derivative counts are not kept
+    if (o->ipcntr > 1 && !res->fileCounts) return MPGPU_ERR_ARG;
+    if (o->igcorr && o->errors && o->ipcntr == 0 && !res->gcor) return MPGPU_ERR_ARG;
     FILE *f = std::fopen(path, "w");
     if (!f) return MPGPU_ERR_ARG;
     std::fprintf(f, " Parameter   ! first 3 elements per line are significant (if used as input)\n");
     for (int32_t i = 0; i < res->nTotal; ++i) {
         const std::string a = fmt_g145((double)(float)res->parameter[i]);
         const std::string b = fmt_g145((double)(float)res->presigma[i]);
-        if (res->varIndex[i] <= 0) {
-            std::fprintf(f, "%10d  %s%s\n", res->labels[i], a.c_str(), b.c_str());
-        } else {
-            const std::string d = fmt_g145((double)(float)res->parameter[i]);
-            if (errors) {
-                const std::string e = fmt_g145((double)(float)res->error[i]);
+        const int32_t iv = res->varIndex[i];
+        int64_t icount = 0;
+        bool lowstat = false;
+        if (iv > 0) {
+            icount = res->counts[i];
+            lowstat = icount < o->mreqena;
+        }
+        if (o->ipcntr > 1) icount = res->fileCounts[i];
+        if (lowstat) icount = -(icount + 1);
+        if (iv <= 0) {
+            if (o->ipcntr != 0)
+                std::fprintf(f, "%10d  %s%s%28s%12lld\n", res->labels[i], a.c_str(), b.c_str(), "", (long long)icount);
+            else
+                std::fprintf(f, "%10d  %s%s\n", res->labels[i], a.c_str(), b.c_str());
+            continue;
+        }
+        const double start = res->start ? res->start[i] : 0.0;
+        const std::string d = fmt_g145((double)(float)(res->parameter[i] - start));
+        if (o->errors) {
+            const std::string e = fmt_g145((double)(float)res->error[i]);
+            if (o->ipcntr != 0)
+                std::fprintf(f, "%10d  %s%s%s%s%12lld\n", res->labels[i], a.c_str(), b.c_str(), d.c_str(), e.c_str(),
+                             (long long)icount);
+            else if (o->igcorr)
+                std::fprintf(f, "%10d  %s%s%s%s%8.3f\n", res->labels[i], a.c_str(), b.c_str(), d.c_str(), e.c_str(),
+                             (double)(float)res->gcor[i]);
+            else
                 std::fprintf(f, "%10d  %s%s%s%s\n", res->labels[i], a.c_str(), b.c_str(), d.c_str(), e.c_str());
-            } else {
+        } else {
+            if (o->ipcntr != 0)
+                std::fprintf(f, "%10d  %s%s%s%14s%12lld\n", res->labels[i], a.c_str(), b.c_str(), d.c_str(), "",
+                             (long long)icount);
+            else
                 std::fprintf(f, "%10d  %s%s%s\n", res->labels[i], a.c_str(), b.c_str(), d.c_str());
-            }
         }
     }
     std::fclose(f);
     return 0;
+}
+
+extern "C" int32_t mpgpu_write_res(const char *path, const mpgpu_result *res, int32_t errors) {
+    const mpgpu_res_opts o{errors, 0, 0, 0};
+    return mpgpu_write_res_opts(path, res, &o);
 }
 
 // ------------------------------------------------------------------ monitor

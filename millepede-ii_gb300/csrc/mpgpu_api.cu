@@ -96,7 +96,15 @@ extern "C" int32_t mpgpu_create(mpgpu_ctx **out, const mpgpu_cfg *cfg) {
     if (e == cudaSuccess) e = cudaMallocHost((void **)&c->hscal, 4096);
     if (e != cudaSuccess) {
         int32_t rc = cuda_err(c, e, "mpgpu_create");
-        delete c;
+        mpgpu_destroy(c);
+        return rc;
+    }
+    // the static area of mpgpu_mupdat_noalloc is reserved now, before the
+    // job's large allocations (its module would otherwise load lazily, on
+    // the first call, when the device memory may be full)
+    const int32_t rc = noalloc_prepare(c);
+    if (rc != MPGPU_OK) {
+        mpgpu_destroy(c);
         return rc;
     }
     *out = c;
@@ -749,19 +757,22 @@ extern "C" int32_t mpgpu_mupdat(mpgpu_ctx *c, int32_t n, const int32_t *i, const
     if (!c || n < 0) return MPGPU_ERR_ARG;
     if (n == 0) return MPGPU_OK;
     DevJob &j = c->j;
-    int32_t *di = nullptr, *dj = nullptr;
-    double *da = nullptr;
+    // the per-call buffers are released on every return
+    struct Bufs {
+        int32_t *di = nullptr, *dj = nullptr;
+        double *da = nullptr;
+        ~Bufs() { dfree(di); dfree(dj); dfree(da); }
+    } b;
     cudaStream_t s = c->stream;
-    MPG_CUDA(c, dupload(di, i, n, s));
-    MPG_CUDA(c, dupload(dj, jj, n, s));
-    MPG_CUDA(c, dupload(da, add, n, s));
+    MPG_CUDA(c, dupload(b.di, i, n, s));
+    MPG_CUDA(c, dupload(b.dj, jj, n, s));
+    MPG_CUDA(c, dupload(b.da, add, n, s));
     int32_t *errFlag = (int32_t *)c->scal;
     MPG_CUDA(c, cudaMemsetAsync(errFlag, 0, 4, s));
-    MPG_CUDA(c, launch_mupdat(n, di, dj, da, j, errFlag, s));
+    MPG_CUDA(c, launch_mupdat(n, b.di, b.dj, b.da, j, errFlag, s));
     int32_t h = 0;
     MPG_CUDA(c, cudaMemcpyAsync(&h, errFlag, 4, cudaMemcpyDeviceToHost, s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
-    dfree(di); dfree(dj); dfree(da);
     if (h) return set_err(c, h, "mupdat index outside the matrix");
     return MPGPU_OK;
 }
@@ -777,15 +788,17 @@ __global__ void k_vadd(int32_t n, const int32_t *idx, const double *v, double *g
 extern "C" int32_t mpgpu_vector_add(mpgpu_ctx *c, int32_t n, const int32_t *vidx, const double *vadd) {
     if (!c || n < 0) return MPGPU_ERR_ARG;
     if (n == 0) return MPGPU_OK;
-    int32_t *di = nullptr;
-    double *da = nullptr;
+    struct Bufs {
+        int32_t *di = nullptr;
+        double *da = nullptr;
+        ~Bufs() { dfree(di); dfree(da); }
+    } b;
     cudaStream_t s = c->stream;
-    MPG_CUDA(c, dupload(di, vidx, n, s));
-    MPG_CUDA(c, dupload(da, vadd, n, s));
-    k_vadd<<<1, 32, 0, s>>>(n, di, da, c->j.gvec, c->j.nVar);
+    MPG_CUDA(c, dupload(b.di, vidx, n, s));
+    MPG_CUDA(c, dupload(b.da, vadd, n, s));
+    k_vadd<<<1, 32, 0, s>>>(n, b.di, b.da, c->j.gvec, c->j.nVar);
     MPG_CUDA(c, cudaGetLastError());
     MPG_CUDA(c, cudaStreamSynchronize(s));
-    dfree(di); dfree(da);
     return MPGPU_OK;
 }
 
@@ -793,6 +806,30 @@ extern "C" int32_t mpgpu_download_matrix(mpgpu_ctx *c, double *globalMatD) {
     if (!c || !globalMatD) return MPGPU_ERR_ARG;
     MPG_CUDA(c, cudaMemcpy(globalMatD, c->j.matD, sizeof(double) * (size_t)c->j.nmat, cudaMemcpyDeviceToHost));
     return MPGPU_OK;
+}
+
+namespace {
+// diagonal of the packed (row i at i(i+1)/2) or sparse (diagonal first) matrix
+__global__ void k_matrix_diag(int32_t n, int32_t matsto, const double *m, double *d) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = matsto == 2 ? m[i] : m[i * (i + 1) / 2 + i];
+}
+}  // namespace
+
+extern "C" int32_t mpgpu_matrix_diagonal(mpgpu_ctx *c, double *diagonal) {
+    if (!c || !diagonal) return MPGPU_ERR_ARG;
+    DevJob &j = c->j;
+    if (!j.matD || j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "no matrix");
+    MPG_CUDA(c, cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    double *d = nullptr;
+    MPG_CUDA(c, cudaMalloc(&d, sizeof(double) * j.nVar));
+    k_matrix_diag<<<(j.nVar + 255) / 256, 256, 0, s>>>(j.nVar, j.matsto, j.matD, d);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(diagonal, d, sizeof(double) * j.nVar, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    return e == cudaSuccess ? MPGPU_OK : cuda_err(c, e, "mpgpu_matrix_diagonal");
 }
 
 extern "C" int32_t mpgpu_download_vector(mpgpu_ctx *c, double *globalVector, int64_t *globalCounter) {

@@ -394,6 +394,10 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
                               const double *glder, const int32_t *recFile, int32_t nfiles,
                               const double *fileWeight);
 
+// resolves the device address of mpgpu_mupdat_noalloc's static area on the
+// context's device (mpgpu_noalloc.cu; called by mpgpu_create)
+int32_t noalloc_prepare(mpgpu_ctx *c);
+
 // error helpers
 int32_t set_err(mpgpu_ctx *c, int32_t code, const std::string &msg);
 void free_resident(ResidentRecords &R);

@@ -457,6 +457,9 @@ extern "C" int32_t mpgpu_dense_cholesky(mpgpu_ctx *c, int32_t n, const double *A
 namespace {
 
 constexpr int kDotBlk = 304;   // fixed reduction shape: deterministic sums
+// the refined solves stop only when the last CG correction is below this
+// fraction of the solution (in addition to the residual test)
+constexpr double kRefineXtol = 1e-13;
 
 // packed lower triangle (n) -> dense lower (factor) and dense full (for the
 // matrix-vector products), both npad x npad row-major; scaled diagonal
@@ -620,9 +623,11 @@ __global__ void k_dotf(const double *part, double *out) {
     if (threadIdx.x == 0) *out = sh[0];
 }
 
-// scalars: [0] rz, [1] pq, [2] rz new, [3] rr, [4] bb
-__global__ void k_cg_step(int64_t n, double *x, double *r, const double *p, const double *q, const double *sc) {
+// scalars: [0] rz, [1] pq, [2] rz new, [3] rr, [4] bb, [5] squared length of the
+// last correction alpha p, [6] p.p, [7] x.x
+__global__ void k_cg_step(int64_t n, double *x, double *r, const double *p, const double *q, double *sc) {
     const double alpha = sc[1] != 0.0 ? sc[0] / sc[1] : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc[5] = alpha * alpha * sc[6];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         x[i] += alpha * p[i];
         r[i] -= alpha * q[i];
@@ -698,7 +703,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
         if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
     if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
-    if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 16);
     if (e == cudaSuccess) e = cudaMalloc(&w.err, sizeof(int32_t));
     if (e != cudaSuccess) { w.release(); return cuda_err(c, e, "dense solve allocation"); }
     cudaEvent_t e0, e1;
@@ -744,7 +749,9 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     MPG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, w.p, w.q);
     dotv(w, w.p, w.q, w.sc + 1, s);
+    dotv(w, w.p, w.p, w.sc + 6, s);
     k_cg_step<<<ge, 256, 0, s>>>(w.npad, w.x, w.r, w.p, w.q, w.sc);
+    dotv(w, w.x, w.x, w.sc + 7, s);
     precond(w, w.r, w.z, s);
     dotv(w, w.r, w.z, w.sc + 2, s);
     k_cg_dir<<<ge, 256, 0, s>>>(w.npad, w.p, w.z, w.sc);
@@ -753,17 +760,22 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     cudaError_t ce = cudaStreamEndCapture(s, &graph);
     if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec, graph, 0);
     if (ce != cudaSuccess) { w.release(); return cuda_err(c, ce, "CG graph"); }
+    // stop when the relative residual is below rtol AND the last correction
+    // is below kRefineXtol of the solution: a residual test alone leaves an
+    // error of about cond(A) * rtol, which differs between factors of
+    // different precision; the correction test brings every form to the
+    // same FP64 solution
     int itn = 0, istop = 0;
-    double hs[5];
-    const double tol2 = rtol * rtol;
+    double hs[8];
+    const double tol2 = rtol * rtol, xtol2 = kRefineXtol * kRefineXtol;
     while (itn < itnlim) {
         const int batch = std::min(4, itnlim - itn);
         for (int k = 0; k < batch; ++k) cudaGraphLaunch(gexec, s);
         itn += batch;
         MPG_CUDA(c, cudaMemcpyAsync(hs, w.sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
         MPG_CUDA(c, cudaStreamSynchronize(s));
-        if (!(hs[3] == hs[3])) { istop = 9; break; }
-        if (hs[3] <= tol2 * hs[4]) { istop = 1; break; }
+        if (!(hs[3] == hs[3]) || !(hs[5] == hs[5])) { istop = 9; break; }
+        if (hs[3] <= tol2 * hs[4] && hs[5] <= xtol2 * hs[7]) { istop = 1; break; }
     }
     if (istop == 0) istop = 3;
     cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
@@ -781,6 +793,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         info->nrank = n;
         info->evmin = shift;
         info->evmax = hs[4] > 0.0 ? std::sqrt(hs[3] / hs[4]) : 0.0;
+        info->dxRel = hs[7] > 0.0 ? std::sqrt(hs[5] / hs[7]) : 0.0;
         info->ms = ms;
     }
     cudaGraphExecDestroy(gexec);

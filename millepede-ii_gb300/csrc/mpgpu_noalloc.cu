@@ -22,9 +22,15 @@
 //    calls that overlap in time on one device (from two host threads, or
 //    through two contexts) race on it and can apply each other's triplets,
 //    so the caller must serialise them;
-//  * the first call on each device looks up the area's address (with that
-//    device current) and keeps it for the later calls; that first call
-//    should come before any stream capture is begun on the device.
+//  * the area's device memory is reserved when the CUDA module holding it
+//    is loaded; CUDA loads modules lazily (on first use), so mpgpu_create
+//    looks up the area's address on its device right away
+//    (noalloc_prepare): from the first context on a device onward the area
+//    is in place, before the job's large allocations, and no call of
+//    mpgpu_mupdat_noalloc loads a module or reserves memory.  The address
+//    is kept per device; a call on a device without a context made there
+//    first looks it up itself, and should then come before any stream
+//    capture is begun on that device.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -43,7 +49,8 @@ constexpr size_t kScratchBytes = kOffA + sizeof(double) * kNoallocMax;
 static_assert(kOffA % alignof(double) == 0, "add[] must be 8-byte aligned");
 }  // namespace
 
-// 1 MiB + 256 bytes per device, reserved when the module is loaded
+// 1 MiB + 256 bytes per device, reserved when the module is loaded (at
+// mpgpu_create on that device, through noalloc_prepare)
 static __device__ __align__(256) unsigned char g_mupdatScratch[kScratchBytes];
 
 namespace {
@@ -68,6 +75,13 @@ int32_t scratch_address(mpgpu_ctx *c, unsigned char **out) {
     return MPGPU_OK;
 }
 }  // namespace
+
+// Called by mpgpu_create with the context's device current: loads the
+// module and resolves the area's address once per device.
+int32_t noalloc_prepare(mpgpu_ctx *c) {
+    unsigned char *base = nullptr;
+    return scratch_address(c, &base);
+}
 
 extern "C" int32_t mpgpu_mupdat_noalloc(mpgpu_ctx *c, int32_t n, const int32_t *i, const int32_t *jj,
                                         const double *add) {

@@ -77,7 +77,8 @@ class FitStats(C.Structure):
 class SolveInfo(C.Structure):
     _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
                 ("nrkd", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
-                ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double)]
+                ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double),
+                ("dxRel", C.c_double)]
 
 
 class Steer(C.Structure):
@@ -110,7 +111,13 @@ class Result(C.Structure):
                 ("nrej", C.c_int64 * 6), ("fvalue", C.c_double), ("ndf", C.c_int64),
                 ("nrank", C.c_int32), ("minresItn", C.c_int32), ("minresIstop", C.c_int32),
                 ("nloopn", C.c_int32), ("exitCode", C.c_int32),
-                ("msBuild", C.c_double), ("msSolve", C.c_double)]
+                ("msBuild", C.c_double), ("msSolve", C.c_double),
+                ("start", f64p), ("gcor", f64p), ("fileCounts", i64p)]
+
+
+class ResOpts(C.Structure):
+    _fields_ = [("errors", C.c_int32), ("ipcntr", C.c_int32), ("igcorr", C.c_int32),
+                ("mreqena", C.c_int32)]
 
 
 class GenCfg(C.Structure):
@@ -156,6 +163,7 @@ EXPORTS = [
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_loop1_device", "mpgpu_loop2_device", "mpgpu_pede_run", "mpgpu_write_res",
+    "mpgpu_write_res_opts", "mpgpu_matrix_diagonal",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
 ]
 
@@ -583,7 +591,7 @@ class JobData:
     """A job's C structures (mpgpu_steer, mpgpu_job, mpgpu_result) with the
     numpy arrays they point to kept alive."""
 
-    def __init__(self, data, constraints=None, **steer):
+    def __init__(self, data, constraints=None, params=None, **steer):
         st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
                   dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
                   mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0, monitor=0,
@@ -607,6 +615,14 @@ class JobData:
             j.ncon = len(self.conStart) - 1
             j.conStart, j.conLabel = ptr(self.conStart, i32p), ptr(self.conLabel, i32p)
             j.conCoef, j.conRhs = ptr(self.conCoef, f64p), ptr(self.conRhs, f64p)
+        if params is not None:
+            # steering "Parameter" lines: labels, start values, pre-sigmas
+            self.parLabel = np.ascontiguousarray(params[0], np.int32)
+            self.parValue = np.ascontiguousarray(params[1], np.float64)
+            self.parSigma = np.ascontiguousarray(params[2], np.float64)
+            j.npar = len(self.parLabel)
+            j.parLabel, j.parValue = ptr(self.parLabel, i32p), ptr(self.parValue, f64p)
+            j.parSigma = ptr(self.parSigma, f64p)
         self.job = j
         cap = len(self.inder) + 16
         self.labels = np.zeros(cap, np.int32)
@@ -615,8 +631,13 @@ class JobData:
         self.error = np.zeros(cap)
         self.counts = np.zeros(cap, np.int64)
         self.varIndex = np.zeros(cap, np.int32)
+        self.start = np.zeros(cap)
+        self.gcor = np.zeros(cap)
+        self.fileCounts = np.zeros(cap, np.int64)
         r = Result()
         r.cap = cap
+        r.start, r.gcor = ptr(self.start, f64p), ptr(self.gcor, f64p)
+        r.fileCounts = ptr(self.fileCounts, i64p)
         r.labels, r.parameter = ptr(self.labels, i32p), ptr(self.parameter, f64p)
         r.presigma, r.error = ptr(self.presigma, f64p), ptr(self.error, f64p)
         r.counts, r.varIndex = ptr(self.counts, i64p), ptr(self.varIndex, i32p)
@@ -625,6 +646,11 @@ class JobData:
     def parameters(self):
         n = self.res.nTotal
         return self.labels[:n].copy(), self.parameter[:n].copy()
+
+    def write_res(self, path, errors=0, ipcntr=0, igcorr=0, mreqena=10):
+        """millepede.res of the job (mpgpu_write_res_opts)."""
+        o = ResOpts(errors=errors, ipcntr=ipcntr, igcorr=igcorr, mreqena=mreqena)
+        return lib().mpgpu_write_res_opts(str(path).encode(), C.byref(self.res), C.byref(o))
 
 
 class ServerCfg(C.Structure):

@@ -287,10 +287,17 @@ typedef struct mpref_result {
     int32_t minresItn, minresIstop;
     int32_t nloopn;
     int32_t exitCode;       /* peend code (0 ok) */
+    double *start;          /* [cap] start values of the steering, globalParStart (may be NULL) */
+    double *gcor;           /* [cap] global correlations of the inversion, -1 undefined (may be NULL) */
+    int64_t *fileCounts;    /* [cap] entries in the records, globalParLabelCounter (may be NULL) */
 } mpref_result;
 
 int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res);
 int mpref_write_res(const char *path, const mpref_result *res, int32_t errors);
+/* prtglo with printcounts (ipcntr 0, 1, > 1) and globalcorr (igcorr),
+ * formats 102 and 110-112 (pede.f90:4546-4590, 4643-4650) */
+int mpref_write_res_opts(const char *path, const mpref_result *res, int32_t errors, int32_t ipcntr,
+                         int32_t igcorr, int32_t mreqena);
 
 #ifdef __cplusplus
 }

@@ -3,10 +3,12 @@
  * writer.  TEST INFRASTRUCTURE ONLY.
  *
  * Control flow follows mptwo/xloopn/loopn/addcst (pede.f90:33-528,
- * 8501-9334, 2479-2885, 704-771) without the line search, the function-value
- * loops and the feasibility step: every iteration rebuilds the matrix,
- * solves and adds the correction.  The chi2-cut schedule per data loop is the
- * one of loopn (pede.f90:2583-2593).
+ * 8501-9334, 2479-2885, 704-771) without the line search and the
+ * function-value loops: every iteration rebuilds the matrix, solves and adds
+ * the correction.  The chi2-cut schedule per data loop is the one of loopn
+ * (pede.f90:2583-2593).  feasib (pede.f90:1553-1680) makes the start values
+ * feasible before the first data loop (cut 1e-12, pede.f90:8693, 8730) and
+ * every corrected parameter set after a solution (cut 1e-6, 8865-8866).
  */
 #include "mpref.h"
 #include <math.h>
@@ -23,6 +25,55 @@ static int32_t find_label(const int32_t *labels, int32_t n, int32_t item)
         if (labels[mid] < item) lo = mid + 1; else hi = mid - 1;
     }
     return -1;
+}
+
+/* feasib (pede.f90:1553-1680) for one constraint group: residuals
+ * r = rhs - C p over all labels, rms test against concut in the first of two
+ * iterations, then p_var += C^T (C C^T)^-1 r.  pinv: the inverse of the
+ * product matrix C C^T (packed, inverted by sqminv as feasma does,
+ * pede.f90:1466-1478); dbsvx (mpnum.f90:1264-1297) multiplies it. */
+static int feasib(const mpref_job *job, const mpref_result *res, int32_t ntot, const double *pinv,
+                  double *gpar, float concut)
+{
+    int32_t ncon = job->ncon, iact = 0;
+    if (ncon <= 0) return 0;
+    double *r = (double *)malloc(sizeof(double) * (size_t)ncon);
+    double *lam = (double *)malloc(sizeof(double) * (size_t)ncon);
+    for (int iter = 1; iter <= 2; iter++) {
+        double sum1 = 0.0;
+        for (int32_t c = 0; c < ncon; c++) {
+            double rhs = job->conRhs ? job->conRhs[c] : 0.0;
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; k++) {
+                int32_t li = find_label(res->labels, ntot, job->conLabel[k]);
+                if (li >= 0) rhs = rhs - job->conCoef[k] * gpar[li];
+            }
+            r[c] = rhs;
+            sum1 = sum1 + rhs * rhs;
+        }
+        sum1 = sqrt(sum1 / (double)ncon);
+        if (iter == 1 && sum1 < concut) break;
+        iact = 1;
+        /* dbsvx: lam = V r with V packed symmetric */
+        int64_t ijs = 0;
+        for (int32_t i = 0; i < ncon; i++) {
+            double dsum = 0.0;
+            int64_t ij = ijs;
+            for (int32_t j = 0; j < ncon; j++) {
+                dsum = dsum + pinv[ij] * r[j];
+                if (j < i) ij += 1; else ij += j + 1;
+            }
+            lam[i] = dsum;
+            ijs += i + 1;
+        }
+        for (int32_t c = 0; c < ncon; c++)
+            for (int32_t k = job->conStart[c]; k < job->conStart[c + 1]; k++) {
+                int32_t li = find_label(res->labels, ntot, job->conLabel[k]);
+                if (li >= 0 && res->varIndex[li] > 0) gpar[li] = gpar[li] + lam[c] * job->conCoef[k];
+            }
+    }
+    free(r);
+    free(lam);
+    return iact;
 }
 
 int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
@@ -103,6 +154,24 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         if (job->parValue) { gpar[li] = job->parValue[i]; gstart[li] = job->parValue[i]; }
         if (job->parSigma) psig[li] = job->parSigma[i];
     }
+    /* product matrix of the constraints over the variable parameters,
+     * summed parameter by parameter (feasma, pede.f90:1466-1476), inverted */
+    double *pinv = NULL;
+    if (ncon > 0) {
+        pinv = (double *)calloc((size_t)ncon * (ncon + 1) / 2, sizeof(double));
+        double *dummy = (double *)calloc((size_t)ncon, sizeof(double));
+        int32_t prank = 0;
+        for (int32_t l = 0; l < nVar; l++) {
+            int64_t ij = 0;
+            for (int32_t a = 0; a < ncon; a++)
+                for (int32_t b = 0; b <= a; b++, ij++)
+                    pinv[ij] = pinv[ij] + A[(int64_t)a * nVar + l] * A[(int64_t)b * nVar + l];
+        }
+        mpref_sqminv(pinv, dummy, ncon, &prank);
+        free(dummy);
+        feasib(job, res, ntot, pinv, gpar, 1.0e-12f);
+    }
+    double *diag0 = (double *)calloc((size_t)nVar, sizeof(double));
     double *pw = (double *)calloc((size_t)nVar, sizeof(double));
     int32_t *v2t = (int32_t *)malloc(sizeof(int32_t) * (size_t)nVar);
     for (i = 0; i < ntot; i++)
@@ -207,7 +276,9 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         for (i = 0; i < nVar; i++) corr[i] = gvec[i];
 
         if (st->metsol == 1 || st->metsol == 3) {
-            double *diag0 = NULL;
+            /* minver saves the diagonal for the global correlations
+             * (pede.f90:7864-7866) */
+            for (int64_t r = 1; r <= nVar; r++) diag0[r - 1] = matD[(r * r - r) / 2 + r - 1];
             if (ncon > 0) {
                 mpref_ql_ssq_packed(q, matD, 1);
                 mpref_ql_bsub(q, cres, csol);
@@ -218,7 +289,6 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
                         corr[i - 1] = corr[i - 1] - matD[(r * r - r) / 2 + i - 1] * csol[j - 1];
                     }
             }
-            (void)diag0;
             int32_t nrank = 0;
             if (st->metsol == 1) {
                 mpref_sqminl(matD, corr, nfit, &nrank);
@@ -275,6 +345,7 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         }
         res->nloopn = nloopn;
         if (rc) break;
+        if (ncon > 0) feasib(job, res, ntot, pinv, gpar, 1.0e-6f);
     }
 
     for (i = 0; i < ntot; i++) {
@@ -283,11 +354,20 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         res->error[i] = 0.0;
         res->counts[i] = 0;
         int32_t iv = res->varIndex[i];
+        if (res->start) res->start[i] = gstart[i];
+        if (res->fileCounts) res->fileCounts[i] = counter[i];
+        if (res->gcor) res->gcor[i] = -1.0;
         if (iv > 0) {
             res->counts[i] = gcnt[iv - 1];
             if (haveErr) {
                 double e = sqrt(fabs(err[iv - 1]));
                 res->error[i] = err[iv - 1] < 0.0 ? -e : e;
+                /* global correlation (prtglo, pede.f90:4537-4544) */
+                double gmati = err[iv - 1], dg = diag0[iv - 1];
+                if (res->gcor && gmati * dg > 0.0) {
+                    double gcor2 = 1.0 - 1.0 / (gmati * dg);
+                    if (gcor2 >= 0.0 && gcor2 <= 1.0) res->gcor[i] = (double)(float)sqrt(gcor2);
+                }
             }
         }
     }
@@ -295,7 +375,7 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
     free(grpStart); free(totGroup); free(counter); free(aig); free(p2g); free(tinder);
     free(offsets); free(columns); free(A); mpref_ql_destroy(q); free(gpar); free(gstart);
     free(psig); free(pw); free(v2t); free(gvec); free(gcnt); free(matD); free(corr);
-    free(cres); free(csol); free(err);
+    free(cres); free(csol); free(err); free(diag0); free(pinv);
     return rc;
 }
 
@@ -331,27 +411,49 @@ static void fmt_g(char *buf, double v)
     }
 }
 
-int mpref_write_res(const char *path, const mpref_result *res, int32_t errors)
+int mpref_write_res_opts(const char *path, const mpref_result *res, int32_t errors, int32_t ipcntr,
+                         int32_t igcorr, int32_t mreqena)
 {
-    FILE *f = fopen(path, "w");
+    FILE *f;
     char a[32], b[32], c[32], d[32];
+    if (ipcntr < 0 || (ipcntr > 1 && !res->fileCounts)) return -1;
+    f = fopen(path, "w");
     if (!f) return -1;
     fprintf(f, " Parameter   ! first 3 elements per line are significant (if used as input)\n");
     for (int32_t i = 0; i < res->nTotal; i++) {
+        int32_t iv = res->varIndex[i];
+        long long icount = 0;
+        int lowstat = 0;
         fmt_g(a, (double)(float)res->parameter[i]);
         fmt_g(b, (double)(float)res->presigma[i]);
-        if (res->varIndex[i] <= 0) {
-            fprintf(f, "%10d  %s%s\n", res->labels[i], a, b);
+        if (iv > 0) {
+            icount = res->counts[i];
+            lowstat = icount < mreqena;
+        }
+        if (ipcntr > 1) icount = res->fileCounts[i];
+        if (lowstat) icount = -(icount + 1);
+        if (iv <= 0) {
+            if (ipcntr != 0) fprintf(f, "%10d  %s%s%28s%12lld\n", res->labels[i], a, b, "", icount);
+            else fprintf(f, "%10d  %s%s\n", res->labels[i], a, b);
+            continue;
+        }
+        fmt_g(c, (double)(float)(res->parameter[i] - (res->start ? res->start[i] : 0.0)));
+        if (errors) {
+            fmt_g(d, (double)(float)res->error[i]);
+            if (ipcntr != 0) fprintf(f, "%10d  %s%s%s%s%12lld\n", res->labels[i], a, b, c, d, icount);
+            else if (igcorr && res->gcor)
+                fprintf(f, "%10d  %s%s%s%s%8.3f\n", res->labels[i], a, b, c, d, (double)(float)res->gcor[i]);
+            else fprintf(f, "%10d  %s%s%s%s\n", res->labels[i], a, b, c, d);
         } else {
-            fmt_g(c, (double)(float)(res->parameter[i]));
-            if (errors) {
-                fmt_g(d, (double)(float)res->error[i]);
-                fprintf(f, "%10d  %s%s%s%s\n", res->labels[i], a, b, c, d);
-            } else {
-                fprintf(f, "%10d  %s%s%s\n", res->labels[i], a, b, c);
-            }
+            if (ipcntr != 0) fprintf(f, "%10d  %s%s%s%14s%12lld\n", res->labels[i], a, b, c, "", icount);
+            else fprintf(f, "%10d  %s%s%s\n", res->labels[i], a, b, c);
         }
     }
     fclose(f);
     return 0;
+}
+
+int mpref_write_res(const char *path, const mpref_result *res, int32_t errors)
+{
+    return mpref_write_res_opts(path, res, errors, 0, 0, 0);
 }

@@ -56,7 +56,8 @@ class Result(C.Structure):
                 ("counts", i64p), ("varIndex", i32p),
                 ("nrej", C.c_int64 * 6), ("fvalue", C.c_double), ("ndf", C.c_int64),
                 ("nrank", C.c_int32), ("minresItn", C.c_int32), ("minresIstop", C.c_int32),
-                ("nloopn", C.c_int32), ("exitCode", C.c_int32)]
+                ("nloopn", C.c_int32), ("exitCode", C.c_int32),
+                ("start", f64p), ("gcor", f64p), ("fileCounts", i64p)]
 
 
 def ptr(a, t):
@@ -146,8 +147,14 @@ def make_result(cap, cls=Result):
     keep.error = np.zeros(cap, np.float64)
     keep.counts = np.zeros(cap, np.int64)
     keep.varIndex = np.zeros(cap, np.int32)
+    keep.start = np.zeros(cap, np.float64)
+    keep.gcor = np.zeros(cap, np.float64)
+    keep.fileCounts = np.zeros(cap, np.int64)
     r = cls()
     r.cap = cap
+    r.start = ptr(keep.start, f64p)
+    r.gcor = ptr(keep.gcor, f64p)
+    r.fileCounts = ptr(keep.fileCounts, i64p)
     r.labels = ptr(keep.labels, i32p)
     r.parameter = ptr(keep.parameter, f64p)
     r.presigma = ptr(keep.presigma, f64p)
@@ -167,6 +174,8 @@ def run(data, steer, **jobkw):
     n = res.nTotal
     out = dict(rc=rc, labels=kr.labels[:n].copy(), parameter=kr.parameter[:n].copy(),
                error=kr.error[:n].copy(), counts=kr.counts[:n].copy(),
+               start=kr.start[:n].copy(), gcor=kr.gcor[:n].copy(),
+               fileCounts=kr.fileCounts[:n].copy(), result=res, arrays=kr,
                varIndex=kr.varIndex[:n].copy(), nrej=list(res.nrej), fvalue=res.fvalue,
                ndf=res.ndf, nrank=res.nrank, itn=res.minresItn, istop=res.minresIstop,
                nVar=res.nVar, nFit=res.nFit, nVarGroups=res.nVarGroups)

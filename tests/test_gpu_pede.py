@@ -92,3 +92,47 @@ def test_barrel_sparse_minresqlp(mp, orc):
     assert g["nrej"] == o["nrej"]
     scale = np.max(np.abs(o["parameter"]))
     assert np.max(np.abs(g["parameter"] - o["parameter"])) <= 1e-8 * scale
+
+
+def test_start_values_feasib_and_res(mp, orc, tmp_path):
+    """Start values that violate the constraints (feasib before the first
+    data loop), inversion with global correlations: parameters, errors,
+    start values, correlations and entries as the oracle's job, and the
+    millepede.res written from both results (printcounts, globalcorr)
+    identical text."""
+    d = mp.generate(mp.gen_config("telescope", ntracks=4000, seed=21))
+    labels = np.unique(d["inder"][d["inder"] > 0])[:40]
+    rng = np.random.default_rng(5)
+    values = rng.normal(0.0, 0.01, len(labels))
+    sigmas = np.zeros(len(labels))
+    sigmas[::13] = -1.0
+    st = orc.make_steer(metsol=1, matsto=1, mitera=2, lhuber=1, chicut=30.0, chirem=6.0)
+    kw = dict(parLabel=labels, parValue=values, parSigma=sigmas)
+    job, keep = orc.make_job(d, **kw)
+    cap = len(d["inder"]) + 16
+    res, kr = orc.make_result(cap, cls=mp.Result)
+    gst = mp.Steer(**{f: getattr(st, f) for f, _ in mp.Steer._fields_ if hasattr(st, f)})
+    gjob = mp.Job(**{f: getattr(job, f) for f, _ in mp.Job._fields_ if hasattr(job, f)})
+    assert mp.lib().mpgpu_pede_run(None, C.byref(gst), C.byref(gjob), C.byref(res)) == 0
+    o = orc.run(d, st, **kw)
+    assert o["rc"] == 0
+    n = res.nTotal
+    np.testing.assert_array_equal(kr.start[:n], o["start"])
+    np.testing.assert_array_equal(kr.fileCounts[:n], o["fileCounts"])
+    np.testing.assert_array_equal(kr.counts[:n], o["counts"])
+    scale = np.max(np.abs(o["parameter"]))
+    assert np.max(np.abs(kr.parameter[:n] - o["parameter"])) <= 1e-10 * scale
+    var = o["varIndex"] > 0
+    assert np.max(np.abs(kr.error[:n][var] - o["error"][var]) / np.abs(o["error"][var])) <= 1e-9
+    assert np.max(np.abs(kr.gcor[:n] - o["gcor"])) <= 1e-6
+    for opts in ((1, 1, 0), (1, 0, 1)):
+        p1, p2 = tmp_path / "gpu.res", tmp_path / "oracle.res"
+        ro = mp.ResOpts(errors=opts[0], ipcntr=opts[1], igcorr=opts[2], mreqena=10)
+        assert mp.lib().mpgpu_write_res_opts(str(p1).encode(), C.byref(res), C.byref(ro)) == 0
+        assert orc.lib().mpref_write_res_opts(str(p2).encode(), C.byref(o["result"]), C.c_int32(opts[0]),
+                                              C.c_int32(opts[1]), C.c_int32(opts[2]), C.c_int32(10)) == 0
+        a, b = p1.read_text().splitlines(), p2.read_text().splitlines()
+        assert len(a) == len(b)
+        # single-precision text of values equal up to the last printed digit
+        diff = sum(1 for x, y in zip(a, b) if x != y)
+        assert diff <= max(2, len(a) // 100), diff

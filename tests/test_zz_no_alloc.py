@@ -1,8 +1,13 @@
 """mpgpu_mupdat_noalloc (staging in a fixed device area, no allocation)
 against mpgpu_mupdat through the C-ABI: the global matrix after a data loop
 plus two update calls in a row agrees within 1e-12 relative (both run the
-same kernel in the same order, so it is expected to be identical); a call
-above the area's capacity is rejected and leaves the matrix unchanged."""
+same kernel in the same order, so it is expected to be identical); both
+against the oracle's mupdat (pede.f90:3134-3204) applied to the same
+matrix, on packed and on mpbits-sparse storage where most random pairs are
+not stored and are suppressed; a call above the area's capacity is
+rejected and leaves the matrix unchanged."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -80,3 +85,45 @@ def test_noalloc_limits(mp):
             ctx.mupdat(bad, bad, np.ones(1))
         ctx.mupdat_noalloc(i[:0], i[:0], np.ones(0))
         np.testing.assert_array_equal(ctx.matrix(), base)
+
+
+def oracle_mupdat(orc, H, matsto, base, batches_):
+    """The oracle's mupdat applied in order to a copy of base."""
+    L = orc.lib()
+    m = np.ascontiguousarray(base.copy())
+    aig = np.ascontiguousarray(H.aig, np.int32)
+    p2g = np.zeros(H.nVar, np.int32)
+    for g in range(len(aig) - 1):
+        p2g[aig[g] - 1:aig[g + 1] - 1] = g + 1
+    off = np.ascontiguousarray(H.offsets, np.int64)
+    col = np.ascontiguousarray(H.columns, np.int32)
+    f64p, i32p, i64p = C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64)
+    mp_ = m.ctypes.data_as(f64p)
+    args = (C.c_int32(H.nG), aig.ctypes.data_as(i32p), p2g.ctypes.data_as(i32p),
+            off.ctypes.data_as(i64p), col.ctypes.data_as(i32p), mp_)
+    for i, j, a in batches_:
+        for q in range(len(i)):
+            L.mpref_mupdat(C.c_int32(matsto), C.c_int32(int(i[q])), C.c_int32(int(j[q])),
+                           C.c_double(float(a[q])), *args)
+    return m
+
+
+@pytest.mark.parametrize("kind,matsto", [("telescope", 1), ("barrel", 2)])
+def test_noalloc_and_mupdat_match_oracle(mp, orc, kind, matsto):
+    ctx, H = setup(mp, kind, matsto, 3000)
+    with ctx:
+        gpar = np.zeros(H.nTotal)
+        bs = batches(ctx.nVar, [4000, 20000], seed=9)
+        ctx.loopbf(gpar)
+        base = ctx.matrix()
+        want = oracle_mupdat(orc, H, matsto, base, bs)
+        for call in (ctx.mupdat, ctx.mupdat_noalloc):
+            ctx.loopbf(gpar)
+            for b in bs:
+                call(*b)
+            close(ctx.matrix(), want)
+    if matsto == 2:
+        # most random pairs fall outside the stored blocks and are dropped:
+        # the matrix changed, but by fewer elements than there were triplets
+        changed = int(np.count_nonzero(want != base))
+        assert 0 < changed < sum(len(b[0]) for b in bs) // 2
