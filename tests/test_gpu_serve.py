@@ -45,3 +45,34 @@ def test_serve_budget_refusal(mp):
         rc, lat, q, b = srv.wait(srv.submit(jd), timeout_ms=600000.0)
     assert rc == 42
     assert b > (1 << 20)
+
+
+def test_serve_mixed_matches_fp64(mp):
+    """Every job solved with the tensor-core factor (metsol 31) in the mix
+    of the serving loop reaches the parameters of the same job solved with
+    the FP64 factor (metsol 32): within 1e-10 relative for one solution
+    (the CG refinement stops on the size of its corrections, not on the
+    residual alone).  Over three Gauss-Newton iterations each new gradient
+    is formed from parameters that differ in their last bits, and the
+    solution amplifies that rounding noise by the condition number: there
+    the two FP64 forms (blocked, metsol 32, and chdec2, metsol 3) differ by
+    about 1e-10 as well, and the mixed form stays within that spread."""
+    specs = jobs(mp)
+    rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+    for mitera in (1, 3):
+        forms = {}
+        with mp.Server(max_active=3) as srv:
+            for ms in (31, 32, 3):
+                forms[ms] = [mp.JobData(d, **dict(st, metsol=ms, mitera=mitera)) for d, st in specs]
+            tickets = [srv.submit(jd) for ms in (31, 32, 3) for jd in forms[ms]]
+            res = [srv.wait(t, timeout_ms=600000.0) for t in tickets]
+        assert all(r[0] == 0 for r in res)
+        for a, b, c in zip(forms[31], forms[32], forms[3]):
+            np.testing.assert_array_equal(a.parameters()[0], b.parameters()[0])
+            mixed = rel(a.parameters()[1], b.parameters()[1])
+            spread = rel(b.parameters()[1], c.parameters()[1])
+            if mitera == 1:
+                assert mixed <= 1e-10, mixed
+            else:
+                assert mixed <= max(1e-10, 4.0 * spread), (mixed, spread)
+            assert a.res.minresItn > 0 and b.res.minresItn > 0
