@@ -335,12 +335,16 @@ def serve_measure(mp, local, njobs=24, rate=8.0, nmin=500, nmax=20000, rmin=10_0
             "refinement_steps_last_solve_mixed": steps_m, "refinement_steps_last_solve_fp64": steps_f}
 
 
-def cpu_reference(d, nsample, nthreads, steps=1):
-    """CPU oracle (loopbf restatement, OpenMP) on the first nsample records."""
-    import oracle_ref as orc
+def sample_of(d, nsample):
     rp = d["recPtr"][:nsample + 1]
-    sub = dict(recPtr=rp, inder=d["inder"][:rp[-1]], glder=d["glder"][:rp[-1]])
-    S = orc.Structure(sub, mreqenf=1)
+    return dict(recPtr=rp, inder=d["inder"][:rp[-1]], glder=d["glder"][:rp[-1]])
+
+
+def cpu_reference(d, nsample, nthreads, steps=1, keep=False):
+    """CPU oracle (loopbf restatement, OpenMP) on the first nsample records;
+    with keep, also the oracle's structure and the output of the last step."""
+    import oracle_ref as orc
+    S = orc.Structure(sample_of(d, nsample), mreqenf=1)
     gpar = np.zeros(S.nTotal)
     times = []
     for _ in range(steps):
@@ -348,7 +352,39 @@ def cpu_reference(d, nsample, nthreads, steps=1):
         o = S.loopbf(gpar, matsto=2, nthreads=nthreads)
         times.append(time.perf_counter() - t0)
         assert o["rc"] == 0
+    if keep:
+        return nsample / statistics.median(times), times, S, o
     return nsample / statistics.median(times), times
+
+
+def bench_parity(mp, device, d, nsample, S, o):
+    """The device data loop on the records the CPU leg timed (the first
+    nsample records of the workload, their own label table and mpbits
+    structure), against the oracle's output of that leg: tables and record
+    decisions bit for bit, matrix, vector and chi2 within 1e-12 relative."""
+    sub = sample_of(d, nsample)
+    H = mp.HostStructure(sub, mreqenf=1)
+    same_tables = bool(np.array_equal(H.labels, S.labels) and np.array_equal(H.varIndex, S.varIndex)
+                       and np.array_equal(H.aig, S.aig) and np.array_equal(H.offsets, S.offsets)
+                       and np.array_equal(H.columns[:H.ncolw], S.columns[:S.ncolw]))
+    with mp.Context(device=device) as ctx:
+        ctx.set_layout(H, 2)
+        ctx.upload(H)
+        g = ctx.loopbf(np.zeros(H.nTotal))
+        M = ctx.matrix()
+        st = ctx.status()
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))
+    out = {"records": nsample, "tables_equal": same_tables,
+           "status_equal": bool(np.array_equal(st, o["status"])),
+           "nrej_equal": bool(list(g["nrej"]) == list(o["nrej"])), "nrej": list(g["nrej"]),
+           "matrix_rel": rel(M, o["matD"]), "vector_rel": rel(g["gvec"], o["gvec"]),
+           "counts_equal": bool(np.array_equal(g["gcnt"], o["gcnt"])),
+           "chi2_rel": abs(g["chi2"] - o["chi2"]) / max(abs(o["chi2"]), 1e-300)}
+    out["ok"] = bool(out["tables_equal"] and out["status_equal"] and out["nrej_equal"] and out["counts_equal"]
+                     and out["matrix_rel"] <= 1e-12 and out["vector_rel"] <= 1e-12)
+    return out
 
 
 def brokenlines_measure(mp, device, nrec, ncores, steps=2):
@@ -610,11 +646,13 @@ def main():
                        "upload_device_ms": up_dev, "pinned_buffers": len(pinned)}
         if rank == 0:
             nsample = min(args.cpu_sample, nrec)
-            val, times = cpu_reference(d, nsample, ncores, steps=1)
+            val, times, So, oo = cpu_reference(d, nsample, ncores, steps=1, keep=True)
             line["cpu_baseline"] = {"value": val, "unit": "records/s", "cores": ncores,
                                     "kind": "port",
                                     "sample": f"first {nsample} records, one sparse data loop"}
     ctx.close()
+    if not args.profile and rank == 0:
+        line["parity"] = bench_parity(mp, local, d, nsample, So, oo)
     if not args.profile:
         line["structure"] = structure_measure(mp, S, pinned, local, host_struct_s, ncores)
     if args.brokenlines > 0 and rank == 0 and not args.profile:

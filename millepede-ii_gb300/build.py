@@ -64,7 +64,7 @@ def build_oracle(verbose=False):
     os.makedirs(ORACLE_BUILD, exist_ok=True)
     srcs = [os.path.join(ORACLE, f) for f in sorted(os.listdir(ORACLE)) if f.endswith(".c")]
     out = os.path.join(ORACLE_BUILD, "libmpref.so")
-    _run(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", "-o", out] + srcs + ["-lm"])
+    _run(["gcc", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp", "-o", out] + srcs + ["-lm"])
     if verbose:
         print("built", out)
     return out

@@ -671,11 +671,18 @@ __device__ __forceinline__ double gtwg_element(const WarpMem &m, int a, int b, b
 
 constexpr int kSformMaxEq = 4;   // equations per group of the S-form update
 
-// one S-form task: row a of block (pg, q) with MQ equations in group q
-template <int MQ>
+// one S-form task: row a of block (pg, q) with MQ equations in group q.
+// Off-diagonal blocks (q < pg): U(a, b) = G^T W G part (the equations the
+// two slots share) + sum_f Z_f g_bf with Z_f = sum_{e in E_a} g_ae S_ef.
+// Diagonal blocks (q == pg, simple word lists: the slots of the group sit in
+// the same MQ equations, one word each): the G^T W G part -sum_f w_f g_af
+// g_bf is folded into Z (Z_f -= w_f g_af), U(a, b) = sum_f Z_f g_bf for
+// b <= a.  The two kinds run in separate passes over the lanes, so that
+// every lane of a pass has the same work.
+template <int MQ, bool DIAG>
 __device__ __forceinline__ void sform_task(const WarpMem &m, const double *S, int neq, int a, int pg, int q,
                                            const int64_t *pdst, double *stage) {
-    const int c0 = m.goff[q], c1 = (q == pg) ? a + 1 : m.goff[q + 1];
+    const int c0 = m.goff[q], c1 = DIAG ? a + 1 : m.goff[q + 1];
     const int qa0 = m.swS[a], ma = m.swS[a + 1] - qa0, qc0 = m.swS[c0];
     double Z[MQ];
 #pragma unroll
@@ -686,17 +693,30 @@ __device__ __forceinline__ void sform_task(const WarpMem &m, const double *S, in
             const int ent = m.sw[qa0 + i];
             z = __fma_rn(m.gl[ent & 0xffff], S[(ent >> 16) * neq + ef], z);
         }
+        if (DIAG) z = __fma_rn(-m.w0[ef], m.gl[m.sw[qa0 + f] & 0xffff], z);
         Z[f] = z;
     }
     const int ii = a - m.goff[pg];
     const int64_t base = __ldg(pdst + pg * (pg + 1) / 2 + q) +
-                         (q == pg ? (int64_t)ii * (ii + 1) / 2 : (int64_t)ii * (m.goff[q + 1] - c0));
+                         (DIAG ? (int64_t)ii * (ii + 1) / 2 : (int64_t)ii * (m.goff[q + 1] - c0));
     for (int b = c0; b < c1; ++b) {
-        double u = gtwg_element(m, a, b, q == pg);
+        double u = DIAG ? 0.0 : gtwg_element(m, a, b, false);
         const int qb0 = m.swS[b];
 #pragma unroll
         for (int f = 0; f < MQ; ++f) u = __fma_rn(Z[f], m.gl[m.sw[qb0 + f] & 0xffff], u);
         stage[base + (b - c0)] = u;
+    }
+}
+
+template <bool DIAG>
+__device__ __forceinline__ void sform_dispatch(const WarpMem &m, const double *S, int neq, int a, int pg, int q,
+                                               const int64_t *pdst, double *stage) {
+    const int c0 = m.goff[q];
+    switch (m.swS[c0 + 1] - m.swS[c0]) {
+        case 1: sform_task<1, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
+        case 2: sform_task<2, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
+        case 3: sform_task<3, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
+        default: sform_task<4, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
     }
 }
 
@@ -1098,12 +1118,13 @@ k_fit(FitParams p, int perWarp) {
                         }
                         Y[t] = y;
                     }
-                    // task prefix over groups: group g has (rows of g) x (g + 1) tasks
+                    // prefix of the off-diagonal tasks over groups: group g
+                    // has (rows of g) x g of them (columns groups q < g)
                     if (ln == 0) {
                         int acc = 0;
                         for (int g = 0; g < ngrp; ++g) {
                             tpre[g] = acc;
-                            acc += (m.goff[g + 1] - m.goff[g]) * (g + 1);
+                            acc += (m.goff[g + 1] - m.goff[g]) * g;
                         }
                         tpre[ngrp] = acc;
                     }
@@ -1124,9 +1145,10 @@ k_fit(FitParams p, int perWarp) {
                         S[f * neq + e] = v;
                     }
                     __syncwarp();
-                    // tasks (slot a, group q): Z_f = sum_{e in E_p} g_ae S_ef over the
-                    // equations f of q, then the row of a in block (p, q):
-                    // U(a, b) = G^T W G part + sum_f Z_f g_bf
+                    // tasks (slot a, group q <= group p of a): Z_f = sum_{e in
+                    // E_p} g_ae S_ef over the equations f of q, then the row of
+                    // a in block (p, q).  Off-diagonal blocks first (every
+                    // task the same size), then the diagonal ones, one per slot
                     const int ntask = tpre[ngrp];
                     for (int t = ln; t < ntask; t += 32) {
                         int lo = 0, hi = ngrp - 1;
@@ -1136,14 +1158,17 @@ k_fit(FitParams p, int perWarp) {
                             else hi = mid - 1;
                         }
                         const int pg = lo, loc = t - tpre[pg];
-                        const int a = m.goff[pg] + loc / (pg + 1), q = loc % (pg + 1);
-                        const int c0 = m.goff[q];
-                        switch (m.swS[c0 + 1] - m.swS[c0]) {
-                            case 1: sform_task<1>(m, S, neq, a, pg, q, pdst, p.stage); break;
-                            case 2: sform_task<2>(m, S, neq, a, pg, q, pdst, p.stage); break;
-                            case 3: sform_task<3>(m, S, neq, a, pg, q, pdst, p.stage); break;
-                            default: sform_task<4>(m, S, neq, a, pg, q, pdst, p.stage); break;
+                        const int a = m.goff[pg] + loc / pg, q = loc % pg;
+                        sform_dispatch<false>(m, S, neq, a, pg, q, pdst, p.stage);
+                    }
+                    for (int a = ln; a < nalg; a += 32) {
+                        int lo = 0, hi = ngrp - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (m.goff[mid] <= a) lo = mid;
+                            else hi = mid - 1;
                         }
+                        sform_dispatch<true>(m, S, neq, a, lo, lo, pdst, p.stage);
                     }
                 } else if (p.icalcm == 1) {
                     // W = B Gamma^-1 (dbavat's c_ik, mpnum.f90:1422-1432):

@@ -141,7 +141,7 @@ int mpref_loopbf_omp(int32_t nthreads, const mpref_fitopt *opt, int64_t nrec,
                      int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
                      const int32_t *parToGroup, const int64_t *offsets,
                      const int32_t *columns, int64_t nmat, double *globalVector,
-                     int64_t *globalCounter, double *matD, mpref_fitout *out);
+                     int64_t *globalCounter, double *matD, mpref_fitout *out, int32_t *status);
 
 /* mupdat (pede.f90:3134-3204): add `add` to element (i,j) (1-based var). */
 void mpref_mupdat(int32_t matsto, int32_t i, int32_t j, double add, int32_t nG,

@@ -695,7 +695,7 @@ int mpref_loopbf_omp(int32_t nthreads, const mpref_fitopt *opt, int64_t nrec,
                      int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
                      const int32_t *parToGroup, const int64_t *offsets,
                      const int32_t *columns, int64_t nmat, double *globalVector,
-                     int64_t *globalCounter, double *matD, mpref_fitout *out)
+                     int64_t *globalCounter, double *matD, mpref_fitout *out, int32_t *status)
 {
     ctx_t c = {opt, recPtr, inder, glder, recFile, fileWeight, globalParameter,
                varIndexOfTotal, nVar, nG, allIndexGroups, parToGroup, offsets, columns};
@@ -714,8 +714,9 @@ int mpref_loopbf_omp(int32_t nthreads, const mpref_fitopt *opt, int64_t nrec,
         memset(&lo, 0, sizeof(lo));
 #pragma omp for schedule(dynamic, 64)
         for (int64_t r = 0; r < nrec; r++) {
-            int32_t st;
+            int32_t st = 0;
             if (rc == 0) rc = fit_record(&c, r, &s, lv, lc, lm, &lo, &st, NULL, NULL, NULL);
+            if (status) status[r] = st;
         }
 #pragma omp critical
         {

@@ -214,7 +214,7 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
             rc = mpref_loopbf_omp(st->nthreads, &fo, job->nrec, job->recPtr, tinder, job->glder,
                                   job->recFile, job->nfiles, job->fileWeight, gpar, res->varIndex,
                                   nVar, nG, aig, p2g, offsets, columns, nmat, gvec, gcnt, matD,
-                                  &out);
+                                  &out, NULL);
         else
             rc = mpref_loopbf(&fo, job->nrec, job->recPtr, tinder, job->glder, job->recFile,
                               job->nfiles, job->fileWeight, gpar, res->varIndex, nVar, nG, aig,

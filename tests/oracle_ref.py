@@ -266,8 +266,7 @@ class Structure:
                                     ptr(self.aig, i32p), ptr(self.p2g, i32p),
                                     ptr(self.offsets, i64p), ptr(self.columns, i32p),
                                     C.c_int64(nmat), ptr(gvec, f64p), ptr(gcnt, i64p),
-                                    ptr(matD, f64p), C.byref(out))
-            status = None
+                                    ptr(matD, f64p), C.byref(out), ptr(status, i32p))
         else:
             rc = L.mpref_loopbf(C.byref(fo), C.c_int64(nrec), ptr(self.recPtr, i64p),
                                 ptr(self.tinder, i32p), ptr(self.glder, f64p), None,
