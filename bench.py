@@ -657,11 +657,11 @@ def main():
         line["structure"] = structure_measure(mp, S, pinned, local, host_struct_s, ncores)
     if args.brokenlines > 0 and rank == 0 and not args.profile:
         line["brokenlines"] = brokenlines_measure(mp, local, args.brokenlines, ncores)
-    if args.serve_jobs > 0 and rank == 0:
+    if args.serve_jobs > 0 and rank == 0 and not args.profile:
         line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
     if args.minres_iters > 0 and rank == 0 and not args.profile:
         line["minres"] = minres_measure(mp, local, iters=args.minres_iters)
-    if args.dense_n > 0 and rank == 0:
+    if args.dense_n > 0 and rank == 0 and not args.profile:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n)
     for arr in pinned:

@@ -57,13 +57,25 @@ __device__ float d_chindl(int n, int nd) {
 // The pivot is the first remaining index with the largest |v_jj| among
 // those above 16*eps*|original diagonal|, which is what the sequential
 // linked-list scan of the reference selects.
+// The comparisons of the pivot search run on the bit patterns: for
+// non-negative doubles that are not NaN the unsigned order of the bits is
+// the numeric order, so the search (and its warp argmax) needs no FP64
+// instruction; a NaN on either side never passes, as in the FP64 compare.
+// diag[] holds the bits of the thresholds 16 eps |v_jj| of the original
+// diagonal.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
 __device__ void warp_sqminv(double *v, double *b, int n, int *nrank_out, double *diag,
                             double *ocol, double *scol, int *used) {
     const int ln = lane_id();
     const double eps = 16.0 * 2.220446049250313e-16;
+    constexpr unsigned long long kInfBits = 0x7ff0000000000000ull;
     const int np = (n * n + n) / 2;
+    unsigned long long *thr = reinterpret_cast<unsigned long long *>(diag);
     for (int i = ln; i < n; i += 32) {
-        diag[i] = fabs(v[(i + 1) * (i + 2) / 2 - 1]);
+        thr[i] = abs_bits(eps * fabs(v[(i + 1) * (i + 2) / 2 - 1]));
         used[i] = 0;
     }
     __syncwarp();
@@ -71,17 +83,17 @@ __device__ void warp_sqminv(double *v, double *b, int n, int *nrank_out, double 
     bool deficient = false;
     for (int it = 0; it < n; ++it) {
         // pivot search: per lane best candidate, then warp argmax (ties -> low index)
-        double best = -1.0;
+        unsigned long long best = 0;
         int bk = -1;
         for (int j = ln; j < n; j += 32) {
             if (used[j]) continue;
-            double a = fabs(v[(j + 1) * (j + 2) / 2 - 1]);
-            if (a > eps * diag[j] && a > best) { best = a; bk = j; }
+            const unsigned long long a = abs_bits(v[(j + 1) * (j + 2) / 2 - 1]), t = thr[j];
+            if (a <= kInfBits && t <= kInfBits && a > t && (bk < 0 || a > best)) { best = a; bk = j; }
         }
         for (int o = 16; o > 0; o >>= 1) {
-            double ob = __shfl_xor_sync(0xffffffffu, best, o);
-            int ok = __shfl_xor_sync(0xffffffffu, bk, o);
-            if (ob > best || (ob == best && ok >= 0 && (bk < 0 || ok < bk))) { best = ob; bk = ok; }
+            const unsigned long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (ok >= 0 && (bk < 0 || ob > best || (ob == best && ok < bk))) { best = ob; bk = ok; }
         }
         if (bk < 0) { deficient = true; break; }
         const int k = bk;              // 0-based pivot
@@ -137,7 +149,9 @@ __device__ void warp_sqminv(double *v, double *b, int n, int *nrank_out, double 
             if (!used[j]) b[j] = 0.0;
         __syncwarp();
     }
-    for (int idx = ln; idx < np; idx += 32) v[idx] = -v[idx];
+    // negation as a sign flip of the bits (exact, like the FP64 negation)
+    for (int idx = ln; idx < np; idx += 32)
+        v[idx] = __longlong_as_double(__double_as_longlong(v[idx]) ^ (long long)0x8000000000000000ull);
     __syncwarp();
     *nrank_out = nrank;
 }
@@ -806,7 +820,41 @@ k_fit(FitParams p, int perWarp) {
                     m.lwgt[e] = wght;
                 }
                 // ---- second loop: normal equations
-                if (denseLoc) {
+                // room for the products w g_j and w r of every equation in the
+                // B/W area, which the local fit does not use otherwise
+                const bool preW = !BIG && (int64_t)neq * (nalc + 1) <= 2 * (int64_t)p.nalcmax * p.nalgmax;
+                if (denseLoc && preW) {
+                    // every equation has the locals 1..nalc: the first products
+                    // c_ej = w_e g_ej and c_e0 = w_e r_e once per equation, then
+                    // a lane per element of clmat (row j >= column k) or blvec,
+                    // equations added in order, each term c_ej g_ek resp.
+                    // c_e0 g_ej: the operations of the equation-by-equation
+                    // form, (w g_j) g_k and (w r) g_j
+                    double *cw = mB;   // neq x (nalc + 1)
+                    for (int t = ln; t < neq * (nalc + 1); t += 32) {
+                        const int e = t / (nalc + 1), j = t - e * (nalc + 1);
+                        cw[t] = m.lwgt[e] * (j == 0 ? m.rm1[e] : m.gl[m.mq[3 * e] + j]);
+                    }
+                    __syncwarp();
+                    const int nq = npk + nalc;
+                    for (int q = ln; q < nq; q += 32) {
+                        const bool isC = q < npk;
+                        int j = q - npk + 1, k = 1;
+                        if (isC) {
+                            j = 1;
+                            k = q + 1;
+                            while (k > j) { k -= j; j++; }
+                        }
+                        double acc = 0.0;
+                        for (int e = 0; e < neq; ++e) {
+                            const double c = cw[e * (nalc + 1) + (isC ? j : 0)];
+                            acc = acc + c * m.gl[m.mq[3 * e] + (isC ? k : j)];
+                        }
+                        if (isC) m.clmat[q] = acc;
+                        else m.blvec[j - 1] = acc;
+                    }
+                    __syncwarp();
+                } else if (denseLoc) {
                     // every equation has the locals 1..nalc: lane per element
                     // of clmat (row j >= column k) or blvec, equations added in
                     // order, each term (w g_j) g_k resp. (w r) g_j as in the
