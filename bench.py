@@ -161,50 +161,101 @@ def record_shape(d):
     return nmeas, nloc, ng, nalg
 
 
-def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000):
+def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=False, cond=0.0,
+                        skip_slow=False):
     """Dense solve of the scaled telescope (10 layers x nmod modules = 20,000
     globals, packed FP64 matrix from the data loop, ncon constraints: the
     generator's 2 weak-mode constraints plus seeded sparse random ones, all
     eliminated by QL in FP64): the reference-structured FP64 Cholesky
     (metsol 3), the blocked FP64 Cholesky (32) and the tensor-core 3xTF32
     Cholesky (31), the latter two refined by FP64 CG to a relative residual
-    of 1e-13."""
+    of 1e-13.  The inversions from the blocked factors (metsol 12 FP64, 11
+    tensor-core; with sqminl, also the reference-structured Gauss-Jordan,
+    metsol 1) give the parameter errors."""
     cfg = mp.gen_config("telescope_dense", ntracks=ntracks, seed=4)
     cfg.nmod = nmod
     d = mp.generate(cfg)
     H = mp.HostStructure(d, mreqenf=5, sparse=False)
     A0 = mp.constraint_matrix(d, H)
     rng = np.random.default_rng(11)
-    extra = np.zeros((ncon - A0.shape[0], H.nVar))
-    for k in range(extra.shape[0]):
-        idx = rng.choice(H.nVar, 64, replace=False)
-        extra[k, idx] = rng.normal(size=64)
+    reg = 0.0
+    if cond:
+        # weak modes partly constrained: the sum of the shifts is fixed, the
+        # shear (shift proportional to z) is left to a small diagonal
+        # regularisation of 1/cond times the largest diagonal element, and
+        # the other constraints sum to zero inside one layer, so they do not
+        # touch either weak mode; cond(reduced matrix) is then about cond
+        A0 = A0[:1]
+        layer = (H.labels[H.varIndex > 0] - 1) // nmod
+        extra = np.zeros((ncon - 1, H.nVar))
+        for k in range(extra.shape[0]):
+            pool = np.flatnonzero(layer == rng.integers(0, 10))
+            idx = rng.choice(pool, 64, replace=False)
+            c = rng.normal(size=64)
+            extra[k, idx] = c - c.mean()
+    else:
+        extra = np.zeros((ncon - A0.shape[0], H.nVar))
+        for k in range(extra.shape[0]):
+            idx = rng.choice(H.nVar, 64, replace=False)
+            extra[k, idx] = rng.normal(size=64)
     A = np.vstack([A0, extra])
     res = {}
-    for metsol in (32, 31, 3):
+    forms = (32, 31) if skip_slow else (32, 31, 3, 12, 11) + ((1,) if sqminl else ())
+    for metsol in forms:
         ctx = mp.Context(device=local)
         ctx.set_layout(H, 1)
         ctx.set_constraints(A)
         ctx.upload(H)
         ctx.loopbf(np.zeros(H.nTotal))
-        corr, _, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-13, itnlim=2000)
-        res[metsol] = (corr, info.ms, info.itn, info.istop, info.msFactor, info.msRefine)
+        if cond:
+            dg = ctx.matrix_diagonal()
+            reg = float(np.max(dg)) / cond
+            iv = np.arange(1, H.nVar + 1, dtype=np.int32)
+            ctx.mupdat(iv, iv, np.full(H.nVar, reg))
+        inv = metsol in (1, 11, 12)
+        corr, err, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-13, itnlim=2000,
+                                    errors=inv)
+        res[metsol] = (corr, info.ms, info.itn, info.istop, info.msFactor, info.msRefine, err, info.msInverse,
+                       info.dxRel)
         ctx.close()
     ref = res[32][0]
 
-    def rel(x):
-        return float(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
-    return {"n": int(H.nVar), "ncon": int(A.shape[0]), "nfit": int(H.nVar - A.shape[0]),
-            "matrix": "scaled telescope, packed FP64 from the data loop",
-            "ms_fp64_chdec2": res[3][1], "ms_fp64_blocked": res[32][1], "ms_mixed_tf32x3": res[31][1],
-            "speedup_mixed_vs_fp64_blocked": res[32][1] / res[31][1],
-            "speedup_mixed_vs_fp64_chdec2": res[3][1] / res[31][1],
-            "ms_factor_fp64_blocked": res[32][4], "ms_factor_mixed": res[31][4],
-            "ms_refine_fp64_blocked": res[32][5], "ms_refine_mixed": res[31][5],
-            "factor_speedup_mixed_vs_fp64_blocked": res[32][4] / max(res[31][4], 1e-9),
-            "cg_iterations_mixed": res[31][2], "cg_iterations_fp64": res[32][2],
-            "rel_err_mixed_vs_fp64": rel(res[31][0]), "rel_err_chdec2_vs_fp64_blocked": rel(res[3][0]),
-            "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
+    def rel(x, r=ref):
+        return float(np.max(np.abs(x - r)) / np.max(np.abs(r)))
+
+    def relerr(e, r):
+        v = np.abs(r) > 0
+        return float(np.max(np.abs(e[v] - r[v]) / np.abs(r[v])))
+    out = {"n": int(H.nVar), "ncon": int(A.shape[0]), "nfit": int(H.nVar - A.shape[0]),
+           "matrix": "scaled telescope, packed FP64 from the data loop" +
+                     (f", shear weak mode regularised by max(diag)/{cond:.0e}" if cond else ""),
+           "regularisation": reg,
+           "ms_fp64_blocked": res[32][1], "ms_mixed_tf32x3": res[31][1],
+           "speedup_mixed_vs_fp64_blocked": res[32][1] / res[31][1],
+           "ms_factor_fp64_blocked": res[32][4], "ms_factor_mixed": res[31][4],
+           "ms_refine_fp64_blocked": res[32][5], "ms_refine_mixed": res[31][5],
+           "factor_speedup_mixed_vs_fp64_blocked": res[32][4] / max(res[31][4], 1e-9),
+           "cg_iterations_mixed": res[31][2], "cg_iterations_fp64": res[32][2],
+           "last_rel_correction_mixed": res[31][8], "last_rel_correction_fp64": res[32][8],
+           "rel_err_mixed_vs_fp64": rel(res[31][0]),
+           "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
+    if 3 in res:
+        out["ms_fp64_chdec2"] = res[3][1]
+        out["speedup_mixed_vs_fp64_chdec2"] = res[3][1] / res[31][1]
+        out["rel_err_chdec2_vs_fp64_blocked"] = rel(res[3][0])
+    if 12 in res:
+        out["inversion"] = {
+               "ms_fp64_blocked": res[12][1], "ms_mixed_tf32x3": res[11][1],
+               "ms_inverse_fp64_blocked": res[12][7], "ms_inverse_mixed": res[11][7],
+               "rel_err_parameters_mixed_vs_fp64": rel(res[11][0], res[12][0]),
+               "rel_err_errors_mixed_vs_fp64": relerr(res[11][6], res[12][6]),
+               "refinement_steps_mixed": res[11][2], "refinement_steps_fp64": res[12][2],
+               "note": "errors of the tensor-core inverse are not refined: about 1e-7 x cond"}
+    if 1 in res:
+        out["inversion"]["ms_sqminl"] = res[1][1]
+        out["inversion"]["rel_err_errors_fp64_blocked_vs_sqminl"] = relerr(res[12][6], res[1][6])
+        out["inversion"]["rel_err_parameters_fp64_blocked_vs_sqminl"] = rel(res[12][0], res[1][0])
+    return out
 
 
 def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
@@ -508,6 +559,11 @@ def main():
     ap.add_argument("--profile", action="store_true", help="small run for profilers (no e2e/cpu)")
     ap.add_argument("--staging-mb", type=int, default=0, help="update staging buffer (0: default)")
     ap.add_argument("--dense-n", type=int, default=20000, help="globals of the dense-solve measurement (0: skip)")
+    ap.add_argument("--dense-sqminl", action="store_true",
+                    help="also time the reference-structured inversion (sqminl) in the dense measurement")
+    ap.add_argument("--dense-cond", type=float, default=0.0,
+                    help="dense measurement on the input with condition number about this (0: as generated)")
+    ap.add_argument("--dense-only", action="store_true", help="only the dense measurement (with --dense-n)")
     ap.add_argument("--minres-iters", type=int, default=300, help="iterations of the MINRES measurement (0: skip)")
     ap.add_argument("--mbandw", type=int, default=0, help="--part minres: preconditioner (0 diagonal, > 0 band width)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
@@ -520,6 +576,12 @@ def main():
     mp = _load_pkg()
     if args.profile and args.part != "loop":
         profile_part(mp, args.part, args.ntracks, local, args.steps, args.mbandw)
+        return
+    if args.dense_only:
+        if rank == 0:
+            print(json.dumps(dense_solve_measure(mp, local, nmod=args.dense_n // 10, ntracks=20 * args.dense_n,
+                                                 sqminl=args.dense_sqminl, cond=args.dense_cond,
+                                                 skip_slow=args.dense_n > 40000)))
         return
     cfg = mp.gen_config("barrel", ntracks=args.ntracks, seed=2 + 1000 * rank)
     t0 = time.time()
@@ -663,7 +725,8 @@ def main():
         line["minres"] = minres_measure(mp, local, iters=args.minres_iters)
     if args.dense_n > 0 and rank == 0 and not args.profile:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
-                                                  ntracks=20 * args.dense_n)
+                                                  ntracks=20 * args.dense_n, sqminl=args.dense_sqminl,
+                                                  cond=args.dense_cond, skip_slow=args.dense_n > 40000)
     for arr in pinned:
         arr.free()
     if rank == 0:

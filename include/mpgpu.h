@@ -269,6 +269,8 @@ typedef struct mpgpu_solveinfo {
     double msRefine;    /* dense solves: device time of the CG refinement */
     double dxRel;       /* dense solves: size of the last CG correction relative to the
                            solution (|alpha p| / |x|) */
+    double msInverse;   /* blocked inversions (metsol 11, 12): device time of the inverse
+                           from the factor */
 } mpgpu_solveinfo;
 
 /* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES,
@@ -278,6 +280,13 @@ typedef struct mpgpu_solveinfo {
  * info->istop 1 residual test, 2 least-squares test, 4 condition limit,
  * 5 iterate longer than maxxnorm (the previous one is returned), 6
  * iteration limit.
+ * Inversion also in blocked dense form (no counterpart in the reference):
+ * metsol 12 the inverse from the FP64 blocked Cholesky factor, metsol 11
+ * from the factor with tensor-core 3xTF32 trailing updates, its inverse
+ * (trtri, lauum) with 3xTF32 tile products too; the solution is refined as
+ * for metsol 31/32, the errors are the diagonal of the inverse (FP64 form:
+ * FP64 accuracy; tensor-core form: about the 3xTF32 product precision times
+ * the condition number, not refined).
  * Decomposition also in blocked dense form (no counterpart in the
  * reference, same solution): metsol 32 FP64 blocked Cholesky, metsol 31
  * Cholesky with tensor-core 3xTF32 trailing updates; both refine the

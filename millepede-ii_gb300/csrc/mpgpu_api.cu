@@ -857,10 +857,11 @@ extern "C" int32_t mpgpu_solve(mpgpu_ctx *c, int32_t metsol, const double *consR
     mpgpu_solveinfo tmp;
     if (!info) info = &tmp;
     memset(info, 0, sizeof(*info));
-    if (metsol == 1 || metsol == 3 || metsol == 31 || metsol == 32) {
+    if (metsol == 1 || metsol == 3 || metsol == 31 || metsol == 32 || metsol == 11 || metsol == 12) {
         if (c->j.matsto != 1) return set_err(c, MPGPU_ERR_ARG, "inversion/decomposition need packed storage");
-        const int dense = metsol == 31 ? 1 : (metsol == 32 ? 0 : -1);
-        return solve_inversion(c, consResiduals, correction, errors, info, metsol != 1, dense, rtol, itnlim);
+        const int dense = (metsol == 31 || metsol == 11) ? 1 : ((metsol == 32 || metsol == 12) ? 0 : -1);
+        const bool inversion = metsol == 1 || metsol == 11 || metsol == 12;
+        return solve_inversion(c, consResiduals, correction, errors, info, !inversion, dense, rtol, itnlim);
     }
     if (metsol == 4 || metsol == 5)
         return solve_minres(c, consResiduals, rtol, itnlim, correction, info, metsol == 5);

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "mpgpu_ctx.h"
+#include "mpgpu_tc.cuh"
 
 namespace {
 
@@ -115,80 +116,21 @@ __global__ void k_split_tf32(const double *A, int64_t ld, int64_t k0, int64_t nr
 }
 
 // --------------------------------------------- tcgen05 3xTF32 trailing update
+using tc::kTK;
+using tc::kStages;
+using tc::kOpBytes;
+using tc::kStageBytes;
+using tc::kTcSmem;
+using tc::kTcThreads;
+using tc::smem_u32;
+using tc::umma_desc;
+using tc::mma_tf32;
+using tc::mbar_wait;
+using tc::tmem_ld32;
+using tc::load_chunk_async;
+
 // One CTA per 128 x 128 tile (bi >= bj) of the trailing matrix:
-// C -= L_i L_j^T with K = 128, streamed in chunks of 16 through a 3-stage
-// cp.async pipeline; one thread issues the tcgen05.mma of a chunk
-// (hi*hi, hi*lo, lo*hi for two K = 8 steps) and commits them to the
-// stage's mbarrier, which frees the stage for the chunk three ahead.
-// Shared-memory operand layout: K-major, no swizzle, core matrices of
-// 8 rows x 16 bytes; core (row group g, k group c) at (g * 4 + c) * 128
-// bytes: leading (K) byte offset 128, stride (row) byte offset 512.
-constexpr int kTK = 16;                          // K per chunk
-constexpr int kStages = 3;
-constexpr int kOpBytes = kNB * kTK * 4;          // 8 KB per operand chunk
-constexpr int kStageBytes = 4 * kOpBytes;        // hi/lo of both operands
-constexpr int kTcSmem = kStages * kStageBytes;  // the epilogue transposes reuse stage 0
-constexpr int kTcThreads = 128;
-constexpr int kWaitLimit = 1 << 22;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(512 >> 4) << 32) |
-           (1ull << 46);
-}
-
-// instruction descriptor: D f32, A/B tf32, both K-major, N = 128, M = 128
-constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kNB >> 3) << 17) |
-                            ((uint32_t)(kNB >> 4) << 24);
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
-    asm volatile(
-        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-        "l"(ad), "l"(bd), "r"(kIdesc), "r"(acc));
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
-    for (int i = 0; i < kWaitLimit; ++i) {
-        uint32_t ok;
-        asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (ok) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-}
-
-// asynchronous copy of a 128 x 16 fp32 chunk (rows of 128 in global) into
-// the core-matrix layout; 4 x 16-byte copies per thread
-__device__ __forceinline__ void load_chunk_async(const float *g, int kc0, uint32_t s) {
-#pragma unroll
-    for (int i = 0; i < kNB * (kTK / 4) / kTcThreads; ++i) {
-        const int idx = threadIdx.x + i * kTcThreads;
-        const int row = idx >> 2, k4 = idx & 3;
-        const float *src = g + (int64_t)row * kNB + kc0 + k4 * 4;
-        const uint32_t dst = s + ((row >> 3) * 4 + k4) * 128 + (row & 7) * 16;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
-    }
-}
-
+// C -= L_i L_j^T with K = 128 (the chunk pipeline of mpgpu_tc.cuh).
 __global__ void __launch_bounds__(kTcThreads) k_syrk_tc(double *A, int64_t ld, int64_t r0, int32_t T,
                                                         const float *hi, const float *lo, int32_t *err) {
     extern __shared__ __align__(128) char tsm[];
@@ -688,7 +630,7 @@ void dotv(const DenseWork &w, const double *a, const double *b, double *out, cud
 // vector bx (b in, x out).  mode 0: FP64 factor, mode 1: tensor-core
 // factor; both refined by preconditioned CG in FP64 to rtol.
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
-                        int32_t itnlim, mpgpu_solveinfo *info) {
+                        int32_t itnlim, mpgpu_solveinfo *info, double *invOut) {
     cudaStream_t s = c->stream;
     DenseWork w;
     w.npad = ((int64_t)n + kNB - 1) / kNB * kNB;
@@ -779,15 +721,32 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     }
     if (istop == 0) istop = 3;
     cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    // the inverse from the same factor (inversion forms): X = L^-1, Z = X^T X
+    cudaEvent_t eR;
+    cudaEventCreate(&eR);
+    cudaEventRecord(eR, s);
+    int32_t rcInv = MPGPU_OK;
+    if (invOut && istop != 9) rcInv = dense_inverse_device(c, w.L, w.npad, n, mode, w.DinvT, w.F, invOut, w.err);
     cudaEventRecord(e1, s);
     MPG_CUDA(c, cudaStreamSynchronize(s));
-    float ms = 0.0f, msF = 0.0f;
+    float ms = 0.0f, msF = 0.0f, msR = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventElapsedTime(&msF, e0, eF);
+    cudaEventElapsedTime(&msR, e0, eR);
     cudaEventDestroy(eF);
+    cudaEventDestroy(eR);
+    if (rcInv != MPGPU_OK) {
+        cudaGraphExecDestroy(gexec);
+        cudaGraphDestroy(graph);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        w.release();
+        return rcInv;
+    }
     if (info) {
         info->msFactor = msF;
-        info->msRefine = ms - msF;
+        info->msRefine = msR - msF;
+        info->msInverse = ms - msR;
         info->itn = itn;
         info->istop = istop;
         info->nrank = n;

@@ -1238,7 +1238,7 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
         k_cons_rhs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, ncon, j.matD, yv, corr);
     }
     int nrank = 0;
-    if (!decomposition) {
+    if (!decomposition && dense < 0) {
         // sqminl (mpnum.f90:230-355) on the leading nfit x nfit block
         k_diag_abs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, j.matD, diag);
         MPG_CUDA(c, cudaMemsetAsync(used, 0, sizeof(int32_t) * nfit, s));
@@ -1256,8 +1256,11 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
     } else if (dense >= 0) {
         // blocked dense Cholesky (FP64, or tensor-core 3xTF32) refined by
         // preconditioned CG in FP64
+        // (inversion forms: the inverse from the same factor replaces the
+        // leading block of the packed matrix, where sqminl leaves it)
         const double tol = rtol > 0.0 ? rtol : 1e-13;
-        const int32_t rcd = dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000, info);
+        const int32_t rcd = dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000, info,
+                                            decomposition ? nullptr : j.matD);
         if (rcd != MPGPU_OK) {
             cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
             cudaFree(used); cudaFree(piv);

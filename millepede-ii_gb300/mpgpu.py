@@ -78,7 +78,7 @@ class SolveInfo(C.Structure):
     _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
                 ("nrkd", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
                 ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double),
-                ("dxRel", C.c_double)]
+                ("dxRel", C.c_double), ("msInverse", C.c_double)]
 
 
 class Steer(C.Structure):
@@ -508,6 +508,11 @@ class Context:
     def matrix(self):
         m = np.zeros(self.nmat, np.float64)
         self.check(self.L.mpgpu_download_matrix(self.h, ptr(m, f64p)))
+        return m
+
+    def matrix_diagonal(self):
+        m = np.zeros(self.nVar, np.float64)
+        self.check(self.L.mpgpu_matrix_diagonal(self.h, ptr(m, f64p)))
         return m
 
     def status(self):

@@ -212,3 +212,40 @@ def test_minresqlp_singular_minimum_length(mp):
     assert np.linalg.matrix_rank(M, tol=1e-9 * np.max(np.abs(M))) <= H.nVar - 2
     assert info.istop in (1, 2, 4)
     assert np.max(np.abs(corr - want)) <= 1e-7 * np.max(np.abs(want))
+
+
+@pytest.mark.parametrize("nmod", [30, 300])
+def test_blocked_inversion_forms(mp, nmod):
+    """Inversion from the blocked Cholesky factor (metsol 12 FP64, metsol 11
+    tensor-core 3xTF32 with its trtri/lauum tile products in 3xTF32 as
+    well) against sqminl (metsol 1) on the same QL-reduced matrix: the
+    refined solutions within 1e-10; the FP64 form's errors within 1e-9 (the
+    sqminl bar).  The tensor-core form's errors are not refined: their
+    relative error is about 1e-7 x the condition number of the reduced
+    matrix (6 % for the 3,000-parameter telescope, cond ~ 1e5), asserted
+    only within 0.2 here.  Sizes above and below one 128 tile and with
+    padding."""
+    cfg = mp.gen_config("telescope", ntracks=40 * nmod * 10, seed=23)
+    cfg.nmod = nmod
+    d = mp.generate(cfg)
+    H = mp.HostStructure(d, mreqenf=5, sparse=False)
+    A = mp.constraint_matrix(d, H)
+    out = {}
+    for metsol in (1, 12, 11):
+        with mp.Context() as ctx:
+            ctx.set_layout(H, 1)
+            ctx.set_constraints(A)
+            ctx.upload(H)
+            ctx.loopbf(np.zeros(H.nTotal))
+            corr, err, info = ctx.solve(metsol, consResiduals=np.zeros(A.shape[0]), rtol=1e-13, errors=True)
+            out[metsol] = (corr, err, info.nrank, info.msInverse)
+    corr1, err1 = out[1][0], out[1][1]
+    scale = np.max(np.abs(corr1))
+    var = np.abs(err1) > 0
+    for metsol, tol in ((12, 1e-9), (11, 0.2)):
+        corr, err, nrank, msinv = out[metsol]
+        assert nrank == H.nVar - A.shape[0]
+        assert np.max(np.abs(corr - corr1)) <= 1e-10 * scale, metsol
+        rel = np.max(np.abs(err[var] - err1[var]) / np.abs(err1[var]))
+        assert rel <= tol, (metsol, rel)
+        assert msinv > 0
