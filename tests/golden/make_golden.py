@@ -3,7 +3,8 @@ python/tinypede.py of the Millepede-II sources (local fits by dense
 inversion, global matrix and vector, constraints by Lagrange multipliers,
 solution and errors by inversion of the bordered matrix).
 
-    python tests/golden/make_golden.py [path to the Millepede-II sources]
+    python tests/golden/make_golden.py <path to the Millepede-II sources>
+    (or the path in the environment variable MILLEPEDE_SOURCES)
 
 For every case the seeded synthetic records are made by the package's
 generator (the SHA-256 of the record arrays is stored so a test can see that
@@ -11,8 +12,15 @@ it regenerates the same input), written as a C-format Mille file, read back
 by tinypede and processed with its Pede class.  Stored per case (.npz):
 the label order, the global matrix (packed lower triangle, or for larger
 cases its diagonal plus products with seeded probe vectors), the global
-vector, the solution and the errors.  tinypede's chi2 scaling factor is set
-huge so that it rejects nothing (its rejection test is not pede's).
+vector, the solution and the errors.
+
+Rejections: tinypede rejects a local fit when prob(chi2 / f, ndf) < 0.0027,
+pede when chi2 > chicut * chindl(3, ndf) * ndf (pede.f90:4106-4131), whose
+table reproduces the same 3-sigma quantile to 4e-5.  With f = chicut the
+two reject the same records unless a chi2 lies within that tolerance of the
+cut, so a case with rejections checks (with tinypede's own record reader)
+that every record's chi2 is at least 1e-3 away from its cut.  The other
+cases set f huge so that nothing is rejected.
 """
 import contextlib
 import hashlib
@@ -37,6 +45,12 @@ CASES = {
                           constraints=False, full=True),
     "brokenlines_band": dict(kind="brokenlines", ntracks=60, seed=13, entries=1, fixed=(),
                              constraints=False, full=False, nmod=288, minHits=6, maxHits=12),
+    # records with outlier hits, rejected by the chi2 cut of the first loop
+    "telescope_rej": dict(kind="telescope", ntracks=3000, seed=14, entries=25, fixed=(),
+                          constraints=False, full=True, outlierFrac=0.02, chicut=30.0),
+    # the barrel (6 dof per module): mpbits-sparse storage on the device
+    "barrel_sparse": dict(kind="barrel", ntracks=3000, seed=15, entries=1, fixed=(),
+                          constraints=False, full=False, nmod=300, sparse=True),
 }
 NPROBE = 4
 
@@ -51,7 +65,7 @@ def load_mp():
 
 def case_data(mp, c):
     cfg = mp.gen_config(c["kind"], ntracks=c["ntracks"], seed=c["seed"])
-    for k in ("nmod", "minHits", "maxHits"):
+    for k in ("nmod", "minHits", "maxHits", "outlierFrac"):
         if k in c:
             setattr(cfg, k, c[k])
     return mp.generate(cfg)
@@ -85,7 +99,7 @@ def run_tinypede(tinypede, mp, d, c, tmp):
         p.addBinaryFile(binf, len(d["recPtr"]) - 1, "C")
         p.defineParameters(c["entries"], list(c["fixed"]))
         p.addConstraints(conf)
-        p.construct(chi2Factor=1e12)
+        p.construct(chi2Factor=c.get("chicut", 1e12))
     npar = p._Pede__numPar
     M = p._Pede__matrix
     vec = p._Pede__vector[:npar].copy()
@@ -104,14 +118,58 @@ def run_tinypede(tinypede, mp, d, c, tmp):
     return out
 
 
+def cut_margin(tinypede, mp, d, c, tmp):
+    """Smallest relative distance of a record's local-fit chi2 from the cut
+    f * q3(ndf) (q3: the 3-sigma quantile), over the records, read with
+    tinypede's record reader and fitted by plain least squares."""
+    from scipy.stats import chi2
+    binf = os.path.join(tmp, "margin.bin")
+    mp.write_mille_c(binf, d["recPtr"], d["inder"], d["glder"])
+    f = c["chicut"]
+    best = np.inf
+    with open(binf, "rb") as fh:
+        for _ in range(len(d["recPtr"]) - 1):
+            rec = tinypede.MilleRecord()
+            rec.readRecord(fh, "C")
+            rows, meas, wts = [], [], []
+            nloc = 0
+            while rec.moreData():
+                if rec.specialDataTag() >= 0:
+                    continue
+                aMeas, aPrec, indLocal, derLocal, _, _ = rec.getData()
+                rows.append(dict(zip(indLocal, derLocal)))
+                meas.append(aMeas)
+                wts.append(aPrec)
+                nloc = max(nloc, max(indLocal))
+            L = np.zeros((len(rows), nloc))
+            for i, r in enumerate(rows):
+                for k, v in r.items():
+                    L[i, k - 1] = v
+            w = np.array(wts)
+            m = np.array(meas)
+            q = np.linalg.solve(L.T @ (w[:, None] * L), L.T @ (w * m))
+            res = m - L @ q
+            c2 = float(res @ (w * res))
+            ndf = len(rows) - nloc
+            cut = f * chi2.ppf(1.0 - 0.0027, ndf)
+            best = min(best, abs(c2 - cut) / cut)
+    return best
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MILLEPEDE_SOURCES")
+    if not ref:
+        sys.exit("usage: make_golden.py <path to the Millepede-II sources> (or set MILLEPEDE_SOURCES)")
     sys.path.insert(0, os.path.join(ref, "python"))
     import tinypede
     mp = load_mp()
     for name, c in CASES.items():
         d = case_data(mp, c)
         with tempfile.TemporaryDirectory() as tmp:
+            if "chicut" in c:
+                margin = cut_margin(tinypede, mp, d, c, tmp)
+                assert margin > 1e-3, f"{name}: a chi2 lies {margin:.1e} from its cut"
+                print(name, "smallest relative distance of a chi2 from its cut", f"{margin:.2e}")
             out = run_tinypede(tinypede, mp, d, c, tmp)
         out["record_sha256"] = np.array(record_hash(d))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)

@@ -1,6 +1,7 @@
 """The device path through the C-ABI against the golden vectors of the
 reference's tinypede.py (tests/golden/make_golden.py): global matrix and
-vector from mpgpu_loopbf within 1e-11 relative; solutions of whole jobs
+vector from mpgpu_loopbf within 1e-11 relative (packed and mpbits-sparse
+storage), the records rejected by the chi2 cut equal; solutions of whole jobs
 (mpgpu_pede_run, inversion) within 1e-9 relative; errors of the
 unconstrained job within 1e-9 relative (constrained errors follow pede's
 qlssq, see test_golden.py)."""
@@ -15,7 +16,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden as G  # noqa: E402
-from test_golden import load, rel  # noqa: E402
+from test_golden import check_rejections, load, products, rel  # noqa: E402
 from test_gpu_pede import gpu_job  # noqa: E402
 
 
@@ -28,25 +29,25 @@ def case(mp, name):
 
 
 @pytest.mark.parametrize("name", list(G.CASES))
-def test_device_matrix_vector(mp, name):
+def test_device_matrix_vector(mp, orc, name):
     c, d, g = case(mp, name)
     fixed = np.array(c["fixed"], np.int32)
+    sparse = c.get("sparse", False)
     H = mp.HostStructure(d, mreqenf=c["entries"], preLabel=fixed, preSigma=-np.ones(len(fixed)),
-                         sparse=False)
+                         sparse=sparse)
+    matsto = 2 if sparse else 1
     with mp.Context() as ctx:
-        ctx.set_layout(H, 1)
+        ctx.set_layout(H, matsto)
         ctx.upload(H)
-        o = ctx.loopbf(np.zeros(H.nTotal))
-        packed = ctx.matrix()
-    assert sum(o["nrej"]) == 0
+        o = ctx.loopbf(np.zeros(H.nTotal), chicut=c.get("chicut", 0.0))
+        m = ctx.matrix()
+    check_rejections(o["nrej"], g)
     n = H.nVar
-    A = np.zeros((n, n))
-    A[np.tril_indices(n)] = packed
-    A = A + np.tril(A, -1).T
-    assert rel(np.diag(A), g["diag"]) <= 1e-11
-    assert rel(A @ G.probes(n).T, g["probe"]) <= 1e-11
+    dg, pr = products(orc, matsto, m, n, H.aig, H.offsets, H.columns)
+    assert rel(dg, g["diag"]) <= 1e-11
+    assert rel(pr, g["probe"]) <= 1e-11
     if "packed" in g:
-        assert rel(A[np.tril_indices(n)], g["packed"]) <= 1e-11
+        assert rel(m, g["packed"]) <= 1e-11
     assert rel(o["gvec"], g["vector"]) <= 1e-11
 
 
