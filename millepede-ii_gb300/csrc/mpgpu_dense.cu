@@ -24,6 +24,7 @@
 namespace {
 
 constexpr int kNB = 128;   // panel width = tile size
+constexpr int kSuperPanels = 4;   // panels per block column of the tensor-core factorisation
 
 // ------------------------------------------------------------ panel kernels
 // Cholesky of the 128 x 128 diagonal block at (k0, k0), in shared memory.
@@ -31,6 +32,7 @@ __global__ void __launch_bounds__(512) k_potrf128(double *A, int64_t ld, int64_t
     extern __shared__ __align__(16) double sa[];   // 128 x 129
     constexpr int S = kNB + 1;
     __shared__ int bad;
+    __shared__ double sinv;   // reciprocal of the pivot: one FP64 division per column, not one per thread
     const int tid = threadIdx.x, nt = blockDim.x;
     if (tid == 0) bad = 0;
     for (int e = tid; e < kNB * kNB; e += nt) {
@@ -41,11 +43,13 @@ __global__ void __launch_bounds__(512) k_potrf128(double *A, int64_t ld, int64_t
     for (int j = 0; j < kNB; ++j) {
         if (tid == 0) {
             const double d = sa[j * S + j];
-            if (!(d > 0.0)) { bad = 1; sa[j * S + j] = 1.0; }
-            else sa[j * S + j] = sqrt(d);
+            const double piv = d > 0.0 ? sqrt(d) : 1.0;
+            if (!(d > 0.0)) bad = 1;
+            sa[j * S + j] = piv;
+            sinv = 1.0 / piv;
         }
         __syncthreads();
-        const double inv = 1.0 / sa[j * S + j];
+        const double inv = sinv;
         for (int i = j + 1 + tid; i < kNB; i += nt) sa[i * S + j] *= inv;
         __syncthreads();
         const int m = kNB - 1 - j;
@@ -100,153 +104,6 @@ __global__ void __launch_bounds__(256) k_trsm128(double *A, int64_t ld, int64_t 
     }
 }
 
-// L21 rows as TF32 pairs (hi, lo), row-major with 128 columns
-__global__ void k_split_tf32(const double *A, int64_t ld, int64_t k0, int64_t nrows, float *hi, float *lo) {
-    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nrows * kNB) return;
-    const int64_t r = e / kNB;
-    const int k = (int)(e % kNB);
-    const double x = A[(k0 + kNB + r) * ld + k0 + k];
-    uint32_t h, l;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
-    const double rest = x - (double)__uint_as_float(h);
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"((float)rest));
-    hi[e] = __uint_as_float(h);
-    lo[e] = __uint_as_float(l);
-}
-
-// --------------------------------------------- tcgen05 3xTF32 trailing update
-using tc::kTK;
-using tc::kStages;
-using tc::kOpBytes;
-using tc::kStageBytes;
-using tc::kTcSmem;
-using tc::kTcThreads;
-using tc::smem_u32;
-using tc::umma_desc;
-using tc::mma_tf32;
-using tc::mbar_wait;
-using tc::tmem_ld32;
-using tc::load_chunk_async;
-
-// One CTA per 128 x 128 tile (bi >= bj) of the trailing matrix:
-// C -= L_i L_j^T with K = 128 (the chunk pipeline of mpgpu_tc.cuh).
-__global__ void __launch_bounds__(kTcThreads) k_syrk_tc(double *A, int64_t ld, int64_t r0, int32_t T,
-                                                        const float *hi, const float *lo, int32_t *err) {
-    extern __shared__ __align__(128) char tsm[];
-    __shared__ uint64_t mbar[kStages];
-    __shared__ uint32_t tbase;
-    const int tid = threadIdx.x, wib = tid >> 5, ln = tid & 31;
-    const int64_t t = blockIdx.x;
-    int bi = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while ((int64_t)bi * (bi + 1) / 2 > t) bi--;
-    while ((int64_t)(bi + 1) * (bi + 2) / 2 <= t) bi++;
-    const int bj = (int)(t - (int64_t)bi * (bi + 1) / 2);
-    if (bi >= T) return;
-    const uint32_t sbase = smem_u32(tsm);
-    float *epi = reinterpret_cast<float *>(tsm) + wib * 32 * 33;   // after the last MMA only
-    if (wib == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tbase)),
-                     "r"(kNB));
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
-    }
-    if (tid == 0) {
-        for (int st = 0; st < kStages; ++st)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar[st])));
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = tbase;
-    const float *ops[4] = {hi + (int64_t)bi * kNB * kNB, lo + (int64_t)bi * kNB * kNB,
-                           hi + (int64_t)bj * kNB * kNB, lo + (int64_t)bj * kNB * kNB};
-    constexpr int nch = kNB / kTK;
-    uint32_t ph = 0;   // bit st: parity of the next completion of stage st's barrier
-    bool ok = true;
-    for (int c = 0; c < kStages - 1; ++c) {
-#pragma unroll
-        for (int o = 0; o < 4; ++o) load_chunk_async(ops[o], c * kTK, sbase + c * kStageBytes + o * kOpBytes);
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    }
-    for (int c = 0; c < nch; ++c) {
-        const int st = c % kStages;
-        asm volatile("cp.async.wait_group %0;\n" ::"n"(kStages - 2) : "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t sb = sbase + st * kStageBytes;
-#pragma unroll
-            for (int kk = 0; kk < kTK / 8; ++kk) {
-                const uint32_t off = kk * 256;   // 8 tf32 = 2 core matrices along K
-                const uint64_t dah = umma_desc(sb + off), dal = umma_desc(sb + kOpBytes + off);
-                const uint64_t dbh = umma_desc(sb + 2 * kOpBytes + off), dbl = umma_desc(sb + 3 * kOpBytes + off);
-                mma_tf32(tmem, dah, dbh, (c > 0 || kk > 0) ? 1u : 0u);
-                mma_tf32(tmem, dah, dbl, 1u);
-                mma_tf32(tmem, dal, dbh, 1u);
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                             smem_u32(&mbar[st]))
-                         : "memory");
-        }
-        // the stage of chunk c + kStages - 1 held chunk c - 1: wait for its MMAs
-        const int cn = c + kStages - 1;
-        if (cn < nch) {
-            const int sn = cn % kStages;
-            if (c >= 1) {
-                if (!mbar_wait(smem_u32(&mbar[sn]), (ph >> sn) & 1)) { ok = false; }
-                ph ^= 1u << sn;
-            }
-            if (ok)
-#pragma unroll
-                for (int o = 0; o < 4; ++o)
-                    load_chunk_async(ops[o], cn * kTK, sbase + sn * kStageBytes + o * kOpBytes);
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-        if (!__syncthreads_and(ok)) { ok = false; break; }
-    }
-    // wait for the MMAs of the chunks not yet waited for (the last kStages-1)
-    if (ok) {
-        for (int c = (nch > kStages - 1 ? nch - (kStages - 1) : 0); c < nch; ++c) {
-            const int st = c % kStages;
-            if (!mbar_wait(smem_u32(&mbar[st]), (ph >> st) & 1)) ok = false;
-            ph ^= 1u << st;
-        }
-    } else {
-        for (int st = 0; st < kStages; ++st) mbar_wait(smem_u32(&mbar[st]), (ph >> st) & 1);
-    }
-    asm volatile("cp.async.wait_all;\n" ::: "memory");
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    if (__syncthreads_and(ok)) {   // every MMA done: the stages are free for the transposes
-        // rows of warp w = tensor-memory lanes 32w .. 32w+31; transpose each
-        // 32 x 32 block through shared memory so the FP64 update is coalesced
-        const int64_t rowBase = r0 + (int64_t)bi * kNB + wib * 32;
-        const int64_t colBase = r0 + (int64_t)bj * kNB;
-        for (int cb = 0; cb < kNB / 32; ++cb) {
-            uint32_t v[32];
-            tmem_ld32(tmem + ((uint32_t)(wib * 32) << 16) + (uint32_t)(cb * 32), v);
-#pragma unroll
-            for (int q = 0; q < 32; ++q) epi[ln * 33 + q] = __uint_as_float(v[q]);
-            __syncwarp();
-            // all 32 loads in flight before the subtractions
-            double cv[32];
-            double *cp = A + rowBase * ld + colBase + cb * 32 + ln;
-#pragma unroll
-            for (int r = 0; r < 32; ++r) cv[r] = cp[r * ld];
-#pragma unroll
-            for (int r = 0; r < 32; ++r) cp[r * ld] = cv[r] - (double)epi[r * 33 + ln];
-            __syncwarp();
-        }
-    } else if (tid == 0) {
-        atomicExch(err, -1);
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-    __syncthreads();
-    if (wib == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kNB));
-}
-
 // ------------------------------------------------ FP64 trailing update
 // 64 x 64 tiles (bi >= bj), 256 threads with 4 x 4 outputs each, K = 128
 // in chunks of 16 from the FP64 panel.
@@ -296,39 +153,145 @@ __global__ void k_pad_identity(double *A, int64_t ld, int64_t n, int64_t npad) {
 // Factorise the dense padded matrix A (npad x npad, row-major, lower
 // triangle) in place.  Returns 0, MPGPU_ERR_FACTOR (non-positive pivot in
 // panel *badPanel) or a CUDA/timeout error.
+// mode 0: right-looking by 128-wide panels, FP64 trailing updates.
+// mode 1: block columns of kSuperPanels panels: inside a block column the
+// 128-wide panels are factorised and update the rest of the block column;
+// the trailing matrix then receives the whole block column at once, K = 512
+// accumulated in tensor memory before one FP64 read-modify-write per tile
+// (tcgen05 3xTF32 tile products, mpgpu_inverse.cu).  hiBuf/loBuf hold the
+// TF32 split of one block column: npad x (128 * kSuperPanels) floats each.
 int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, float *hiBuf, float *loBuf,
                               int32_t *dErr, int32_t *badPanel) {
     cudaStream_t s = c->stream;
     const int64_t ld = npad;
-    const int64_t np = npad / kNB;
+    const int32_t np = (int32_t)(npad / kNB);
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
     const int potrfSmem = kNB * (kNB + 1) * (int)sizeof(double);
     const int trsmSmem = (kNB * kNB + kNB) * (int)sizeof(double);
-    const int tcSmem = kTcSmem;
     MPG_CUDA(c, cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, potrfSmem));
     MPG_CUDA(c, cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize, trsmSmem));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tcSmem));
     MPG_CUDA(c, cudaMemsetAsync(dErr, 0, sizeof(int32_t), s));
-    for (int64_t p = 0; p < np; ++p) {
-        const int64_t k0 = p * kNB;
-        k_potrf128<<<1, 512, potrfSmem, s>>>(A, ld, k0, dErr);
+    auto panel = [&](int32_t p, cudaStream_t st) -> int64_t {   // potrf + trsm of panel p; rows below it
+        const int64_t k0 = (int64_t)p * kNB;
+        k_potrf128<<<1, 512, potrfSmem, st>>>(A, ld, k0, dErr);
         const int64_t rows = npad - k0 - kNB;
-        if (rows <= 0) break;
-        const int64_t tb = std::min<int64_t>((rows + 7) / 8, (int64_t)nsm);
-        k_trsm128<<<(unsigned)tb, 256, trsmSmem, s>>>(A, ld, k0, rows);
-        const int64_t r0 = k0 + kNB;
-        if (mode == 1) {
-            k_split_tf32<<<(unsigned)((rows * kNB + 255) / 256), 256, 0, s>>>(A, ld, k0, rows, hiBuf, loBuf);
-            const int32_t T = (int32_t)(rows / kNB);
-            const int64_t ntile = (int64_t)T * (T + 1) / 2;
-            k_syrk_tc<<<(unsigned)ntile, kTcThreads, tcSmem, s>>>(A, ld, r0, T, hiBuf, loBuf, dErr);
-        } else {
+        if (rows > 0) {
+            const int64_t tb = std::min<int64_t>((rows + 7) / 8, (int64_t)nsm);
+            k_trsm128<<<(unsigned)tb, 256, trsmSmem, st>>>(A, ld, k0, rows);
+        }
+        return rows;
+    };
+    if (mode == 0) {
+        for (int32_t p = 0; p < np; ++p) {
+            const int64_t rows = panel(p, s);
+            if (rows <= 0) break;
             const int32_t T = (int32_t)(rows / 64);
             const int64_t ntile = (int64_t)T * (T + 1) / 2;
-            k_syrk_fp64<<<(unsigned)ntile, 256, 0, s>>>(A, ld, k0, r0, T);
+            k_syrk_fp64<<<(unsigned)ntile, 256, 0, s>>>(A, ld, (int64_t)p * kNB, (int64_t)(p + 1) * kNB, T);
+            MPG_CUDA(c, cudaGetLastError());
+        }
+    } else {
+        // Task lists, copied once: (1) the updates inside every block
+        // column (panel p updates the tiles (i, j) of the later panels j of
+        // its block column, i >= j); (2) per block column, the trailing
+        // tiles of the next block column, which the next panels need first.
+        std::vector<tc::TileTask> tk;
+        std::vector<int64_t> off(np + 1, 0);
+        const int32_t nbc = (np + kSuperPanels - 1) / kSuperPanels;
+        std::vector<int64_t> offN(nbc + 1, 0);
+        for (int32_t s0 = 0; s0 < np; s0 += kSuperPanels) {
+            const int32_t e = std::min(s0 + kSuperPanels, np);
+            for (int32_t p = s0; p < e; ++p) {
+                off[p] = (int64_t)tk.size();
+                for (int32_t jj = p + 1; jj < e; ++jj)
+                    for (int32_t i = jj; i < np; ++i) tk.push_back({i, jj, p - s0, p - s0 + 1, i, jj});
+            }
+        }
+        off[np] = (int64_t)tk.size();
+        for (int32_t b = 0; b < nbc; ++b) {
+            const int32_t s0 = b * kSuperPanels, e = std::min(s0 + kSuperPanels, np);
+            const int32_t e2 = std::min(e + kSuperPanels, np);
+            offN[b] = (int64_t)tk.size();
+            for (int32_t jj = e; jj < e2; ++jj)
+                for (int32_t i = jj; i < np; ++i) tk.push_back({i, jj, 0, e - s0, i, jj});
+        }
+        offN[nbc] = (int64_t)tk.size();
+        // panels (and the tiles the next panels need) on a high-priority
+        // stream, the bulk of each trailing update on a second stream: the
+        // panels of block column b + 1 run while the bulk of block column b
+        // is updated (look-ahead); the TF32 split of a block column is
+        // double-buffered for that overlap
+        struct Res {
+            tc::TileTask *task = nullptr;
+            float *hl[4] = {nullptr, nullptr, nullptr, nullptr};
+            cudaStream_t sp = nullptr, sb = nullptr;
+            cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+            ~Res() {
+                if (sp) cudaStreamSynchronize(sp);
+                if (sb) cudaStreamSynchronize(sb);
+                cudaFree(task);
+                cudaFree(hl[2]);   // hl[0], hl[1] are the caller's
+                cudaFree(hl[3]);
+                for (cudaEvent_t e : ev)
+                    if (e) cudaEventDestroy(e);
+                if (sp) cudaStreamDestroy(sp);
+                if (sb) cudaStreamDestroy(sb);
+            }
+        } R;
+        const int64_t splitLen = npad * kNB * kSuperPanels;
+        MPG_CUDA(c, cudaMalloc(&R.task, sizeof(tc::TileTask) * std::max<size_t>(tk.size(), 1)));
+        R.hl[0] = hiBuf;
+        R.hl[1] = loBuf;
+        MPG_CUDA(c, cudaMalloc(&R.hl[2], sizeof(float) * splitLen));
+        MPG_CUDA(c, cudaMalloc(&R.hl[3], sizeof(float) * splitLen));
+        int lo = 0, hiPrio = 0;
+        MPG_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hiPrio));
+        MPG_CUDA(c, cudaStreamCreateWithPriority(&R.sp, cudaStreamNonBlocking, hiPrio));
+        MPG_CUDA(c, cudaStreamCreateWithPriority(&R.sb, cudaStreamNonBlocking, lo));
+        for (cudaEvent_t &e : R.ev) MPG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        cudaEvent_t evStart = R.ev[0], evBulk = R.ev[1], evPanels = R.ev[2], evEnd = R.ev[3];
+        if (!tk.empty())
+            MPG_CUDA(c, cudaMemcpyAsync(R.task, tk.data(), sizeof(tc::TileTask) * tk.size(), cudaMemcpyHostToDevice,
+                                        s));
+        MPG_CUDA(c, cudaEventRecord(evStart, s));
+        MPG_CUDA(c, cudaStreamWaitEvent(R.sp, evStart, 0));
+        MPG_CUDA(c, cudaStreamWaitEvent(R.sb, evStart, 0));
+        MPG_CUDA(c, cudaEventRecord(evBulk, R.sb));
+        hiBuf = nullptr;   // the buffers are R.hl from here on
+        loBuf = nullptr;
+        for (int32_t b = 0; b < nbc; ++b) {
+            const int32_t s0 = b * kSuperPanels, e = std::min(s0 + kSuperPanels, np);
+            const int32_t e2 = std::min(e + kSuperPanels, np);
+            float *hb = R.hl[2 * (b & 1)], *lb = R.hl[2 * (b & 1) + 1];
+            const tc::TcOp op{hb, lb, kSuperPanels};
+            bool last = false;
+            for (int32_t p = s0; p < e; ++p) {
+                const int64_t rows = panel(p, R.sp);
+                if (rows <= 0) { last = true; break; }
+                MPG_CUDA(c, tc_split_tiles(A, ld, p + 1, np, p, p + 1, hb, lb, kSuperPanels, s0, R.sp));
+                MPG_CUDA(c, tc_tile_gemm(op, op, A, ld, R.task + off[p], off[p + 1] - off[p], 0, 0, -1.0, 1.0,
+                                         dErr, R.sp));
+            }
+            if (last) break;
+            if (e >= np) break;
+            // the next block column's tiles, after the previous bulk update
+            MPG_CUDA(c, cudaStreamWaitEvent(R.sp, evBulk, 0));
+            MPG_CUDA(c, tc_tile_gemm(op, op, A, ld, R.task + offN[b], offN[b + 1] - offN[b], 0, 0, -1.0, 1.0, dErr,
+                                     R.sp));
+            MPG_CUDA(c, cudaEventRecord(evPanels, R.sp));
+            // the bulk: tiles (i, j >= e2), on the second stream
+            const int64_t T = np - e2;
+            MPG_CUDA(c, cudaStreamWaitEvent(R.sb, evPanels, 0));
+            if (T > 0)
+                MPG_CUDA(c, tc_tile_gemm(op, op, A, ld, nullptr, T * (T + 1) / 2, e2, e - s0, -1.0, 1.0, dErr, R.sb));
+            MPG_CUDA(c, cudaEventRecord(evBulk, R.sb));
         }
         MPG_CUDA(c, cudaGetLastError());
+        MPG_CUDA(c, cudaEventRecord(evEnd, R.sb));
+        MPG_CUDA(c, cudaStreamWaitEvent(s, evEnd, 0));
+        MPG_CUDA(c, cudaEventRecord(evPanels, R.sp));
+        MPG_CUDA(c, cudaStreamWaitEvent(s, evPanels, 0));
     }
     int32_t h = 0;
     MPG_CUDA(c, cudaMemcpyAsync(&h, dErr, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -354,8 +317,8 @@ extern "C" int32_t mpgpu_dense_cholesky(mpgpu_ctx *c, int32_t n, const double *A
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     auto fail = [&](cudaError_t e, const char *w) { rc = cuda_err(c, e, w); };
     cudaError_t e = cudaMalloc(&dA, sizeof(double) * npad * npad);
-    if (e == cudaSuccess) e = cudaMalloc(&hi, sizeof(float) * npad * kNB);
-    if (e == cudaSuccess) e = cudaMalloc(&lo, sizeof(float) * npad * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&hi, sizeof(float) * npad * kNB * kSuperPanels);
+    if (e == cudaSuccess) e = cudaMalloc(&lo, sizeof(float) * npad * kNB * kSuperPanels);
     if (e == cudaSuccess) e = cudaMalloc(&dErr, sizeof(int32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(dA, 0, sizeof(double) * npad * npad, s);
     if (e == cudaSuccess)
@@ -640,8 +603,8 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&w.DinvT, sizeof(double) * w.np * kNB * kNB);
-    if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB);
-    if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB * kSuperPanels);
+    if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB * kSuperPanels);
     for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
         if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
     if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);

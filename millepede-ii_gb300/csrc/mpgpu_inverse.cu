@@ -31,10 +31,7 @@ using tc::kOpBytes;
 using tc::kTK;
 constexpr int64_t kTileEl = (int64_t)kNB * kNB;
 
-// C tile (cRow, cCol) = alpha sum_{k0 <= k < k1} A(aRow, k) B(bRow, k)^T + beta C
-struct TileTask {
-    int32_t aRow, bRow, k0, k1, cRow, cCol;
-};
+using tc::TileTask;
 
 // ------------------------------------------------------------ FP64 form
 // An operand tile (row, k) of a dense row-major FP64 matrix M, or of M^T
@@ -97,22 +94,19 @@ __global__ void __launch_bounds__(256) k_tile_gemm_fp64(Fp64Op A, Fp64Op B, doub
 }
 
 // ------------------------------------------------------------ tensor-core form
-// Tile-major TF32 operands: tile (r, c) of an array with nt tiles per row at
-// ((r * nt + c) << 14) floats, row-major inside the tile.
-struct TcOp {
-    const float *hi, *lo;
-    int64_t nt;
-};
+using tc::TcOp;
 
 // Tiles rows [r0, r1) x columns [c0, c1) of the dense FP64 matrix M (or
 // the tiles of M^T: tile (c, r) of the destination receives tile (r, c) of
-// M transposed) split into TF32 hi + lo.
+// M transposed) split into TF32 hi + lo; the destination's tile column is
+// the source's column less cOff (rows keep their index).
 __global__ void k_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r1, int32_t c0, int32_t c1,
-                              int32_t trans, float *hi, float *lo, int64_t ntDst) {
+                              int32_t trans, float *hi, float *lo, int64_t ntDst, int32_t cOff) {
     const int64_t nc = c1 - c0;
     const int32_t tr = r0 + (int32_t)(blockIdx.x / nc), tcc = c0 + (int32_t)(blockIdx.x % nc);
     if (tr >= r1) return;
-    const int64_t dst = trans ? ((int64_t)tcc * ntDst + tr) * kTileEl : ((int64_t)tr * ntDst + tcc) * kTileEl;
+    const int64_t dst = trans ? ((int64_t)tcc * ntDst + tr) * kTileEl
+                              : ((int64_t)tr * ntDst + (tcc - cOff)) * kTileEl;
     for (int e = threadIdx.x; e < kTileEl; e += blockDim.x) {
         // destination element (u, v) contiguous; source element (u, v) or (v, u)
         const int u = e / kNB, v = e % kNB;
@@ -133,15 +127,28 @@ __global__ void k_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r
 // hi*lo + lo*hi accumulated in one FP32 tensor-memory accumulator over all
 // chunks, then C = alpha acc + beta C in FP64 (coalesced through shared
 // memory).  Bounded mbarrier waits: a wait that runs out sets *err = -1
-// and the CTA finishes without writing C.
+// and the CTA finishes without writing C.  Without a task list the CTAs
+// take the lower triangle of tiles from tile (trail0, trail0) on, each
+// with K tiles [0, trailK) of rows i and j: the trailing update of a
+// block column.
 __global__ void __launch_bounds__(kTcThreads) k_tile_gemm_tc(TcOp A, TcOp B, double *C, int64_t ldc,
-                                                             const TileTask *tasks, double alpha, double beta,
-                                                             int32_t *err) {
+                                                             const TileTask *tasks, int32_t trail0, int32_t trailK,
+                                                             double alpha, double beta, int32_t *err) {
     extern __shared__ __align__(128) char tsm[];
     __shared__ uint64_t mbar[kStages];
     __shared__ uint32_t tbase;
     const int tid = threadIdx.x, wib = tid >> 5, ln = tid & 31;
-    const TileTask t = tasks[blockIdx.x];
+    TileTask t;
+    if (tasks) {
+        t = tasks[blockIdx.x];
+    } else {
+        const int64_t q = blockIdx.x;
+        int bi = (int)((sqrt(8.0 * (double)q + 1.0) - 1.0) * 0.5);
+        while ((int64_t)bi * (bi + 1) / 2 > q) bi--;
+        while ((int64_t)(bi + 1) * (bi + 2) / 2 <= q) bi++;
+        const int bj = (int)(q - (int64_t)bi * (bi + 1) / 2);
+        t = TileTask{trail0 + bi, trail0 + bj, 0, trailK, trail0 + bi, trail0 + bj};
+    }
     const int per = kNB / kTK;   // chunks per K tile
     const int nch = (t.k1 - t.k0) * per;
     if (nch <= 0) return;
@@ -336,7 +343,7 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
         MPG_CUDA(c, cudaFuncSetAttribute(k_tile_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
         // L^T tiles (p, k) for k > p: the panels of the original factor
         for (int32_t p = 0; p < np - 1; ++p)
-            k_split_tiles<<<np - 1 - p, 256, 0, s>>>(L, ld, p + 1, np, p, p + 1, 1, phi, plo, np);
+            k_split_tiles<<<np - 1 - p, 256, 0, s>>>(L, ld, p + 1, np, p, p + 1, 1, phi, plo, np, 0);
     }
     MPG_CUDA(c, cudaMemsetAsync(dErr, 0, sizeof(int32_t), s));
     // ---- trtri, panels from the last
@@ -345,11 +352,11 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
         if (m > 0) {
             if (mode == 1) {
                 k_tile_gemm_tc<<<m, kTcThreads, kTcSmem, s>>>(TcOp{xhi, xlo, np}, TcOp{phi, plo, np}, T, kNB,
-                                                              dTask + stepT[p], 1.0, 0.0, dErr);
-                k_split_tiles<<<m, 256, 0, s>>>(T, kNB, 0, m, 0, 1, 0, thi, tlo, 1);
-                k_split_tiles<<<1, 256, 0, s>>>(DinvT + (int64_t)p * kTileEl, kNB, 0, 1, 0, 1, 0, dhi, dlo, 1);
+                                                              dTask + stepT[p], 0, 0, 1.0, 0.0, dErr);
+                k_split_tiles<<<m, 256, 0, s>>>(T, kNB, 0, m, 0, 1, 0, thi, tlo, 1, 0);
+                k_split_tiles<<<1, 256, 0, s>>>(DinvT + (int64_t)p * kTileEl, kNB, 0, 1, 0, 1, 0, dhi, dlo, 1, 0);
                 k_tile_gemm_tc<<<m, kTcThreads, kTcSmem, s>>>(TcOp{thi, tlo, 1}, TcOp{dhi, dlo, 1}, L, ld,
-                                                              dTask + stepS[p], -1.0, 0.0, dErr);
+                                                              dTask + stepS[p], 0, 0, -1.0, 0.0, dErr);
             } else {
                 k_tile_gemm_fp64<<<4 * m, 256, 0, s>>>(Fp64Op{L, ld, 0}, Fp64Op{L, ld, 1}, T, kNB, dTask + stepT[p],
                                                        1.0, 0.0);
@@ -360,7 +367,7 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
         }
         k_set_diag_inverse<<<16, 256, 0, s>>>(L, ld, p, DinvT);
         // the finished column of X, split for the later steps' products
-        if (mode == 1) k_split_tiles<<<m + 1, 256, 0, s>>>(L, ld, p, np, p, p + 1, 0, xhi, xlo, np);
+        if (mode == 1) k_split_tiles<<<m + 1, 256, 0, s>>>(L, ld, p, np, p, p + 1, 0, xhi, xlo, np, 0);
         MPG_CUDA(c, cudaGetLastError());
     }
     // ---- lauum
@@ -368,9 +375,9 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
     if (mode == 1) {
         // X^T tiles (i, k) for k >= i (into the L^T area)
         for (int32_t i = 0; i < np; ++i)
-            k_split_tiles<<<np - i, 256, 0, s>>>(L, ld, i, np, i, i + 1, 1, phi, plo, np);
+            k_split_tiles<<<np - i, 256, 0, s>>>(L, ld, i, np, i, i + 1, 1, phi, plo, np, 0);
         k_tile_gemm_tc<<<(unsigned)nla, kTcThreads, kTcSmem, s>>>(TcOp{phi, plo, np}, TcOp{phi, plo, np}, Zd, ld,
-                                                                  dTask + lauum0, 1.0, 0.0, dErr);
+                                                                  dTask + lauum0, 0, 0, 1.0, 0.0, dErr);
     } else {
         k_tile_gemm_fp64<<<(unsigned)(4 * nla), 256, 0, s>>>(Fp64Op{L, ld, 1}, Fp64Op{L, ld, 1}, Zd, ld,
                                                              dTask + lauum0, 1.0, 0.0);
@@ -384,4 +391,22 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
     if (e != cudaSuccess) return cuda_err(c, e, "blocked inverse");
     if (h < 0) return set_err(c, MPGPU_ERR_TIMEOUT, "tensor-core tile product: barrier wait ran out");
     return MPGPU_OK;
+}
+
+// Launchers for the blocked Cholesky (mpgpu_dense.cu).
+cudaError_t tc_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r1, int32_t c0, int32_t c1, float *hi,
+                           float *lo, int64_t ntDst, int32_t cOff, cudaStream_t s) {
+    const int64_t n = (int64_t)(r1 - r0) * (c1 - c0);
+    if (n <= 0) return cudaSuccess;
+    k_split_tiles<<<(unsigned)n, 256, 0, s>>>(M, ld, r0, r1, c0, c1, 0, hi, lo, ntDst, cOff);
+    return cudaGetLastError();
+}
+
+cudaError_t tc_tile_gemm(const TcOp &A, const TcOp &B, double *C, int64_t ldc, const TileTask *tasks, int64_t ntask,
+                         int32_t trail0, int32_t trailK, double alpha, double beta, int32_t *err, cudaStream_t s) {
+    if (ntask <= 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_tile_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e != cudaSuccess) return e;
+    k_tile_gemm_tc<<<(unsigned)ntask, kTcThreads, kTcSmem, s>>>(A, B, C, ldc, tasks, trail0, trailK, alpha, beta, err);
+    return cudaGetLastError();
 }

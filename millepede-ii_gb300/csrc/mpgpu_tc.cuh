@@ -12,6 +12,18 @@ namespace tc {
 
 constexpr int kNB = 128;   // tile size (rows and columns of an accumulator)
 
+// C tile (cRow, cCol) = alpha sum_{k0 <= k < k1} A(aRow, k) B(bRow, k)^T + beta C
+struct TileTask {
+    int32_t aRow, bRow, k0, k1, cRow, cCol;
+};
+
+// Tile-major TF32 operands: tile (r, c) of an array with nt tiles per row at
+// ((r * nt + c) << 14) floats, row-major inside the tile.
+struct TcOp {
+    const float *hi, *lo;
+    int64_t nt;
+};
+
 // Operands stream in chunks of K = 16 through a 3-stage cp.async pipeline;
 // one thread issues the tcgen05.mma of a chunk (hi*hi, hi*lo, lo*hi for two
 // K = 8 steps) and commits them to the stage's mbarrier, which frees the
@@ -87,3 +99,10 @@ __device__ __forceinline__ void load_chunk_async(const float *g, int kc0, uint32
 
 
 }  // namespace tc
+
+// tile products and operand splits (mpgpu_inverse.cu)
+cudaError_t tc_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r1, int32_t c0, int32_t c1, float *hi,
+                           float *lo, int64_t ntDst, int32_t cOff, cudaStream_t s);
+cudaError_t tc_tile_gemm(const tc::TcOp &A, const tc::TcOp &B, double *C, int64_t ldc, const tc::TileTask *tasks,
+                         int64_t ntask, int32_t trail0, int32_t trailK, double alpha, double beta, int32_t *err,
+                         cudaStream_t s);

@@ -1,7 +1,8 @@
 """Dense blocked Cholesky through the C-ABI (mpgpu_dense_cholesky) against
 numpy on seeded SPD matrices: FP64 form within 1e-12 relative of numpy's
-factor; tensor-core 3xTF32 form within 2e-5 relative (its trailing updates
-are products of TF32 pairs accumulated in FP32)."""
+factor; tensor-core 3xTF32 form within 1e-4 relative (its trailing updates
+are products of TF32 pairs accumulated in FP32 over a block column of up to
+512 columns, then subtracted from the FP64 matrix)."""
 import numpy as np
 import pytest
 
@@ -16,7 +17,7 @@ def spd(n, seed, cond=1e4):
 
 
 @pytest.mark.parametrize("n", [128, 200, 640])
-@pytest.mark.parametrize("mode,tol", [(0, 1e-12), (1, 2e-5)])
+@pytest.mark.parametrize("mode,tol", [(0, 1e-12), (1, 1e-4)])
 def test_dense_cholesky(mp, n, mode, tol):
     A = spd(n, n)
     ref = np.linalg.cholesky(A)
