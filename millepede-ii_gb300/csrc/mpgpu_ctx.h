@@ -382,10 +382,19 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corr,
 // dense blocked Cholesky (mpgpu_dense.cu): mode 0 FP64, mode 1 tensor-core 3xTF32 trailing updates
 int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, float *hiBuf, float *loBuf,
                               int32_t *dErr, int32_t *badPanel);
+// constraint elimination inside the dense solve (device arrays): the
+// Householder vectors of the QL decomposition (V, Vk), the compact WY factor
+// T (ncon x ncon) and the constraint part y of the solution
+struct DenseWyElim {
+    int32_t ncon;
+    const double *V, *Vk, *T, *y;
+};
 // packed SPD solve refined by preconditioned CG in FP64 (b in, x out, device);
-// with invOut, also the inverse of Ap from the same factor (packed, n)
+// with invOut, also the inverse of Ap from the same factor (packed, n);
+// with wy, the constraints are eliminated inside (mpgpu_dense.cu)
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
-                        int32_t itnlim, mpgpu_solveinfo *info, double *invOut = nullptr);
+                        int32_t itnlim, mpgpu_solveinfo *info, double *invOut = nullptr,
+                        const DenseWyElim *wy = nullptr);
 // blocked inverse from the dense Cholesky factor (mpgpu_inverse.cu)
 int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, int mode, const double *DinvT,
                              double *Zd, double *Zp, int32_t *dErr);

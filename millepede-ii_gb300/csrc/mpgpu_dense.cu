@@ -587,18 +587,160 @@ void dotv(const DenseWork &w, const double *a, const double *b, double *out, cud
     k_dotf<<<1, 256, 0, s>>>(w.part, out);
 }
 
+// ---- constraint elimination in compact WY form (Q = H_1 ... H_m = I - U T U^T)
+constexpr int kWy = 128;      // padded number of constraints (columns of U)
+constexpr int kWyBlk = 152;   // fixed reduction shape of U^T x
+
+// U (npad x 128, row-major) and U^T (128 x npad) from the Householder
+// vectors: u_k = V_k on [0, kn_k), Vk_k at kn_k = npar - ncon + k, 0 beyond
+__global__ void k_build_u(const double *V, const double *Vk, int32_t npar, int32_t m, int64_t npad, double *U,
+                          double *UT) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < npad * kWy;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / kWy;
+        const int k = (int)(e % kWy);
+        double u = 0.0;
+        if (k < m && i < npar) {
+            const int64_t kn = npar - m + k;
+            u = i < kn ? V[(int64_t)k * npar + i] : (i == kn ? Vk[k] : 0.0);
+        }
+        U[e] = u;
+        UT[(int64_t)k * npad + i] = u;
+    }
+}
+
+// T padded to 128 x 128, and its transpose
+__global__ void k_pad_t(const double *T, int32_t m, double *T128, double *TT128) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < kWy * kWy; e += gridDim.x * blockDim.x) {
+        const int r = e / kWy, c = e % kWy;
+        const double t = (r < m && c < m) ? T[r * m + c] : 0.0;
+        T128[e] = t;
+        TT128[c * kWy + r] = t;
+    }
+}
+
+// C (128 x 128) = op(A) op(B) for 128 x 128 row-major A, B (op: transpose when t)
+__global__ void k_small_mm(const double *A, int ta, const double *B, int tb, double *C) {
+    const int r = blockIdx.x, cc = threadIdx.x;
+    double acc = 0.0;
+    for (int k = 0; k < kWy; ++k)
+        acc = fma(ta ? A[k * kWy + r] : A[r * kWy + k], tb ? B[cc * kWy + k] : B[k * kWy + cc], acc);
+    C[r * kWy + cc] = acc;
+}
+
+// M = U^T W (128 x 128): block a, thread b, rows in order
+__global__ void k_utw(int64_t npad, const double *U, const double *W, double *M) {
+    const int a = blockIdx.x, b = threadIdx.x;
+    double acc = 0.0;
+    for (int64_t i = 0; i < npad; ++i) acc = fma(U[i * kWy + a], W[i * kWy + b], acc);
+    M[a * kWy + b] = acc;
+}
+
+// Z = W T^T - 1/2 U S (TT = T^T), then ZU = [Z | U] and UZ = [U | Z] (npad x 256)
+__global__ void k_wy_z(int64_t npad, const double *W, const double *U, const double *TT, const double *S, double *ZU,
+                       double *UZ) {
+    const int a = threadIdx.x;
+    for (int64_t i = blockIdx.x; i < npad; i += gridDim.x) {
+        double z = 0.0, h = 0.0;
+        for (int b = 0; b < kWy; ++b) {
+            z = fma(W[i * kWy + b], TT[b * kWy + a], z);
+            h = fma(U[i * kWy + b], S[b * kWy + a], h);
+        }
+        z -= 0.5 * h;
+        const double u = U[i * kWy + a];
+        ZU[i * 2 * kWy + a] = z;
+        ZU[i * 2 * kWy + kWy + a] = u;
+        UZ[i * 2 * kWy + a] = u;
+        UZ[i * 2 * kWy + kWy + a] = z;
+    }
+}
+
+// the eliminated rows and columns of the factor's input set to the identity
+__global__ void k_identity_rows(double *L, int64_t ld, int64_t nfit, int64_t npad) {
+    for (int64_t i = nfit + blockIdx.x; i < npad; i += gridDim.x)
+        for (int64_t j = threadIdx.x; j <= i; j += blockDim.x) L[i * ld + j] = i == j ? 1.0 : 0.0;
+}
+
+__global__ void k_scale_diag(double *L, int64_t ld, int64_t n, double f) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) L[i * ld + i] *= f;
+}
+
+// partial sums of U^T x over fixed row ranges (block b: rows b, b + kWyBlk, ...)
+__global__ void k_ut_x(int64_t npad, const double *U, const double *x, double *part) {
+    const int k = threadIdx.x;
+    double acc = 0.0;
+    for (int64_t i = blockIdx.x; i < npad; i += kWyBlk) acc = fma(U[i * kWy + k], x[i], acc);
+    part[blockIdx.x * kWy + k] = acc;
+}
+
+// v = T t or T^T t, t = sum of the partials in block order
+__global__ void k_t_coef(const double *part, const double *T, int trans, double *v) {
+    __shared__ double t[kWy];
+    const int k = threadIdx.x;
+    double acc = 0.0;
+    for (int b = 0; b < kWyBlk; ++b) acc += part[b * kWy + k];
+    t[k] = acc;
+    __syncthreads();
+    double r = 0.0;
+    for (int c = 0; c < kWy; ++c) r = fma(trans ? T[c * kWy + k] : T[k * kWy + c], t[c], r);
+    v[k] = r;
+}
+
+// x -= U v
+__global__ void k_sub_uv(int64_t npad, const double *U, const double *v, double *x) {
+    __shared__ double sv[kWy];
+    if (threadIdx.x < kWy) sv[threadIdx.x] = v[threadIdx.x];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int k = 0; k < kWy; ++k) acc = fma(U[i * kWy + k], sv[k], acc);
+        x[i] -= acc;
+    }
+}
+
+// y = P b + (I - P) x, P keeping the first nfit components
+__global__ void k_reduce_op(int64_t npad, int64_t nfit, const double *b, const double *x, double *y) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = i < nfit ? b[i] : x[i];
+}
+
+// a = P x (first nfit components, zeros beyond), or with y: [x_fit; y] at nfit..
+__global__ void k_expand(int64_t npad, int64_t nfit, int64_t nfull, const double *x, const double *y, double *a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npad; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = i < nfit ? (x ? x[i] : 0.0) : ((y && i < nfull) ? y[i - nfit] : 0.0);
+}
+
+__global__ void k_sub_to(int64_t n, const double *a, const double *b, double *r) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = a[i] - b[i];
+}
+
 }  // namespace
 
 // Solve A x = b for the packed SPD matrix Ap (n, device) and the device
 // vector bx (b in, x out).  mode 0: FP64 factor, mode 1: tensor-core
 // factor; both refined by preconditioned CG in FP64 to rtol.
+// With wy (mode 1): Ap is the original packed matrix of all n = N
+// parameters and the ncon constraints are eliminated inside the solve.
+// With P = H_1 ... H_m = I - U T U^T (compact WY of the QL reflections; P A
+// P^T is what qlssq forms, P x what qlmlq calls Q^T x), the factor is that
+// of the reduced matrix P A P^T formed by tensor-core 3xTF32 products (A' =
+// A - Z U^T - U Z^T), a preconditioner only; CG runs in FP64 on the
+// operator x -> (P A P^T x) restricted to the nfit = N - ncon fit
+// parameters, with A the FP64 matrix and P applied in FP64.  bx: in the
+// vector g of all N parameters, out the full correction P^T [x; y] (y:
+// wy->y, the constraint part).  invOut: the inverse of the reduced matrix
+// from the factor, packed over the nfit fit parameters.
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
-                        int32_t itnlim, mpgpu_solveinfo *info, double *invOut) {
+                        int32_t itnlim, mpgpu_solveinfo *info, double *invOut, const DenseWyElim *wy) {
     cudaStream_t s = c->stream;
     DenseWork w;
     w.npad = ((int64_t)n + kNB - 1) / kNB * kNB;
     w.np = w.npad / kNB;
     const int64_t nn = w.npad * w.npad;
+    const int32_t m = wy ? wy->ncon : 0;
+    const int64_t nfit = n - m;
     int32_t rc = MPGPU_OK;
     cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
@@ -610,7 +752,51 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
     if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 16);
     if (e == cudaSuccess) e = cudaMalloc(&w.err, sizeof(int32_t));
+    // WY elimination: U, U^T, T, T^T, W, M, S, the split operands, scratch
+    struct WyBufs {
+        double *U = nullptr, *UT = nullptr, *T = nullptr, *TT = nullptr, *W = nullptr, *M = nullptr, *S = nullptr,
+               *X = nullptr, *ZU = nullptr, *UZ = nullptr, *a = nullptr, *part = nullptr, *v = nullptr;
+        float *zh = nullptr, *zl = nullptr, *uh = nullptr, *ul = nullptr;
+        ~WyBufs() {
+            for (double *p : {U, UT, T, TT, W, M, S, X, ZU, UZ, a, part, v}) cudaFree(p);
+            for (float *p : {zh, zl, uh, ul}) cudaFree(p);
+        }
+    } y;
+    if (wy) {
+        for (double **v : {&y.U, &y.UT, &y.W, &y.ZU, &y.UZ}) {
+            const int64_t len = (v == &y.ZU || v == &y.UZ) ? 2 * w.npad * kWy : w.npad * kWy;
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * len);
+        }
+        for (double **v : {&y.T, &y.TT, &y.M, &y.S, &y.X, &y.v})
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * kWy * kWy);
+        if (e == cudaSuccess) e = cudaMalloc(&y.a, sizeof(double) * w.npad);
+        if (e == cudaSuccess) e = cudaMalloc(&y.part, sizeof(double) * kWyBlk * kWy);
+        for (float **v : {&y.zh, &y.zl, &y.uh, &y.ul})
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(float) * w.npad * 2 * kWy);
+    }
     if (e != cudaSuccess) { w.release(); return cuda_err(c, e, "dense solve allocation"); }
+    const unsigned gv = (unsigned)std::min<int64_t>((w.npad + 7) / 8, 4096);
+    const unsigned ge = (unsigned)std::min<int64_t>((w.npad + 255) / 256, 4096);
+    // x -= U op(T) U^T x: with P = H_1 ... H_m = I - U T U^T, op = T gives
+    // P x (qlmlq's "Q^T x", reflections m..1) and op = T^T gives P^T x
+    auto qapply = [&](double *xv, bool transT) {
+        k_ut_x<<<kWyBlk, kWy, 0, s>>>(w.npad, y.U, xv, y.part);
+        k_t_coef<<<1, kWy, 0, s>>>(y.part, y.T, transT ? 1 : 0, y.v);
+        k_sub_uv<<<ge, 256, 0, s>>>(w.npad, y.U, y.v, xv);
+    };
+    // the CG operator: F x, or with wy the reduced matrix (P A P^T)_fit x
+    // on the first nfit components and the identity on the others
+    auto op = [&](const double *xin, double *out) {
+        if (!wy) {
+            k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, xin, out);
+            return;
+        }
+        k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, xin, nullptr, y.a);
+        qapply(y.a, true);
+        k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, y.a, out);
+        qapply(out, false);
+        k_reduce_op<<<ge, 256, 0, s>>>(w.npad, nfit, out, xin, out);
+    };
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -619,13 +805,74 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     k_packed_to_dense<<<4096, 256, 0, s>>>(Ap, n, w.npad, w.L, w.F);
     if (w.npad > n) k_pad_identity<<<(unsigned)((w.npad - n + 255) / 256), 256, 0, s>>>(w.F, w.npad, n, w.npad);
     cudaMemsetAsync(w.b, 0, sizeof(double) * w.npad, s);
-    cudaMemcpyAsync(w.b, bx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    if (!wy) {
+        cudaMemcpyAsync(w.b, bx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    } else {
+        // reduced right-hand side (P (g - A P^T [0; y]))_fit
+        const int64_t np_ = w.np;
+        k_build_u<<<2048, 256, 0, s>>>(wy->V, wy->Vk, n, m, w.npad, y.U, y.UT);
+        k_pad_t<<<64, 256, 0, s>>>(wy->T, m, y.T, y.TT);
+        k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, nullptr, wy->y, y.a);
+        qapply(y.a, true);
+        k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, y.a, w.q);
+        cudaMemcpyAsync(w.r, bx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+        if (w.npad > n) cudaMemsetAsync(w.r + n, 0, sizeof(double) * (w.npad - n), s);
+        k_sub_to<<<ge, 256, 0, s>>>(w.npad, w.r, w.q, w.r);
+        qapply(w.r, false);
+        k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, w.r, nullptr, w.b);
+        // Q^T A Q for the preconditioner: W = A U by tensor-core 3xTF32
+        // tile products (A split tile by tile into the factor's buffer area
+        // of F's size: the split of F lands in L, which is rebuilt below)
+        float *fh = reinterpret_cast<float *>(w.L), *fl = fh + nn;
+        MPG_CUDA(c, tc_split_tiles(w.F, w.npad, 0, (int32_t)np_, 0, (int32_t)np_, fh, fl, np_, 0, s));
+        MPG_CUDA(c, tc_split_tiles(y.UT, w.npad, 0, 1, 0, (int32_t)np_, y.uh, y.ul, np_, 0, s));
+        std::vector<tc::TileTask> tk(np_);
+        for (int64_t i = 0; i < np_; ++i) tk[i] = {(int32_t)i, 0, 0, (int32_t)np_, (int32_t)i, 0};
+        tc::TileTask *dt = nullptr;
+        MPG_CUDA(c, cudaMalloc(&dt, sizeof(tc::TileTask) * np_));
+        struct G { tc::TileTask *p; ~G() { cudaFree(p); } } gd{dt};
+        MPG_CUDA(c, cudaMemcpyAsync(dt, tk.data(), sizeof(tc::TileTask) * np_, cudaMemcpyHostToDevice, s));
+        MPG_CUDA(c, cudaMemsetAsync(w.err, 0, sizeof(int32_t), s));
+        MPG_CUDA(c, tc_tile_gemm(tc::TcOp{fh, fl, np_}, tc::TcOp{y.uh, y.ul, np_}, y.W, kWy, dt, np_, 0, 0, 1.0,
+                                 0.0, w.err, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));   // the task list and the split of A are released below
+        // M = U^T W, S = T M T^T, Z = W T^T - S U / 2 (FP64, m x m sized)
+        k_utw<<<kWy, kWy, 0, s>>>(w.npad, y.U, y.W, y.M);
+        k_small_mm<<<kWy, kWy, 0, s>>>(y.T, 0, y.M, 0, y.X);
+        k_small_mm<<<kWy, kWy, 0, s>>>(y.X, 0, y.T, 1, y.S);
+        k_wy_z<<<(unsigned)std::min<int64_t>(w.npad, 4096), kWy, 0, s>>>(w.npad, y.W, y.U, y.TT, y.S, y.ZU, y.UZ);
+        MPG_CUDA(c, tc_split_tiles(y.ZU, 2 * kWy, 0, (int32_t)np_, 0, 2, y.zh, y.zl, 2, 0, s));
+        MPG_CUDA(c, tc_split_tiles(y.UZ, 2 * kWy, 0, (int32_t)np_, 0, 2, y.uh, y.ul, 2, 0, s));
+        MPG_CUDA(c, cudaGetLastError());
+    }
+    // the matrix to factorise: A, or A' = A - Z U^T - U Z^T with the
+    // eliminated rows and columns replaced by the identity
+    auto prepare = [&](double sh) -> int32_t {
+        if (!wy) {
+            k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, sh);
+            return MPGPU_OK;
+        }
+        k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, 0.0);
+        const int64_t T = w.np;
+        MPG_CUDA(c, tc_tile_gemm(tc::TcOp{y.zh, y.zl, 2}, tc::TcOp{y.uh, y.ul, 2}, w.L, w.npad, nullptr,
+                                 T * (T + 1) / 2, 0, 2, -1.0, 1.0, w.err, s));
+        k_identity_rows<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(w.npad - nfit, 4096)), 256, 0, s>>>(
+            w.L, w.npad, nfit, w.npad);
+        if (sh != 0.0) k_scale_diag<<<(unsigned)((nfit + 255) / 256), 256, 0, s>>>(w.L, w.npad, nfit, 1.0 + sh);
+        // a tile product whose barrier wait ran out has flagged w.err
+        int32_t h = 0;
+        MPG_CUDA(c, cudaMemcpyAsync(&h, w.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+        MPG_CUDA(c, cudaStreamSynchronize(s));
+        if (h < 0) return set_err(c, MPGPU_ERR_TIMEOUT, "tensor-core tile product: barrier wait ran out");
+        return MPGPU_OK;
+    };
     // factorisation; a non-positive pivot of the low-precision factor is
     // cured by a growing diagonal shift (the CG iterations remove it)
     double shift = 0.0;
     int tries = 0;
     for (;; ++tries) {
-        k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, shift);
+        rc = prepare(shift);
+        if (rc != MPGPU_OK) break;
         int32_t bad = -1;
         rc = dense_cholesky_device(c, w.L, w.npad, mode, w.hi, w.lo, w.err, &bad);
         if (rc != MPGPU_ERR_FACTOR || tries >= 6) break;
@@ -640,8 +887,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
     // x0 = M^-1 b, r = b - A x0, z = M^-1 r, p = z
     precond(w, w.b, w.x, s);
-    const unsigned gv = (unsigned)std::min<int64_t>((w.npad + 7) / 8, 4096);
-    k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, w.x, w.q);
+    op(w.x, w.q);
     k_sub_vec<<<(unsigned)((w.npad + 255) / 256), 256, 0, s>>>(w.npad, w.b, w.q, w.r);
     precond(w, w.r, w.z, s);
     cudaMemcpyAsync(w.p, w.z, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
@@ -650,9 +896,8 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
     // one CG iteration as a CUDA graph (its ~600 launches replayed cheaply)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    const unsigned ge = (unsigned)std::min<int64_t>((w.npad + 255) / 256, 4096);
     MPG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    k_gemv<<<gv, 256, 0, s>>>(w.F, w.npad, w.npad, w.p, w.q);
+    op(w.p, w.q);
     dotv(w, w.p, w.q, w.sc + 1, s);
     dotv(w, w.p, w.p, w.sc + 6, s);
     k_cg_step<<<ge, 256, 0, s>>>(w.npad, w.x, w.r, w.p, w.q, w.sc);
@@ -683,13 +928,21 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         if (hs[3] <= tol2 * hs[4] && hs[5] <= xtol2 * hs[7]) { istop = 1; break; }
     }
     if (istop == 0) istop = 3;
-    cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    if (!wy) {
+        cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    } else {
+        // the full correction P^T [x; y]
+        k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, w.x, wy->y, y.a);
+        qapply(y.a, true);
+        cudaMemcpyAsync(bx, y.a, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
+    }
     // the inverse from the same factor (inversion forms): X = L^-1, Z = X^T X
     cudaEvent_t eR;
     cudaEventCreate(&eR);
     cudaEventRecord(eR, s);
     int32_t rcInv = MPGPU_OK;
-    if (invOut && istop != 9) rcInv = dense_inverse_device(c, w.L, w.npad, n, mode, w.DinvT, w.F, invOut, w.err);
+    if (invOut && istop != 9)
+        rcInv = dense_inverse_device(c, w.L, w.npad, nfit, mode, w.DinvT, w.F, invOut, w.err);
     cudaEventRecord(e1, s);
     MPG_CUDA(c, cudaStreamSynchronize(s));
     float ms = 0.0f, msF = 0.0f, msR = 0.0f;
@@ -712,7 +965,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         info->msInverse = ms - msR;
         info->itn = itn;
         info->istop = istop;
-        info->nrank = n;
+        info->nrank = (int32_t)nfit;
         info->evmin = shift;
         info->evmax = hs[4] > 0.0 ? std::sqrt(hs[3] / hs[4]) : 0.0;
         info->dxRel = hs[7] > 0.0 ? std::sqrt(hs[5] / hs[7]) : 0.0;

@@ -1224,9 +1224,13 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
             k_qlssq_update<<<S.wgrid(n), kThreads, 0, s>>>(n, j.matD, v, vkv, Av, scal, ilast, kn);
         }
     };
+    // tensor-core forms with up to 128 constraints: Q^T A Q is formed inside
+    // the dense solve for the preconditioner only (compact WY, 3xTF32) and
+    // the refinement applies Q in FP64; no FP64 sweep of the matrix here
+    const bool wyElim = dense == 1 && ncon >= 1 && ncon <= 128;
     std::vector<double> y(ncon > 0 ? ncon : 1, 0.0);
     if (ncon > 0) {
-        qlssq(1);
+        if (!wyElim) qlssq(1);
         // qlbsub (mpqldec.f90:991-1014) on the host
         for (int k = ncon; k >= 1; --k) {
             double d = 0.0;
@@ -1234,8 +1238,10 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
             y[k - 1] = ((consResiduals ? consResiduals[k - 1] : 0.0) - d) / j.hL[(size_t)(k - 1) * ncon + k - 1];
         }
         MPG_CUDA(c, cudaMemcpyAsync(yv, y.data(), sizeof(double) * ncon, cudaMemcpyHostToDevice, s));
-        S.qlmlq(corr, 1);
-        k_cons_rhs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, ncon, j.matD, yv, corr);
+        if (!wyElim) {
+            S.qlmlq(corr, 1);
+            k_cons_rhs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, ncon, j.matD, yv, corr);
+        }
     }
     int nrank = 0;
     if (!decomposition && dense < 0) {
@@ -1259,8 +1265,11 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
         // (inversion forms: the inverse from the same factor replaces the
         // leading block of the packed matrix, where sqminl leaves it)
         const double tol = rtol > 0.0 ? rtol : 1e-13;
-        const int32_t rcd = dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000, info,
-                                            decomposition ? nullptr : j.matD);
+        const DenseWyElim wye{ncon, j.qlV, j.qlVk, j.qlT, yv};
+        const int32_t rcd = wyElim ? dense_solve_pcg(c, n, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000,
+                                                     info, decomposition ? nullptr : j.matD, &wye)
+                                   : dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000,
+                                                     info, decomposition ? nullptr : j.matD);
         if (rcd != MPGPU_OK) {
             cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
             cudaFree(used); cudaFree(piv);
@@ -1286,7 +1295,7 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
         nrank = (int)st[2];
     }
     info->nrank = nrank;
-    if (ncon > 0) {
+    if (ncon > 0 && !wyElim) {   // (the WY form returns the full correction)
         MPG_CUDA(c, cudaMemcpyAsync(corr + nfit, yv, sizeof(double) * ncon, cudaMemcpyDeviceToDevice, s));
         S.qlmlq(corr, 0);
     }
