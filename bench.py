@@ -258,6 +258,33 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
     return out
 
 
+def whole_job_measure(mp, d, local, cpu_loop_rate, cpu_minres_ms):
+    """The 2M-record barrel as a whole job through mpgpu_pede_run: structure
+    passes on the device, mpbits-sparse storage, 18 constraints eliminated,
+    three solutions by MINRES with the diagonal preconditioner to a relative
+    residual of 1e-12, outlier down-weighting in the second and third data
+    loop (lhuber 2), chi2 cuts 30 then 6.  Wall time of the call; the CPU
+    estimate is three loops at the measured CPU loop rate plus the MINRES
+    iterations at the measured CPU time per iteration."""
+    jd = mp.JobData(d, metsol=4, matsto=2, mitera=3, lhuber=2, chicut=30.0, chirem=6.0, mrestl=1e-12,
+                    itnlim=6000, mreqenf=25, structDevice=1)
+    t0 = time.perf_counter()
+    rc = mp.run_job(jd)
+    wall = time.perf_counter() - t0
+    nrec = len(d["recPtr"]) - 1
+    out = {"records": nrec, "rc": int(rc), "wall_s": wall, "solutions": 3, "metsol": 4, "rtol": 1e-12,
+           "nrej_last": [int(v) for v in jd.res.nrej], "minres_iterations_last": int(jd.res.minresItn),
+           "minres_istop_last": int(jd.res.minresIstop), "ms_loop_last": jd.res.msBuild,
+           "ms_solve_last": jd.res.msSolve}
+    if cpu_loop_rate and cpu_minres_ms:
+        est = 3 * nrec / cpu_loop_rate + 3 * jd.res.minresItn * cpu_minres_ms * 1e-3
+        out["cpu_estimate_s"] = est
+        out["cpu_estimate"] = ("3 data loops at the oracle's measured loop rate + 3 x the last solve's MINRES "
+                               "iterations at the oracle's measured time per iteration (all host cores)")
+        out["speedup_vs_cpu_estimate"] = est / wall
+    return out
+
+
 def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
     """MINRES on the sparse barrel (30,000 tracks: 30,000 globals, 6.1M
     stored elements, 18 constraints eliminated by QL): device time per
@@ -313,6 +340,7 @@ def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
     itn, nrkd = C.c_int32(), C.c_int32()
     off = np.ascontiguousarray(H.offsets, np.int64)
     col = np.ascontiguousarray(H.columns, np.int32)
+    L.mpref_set_threads(C.c_int32(ncores))
     t0 = time.perf_counter()
     L.mpref_minres_precond(C.c_int32(0), C.c_int32(2), C.c_int32(H.nVar), C.c_int32(H.nG),
                            H.aig.ctypes.data_as(i32p), off.ctypes.data_as(i64p), col.ctypes.data_as(i32p),
@@ -320,8 +348,9 @@ def minres_measure(mp, local, iters=300, cpu_iters=20, ncores=1):
                            C.c_double(1e-30), C.c_int32(cpu_iters), C.c_int32(0), C.c_int32(0), C.byref(itn),
                            C.byref(nrkd))
     cpu_s = time.perf_counter() - t0
+    L.mpref_set_threads(C.c_int32(1))
     L.mpref_ql_destroy(C.c_void_p(q))
-    out["cpu_baseline"] = {"ms_per_iteration": cpu_s * 1e3 / max(itn.value, 1), "cores": 1, "kind": "port",
+    out["cpu_baseline"] = {"ms_per_iteration": cpu_s * 1e3 / max(itn.value, 1), "cores": ncores, "kind": "port",
                            "sample": f"{itn.value} iterations including the preconditioner set-up"}
     out["speedup_vs_cpu_diagonal"] = out["cpu_baseline"]["ms_per_iteration"] / out["ms_per_iteration_diagonal"]
     return out
@@ -389,6 +418,196 @@ def serve_measure(mp, local, njobs=24, rate=8.0, nmin=500, nmax=20000, rmin=10_0
 def sample_of(d, nsample):
     rp = d["recPtr"][:nsample + 1]
     return dict(recPtr=rp, inder=d["inder"][:rp[-1]], glder=d["glder"][:rp[-1]])
+
+
+SERVE_SPEC_STEER = dict(matsto=1, mitera=3, lhuber=2, chicut=30.0, chirem=6.0, mreqenf=5)
+
+
+def serve_spec_plan(njobs, rate=4.0, nmin=500, nmax=40000, rmin=10_000, rmax=1_000_000):
+    """Per job (model, globals drawn, records, constraints) and the Poisson
+    arrival times of the serving stream (seeded)."""
+    rng = np.random.default_rng(29)
+    specs = []
+    for k in range(njobs):
+        n = int(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        nrec = int(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
+        kind = "barrel" if rng.random() < 0.5 else "brokenlines"
+        specs.append((kind, n, nrec, int(rng.integers(6, 61))))
+    return specs, np.cumsum(rng.exponential(1.0 / rate, njobs))
+
+
+def serve_spec_job(mp, specs, k):
+    """Records and constraints of job k of the serving stream (seed 1000 + k):
+    the barrel with n/6 modules, helix or broken-line (4-28 hits) tracks,
+    the model's weak-mode constraints plus seeded sparse ones up to the
+    drawn count; returns (data, constraints, number of labels)."""
+    kind, n, nrec, ncon = specs[k]
+    cfg = mp.gen_config(kind, ntracks=nrec, seed=1000 + k)
+    cfg.nmod = max(n // 6, 1)
+    if kind == "brokenlines":
+        cfg.maxHits = 28
+    d = mp.generate(cfg)
+    crng = np.random.default_rng(5000 + k)
+    labels = np.unique(d["inder"][d["inder"] > 0])
+    cs, cl, cc = list(d["conStart"]), list(d["conLabel"]), list(d["conCoef"])
+    for _ in range(max(0, ncon - d["ncon"])):
+        pick = crng.choice(labels, min(64, len(labels)), replace=False)
+        c = crng.normal(size=len(pick))
+        cl += [int(x) for x in pick]
+        cc += [float(x) for x in c - c.mean()]
+        cs.append(len(cl))
+    return d, (np.array(cs, np.int32), np.array(cl, np.int32), np.array(cc)), len(labels)
+
+
+def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmin=10_000, rmax=1_000_000,
+                       fp64="all", budget_gb=150, gen_threads=6, lookahead=12):
+    """The stream of alignment jobs at its specified shape: njobs jobs with
+    Poisson arrivals at `rate` per second, each generated from its own seed
+    (1000 + job) with the barrel detector model, as helix tracks (12 hits,
+    nloc 5) or broken lines (4-28 hits, nloc 12-60), globals log-uniform in
+    [nmin, nmax] (the barrel's smallest layout has 1,728), records
+    log-uniform in [rmin, rmax], 6-60 linear constraints (the 18 weak-mode
+    constraints of the barrel plus seeded sparse ones), 3 iterations with
+    outlier down-weighting, dense tensor-core Cholesky + FP64 refinement
+    (every size is at most 40,000), admitted by device footprint against
+    budget_gb, 4 jobs active.  Jobs are generated by a host thread pool
+    ahead of their arrival (at most `lookahead` in memory).  The same jobs
+    then run one at a time with the FP64 blocked solve (fp64 "all", or
+    "every8" for every 8th job), whose latencies under the same arrivals are
+    those of a first-come-first-served queue over the measured service
+    times."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+    specs, arrivals = serve_spec_plan(njobs, rate, nmin, nmax, rmin, rmax)
+    steer = SERVE_SPEC_STEER
+
+    def make(k):
+        return serve_spec_job(mp, specs, k)
+
+    errors = []
+
+    def phases(jd):
+        r = jd.res
+        return dict(structure_ms=r.msStructure, upload_ms=r.msUpload, loops_ms=r.msLoops, solves_ms=r.msSolves,
+                    host_iter_ms=r.msHostIter, job_ms=r.msJob, nrej=int(sum(r.nrej)))
+
+    def stream(metsol, serve):
+        """(per-job records, span): served concurrently at the arrival times,
+        or one at a time back to back (service times)."""
+        out = [None] * njobs
+        pool = ThreadPoolExecutor(gen_threads)
+        fut = {}
+        nxt = 0
+
+        def ahead(upto):
+            nonlocal nxt
+            while nxt < min(upto, njobs):
+                fut[nxt] = pool.submit(make, nxt)
+                nxt += 1
+        ahead(lookahead)
+        keep = set(range(0, njobs, 8)) if fp64 == "every8" else set(range(njobs))
+        if serve:
+            srv = mp.Server(device=local, max_active=4, budget_bytes=budget_gb << 30)
+            tickets = []
+            done = threading.Event()
+
+            def waiter():
+                for k in range(njobs):
+                    while len(tickets) <= k:
+                        time.sleep(0.005)
+                    t, jd, lag, nglob = tickets[k]
+                    rc, lat, q, b = srv.wait(t, timeout_ms=3.6e6)
+                    out[k] = dict(rc=int(rc), lat_ms=lat, queue_ms=q, bytes=int(b), lag_ms=lag, n=int(jd.res.nVar),
+                                  globals=nglob, nrec=int(jd.job.nrec), ncon=int(jd.job.ncon),
+                                  cg_last=int(jd.res.minresItn), **phases(jd),
+                                  par=jd.parameters()[1] if k in keep else None)
+                    tickets[k] = None   # the job's host arrays go
+                    del jd
+                done.set()
+            wt = threading.Thread(target=waiter)
+            wt.start()
+            t0 = time.perf_counter()
+            for k in range(njobs):
+                d, con, nglob = fut.pop(k).result()
+                ahead(k + 1 + lookahead)
+                jd = mp.JobData(d, constraints=con, metsol=metsol, **steer)
+                del d
+                now = time.perf_counter() - t0
+                if arrivals[k] > now:
+                    time.sleep(arrivals[k] - now)
+                lag = max(0.0, (time.perf_counter() - t0) - arrivals[k]) * 1e3
+                tickets.append((srv.submit(jd), jd, lag, nglob))
+            done.wait()
+            span = time.perf_counter() - t0
+            wt.join()
+            errors.append(srv.last_error())
+            srv.close()
+        else:
+            span = 0.0
+            for k in range(njobs):
+                d, con, nglob = fut.pop(k).result()
+                ahead(k + 1 + lookahead)
+                if k not in keep:
+                    continue
+                jd = mp.JobData(d, constraints=con, metsol=metsol, **steer)
+                del d
+                ctx = mp.Context(device=local)
+                t1 = time.perf_counter()
+                rc = mp.run_job(jd, ctx)
+                ms = (time.perf_counter() - t1) * 1e3
+                ctx.close()
+                span += ms * 1e-3
+                out[k] = dict(rc=int(rc), service_ms=ms, n=int(jd.res.nVar), cg_last=int(jd.res.minresItn),
+                              **phases(jd), par=jd.parameters()[1])
+                if rc:
+                    out[k]["error"] = ctx.last_error()
+        pool.shutdown()
+        return out, span
+
+    served, span = stream(31, True)
+    lat = np.array([o["lat_ms"] for o in served])
+    ok = [o["rc"] == 0 for o in served]
+    res = {"jobs": njobs, "arrival_rate_per_s": rate, "globals_drawn": [nmin, nmax],
+           "globals_actual": [min(o["n"] for o in served), max(o["n"] for o in served)],
+           "records": [min(o["nrec"] for o in served), max(o["nrec"] for o in served)],
+           "models": {m: sum(1 for s in specs if s[0] == m) for m in ("barrel", "brokenlines")},
+           "constraints": [min(o["ncon"] for o in served), max(o["ncon"] for o in served)],
+           "iterations": 3, "budget_gb": budget_gb, "max_active": 4, "solve": "metsol 31 (tensor-core factor, "
+           "FP64 CG refinement, factor kept across the job's iterations)",
+           "served_mixed": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                            "jobs_per_s": njobs / span, "span_s": span, "ok": all(ok),
+                            "rc": sorted(set(o["rc"] for o in served)),
+                            "queue_p50_ms": float(np.percentile([o["queue_ms"] for o in served], 50)),
+                            "arrival_lag_max_ms": max(o["lag_ms"] for o in served),
+                            "last_error": errors[0] if errors else ""}}
+    res["per_job"] = [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in o.items() if k != "par"}
+                      for o in served]
+    if fp64:
+        plain, busy = stream(32, False)
+        idx = [k for k in range(njobs) if plain[k] is not None]
+        svc = np.array([plain[k]["service_ms"] for k in idx])
+        entry = {"jobs": len(idx), "service_p50_ms": float(np.percentile(svc, 50)),
+                 "service_p99_ms": float(np.percentile(svc, 99)), "busy_s": busy,
+                 "ok": all(plain[k]["rc"] == 0 for k in idx)}
+        if len(idx) == njobs:
+            # first-come-first-served single server over the measured service
+            # times at the same arrival times
+            fin, lq = 0.0, []
+            for k in range(njobs):
+                start = max(arrivals[k] * 1e3, fin)
+                fin = start + svc[k]
+                lq.append(fin - arrivals[k] * 1e3)
+            entry.update({"p50_ms": float(np.percentile(lq, 50)), "p99_ms": float(np.percentile(lq, 99)),
+                          "jobs_per_s": njobs / (max(fin * 1e-3, arrivals[-1]))})
+        res["one_at_a_time_fp64"] = entry
+        diffs = [float(np.max(np.abs(served[k]["par"] - plain[k]["par"])) /
+                       max(float(np.max(np.abs(plain[k]["par"]))), 1e-300))
+                 for k in idx if served[k]["rc"] == 0 and plain[k]["rc"] == 0]
+        res["max_rel_diff_parameters_iterated"] = max(diffs) if diffs else None
+        res["median_rel_diff_parameters_iterated"] = float(np.median(diffs)) if diffs else None
+        for k in idx:
+            res["per_job"][k]["fp64_service_ms"] = round(plain[k]["service_ms"], 3)
+    return res
 
 
 def cpu_reference(d, nsample, nthreads, steps=1, keep=False):
@@ -564,6 +783,11 @@ def main():
     ap.add_argument("--dense-cond", type=float, default=0.0,
                     help="dense measurement on the input with condition number about this (0: as generated)")
     ap.add_argument("--dense-only", action="store_true", help="only the dense measurement (with --dense-n)")
+    ap.add_argument("--serve-spec", type=int, default=0,
+                    help="only the serving stream at its specified shape with this many jobs (256)")
+    ap.add_argument("--serve-fp64", default="all", choices=["all", "every8", ""],
+                    help="--serve-spec: the one-at-a-time FP64 comparison over all jobs, every 8th, or none")
+    ap.add_argument("--whole-job", type=int, default=1, help="time the barrel as a whole job (0: skip)")
     ap.add_argument("--minres-iters", type=int, default=300, help="iterations of the MINRES measurement (0: skip)")
     ap.add_argument("--mbandw", type=int, default=0, help="--part minres: preconditioner (0 diagonal, > 0 band width)")
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
@@ -576,6 +800,10 @@ def main():
     mp = _load_pkg()
     if args.profile and args.part != "loop":
         profile_part(mp, args.part, args.ntracks, local, args.steps, args.mbandw)
+        return
+    if args.serve_spec:
+        if rank == 0:
+            print(json.dumps(serve_spec_measure(mp, local, njobs=args.serve_spec, fp64=args.serve_fp64)))
         return
     if args.dense_only:
         if rank == 0:
@@ -722,7 +950,11 @@ def main():
     if args.serve_jobs > 0 and rank == 0 and not args.profile:
         line["serving"] = serve_measure(mp, local, njobs=args.serve_jobs)
     if args.minres_iters > 0 and rank == 0 and not args.profile:
-        line["minres"] = minres_measure(mp, local, iters=args.minres_iters)
+        line["minres"] = minres_measure(mp, local, iters=args.minres_iters, ncores=ncores)
+        if args.whole_job:
+            cpu_rate = line.get("cpu_baseline", {}).get("value")
+            line["whole_job"] = whole_job_measure(mp, d, local, cpu_rate,
+                                                  line["minres"]["cpu_baseline"]["ms_per_iteration"])
     if args.dense_n > 0 and rank == 0 and not args.profile:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n, sqminl=args.dense_sqminl,

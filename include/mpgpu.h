@@ -83,6 +83,9 @@ typedef struct mpgpu_ctx mpgpu_ctx;
 #define MPGPU_FLAG_ONE_RECORD_PER_BLOCK 4
 /* no timing of warps-per-CTA candidates on the first data loop */
 #define MPGPU_FLAG_NO_AUTOTUNE 8
+/* the tensor-core dense solve (metsol 31) factorises at every solve instead
+ * of first preconditioning with the factor of the job's previous solve */
+#define MPGPU_FLAG_FRESH_FACTOR 16
 
 typedef struct mpgpu_cfg {
     int32_t device;             /* CUDA device ordinal */
@@ -94,6 +97,12 @@ int32_t mpgpu_create(mpgpu_ctx **ctx, const mpgpu_cfg *cfg);
 int32_t mpgpu_destroy(mpgpu_ctx *ctx);
 /* last error message of the context (static storage inside ctx) */
 const char *mpgpu_last_error(const mpgpu_ctx *ctx);
+
+/* Frees the device memory of the context's current job (records, layout,
+ * global matrix, constraints, dense-solve workspace with its kept factor);
+ * the context stays usable for the next job.  No reference counterpart:
+ * pede runs one job per process. */
+int32_t mpgpu_release(mpgpu_ctx *ctx);
 
 /* Global-parameter layout.  varIndexOfTotal[nTotal]: variable index (1..nVar)
  * of each total parameter index, <=0 for fixed (globalParLabelIndex(2,:)).
@@ -271,6 +280,9 @@ typedef struct mpgpu_solveinfo {
                            solution (|alpha p| / |x|) */
     double msInverse;   /* blocked inversions (metsol 11, 12): device time of the inverse
                            from the factor */
+    int32_t factorReused;  /* metsol 31: 1 the previous solve's factor preconditioned this
+                              one, 2 it was tried and dropped, 0 not tried */
+    int32_t itnReuse;      /* CG iterations spent on a dropped factor (included in itn) */
 } mpgpu_solveinfo;
 
 /* Global solve (metsol 1 inversion, 3 decomposition = Cholesky, 4 MINRES,
@@ -295,7 +307,11 @@ typedef struct mpgpu_solveinfo {
  * that factors of either precision reach the same FP64 solution
  * (info->itn iterations, info->istop 1 converged / 3 limit, info->evmin the
  * diagonal shift the low-precision factor needed, info->evmax the final
- * relative residual, info->dxRel the last relative correction).
+ * relative residual, info->dxRel the last relative correction).  metsol 31
+ * keeps its factor in the context: the next solve of a matrix of the same
+ * sizes (the job's next outlier iteration) is first preconditioned with it
+ * and factorises only when CG has not converged within 40 iterations
+ * (info->factorReused; MPGPU_FLAG_FRESH_FACTOR turns this off).
  * consResiduals[ncon] = d - C p (addcst); correction[nVar] receives the
  * step; errors[nVar] (metsol 1, may be NULL) the diagonal of the covariance
  * (sqrt gives the parameter errors).  rtol/itnlim: MINRES(-QLP) tolerance and
@@ -410,6 +426,12 @@ typedef struct mpgpu_result {
     double *start;
     double *gcor;
     int64_t *fileCounts;
+    /* where the job's time went (mpgpu_pede_run): host wall of the
+     * structure passes (labels, translation, sparse structure), host wall of
+     * the record upload, device time of all data loops and of all solves,
+     * wall of the host work between them (constraint residuals, feasib,
+     * measurement lines), wall of the whole job */
+    double msStructure, msUpload, msLoops, msSolves, msHostIter, msJob;
 } mpgpu_result;
 
 /* loop1 equivalent: label table (sorted), entries per label, parameter
@@ -519,6 +541,9 @@ int32_t mpgpu_server_submit(mpgpu_server *srv, const mpgpu_steer *st, const mpgp
  * wait for a worker and its admitted device footprint. */
 int32_t mpgpu_server_wait(mpgpu_server *srv, int64_t ticket, double timeoutMs, double *msLatency,
                           double *msQueue, int64_t *bytes);
+/* Message of the last job that ended with an error ("ticket N: ...";
+ * empty when none has); valid until the next call on the server. */
+const char *mpgpu_server_last_error(mpgpu_server *srv);
 /* Runs the queued jobs to the end, then releases the workers. */
 int32_t mpgpu_server_destroy(mpgpu_server *srv);
 

@@ -5,6 +5,7 @@
 // in pede itself; this C++ version drives the C-ABI for tests, the
 // benchmark and the pede_gpu command.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -401,6 +402,12 @@ void feasib(const mpgpu_job *job, const std::vector<int32_t> &lab, const int32_t
 int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job, mpgpu_result *res,
                           const std::function<bool(int64_t)> &admit) {
     if (!st || !job || !res) return MPGPU_ERR_ARG;
+    using Clock = std::chrono::steady_clock;
+    const auto msSince = [](Clock::time_point a) {
+        return std::chrono::duration<double, std::milli>(Clock::now() - a).count();
+    };
+    const Clock::time_point tJob = Clock::now();
+    res->msStructure = res->msUpload = res->msLoops = res->msSolves = res->msHostIter = res->msJob = 0.0;
     mpgpu_ctx *ctx = ctxIn;
     if (!ctx) {
         mpgpu_cfg cfg{0, 0, 0};
@@ -476,6 +483,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             capc = onDevice ? std::max<int64_t>(ncolw, 1) : capc * 4;
         }
     }
+    res->msStructure = msSince(tJob);
     if (admit) {
         // device footprint: records and their tables, update staging
         // (bounded by the squared words per record), matrix, dense solve
@@ -486,7 +494,9 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         }
         const int64_t nm = st->matsto == 2 ? nmat : (int64_t)nVar * (nVar + 1) / 2;
         const int64_t npad = ((int64_t)nVar + 127) / 128 * 128;
-        const int64_t dense = (st->metsol == 31 || st->metsol == 32) ? 2 * npad * npad : 0;
+        // dense forms: F and L (npad^2 each), the split panels and the WY
+        // buffers of the constraint elimination (about 3 KB per row)
+        const int64_t dense = (st->metsol == 31 || st->metsol == 32) ? 2 * npad * npad + 3072 * npad : 0;
         const int64_t stageCap = (int64_t)2 << 30;   // 2 x 8 GiB staging buffers at most (in doubles)
         const int64_t bytes = 40 * nw + 8 * (std::min(stage, stageCap) + nm + dense) + 64 * (int64_t)nVar +
                               ((int64_t)64 << 20);
@@ -511,9 +521,11 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             }
         rc = mpgpu_set_constraints(ctx, ncon, A.data());
     }
+    const Clock::time_point tUp = Clock::now();
     if (!rc)
         rc = mpgpu_upload_records(ctx, job->nrec, job->recPtr, onDevice ? nullptr : tinder.data(),
                                   onDevice ? nullptr : job->glder, job->recFile, job->nfiles, job->fileWeight);
+    res->msUpload = msSince(tUp);
     const int32_t nfit = nVar - ncon;
     res->nFit = nfit;
     std::vector<double> gpar(ntot, 0.0), psig(ntot, 0.0);
@@ -602,6 +614,8 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     std::memset(res->nrej, 0, sizeof(res->nrej));
     res->msBuild = res->msSolve = 0.0;
     if (!rc && (st->metsol == 4 || st->metsol == 5)) rc = mpgpu_set_preconditioner(ctx, st->mbandw, st->lprecm);
+    const Clock::time_point tIter = Clock::now();
+    double msLoopWall = 0.0, msSolveWall = 0.0;
     for (int32_t iter = 1; !rc && iter <= st->mitera; ++iter) {
         const int32_t nloopn = iter;
         if (nloopn > 1) {
@@ -614,8 +628,12 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         }
         mpgpu_fitopts fo{1, nloopn, st->lhuber, st->lfitbb, chicut, st->chhuge, st->dwcut, st->cndlmx};
         mpgpu_fitstats fs;
+        const Clock::time_point tL = Clock::now();
         rc = mpgpu_loopbf(ctx, &fo, gpar.data(), nullptr, nullptr, &fs, nullptr, nullptr, nullptr);
+        msLoopWall += msSince(tL);
         if (rc) break;
+        res->msBuild = fs.msLoop;
+        res->msLoops += fs.msLoop;
         if (monitor) {
             rc = mpgpu_get_monitor(ctx, monHist.data(), monMeas.data());
             monLoop = nloopn;
@@ -686,10 +704,13 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             rc = mpgpu_matrix_diagonal(ctx, diag0.data());
             if (rc) break;
         }
+        const Clock::time_point tS = Clock::now();
         rc = mpgpu_solve(ctx, st->metsol, cres.data(), st->mrestl, st->itnlim, corr.data(),
                          wantErr ? err.data() : nullptr, &si);
+        msSolveWall += msSince(tS);
         if (rc) break;
         res->msSolve = si.ms;
+        res->msSolves += si.ms;
         res->nrank = si.nrank;
         res->minresItn = si.itn;
         res->minresIstop = si.istop;
@@ -702,6 +723,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         // the corrected parameters made feasible (cut 1e-6, pede.f90:8865-8866)
         if (!rc && ncon > 0) feasib(job, lab, res->varIndex, cfac, gpar, 1.0e-6f);
     }
+    res->msHostIter = msSince(tIter) - msLoopWall - msSolveWall;
     if (!rc && monitor && st->monitor > 0 && (st->monitor & 2) && monLoop > 0) rc = writeMon(monLoop);
     for (int32_t i = 0; i < ntot; ++i) {
         res->parameter[i] = gpar[i];
@@ -730,6 +752,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     }
     res->exitCode = rc;
     if (!ctxIn) mpgpu_destroy(ctx);
+    res->msJob = msSince(tJob);
     return rc;
 }
 

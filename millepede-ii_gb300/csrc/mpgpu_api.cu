@@ -115,6 +115,7 @@ extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
     if (!c) return MPGPU_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    dense_release(c);
     free_records(c->j);
     free_layout(c->j);
     free_constraints(c->j);
@@ -128,6 +129,23 @@ extern "C" int32_t mpgpu_destroy(mpgpu_ctx *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     delete c;
+    return MPGPU_OK;
+}
+
+// the device memory of the current job (records, layout, matrix,
+// constraints, resident structure, dense workspace); streams and the
+// static areas stay, so the context takes the next job as a fresh one
+extern "C" int32_t mpgpu_release(mpgpu_ctx *c) {
+    if (!c) return MPGPU_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->stream2) cudaStreamSynchronize(c->stream2);
+    dense_release(c);
+    free_records(c->j);
+    free_layout(c->j);
+    free_constraints(c->j);
+    free_resident(c->res);
+    c->j.nVar = 0;
     return MPGPU_OK;
 }
 
@@ -147,6 +165,7 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
     if (allIndexGroups[nGroups] != nVar + 1) return set_err(c, MPGPU_ERR_SIZE, "groups do not end at nVar+1");
     cudaSetDevice(c->device);
     DevJob &j = c->j;
+    dense_release(c);
     free_layout(j);
     free_records(j);
     j.nTotal = nTotal; j.nVar = nVar; j.nG = nGroups; j.matsto = matsto;
@@ -241,6 +260,7 @@ extern "C" int32_t mpgpu_set_constraints(mpgpu_ctx *c, int32_t ncon, const doubl
     if (!c) return MPGPU_ERR_ARG;
     DevJob &j = c->j;
     if (j.nVar <= 0) return set_err(c, MPGPU_ERR_ARG, "set the layout before the constraints");
+    dense_invalidate(c);
     free_constraints(j);
     if (ncon <= 0) return MPGPU_OK;
     if (ncon >= j.nVar) return set_err(c, MPGPU_ERR_SIZE, "more constraints than parameters");

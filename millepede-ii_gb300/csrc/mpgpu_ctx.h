@@ -183,6 +183,7 @@ struct Monitor {
     unsigned long long *meas = nullptr;  // device [numMeas * measBins]
 };
 
+struct DenseResident;   // workspace of the refined dense solves (mpgpu_dense.cu)
 struct mpgpu_ctx {
     int device = 0;
     int32_t flags = 0;                 // mpgpu_cfg.flags
@@ -198,6 +199,7 @@ struct mpgpu_ctx {
     int64_t lastNaccepted = 0;
     int32_t mbandw = 0;          // MINRES preconditioner: < 0 none, 0 diagonal, > 0 band width
     int32_t lprecm = 0;          // lltdec option of the band preconditioner
+    DenseResident *dense = nullptr;  // kept between the dense solves of a job
 };
 
 // variable-band preconditioner of MINRES (mpgpu_precond.cu): band of
@@ -395,6 +397,10 @@ struct DenseWyElim {
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
                         int32_t itnlim, mpgpu_solveinfo *info, double *invOut = nullptr,
                         const DenseWyElim *wy = nullptr);
+// frees the dense-solve workspace (and with it the kept factor)
+void dense_release(mpgpu_ctx *c);
+// the kept factor no longer belongs to the job's matrix (new constraints)
+void dense_invalidate(mpgpu_ctx *c);
 // blocked inverse from the dense Cholesky factor (mpgpu_inverse.cu)
 int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, int mode, const double *DinvT,
                              double *Zd, double *Zp, int32_t *dErr);

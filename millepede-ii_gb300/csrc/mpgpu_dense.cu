@@ -366,8 +366,9 @@ constexpr int kDotBlk = 304;   // fixed reduction shape: deterministic sums
 // fraction of the solution (in addition to the residual test)
 constexpr double kRefineXtol = 1e-13;
 
-// packed lower triangle (n) -> dense lower (factor) and dense full (for the
-// matrix-vector products), both npad x npad row-major; scaled diagonal
+// packed lower triangle (n) -> dense lower (factor; not written when Lo is
+// null) and dense full (for the matrix-vector products), both npad x npad
+// row-major
 __global__ void k_packed_to_dense(const double *Ap, int64_t n, int64_t npad, double *Lo, double *F) {
     const int64_t nn = n * (n + 1) / 2;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nn; e += (int64_t)gridDim.x * blockDim.x) {
@@ -376,7 +377,7 @@ __global__ void k_packed_to_dense(const double *Ap, int64_t n, int64_t npad, dou
         while ((i + 1) * (i + 2) / 2 <= e) i++;
         const int64_t j = e - i * (i + 1) / 2;
         const double v = Ap[e];
-        Lo[i * npad + j] = v;
+        if (Lo) Lo[i * npad + j] = v;
         F[i * npad + j] = v;
         F[j * npad + i] = v;
     }
@@ -716,6 +717,101 @@ __global__ void k_sub_to(int64_t n, const double *a, const double *b, double *r)
         r[i] = a[i] - b[i];
 }
 
+// WY buffers of the constraint elimination: U, U^T, T, T^T, W, M, S, the
+// split operands, scratch
+struct WyBufs {
+    double *U = nullptr, *UT = nullptr, *T = nullptr, *TT = nullptr, *W = nullptr, *M = nullptr, *S = nullptr,
+           *X = nullptr, *ZU = nullptr, *UZ = nullptr, *a = nullptr, *part = nullptr, *v = nullptr;
+    float *zh = nullptr, *zl = nullptr, *uh = nullptr, *ul = nullptr;
+    void release() {
+        for (double *p : {U, UT, T, TT, W, M, S, X, ZU, UZ, a, part, v}) cudaFree(p);
+        for (float *p : {zh, zl, uh, ul}) cudaFree(p);
+        *this = WyBufs();
+    }
+};
+
+// CG iterations a solve spends on the previous solve's factor before it
+// factorises its own matrix
+constexpr int kReuseItn = 40;
+
+}  // namespace
+
+// Workspace of the refined dense solve, kept in the context between the
+// solves of a job: F (full FP64 matrix), L (the factor; also the split area
+// of the WY products), the inverted diagonal blocks, the CG vectors and the
+// WY buffers.  factorValid: L and DinvT hold the factor of an earlier solve
+// with these sizes (cleared by a new layout or constraint set).
+struct DenseResident {
+    DenseWork w;
+    WyBufs y;
+    bool haveWy = false;
+    bool factorValid = false;
+    int factorMode = -1;
+    int32_t factorN = 0, factorM = 0;
+    double factorShift = 0.0;
+};
+
+void dense_release(mpgpu_ctx *c) {
+    if (!c->dense) return;
+    cudaStreamSynchronize(c->stream);
+    c->dense->w.release();
+    c->dense->y.release();
+    delete c->dense;
+    c->dense = nullptr;
+}
+
+void dense_invalidate(mpgpu_ctx *c) {
+    if (c->dense) c->dense->factorValid = false;
+}
+
+namespace {
+// the context's workspace for npad rows (with the WY buffers when wy),
+// reallocated when the sizes differ
+int32_t dense_workspace(mpgpu_ctx *c, int64_t npad, bool wy, DenseResident *&out) {
+    if (c->dense && c->dense->w.npad == npad && (c->dense->haveWy || !wy)) {
+        out = c->dense;
+        return MPGPU_OK;
+    }
+    dense_release(c);
+    DenseResident *D = new DenseResident();
+    DenseWork &w = D->w;
+    WyBufs &y = D->y;
+    w.npad = npad;
+    w.np = npad / kNB;
+    const int64_t nn = npad * npad;
+    cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
+    if (e == cudaSuccess) e = cudaMalloc(&w.DinvT, sizeof(double) * w.np * kNB * kNB);
+    if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB * kSuperPanels);
+    if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB * kSuperPanels);
+    for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
+        if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
+    if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
+    if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&w.err, sizeof(int32_t));
+    if (wy) {
+        for (double **v : {&y.U, &y.UT, &y.W, &y.ZU, &y.UZ}) {
+            const int64_t len = (v == &y.ZU || v == &y.UZ) ? 2 * w.npad * kWy : w.npad * kWy;
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * len);
+        }
+        for (double **v : {&y.T, &y.TT, &y.M, &y.S, &y.X, &y.v})
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * kWy * kWy);
+        if (e == cudaSuccess) e = cudaMalloc(&y.a, sizeof(double) * w.npad);
+        if (e == cudaSuccess) e = cudaMalloc(&y.part, sizeof(double) * kWyBlk * kWy);
+        for (float **v : {&y.zh, &y.zl, &y.uh, &y.ul})
+            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(float) * w.npad * 2 * kWy);
+    }
+    D->haveWy = wy;
+    if (e != cudaSuccess) {
+        w.release();
+        y.release();
+        delete D;
+        return cuda_err(c, e, "dense solve allocation");
+    }
+    c->dense = D;
+    out = D;
+    return MPGPU_OK;
+}
 }  // namespace
 
 // Solve A x = b for the packed SPD matrix Ap (n, device) and the device
@@ -732,49 +828,26 @@ __global__ void k_sub_to(int64_t n, const double *a, const double *b, double *r)
 // vector g of all N parameters, out the full correction P^T [x; y] (y:
 // wy->y, the constraint part).  invOut: the inverse of the reduced matrix
 // from the factor, packed over the nfit fit parameters.
+// Mode 1 without invOut first preconditions with the factor of the
+// previous solve of the same sizes (the matrix of the previous outlier
+// iteration, kept in the context's workspace) and factorises only when CG
+// has not converged within kReuseItn iterations; the stop rule is the same,
+// so either way the solution is the refined FP64 one (MPGPU_FLAG_FRESH_FACTOR
+// factorises at every solve).
 int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, int mode, double rtol,
                         int32_t itnlim, mpgpu_solveinfo *info, double *invOut, const DenseWyElim *wy) {
     cudaStream_t s = c->stream;
-    DenseWork w;
-    w.npad = ((int64_t)n + kNB - 1) / kNB * kNB;
-    w.np = w.npad / kNB;
+    const int64_t npadN = ((int64_t)n + kNB - 1) / kNB * kNB;
+    DenseResident *D = nullptr;
+    int32_t rc = dense_workspace(c, npadN, wy != nullptr, D);
+    if (rc != MPGPU_OK) return rc;
+    DenseWork &w = D->w;
+    WyBufs &y = D->y;
     const int64_t nn = w.npad * w.npad;
     const int32_t m = wy ? wy->ncon : 0;
     const int64_t nfit = n - m;
-    int32_t rc = MPGPU_OK;
-    cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
-    if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
-    if (e == cudaSuccess) e = cudaMalloc(&w.DinvT, sizeof(double) * w.np * kNB * kNB);
-    if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB * kSuperPanels);
-    if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB * kSuperPanels);
-    for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
-        if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
-    if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
-    if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 16);
-    if (e == cudaSuccess) e = cudaMalloc(&w.err, sizeof(int32_t));
-    // WY elimination: U, U^T, T, T^T, W, M, S, the split operands, scratch
-    struct WyBufs {
-        double *U = nullptr, *UT = nullptr, *T = nullptr, *TT = nullptr, *W = nullptr, *M = nullptr, *S = nullptr,
-               *X = nullptr, *ZU = nullptr, *UZ = nullptr, *a = nullptr, *part = nullptr, *v = nullptr;
-        float *zh = nullptr, *zl = nullptr, *uh = nullptr, *ul = nullptr;
-        ~WyBufs() {
-            for (double *p : {U, UT, T, TT, W, M, S, X, ZU, UZ, a, part, v}) cudaFree(p);
-            for (float *p : {zh, zl, uh, ul}) cudaFree(p);
-        }
-    } y;
-    if (wy) {
-        for (double **v : {&y.U, &y.UT, &y.W, &y.ZU, &y.UZ}) {
-            const int64_t len = (v == &y.ZU || v == &y.UZ) ? 2 * w.npad * kWy : w.npad * kWy;
-            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * len);
-        }
-        for (double **v : {&y.T, &y.TT, &y.M, &y.S, &y.X, &y.v})
-            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * kWy * kWy);
-        if (e == cudaSuccess) e = cudaMalloc(&y.a, sizeof(double) * w.npad);
-        if (e == cudaSuccess) e = cudaMalloc(&y.part, sizeof(double) * kWyBlk * kWy);
-        for (float **v : {&y.zh, &y.zl, &y.uh, &y.ul})
-            if (e == cudaSuccess) e = cudaMalloc(v, sizeof(float) * w.npad * 2 * kWy);
-    }
-    if (e != cudaSuccess) { w.release(); return cuda_err(c, e, "dense solve allocation"); }
+    const bool tryReuse = mode == 1 && !invOut && !(c->flags & MPGPU_FLAG_FRESH_FACTOR) && D->factorValid &&
+                          D->factorMode == mode && D->factorN == n && D->factorM == m;
     const unsigned gv = (unsigned)std::min<int64_t>((w.npad + 7) / 8, 4096);
     const unsigned ge = (unsigned)std::min<int64_t>((w.npad + 255) / 256, 4096);
     // x -= U op(T) U^T x: with P = H_1 ... H_m = I - U T U^T, op = T gives
@@ -797,19 +870,21 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         qapply(out, false);
         k_reduce_op<<<ge, 256, 0, s>>>(w.npad, nfit, out, xin, out);
     };
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    struct Ev {
+        cudaEvent_t e[6] = {};
+        Ev() { for (cudaEvent_t &x : e) cudaEventCreate(&x); }
+        ~Ev() { for (cudaEvent_t x : e) cudaEventDestroy(x); }
+    } ev;
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1], eFa = ev.e[2], eFb = ev.e[3], eR = ev.e[4];
     cudaEventRecord(e0, s);
     cudaMemsetAsync(w.F, 0, sizeof(double) * nn, s);
-    k_packed_to_dense<<<4096, 256, 0, s>>>(Ap, n, w.npad, w.L, w.F);
+    k_packed_to_dense<<<4096, 256, 0, s>>>(Ap, n, w.npad, nullptr, w.F);
     if (w.npad > n) k_pad_identity<<<(unsigned)((w.npad - n + 255) / 256), 256, 0, s>>>(w.F, w.npad, n, w.npad);
     cudaMemsetAsync(w.b, 0, sizeof(double) * w.npad, s);
     if (!wy) {
         cudaMemcpyAsync(w.b, bx, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
     } else {
         // reduced right-hand side (P (g - A P^T [0; y]))_fit
-        const int64_t np_ = w.np;
         k_build_u<<<2048, 256, 0, s>>>(wy->V, wy->Vk, n, m, w.npad, y.U, y.UT);
         k_pad_t<<<64, 256, 0, s>>>(wy->T, m, y.T, y.TT);
         k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, nullptr, wy->y, y.a);
@@ -820,114 +895,154 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         k_sub_to<<<ge, 256, 0, s>>>(w.npad, w.r, w.q, w.r);
         qapply(w.r, false);
         k_expand<<<ge, 256, 0, s>>>(w.npad, nfit, n, w.r, nullptr, w.b);
-        // Q^T A Q for the preconditioner: W = A U by tensor-core 3xTF32
-        // tile products (A split tile by tile into the factor's buffer area
-        // of F's size: the split of F lands in L, which is rebuilt below)
-        float *fh = reinterpret_cast<float *>(w.L), *fl = fh + nn;
-        MPG_CUDA(c, tc_split_tiles(w.F, w.npad, 0, (int32_t)np_, 0, (int32_t)np_, fh, fl, np_, 0, s));
-        MPG_CUDA(c, tc_split_tiles(y.UT, w.npad, 0, 1, 0, (int32_t)np_, y.uh, y.ul, np_, 0, s));
-        std::vector<tc::TileTask> tk(np_);
-        for (int64_t i = 0; i < np_; ++i) tk[i] = {(int32_t)i, 0, 0, (int32_t)np_, (int32_t)i, 0};
-        tc::TileTask *dt = nullptr;
-        MPG_CUDA(c, cudaMalloc(&dt, sizeof(tc::TileTask) * np_));
-        struct G { tc::TileTask *p; ~G() { cudaFree(p); } } gd{dt};
-        MPG_CUDA(c, cudaMemcpyAsync(dt, tk.data(), sizeof(tc::TileTask) * np_, cudaMemcpyHostToDevice, s));
-        MPG_CUDA(c, cudaMemsetAsync(w.err, 0, sizeof(int32_t), s));
-        MPG_CUDA(c, tc_tile_gemm(tc::TcOp{fh, fl, np_}, tc::TcOp{y.uh, y.ul, np_}, y.W, kWy, dt, np_, 0, 0, 1.0,
-                                 0.0, w.err, s));
-        MPG_CUDA(c, cudaStreamSynchronize(s));   // the task list and the split of A are released below
-        // M = U^T W, S = T M T^T, Z = W T^T - S U / 2 (FP64, m x m sized)
-        k_utw<<<kWy, kWy, 0, s>>>(w.npad, y.U, y.W, y.M);
-        k_small_mm<<<kWy, kWy, 0, s>>>(y.T, 0, y.M, 0, y.X);
-        k_small_mm<<<kWy, kWy, 0, s>>>(y.X, 0, y.T, 1, y.S);
-        k_wy_z<<<(unsigned)std::min<int64_t>(w.npad, 4096), kWy, 0, s>>>(w.npad, y.W, y.U, y.TT, y.S, y.ZU, y.UZ);
-        MPG_CUDA(c, tc_split_tiles(y.ZU, 2 * kWy, 0, (int32_t)np_, 0, 2, y.zh, y.zl, 2, 0, s));
-        MPG_CUDA(c, tc_split_tiles(y.UZ, 2 * kWy, 0, (int32_t)np_, 0, 2, y.uh, y.ul, 2, 0, s));
-        MPG_CUDA(c, cudaGetLastError());
     }
-    // the matrix to factorise: A, or A' = A - Z U^T - U Z^T with the
-    // eliminated rows and columns replaced by the identity
-    auto prepare = [&](double sh) -> int32_t {
-        if (!wy) {
-            k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, sh);
-            return MPGPU_OK;
+    MPG_CUDA(c, cudaGetLastError());
+    // the factorisation of this solve's matrix: with wy the WY products of
+    // P A P^T first (W = A U by tensor-core 3xTF32 tile products, A split
+    // tile by tile into L's area, which the factor overwrites below)
+    auto factorise = [&]() -> int32_t {
+        D->factorValid = false;
+        if (wy) {
+            const int64_t np_ = w.np;
+            float *fh = reinterpret_cast<float *>(w.L), *fl = fh + nn;
+            MPG_CUDA(c, tc_split_tiles(w.F, w.npad, 0, (int32_t)np_, 0, (int32_t)np_, fh, fl, np_, 0, s));
+            MPG_CUDA(c, tc_split_tiles(y.UT, w.npad, 0, 1, 0, (int32_t)np_, y.uh, y.ul, np_, 0, s));
+            std::vector<tc::TileTask> tk(np_);
+            for (int64_t i = 0; i < np_; ++i) tk[i] = {(int32_t)i, 0, 0, (int32_t)np_, (int32_t)i, 0};
+            tc::TileTask *dt = nullptr;
+            MPG_CUDA(c, cudaMalloc(&dt, sizeof(tc::TileTask) * np_));
+            struct G { tc::TileTask *p; ~G() { cudaFree(p); } } gd{dt};
+            MPG_CUDA(c, cudaMemcpyAsync(dt, tk.data(), sizeof(tc::TileTask) * np_, cudaMemcpyHostToDevice, s));
+            MPG_CUDA(c, cudaMemsetAsync(w.err, 0, sizeof(int32_t), s));
+            MPG_CUDA(c, tc_tile_gemm(tc::TcOp{fh, fl, np_}, tc::TcOp{y.uh, y.ul, np_}, y.W, kWy, dt, np_, 0, 0, 1.0,
+                                     0.0, w.err, s));
+            MPG_CUDA(c, cudaStreamSynchronize(s));   // the task list is released below
+            // M = U^T W, S = T M T^T, Z = W T^T - S U / 2 (FP64, m x m sized)
+            k_utw<<<kWy, kWy, 0, s>>>(w.npad, y.U, y.W, y.M);
+            k_small_mm<<<kWy, kWy, 0, s>>>(y.T, 0, y.M, 0, y.X);
+            k_small_mm<<<kWy, kWy, 0, s>>>(y.X, 0, y.T, 1, y.S);
+            k_wy_z<<<(unsigned)std::min<int64_t>(w.npad, 4096), kWy, 0, s>>>(w.npad, y.W, y.U, y.TT, y.S, y.ZU,
+                                                                                  y.UZ);
+            MPG_CUDA(c, tc_split_tiles(y.ZU, 2 * kWy, 0, (int32_t)np_, 0, 2, y.zh, y.zl, 2, 0, s));
+            MPG_CUDA(c, tc_split_tiles(y.UZ, 2 * kWy, 0, (int32_t)np_, 0, 2, y.uh, y.ul, 2, 0, s));
+            MPG_CUDA(c, cudaGetLastError());
         }
-        k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, 0.0);
-        const int64_t T = w.np;
-        MPG_CUDA(c, tc_tile_gemm(tc::TcOp{y.zh, y.zl, 2}, tc::TcOp{y.uh, y.ul, 2}, w.L, w.npad, nullptr,
-                                 T * (T + 1) / 2, 0, 2, -1.0, 1.0, w.err, s));
-        k_identity_rows<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(w.npad - nfit, 4096)), 256, 0, s>>>(
-            w.L, w.npad, nfit, w.npad);
-        if (sh != 0.0) k_scale_diag<<<(unsigned)((nfit + 255) / 256), 256, 0, s>>>(w.L, w.npad, nfit, 1.0 + sh);
-        // a tile product whose barrier wait ran out has flagged w.err
-        int32_t h = 0;
-        MPG_CUDA(c, cudaMemcpyAsync(&h, w.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-        MPG_CUDA(c, cudaStreamSynchronize(s));
-        if (h < 0) return set_err(c, MPGPU_ERR_TIMEOUT, "tensor-core tile product: barrier wait ran out");
+        // the matrix to factorise: A, or A' = A - Z U^T - U Z^T with the
+        // eliminated rows and columns replaced by the identity
+        auto prepare = [&](double sh) -> int32_t {
+            if (!wy) {
+                k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, sh);
+                return MPGPU_OK;
+            }
+            k_copy_lower_shift<<<4096, 256, 0, s>>>(w.F, w.L, w.npad, 0.0);
+            const int64_t T = w.np;
+            MPG_CUDA(c, tc_tile_gemm(tc::TcOp{y.zh, y.zl, 2}, tc::TcOp{y.uh, y.ul, 2}, w.L, w.npad, nullptr,
+                                     T * (T + 1) / 2, 0, 2, -1.0, 1.0, w.err, s));
+            k_identity_rows<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(w.npad - nfit, 4096)), 256, 0, s>>>(
+                w.L, w.npad, nfit, w.npad);
+            if (sh != 0.0)
+                k_scale_diag<<<(unsigned)((nfit + 255) / 256), 256, 0, s>>>(w.L, w.npad, nfit, 1.0 + sh);
+            // a tile product whose barrier wait ran out has flagged w.err
+            int32_t h = 0;
+            MPG_CUDA(c, cudaMemcpyAsync(&h, w.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+            MPG_CUDA(c, cudaStreamSynchronize(s));
+            if (h < 0) return set_err(c, MPGPU_ERR_TIMEOUT, "tensor-core tile product: barrier wait ran out");
+            return MPGPU_OK;
+        };
+        // a non-positive pivot of the low-precision factor is cured by a
+        // growing diagonal shift (the CG iterations remove it)
+        double shift = 0.0;
+        int32_t r = MPGPU_OK;
+        for (int tries = 0;; ++tries) {
+            r = prepare(shift);
+            if (r != MPGPU_OK) break;
+            int32_t bad = -1;
+            r = dense_cholesky_device(c, w.L, w.npad, mode, w.hi, w.lo, w.err, &bad);
+            if (r != MPGPU_ERR_FACTOR || tries >= 6) break;
+            shift = shift == 0.0 ? 1e-7 : shift * 10.0;
+        }
+        if (r != MPGPU_OK) return r;
+        const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
+        MPG_CUDA(c, cudaFuncSetAttribute(k_trtri_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, trtriSmem));
+        k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
+        MPG_CUDA(c, cudaGetLastError());
+        D->factorValid = true;
+        D->factorMode = mode;
+        D->factorN = n;
+        D->factorM = m;
+        D->factorShift = shift;
         return MPGPU_OK;
     };
-    // factorisation; a non-positive pivot of the low-precision factor is
-    // cured by a growing diagonal shift (the CG iterations remove it)
-    double shift = 0.0;
-    int tries = 0;
-    for (;; ++tries) {
-        rc = prepare(shift);
-        if (rc != MPGPU_OK) break;
-        int32_t bad = -1;
-        rc = dense_cholesky_device(c, w.L, w.npad, mode, w.hi, w.lo, w.err, &bad);
-        if (rc != MPGPU_ERR_FACTOR || tries >= 6) break;
-        shift = shift == 0.0 ? 1e-7 : shift * 10.0;
+    // preconditioned CG from x0 = M^-1 b; stop when the relative residual
+    // is below rtol AND the last correction is below kRefineXtol of the
+    // solution: a residual test alone leaves an error of about cond(A) *
+    // rtol, which differs between factors of different precision; the
+    // correction test brings every form to the same FP64 solution
+    double hs[8] = {};
+    auto run_cg = [&](int32_t limit, int32_t &itn, int32_t &istop) -> int32_t {
+        precond(w, w.b, w.x, s);
+        op(w.x, w.q);
+        k_sub_vec<<<(unsigned)((w.npad + 255) / 256), 256, 0, s>>>(w.npad, w.b, w.q, w.r);
+        precond(w, w.r, w.z, s);
+        cudaMemcpyAsync(w.p, w.z, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
+        dotv(w, w.r, w.z, w.sc + 0, s);
+        dotv(w, w.b, w.b, w.sc + 4, s);
+        // one CG iteration as a CUDA graph (its ~600 launches replayed cheaply)
+        struct Gr {
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t x = nullptr;
+            ~Gr() { if (x) cudaGraphExecDestroy(x); if (g) cudaGraphDestroy(g); }
+        } gr;
+        MPG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        op(w.p, w.q);
+        dotv(w, w.p, w.q, w.sc + 1, s);
+        dotv(w, w.p, w.p, w.sc + 6, s);
+        k_cg_step<<<ge, 256, 0, s>>>(w.npad, w.x, w.r, w.p, w.q, w.sc);
+        dotv(w, w.x, w.x, w.sc + 7, s);
+        precond(w, w.r, w.z, s);
+        dotv(w, w.r, w.z, w.sc + 2, s);
+        k_cg_dir<<<ge, 256, 0, s>>>(w.npad, w.p, w.z, w.sc);
+        k_cg_roll<<<1, 32, 0, s>>>(w.sc);
+        dotv(w, w.r, w.r, w.sc + 3, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &gr.g);
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gr.x, gr.g, 0);
+        if (ce != cudaSuccess) return cuda_err(c, ce, "CG graph");
+        itn = 0;
+        istop = 0;
+        const double tol2 = rtol * rtol, xtol2 = kRefineXtol * kRefineXtol;
+        while (itn < limit) {
+            const int batch = std::min(4, limit - itn);
+            for (int k = 0; k < batch; ++k) cudaGraphLaunch(gr.x, s);
+            itn += batch;
+            MPG_CUDA(c, cudaMemcpyAsync(hs, w.sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
+            MPG_CUDA(c, cudaStreamSynchronize(s));
+            if (!(hs[3] == hs[3]) || !(hs[5] == hs[5])) { istop = 9; break; }
+            if (hs[3] <= tol2 * hs[4] && hs[5] <= xtol2 * hs[7]) { istop = 1; break; }
+        }
+        if (istop == 0) istop = 3;
+        return MPGPU_OK;
+    };
+    int32_t itn = 0, istop = 0, reused = 0, itnReuse = 0;
+    bool factored = false;
+    if (tryReuse) {
+        rc = run_cg(std::min<int32_t>(itnlim, kReuseItn), itn, istop);
+        if (rc != MPGPU_OK) return rc;
+        if (istop == 1) {
+            reused = 1;
+        } else {
+            reused = 2;
+            itnReuse = itn;
+        }
     }
-    if (rc != MPGPU_OK) { w.release(); return rc; }
-    cudaEvent_t eF;
-    cudaEventCreate(&eF);
-    cudaEventRecord(eF, s);
-    const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
-    MPG_CUDA(c, cudaFuncSetAttribute(k_trtri_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, trtriSmem));
-    k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
-    // x0 = M^-1 b, r = b - A x0, z = M^-1 r, p = z
-    precond(w, w.b, w.x, s);
-    op(w.x, w.q);
-    k_sub_vec<<<(unsigned)((w.npad + 255) / 256), 256, 0, s>>>(w.npad, w.b, w.q, w.r);
-    precond(w, w.r, w.z, s);
-    cudaMemcpyAsync(w.p, w.z, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
-    dotv(w, w.r, w.z, w.sc + 0, s);
-    dotv(w, w.b, w.b, w.sc + 4, s);
-    // one CG iteration as a CUDA graph (its ~600 launches replayed cheaply)
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    MPG_CUDA(c, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    op(w.p, w.q);
-    dotv(w, w.p, w.q, w.sc + 1, s);
-    dotv(w, w.p, w.p, w.sc + 6, s);
-    k_cg_step<<<ge, 256, 0, s>>>(w.npad, w.x, w.r, w.p, w.q, w.sc);
-    dotv(w, w.x, w.x, w.sc + 7, s);
-    precond(w, w.r, w.z, s);
-    dotv(w, w.r, w.z, w.sc + 2, s);
-    k_cg_dir<<<ge, 256, 0, s>>>(w.npad, w.p, w.z, w.sc);
-    k_cg_roll<<<1, 32, 0, s>>>(w.sc);
-    dotv(w, w.r, w.r, w.sc + 3, s);
-    cudaError_t ce = cudaStreamEndCapture(s, &graph);
-    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&gexec, graph, 0);
-    if (ce != cudaSuccess) { w.release(); return cuda_err(c, ce, "CG graph"); }
-    // stop when the relative residual is below rtol AND the last correction
-    // is below kRefineXtol of the solution: a residual test alone leaves an
-    // error of about cond(A) * rtol, which differs between factors of
-    // different precision; the correction test brings every form to the
-    // same FP64 solution
-    int itn = 0, istop = 0;
-    double hs[8];
-    const double tol2 = rtol * rtol, xtol2 = kRefineXtol * kRefineXtol;
-    while (itn < itnlim) {
-        const int batch = std::min(4, itnlim - itn);
-        for (int k = 0; k < batch; ++k) cudaGraphLaunch(gexec, s);
-        itn += batch;
-        MPG_CUDA(c, cudaMemcpyAsync(hs, w.sc, sizeof(hs), cudaMemcpyDeviceToHost, s));
-        MPG_CUDA(c, cudaStreamSynchronize(s));
-        if (!(hs[3] == hs[3]) || !(hs[5] == hs[5])) { istop = 9; break; }
-        if (hs[3] <= tol2 * hs[4] && hs[5] <= xtol2 * hs[7]) { istop = 1; break; }
+    if (reused != 1) {
+        cudaEventRecord(eFa, s);
+        rc = factorise();
+        if (rc != MPGPU_OK) return rc;
+        cudaEventRecord(eFb, s);
+        factored = true;
+        rc = run_cg(itnlim, itn, istop);
+        if (rc != MPGPU_OK) return rc;
     }
-    if (istop == 0) istop = 3;
     if (!wy) {
         cudaMemcpyAsync(bx, w.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
     } else {
@@ -937,44 +1052,33 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         cudaMemcpyAsync(bx, y.a, sizeof(double) * n, cudaMemcpyDeviceToDevice, s);
     }
     // the inverse from the same factor (inversion forms): X = L^-1, Z = X^T X
-    cudaEvent_t eR;
-    cudaEventCreate(&eR);
     cudaEventRecord(eR, s);
     int32_t rcInv = MPGPU_OK;
-    if (invOut && istop != 9)
+    if (invOut && istop != 9) {
         rcInv = dense_inverse_device(c, w.L, w.npad, nfit, mode, w.DinvT, w.F, invOut, w.err);
+        // the inverse overwrites L and F
+        D->factorValid = false;
+    }
     cudaEventRecord(e1, s);
     MPG_CUDA(c, cudaStreamSynchronize(s));
+    if (rcInv != MPGPU_OK) return rcInv;
     float ms = 0.0f, msF = 0.0f, msR = 0.0f;
     cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventElapsedTime(&msF, e0, eF);
+    if (factored) cudaEventElapsedTime(&msF, eFa, eFb);
     cudaEventElapsedTime(&msR, e0, eR);
-    cudaEventDestroy(eF);
-    cudaEventDestroy(eR);
-    if (rcInv != MPGPU_OK) {
-        cudaGraphExecDestroy(gexec);
-        cudaGraphDestroy(graph);
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-        w.release();
-        return rcInv;
-    }
     if (info) {
         info->msFactor = msF;
         info->msRefine = msR - msF;
         info->msInverse = ms - msR;
-        info->itn = itn;
+        info->itn = itn + itnReuse;
         info->istop = istop;
         info->nrank = (int32_t)nfit;
-        info->evmin = shift;
+        info->evmin = D->factorShift;
         info->evmax = hs[4] > 0.0 ? std::sqrt(hs[3] / hs[4]) : 0.0;
         info->dxRel = hs[7] > 0.0 ? std::sqrt(hs[5] / hs[7]) : 0.0;
         info->ms = ms;
+        info->factorReused = reused;
+        info->itnReuse = itnReuse;
     }
-    cudaGraphExecDestroy(gexec);
-    cudaGraphDestroy(graph);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    w.release();
     return istop == 9 ? set_err(c, MPGPU_ERR_NAN, "NaN in the refined dense solve") : MPGPU_OK;
 }

@@ -16,6 +16,7 @@
 #include <functional>
 #include <map>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -52,6 +53,7 @@ struct mpgpu_server {
     bool stop = false;
     std::vector<std::thread> workers;
     std::vector<mpgpu_ctx *> ctxs;
+    std::string lastErr, lastErrOut;   // the last failed job's message, and the copy handed out
 
     void work(int w) {
         mpgpu_ctx *ctx = ctxs[w];
@@ -83,8 +85,12 @@ struct mpgpu_server {
                 return true;
             };
             const int32_t rc = pede_run_admitted(ctx, &J->st, &J->job, J->res, admit);
+            const std::string msg = rc ? mpgpu_last_error(ctx) : std::string();
+            // the job's device memory goes back before its budget share does
+            mpgpu_release(ctx);
             {
                 std::lock_guard<std::mutex> lk(m);
+                if (rc) lastErr = "ticket " + std::to_string(id) + ": status " + std::to_string(rc) + ": " + msg;
                 if (J->admitted) inUse -= J->bytes;
                 J->rc = rc;
                 J->tEnd = Clock::now();
@@ -159,6 +165,13 @@ extern "C" int32_t mpgpu_server_wait(mpgpu_server *s, int64_t ticket, double tim
     const int32_t rc = J.rc;
     s->jobs.erase(it);
     return rc;
+}
+
+extern "C" const char *mpgpu_server_last_error(mpgpu_server *s) {
+    if (!s) return "";
+    std::lock_guard<std::mutex> lk(s->m);
+    s->lastErrOut = s->lastErr;
+    return s->lastErrOut.c_str();
 }
 
 extern "C" int32_t mpgpu_server_destroy(mpgpu_server *s) {

@@ -78,7 +78,8 @@ class SolveInfo(C.Structure):
     _fields_ = [("nrank", C.c_int32), ("itn", C.c_int32), ("istop", C.c_int32),
                 ("nrkd", C.c_int32), ("evmin", C.c_double), ("evmax", C.c_double),
                 ("ms", C.c_double), ("msFactor", C.c_double), ("msRefine", C.c_double),
-                ("dxRel", C.c_double), ("msInverse", C.c_double)]
+                ("dxRel", C.c_double), ("msInverse", C.c_double), ("factorReused", C.c_int32),
+                ("itnReuse", C.c_int32)]
 
 
 class Steer(C.Structure):
@@ -112,7 +113,9 @@ class Result(C.Structure):
                 ("nrank", C.c_int32), ("minresItn", C.c_int32), ("minresIstop", C.c_int32),
                 ("nloopn", C.c_int32), ("exitCode", C.c_int32),
                 ("msBuild", C.c_double), ("msSolve", C.c_double),
-                ("start", f64p), ("gcor", f64p), ("fileCounts", i64p)]
+                ("start", f64p), ("gcor", f64p), ("fileCounts", i64p),
+                ("msStructure", C.c_double), ("msUpload", C.c_double), ("msLoops", C.c_double),
+                ("msSolves", C.c_double), ("msHostIter", C.c_double), ("msJob", C.c_double)]
 
 
 class ResOpts(C.Structure):
@@ -145,8 +148,9 @@ def lib():
         if not os.path.exists(LIBPATH):
             raise RuntimeError(f"libmpgpu.so not built ({LIBPATH}); run __graft_entry__.build()")
         L = C.CDLL(LIBPATH)
-        if hasattr(L, "mpgpu_last_error"):
-            L.mpgpu_last_error.restype = C.c_char_p
+        for f in ("mpgpu_last_error", "mpgpu_server_last_error"):
+            if hasattr(L, f):
+                getattr(L, f).restype = C.c_char_p
         _lib = L
     return _lib
 
@@ -159,11 +163,12 @@ EXPORTS = [
     "mpgpu_dense_cholesky", "mpgpu_upload_timing", "mpgpu_fit_buckets",
     "mpgpu_set_monitor", "mpgpu_get_monitor", "mpgpu_monitor_groups", "mpgpu_write_mon",
     "mpgpu_server_create", "mpgpu_server_submit", "mpgpu_server_wait", "mpgpu_server_destroy",
+    "mpgpu_server_last_error",
     "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
     "mpgpu_host_labels",
     "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_loop1_device", "mpgpu_loop2_device", "mpgpu_pede_run", "mpgpu_write_res",
-    "mpgpu_write_res_opts", "mpgpu_matrix_diagonal",
+    "mpgpu_write_res_opts", "mpgpu_matrix_diagonal", "mpgpu_release",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
 ]
 
@@ -415,6 +420,10 @@ class Context:
         if self.h:
             self.L.mpgpu_destroy(self.h)
             self.h = C.c_void_p()
+
+    def release(self):
+        """Free the current job's device memory (mpgpu_release)."""
+        self.check(self.L.mpgpu_release(self.h))
 
     def __enter__(self):
         return self
@@ -686,6 +695,10 @@ class Server:
         rc = self.L.mpgpu_server_wait(self.h, C.c_int64(ticket), C.c_double(timeout_ms), C.byref(lat),
                                       C.byref(q), C.byref(b))
         return rc, lat.value, q.value, b.value
+
+    def last_error(self):
+        msg = self.L.mpgpu_server_last_error(self.h) if self.h else b""
+        return msg.decode() if msg else ""
 
     def close(self):
         if self.h:

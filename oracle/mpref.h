@@ -189,6 +189,8 @@ void mpref_ql_ssq_packed(const mpref_ql *q, double *A, int32_t t);
 void mpref_ql_export(const mpref_ql *q, double *V, double *Vk, double *L);
 
 /* avprd0 (pede.f90:5069-5232): b = A x for packed (matsto 1) or sparse. */
+/* host threads of the sparse avprd0 (CPU baseline timing; default 1) */
+void mpref_set_threads(int32_t n);
 void mpref_avprd0(int32_t matsto, int32_t n, const double *x, double *b, int32_t nG,
                   const int32_t *allIndexGroups, const int64_t *offsets,
                   const int32_t *columns, const double *matD);

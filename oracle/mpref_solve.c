@@ -7,6 +7,9 @@
  * preconditioned MINRES written from Paige & Saunders (1975).
  */
 #include "mpref.h"
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <float.h>
 #include <math.h>
 #include <stdlib.h>
@@ -333,6 +336,66 @@ void mpref_ql_ssq_packed(const mpref_ql *q, double *A0, int32_t t)
 }
 
 /* avprd0, pede.f90:5069-5232 (nspc = 1, mextnd = 0) */
+/* Host threads of the sparse product (the CPU baseline's timing only; the
+ * tests keep the default 1, the reference's sequential order).  With
+ * several threads every thread adds its row groups into its own copy of b,
+ * and the copies are summed in thread order (the array reduction of the
+ * reference's OpenMP loop, pede.f90:5110-5229). */
+static int g_avprd0_threads = 1;
+void mpref_set_threads(int32_t n) { g_avprd0_threads = n > 1 ? n : 1; }
+
+static void avprd0_groups(int32_t g0, int32_t g1, int32_t nG, const int32_t *allIndexGroups,
+                          const int64_t *offsets, const int32_t *columns, const double *matD,
+                          const double *x0, double *b0, int first)
+{
+    const double *x = x0 - 1, *A = matD - 1;
+    double *b = b0 - 1;
+    int32_t i, j;
+    const int32_t *npgrp = allIndexGroups - 1;
+    const int32_t *col = columns - 1;
+    (void)nG;
+    for (int32_t ipg = g0; ipg <= g1; ipg++) {
+        int32_t ia = npgrp[ipg], ib = npgrp[ipg + 1] - 1, in = ib - ia + 1;
+        for (i = ia; i <= ib; i++) b[i] = (first ? 0.0 : b[i]) + A[i] * x[i];
+        int64_t kk = offsets[2 * (ipg - 1)], ll = offsets[2 * (ipg - 1) + 1];
+        int64_t ku = offsets[2 * ipg] - kk, indid = kk, indij = ll, k;
+        if (ku <= 0) continue;
+        if (col[indid + 1] != 0) {
+            for (i = ia; i <= ib; i++) {
+                for (k = 1; k <= ku; k++) {
+                    j = col[indid + k];
+                    b[j] = b[j] + A[indij + k] * x[i];
+                    b[i] = b[i] + A[indij + k] * x[j];
+                }
+                indij = indij + ku;
+            }
+        } else {
+            for (k = 2; k <= ku - 2; k += 2) {
+                int32_t jg = col[indid + k];
+                int32_t ja = npgrp[jg];
+                int32_t lj = col[indid + k - 1];
+                int32_t jn = col[indid + k + 1] - lj;
+                int32_t jb = ja + jn - 1, l;
+                lj = 1;
+                for (i = ia; i <= ib; i++) {
+                    double s = 0.0;
+                    for (l = 0; l < jn; l++) s = s + A[indij + lj + l] * x[ja + l];
+                    b[i] = b[i] + s;
+                    lj = lj + jn;
+                }
+                lj = 1;
+                for (j = ja; j <= jb; j++) {
+                    double s = 0.0;
+                    for (l = 0; l < in; l++) s = s + A[indij + lj + (int64_t)l * jn] * x[ia + l];
+                    b[j] = b[j] + s;
+                    lj = lj + 1;
+                }
+                indij = indij + (int64_t)in * jn;
+            }
+        }
+    }
+}
+
 void mpref_avprd0(int32_t matsto, int32_t n, const double *x0, double *b0, int32_t nG,
                   const int32_t *allIndexGroups, const int64_t *offsets,
                   const int32_t *columns, const double *matD)
@@ -340,6 +403,28 @@ void mpref_avprd0(int32_t matsto, int32_t n, const double *x0, double *b0, int32
     const double *x = x0 - 1, *A = matD - 1;
     double *b = b0 - 1;
     int32_t i, j;
+    if (matsto == 2 && g_avprd0_threads > 1) {
+        const int nt = g_avprd0_threads;
+        double *copies = (double *)calloc((size_t)nt * (size_t)n, sizeof(double));
+#pragma omp parallel num_threads(nt)
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            double *bt = copies + (size_t)t * (size_t)n;
+#pragma omp for schedule(dynamic, 16)
+            for (int32_t g = 1; g <= nG; g++)
+                avprd0_groups(g, g, nG, allIndexGroups, offsets, columns, matD, x0, bt, 0);
+        }
+        for (int64_t q = 0; q < n; q++) {
+            double v = 0.0;
+            for (int t = 0; t < nt; t++) v += copies[(size_t)t * (size_t)n + q];
+            b0[q] = v;
+        }
+        free(copies);
+        return;
+    }
     if (matsto != 2) {
         for (i = 1; i <= n; i++) {
             int64_t ij = ((int64_t)i * i - i) / 2;

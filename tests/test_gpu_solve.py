@@ -249,3 +249,42 @@ def test_blocked_inversion_forms(mp, nmod):
         rel = np.max(np.abs(err[var] - err1[var]) / np.abs(err1[var]))
         assert rel <= tol, (metsol, rel)
         assert msinv > 0
+
+
+def test_mixed_factor_reuse(mp):
+    """The tensor-core dense solve (metsol 31) keeps its factor in the
+    context: the next outlier iteration's matrix (Huber down-weighting and
+    a chi2 cut change the record weights) is first solved with the previous
+    factor as the CG preconditioner.  That solution equals the one with a
+    fresh factor (MPGPU_FLAG_FRESH_FACTOR) within 1e-10 relative, the solve
+    reports the reuse, and a new constraint set drops the kept factor."""
+    d = mp.generate(mp.gen_config("telescope", ntracks=20000, seed=23))
+    H = mp.HostStructure(d, mreqenf=5)
+    A = mp.constraint_matrix(d, H)
+    z = np.zeros(A.shape[0])
+    sol, infos = {}, {}
+    for flags in (0, 16):
+        with mp.Context(flags=flags) as ctx:
+            ctx.set_layout(H, 1)
+            ctx.set_constraints(A)
+            ctx.upload(H)
+            gpar = np.zeros(H.nTotal)
+            got = []
+            for it, (hub, cut) in enumerate([(0, 0.0), (2, 6.0), (2, 3.0)], start=1):
+                lb = ctx.loopbf(gpar, nloopn=it, lhuber=hub, chicut=cut)
+                corr, _, info = ctx.solve(31, consResiduals=z, rtol=1e-12, itnlim=500)
+                assert info.istop == 1, (flags, it, info.istop, info.itn)
+                got.append((corr, info.factorReused, info.itn, sum(lb["nrej"])))
+            # new constraints: the kept factor is not used again
+            ctx.set_constraints(A)
+            ctx.loopbf(gpar, nloopn=2, lhuber=2, chicut=6.0)
+            _, _, info = ctx.solve(31, consResiduals=z, rtol=1e-12, itnlim=500)
+            assert info.factorReused == 0
+        sol[flags] = got
+    assert [g[1] for g in sol[16]] == [0, 0, 0]
+    assert sol[0][0][1] == 0
+    assert all(g[1] in (1, 2) for g in sol[0][1:])
+    assert sol[0][1][1] == 1, sol[0][1][1:]
+    for a, b in zip(sol[0], sol[16]):
+        x, y = a[0], b[0]
+        assert np.max(np.abs(x - y)) <= 1e-10 * np.max(np.abs(y)), (a[1:], b[1:])
