@@ -607,6 +607,10 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
         res["median_rel_diff_parameters_iterated"] = float(np.median(diffs)) if diffs else None
         for k in idx:
             res["per_job"][k]["fp64_service_ms"] = round(plain[k]["service_ms"], 3)
+            res["per_job"][k]["fp64_rc"] = plain[k]["rc"]
+            res["per_job"][k]["fp64_nrej"] = plain[k]["nrej"]
+            if plain[k]["rc"]:
+                res["per_job"][k]["fp64_error"] = plain[k].get("error", "")
     return res
 
 

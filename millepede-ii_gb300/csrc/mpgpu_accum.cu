@@ -452,7 +452,7 @@ __global__ void k_mupdat(int32_t n, const int32_t *iv, const int32_t *jv, const 
 cudaError_t launch_accumulate(const AccParams &p, int nsm, cudaStream_t s) {
     if (p.icalcm == 1 && p.nitem > 0) {
         const int smem = kAccWarps * kFlatMax * (int)sizeof(double);
-        cudaError_t e = cudaFuncSetAttribute(k_acc_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = smem_optin((const void *)k_acc_blocks);
         if (e != cudaSuccess) return e;
         int64_t blocks = (p.nitem + kAccWarps - 1) / kAccWarps;
         const int64_t maxb = (int64_t)nsm * 4;

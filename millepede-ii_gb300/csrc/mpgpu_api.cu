@@ -547,7 +547,13 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         q.bigMode = (c->flags & MPGPU_FLAG_LARGE_RECORDS) || fit_warps_per_cta(cap) < 4 ? 1 : 0;
         if (bucketed && !j.bucketWpc.empty() && j.bucketWpc[b] > 0) q.wpc = j.bucketWpc[b];
         if (q.bigMode) {
-            q.bwStride = 2 * (int64_t)q.nalgmax * q.nalcmax;
+            // B and W, or the S-form's Y (neq x nalc), S (neq x neq) and its
+            // group and equation lists, whichever is larger, so that the
+            // S-form is not ruled out by the room of a class whose records
+            // have more equations than global slots (broken lines)
+            const int64_t sNeed = (int64_t)q.neqmax * q.nalcmax + (int64_t)q.neqmax * q.neqmax +
+                                  (q.ngrpmax + 2) / 2 + (q.neqmax + 2) / 2 + 2;
+            q.bwStride = std::max<int64_t>(2 * (int64_t)q.nalgmax * q.nalcmax, sNeed);
             // records per fit launch: their B and W within 2 GiB
             bsub[b] = std::max<int64_t>(1, ((int64_t)2 << 30) / (8 * std::max<int64_t>(q.bwStride, 1)));
             bwNeed = std::max(bwNeed, bsub[b] * q.bwStride);

@@ -4,8 +4,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <set>
 #include <string>
 #include <unordered_map>
+#include <utility>
 #include <vector>
 
 #include "../../include/mpgpu.h"
@@ -223,6 +226,30 @@ cudaError_t band_factor(const BandPre &P, int32_t lprecm, cudaStream_t s);
 // y := (L L^T)^-1 y on the nfit rows; nothing when *done is set
 cudaError_t band_solve(const BandPre &P, const int *done, double *y, cudaStream_t s);
 int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double *cOut, int32_t *nrkd);
+
+// Raises a kernel's dynamic shared-memory limit to what the device allows
+// (its opt-in maximum less the kernel's static shared memory), once per
+// kernel and device.  The limit is an attribute of the function, not of a
+// launch: set per launch to the launch's size, two host threads (the
+// serving workers) launching the same kernel with different sizes could
+// each find the other's smaller limit in place.
+inline cudaError_t smem_optin(const void *kern) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done.count({dev, kern})) return cudaSuccess;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.insert({dev, kern});
+    return e;
+}
 
 // Device allocation that keeps its capacity between uploads and loops (no
 // free / alloc when the next request fits).

@@ -169,8 +169,8 @@ int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, f
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
     const int potrfSmem = kNB * (kNB + 1) * (int)sizeof(double);
     const int trsmSmem = (kNB * kNB + kNB) * (int)sizeof(double);
-    MPG_CUDA(c, cudaFuncSetAttribute(k_potrf128, cudaFuncAttributeMaxDynamicSharedMemorySize, potrfSmem));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_trsm128, cudaFuncAttributeMaxDynamicSharedMemorySize, trsmSmem));
+    MPG_CUDA(c, smem_optin((const void *)k_potrf128));
+    MPG_CUDA(c, smem_optin((const void *)k_trsm128));
     MPG_CUDA(c, cudaMemsetAsync(dErr, 0, sizeof(int32_t), s));
     auto panel = [&](int32_t p, cudaStream_t st) -> int64_t {   // potrf + trsm of panel p; rows below it
         const int64_t k0 = (int64_t)p * kNB;
@@ -963,7 +963,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         }
         if (r != MPGPU_OK) return r;
         const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
-        MPG_CUDA(c, cudaFuncSetAttribute(k_trtri_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, trtriSmem));
+        MPG_CUDA(c, smem_optin((const void *)k_trtri_blocks));
         k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
         MPG_CUDA(c, cudaGetLastError());
         D->factorValid = true;

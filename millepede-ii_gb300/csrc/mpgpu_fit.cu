@@ -572,6 +572,24 @@ __device__ void w_band_inverse(int side, double *v, int n, int nbdr, int nbnd, c
     __syncwarp();
     const int total = n * (n + 1) / 2;
     const int ab = side == 1 ? nbdr + 1 : 1;   // aux position of band index 0
+    // border products P(ib, i) = sum_jb K(ib, jb) aux(jb, i) with K = vbk,
+    // once per record in the per-lane vector area (free after the column
+    // solves): the border-band elements are -P, the band elements
+    // Vs + sum_ib aux(ib, i) P(ib, j)
+    const bool useP = nbdr <= 32;
+    double *P = X;
+    if (useP) {
+        for (int q = ln; q < nbdr * nmb; q += 32) {
+            const int ib = 1 + q / nmb, i = q % nmb;
+            double t = 0.0;
+            for (int jb = 1; jb <= nbdr; ++jb) {
+                const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
+                t = t + vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (jb - 1) * n + i];
+            }
+            P[(ib - 1) * nmb + i] = t;
+        }
+        __syncwarp();
+    }
     for (int e = ln; e < total; e += 32) {
         int R = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
         while (R > 0 && R * (R + 1) / 2 > e) R--;
@@ -587,19 +605,28 @@ __device__ void w_band_inverse(int side, double *v, int n, int nbdr, int nbnd, c
         } else if (rB || cB) {
             const int ib = rB ? (side == 1 ? R : R - nmb) : (side == 1 ? C : C - nmb);
             const int i = (rB ? C : R) - (side == 1 ? nbdr + 1 : 1);   // band index, 0-based
-            val = 0.0;
-            for (int jb = 1; jb <= nbdr; ++jb) {
-                const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
-                val = val - vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (jb - 1) * n + i];
+            if (useP) {
+                val = -P[(ib - 1) * nmb + i];
+            } else {
+                val = 0.0;
+                for (int jb = 1; jb <= nbdr; ++jb) {
+                    const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
+                    val = val - vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (jb - 1) * n + i];
+                }
             }
         } else {
             const int i = R - (side == 1 ? nbdr + 1 : 1), j = C - (side == 1 ? nbdr + 1 : 1);
             val = Vs[((i + 1) * i) / 2 + j + 1];
-            for (int ib = 1; ib <= nbdr; ++ib)
-                for (int jb = 1; jb <= nbdr; ++jb) {
-                    const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
-                    val = val + vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (ib - 1) * n + i] * aux[ab + (jb - 1) * n + j];
-                }
+            if (useP) {
+                for (int ib = 1; ib <= nbdr; ++ib) val = val + aux[ab + (ib - 1) * n + i] * P[(ib - 1) * nmb + j];
+            } else {
+                for (int ib = 1; ib <= nbdr; ++ib)
+                    for (int jb = 1; jb <= nbdr; ++jb) {
+                        const int hi = ib > jb ? ib : jb, lo = ib > jb ? jb : ib;
+                        val = val + vbk[(hi * hi - hi) / 2 + lo] * aux[ab + (ib - 1) * n + i] *
+                                        aux[ab + (jb - 1) * n + j];
+                    }
+            }
         }
         v[e] = val;
     }
@@ -683,7 +710,21 @@ __device__ __forceinline__ double gtwg_element(const WarpMem &m, int a, int b, b
     return u;
 }
 
-constexpr int kSformMaxEq = 4;   // equations per group of the S-form update
+constexpr int kSformMaxEq = 8;   // equations per group of the S-form update
+
+// whether slots a and c have an equation in common (both lists ordered by
+// equation): when not, the G^T W G part of every element of a with the
+// group of c (whose slots all share c's list) is the empty sum 0
+__device__ __forceinline__ bool eq_lists_meet(const WarpMem &m, int a, int c) {
+    int qa = m.swS[a], qae = m.swS[a + 1], qc = m.swS[c], qce = m.swS[c + 1];
+    while (qa < qae && qc < qce) {
+        const int ea = m.sw[qa] >> 16, ec = m.sw[qc] >> 16;
+        if (ea == ec) return true;
+        if (ea < ec) qa++;
+        else qc++;
+    }
+    return false;
+}
 
 // one S-form task: row a of block (pg, q) with MQ equations in group q.
 // Off-diagonal blocks (q < pg): U(a, b) = G^T W G part (the equations the
@@ -713,8 +754,9 @@ __device__ __forceinline__ void sform_task(const WarpMem &m, const double *S, in
     const int ii = a - m.goff[pg];
     const int64_t base = __ldg(pdst + pg * (pg + 1) / 2 + q) +
                          (DIAG ? (int64_t)ii * (ii + 1) / 2 : (int64_t)ii * (m.goff[q + 1] - c0));
+    const bool meet = !DIAG && eq_lists_meet(m, a, c0);
     for (int b = c0; b < c1; ++b) {
-        double u = DIAG ? 0.0 : gtwg_element(m, a, b, false);
+        double u = meet ? gtwg_element(m, a, b, false) : 0.0;
         const int qb0 = m.swS[b];
 #pragma unroll
         for (int f = 0; f < MQ; ++f) u = __fma_rn(Z[f], m.gl[m.sw[qb0 + f] & 0xffff], u);
@@ -722,15 +764,124 @@ __device__ __forceinline__ void sform_task(const WarpMem &m, const double *S, in
     }
 }
 
+// sform_task for groups in 5 to kSformMaxEq equations (a group hit more
+// than twice, e.g. a module crossed again by a looping track): the same
+// operations with the equation count at run time
+template <bool DIAG>
+__device__ void sform_task_var(const WarpMem &m, const double *S, int neq, int a, int pg, int q, int mq,
+                               const int64_t *pdst, double *stage) {
+    const int c0 = m.goff[q], c1 = DIAG ? a + 1 : m.goff[q + 1];
+    const int qa0 = m.swS[a], ma = m.swS[a + 1] - qa0, qc0 = m.swS[c0];
+    double Z[kSformMaxEq];
+#pragma unroll
+    for (int f = 0; f < kSformMaxEq; ++f) {
+        if (f >= mq) break;
+        const int ef = m.sw[qc0 + f] >> 16;
+        double z = 0.0;
+        for (int i = 0; i < ma; ++i) {
+            const int ent = m.sw[qa0 + i];
+            z = __fma_rn(m.gl[ent & 0xffff], S[(ent >> 16) * neq + ef], z);
+        }
+        if (DIAG) z = __fma_rn(-m.w0[ef], m.gl[m.sw[qa0 + f] & 0xffff], z);
+        Z[f] = z;
+    }
+    const int ii = a - m.goff[pg];
+    const int64_t base = __ldg(pdst + pg * (pg + 1) / 2 + q) +
+                         (DIAG ? (int64_t)ii * (ii + 1) / 2 : (int64_t)ii * (m.goff[q + 1] - c0));
+    const bool meet = !DIAG && eq_lists_meet(m, a, c0);
+    for (int b = c0; b < c1; ++b) {
+        double u = meet ? gtwg_element(m, a, b, false) : 0.0;
+        const int qb0 = m.swS[b];
+#pragma unroll
+        for (int f = 0; f < kSformMaxEq; ++f) {
+            if (f >= mq) break;
+            u = __fma_rn(Z[f], m.gl[m.sw[qb0 + f] & 0xffff], u);
+        }
+        stage[base + (b - c0)] = u;
+    }
+}
+
+// one off-diagonal S-form block (groups pg > q) by one lane: the block of S
+// over the equations of the two groups is loaded once into registers
+// (large records keep S in global memory), then the rows a of pg as in
+// sform_task: Z_f = sum_i g_ai S(e_i, f), U(a, b) = G^T W G part + sum_f Z_f
+// g_bf; the same operations in the same order as the per-row tasks
+template <int MP, int MQ>
+__device__ __forceinline__ void sform_block(const WarpMem &m, const double *S, int neq, int pg, int q,
+                                            const int64_t *pdst, double *stage) {
+    const int a0 = m.goff[pg], a1 = m.goff[pg + 1], c0 = m.goff[q], c1 = m.goff[q + 1];
+    const int qa0 = m.swS[a0], qc0 = m.swS[c0];
+    double Sb[MP][MQ];
+#pragma unroll
+    for (int i = 0; i < MP; ++i) {
+        const int ei = m.sw[qa0 + i] >> 16;
+#pragma unroll
+        for (int f = 0; f < MQ; ++f) Sb[i][f] = S[ei * neq + (m.sw[qc0 + f] >> 16)];
+    }
+    const bool meet = eq_lists_meet(m, a0, c0);
+    const int ncol = c1 - c0;
+    const int64_t base = __ldg(pdst + pg * (pg + 1) / 2 + q);
+    for (int a = a0; a < a1; ++a) {
+        const int qa = m.swS[a];
+        double Z[MQ];
+#pragma unroll
+        for (int f = 0; f < MQ; ++f) {
+            double z = 0.0;
+#pragma unroll
+            for (int i = 0; i < MP; ++i) z = __fma_rn(m.gl[m.sw[qa + i] & 0xffff], Sb[i][f], z);
+            Z[f] = z;
+        }
+        const int64_t row = base + (int64_t)(a - a0) * ncol;
+        for (int b = c0; b < c1; ++b) {
+            double u = meet ? gtwg_element(m, a, b, false) : 0.0;
+            const int qb0 = m.swS[b];
+#pragma unroll
+            for (int f = 0; f < MQ; ++f) u = __fma_rn(Z[f], m.gl[m.sw[qb0 + f] & 0xffff], u);
+            stage[row + (b - c0)] = u;
+        }
+    }
+}
+
+__device__ __forceinline__ void sform_block_dispatch(const WarpMem &m, const double *S, int neq, int pg, int q,
+                                                     const int64_t *pdst, double *stage) {
+    const int mp = m.swS[m.goff[pg] + 1] - m.swS[m.goff[pg]];
+    const int mq = m.swS[m.goff[q] + 1] - m.swS[m.goff[q]];
+    if (mp > 4 || mq > 4) {
+        // a group in more than four equations: row by row with S read as needed
+        for (int a = m.goff[pg]; a < m.goff[pg + 1]; ++a) sform_task_var<false>(m, S, neq, a, pg, q, mq, pdst, stage);
+        return;
+    }
+    switch ((mp - 1) * 4 + (mq - 1)) {
+        case 0: sform_block<1, 1>(m, S, neq, pg, q, pdst, stage); break;
+        case 1: sform_block<1, 2>(m, S, neq, pg, q, pdst, stage); break;
+        case 2: sform_block<1, 3>(m, S, neq, pg, q, pdst, stage); break;
+        case 3: sform_block<1, 4>(m, S, neq, pg, q, pdst, stage); break;
+        case 4: sform_block<2, 1>(m, S, neq, pg, q, pdst, stage); break;
+        case 5: sform_block<2, 2>(m, S, neq, pg, q, pdst, stage); break;
+        case 6: sform_block<2, 3>(m, S, neq, pg, q, pdst, stage); break;
+        case 7: sform_block<2, 4>(m, S, neq, pg, q, pdst, stage); break;
+        case 8: sform_block<3, 1>(m, S, neq, pg, q, pdst, stage); break;
+        case 9: sform_block<3, 2>(m, S, neq, pg, q, pdst, stage); break;
+        case 10: sform_block<3, 3>(m, S, neq, pg, q, pdst, stage); break;
+        case 11: sform_block<3, 4>(m, S, neq, pg, q, pdst, stage); break;
+        case 12: sform_block<4, 1>(m, S, neq, pg, q, pdst, stage); break;
+        case 13: sform_block<4, 2>(m, S, neq, pg, q, pdst, stage); break;
+        case 14: sform_block<4, 3>(m, S, neq, pg, q, pdst, stage); break;
+        default: sform_block<4, 4>(m, S, neq, pg, q, pdst, stage); break;
+    }
+}
+
 template <bool DIAG>
 __device__ __forceinline__ void sform_dispatch(const WarpMem &m, const double *S, int neq, int a, int pg, int q,
                                                const int64_t *pdst, double *stage) {
     const int c0 = m.goff[q];
-    switch (m.swS[c0 + 1] - m.swS[c0]) {
+    const int mq = m.swS[c0 + 1] - m.swS[c0];
+    switch (mq) {
         case 1: sform_task<1, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
         case 2: sform_task<2, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
         case 3: sform_task<3, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
-        default: sform_task<4, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
+        case 4: sform_task<4, DIAG>(m, S, neq, a, pg, q, pdst, stage); break;
+        default: sform_task_var<DIAG>(m, S, neq, a, pg, q, mq, pdst, stage); break;
     }
 }
 
@@ -1110,7 +1261,8 @@ k_fit(FitParams p, int perWarp) {
                     // Y, S and the task prefix in the B/W area (large records:
                     // the record's slot in global memory)
                     const int64_t room = BIG ? p.bwStride : 2 * (int64_t)p.nalcmax * p.nalgmax;
-                    const int64_t need = (int64_t)neq * nalc + (int64_t)neq * neq + (ngrp + 2) / 2 + 1;
+                    const int64_t need = (int64_t)neq * nalc + (int64_t)neq * neq + (ngrp + 2) / 2 + 1 +
+                                         (neq + 2) / 2 + 1;
                     if (mmax >= 1 && mmax <= kSformMaxEq && need <= room) {
                         const int64_t ngg = ((int64_t)nalg * nalg + nalg) / 2;
                         const int64_t costB = (int64_t)nalg * nalc * (nalc + 1) + ngg * nalc;
@@ -1154,9 +1306,22 @@ k_fit(FitParams p, int perWarp) {
                     double *Y = mB;                               // neq x nalc: L Gamma^-1
                     double *S = mB + (int64_t)neq * nalc;         // neq x neq
                     int32_t *tpre = reinterpret_cast<int32_t *>(S + (int64_t)neq * neq);   // ngrp + 1
+                    // the equations with global parameters, in order: the
+                    // update reads Y and S only on those (a broken-line
+                    // record's kink equations have none)
+                    int32_t *geq = tpre + ngrp + 2;
+                    int nge = 0;
+                    for (int base = 0; base < neq; base += 32) {
+                        const int e = base + ln;
+                        const bool has = e < neq && m.mq[3 * e + 2] > m.mq[3 * e + 1];
+                        const unsigned bal = __ballot_sync(0xffffffffu, has);
+                        if (has) geq[nge + __popc(bal & ((1u << ln) - 1u))] = e;
+                        nge += __popc(bal);
+                    }
+                    __syncwarp();
                     // Y_ek = sum over the locals j of equation e of l_ej Gamma^-1_jk
-                    for (int t = ln; t < neq * nalc; t += 32) {
-                        const int e = t / nalc, k = t - e * nalc + 1;
+                    for (int t = ln; t < nge * nalc; t += 32) {
+                        const int e = geq[t / nalc], k = t - (t / nalc) * nalc + 1;
                         const int sl = m.mq[3 * e], sg = m.mq[3 * e + 1];
                         double y = 0.0;
                         for (int jj = 1; jj <= sg - sl - 1; ++jj) {
@@ -1164,11 +1329,11 @@ k_fit(FitParams p, int perWarp) {
                             const double g = l <= k ? m.clmat[(k * k - k) / 2 + l - 1] : m.clmat[(l * l - l) / 2 + k - 1];
                             y = __fma_rn(m.gl[sl + jj], g, y);
                         }
-                        Y[t] = y;
+                        Y[e * nalc + k - 1] = y;
                     }
                     // prefix of the off-diagonal tasks over groups: group g
                     // has (rows of g) x g of them (columns groups q < g)
-                    if (ln == 0) {
+                    if (!BIG && ln == 0) {
                         int acc = 0;
                         for (int g = 0; g < ngrp; ++g) {
                             tpre[g] = acc;
@@ -1178,12 +1343,12 @@ k_fit(FitParams p, int perWarp) {
                     }
                     __syncwarp();
                     // S_ef = t2_e t2_f sum over the locals k of equation f of Y_ek l_fk
-                    const int ns = neq * (neq + 1) / 2;
+                    const int ns = nge * (nge + 1) / 2;
                     for (int t = ln; t < ns; t += 32) {
-                        int e = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-                        while (e > 0 && e * (e + 1) / 2 > t) e--;
-                        while ((e + 1) * (e + 2) / 2 <= t) e++;
-                        const int f = t - e * (e + 1) / 2;
+                        int ie = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+                        while (ie > 0 && ie * (ie + 1) / 2 > t) ie--;
+                        while ((ie + 1) * (ie + 2) / 2 <= t) ie++;
+                        const int e = geq[ie], f = geq[t - ie * (ie + 1) / 2];
                         const int sl = m.mq[3 * f], sg = m.mq[3 * f + 1];
                         double acc = 0.0;
                         for (int jj = 1; jj <= sg - sl - 1; ++jj)
@@ -1197,7 +1362,18 @@ k_fit(FitParams p, int perWarp) {
                     // E_p} g_ae S_ef over the equations f of q, then the row of
                     // a in block (p, q).  Off-diagonal blocks first (every
                     // task the same size), then the diagonal ones, one per slot
-                    const int ntask = tpre[ngrp];
+                    const int ntask = BIG ? 0 : tpre[ngrp];
+                    if (BIG) {
+                        // large records (S in global memory): a lane per
+                        // off-diagonal block (pg, q), q < pg, t = pg (pg - 1) / 2 + q
+                        const int nblk = ngrp * (ngrp - 1) / 2;
+                        for (int t = ln; t < nblk; t += 32) {
+                            int pg = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)t)) * 0.5f);
+                            while (pg > 1 && pg * (pg - 1) / 2 > t) pg--;
+                            while ((pg + 1) * pg / 2 <= t) pg++;
+                            sform_block_dispatch(m, S, neq, pg, t - pg * (pg - 1) / 2, pdst, p.stage);
+                        }
+                    }
                     for (int t = ln; t < ntask; t += 32) {
                         int lo = 0, hi = ngrp - 1;
                         while (lo < hi) {
@@ -1388,7 +1564,7 @@ cudaError_t launch_fit(const FitParams &p, int nsm, int maxPerSM, cudaStream_t s
     const int wpc = fit_warps_per_cta(p);
     if (wpc < 1) return cudaErrorInvalidConfiguration;
     const int bytes = per * wpc;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaError_t e = smem_optin((const void *)kern);
     if (e != cudaSuccess) return e;
     int perSM = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kern, 32 * wpc, bytes);

@@ -340,7 +340,7 @@ int32_t dense_inverse_device(mpgpu_ctx *c, double *L, int64_t npad, int64_t n, i
         e = cudaMemcpyAsync(dTask, tk.data(), sizeof(TileTask) * tk.size(), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) { release(); return cuda_err(c, e, "blocked inverse workspace"); }
     if (mode == 1) {
-        MPG_CUDA(c, cudaFuncSetAttribute(k_tile_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+        MPG_CUDA(c, smem_optin((const void *)k_tile_gemm_tc));
         // L^T tiles (p, k) for k > p: the panels of the original factor
         for (int32_t p = 0; p < np - 1; ++p)
             k_split_tiles<<<np - 1 - p, 256, 0, s>>>(L, ld, p + 1, np, p, p + 1, 1, phi, plo, np, 0);
@@ -405,7 +405,7 @@ cudaError_t tc_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r1, 
 cudaError_t tc_tile_gemm(const TcOp &A, const TcOp &B, double *C, int64_t ldc, const TileTask *tasks, int64_t ntask,
                          int32_t trail0, int32_t trailK, double alpha, double beta, int32_t *err, cudaStream_t s) {
     if (ntask <= 0) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(k_tile_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    cudaError_t e = smem_optin((const void *)k_tile_gemm_tc);
     if (e != cudaSuccess) return e;
     k_tile_gemm_tc<<<(unsigned)ntask, kTcThreads, kTcSmem, s>>>(A, B, C, ldc, tasks, trail0, trailK, alpha, beta, err);
     return cudaGetLastError();

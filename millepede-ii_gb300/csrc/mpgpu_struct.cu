@@ -616,10 +616,10 @@ int32_t loop1_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr, const in
     P.nrec = nrec; P.recPtr = R.recPtr; P.inder = R.inder; P.glder = R.glder;
     P.count = dCount; P.fail = dFail; P.err = dErr; P.ovList = ovList; P.ovCount = dOvN;
     const int smemS = kL1Warps * (int)sizeof(UpWarp<false>), smemB = kL1Warps * (int)sizeof(UpWarp<true>);
-    L1_CUDA(cudaFuncSetAttribute(k_l1_collect<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
-    L1_CUDA(cudaFuncSetAttribute(k_l1_collect<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
-    L1_CUDA(cudaFuncSetAttribute(k_l1_translate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
-    L1_CUDA(cudaFuncSetAttribute(k_l1_translate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
+    L1_CUDA(smem_optin((const void *)k_l1_collect<false>));
+    L1_CUDA(smem_optin((const void *)k_l1_collect<true>));
+    L1_CUDA(smem_optin((const void *)k_l1_translate<false>));
+    L1_CUDA(smem_optin((const void *)k_l1_translate<true>));
     int perSm = 0;
     L1_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_l1_collect<false>, 32 * kL1Warps, smemS));
     const unsigned gS = (unsigned)std::max<int64_t>(
@@ -789,8 +789,8 @@ int32_t loop2_device(mpgpu_ctx *c, const int32_t *varIndexOfTotal, int32_t nVar,
     Q.rowWord = dRow;
     Q.bits = bits;
     const int smemS = kL1Warps * (int)sizeof(UpWarp<false>), smemB = kL1Warps * (int)sizeof(UpWarp<true>);
-    MPG_CUDA(c, cudaFuncSetAttribute(k_l2_bits<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_l2_bits<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
+    MPG_CUDA(c, smem_optin((const void *)k_l2_bits<false>));
+    MPG_CUDA(c, smem_optin((const void *)k_l2_bits<true>));
     int perSm = 0;
     MPG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_l2_bits<false>, 32 * kL1Warps, smemS));
     const unsigned gS = (unsigned)std::max<int64_t>(

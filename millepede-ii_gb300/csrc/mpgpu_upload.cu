@@ -535,10 +535,10 @@ int32_t upload_records_device(mpgpu_ctx *c, int64_t nrec, const int64_t *recPtr,
     // large kernels: two CTAs per SM over the overflow list
     const int smemS = kUpWarps * (int)sizeof(UpWarp<false>);
     const int smemB = kUpWarps * (int)sizeof(UpWarp<true>);
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_scan<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_fill<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemS));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_scan<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
-    MPG_CUDA(c, cudaFuncSetAttribute(k_up_fill<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smemB));
+    MPG_CUDA(c, smem_optin((const void *)k_up_scan<false>));
+    MPG_CUDA(c, smem_optin((const void *)k_up_fill<false>));
+    MPG_CUDA(c, smem_optin((const void *)k_up_scan<true>));
+    MPG_CUDA(c, smem_optin((const void *)k_up_fill<true>));
     int perSm = 0;
     MPG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_up_scan<false>, 32 * kUpWarps, smemS));
     const unsigned upBlocks = (unsigned)std::max<int64_t>(
