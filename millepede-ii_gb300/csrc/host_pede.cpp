@@ -494,9 +494,10 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         }
         const int64_t nm = st->matsto == 2 ? nmat : (int64_t)nVar * (nVar + 1) / 2;
         const int64_t npad = ((int64_t)nVar + 127) / 128 * 128;
-        // dense forms: F and L (npad^2 each), the split panels and the WY
-        // buffers of the constraint elimination (about 3 KB per row)
-        const int64_t dense = (st->metsol == 31 || st->metsol == 32) ? 2 * npad * npad + 3072 * npad : 0;
+        // dense forms: F and L (npad^2 each), the split panels, the WY
+        // buffers of the constraint elimination and the preconditioner's
+        // super-block inverses (about 40 KB per row)
+        const int64_t dense = (st->metsol == 31 || st->metsol == 32) ? 2 * npad * npad + 5120 * npad : 0;
         const int64_t stageCap = (int64_t)2 << 30;   // 2 x 8 GiB staging buffers at most (in doubles)
         const int64_t bytes = 40 * nw + 8 * (std::min(stage, stageCap) + nm + dense) + 64 * (int64_t)nVar +
                               ((int64_t)64 << 20);

@@ -227,12 +227,12 @@ int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, f
             float *hl[4] = {nullptr, nullptr, nullptr, nullptr};
             cudaStream_t sp = nullptr, sb = nullptr;
             cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+            cudaStream_t s0 = nullptr;   // the caller's stream (the buffers are ordered on it)
             ~Res() {
                 if (sp) cudaStreamSynchronize(sp);
                 if (sb) cudaStreamSynchronize(sb);
-                cudaFree(task);
-                cudaFree(hl[2]);   // hl[0], hl[1] are the caller's
-                cudaFree(hl[3]);
+                for (void *p : {(void *)task, (void *)hl[2], (void *)hl[3]})   // hl[0], hl[1] are the caller's
+                    if (p) cudaFreeAsync(p, s0);
                 for (cudaEvent_t e : ev)
                     if (e) cudaEventDestroy(e);
                 if (sp) cudaStreamDestroy(sp);
@@ -240,11 +240,12 @@ int32_t dense_cholesky_device(mpgpu_ctx *c, double *A, int64_t npad, int mode, f
             }
         } R;
         const int64_t splitLen = npad * kNB * kSuperPanels;
-        MPG_CUDA(c, cudaMalloc(&R.task, sizeof(tc::TileTask) * std::max<size_t>(tk.size(), 1)));
+        R.s0 = s;
+        MPG_CUDA(c, cudaMallocAsync(&R.task, sizeof(tc::TileTask) * std::max<size_t>(tk.size(), 1), s));
         R.hl[0] = hiBuf;
         R.hl[1] = loBuf;
-        MPG_CUDA(c, cudaMalloc(&R.hl[2], sizeof(float) * splitLen));
-        MPG_CUDA(c, cudaMalloc(&R.hl[3], sizeof(float) * splitLen));
+        MPG_CUDA(c, cudaMallocAsync(&R.hl[2], sizeof(float) * splitLen, s));
+        MPG_CUDA(c, cudaMallocAsync(&R.hl[3], sizeof(float) * splitLen, s));
         int lo = 0, hiPrio = 0;
         MPG_CUDA(c, cudaDeviceGetStreamPriorityRange(&lo, &hiPrio));
         MPG_CUDA(c, cudaStreamCreateWithPriority(&R.sp, cudaStreamNonBlocking, hiPrio));
@@ -429,64 +430,6 @@ __global__ void __launch_bounds__(256) k_trtri_blocks(const double *A, int64_t l
     }
 }
 
-// forward solve, block p: y_p <- L_pp^-1 y_p
-__global__ void k_fwd_diag(const double *DinvT, int64_t p, double *y) {
-    __shared__ double yp[kNB];
-    const int i = threadIdx.x;
-    double *yb = y + p * kNB;
-    yp[i] = yb[i];
-    __syncthreads();
-    const double *D = DinvT + p * kNB * kNB;
-    double s = 0.0;
-    for (int m = 0; m <= i; ++m) s += D[(int64_t)m * kNB + i] * yp[m];
-    yb[i] = s;
-}
-
-// forward solve, rows below block p: y_R -= L[R][block p] y_p (warp per row)
-__global__ void k_fwd_upd(const double *L, int64_t ld, int64_t p, int64_t npad, double *y) {
-    __shared__ double yp[kNB];
-    const int ln = threadIdx.x & 31;
-    if (threadIdx.x < kNB) yp[threadIdx.x] = y[p * kNB + threadIdx.x];
-    __syncthreads();
-    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t R = (p + 1) * kNB + w; R < npad; R += nw) {
-        const double *row = L + R * ld + p * kNB;
-        double s = 0.0;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) s += row[q * 32 + ln] * yp[q * 32 + ln];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (ln == 0) y[R] -= s;
-    }
-}
-
-// backward solve, block p: y_p <- L_pp^-T y_p
-__global__ void k_bwd_diag(const double *DinvT, int64_t p, double *y) {
-    __shared__ double yp[kNB];
-    const int i = threadIdx.x;
-    double *yb = y + p * kNB;
-    yp[i] = yb[i];
-    __syncthreads();
-    const double *D = DinvT + p * kNB * kNB + (int64_t)i * kNB;
-    double s = 0.0;
-    for (int m = i; m < kNB; ++m) s += D[m] * yp[m];
-    yb[i] = s;
-}
-
-// backward solve, columns left of block p: y_c -= sum_m L[p*128+m][c] x_p[m]
-__global__ void k_bwd_upd(const double *L, int64_t ld, int64_t p, double *y) {
-    __shared__ double xp[kNB];
-    if (threadIdx.x < kNB) xp[threadIdx.x] = y[p * kNB + threadIdx.x];
-    __syncthreads();
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= p * kNB) return;
-    const double *col = L + p * kNB * ld + c;
-    double s = 0.0;
-    for (int m = 0; m < kNB; ++m) s += col[(int64_t)m * ld] * xp[m];
-    y[c] -= s;
-}
-
 // y = F x, dense full matrix, one warp per row
 __global__ void k_gemv(const double *F, int64_t ld, int64_t npad, const double *x, double *y) {
     const int ln = threadIdx.x & 31;
@@ -555,31 +498,164 @@ __global__ void k_sub_vec(int64_t n, const double *b, const double *ax, double *
     if (i < n) r[i] = b[i] - ax[i];
 }
 
+// ---- the preconditioner's triangular solves by super-blocks of kSB rows:
+// X_b = L_bb^-1 of every diagonal super-block (from the 128-row inverse
+// blocks by block forward substitution in FP64 tile products), then each
+// solve is nsb steps of (X_b times the block, update of the rows below or
+// the columns left) instead of np steps of 128 rows: a quarter of the
+// dependent launches of a CG iteration
+constexpr int kSB = 4 * kNB;   // rows of a super-block
+
+// XS rows of panel p, local columns of its 128-column slot: L_pp^-1 (lower)
+__global__ void k_sb_set_diag(const double *DinvT, int64_t np, double *XS) {
+    const int64_t total = np * kNB * kNB;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = e / (kNB * kNB);
+        const int r = (int)(e % (kNB * kNB)) / kNB, c = (int)(e % kNB);
+        const double v = c <= r ? DinvT[p * kNB * kNB + (int64_t)c * kNB + r] : 0.0;
+        XS[(p * kNB + r) * kSB + (p % 4) * kNB + c] = v;
+    }
+}
+
+// XT_b = X_b^T per super-block (rows of the super-block, kSB columns each)
+__global__ void k_sb_transpose(const double *XS, int64_t npad, double *XT) {
+    const int64_t total = npad * kSB;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t row = e / kSB;
+        const int c = (int)(e % kSB);
+        const int64_t b0 = row / kSB * kSB;
+        const int r = (int)(row - b0);
+        if (b0 + c < npad) XT[(b0 + c) * kSB + r] = XS[e];
+    }
+}
+
+// out[row0 + r] = sum_c X[row0 + r][c] in[row0 + c] over c <= r (lower) or
+// c >= r, c < size; a warp per row, lanes over c, tree sum over the lanes
+__global__ void k_sb_diag(const double *X, int64_t row0, int size, const double *in, double *out, int lower) {
+    const int ln = threadIdx.x & 31;
+    const int r = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (r >= size) return;
+    const double *xr = X + (row0 + r) * kSB;
+    const int c0 = lower ? 0 : r, c1 = lower ? r + 1 : size;
+    double sum = 0.0;
+    for (int c = c0 + ln; c < c1; c += 32) sum += xr[c] * in[row0 + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (ln == 0) out[row0 + r] = sum;
+}
+
+// v_R -= L[R][row0 .. row0 + size) z_b for the rows R >= row0 + size (warp per row)
+__global__ void k_sb_fwd_upd(const double *L, int64_t ld, int64_t row0, int size, int64_t npad, const double *z,
+                             double *v) {
+    const int ln = threadIdx.x & 31;
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t R = row0 + size + w; R < npad; R += nw) {
+        const double *row = L + R * ld + row0;
+        double sum = 0.0;
+        for (int c = ln; c < size; c += 32) sum += row[c] * z[row0 + c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (ln == 0) v[R] -= sum;
+    }
+}
+
+// z_c -= sum_m L[row0 + m][c] o[row0 + m] for the columns c < row0: 64
+// columns per CTA, the m range in four quarters summed in order
+__global__ void __launch_bounds__(256) k_sb_bwd_upd(const double *L, int64_t ld, int64_t row0, int size,
+                                                    const double *o, double *z) {
+    __shared__ double part[4][64];
+    const int cl = threadIdx.x & 63, g = threadIdx.x >> 6;
+    const int64_t c = (int64_t)blockIdx.x * 64 + cl;
+    const int q = (size + 3) / 4, m0 = g * q, m1 = min(size, m0 + q);
+    double sum = 0.0;
+    if (c < row0) {
+        const double *col = L + row0 * ld + c;
+#pragma unroll 8
+        for (int m = m0; m < m1; ++m) sum += col[(int64_t)m * ld] * o[row0 + m];
+    }
+    part[g][cl] = sum;
+    __syncthreads();
+    if (g == 0 && c < row0) z[c] -= ((part[0][cl] + part[1][cl]) + part[2][cl]) + part[3][cl];
+}
+
 struct DenseWork {
     int64_t npad = 0, np = 0;
-    double *L = nullptr, *F = nullptr, *DinvT = nullptr;
+    double *L = nullptr, *F = nullptr, *DinvT = nullptr;   // factor, matrix, inverse 128-row blocks (transposed)
+    double *XS = nullptr, *XT = nullptr, *XW = nullptr;    // super-block inverses, their transposes, scratch
+    tc::TileTask *sbTask = nullptr;                        // task lists of the super-block inverses
     float *hi = nullptr, *lo = nullptr;
     double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+    double *t1 = nullptr, *t2 = nullptr;                   // the preconditioner's working vectors
     double *part = nullptr, *sc = nullptr;
     int32_t *err = nullptr;
     void release() {
-        cudaFree(L); cudaFree(F); cudaFree(DinvT); cudaFree(hi); cudaFree(lo);
-        cudaFree(b); cudaFree(x); cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q);
+        cudaFree(L); cudaFree(F); cudaFree(DinvT); cudaFree(XS); cudaFree(XT); cudaFree(XW); cudaFree(sbTask);
+        cudaFree(hi); cudaFree(lo);
+        cudaFree(b); cudaFree(x); cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(t1); cudaFree(t2);
         cudaFree(part); cudaFree(sc); cudaFree(err);
     }
 };
 
-void precond(const DenseWork &w, const double *in, double *out, cudaStream_t s) {
-    cudaMemcpyAsync(out, in, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
-    for (int64_t p = 0; p < w.np; ++p) {
-        k_fwd_diag<<<1, kNB, 0, s>>>(w.DinvT, p, out);
-        const int64_t rows = w.npad - (p + 1) * kNB;
-        if (rows > 0)
-            k_fwd_upd<<<(unsigned)std::min<int64_t>((rows + 7) / 8, 1216), 256, 0, s>>>(w.L, w.npad, p, w.npad, out);
+// X_b for every super-block from L and the 128-row inverse blocks:
+// X_jj = L_jj^-1, and for i = j + d (d = 1, 2, 3) T = sum_{k=j}^{i-1} L_ik X_kj,
+// X_ij = -L_ii^-1 T (one wave of tile products per d over all super-blocks)
+cudaError_t build_super_inverse(DenseWork &w, cudaStream_t s) {
+    const int64_t np = w.np, nsb = (np + 3) / 4;
+    cudaError_t e = cudaMemsetAsync(w.XS, 0, sizeof(double) * w.npad * kSB, s);
+    if (e != cudaSuccess) return e;
+    k_sb_set_diag<<<(unsigned)std::min<int64_t>(np * 64, 4096), 256, 0, s>>>(w.DinvT, np, w.XS);
+    std::vector<tc::TileTask> tk;
+    std::vector<int64_t> wave(7, 0);
+    for (int d = 1; d <= 3; ++d) {
+        wave[2 * d - 2] = (int64_t)tk.size();
+        for (int64_t b = 0; b < nsb; ++b) {
+            const int32_t t0 = (int32_t)(4 * b), npb = (int32_t)std::min<int64_t>(4, np - 4 * b);
+            for (int32_t j = 0; j + d < npb; ++j) tk.push_back({t0 + j + d, j, t0 + j, t0 + j + d, t0 + j + d, j});
+        }
+        wave[2 * d - 1] = (int64_t)tk.size();
+        for (int64_t b = 0; b < nsb; ++b) {
+            const int32_t t0 = (int32_t)(4 * b), npb = (int32_t)std::min<int64_t>(4, np - 4 * b);
+            for (int32_t j = 0; j + d < npb; ++j) tk.push_back({0, j, t0 + j + d, t0 + j + d + 1, t0 + j + d, j});
+        }
     }
-    for (int64_t p = w.np - 1; p >= 0; --p) {
-        k_bwd_diag<<<1, kNB, 0, s>>>(w.DinvT, p, out);
-        if (p > 0) k_bwd_upd<<<(unsigned)((p * kNB + 255) / 256), 256, 0, s>>>(w.L, w.npad, p, out);
+    wave[6] = (int64_t)tk.size();
+    if (!tk.empty()) {
+        e = cudaMemcpyAsync(w.sbTask, tk.data(), sizeof(tc::TileTask) * tk.size(), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        for (int d = 1; d <= 3 && e == cudaSuccess; ++d) {
+            const int64_t a0 = wave[2 * d - 2], a1 = wave[2 * d - 1], a2 = wave[2 * d];
+            e = fp64_tile_gemm(w.L, w.npad, 0, w.XS, kSB, 1, w.XW, kSB, w.sbTask + a0, a1 - a0, 1.0, 0.0, s);
+            if (e == cudaSuccess)
+                e = fp64_tile_gemm(w.DinvT, kNB, 1, w.XW, kSB, 1, w.XS, kSB, w.sbTask + a1, a2 - a1, -1.0, 0.0, s);
+        }
+        // the host task list must live until the copy has run
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e != cudaSuccess) return e;
+    k_sb_transpose<<<(unsigned)std::min<int64_t>((w.npad * kSB + 255) / 256, 8192), 256, 0, s>>>(w.XS, w.npad, w.XT);
+    return cudaGetLastError();
+}
+
+// out = L^-T L^-1 in by super-block steps (in is not modified)
+void precond(const DenseWork &w, const double *in, double *out, cudaStream_t s) {
+    const int64_t nsb = (w.np + 3) / 4;
+    double *v = w.t1, *zz = w.t2;
+    cudaMemcpyAsync(v, in, sizeof(double) * w.npad, cudaMemcpyDeviceToDevice, s);
+    for (int64_t b = 0; b < nsb; ++b) {
+        const int64_t row0 = b * kSB;
+        const int size = (int)std::min<int64_t>(kSB, w.npad - row0);
+        k_sb_diag<<<(unsigned)((size + 7) / 8), 256, 0, s>>>(w.XS, row0, size, v, zz, 1);
+        const int64_t rows = w.npad - row0 - size;
+        if (rows > 0)
+            k_sb_fwd_upd<<<(unsigned)std::min<int64_t>((rows + 7) / 8, 1216), 256, 0, s>>>(w.L, w.npad, row0, size,
+                                                                                           w.npad, zz, v);
+    }
+    for (int64_t b = nsb - 1; b >= 0; --b) {
+        const int64_t row0 = b * kSB;
+        const int size = (int)std::min<int64_t>(kSB, w.npad - row0);
+        k_sb_diag<<<(unsigned)((size + 7) / 8), 256, 0, s>>>(w.XT, row0, size, zz, out, 0);
+        if (row0 > 0) k_sb_bwd_upd<<<(unsigned)((row0 + 63) / 64), 256, 0, s>>>(w.L, w.npad, row0, size, out, zz);
     }
 }
 
@@ -782,9 +858,12 @@ int32_t dense_workspace(mpgpu_ctx *c, int64_t npad, bool wy, DenseResident *&out
     cudaError_t e = cudaMalloc(&w.L, sizeof(double) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&w.F, sizeof(double) * nn);
     if (e == cudaSuccess) e = cudaMalloc(&w.DinvT, sizeof(double) * w.np * kNB * kNB);
+    for (double **v : {&w.XS, &w.XT, &w.XW})
+        if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad * kSB);
+    if (e == cudaSuccess) e = cudaMalloc(&w.sbTask, sizeof(tc::TileTask) * (12 * ((w.np + 3) / 4) + 1));
     if (e == cudaSuccess) e = cudaMalloc(&w.hi, sizeof(float) * w.npad * kNB * kSuperPanels);
     if (e == cudaSuccess) e = cudaMalloc(&w.lo, sizeof(float) * w.npad * kNB * kSuperPanels);
-    for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q})
+    for (double **v : {&w.b, &w.x, &w.r, &w.z, &w.p, &w.q, &w.t1, &w.t2})
         if (e == cudaSuccess) e = cudaMalloc(v, sizeof(double) * w.npad);
     if (e == cudaSuccess) e = cudaMalloc(&w.part, sizeof(double) * kDotBlk);
     if (e == cudaSuccess) e = cudaMalloc(&w.sc, sizeof(double) * 16);
@@ -910,8 +989,8 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
             std::vector<tc::TileTask> tk(np_);
             for (int64_t i = 0; i < np_; ++i) tk[i] = {(int32_t)i, 0, 0, (int32_t)np_, (int32_t)i, 0};
             tc::TileTask *dt = nullptr;
-            MPG_CUDA(c, cudaMalloc(&dt, sizeof(tc::TileTask) * np_));
-            struct G { tc::TileTask *p; ~G() { cudaFree(p); } } gd{dt};
+            MPG_CUDA(c, cudaMallocAsync(&dt, sizeof(tc::TileTask) * np_, s));
+            struct G { tc::TileTask *p; cudaStream_t s; ~G() { cudaFreeAsync(p, s); } } gd{dt, s};
             MPG_CUDA(c, cudaMemcpyAsync(dt, tk.data(), sizeof(tc::TileTask) * np_, cudaMemcpyHostToDevice, s));
             MPG_CUDA(c, cudaMemsetAsync(w.err, 0, sizeof(int32_t), s));
             MPG_CUDA(c, tc_tile_gemm(tc::TcOp{fh, fl, np_}, tc::TcOp{y.uh, y.ul, np_}, y.W, kWy, dt, np_, 0, 0, 1.0,
@@ -965,6 +1044,7 @@ int32_t dense_solve_pcg(mpgpu_ctx *c, int32_t n, const double *Ap, double *bx, i
         const int trtriSmem = (kNB * kNB + kNB) * (int)sizeof(double);
         MPG_CUDA(c, smem_optin((const void *)k_trtri_blocks));
         k_trtri_blocks<<<(unsigned)w.np, 256, trtriSmem, s>>>(w.L, w.npad, w.DinvT);
+        MPG_CUDA(c, build_super_inverse(w, s));
         MPG_CUDA(c, cudaGetLastError());
         D->factorValid = true;
         D->factorMode = mode;

@@ -93,6 +93,21 @@ __global__ void __launch_bounds__(256) k_tile_gemm_fp64(Fp64Op A, Fp64Op B, doub
         }
 }
 
+}  // namespace
+
+// FP64 tile products C(cRow, cCol) = alpha sum_k op(A)(aRow, k) op(B)(k, bRow)
+// + beta C over a device task list (op: trans 0 takes tile (r, k) of A or
+// (bRow, k) of B transposed, trans 1 the tile as stored)
+cudaError_t fp64_tile_gemm(const double *A, int64_t lda, int32_t ta, const double *B, int64_t ldb, int32_t tb,
+                           double *C, int64_t ldc, const tc::TileTask *tasks, int64_t ntask, double alpha,
+                           double beta, cudaStream_t s) {
+    if (ntask <= 0) return cudaSuccess;
+    k_tile_gemm_fp64<<<(unsigned)(ntask * 4), 256, 0, s>>>(Fp64Op{A, lda, ta}, Fp64Op{B, ldb, tb}, C, ldc, tasks,
+                                                            alpha, beta);
+    return cudaGetLastError();
+}
+
+namespace {
 // ------------------------------------------------------------ tensor-core form
 using tc::TcOp;
 

@@ -922,6 +922,9 @@ struct Solver {
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device);
     }
     ~Solver() {
+        // part is stream-ordered (cudaMallocAsync on the context's stream)
+        if (part) cudaFreeAsync(part, s);
+        part = nullptr;
         dfree(wyPart); dfree(wyT);
         dfree(sb.rowStart); dfree(sb.bcol); dfree(sb.boff); dfree(sb.bld); dfree(sb.tOff);
         dfree(sb.colStart); dfree(sb.colBlk); dfree(sb.tBase); dfree(sb.tbuf); dfree(part);
@@ -1193,17 +1196,29 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
     DevJob &j = c->j;
     cudaStream_t s = c->stream;
     const int32_t n = j.nVar, ncon = j.ncon, nfit = n - ncon;
-    double *corr = nullptr, *vbuf = nullptr, *Av = nullptr, *vk = nullptr, *diag = nullptr, *yv = nullptr;
-    int32_t *used = nullptr, *piv = nullptr;
-    MPG_CUDA(c, cudaMalloc(&corr, sizeof(double) * n));
-    MPG_CUDA(c, cudaMalloc(&vbuf, sizeof(double) * n));
-    MPG_CUDA(c, cudaMalloc(&Av, sizeof(double) * n));
-    MPG_CUDA(c, cudaMalloc(&vk, sizeof(double) * n));
-    MPG_CUDA(c, cudaMalloc(&diag, sizeof(double) * n));
-    MPG_CUDA(c, cudaMalloc(&yv, sizeof(double) * (ncon + 1)));
-    MPG_CUDA(c, cudaMalloc(&used, sizeof(int32_t) * n));
-    MPG_CUDA(c, cudaMalloc(&piv, sizeof(int32_t) * 4));
-    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    // per-solve vectors from the stream-ordered pool: a cudaFree would wait
+    // for the whole device, i.e. for the other jobs' work in a served mix
+    struct Tmp {
+        cudaStream_t s;
+        double *corr = nullptr, *vbuf = nullptr, *Av = nullptr, *vk = nullptr, *diag = nullptr, *yv = nullptr;
+        int32_t *used = nullptr, *piv = nullptr;
+        ~Tmp() {
+            for (void *p : {(void *)corr, (void *)vbuf, (void *)Av, (void *)vk, (void *)diag, (void *)yv,
+                            (void *)used, (void *)piv})
+                if (p) cudaFreeAsync(p, s);
+        }
+    } T{s};
+    double *&corr = T.corr, *&vbuf = T.vbuf, *&Av = T.Av, *&vk = T.vk, *&diag = T.diag, *&yv = T.yv;
+    int32_t *&used = T.used, *&piv = T.piv;
+    MPG_CUDA(c, cudaMallocAsync(&corr, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&vbuf, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&Av, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&vk, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&diag, sizeof(double) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&yv, sizeof(double) * (ncon + 1), s));
+    MPG_CUDA(c, cudaMallocAsync(&used, sizeof(int32_t) * n, s));
+    MPG_CUDA(c, cudaMallocAsync(&piv, sizeof(int32_t) * 4, s));
+    MPG_CUDA(c, cudaMallocAsync(&S.part, sizeof(double) * (kDotBlocks + 8), s));
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1270,11 +1285,7 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
                                                      info, decomposition ? nullptr : j.matD, &wye)
                                    : dense_solve_pcg(c, nfit, j.matD, corr, dense, tol, itnlim > 0 ? itnlim : 2000,
                                                      info, decomposition ? nullptr : j.matD);
-        if (rcd != MPGPU_OK) {
-            cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
-            cudaFree(used); cudaFree(piv);
-            return rcd;
-        }
+        if (rcd != MPGPU_OK) return rcd;
         nrank = info->nrank;
     } else {
         // chdec2 + chslv2 (mpnum.f90:891-987)
@@ -1317,8 +1328,6 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
     info->ms = ms;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    cudaFree(corr); cudaFree(vbuf); cudaFree(Av); cudaFree(vk); cudaFree(diag); cudaFree(yv);
-    cudaFree(used); cudaFree(piv);
     return MPGPU_OK;
 }
 
@@ -1338,7 +1347,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
         int32_t rc = S.build_blocks();
         if (rc) return rc;
     }
-    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    MPG_CUDA(c, cudaMallocAsync(&S.part, sizeof(double) * (kDotBlocks + 8), s));
     // workspace released on every return
     struct Scratch {
         std::vector<double *> bufs;
@@ -1543,7 +1552,7 @@ int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double
         int32_t rc = S.build_blocks();
         if (rc) return rc;
     }
-    MPG_CUDA(c, cudaMalloc(&S.part, sizeof(double) * (kDotBlocks + 8)));
+    MPG_CUDA(c, cudaMallocAsync(&S.part, sizeof(double) * (kDotBlocks + 8), s));
     struct Bufs {
         double *v = nullptr, *tmp = nullptr, *yk = nullptr;
         BandPre P;

@@ -106,3 +106,6 @@ cudaError_t tc_split_tiles(const double *M, int64_t ld, int32_t r0, int32_t r1, 
 cudaError_t tc_tile_gemm(const tc::TcOp &A, const tc::TcOp &B, double *C, int64_t ldc, const tc::TileTask *tasks,
                          int64_t ntask, int32_t trail0, int32_t trailK, double alpha, double beta, int32_t *err,
                          cudaStream_t s);
+cudaError_t fp64_tile_gemm(const double *A, int64_t lda, int32_t ta, const double *B, int64_t ldb, int32_t tb,
+                           double *C, int64_t ldc, const tc::TileTask *tasks, int64_t ntask, double alpha,
+                           double beta, cudaStream_t s);
