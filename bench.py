@@ -440,15 +440,18 @@ def serve_spec_job(mp, specs, k):
     """Records and constraints of job k of the serving stream (seed 1000 + k):
     the barrel with n/6 modules, helix or broken-line (4-28 hits) tracks,
     the model's weak-mode constraints plus seeded sparse ones up to the
-    drawn count; returns (data, constraints, number of labels)."""
+    drawn count; returns (data, constraints, number of detector labels)."""
     kind, n, nrec, ncon = specs[k]
     cfg = mp.gen_config(kind, ntracks=nrec, seed=1000 + k)
     cfg.nmod = max(n // 6, 1)
+    cfg.threads = 6   # tracks on six host threads, each from its own stream
     if kind == "brokenlines":
         cfg.maxHits = 28
     d = mp.generate(cfg)
     crng = np.random.default_rng(5000 + k)
-    labels = np.unique(d["inder"][d["inder"] > 0])
+    # the detector's labels 1..6 nmod (a label no record carries is dropped
+    # from its constraint by the job driver)
+    labels = np.arange(1, len(d["truth"]) + 1, dtype=np.int32)
     cs, cl, cc = list(d["conStart"]), list(d["conLabel"]), list(d["conCoef"])
     for _ in range(max(0, ncon - d["ncon"])):
         pick = crng.choice(labels, min(64, len(labels)), replace=False)
@@ -460,7 +463,7 @@ def serve_spec_job(mp, specs, k):
 
 
 def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmin=10_000, rmax=1_000_000,
-                       fp64="all", budget_gb=150, gen_threads=6, lookahead=12):
+                       fp64="all", budget_gb=150, gen_threads=2, lookahead=12):
     """The stream of alignment jobs at its specified shape: njobs jobs with
     Poisson arrivals at `rate` per second, each generated from its own seed
     (1000 + job) with the barrel detector model, as helix tracks (12 hits,
@@ -470,8 +473,8 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
     constraints of the barrel plus seeded sparse ones), 3 iterations with
     outlier down-weighting, dense tensor-core Cholesky + FP64 refinement
     (every size is at most 40,000), admitted by device footprint against
-    budget_gb, 4 jobs active.  Jobs are generated by a host thread pool
-    ahead of their arrival (at most `lookahead` in memory).  The same jobs
+    budget_gb, 4 jobs active.  Jobs are generated ahead of their arrival
+    (two at a time, each on six host threads; at most `lookahead` in memory).  The same jobs
     then run one at a time with the FP64 blocked solve (fp64 "all", or
     "every8" for every 8th job), whose latencies under the same arrivals are
     those of a first-come-first-served queue over the measured service

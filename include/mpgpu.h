@@ -561,6 +561,9 @@ typedef struct mpgen_cfg {
     double misal;              /* misalignment scale (cm) */
     double outlierFrac;        /* fraction of hits with 20x wider noise */
     double theta0;             /* multiple-scattering angle (rad) */
+    int32_t threads;           /* > 1: tracks generated on that many threads, each
+                                  track from its own random stream (seed, track);
+                                  other data than the sequential stream of <= 1 */
 } mpgen_cfg;
 
 int mpgen_count(const mpgen_cfg *cfg, int64_t *nrec, int64_t *nwords, int32_t *nlabels);

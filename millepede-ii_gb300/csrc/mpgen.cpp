@@ -22,9 +22,12 @@
 // Random numbers: xoshiro256** seeded by splitmix64 (public-domain
 // algorithms by Blackman & Vigna), Gaussian deviates by the Box-Muller
 // transform.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/mpgpu.h"
@@ -63,8 +66,8 @@ struct Writer {
     int64_t *recPtr; int32_t *inder; double *glder;
     int64_t nrec = 0, nw = 0;
     bool fill;
-    void beginRecord() {
-        if (fill) { recPtr[nrec] = nw; inder[nw] = 0; glder[nw] = 0.0; }
+    void beginRecord() {   // (recPtr[nrec] was set by the previous record's end, or is 0)
+        if (fill) { inder[nw] = 0; glder[nw] = 0.0; }
         nw++;
     }
     void endRecord() { nrec++; if (fill) recPtr[nrec] = nw; }
@@ -83,15 +86,22 @@ struct Writer {
 };
 
 // ---------------------------------------------------------------- kind 1
-void gen_telescope(const mpgen_cfg &c, Writer &w, double *truth) {
-    Rng rng(c.seed);
+// track t's own random stream when the tracks are generated in parallel
+// (cfg.threads > 1): seeded from (seed, t), so that any range of tracks can
+// be made on its own; otherwise every track continues the geometry's stream
+Rng track_rng(uint64_t seed, int64_t t) { return Rng(seed * 0x9E3779B97F4A7C15ull + (uint64_t)t + 1ull); }
+
+void gen_telescope(const mpgen_cfg &c, Writer &w, double *truth, int64_t t0, int64_t t1, bool perTrack) {
+    Rng rngG(c.seed);
     const int nl = c.nlayers, nm = c.nmod;
     const double pitch = 2.0, span = pitch * nm;
     std::vector<double> shift((size_t)nl * nm);
-    for (size_t i = 0; i < shift.size(); ++i) shift[i] = rng.uni(-c.misal, c.misal);
+    for (size_t i = 0; i < shift.size(); ++i) shift[i] = rngG.uni(-c.misal, c.misal);
     if (truth) for (size_t i = 0; i < shift.size(); ++i) truth[i] = shift[i];
     const double sig = c.sigma1;
-    for (int64_t t = 0; t < c.ntracks; ++t) {
+    for (int64_t t = t0; t < t1; ++t) {
+        Rng rngT = perTrack ? track_rng(c.seed, t) : Rng(0);
+        Rng &rng = perTrack ? rngT : rngG;
         double a, b;
         for (;;) {
             a = rng.uni(0.0, span);
@@ -162,16 +172,19 @@ void rigid_derivs(double u, double v, double tu, double tv, double gu[6], double
     gv[0] = 0.0; gv[1] = -1.0; gv[2] = tv; gv[3] = tv * v; gv[4] = -tv * u; gv[5] = u;
 }
 
-void gen_barrel(const mpgen_cfg &c, Writer &w, double *truth, bool brokenLines) {
-    Rng rng(c.seed);
+void gen_barrel(const mpgen_cfg &c, Writer &w, double *truth, bool brokenLines, int64_t t0, int64_t t1,
+                bool perTrack) {
+    Rng rngG(c.seed);
     Barrel B;
-    B.build(c.nmod, rng, c.misal);
+    B.build(c.nmod, rngG, c.misal);
     if (truth) for (size_t i = 0; i < B.mis.size(); ++i) truth[i] = B.mis[i];
     const double cs = std::cos(kStereo), sn = std::sin(kStereo);
     const double bfield = 0.006;  // 0.3 * 2 T, in 1/(GeV cm) after / 100
     const double twopi = 6.283185307179586;
     std::vector<double> dp(2 + 4 + 2 * 64);
-    for (int64_t t = 0; t < c.ntracks; ++t) {
+    for (int64_t t = t0; t < t1; ++t) {
+        Rng rngT = perTrack ? track_rng(c.seed, t) : Rng(0);
+        Rng &rng = perTrack ? rngT : rngG;
         // true track (for the hit positions)
         double pt = std::exp(rng.uni(std::log(1.0), std::log(100.0)));
         double q = rng.uni() < 0.5 ? -1.0 : 1.0;
@@ -279,14 +292,57 @@ void gen_barrel(const mpgen_cfg &c, Writer &w, double *truth, bool brokenLines) 
     }
 }
 
-int run(const mpgen_cfg *c, Writer &w, double *truth) {
-    if (!c) return 24;
+int run_range(const mpgen_cfg *c, Writer &w, double *truth, int64_t t0, int64_t t1, bool perTrack) {
     switch (c->kind) {
-    case 1: gen_telescope(*c, w, truth); return 0;
-    case 2: gen_barrel(*c, w, truth, false); return 0;
-    case 3: gen_barrel(*c, w, truth, true); return 0;
+    case 1: gen_telescope(*c, w, truth, t0, t1, perTrack); return 0;
+    case 2: gen_barrel(*c, w, truth, false, t0, t1, perTrack); return 0;
+    case 3: gen_barrel(*c, w, truth, true, t0, t1, perTrack); return 0;
     default: return 24;
     }
+}
+
+// all tracks; with cfg.threads > 1 in ranges on that many threads (a
+// counting pass per range gives each range its record and word offsets)
+int run(const mpgen_cfg *c, Writer &w, double *truth) {
+    if (!c) return 24;
+    if (c->kind < 1 || c->kind > 3) return 24;
+    const int nt = (int)std::min<int64_t>(std::max(c->threads, 1), std::max<int64_t>(c->ntracks / 1024, 1));
+    if (nt <= 1) return run_range(c, w, truth, 0, c->ntracks, false);
+    std::vector<int64_t> nr(nt + 1, 0), nwd(nt + 1, 0);
+    auto range = [&](int i) { return std::make_pair(c->ntracks * i / nt, c->ntracks * (i + 1) / nt); };
+    {
+        std::vector<std::thread> th;
+        for (int i = 0; i < nt; ++i)
+            th.emplace_back([&, i] {
+                Writer wc{nullptr, nullptr, nullptr};
+                wc.fill = false;
+                const auto r = range(i);
+                run_range(c, wc, nullptr, r.first, r.second, true);
+                nr[i + 1] = wc.nrec;
+                nwd[i + 1] = wc.nw;
+            });
+        for (std::thread &t : th) t.join();
+    }
+    for (int i = 0; i < nt; ++i) { nr[i + 1] += nr[i]; nwd[i + 1] += nwd[i]; }
+    if (!w.fill) {
+        w.nrec = nr[nt];
+        w.nw = nwd[nt];
+        return 0;
+    }
+    std::vector<std::thread> th;
+    for (int i = 0; i < nt; ++i)
+        th.emplace_back([&, i] {
+            Writer wf{w.recPtr, w.inder, w.glder};
+            wf.fill = true;
+            wf.nrec = nr[i];
+            wf.nw = nwd[i];
+            const auto r = range(i);
+            run_range(c, wf, i == 0 ? truth : nullptr, r.first, r.second, true);
+        });
+    for (std::thread &t : th) t.join();
+    w.nrec = nr[nt];
+    w.nw = nwd[nt];
+    return 0;
 }
 
 }  // namespace

@@ -127,7 +127,8 @@ class GenCfg(C.Structure):
     _fields_ = [("kind", C.c_int32), ("nlayers", C.c_int32), ("nmod", C.c_int32),
                 ("minHits", C.c_int32), ("maxHits", C.c_int32), ("ntracks", C.c_int64),
                 ("seed", C.c_uint64), ("sigma1", C.c_double), ("sigma2", C.c_double),
-                ("misal", C.c_double), ("outlierFrac", C.c_double), ("theta0", C.c_double)]
+                ("misal", C.c_double), ("outlierFrac", C.c_double), ("theta0", C.c_double),
+                ("threads", C.c_int32)]
 
 
 def ptr(a, t):
