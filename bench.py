@@ -463,7 +463,7 @@ def serve_spec_job(mp, specs, k):
 
 
 def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmin=10_000, rmax=1_000_000,
-                       fp64="all", budget_gb=150, gen_threads=2, lookahead=12):
+                       fp64="all", budget_gb=150, gen_threads=2, lookahead=12, max_active=4):
     """The stream of alignment jobs at its specified shape: njobs jobs with
     Poisson arrivals at `rate` per second, each generated from its own seed
     (1000 + job) with the barrel detector model, as helix tracks (12 hits,
@@ -473,7 +473,7 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
     constraints of the barrel plus seeded sparse ones), 3 iterations with
     outlier down-weighting, dense tensor-core Cholesky + FP64 refinement
     (every size is at most 40,000), admitted by device footprint against
-    budget_gb, 4 jobs active.  Jobs are generated ahead of their arrival
+    budget_gb, max_active jobs active.  Jobs are generated ahead of their arrival
     (two at a time, each on six host threads; at most `lookahead` in memory).  The same jobs
     then run one at a time with the FP64 blocked solve (fp64 "all", or
     "every8" for every 8th job), whose latencies under the same arrivals are
@@ -510,7 +510,7 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
         ahead(lookahead)
         keep = set(range(0, njobs, 8)) if fp64 == "every8" else set(range(njobs))
         if serve:
-            srv = mp.Server(device=local, max_active=4, budget_bytes=budget_gb << 30)
+            srv = mp.Server(device=local, max_active=max_active, budget_bytes=budget_gb << 30)
             tickets = []
             done = threading.Event()
 
@@ -575,7 +575,7 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
            "records": [min(o["nrec"] for o in served), max(o["nrec"] for o in served)],
            "models": {m: sum(1 for s in specs if s[0] == m) for m in ("barrel", "brokenlines")},
            "constraints": [min(o["ncon"] for o in served), max(o["ncon"] for o in served)],
-           "iterations": 3, "budget_gb": budget_gb, "max_active": 4, "solve": "metsol 31 (tensor-core factor, "
+           "iterations": 3, "budget_gb": budget_gb, "max_active": max_active, "solve": "metsol 31 (tensor-core factor, "
            "FP64 CG refinement, factor kept across the job's iterations)",
            "served_mixed": {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                             "jobs_per_s": njobs / span, "span_s": span, "ok": all(ok),
