@@ -219,6 +219,21 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
                        info.dxRel)
         ctx.close()
     ref = res[32][0]
+    # CPU baseline: the oracle's chdec2 (pede's method cholesky,
+    # mpnum.f90:891-987, one core) on the leading nsub rows of the same
+    # packed matrix, scaled by (n / nsub)^3
+    import oracle_ref as orc
+    nsub = min(2000, H.nVar)
+    with mp.Context(device=local) as ctx:
+        ctx.set_layout(H, 1)
+        ctx.upload(H)
+        ctx.loopbf(np.zeros(H.nTotal))
+        g = np.ascontiguousarray(ctx.matrix()[:nsub * (nsub + 1) // 2])
+    nrank, evmax, evmin = C.c_int32(), C.c_double(), C.c_double()
+    t0 = time.perf_counter()
+    orc.lib().mpref_chdec2(orc.ptr(g, orc.f64p), C.c_int32(nsub), C.byref(nrank), C.byref(evmax), C.byref(evmin))
+    cpu_s = time.perf_counter() - t0
+    cpu_est_ms = cpu_s * 1e3 * (H.nVar / nsub) ** 3
 
     def rel(x, r=ref):
         return float(np.max(np.abs(x - r)) / np.max(np.abs(r)))
@@ -238,7 +253,11 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
            "cg_iterations_mixed": res[31][2], "cg_iterations_fp64": res[32][2],
            "last_rel_correction_mixed": res[31][8], "last_rel_correction_fp64": res[32][8],
            "rel_err_mixed_vs_fp64": rel(res[31][0]),
-           "converged": bool(res[31][3] == 1 and res[32][3] == 1)}
+           "converged": bool(res[31][3] == 1 and res[32][3] == 1),
+           "cpu_baseline": {"value": cpu_est_ms, "unit": "ms", "cores": 1, "kind": "port",
+                            "sample": f"oracle chdec2 on the leading {nsub} rows ({cpu_s:.2f} s), "
+                                      f"scaled by (n/{nsub})^3"},
+           "speedup_mixed_vs_cpu_chdec2_estimate": cpu_est_ms / res[31][1]}
     if 3 in res:
         out["ms_fp64_chdec2"] = res[3][1]
         out["speedup_mixed_vs_fp64_chdec2"] = res[3][1] / res[31][1]
@@ -669,8 +688,13 @@ def brokenlines_measure(mp, device, nrec, ncores, steps=2):
     hits, nloc 8-84, nalg 24-240; sparse storage): device data loops with
     the records in fit size classes (tuned warps per CTA), with one launch
     sized for the largest record, and with one record per CTA; the CPU
-    oracle on a sample."""
-    d = mp.generate(mp.gen_config("brokenlines", ntracks=nrec, seed=3))
+    oracle on a sample; then the same records as a whole job solved by the
+    tensor-core Cholesky (metsol 31, full storage, 18 constraints
+    eliminated, one iteration).  The tracks are generated on all host
+    threads, each from its own seeded stream."""
+    cfg = mp.gen_config("brokenlines", ntracks=nrec, seed=3)
+    cfg.threads = ncores
+    d = mp.generate(cfg)
     H = mp.HostStructure(d, mreqenf=25)
     gpar = np.zeros(H.nTotal)
     out = {"records": nrec, "hits": [4, 40], "nloc": [8, 84]}
@@ -695,6 +719,16 @@ def brokenlines_measure(mp, device, nrec, ncores, steps=2):
         out[name] = e
     base = out["one_record_per_block"]["records_per_s"]
     out["speedup_size_classes_vs_one_record_per_block"] = out["size_classes"]["records_per_s"] / base
+    # the configuration's solve: method cholesky of the 30,000 globals
+    jd = mp.JobData(d, metsol=31, matsto=1, mitera=1, mreqenf=25, mrestl=1e-13, itnlim=2000)
+    with mp.Context(device=device) as ctx:
+        t0 = time.perf_counter()
+        rc = mp.run_job(jd, ctx)
+        wall = time.perf_counter() - t0
+    r = jd.res
+    out["cholesky_job"] = {"rc": int(rc), "metsol": 31, "globals": int(r.nVar), "constraints": 18,
+                           "wall_s": wall, "ms_structure": r.msStructure, "ms_upload": r.msUpload,
+                           "ms_loop": r.msLoops, "ms_solve": r.msSolves, "cg_iterations": int(r.minresItn)}
     nsample = min(5000, nrec)
     val, _ = cpu_reference(d, nsample, ncores, steps=1)
     out["cpu_baseline"] = {"value": val, "unit": "records/s", "cores": ncores, "kind": "port",
@@ -800,7 +834,7 @@ def main():
     ap.add_argument("--serve-jobs", type=int, default=24, help="jobs of the serving measurement (0: skip)")
     ap.add_argument("--part", default="loop", choices=["loop", "upload", "structure", "brokenlines", "minres"],
                     help="with --profile: the part to run on --ntracks records (for profilers)")
-    ap.add_argument("--brokenlines", type=int, default=200_000,
+    ap.add_argument("--brokenlines", type=int, default=1_000_000,
                     help="records of the uneven-record (broken-line) measurement (0: skip)")
     args = ap.parse_args()
     rank, world, local, pg = dist_setup(args.gpus)

@@ -377,7 +377,9 @@ typedef struct mpgpu_steer {
     int32_t lhuber;     /* outlierdownweighting */
     float chicut, chirem, chhuge, dwcut, cndlmx;
     int32_t lfitbb;
-    int32_t mreqenf, mreqena, mreqpe;
+    int32_t mreqenf, mreqena, mreqpe;   /* mreqpe: pede's pairentries; only 1 (every pair
+                                           met in a record is stored) is built, larger
+                                           values are refused with status 44 */
     double mrestl;
     int32_t itnlim;
     int32_t nthreads;   /* host threads for the structure passes */

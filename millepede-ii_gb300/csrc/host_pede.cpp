@@ -402,6 +402,13 @@ void feasib(const mpgpu_job *job, const std::vector<int32_t> &lab, const int32_t
 int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job, mpgpu_result *res,
                           const std::function<bool(int64_t)> &admit) {
     if (!st || !job || !res) return MPGPU_ERR_ARG;
+    // pairentries > 1 (pairs met in fewer records left out of the sparse
+    // matrix, clbits/inbits mpbits.f90:182-243) is not built: refused rather
+    // than run with every pair stored
+    if (st->mreqpe > 1) {
+        res->exitCode = MPGPU_ERR_ARG;
+        return MPGPU_ERR_ARG;
+    }
     using Clock = std::chrono::steady_clock;
     const auto msSince = [](Clock::time_point a) {
         return std::chrono::duration<double, std::milli>(Clock::now() - a).count();

@@ -1,5 +1,6 @@
 """Dense blocked Cholesky through the C-ABI (mpgpu_dense_cholesky) against
-numpy on seeded SPD matrices: FP64 form within 1e-12 relative of numpy's
+numpy on seeded SPD matrices (up to n = 2,100: five block columns, the
+last one ragged): FP64 form within 1e-12 relative of numpy's
 factor; tensor-core 3xTF32 form within 1e-4 relative (its trailing updates
 are products of TF32 pairs accumulated in FP32 over a block column of up to
 512 columns, then subtracted from the FP64 matrix)."""
@@ -16,7 +17,7 @@ def spd(n, seed, cond=1e4):
     return (Q * ev) @ Q.T
 
 
-@pytest.mark.parametrize("n", [128, 200, 640])
+@pytest.mark.parametrize("n", [128, 200, 640, 2100])
 @pytest.mark.parametrize("mode,tol", [(0, 1e-12), (1, 1e-4)])
 def test_dense_cholesky(mp, n, mode, tol):
     A = spd(n, n)
