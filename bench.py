@@ -220,15 +220,20 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
         ctx.close()
     ref = res[32][0]
     # CPU baseline: the oracle's chdec2 (pede's method cholesky,
-    # mpnum.f90:891-987, one core) on the leading nsub rows of the same
-    # packed matrix, scaled by (n / nsub)^3
+    # mpnum.f90:891-987, one core) on the same telescope with 2,000 globals
+    # (200 modules per layer, tracks in proportion), scaled by (n / 2000)^3
     import oracle_ref as orc
-    nsub = min(2000, H.nVar)
+    nsub = 2000
+    cfg_s = mp.gen_config("telescope_dense", ntracks=max(ntracks * 200 // nmod, 1000), seed=4)
+    cfg_s.nmod = 200
+    d_s = mp.generate(cfg_s)
+    H_s = mp.HostStructure(d_s, mreqenf=5, sparse=False)
+    nsub = H_s.nVar
     with mp.Context(device=local) as ctx:
-        ctx.set_layout(H, 1)
-        ctx.upload(H)
-        ctx.loopbf(np.zeros(H.nTotal))
-        g = np.ascontiguousarray(ctx.matrix()[:nsub * (nsub + 1) // 2])
+        ctx.set_layout(H_s, 1)
+        ctx.upload(H_s)
+        ctx.loopbf(np.zeros(H_s.nTotal))
+        g = np.ascontiguousarray(ctx.matrix())
     nrank, evmax, evmin = C.c_int32(), C.c_double(), C.c_double()
     t0 = time.perf_counter()
     orc.lib().mpref_chdec2(orc.ptr(g, orc.f64p), C.c_int32(nsub), C.byref(nrank), C.byref(evmax), C.byref(evmin))
@@ -255,8 +260,8 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
            "rel_err_mixed_vs_fp64": rel(res[31][0]),
            "converged": bool(res[31][3] == 1 and res[32][3] == 1),
            "cpu_baseline": {"value": cpu_est_ms, "unit": "ms", "cores": 1, "kind": "port",
-                            "sample": f"oracle chdec2 on the leading {nsub} rows ({cpu_s:.2f} s), "
-                                      f"scaled by (n/{nsub})^3"},
+                            "sample": f"oracle chdec2 of the same telescope with {nsub} globals "
+                                      f"({cpu_s:.2f} s), scaled by (n/{nsub})^3"},
            "speedup_mixed_vs_cpu_chdec2_estimate": cpu_est_ms / res[31][1]}
     if 3 in res:
         out["ms_fp64_chdec2"] = res[3][1]
@@ -277,23 +282,33 @@ def dense_solve_measure(mp, local, ncon=120, nmod=2000, ntracks=400_000, sqminl=
     return out
 
 
-def whole_job_measure(mp, d, local, cpu_loop_rate, cpu_minres_ms):
+def whole_job_measure(mp, d, local, cpu_loop_rate, cpu_minres_ms, pinned=None):
     """The 2M-record barrel as a whole job through mpgpu_pede_run: structure
     passes on the device, mpbits-sparse storage, 18 constraints eliminated,
     three solutions by MINRES with the diagonal preconditioner to a relative
     residual of 1e-12, outlier down-weighting in the second and third data
     loop (lhuber 2), chi2 cuts 30 then 6.  Wall time of the call; the CPU
     estimate is three loops at the measured CPU loop rate plus the MINRES
-    iterations at the measured CPU time per iteration."""
+    iterations at the measured CPU time per iteration.  The records come
+    from page-locked host buffers (recPtr and glder of the e2e steps, the
+    raw labels copied into one more)."""
+    raw = None
+    if pinned is not None:
+        raw = mp.PinnedArray(np.asarray(d["inder"]))
+        d = dict(d, recPtr=pinned[0].a, inder=raw.a, glder=pinned[2].a)
     jd = mp.JobData(d, metsol=4, matsto=2, mitera=3, lhuber=2, chicut=30.0, chirem=6.0, mrestl=1e-12,
                     itnlim=6000, mreqenf=25, structDevice=1)
     t0 = time.perf_counter()
     rc = mp.run_job(jd)
     wall = time.perf_counter() - t0
+    if raw is not None:
+        raw.free()
     nrec = len(d["recPtr"]) - 1
     out = {"records": nrec, "rc": int(rc), "wall_s": wall, "solutions": 3, "metsol": 4, "rtol": 1e-12,
            "nrej_last": [int(v) for v in jd.res.nrej], "minres_iterations_last": int(jd.res.minresItn),
            "minres_istop_last": int(jd.res.minresIstop), "ms_loop_last": jd.res.msBuild,
+           "ms_structure": jd.res.msStructure, "ms_upload": jd.res.msUpload, "ms_loops": jd.res.msLoops,
+           "ms_solves": jd.res.msSolves, "ms_host_between": jd.res.msHostIter,
            "ms_solve_last": jd.res.msSolve}
     if cpu_loop_rate and cpu_minres_ms:
         est = 3 * nrec / cpu_loop_rate + 3 * jd.res.minresItn * cpu_minres_ms * 1e-3
@@ -573,7 +588,9 @@ def serve_spec_measure(mp, local, njobs=256, rate=4.0, nmin=500, nmax=40000, rmi
                     continue
                 jd = mp.JobData(d, constraints=con, metsol=metsol, **steer)
                 del d
-                ctx = mp.Context(device=local)
+                # the serving workers' fixed 8 GiB update staging (the same
+                # chunking, so the same loop sums as in the served stream)
+                ctx = mp.Context(device=local, staging_bytes=8 << 30)
                 t1 = time.perf_counter()
                 rc = mp.run_job(jd, ctx)
                 ms = (time.perf_counter() - t1) * 1e3
@@ -995,7 +1012,8 @@ def main():
         if args.whole_job:
             cpu_rate = line.get("cpu_baseline", {}).get("value")
             line["whole_job"] = whole_job_measure(mp, d, local, cpu_rate,
-                                                  line["minres"]["cpu_baseline"]["ms_per_iteration"])
+                                                  line["minres"]["cpu_baseline"]["ms_per_iteration"],
+                                                  pinned=pinned)
     if args.dense_n > 0 and rank == 0 and not args.profile:
         line["dense_solve"] = dense_solve_measure(mp, local, nmod=args.dense_n // 10,
                                                   ntracks=20 * args.dense_n, sqminl=args.dense_sqminl,

@@ -644,10 +644,18 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         cudaEventCreate(&evF0[ch]); cudaEventCreate(&evF1[ch]);
         cudaEventCreate(&evA0[ch]); cudaEventCreate(&evA1[ch]);
     }
+    int32_t launches = 0;
+    const int32_t nf = j.nfiles;
+    int64_t *iout = (int64_t *)(c->scal + 8);
+    double *dout = c->scal + 4;
+    float *fout = (float *)(c->scal + 256);
+    const int64_t nint = 9 + 2 * (int64_t)nf;
+    if (nint > 240 || nf > 400) return set_err(c, MPGPU_ERR_LIMIT, "too many files for the statistics buffer");
+    auto body = [&]() -> int32_t {
+    launches = 0;
     cudaEventRecord(evStart, s);
     cudaEventRecord(evZero, s);
     MPG_CUDA(c, cudaStreamWaitEvent(s2, evZero, 0));
-    int32_t launches = 0;
     for (int64_t ch = 0; ch < nchunk; ++ch) {
         fp.r0 = j.chunkRec[ch];
         fp.r1 = j.chunkRec[ch + 1];
@@ -688,18 +696,22 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
     }
     if (nchunk > 0) MPG_CUDA(c, cudaStreamWaitEvent(s, evA1[nchunk - 1], 0));
     // statistics
-    const int32_t nf = j.nfiles;
-    int64_t *iout = (int64_t *)(c->scal + 8);
-    double *dout = c->scal + 4;
-    float *fout = (float *)(c->scal + 256);
-    const int64_t nint = 9 + 2 * (int64_t)nf;
-    if (nint > 240 || nf > 400) return set_err(c, MPGPU_ERR_LIMIT, "too many files for the statistics buffer");
     MPG_CUDA(c, cudaMemsetAsync(iout, 0, sizeof(int64_t) * nint, s));
     StatParams sp{j.status, j.chi2add, j.ndfadd, j.chndf, j.rec, j.fileWeight, j.nrec, nf,
                   dout, iout, fout};
     MPG_CUDA(c, launch_stats(sp, s));
     launches += 2;
     cudaEventRecord(evEnd, s);
+    return MPGPU_OK;
+    };
+    {
+        // direct launches: the per-chunk fit and accumulation times come
+        // from events on the launching streams, which a captured graph's
+        // event nodes do not give
+        const int32_t rcb = body();
+        if (rcb != MPGPU_OK) return rcb;
+        c->loopGraphed = false;
+    }
     MPG_CUDA(c, cudaMemcpyAsync(c->hscal, c->scal, 4096, cudaMemcpyDeviceToHost, s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
     double msFit = 0.0, msAcc = 0.0;
@@ -738,6 +750,7 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         stats->msAccum = msAcc;
         stats->msLoop = msLoop;
         stats->launches = launches;
+        stats->graphed = c->loopGraphed ? 1 : 0;
     }
     c->lastNaccepted = hi[8];
     for (int32_t f = 0; f < nf; ++f) {

@@ -681,8 +681,7 @@ __global__ void k_mr_y2(int32_t n, const MinresState *S, double *y, double *r1, 
     }
 }
 
-__global__ void k_mr_rot(MinresState *S) {
-    if (threadIdx.x || S->done) return;
+__device__ void mr_rot_body(MinresState *S) {
     double b2 = S->dotv;
     if (b2 < 0.0) { S->istop = 9; S->done = 1; return; }
     S->oldb = S->beta;
@@ -706,6 +705,11 @@ __global__ void k_mr_rot(MinresState *S) {
     S->gmin = fmin(S->gmin, gamma);
 }
 
+__global__ void k_mr_rot(MinresState *S) {
+    if (threadIdx.x || S->done) return;
+    mr_rot_body(S);
+}
+
 __global__ void k_mr_w(int32_t n, const MinresState *S, const double *v, double *w, double *w1, double *w2,
                        double *x) {
     if (S->done) return;
@@ -720,8 +724,7 @@ __global__ void k_mr_w(int32_t n, const MinresState *S, const double *v, double 
     }
 }
 
-__global__ void k_mr_test(MinresState *S) {
-    if (threadIdx.x || S->done) return;
+__device__ void mr_test_body(MinresState *S) {
     S->itn += 1;
     S->Anorm = sqrt(S->tnorm2);
     S->ynorm = sqrt(S->dotv);
@@ -735,6 +738,102 @@ __global__ void k_mr_test(MinresState *S) {
     if (test2 <= S->rtol) istop = 2;
     if (test1 <= S->rtol) istop = 1;
     if (istop) { S->istop = istop; S->done = 1; }
+}
+
+__global__ void k_mr_test(MinresState *S) {
+    if (threadIdx.x || S->done) return;
+    mr_test_body(S);
+}
+
+// Fused forms of one MINRES iteration (diagonal or no preconditioner): each
+// vector update also forms its dot product's partial sums with the grid and
+// element order of k_dot_partial (kDotBlocks x kThreads, grid-stride), and
+// each scalar step sums the partials as k_sum_final does, so the iterates
+// are bit-identical to the unfused sequence with half the launches.
+__global__ void k_mr_v_pad(int32_t nfit, int32_t n, const MinresState *S, const double *y, double *v, double *xa) {
+    if (S->done) return;
+    const double s = 1.0 / S->beta;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double vi = 0.0;
+        if (i < nfit) {
+            vi = s * y[i];
+            v[i] = vi;
+        }
+        xa[i] = vi;
+    }
+}
+
+// y = ba - (beta / oldbeta) r1 (from the second iteration on), partials of v . y
+__global__ void k_mr_y1_dot(int32_t n, const MinresState *S, const double *ba, double *y, const double *r1,
+                            const double *v, double *part) {
+    __shared__ double sh[kThreads];
+    if (S->done) return;
+    const bool upd = S->itn >= 1;
+    const double f = upd ? S->beta / S->oldb : 0.0;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double yi = ba[i];
+        if (upd) yi = yi - f * r1[i];
+        y[i] = yi;
+        acc += v[i] * yi;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// k_mr_y2, partials of r2 . y
+__global__ void k_mr_y2_dot(int32_t n, const MinresState *S, double *y, double *r1, double *r2, const double *cu,
+                            double *part) {
+    __shared__ double sh[kThreads];
+    if (S->done) return;
+    const double f = S->alfa / S->beta;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double yi = y[i] - f * r2[i];
+        r1[i] = r2[i];
+        r2[i] = yi;
+        const double zi = (yi * cu[i]) * cu[i];
+        y[i] = zi;
+        acc += yi * zi;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// k_mr_w, partials of x . x
+__global__ void k_mr_w_dot(int32_t n, const MinresState *S, const double *v, double *w, double *w1, double *w2,
+                           double *x, double *part) {
+    __shared__ double sh[kThreads];
+    if (S->done) return;
+    const double oe = S->oldeps, de = S->delta, dn = S->denom, ph = S->phi;
+    double acc = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double a = w2[i], b = w[i];
+        w1[i] = a;
+        w2[i] = b;
+        const double wn = (v[i] - oe * a - de * b) * dn;
+        w[i] = wn;
+        const double xi = x[i] + ph * wn;
+        x[i] = xi;
+        acc += xi * xi;
+    }
+    acc = block_sum(acc, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+// the partials summed as k_sum_final, then the scalar step: 0 alfa, 1 the
+// rotation, 2 the convergence test
+__global__ void k_mr_sum_step(const double *part, int np, MinresState *S, int step) {
+    __shared__ double sh[kThreads];
+    if (S->done) return;
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) acc += part[i];
+    acc = block_sum(acc, sh);
+    if (threadIdx.x) return;
+    S->dotv = acc;
+    if (step == 0) S->alfa = acc;
+    else if (step == 1) mr_rot_body(S);
+    else mr_test_body(S);
 }
 
 // MINRES-QLP (Choi, Paige & Saunders 2011; minresqlpModule.f90:411-1333 in
@@ -943,18 +1042,29 @@ struct Solver {
     // packed symmetric product (two passes; buffers kept for the solve)
     double *pmvRow = nullptr, *pmvPart = nullptr;
     int64_t pmvN = 0;
-    void alloc_pmv(int32_t n) {
-        if (pmvN == n) return;
+    // scratch of the packed product; a failed allocation leaves none (the
+    // product is then not launched and pmvFailed is set)
+    cudaError_t alloc_pmv(int32_t n) {
+        if (pmvN == n && pmvRow && pmvPart) return cudaSuccess;
         const int64_t nb = ((int64_t)n + kMvRows - 1) / kMvRows;
         dfree(pmvRow);
         dfree(pmvPart);
-        cudaMalloc(&pmvRow, sizeof(double) * std::max<int64_t>(n, 1));
-        cudaMalloc(&pmvPart, sizeof(double) * std::max<int64_t>(nb * n, 1));
+        pmvN = -1;
+        cudaError_t e = cudaMalloc(&pmvRow, sizeof(double) * std::max<int64_t>(n, 1));
+        if (e == cudaSuccess) e = cudaMalloc(&pmvPart, sizeof(double) * std::max<int64_t>(nb * n, 1));
+        if (e != cudaSuccess) {
+            dfree(pmvRow);
+            dfree(pmvPart);
+            pmvFailed = true;
+            return e;
+        }
         pmvN = n;
+        return cudaSuccess;
     }
+    bool pmvFailed = false;
     void packed_matvec(int32_t n, const double *A, const double *x, double *y) {
         const int64_t nb = ((int64_t)n + kMvRows - 1) / kMvRows;
-        alloc_pmv(n);
+        if (alloc_pmv(n) != cudaSuccess) return;
         k_pmv_blocks<<<(unsigned)nb, 256, 0, s>>>(n, A, x, pmvRow, pmvPart);
         k_pmv_final<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nb, pmvRow, pmvPart, y);
     }
@@ -1196,6 +1306,7 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
     DevJob &j = c->j;
     cudaStream_t s = c->stream;
     const int32_t n = j.nVar, ncon = j.ncon, nfit = n - ncon;
+    if (j.matsto != 2 && ncon > 0) MPG_CUDA(c, S.alloc_pmv(n));   // the packed products of qlssq
     // per-solve vectors from the stream-ordered pool: a cudaFree would wait
     // for the whole device, i.e. for the other jobs' work in a served mix
     struct Tmp {
@@ -1258,6 +1369,7 @@ int32_t solve_inversion(mpgpu_ctx *c, const double *consResiduals, double *corrO
             k_cons_rhs<<<S.grid(nfit), kThreads, 0, s>>>(nfit, ncon, j.matD, yv, corr);
         }
     }
+    if (S.pmvFailed) return set_err(c, MPGPU_ERR_ALLOC, "packed product scratch");
     int nrank = 0;
     if (!decomposition && dense < 0) {
         // sqminl (mpnum.f90:230-355) on the leading nfit x nfit block
@@ -1346,6 +1458,8 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     if (j.matsto == 2) {
         int32_t rc = S.build_blocks();
         if (rc) return rc;
+    } else {
+        MPG_CUDA(c, S.alloc_pmv(n));
     }
     MPG_CUDA(c, cudaMallocAsync(&S.part, sizeof(double) * (kDotBlocks + 8), s));
     // workspace released on every return
@@ -1446,8 +1560,22 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
     // the iterations of one batch are recorded once as a CUDA graph and
     // replayed (all scalars live on the device); direct launches if the
     // capture is refused
+    const bool fused = !qlp && mbandw <= 0;
     auto batchBody = [&] {
         for (int q = 0; q < batch; ++q) {
+            if (fused) {
+                k_mr_v_pad<<<S.grid(n), kThreads, 0, s>>>(nfit, n, St, y, v, xa);
+                S.qlmlq(xa, 0);
+                S.avprd0(xa, ba);
+                S.qlmlq(ba, 1);
+                k_mr_y1_dot<<<kDotBlocks, kThreads, 0, s>>>(nfit, St, ba, y, r1, v, S.part);
+                k_mr_sum_step<<<1, kThreads, 0, s>>>(S.part, kDotBlocks, St, 0);
+                k_mr_y2_dot<<<kDotBlocks, kThreads, 0, s>>>(nfit, St, y, r1, r2, cu, S.part);
+                k_mr_sum_step<<<1, kThreads, 0, s>>>(S.part, kDotBlocks, St, 1);
+                k_mr_w_dot<<<kDotBlocks, kThreads, 0, s>>>(nfit, St, v, w, w1, w2, x, S.part);
+                k_mr_sum_step<<<1, kThreads, 0, s>>>(S.part, kDotBlocks, St, 2);
+                continue;
+            }
             k_mr_scale_v<<<S.grid(nfit), kThreads, 0, s>>>(nfit, St, y, v);
             // y = (Q^T A Q v)(1:nfit)
             k_copy_pad<<<S.grid(n), kThreads, 0, s>>>(nfit, n, v, xa);
@@ -1475,7 +1603,7 @@ int32_t solve_minres(mpgpu_ctx *c, const double *consResiduals, double rtol, int
             }
         }
     };
-    if (j.matsto != 2) S.alloc_pmv(n);  // no allocation while the graph is recorded
+    if (j.matsto != 2) MPG_CUDA(c, S.alloc_pmv(n));  // no allocation while the graph is recorded
     struct GraphGuard {
         cudaGraph_t g = nullptr;
         cudaGraphExec_t e = nullptr;
@@ -1523,6 +1651,8 @@ int32_t avprod_host(mpgpu_ctx *c, int32_t n, const double *x, double *b) {
     if (j.matsto == 2) {
         int32_t rc = S.build_blocks();
         if (rc) return rc;
+    } else {
+        MPG_CUDA(c, S.alloc_pmv(j.nVar));
     }
     double *xa = nullptr, *ba = nullptr;
     MPG_CUDA(c, cudaMalloc(&xa, sizeof(double) * j.nVar));
@@ -1551,6 +1681,8 @@ int32_t band_precond_factor(mpgpu_ctx *c, int32_t mbandw, int32_t lprecm, double
     if (j.matsto == 2) {
         int32_t rc = S.build_blocks();
         if (rc) return rc;
+    } else {
+        MPG_CUDA(c, S.alloc_pmv(n));
     }
     MPG_CUDA(c, cudaMallocAsync(&S.part, sizeof(double) * (kDotBlocks + 8), s));
     struct Bufs {

@@ -91,6 +91,8 @@ def test_deterministic_repeat(mp):
         b = ctx.loopbf(np.zeros(H.nTotal))
         mb = ctx.matrix()
     assert np.array_equal(ma, mb) and np.array_equal(a["gvec"], b["gvec"])
+    # device times of the fit and the accumulation from events on their streams
+    assert b["msFit"] > 0 and b["msAccum"] > 0 and b["msLoop"] >= b["msFit"]
 
 
 def test_chunking_consistent(mp):
