@@ -955,9 +955,17 @@ def main():
     acc_bytes = 8.0 * ngg * nrec + 16.0 * ctx.nmat
     acc_ms = statistics.median(ms_acc)
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # DRAM traffic of k_fit per record from one ncu capture of the barrel
+    # (dram__bytes_read.sum + dram__bytes_write.sum of a launch over a sample
+    # of 45.5k records: 331 MB read, 961 MB written), scaled to this launch's
+    # records; the writes are the block-major staging (21.1 KB per record)
+    traffic_per_record = (331.5e6 + 961.3e6) / 45.5e3
     roof = {"bound": "fp64", "kernel": "k_fit (local fit + Schur update)",
             "achieved": achieved, "peak": fp64.value, "unit": "TFLOP/s",
-            "frac": achieved / fp64.value if fp64.value else None, "traffic": None,
+            "frac": achieved / fp64.value if fp64.value else None,
+            "traffic": traffic_per_record * nrec,
+            "traffic_source": "ncu dram bytes of one k_fit launch on a 45.5k-record barrel sample, "
+                              "scaled per record",
             "flops_per_record": fpr,
             "peak_source": "FP64 FMA throughput measured in this run (mpgpu_probe_fp64)",
             "accumulate": {"bound": "hbm", "achieved": acc_bytes / (acc_ms * 1e-3) / 1e9,
