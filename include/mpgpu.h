@@ -213,8 +213,7 @@ typedef struct mpgpu_fitstats {
     double msAccum;     /* device time of the accumulation kernels */
     double msLoop;      /* device time of the whole data loop */
     int32_t launches;   /* kernels launched by the loop */
-    int32_t graphed;    /* 1: the loop's launches ran as one captured CUDA graph (0: direct
-                           launches, which the per-kernel event times need) */
+    int32_t pad;
 } mpgpu_fitstats;
 
 /* One data loop (loopbf): local fits of all records with the given global

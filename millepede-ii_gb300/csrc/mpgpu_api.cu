@@ -710,7 +710,6 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         // event nodes do not give
         const int32_t rcb = body();
         if (rcb != MPGPU_OK) return rcb;
-        c->loopGraphed = false;
     }
     MPG_CUDA(c, cudaMemcpyAsync(c->hscal, c->scal, 4096, cudaMemcpyDeviceToHost, s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
@@ -750,7 +749,6 @@ static int32_t run_loop(mpgpu_ctx *c, const mpgpu_fitopts *opt, mpgpu_fitstats *
         stats->msAccum = msAcc;
         stats->msLoop = msLoop;
         stats->launches = launches;
-        stats->graphed = c->loopGraphed ? 1 : 0;
     }
     c->lastNaccepted = hi[8];
     for (int32_t f = 0; f < nf; ++f) {

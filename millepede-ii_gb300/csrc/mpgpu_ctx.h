@@ -203,7 +203,6 @@ struct mpgpu_ctx {
     int32_t mbandw = 0;          // MINRES preconditioner: < 0 none, 0 diagonal, > 0 band width
     int32_t lprecm = 0;          // lltdec option of the band preconditioner
     DenseResident *dense = nullptr;  // kept between the dense solves of a job
-    bool loopGraphed = false;        // the last data loop ran as a captured CUDA graph
 };
 
 // variable-band preconditioner of MINRES (mpgpu_precond.cu): band of

@@ -71,7 +71,7 @@ class FitStats(C.Structure):
                 ("ndfSum", C.c_int64), ("ndfSumW", C.c_double), ("nbndr", C.c_int32 * 2),
                 ("nbdrx", C.c_int32), ("nbndx", C.c_int32), ("naccepted", C.c_int64),
                 ("msFit", C.c_double), ("msAccum", C.c_double), ("msLoop", C.c_double),
-                ("launches", C.c_int32), ("graphed", C.c_int32)]
+                ("launches", C.c_int32), ("pad", C.c_int32)]
 
 
 class SolveInfo(C.Structure):
@@ -513,8 +513,7 @@ class Context:
         return dict(gvec=gvec, gcnt=gcnt, nrej=list(st.nrej), chi2=st.chi2SumD + st.chi2SumI,
                     ndf=st.ndfSum, naccepted=st.naccepted, nbndr=list(st.nbndr),
                     nbdrx=st.nbdrx, nbndx=st.nbndx, naccf=naccf, chi2f=chi2f, ndff=ndff,
-                    msFit=st.msFit, msAccum=st.msAccum, msLoop=st.msLoop, launches=st.launches,
-                    graphed=st.graphed)
+                    msFit=st.msFit, msAccum=st.msAccum, msLoop=st.msLoop, launches=st.launches)
 
     def matrix(self):
         m = np.zeros(self.nmat, np.float64)
