@@ -433,7 +433,9 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     // structure passes on the device: the records are copied once and stay
     // there translated (not under an admission hook, which must see the
     // footprint before any device allocation of the job)
-    const bool onDevice = st->structDevice != 0 && !admit;
+    // (measurement lines in sparse storage add structure-only records, which
+    // the host passes take)
+    const bool onDevice = st->structDevice != 0 && !admit && !(st->matsto == 2 && job->nmeas > 0);
     int32_t ntot = onDevice
                        ? mpgpu_loop1_device(ctx, job->nrec, job->recPtr, job->inder, job->glder,
                                             (int32_t)steer.size(), steer.data(), job->npar, job->parLabel,
@@ -471,6 +473,45 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     std::vector<int64_t> offsets;
     std::vector<int32_t> columns;
     int64_t ncolw = 0, nmat = 0;
+    // the parameter pairs of the measurement lines belong to the sparse
+    // structure whatever the records hold (pede.f90:7007-7042, increment
+    // mreqpe: always kept): one structure-only record per measurement line
+    // (header, value, positive sigma, its labels as global words)
+    int64_t nrecS = job->nrec;
+    const int64_t *rpS = job->recPtr;
+    const int32_t *inS = tinder.data();
+    const double *glS = job->glder;
+    std::vector<int64_t> rpA;
+    std::vector<int32_t> inA;
+    std::vector<double> glA;
+    if (st->matsto == 2 && job->nmeas > 0) {
+        std::vector<int64_t> rpRaw(1, 0);
+        std::vector<int32_t> raw;
+        std::vector<double> glRaw;
+        for (int32_t m = 0; m < job->nmeas; ++m) {
+            for (int k = 0; k < 3; ++k) {
+                raw.push_back(0);
+                glRaw.push_back(k == 2 ? 1.0 : 0.0);
+            }
+            for (int32_t q = job->msStart[m]; q < job->msStart[m + 1]; ++q) {
+                raw.push_back(job->msLabel[q]);
+                glRaw.push_back(1.0);
+            }
+            rpRaw.push_back((int64_t)raw.size());
+        }
+        std::vector<int32_t> trRaw(raw.size());
+        mpgpu_host_translate(job->nmeas, rpRaw.data(), raw.data(), glRaw.data(), ntot, res->labels, trRaw.data());
+        rpA.assign(job->recPtr, job->recPtr + job->nrec + 1);
+        for (int32_t m = 1; m <= job->nmeas; ++m) rpA.push_back(nw + rpRaw[m]);
+        inA.assign(tinder.begin(), tinder.end());
+        inA.insert(inA.end(), trRaw.begin(), trRaw.end());
+        glA.assign(job->glder, job->glder + nw);
+        glA.insert(glA.end(), glRaw.begin(), glRaw.end());
+        nrecS = job->nrec + job->nmeas;
+        rpS = rpA.data();
+        inS = inA.data();
+        glS = glA.data();
+    }
     if (st->matsto == 2) {
         offsets.resize(2 * (nG + 1));
         int64_t capc = 1 << 20;
@@ -479,7 +520,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
             const int32_t r2 =
                 onDevice ? mpgpu_loop2_device(ctx, res->varIndex, nVar, nG, aig.data(), capc, offsets.data(),
                                               columns.data(), &ncolw, &nmat)
-                         : mpgpu_host_mpbits(job->nrec, job->recPtr, tinder.data(), job->glder, res->varIndex, nVar,
+                         : mpgpu_host_mpbits(nrecS, rpS, inS, glS, res->varIndex, nVar,
                                              nG, aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat);
             if (r2 == 0) break;
             if (r2 != -1) {
@@ -656,8 +697,9 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         double chi2D = fs.chi2SumD;
         int64_t chi2I = fs.chi2SumI, ndfS = fs.ndfSum;
         // measurement lines (loopn, pede.f90:2743-2798)
+        std::vector<int32_t> vi;   // their variable entries (each adds 1 to globalCounter)
         if (job->nmeas > 0) {
-            std::vector<int32_t> mi, mj, vi;
+            std::vector<int32_t> mi, mj;
             std::vector<double> ma, va;
             for (int32_t m = 0; m < job->nmeas; ++m) {
                 const double rhs = job->msRhs[m], sgm = job->msSigma[m];
@@ -696,6 +738,7 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         res->ndf = ndfS;
         rc = mpgpu_download_vector(ctx, nullptr, gcnt.data());
         if (rc) break;
+        for (int32_t iv : vi) gcnt[iv - 1] += 1;
         // addcst: constraint residuals d - C p
         for (int32_t c = 0; c < ncon; ++c) {
             double rhs = job->conRhs ? job->conRhs[c] : 0.0;

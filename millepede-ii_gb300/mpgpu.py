@@ -606,7 +606,7 @@ class JobData:
     """A job's C structures (mpgpu_steer, mpgpu_job, mpgpu_result) with the
     numpy arrays they point to kept alive."""
 
-    def __init__(self, data, constraints=None, params=None, **steer):
+    def __init__(self, data, constraints=None, params=None, measurements=None, **steer):
         st = dict(metsol=1, matsto=1, mitera=1, lhuber=0, chicut=0.0, chirem=0.0, chhuge=50.0,
                   dwcut=0.0, cndlmx=100.0, lfitbb=1, mreqenf=25, mreqena=10, mreqpe=1,
                   mrestl=1e-10, itnlim=2000, nthreads=0, structDevice=0, monitor=0,
@@ -638,6 +638,17 @@ class JobData:
             j.npar = len(self.parLabel)
             j.parLabel, j.parValue = ptr(self.parLabel, i32p), ptr(self.parValue, f64p)
             j.parSigma = ptr(self.parSigma, f64p)
+        if measurements is not None:
+            # steering "measurement" lines: (start, labels, coefficients, rhs, sigma)
+            self.msStart = np.ascontiguousarray(measurements[0], np.int32)
+            self.msLabel = np.ascontiguousarray(measurements[1], np.int32)
+            self.msCoef = np.ascontiguousarray(measurements[2], np.float64)
+            self.msRhs = np.ascontiguousarray(measurements[3], np.float64)
+            self.msSigma = np.ascontiguousarray(measurements[4], np.float64)
+            j.nmeas = len(self.msStart) - 1
+            j.msStart, j.msLabel = ptr(self.msStart, i32p), ptr(self.msLabel, i32p)
+            j.msCoef, j.msRhs = ptr(self.msCoef, f64p), ptr(self.msRhs, f64p)
+            j.msSigma = ptr(self.msSigma, f64p)
         self.job = j
         cap = len(self.inder) + 16
         self.labels = np.zeros(cap, np.int32)

@@ -113,16 +113,55 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
     int64_t *offsets = NULL, nmat, ncolw = 0;
     int32_t *columns = NULL;
     if (st->matsto == 2) {
+        /* the pairs of the measurement lines belong to the sparse structure
+         * whatever the records hold (pede.f90:7007-7042, with the
+         * increment mreqpe, so they are always kept): one structure-only
+         * record per measurement line, its labels as global words */
+        int64_t nrecS = job->nrec, *rpS = (int64_t *)job->recPtr;
+        int32_t *inS = tinder;
+        double *glS = (double *)job->glder;
+        if (job->nmeas > 0) {
+            int64_t extra = 0;
+            for (int32_t m = 0; m < job->nmeas; m++) extra += 3 + (job->msStart[m + 1] - job->msStart[m]);
+            nrecS = job->nrec + job->nmeas;
+            rpS = (int64_t *)malloc(sizeof(int64_t) * ((size_t)nrecS + 1));
+            inS = (int32_t *)malloc(sizeof(int32_t) * (size_t)(nw + extra));
+            glS = (double *)malloc(sizeof(double) * (size_t)(nw + extra));
+            int32_t *raw = (int32_t *)malloc(sizeof(int32_t) * (size_t)extra);
+            int64_t *rpRaw = (int64_t *)malloc(sizeof(int64_t) * ((size_t)job->nmeas + 1));
+            memcpy(rpS, job->recPtr, sizeof(int64_t) * ((size_t)job->nrec + 1));
+            memcpy(inS, tinder, sizeof(int32_t) * (size_t)nw);
+            memcpy(glS, job->glder, sizeof(double) * (size_t)nw);
+            int64_t q = 0;
+            for (int32_t m = 0; m < job->nmeas; m++) {
+                rpRaw[m] = q;
+                /* header, value, sigma (positive: not a special block), labels */
+                raw[q] = 0; glS[nw + q] = 0.0; q++;
+                raw[q] = 0; glS[nw + q] = 0.0; q++;
+                raw[q] = 0; glS[nw + q] = 1.0; q++;
+                for (int32_t k = job->msStart[m]; k < job->msStart[m + 1]; k++) {
+                    raw[q] = job->msLabel[k];
+                    glS[nw + q] = 1.0;
+                    q++;
+                }
+            }
+            rpRaw[job->nmeas] = q;
+            mpref_translate(job->nmeas, rpRaw, raw, glS + nw, ntot, res->labels, inS + nw);
+            for (int32_t m = 0; m <= job->nmeas; m++) rpS[job->nrec + m] = nw + rpRaw[m];
+            free(raw);
+            free(rpRaw);
+        }
         int64_t capc = 64 + 4 * (int64_t)nVar * 64;
         offsets = (int64_t *)malloc(sizeof(int64_t) * 2 * ((size_t)nG + 1));
         for (;;) {
             columns = (int32_t *)malloc(sizeof(int32_t) * (size_t)capc);
-            if (mpref_mpbits(job->nrec, job->recPtr, tinder, job->glder, res->varIndex, nVar, nG,
+            if (mpref_mpbits(nrecS, rpS, inS, glS, res->varIndex, nVar, nG,
                              aig, p2g, st->mreqpe, capc, offsets, columns, &ncolw, &nmat) == 0)
                 break;
             free(columns);
             capc *= 4;
         }
+        if (job->nmeas > 0) { free(rpS); free(inS); free(glS); }
     } else {
         nmat = (int64_t)nVar * (nVar + 1) / 2;
     }

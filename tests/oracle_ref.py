@@ -100,7 +100,7 @@ class Arrays:
 
 
 def make_job(data, parLabel=None, parValue=None, parSigma=None, constraints=True,
-             recFile=None, fileWeight=None):
+             recFile=None, fileWeight=None, measurements=None):
     keep = Arrays()
     keep.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
     keep.inder = np.ascontiguousarray(data["inder"], np.int32)
@@ -136,6 +136,17 @@ def make_job(data, parLabel=None, parValue=None, parSigma=None, constraints=True
         j.conLabel = ptr(keep.conLabel, i32p)
         j.conCoef = ptr(keep.conCoef, f64p)
         j.conRhs = ptr(keep.conRhs, f64p)
+    if measurements is not None:
+        # steering "measurement" lines: (start, labels, coefficients, rhs, sigma)
+        keep.msStart = np.ascontiguousarray(measurements[0], np.int32)
+        keep.msLabel = np.ascontiguousarray(measurements[1], np.int32)
+        keep.msCoef = np.ascontiguousarray(measurements[2], np.float64)
+        keep.msRhs = np.ascontiguousarray(measurements[3], np.float64)
+        keep.msSigma = np.ascontiguousarray(measurements[4], np.float64)
+        j.nmeas = len(keep.msStart) - 1
+        j.msStart, j.msLabel = ptr(keep.msStart, i32p), ptr(keep.msLabel, i32p)
+        j.msCoef, j.msRhs = ptr(keep.msCoef, f64p), ptr(keep.msRhs, f64p)
+        j.msSigma = ptr(keep.msSigma, f64p)
     return j, keep
 
 

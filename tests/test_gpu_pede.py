@@ -136,3 +136,22 @@ def test_start_values_feasib_and_res(mp, orc, tmp_path):
         # single-precision text of values equal up to the last printed digit
         diff = sum(1 for x, y in zip(a, b) if x != y)
         assert diff <= max(2, len(a) // 100), diff
+
+
+def test_measurement_lines(mp, orc):
+    """Steering measurement lines (pede.f90:2743-2798) in a whole job: the
+    GPU job equals the oracle's in packed storage (inversion, with errors)
+    and in sparse storage (MINRES), where the pairs of the lines, two
+    modules of one telescope layer that no track crosses together, are in
+    the structure (pede.f90:7007-7042)."""
+    import test_measurement_pairs as T
+    d, meas = T.telescope_with_measurements(mp)
+    st = orc.make_steer(metsol=1, matsto=1, mitera=1)
+    compare(gpu_job(mp, orc, d, st, measurements=meas), orc.run(d, st, measurements=meas), errors=True)
+    st = orc.make_steer(metsol=4, matsto=2, mitera=1, mrestl=1e-14, itnlim=4000)
+    g = gpu_job(mp, orc, d, st, measurements=meas)
+    o = orc.run(d, st, measurements=meas)
+    assert g["rc"] == 0 and o["rc"] == 0
+    np.testing.assert_array_equal(g["labels"], o["labels"])
+    scale = np.max(np.abs(o["parameter"]))
+    assert np.max(np.abs(g["parameter"] - o["parameter"])) <= 1e-9 * scale
