@@ -14,7 +14,9 @@ import pytest
 
 import oracle_ref as orc
 
-REF_RES = "/root/reference/CI/refFiles/millepede.res"
+# the reference's golden file, read where the Millepede-II sources are
+# (MILLEPEDE_SOURCES, as for tests/golden/make_golden.py)
+REF_RES = os.path.join(os.environ.get("MILLEPEDE_SOURCES", ""), "CI", "refFiles", "millepede.res")
 
 # prtglo's record layouts: i10, 2X, then 2..4 G14.5 fields, then either
 # F8.3 (102 with globalcorr) or blanks + I12 (110: 28X, 111: 14X, 112: none)
@@ -145,7 +147,8 @@ def test_writer_columns(mp, tmp_path, errors, ipcntr, igcorr):
         assert len(line) == width
 
 
-@pytest.mark.skipif(not os.path.exists(REF_RES), reason="reference golden file not mounted")
+@pytest.mark.skipif(not os.environ.get("MILLEPEDE_SOURCES") or not os.path.exists(REF_RES),
+                    reason="MILLEPEDE_SOURCES not set or without CI/refFiles/millepede.res")
 def test_layout_of_reference_golden_file(mp, tmp_path):
     """Every line of the reference's golden millepede.res (printcounts,
     no errors: formats 110/111) parses with the column parser above, and a
