@@ -22,6 +22,8 @@
  *   mpgpu_set_layout      loop2 results: globalAllIndexGroups,
  *                         sparseMatrixOffsets/Columns (pede.f90:6509-6545,
  *                         7174, 7426)
+ *   mpgpu_set_suppressed_pairs  pairs left out by pairentries, whose
+ *                         updates mupdat drops (pede.f90:3172, mpbits.f90:409)
  *   mpgpu_set_constraints feasma / qldecb (pede.f90:1377-1544,
  *                         mpqldec.f90:219-393)
  *   mpgpu_upload_records  readFromBinary + prepareRecords(1) buffers
@@ -115,6 +117,16 @@ int32_t mpgpu_set_layout(mpgpu_ctx *ctx, int32_t nTotal, const int32_t *varIndex
                          int32_t nVar, int32_t nGroups, const int32_t *allIndexGroups,
                          int32_t matsto, const int64_t *sparseOffsets,
                          const int32_t *sparseColumns, int64_t ncolw, int64_t nmat);
+
+/* pairentries: the group pairs met in the records that the sparse layout
+ * leaves out (the list of mpgpu_host_mpbits_pairentries, 1-based group
+ * numbers, either order).  The records' updates of these pairs are dropped,
+ * as mupdat drops an element that is not stored (pede.f90:3172); without
+ * this call such a pair is an upload error (23).  Call after
+ * mpgpu_set_layout (sparse) and before mpgpu_upload_records; records
+ * uploaded earlier are released; a later call replaces the list.  A pair
+ * that the layout stores is refused (24). */
+int32_t mpgpu_set_suppressed_pairs(mpgpu_ctx *ctx, int64_t npair, const int32_t *pairs);
 
 /* Linear constraints over the variable parameters, eliminated by QL:
  * A[ncon*nVar], row k = constraint k (the reference's matConstraintsT). */
@@ -377,9 +389,11 @@ typedef struct mpgpu_steer {
     int32_t lhuber;     /* outlierdownweighting */
     float chicut, chirem, chhuge, dwcut, cndlmx;
     int32_t lfitbb;
-    int32_t mreqenf, mreqena, mreqpe;   /* mreqpe: pede's pairentries; only 1 (every pair
-                                           met in a record is stored) is built, larger
-                                           values are refused with status 44 */
+    int32_t mreqenf, mreqena, mreqpe;   /* mreqpe: pede's pairentries (sparse storage):
+                                           group pairs met in fewer records are left out
+                                           of the matrix and their updates dropped; 1
+                                           stores every pair met.  The structure passes
+                                           then run on the host. */
     double mrestl;
     int32_t itnlim;
     int32_t nthreads;   /* host threads for the structure passes */
@@ -455,6 +469,23 @@ int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *in
                           const double *glder, const int32_t *varIndexOfTotal, int32_t nVar,
                           int32_t nG, const int32_t *allIndexGroups, int64_t cap,
                           int64_t *offsets, int32_t *columns, int64_t *ncolw, int64_t *nmat);
+/* loop2 sparse structure with pairentries mreqpe (clbits/inbits/ndbits,
+ * mpbits.f90:73-142, 182-243, 305-566; record pairs pede.f90:6889-6908):
+ * every group pair is counted once per record, records nrecData..nrec-1
+ * (the structure-only records of the measurement lines) count mreqpe
+ * (pede.f90:7036); pairs counted at least mreqpe times are stored, the
+ * others met are listed in suppressed[2*k], [2*k+1] (row group >= column
+ * group, by row, then column) for mpgpu_set_suppressed_pairs.  Returns 0,
+ * 44 on bad arguments, or -1 when columns needs more than cap words or the
+ * list more than capSup pairs (*ncolw, *nmat and *nsup then hold the sizes;
+ * call again with larger arrays).  mreqpe <= 1 is mpgpu_host_mpbits. */
+int32_t mpgpu_host_mpbits_pairentries(int64_t nrec, int64_t nrecData, const int64_t *recPtr,
+                                      const int32_t *inder, const double *glder,
+                                      const int32_t *varIndexOfTotal, int32_t nVar, int32_t nG,
+                                      const int32_t *allIndexGroups, int32_t mreqpe, int64_t cap,
+                                      int64_t *offsets, int32_t *columns, int64_t *ncolw,
+                                      int64_t *nmat, int64_t capSup, int32_t *suppressed,
+                                      int64_t *nsup);
 
 /* loop1 on the device: the tables of mpgpu_host_labels (same arguments,
  * outputs and results) for the label passes of pede's loop1 (label table

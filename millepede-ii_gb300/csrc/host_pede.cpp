@@ -243,30 +243,47 @@ extern "C" int32_t mpgpu_host_translate(int64_t nrec, const int64_t *recPtr, con
     return 0;
 }
 
-// loop2 sparse structure: every pair of parameter groups met in one record
-// (pede.f90:6889-6908) is stored; per row group the columns are kept either
-// as a list of parameter indices or, when that is shorter, as regions of
-// consecutive groups (offset, first group) closed by (end offset, nG+1)
-// (ndbits/spbits, mpbits.f90:305-566, 1220-1350).
-extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
-                                     const double *glder, const int32_t *varIndexOfTotal,
-                                     int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
-                                     int64_t cap, int64_t *offsets, int32_t *columns,
-                                     int64_t *ncolw, int64_t *nmat) {
+// loop2 sparse structure: the pairs of parameter groups met in the records
+// (each counted once per record, pede.f90:6889-6908; the structure-only
+// records of the measurement lines from nrecData on count mreqpe,
+// pede.f90:7036) whose count reaches mreqpe are stored (clbits/inbits/ndbits,
+// mpbits.f90:73-142, 182-243, 305-566); per row group the columns are kept
+// either as a list of parameter indices or, when that is shorter, as regions
+// of consecutive groups (offset, first group) closed by (end offset, nG+1)
+// (spbits, mpbits.f90:1220-1350).  The counters saturate at the largest
+// value of their bit field, which is at least mreqpe, as pede's do; the
+// fields are a power of two bits wide so that none crosses a 64-bit word.
+extern "C" int32_t mpgpu_host_mpbits_pairentries(int64_t nrec, int64_t nrecData, const int64_t *recPtr,
+                                                 const int32_t *inder, const double *glder,
+                                                 const int32_t *varIndexOfTotal, int32_t nVar, int32_t nG,
+                                                 const int32_t *allIndexGroups, int32_t mreqpe, int64_t cap,
+                                                 int64_t *offsets, int32_t *columns, int64_t *ncolw,
+                                                 int64_t *nmat, int64_t capSup, int32_t *suppressed,
+                                                 int64_t *nsup) {
+    if (nrec < 0 || nG <= 0 || nVar <= 0 || !recPtr || !allIndexGroups || !offsets || !ncolw || !nmat ||
+        (capSup > 0 && !suppressed))
+        return MPGPU_ERR_ARG;
+    const uint64_t req = (uint64_t)std::max<int32_t>(mreqpe, 1);
+    uint32_t fw = 1;
+    while (fw < 32 && ((1ull << fw) - 1) < req) fw *= 2;
+    const uint64_t mx = (1ull << fw) - 1;
     std::vector<int32_t> p2g(nVar);
     for (int32_t g = 1; g <= nG; ++g)
         for (int32_t v = allIndexGroups[g - 1]; v < allIndexGroups[g]; ++v) p2g[v - 1] = g;
-    // lower-triangular bitmap over group pairs, row I holds J = 1..I
+    // lower-triangular counters over group pairs, row I holds J = 1..I
     std::vector<uint64_t> rowWord(nG + 2, 0);   // first word of row I
-    for (int32_t I = 1; I <= nG; ++I) rowWord[I + 1] = rowWord[I] + ((uint64_t)I + 63) / 64;
+    for (int32_t I = 1; I <= nG; ++I) rowWord[I + 1] = rowWord[I] + ((uint64_t)I * fw + 63) / 64;
     std::vector<uint64_t> bits(rowWord[nG + 1] + 1, 0);
     const int nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
-    // records split over threads; bits set with atomic OR (idempotent)
+    // records split over threads; a counter is raised by compare-and-swap of
+    // its word (saturating adds commute, so the counts do not depend on the
+    // order)
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t) {
         th.emplace_back([&, t] {
             std::vector<int32_t> grp;
             for (int64_t r = nrec * t / nt; r < nrec * (t + 1) / nt; ++r) {
+                const uint64_t inc = r < nrecData ? 1 : req;
                 grp.clear();
                 for_each_measurement(inder, glder, recPtr[r], recPtr[r + 1], [&](int64_t, int64_t sg, int64_t lg) {
                     for (int64_t w = sg + 1; w <= lg; ++w) {
@@ -278,28 +295,49 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
                 grp.erase(std::unique(grp.begin(), grp.end()), grp.end());
                 for (size_t a = 0; a < grp.size(); ++a)
                     for (size_t b = 0; b <= a; ++b) {
-                        const uint64_t bit = rowWord[grp[a]] * 64 + (uint64_t)(grp[b] - 1);
-                        __atomic_fetch_or(&bits[bit >> 6], 1ull << (bit & 63), __ATOMIC_RELAXED);
+                        const uint64_t pos = rowWord[grp[a]] * 64 + (uint64_t)(grp[b] - 1) * fw;
+                        uint64_t *word = &bits[pos >> 6];
+                        const uint32_t sh = (uint32_t)(pos & 63);
+                        if (fw == 1) {
+                            __atomic_fetch_or(word, 1ull << sh, __ATOMIC_RELAXED);
+                            continue;
+                        }
+                        uint64_t old = __atomic_load_n(word, __ATOMIC_RELAXED);
+                        for (;;) {
+                            const uint64_t c = (old >> sh) & mx;
+                            if (c >= mx) break;
+                            const uint64_t nc = std::min(c + inc, mx);
+                            const uint64_t nw = (old & ~(mx << sh)) | (nc << sh);
+                            if (__atomic_compare_exchange_n(word, &old, nw, true, __ATOMIC_RELAXED,
+                                                            __ATOMIC_RELAXED))
+                                break;
+                        }
                     }
             }
         });
     }
     for (auto &x : th) x.join();
-    auto test = [&](int32_t I, int32_t J) {
-        const uint64_t bit = rowWord[I] * 64 + (uint64_t)(J - 1);
-        return (bits[bit >> 6] >> (bit & 63)) & 1ull;
+    auto count = [&](int32_t I, int32_t J) {
+        const uint64_t pos = rowWord[I] * 64 + (uint64_t)(J - 1) * fw;
+        return (bits[pos >> 6] >> (pos & 63)) & mx;
     };
+    auto test = [&](int32_t I, int32_t J) { return count(I, J) >= req; };
     const int64_t nd = allIndexGroups[nG] - allIndexGroups[0];
     std::vector<int64_t> nw(nG + 1), nm(nG + 1);
     std::vector<uint8_t> comp(nG + 1, 0);
+    int64_t ns = 0;
     for (int32_t I = 1; I <= nG; ++I) {
         int64_t inr = 0, irgn = 1;
         bool last = false;
         for (int32_t J = 1; J <= I; ++J) {
-            const bool on = test(I, J);
+            const uint64_t c = count(I, J);
+            const bool on = c >= req;
             if (on) {
                 inr += allIndexGroups[J] - allIndexGroups[J - 1];
                 if (!last) irgn++;
+            } else if (c > 0) {
+                if (ns < capSup) { suppressed[2 * ns] = I; suppressed[2 * ns + 1] = J; }
+                ns++;
             }
             last = on;
         }
@@ -308,6 +346,7 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
         nw[I] = comp[I] ? 2 * irgn : inr;
         nm[I] = inr * np;
     }
+    if (nsup) *nsup = ns;
     int64_t lb = 0, ll = nd;
     for (int32_t I = 1; I <= nG; ++I) {
         offsets[2 * (I - 1)] = lb;
@@ -317,7 +356,9 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
     }
     offsets[2 * nG] = lb;
     offsets[2 * nG + 1] = ll;
-    if (lb > cap) return -1;
+    *ncolw = lb;
+    *nmat = ll;
+    if (lb > cap || ns > capSup) return -1;
     for (int32_t I = 1; I <= nG; ++I) {
         int64_t k = offsets[2 * (I - 1)];
         int64_t width = 0;
@@ -337,9 +378,19 @@ extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const 
         }
         if (comp[I]) { columns[k++] = (int32_t)width; columns[k++] = nG + 1; }
     }
-    *ncolw = lb;
-    *nmat = ll;
     return 0;
+}
+
+// every pair met stored (pairentries 1)
+extern "C" int32_t mpgpu_host_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+                                     const double *glder, const int32_t *varIndexOfTotal,
+                                     int32_t nVar, int32_t nG, const int32_t *allIndexGroups,
+                                     int64_t cap, int64_t *offsets, int32_t *columns,
+                                     int64_t *ncolw, int64_t *nmat) {
+    int64_t nsup = 0;
+    return mpgpu_host_mpbits_pairentries(nrec, nrec, recPtr, inder, glder, varIndexOfTotal, nVar, nG,
+                                         allIndexGroups, 1, cap, offsets, columns, ncolw, nmat, 0, nullptr,
+                                         &nsup);
 }
 
 // ------------------------------------------------------------------ job
@@ -402,13 +453,6 @@ void feasib(const mpgpu_job *job, const std::vector<int32_t> &lab, const int32_t
 int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_job *job, mpgpu_result *res,
                           const std::function<bool(int64_t)> &admit) {
     if (!st || !job || !res) return MPGPU_ERR_ARG;
-    // pairentries > 1 (pairs met in fewer records left out of the sparse
-    // matrix, clbits/inbits mpbits.f90:182-243) is not built: refused rather
-    // than run with every pair stored
-    if (st->mreqpe > 1) {
-        res->exitCode = MPGPU_ERR_ARG;
-        return MPGPU_ERR_ARG;
-    }
     using Clock = std::chrono::steady_clock;
     const auto msSince = [](Clock::time_point a) {
         return std::chrono::duration<double, std::milli>(Clock::now() - a).count();
@@ -435,7 +479,11 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     // footprint before any device allocation of the job)
     // (measurement lines in sparse storage add structure-only records, which
     // the host passes take)
-    const bool onDevice = st->structDevice != 0 && !admit && !(st->matsto == 2 && job->nmeas > 0);
+    // pairentries (mreqpe > 1, sparse storage only as in pede) counts the
+    // group pairs on the host
+    const int32_t mreqpe = st->matsto == 2 ? std::max<int32_t>(st->mreqpe, 1) : 1;
+    const bool onDevice =
+        st->structDevice != 0 && !admit && !(st->matsto == 2 && job->nmeas > 0) && mreqpe == 1;
     int32_t ntot = onDevice
                        ? mpgpu_loop1_device(ctx, job->nrec, job->recPtr, job->inder, job->glder,
                                             (int32_t)steer.size(), steer.data(), job->npar, job->parLabel,
@@ -471,8 +519,8 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
         mpgpu_host_translate(job->nrec, job->recPtr, job->inder, job->glder, ntot, res->labels, tinder.data());
     }
     std::vector<int64_t> offsets;
-    std::vector<int32_t> columns;
-    int64_t ncolw = 0, nmat = 0;
+    std::vector<int32_t> columns, suppressed;
+    int64_t ncolw = 0, nmat = 0, nsup = 0;
     // the parameter pairs of the measurement lines belong to the sparse
     // structure whatever the records hold (pede.f90:7007-7042, increment
     // mreqpe: always kept): one structure-only record per measurement line
@@ -514,21 +562,25 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     }
     if (st->matsto == 2) {
         offsets.resize(2 * (nG + 1));
-        int64_t capc = 1 << 20;
+        int64_t capc = 1 << 20, caps = mreqpe > 1 ? 1 << 18 : 0;
         for (;;) {
             columns.assign(capc, 0);
+            suppressed.assign(2 * std::max<int64_t>(caps, 1), 0);
             const int32_t r2 =
                 onDevice ? mpgpu_loop2_device(ctx, res->varIndex, nVar, nG, aig.data(), capc, offsets.data(),
                                               columns.data(), &ncolw, &nmat)
-                         : mpgpu_host_mpbits(nrecS, rpS, inS, glS, res->varIndex, nVar,
-                                             nG, aig.data(), capc, offsets.data(), columns.data(), &ncolw, &nmat);
+                         : mpgpu_host_mpbits_pairentries(nrecS, job->nrec, rpS, inS, glS, res->varIndex, nVar,
+                                                         nG, aig.data(), mreqpe, capc, offsets.data(),
+                                                         columns.data(), &ncolw, &nmat, caps,
+                                                         suppressed.data(), &nsup);
             if (r2 == 0) break;
             if (r2 != -1) {
                 res->exitCode = r2;
                 if (!ctxIn) mpgpu_destroy(ctx);
                 return r2;
             }
-            capc = onDevice ? std::max<int64_t>(ncolw, 1) : capc * 4;
+            capc = std::max<int64_t>(ncolw, 1);
+            caps = nsup;
         }
     }
     res->msStructure = msSince(tJob);
@@ -558,6 +610,8 @@ int32_t pede_run_admitted(mpgpu_ctx *ctxIn, const mpgpu_steer *st, const mpgpu_j
     rc = mpgpu_set_layout(ctx, ntot, res->varIndex, nVar, nG, aig.data(), st->matsto,
                           offsets.empty() ? nullptr : offsets.data(), columns.empty() ? nullptr : columns.data(),
                           ncolw, nmat);
+    // the records' updates of the pairs left out are summed apart and dropped
+    if (!rc && nsup > 0) rc = mpgpu_set_suppressed_pairs(ctx, nsup, suppressed.data());
     const int32_t ncon = job->ncon;
     std::vector<double> A;
     if (!rc && ncon > 0) {

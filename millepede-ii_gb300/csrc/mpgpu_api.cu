@@ -70,7 +70,7 @@ void free_records(DevJob &j) {
 void free_layout(DevJob &j) {
     dfree(j.varOfTot); dfree(j.aig); dfree(j.p2g); dfree(j.off); dfree(j.col);
     dfree(j.matD); dfree(j.gvec); dfree(j.gcnt); dfree(j.gpar); dfree(j.work);
-    dfree(j.rowBlk0); dfree(j.blkJ); dfree(j.blkOff); dfree(j.blkLd); dfree(j.blkCol);
+    dfree(j.rowBlk0); dfree(j.blkJ); dfree(j.blkOff); dfree(j.blkLd);
     dfree(j.rowWidth);
 }
 
@@ -189,7 +189,7 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
     // the blocks of sparseMatrixOffsets/Columns, ijpgrp pede.f90:5371-5461)
     {
         std::vector<int64_t> rowBlk0(nGroups + 1, 0), bOff;
-        std::vector<int32_t> bJ, bLd, bCol, width(nGroups, 0);
+        std::vector<int32_t> bJ, bLd, width(nGroups, 0);
         for (int32_t I = 1; I <= nGroups; ++I) {
             const int32_t np = allIndexGroups[I] - allIndexGroups[I - 1];
             if (matsto == 2) {
@@ -203,7 +203,6 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
                         const int32_t J = p2g[first - 1];
                         const int32_t nj = allIndexGroups[J] - allIndexGroups[J - 1];
                         bJ.push_back(J); bOff.push_back(ll + k); bLd.push_back((int32_t)ku);
-                        bCol.push_back((int32_t)k);
                         k += nj;
                     }
                     width[I - 1] = (int32_t)ku;
@@ -216,7 +215,7 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
                             if (J < 1 || J > nGroups) return set_err(c, MPGPU_ERR_SIZE, "bad sparse regions");
                             const int32_t nj = allIndexGroups[J] - allIndexGroups[J - 1];
                             bJ.push_back(J); bOff.push_back(ll + (int64_t)o0 * np + inreg);
-                            bLd.push_back(o1 - o0); bCol.push_back(o0 + inreg);
+                            bLd.push_back(o1 - o0);
                             inreg += nj;
                             J++;
                         }
@@ -239,7 +238,6 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
             MPG_CUDA(c, dupload(j.blkJ, bJ.data(), (int64_t)bJ.size(), s));
             MPG_CUDA(c, dupload(j.blkOff, bOff.data(), (int64_t)bOff.size(), s));
             MPG_CUDA(c, dupload(j.blkLd, bLd.data(), (int64_t)bLd.size(), s));
-            MPG_CUDA(c, dupload(j.blkCol, bCol.data(), (int64_t)bCol.size(), s));
             MPG_CUDA(c, cudaStreamSynchronize(s));
         }
     }
@@ -248,6 +246,85 @@ extern "C" int32_t mpgpu_set_layout(mpgpu_ctx *c, int32_t nTotal, const int32_t 
     MPG_CUDA(c, dalloc(j.gvec, nVar));
     MPG_CUDA(c, dalloc(j.gcnt, nVar));
     MPG_CUDA(c, dalloc(j.gpar, nTotal));
+    MPG_CUDA(c, cudaStreamSynchronize(s));
+    return MPGPU_OK;
+}
+
+// ------------------------------------------------------------------ pairentries
+// Group pairs met in the records but left out of the sparse structure
+// (pairentries: counted fewer than mreqpe times, clbits/ndbits
+// mpbits.f90:182-243, 305-566).  Their blocks join the accumulation table
+// of their row, in column order, with the offset of a discard area after
+// the nmat matrix elements and the row stride of their own column group, so
+// the records' updates of those pairs are summed there and dropped, as
+// mupdat drops an element of a pair that is not stored (pede.f90:3172); the
+// diagonal elements of a left-out diagonal pair still reach the diagonal.
+// The discard area is as large as the largest of these blocks, the blocks
+// share it and nothing reads it; the sparse products, preconditioners and
+// downloads use offsets and columns, which hold only the stored pairs.  A
+// later call replaces the list.
+extern "C" int32_t mpgpu_set_suppressed_pairs(mpgpu_ctx *c, int64_t npair, const int32_t *pairs) {
+    if (!c) return MPGPU_ERR_ARG;
+    DevJob &j = c->j;
+    if (j.matsto != 2 || !j.matD) return set_err(c, MPGPU_ERR_ARG, "suppressed pairs need a sparse layout");
+    if (npair < 0 || (npair > 0 && !pairs))
+        return set_err(c, MPGPU_ERR_ARG, "mpgpu_set_suppressed_pairs: bad arguments");
+    cudaSetDevice(c->device);
+    const int32_t nG = j.nG;
+    const std::vector<int32_t> &aig = j.hAig;
+    std::vector<std::vector<int32_t>> add(nG + 1);
+    for (int64_t q = 0; q < npair; ++q) {
+        const int32_t I = std::max(pairs[2 * q], pairs[2 * q + 1]);
+        const int32_t J = std::min(pairs[2 * q], pairs[2 * q + 1]);
+        if (J < 1 || I > nG) return set_err(c, MPGPU_ERR_SIZE, "suppressed pair outside the groups");
+        add[I].push_back(J);
+    }
+    std::vector<int64_t> rowBlk0(nG + 1, 0), bOff;
+    std::vector<int32_t> bJ, bLd;
+    int64_t area = 0;
+    for (int32_t I = 1; I <= nG; ++I) {
+        std::vector<int32_t> &a = add[I];
+        std::sort(a.begin(), a.end());
+        a.erase(std::unique(a.begin(), a.end()), a.end());
+        const int64_t ni = aig[I] - aig[I - 1];
+        int64_t k = j.hRowBlk0[I - 1];
+        const int64_t ke = j.hRowBlk0[I];
+        size_t q = 0;
+        while (k < ke || q < a.size()) {
+            if (q < a.size() && (k >= ke || a[q] < j.hBlkJ[k])) {
+                const int32_t J = a[q++];
+                const int32_t nj = aig[J] - aig[J - 1];
+                bJ.push_back(J);
+                bOff.push_back(j.nmat);
+                bLd.push_back(nj);
+                area = std::max<int64_t>(area, ni * nj);
+            } else if (j.hBlkOff[k] >= j.nmat) {
+                ++k;   // a block of an earlier call: the new list replaces it
+            } else {
+                if (q < a.size() && a[q] == j.hBlkJ[k])
+                    return set_err(c, MPGPU_ERR_SIZE, "a suppressed pair is stored in the structure");
+                bJ.push_back(j.hBlkJ[k]);
+                bOff.push_back(j.hBlkOff[k]);
+                bLd.push_back(j.hBlkLd[k]);
+                ++k;
+            }
+        }
+        rowBlk0[I] = (int64_t)bJ.size();
+    }
+    // block ids change: records uploaded before are released
+    dense_release(c);
+    free_records(j);
+    cudaStream_t s = c->stream;
+    j.hRowBlk0 = rowBlk0;
+    j.hBlkJ = bJ;
+    j.hBlkOff = bOff;
+    j.hBlkLd = bLd;
+    MPG_CUDA(c, dupload(j.rowBlk0, rowBlk0.data(), nG + 1, s));
+    MPG_CUDA(c, dupload(j.blkJ, bJ.data(), (int64_t)bJ.size(), s));
+    MPG_CUDA(c, dupload(j.blkOff, bOff.data(), (int64_t)bOff.size(), s));
+    MPG_CUDA(c, dupload(j.blkLd, bLd.data(), (int64_t)bLd.size(), s));
+    MPG_CUDA(c, dalloc(j.matD, j.nmat + area));
+    MPG_CUDA(c, cudaMemsetAsync(j.matD, 0, sizeof(double) * (size_t)(j.nmat + area), s));
     MPG_CUDA(c, cudaStreamSynchronize(s));
     return MPGPU_OK;
 }

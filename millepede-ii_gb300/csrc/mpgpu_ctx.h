@@ -70,13 +70,13 @@ struct DevJob {
     int64_t *gcnt = nullptr;       // [nVar]
     double *gpar = nullptr;        // [nTotal]
     // block rows of the global matrix: blocks (I, J <= I) of row group I,
-    // ordered by J, with the offset of element (0,0) in globalMatD, the row
-    // stride and the column offset in the dense row layout of I
+    // ordered by J, with the offset of element (0,0) in globalMatD and the
+    // row stride (the blocks of pairs left out by pairentries point at the
+    // discard area after the nmat elements, mpgpu_set_suppressed_pairs)
     int64_t *rowBlk0 = nullptr;    // [nG+1]
     int32_t *blkJ = nullptr;
     int64_t *blkOff = nullptr;
     int32_t *blkLd = nullptr;
-    int32_t *blkCol = nullptr;
     int32_t *rowWidth = nullptr;   // [nG] columns of the dense row layout
     std::vector<int32_t> hRowWidth;
     std::vector<int64_t> hRowBlk0, hBlkOff;

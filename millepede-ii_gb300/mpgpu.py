@@ -168,7 +168,8 @@ EXPORTS = [
     "mpgpu_read_mille",
     "mpgpu_host_register", "mpgpu_host_unregister", "mpgpu_host_alloc", "mpgpu_host_free",
     "mpgpu_host_labels",
-    "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_loop1_device", "mpgpu_loop2_device", "mpgpu_pede_run", "mpgpu_write_res",
+    "mpgpu_host_translate", "mpgpu_host_mpbits", "mpgpu_host_mpbits_pairentries",
+    "mpgpu_set_suppressed_pairs", "mpgpu_loop1_device", "mpgpu_loop2_device", "mpgpu_pede_run", "mpgpu_write_res",
     "mpgpu_write_res_opts", "mpgpu_matrix_diagonal", "mpgpu_release",
     "mpgen_count", "mpgen_fill", "mpgen_constraints", "mpgen_constraint_words",
 ]
@@ -277,9 +278,12 @@ def read_mille_c(path):
 class HostStructure:
     """loop1/loop2 products computed by the library's host side:
     sorted labels, entries, variable indices, parameter groups, translated
-    records and (sparse storage) the mpbits row structure."""
+    records and (sparse storage) the mpbits row structure; with mreqpe > 1
+    (pairentries) the group pairs met fewer times are left out and listed in
+    `suppressed` (one (row group, column group) pair per row)."""
 
-    def __init__(self, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True):
+    def __init__(self, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True,
+                 mreqpe=1):
         L = lib()
         self.recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
         inder = np.ascontiguousarray(data["inder"], np.int32)
@@ -312,22 +316,36 @@ class HostStructure:
             raise RuntimeError(f"mpgpu_host_translate failed ({rc})")
         self.offsets = np.zeros(2 * (self.nG + 1), np.int64)
         self.columns = np.zeros(1, np.int32)
+        self.suppressed = np.zeros((0, 2), np.int32)
         self.ncolw = 0
         self.nmatSparse = 0
         if sparse:
-            capc = 1 << 20
+            capc, caps = 1 << 20, 0
             while True:
                 cols = np.zeros(capc, np.int32)
-                ncolw, nmat = C.c_int64(), C.c_int64()
-                rc = L.mpgpu_host_mpbits(C.c_int64(nrec), ptr(self.recPtr, i64p),
-                                         ptr(self.tinder, i32p), ptr(self.glder, f64p),
-                                         ptr(self.varIndex, i32p), C.c_int32(self.nVar),
-                                         C.c_int32(self.nG), ptr(self.aig, i32p), C.c_int64(capc),
-                                         ptr(self.offsets, i64p), ptr(cols, i32p),
-                                         C.byref(ncolw), C.byref(nmat))
+                sup = np.zeros(2 * max(caps, 1), np.int32)
+                ncolw, nmat, nsup = C.c_int64(), C.c_int64(), C.c_int64()
+                if mreqpe > 1:
+                    rc = L.mpgpu_host_mpbits_pairentries(
+                        C.c_int64(nrec), C.c_int64(nrec), ptr(self.recPtr, i64p),
+                        ptr(self.tinder, i32p), ptr(self.glder, f64p), ptr(self.varIndex, i32p),
+                        C.c_int32(self.nVar), C.c_int32(self.nG), ptr(self.aig, i32p),
+                        C.c_int32(mreqpe), C.c_int64(capc), ptr(self.offsets, i64p),
+                        ptr(cols, i32p), C.byref(ncolw), C.byref(nmat), C.c_int64(caps),
+                        ptr(sup, i32p), C.byref(nsup))
+                else:
+                    rc = L.mpgpu_host_mpbits(C.c_int64(nrec), ptr(self.recPtr, i64p),
+                                             ptr(self.tinder, i32p), ptr(self.glder, f64p),
+                                             ptr(self.varIndex, i32p), C.c_int32(self.nVar),
+                                             C.c_int32(self.nG), ptr(self.aig, i32p), C.c_int64(capc),
+                                             ptr(self.offsets, i64p), ptr(cols, i32p),
+                                             C.byref(ncolw), C.byref(nmat))
                 if rc == 0:
                     break
-                capc *= 4
+                if rc != -1:
+                    raise RuntimeError(f"mpgpu_host_mpbits failed ({rc})")
+                capc, caps = max(capc * 4, ncolw.value), nsup.value
+            self.suppressed = sup[:2 * nsup.value].reshape(-1, 2).copy()
             self.columns = cols[:max(ncolw.value, 1)].copy()
             self.ncolw, self.nmatSparse = ncolw.value, nmat.value
         self.nmatPacked = self.nVar * (self.nVar + 1) // 2
@@ -442,6 +460,13 @@ class Context:
             ptr(S.offsets if matsto == 2 else None, i64p),
             ptr(S.columns if matsto == 2 else None, i32p), C.c_int64(S.ncolw),
             C.c_int64(self.nmat)))
+        sup = getattr(S, "suppressed", None)
+        if matsto == 2 and sup is not None and len(sup) > 0:
+            self.set_suppressed_pairs(sup)
+
+    def set_suppressed_pairs(self, pairs):
+        p = np.ascontiguousarray(pairs, np.int32).reshape(-1)
+        self.check(self.L.mpgpu_set_suppressed_pairs(self.h, C.c_int64(len(p) // 2), ptr(p, i32p)))
 
     def set_constraints(self, A):
         A = np.ascontiguousarray(A, np.float64)

@@ -72,14 +72,17 @@ int mpref_translate(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
 /* ---------------------------------------------------------------------
  * Sparse structure (matsto=2): clbits/inbits/ndbits/spbits
  * (mpbits.f90:73-142,182-243,305-566,1220-1350) with the record pair fill
- * of loop2 (pede.f90:6889-6908).  nspc=1 (mreqpe >= 1, msngpe < 1),
- * mextnd=0.  Records hold total indices.
+ * of loop2 (pede.f90:6889-6908).  nspc=1 (msngpe < 1), mextnd=0.  Records
+ * hold total indices; records from nrecData on are the structure-only
+ * records of the measurement lines, whose pairs count mreqpe
+ * (pede.f90:7036).  Group pairs counted fewer than mreqpe times
+ * (pairentries) are left out.
  * Outputs: offsets[2*(nG+1)] = sparseMatrixOffsets (column-major 2 x (nG+1)),
  * columns[] (cap words) = sparseMatrixColumns; *ncolw words used;
  * *nmat = length of globalMatD (diagonal + off-diagonal).
  * Returns 0 or -1 (capacity).
  * ------------------------------------------------------------------- */
-int mpref_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+int mpref_mpbits(int64_t nrec, int64_t nrecData, const int64_t *recPtr, const int32_t *inder,
                  const double *glder, const int32_t *varIndexOfTotal, int32_t nVar,
                  int32_t nG, const int32_t *allIndexGroups, const int32_t *parToGroup,
                  int32_t mreqpe, int64_t cap, int64_t *offsets, int32_t *columns,
@@ -104,6 +107,10 @@ typedef struct mpref_fitopt {
     float chhuge;     /* huge chi2 cut factor */
     float dwcut;      /* down-weight fraction cut */
     float cndlmx;     /* max log10(cond) of band part */
+    int32_t mreqpe;   /* pairentries: above 1 (sparse), the updates of group
+                         pairs left out of the structure are dropped as mupdat
+                         drops them (pede.f90:3172); otherwise a pair missing
+                         from the structure is error 23 */
 } mpref_fitopt;
 
 typedef struct mpref_fitout {

@@ -241,7 +241,9 @@ typedef struct {
 } ctx_t;
 
 /* subtract one record's update (packed nalg x nalg over the sorted variable
- * indices usage[1..nalg]) from the global matrix (mgupdt semantics) */
+ * indices usage[1..nalg]) from the global matrix (mgupdt semantics; an
+ * element of a pair left out by pairentries is dropped as mupdat drops it,
+ * pede.f90:3172, where mgupdt itself stops, pede.f90:3313-3319) */
 static int apply_update(const ctx_t *c, const int32_t *usage, int32_t nalg, const double *upd,
                         double *matD)
 {
@@ -257,7 +259,10 @@ static int apply_update(const ctx_t *c, const int32_t *usage, int32_t nalg, cons
                 } else {
                     int64_t ij = mpref_ijadd((int32_t)gi, (int32_t)gj, c->nG, c->aig, c->p2g,
                                              c->off, c->col);
-                    if (ij <= 0) return 23;
+                    if (ij <= 0) {
+                        if (c->opt->mreqpe > 1) continue;  /* pair left out (pairentries) */
+                        return 23;
+                    }
                     matD[ij - 1] -= s;
                 }
             } else {

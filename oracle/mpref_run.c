@@ -116,7 +116,8 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         /* the pairs of the measurement lines belong to the sparse structure
          * whatever the records hold (pede.f90:7007-7042, with the
          * increment mreqpe, so they are always kept): one structure-only
-         * record per measurement line, its labels as global words */
+         * record per measurement line, its labels as global words, after
+         * the data records */
         int64_t nrecS = job->nrec, *rpS = (int64_t *)job->recPtr;
         int32_t *inS = tinder;
         double *glS = (double *)job->glder;
@@ -155,7 +156,7 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
         offsets = (int64_t *)malloc(sizeof(int64_t) * 2 * ((size_t)nG + 1));
         for (;;) {
             columns = (int32_t *)malloc(sizeof(int32_t) * (size_t)capc);
-            if (mpref_mpbits(nrecS, rpS, inS, glS, res->varIndex, nVar, nG,
+            if (mpref_mpbits(nrecS, job->nrec, rpS, inS, glS, res->varIndex, nVar, nG,
                              aig, p2g, st->mreqpe, capc, offsets, columns, &ncolw, &nmat) == 0)
                 break;
             free(columns);
@@ -243,7 +244,8 @@ int mpref_run(const mpref_steer *st, const mpref_job *job, mpref_result *res)
             }
         }
         mpref_fitopt fo = {1, nloopn, st->lhuber, st->lfitbb, st->matsto,
-                           chicut, st->chhuge, st->dwcut, st->cndlmx};
+                           chicut, st->chhuge, st->dwcut, st->cndlmx,
+                           st->matsto == 2 ? st->mreqpe : 1};
         mpref_fitout out;
         memset(&out, 0, sizeof(out));
         memset(gvec, 0, sizeof(double) * (size_t)nVar);

@@ -278,21 +278,45 @@ int mpref_translate(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
     return 0;
 }
 
-/* ---------------- mpbits (nspc=1, ibfw=1, mextnd=0) ---------------- */
+/* ---------------- mpbits (nspc=1, mextnd=0) ---------------- */
 #define BS 32
 
-static void inbits(uint32_t *bits, int32_t n, int32_t im, int32_t jm)
+/* bit m (may pass the end of the word) counted from bit 0 of word l */
+static int bit_get(const uint32_t *bits, int64_t l, int32_t m)
 {
-    int32_t j = im < jm ? im : jm, i = im < jm ? jm : im;
-    if (j <= 0 || i > n) return;
-    int64_t noffi = (int64_t)(i - 1) * (int64_t)i / 2;  /* ibfw = 1 */
-    int64_t noffj = (int64_t)(j - 1);
-    int64_t l = noffi / BS + i + noffj / BS;             /* 1-based word */
-    int32_t m = (int32_t)(noffj % BS);
-    bits[l] |= (1u << m);
+    return (int)((bits[l + m / BS] >> (m % BS)) & 1u);
 }
 
-int mpref_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
+static void bit_put(uint32_t *bits, int64_t l, int32_t m, int v)
+{
+    uint32_t *w = &bits[l + m / BS];
+    if (v) *w |= 1u << (m % BS);
+    else *w &= ~(1u << (m % BS));
+}
+
+/* inbits (mpbits.f90:73-142), lower triangle: the counter of the group
+ * pair (i, j) is the ibfw-bit field at bit (j-1)*ibfw of row i, whose bits
+ * start at word noffi/BS + i (each row in words of its own); it is raised
+ * by inc and saturates at mxcnt.  With ibfw = 1 the field is a flag. */
+static void inbits(uint32_t *bits, int32_t n, int32_t ibfw, int32_t mxcnt, int32_t im, int32_t jm,
+                   int32_t inc)
+{
+    int32_t j = im < jm ? im : jm, i = im < jm ? jm : im, b, icount = 0, jcount;
+    if (j <= 0 || i > n) return;
+    int64_t noffi = (int64_t)(i - 1) * (int64_t)i * ibfw / 2;
+    int64_t noffj = (int64_t)(j - 1) * ibfw;
+    int64_t l = noffi / BS + i + noffj / BS;             /* 1-based word */
+    int32_t m = (int32_t)(noffj % BS);
+    if (ibfw <= 1) { bits[l] |= (1u << m); return; }
+    for (b = 0; b < ibfw; b++)
+        if (bit_get(bits, l, m + b)) icount |= 1 << b;
+    jcount = icount;
+    icount = icount + inc < mxcnt ? icount + inc : mxcnt;
+    if (icount != jcount)
+        for (b = 0; b < ibfw; b++) bit_put(bits, l, m + b, (icount >> b) & 1);
+}
+
+int mpref_mpbits(int64_t nrec, int64_t nrecData, const int64_t *recPtr, const int32_t *inder,
                  const double *glder, const int32_t *varIndexOfTotal, int32_t nVar,
                  int32_t nG, const int32_t *allIndexGroups, const int32_t *parToGroup,
                  int32_t mreqpe, int64_t cap, int64_t *offsets, int32_t *columns,
@@ -300,20 +324,28 @@ int mpref_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
 {
     int32_t n = nG, i, j;
     const int32_t *npgrp = allIndexGroups - 1;  /* npgrp[1..n+1] */
+    /* clbits (mpbits.f90:182-243) with msngpe = mhispe = 0: counters wide
+     * enough to count to mreqpe */
+    int32_t ireqpe = mreqpe > 1 ? mreqpe : 1, ibfw = 1, mxcnt = 1;
+    for (i = 1; i <= 30; i++)
+        if (ireqpe > mxcnt) { ibfw++; mxcnt = mxcnt * 2 + 1; }
     int64_t noffd = (int64_t)n * (int64_t)(n + 1) / 2;
     int64_t ndimb = noffd / BS + n;
+    int64_t ndimc = noffd * ibfw / BS + n;
     uint32_t *bits = (uint32_t *)calloc((size_t)ndimb + 2, sizeof(uint32_t));
+    uint32_t *cnt = (uint32_t *)calloc((size_t)ndimc + 2, sizeof(uint32_t));
     int32_t *back = (int32_t *)calloc((size_t)nVar + 2, sizeof(int32_t));
     int32_t *use = (int32_t *)malloc(sizeof(int32_t) * ((size_t)nVar + 2));
     int32_t *grp = (int32_t *)malloc(sizeof(int32_t) * ((size_t)nG + 2));
     int64_t r, lastGlobal, startLocal, startGlobal, startSpecial, endOfEntry;
-    if (!bits || !back || !use || !grp) return -1;
-    (void)mreqpe;
+    if (!bits || !cnt || !back || !use || !grp) return -1;
 
     /* loop2 second pass (pede.f90:6700-6862, 6889-6908): sorted variable
-     * indices per record -> groups -> all group pairs */
+     * indices per record -> groups -> all group pairs, each counted once per
+     * record; records from nrecData on are measurement lines, whose pairs
+     * count mreqpe (pede.f90:7036) and so are always kept */
     for (r = 0; r < nrec; r++) {
-        int32_t ng = 0, ngrp = 0;
+        int32_t ng = 0, ngrp = 0, inc = r < nrecData ? 1 : ireqpe;
         endOfEntry = recPtr[r + 1] - 1;
         lastGlobal = recPtr[r];
         for (;;) {
@@ -338,26 +370,33 @@ int mpref_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
             if (g != prev) { grp[++ngrp] = g; prev = g; }
         }
         for (i = 1; i <= ngrp; i++)
-            for (j = 1; j <= i; j++) inbits(bits, n, grp[i], grp[j]);
+            for (j = 1; j <= i; j++) inbits(cnt, n, ibfw, mxcnt, grp[i], grp[j], inc);
     }
 
-    /* ndbits (mpbits.f90:305-566) */
+    /* ndbits (mpbits.f90:305-566): a pair is kept when its counter reaches
+     * mreqpe (mpbits.f90:409); the kept flags go to `bits` (one bit per
+     * pair, the layout of ibfw = 1) for the column lists of spbits */
     int64_t *nsparr = offsets;  /* nsparr(1,k) = offsets[2*(k-1)], (2,k) = offsets[2*(k-1)+1] */
 #define NS1(k) nsparr[2 * ((k) - 1)]
 #define NS2(k) nsparr[2 * ((k) - 1) + 1]
     int64_t nd = npgrp[n + 1] - npgrp[1];
     for (i = 1; i <= n; i++) {
-        int64_t noffi = (int64_t)(i - 1) * (int64_t)i / 2;
+        int64_t noffi = (int64_t)(i - 1) * (int64_t)i * ibfw / 2;
         int64_t ll = noffi / BS + i;
-        int32_t mm = 0, last = 0, next;
+        int64_t lk = (int64_t)(i - 1) * (int64_t)i / 2 / BS + i;
+        int32_t mm = 0, last = 0, next, ib;
         int64_t inr = 0, irgn = 1;
         for (j = 1; j <= i; j++) {
-            int32_t icount = (bits[ll] >> mm) & 1u;
-            mm++;
-            if (mm >= BS) { ll++; mm -= BS; }
+            int32_t icount = 0;
+            for (ib = 0; ib < ibfw; ib++) {
+                if ((cnt[ll] >> mm) & 1u) icount |= 1 << ib;
+                mm++;
+                if (mm >= BS) { ll++; mm -= BS; }
+            }
             next = 0;
-            if (icount >= 1) {
+            if (icount >= ireqpe) {
                 next = 1;
+                bit_put(bits, lk, j - 1, 1);
                 inr += npgrp[j + 1] - npgrp[j];
                 if (next != last) irgn++;
             }
@@ -366,6 +405,7 @@ int mpref_mpbits(int64_t nrec, const int64_t *recPtr, const int32_t *inder,
         NS1(i + 1) = irgn;
         NS2(i + 1) = inr;
     }
+    free(cnt);
     int64_t ncw = 0;
     for (i = 1; i <= n; i++) {
         int64_t irgn = NS1(i + 1), inr = NS2(i + 1);

@@ -20,7 +20,8 @@ f32p = C.POINTER(C.c_float)
 class FitOpt(C.Structure):
     _fields_ = [("icalcm", C.c_int32), ("nloopn", C.c_int32), ("lhuber", C.c_int32),
                 ("lfitbb", C.c_int32), ("matsto", C.c_int32), ("chicut", C.c_float),
-                ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float)]
+                ("chhuge", C.c_float), ("dwcut", C.c_float), ("cndlmx", C.c_float),
+                ("mreqpe", C.c_int32)]
 
 
 class FitOut(C.Structure):
@@ -196,7 +197,8 @@ def run(data, steer, **jobkw):
 class Structure:
     """loop1 + loop2 products computed by the oracle for one record set."""
 
-    def __init__(self, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True):
+    def __init__(self, data, mreqenf=25, steerLabels=(), preLabel=(), preSigma=(), sparse=True,
+                 mreqpe=1):
         L = lib()
         recPtr = np.ascontiguousarray(data["recPtr"], np.int64)
         inder = np.ascontiguousarray(data["inder"], np.int32)
@@ -234,6 +236,7 @@ class Structure:
                                ptr(self.tinder, i32p))
         assert rc == 0
         self.recPtr, self.glder = recPtr, glder
+        self.mreqpe = mreqpe
         self.offsets = np.zeros(2 * (self.nG + 1), np.int64)
         self.columns = np.zeros(1, np.int32)
         if sparse:
@@ -241,10 +244,11 @@ class Structure:
             while True:
                 self.columns = np.zeros(capc, np.int32)
                 ncolw, nmat = C.c_int64(), C.c_int64()
-                rc = L.mpref_mpbits(C.c_int64(nrec), ptr(recPtr, i64p), ptr(self.tinder, i32p),
+                rc = L.mpref_mpbits(C.c_int64(nrec), C.c_int64(nrec), ptr(recPtr, i64p),
+                                    ptr(self.tinder, i32p),
                                     ptr(glder, f64p), ptr(self.varIndex, i32p),
                                     C.c_int32(self.nVar), C.c_int32(self.nG),
-                                    ptr(self.aig, i32p), ptr(self.p2g, i32p), C.c_int32(1),
+                                    ptr(self.aig, i32p), ptr(self.p2g, i32p), C.c_int32(mreqpe),
                                     C.c_int64(capc), ptr(self.offsets, i64p),
                                     ptr(self.columns, i32p), C.byref(ncolw), C.byref(nmat))
                 if rc == 0:
@@ -257,7 +261,7 @@ class Structure:
     def loopbf(self, gpar, matsto=2, nthreads=1, **opt):
         L = lib()
         o = dict(icalcm=1, nloopn=1, lhuber=0, lfitbb=1, matsto=matsto, chicut=0.0,
-                 chhuge=50.0, dwcut=0.0, cndlmx=100.0)
+                 chhuge=50.0, dwcut=0.0, cndlmx=100.0, mreqpe=self.mreqpe)
         o.update(opt)
         fo = FitOpt(**o)
         out = FitOut()

@@ -27,14 +27,3 @@ def test_library_exports_all_declared(mp):
 
 def test_python_export_list_matches_header(mp):
     assert sorted(set(mp.EXPORTS)) == declared_symbols()
-
-
-def test_pairentries_above_one_refused(mp):
-    """pede's pairentries (mreqpe > 1) is not built: mpgpu_pede_run refuses
-    it with status 44 before any device work instead of storing every pair."""
-    import numpy as np
-    d = {"recPtr": np.array([0, 1], np.int64), "inder": np.zeros(1, np.int32),
-         "glder": np.zeros(1), "ncon": 0}
-    jd = mp.JobData(d, mreqpe=2)
-    assert mp.run_job(jd) == 44
-    assert jd.res.exitCode == 44
