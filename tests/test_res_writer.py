@@ -4,7 +4,9 @@ the constraints (feasib makes them feasible before the first data loop),
 the writer's columns ("differ" = parameter - start value, printcounts with
 the lowstat sign, globalcorr), the library's writer equal to the oracle's
 byte for byte, and the fixed-column layout of the reference's own golden
-file CI/refFiles/millepede.res (read only where the reference is mounted)."""
+file CI/refFiles/millepede.res (its layout facts from
+tests/golden/millepede_res_layout.json; every line where MILLEPEDE_SOURCES
+names the sources)."""
 import ctypes as C
 import os
 import re
@@ -172,6 +174,30 @@ def test_layout_of_reference_golden_file(mp, tmp_path):
             ours.add((len(vals), len(line)))
     assert ours and ours <= shapes | {(3, 80)}
     assert (3, 80) in shapes
+
+
+def test_layout_of_reference_golden_fixture(mp, tmp_path):
+    """The layout facts of the reference's golden millepede.res
+    (tests/golden/millepede_res_layout.json, made by make_res_layout.py):
+    its sample lines parse with the column parser above (value, presigma,
+    difference and the count of format 110/111), and a result written with
+    the same options has lines of the same length."""
+    import json
+    with open(os.path.join(os.path.dirname(__file__), "golden", "millepede_res_layout.json")) as f:
+        fx = json.load(f)
+    assert fx["header"].strip().startswith("Parameter")
+    assert [s[2] for s in fx["shapes"]] == [fx["nlines"]]
+    width = fx["shapes"][0][1]
+    for line in fx["samples"]:
+        lab, vals, count, gcor = parse_line(line)
+        assert len(vals) == 3 and count is not None and gcor is None
+        assert len(line) == width
+    d, labels, values, sigmas = telescope_job(mp, 0.002)
+    st = orc.make_steer(metsol=3, matsto=1, mitera=1, mreqena=10)
+    o = orc.run(d, st, parLabel=labels, parValue=values, parSigma=sigmas)
+    a, _ = write_both(mp, o, tmp_path, errors=0, ipcntr=1, igcorr=0, mreqena=10)
+    ours = [line for line in a.splitlines()[1:] if len(parse_line(line)[1]) == 3]
+    assert ours and all(len(line) == width for line in ours)
 
 
 def test_writer_rejects_zero_counts(mp, tmp_path):
