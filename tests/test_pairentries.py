@@ -91,9 +91,11 @@ def data(mp, name, ntracks, seed):
     return mp.generate(mp.gen_config(name, ntracks=ntracks, seed=seed))
 
 
-# counters of 2, 3 (fields crossing the oracle's 32-bit words) and 5 bits
+# counters of 2, 3 (fields crossing the oracle's 32-bit words) and 5 bits;
+# column lists and compressed regions (telescope), regions only and rows
+# left empty when a group's own pair is left out (barrel, broken lines)
 CASES = [("telescope", 300, 5, 2), ("telescope", 300, 5, 4), ("telescope", 300, 5, 20),
-         ("barrel", 200, 6, 2), ("barrel", 200, 6, 3)]
+         ("barrel", 200, 6, 2), ("barrel", 200, 6, 3), ("brokenlines", 300, 7, 2)]
 
 
 @pytest.mark.parametrize("name,ntracks,seed,mreqpe", CASES)
