@@ -4,8 +4,9 @@ plus two update calls in a row agrees within 1e-12 relative (both run the
 same kernel in the same order, so it is expected to be identical); both
 against the oracle's mupdat (pede.f90:3134-3204) applied to the same
 matrix, on packed and on mpbits-sparse storage where most random pairs are
-not stored and are suppressed; a call above the area's capacity is
-rejected and leaves the matrix unchanged."""
+not stored and are suppressed, and on a pairentries layout whose left-out
+pairs are dropped; a call above the area's capacity is rejected and leaves
+the matrix unchanged."""
 import ctypes as C
 
 import numpy as np
@@ -127,3 +128,34 @@ def test_noalloc_and_mupdat_match_oracle(mp, orc, kind, matsto):
         # the matrix changed, but by fewer elements than there were triplets
         changed = int(np.count_nonzero(want != base))
         assert 0 < changed < sum(len(b[0]) for b in bs) // 2
+
+
+def test_mupdat_on_pairentries_layout(mp, orc):
+    """mpgpu_mupdat and mpgpu_mupdat_noalloc on a sparse layout with
+    pairentries 2: elements of the left-out group pairs (pairs the records
+    hold) are dropped as the oracle's mupdat drops them
+    (pede.f90:3170-3173), the others land as there"""
+    d = mp.generate(mp.gen_config("barrel", ntracks=3000, seed=17))
+    H = mp.HostStructure(d, mreqenf=5, sparse=True, mreqpe=2)
+    sup = H.suppressed
+    assert len(sup) > 0
+    first = H.aig[sup[:, 0] - 1]
+    i = np.where(sup[:, 0] == sup[:, 1], first + 1, first).astype(np.int32)
+    j = H.aig[sup[:, 1] - 1].astype(np.int32)
+    left = (i, j, np.ones(len(i)))
+    bs = [left] + batches(H.nVar, [20000], seed=5)
+    with mp.Context() as ctx:
+        ctx.set_layout(H, 2)
+        ctx.upload(H)
+        gpar = np.zeros(H.nTotal)
+        ctx.loopbf(gpar)
+        base = ctx.matrix()
+        np.testing.assert_array_equal(oracle_mupdat(orc, H, 2, base, [left]), base)
+        want = oracle_mupdat(orc, H, 2, base, bs)
+        for call in (ctx.mupdat, ctx.mupdat_noalloc):
+            ctx.loopbf(gpar)
+            call(*left)
+            np.testing.assert_array_equal(ctx.matrix(), base)
+            for b in bs[1:]:
+                call(*b)
+            close(ctx.matrix(), want)
