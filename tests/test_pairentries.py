@@ -337,3 +337,28 @@ def test_gpu_job_pairentries(mp):
     assert g["nrej"] == o["nrej"]
     scale = np.max(np.abs(o["parameter"]))
     assert np.max(np.abs(g["parameter"] - o["parameter"])) <= 1e-9 * scale
+
+
+def test_host_structure_bad_arguments(mp):
+    """status 44 for arguments the pass cannot use (no groups, no
+    parameters, a list capacity without a list)"""
+    rp = np.array([0, 1], np.int64)
+    ind = np.zeros(1, np.int32)
+    gl = np.zeros(1)
+    vi = np.ones(1, np.int32)
+    aig = np.array([1, 2], np.int32)
+    off = np.zeros(4, np.int64)
+    col = np.zeros(4, np.int32)
+    ncolw, nmat, nsup = C.c_int64(), C.c_int64(), C.c_int64()
+    L = mp.lib()
+
+    def call(nVar, nG, capSup, sup):
+        return L.mpgpu_host_mpbits_pairentries(
+            C.c_int64(1), C.c_int64(1), mp.ptr(rp, i64p), mp.ptr(ind, i32p), mp.ptr(gl, f64p),
+            mp.ptr(vi, i32p), C.c_int32(nVar), C.c_int32(nG), mp.ptr(aig, i32p), C.c_int32(2),
+            C.c_int64(4), mp.ptr(off, i64p), mp.ptr(col, i32p), C.byref(ncolw), C.byref(nmat),
+            C.c_int64(capSup), sup, C.byref(nsup))
+    assert call(1, 0, 0, None) == 44
+    assert call(0, 1, 0, None) == 44
+    assert call(1, 1, 8, None) == 44
+    assert call(1, 1, 0, None) == 0 and nsup.value == 0 and nmat.value == 1
